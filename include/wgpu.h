@@ -1,0 +1,224 @@
+/*
+ * wgpu -- GB300-native w-gridder, C ABI.
+ *
+ * This is the thin C layer between WSClean's C++ gridder interface
+ * (wgridder/gridder_simple.h:19-41, WGriddingGridderBase) and the sm_103a CUDA
+ * kernels.  Each entry point below names the reference method it replaces.
+ * The C++ drop-in class wsclean::WGriddingGridder_Simple<NumT> in
+ * include/wgpu_gridder.h is written on top of these functions.
+ *
+ * Conventions
+ *  - All pointers are caller-owned and borrowed for the duration of the call
+ *    (gridder_simple.h:106-124).  "_device" variants take device pointers and
+ *    run on the gridder's CUDA stream; every other entry point takes host
+ *    pointers and copies them itself.
+ *  - Visibilities are interleaved complex64 (float re, float im), indexed
+ *    [row * n_chan + chan]; uvw are metres [row][3]; frequencies are Hz and
+ *    may be descending (gridder_simple_implementation.h:79-88).
+ *  - Images passed to and from the API are row-major [x + y * width] over the
+ *    UNTRIMMED width x height, exactly like RealImage()/InitializePrediction()
+ *    (gridder_simple_implementation.h:147-168).
+ *  - Every function returns WGPU_OK (0) or a negative status; the message of
+ *    the last failure on the calling thread is returned by wgpu_last_error().
+ *    There is no CPU fallback: without a usable CUDA device every compute
+ *    entry point fails with WGPU_ERR_CUDA.
+ */
+#ifndef WGPU_H_
+#define WGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WGPU_OK 0
+#define WGPU_ERR_INVALID (-1)  /* bad argument or unsupported combination */
+#define WGPU_ERR_CUDA (-2)     /* CUDA runtime error / no device */
+#define WGPU_ERR_NOMEM (-3)    /* device memory could not be obtained */
+#define WGPU_ERR_STATE (-4)    /* call order violated (e.g. predict before init) */
+#define WGPU_ERR_TIMEOUT (-5)  /* a bounded device-side wait expired */
+
+/* Gain modes, numbered as gridding/gainmode.h:16-31 declares them. */
+#define WGPU_GAIN_XX 0
+#define WGPU_GAIN_YY 1
+#define WGPU_GAIN_TRACE 2
+#define WGPU_GAIN_2VIS_DIAGONAL 3
+#define WGPU_GAIN_FULL 4
+
+/* Polarisation selector for the 4-visibility collapse
+ * (gridding/msgridderdata.h:46-50). */
+#define WGPU_POL_STOKES_I 0
+#define WGPU_POL_STOKES_Q 1
+#define WGPU_POL_STOKES_U 2
+#define WGPU_POL_STOKES_V 3
+#define WGPU_POL_XX 4
+#define WGPU_POL_XY 5
+#define WGPU_POL_YX 6
+#define WGPU_POL_YY 7
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *wgpu_last_error(void);
+
+/* Library version string. */
+const char *wgpu_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Planner (host only; no device needed)                                      */
+/* ------------------------------------------------------------------------ */
+
+/* One gridding plan: grid sizes, ES kernel, w-planes.  Chosen per call from
+ * the requested accuracy and the data's w range (the reference leaves this to
+ * ducc0 inside ms2dirty/dirty2ms, gridder_simple.h:217-225). */
+typedef struct wgpu_plan {
+  int64_t width, height;  /* trimmed image */
+  int64_t nu, nv;         /* padded uv grid (multiples of tile) */
+  int64_t support;        /* kernel support W in cells (also in w) */
+  int64_t tile;           /* uv tile edge (cells) */
+  int64_t n_planes;       /* w planes (1 = no w-gridding) */
+  int64_t plane_batch;    /* planes resident per pipeline step */
+  int64_t fft_n1, fft_n2; /* nv = n1 * n2 column decomposition */
+  double sigma;           /* oversampling of the table entry used */
+  double beta;            /* ES kernel beta */
+  double dl, dm, l_shift, m_shift;
+  double w0, dw;          /* plane p at w0 + p * dw (wavelengths) */
+  double nm1_min, nm1_max, nm1_center;
+  double est_error;       /* model estimate of the relative L2 error */
+  double est_seconds;     /* cost-model estimate */
+} wgpu_plan_t;
+
+typedef struct wgpu_plan_request {
+  int64_t width, height;       /* trimmed image */
+  double dl, dm, l_shift, m_shift;
+  double epsilon;
+  double w_min, w_max;         /* data w range in wavelengths */
+  int64_t n_vis;               /* visibilities to grid */
+  double sigma_min, sigma_max; /* 0 -> 1.1 / 2.0 (gridder_simple.h:57-58) */
+  int64_t force_support;       /* >0 pins W (autotuner / tests) */
+  double force_sigma;          /* >0 pins sigma */
+  int64_t force_tile;          /* >0 pins the tile edge (16 or 32) */
+  int64_t max_plane_batch;     /* >0 caps planes per step */
+  double memory_budget_bytes;  /* >0 caps plane-batch memory */
+} wgpu_plan_request_t;
+
+int wgpu_plan_make(const wgpu_plan_request_t *request, wgpu_plan_t *plan);
+
+/* ------------------------------------------------------------------------ */
+/* Gridder instance: WGriddingGridder_Simple<NumT>                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct wgpu_gridder wgpu_gridder_t;
+
+/* gridder_simple.h:84-88 / gridder_simple_implementation.h:32-50.
+ * precision_bytes is sizeof(NumT): 4 or 8 (the type of the accumulated
+ * image; the device arithmetic is FP32 with compensated accumulation either
+ * way).  verbosity must be 0, 1 or 2 (the reference's MR_assert). */
+int wgpu_gridder_create(size_t width, size_t height, size_t width_t,
+                        size_t height_t, double pixel_size_x,
+                        double pixel_size_y, double l_shift, double m_shift,
+                        size_t nthreads, double epsilon, size_t verbosity,
+                        int tuning, int precision_bytes,
+                        wgpu_gridder_t **gridder);
+
+void wgpu_gridder_destroy(wgpu_gridder_t *gridder);
+
+/* gridder_simple_implementation.h:53-61 and :63-68 (same formulas). */
+size_t wgpu_gridder_constant_memory(const wgpu_gridder_t *gridder);
+size_t wgpu_gridder_per_visibility_memory(const wgpu_gridder_t *gridder);
+
+/* gridder_simple_implementation.h:71-74: zero the accumulated image. */
+int wgpu_gridder_initialize_inversion(wgpu_gridder_t *gridder);
+
+/* gridder_simple_implementation.h:76-90 (AddInversionData): grid n_rows x
+ * n_chan weighted, corrected visibilities and add the dirty image to the
+ * accumulated image.  Visibilities equal to 0 are skipped
+ * (gridder_simple.h:111). */
+int wgpu_gridder_add_inversion_data(wgpu_gridder_t *gridder, size_t n_rows,
+                                    size_t n_chan, const double *uvw,
+                                    const double *freq, const float *vis);
+
+/* Same, with device-resident uvw / freq / vis. */
+int wgpu_gridder_add_inversion_data_device(wgpu_gridder_t *gridder,
+                                           size_t n_rows, size_t n_chan,
+                                           const double *d_uvw,
+                                           const double *d_freq,
+                                           const float *d_vis);
+
+/* gridder_simple_implementation.h:92-110 (AddInversionDataWithCorrectionCallback)
+ * with the per-row correction that VisibilityCallbackBuffer::raw performs on
+ * the host (callback_implementation.h:53-101) moved onto the device: the
+ * caller passes the cached solution table instead of an MsGridder pointer.
+ *   vis:           [row][chan][n_pol] complex64, weighted, uncorrected
+ *   antenna_pairs: [row][2] antenna indices (std::pair<size_t,size_t> layout)
+ *   time_offsets:  [row] time offsets into the solution table
+ *   solutions:     complex64, index ((t * n_chan + ch) * n_ant + ant) * nparms
+ *                  (visibilitymodifier.h:547-551), nparms 2 (diagonal) or 4
+ *   n_times:       number of time slots in the solution table
+ * mode must match n_pol (1 for XX/YY/TRACE, 2 for 2VIS_DIAGONAL, 4 for FULL). */
+int wgpu_gridder_add_inversion_data_corrected(
+    wgpu_gridder_t *gridder, int mode, size_t n_pol, size_t n_rows,
+    const double *uvw, const double *freq, size_t n_chan,
+    const uint64_t *antenna_pairs, const float *vis,
+    const uint64_t *time_offsets, const float *solutions, size_t nparms,
+    size_t n_times, size_t n_ant, int polarization);
+
+/* gridder_simple_implementation.h:142-145. */
+int wgpu_gridder_finalize_image(wgpu_gridder_t *gridder, double factor);
+
+/* gridder_simple_implementation.h:147-157: untrimmed width*height floats,
+ * NaN outside the trimmed region. */
+int wgpu_gridder_real_image(wgpu_gridder_t *gridder, float *image);
+
+/* gridder_simple_implementation.h:159-168: untrimmed width*height model. */
+int wgpu_gridder_initialize_prediction(wgpu_gridder_t *gridder,
+                                       const float *image);
+
+/* gridder_simple_implementation.h:170-196 (PredictVisibilities). */
+int wgpu_gridder_predict_visibilities(wgpu_gridder_t *gridder, size_t n_rows,
+                                      size_t n_chan, const double *uvw,
+                                      const double *freq, float *vis);
+
+/* Same, with device-resident uvw / freq and a device output buffer. */
+int wgpu_gridder_predict_visibilities_device(wgpu_gridder_t *gridder,
+                                             size_t n_rows, size_t n_chan,
+                                             const double *d_uvw,
+                                             const double *d_freq,
+                                             float *d_vis);
+
+/* Plan used by the last inversion/prediction call of this gridder. */
+int wgpu_gridder_last_plan(const wgpu_gridder_t *gridder, wgpu_plan_t *plan);
+
+/* Per-stage device times of the last call (milliseconds, CUDA events on the
+ * gridder's stream): names are written as a ';'-separated list. */
+int wgpu_gridder_last_timings(const wgpu_gridder_t *gridder, double *ms,
+                              int max_entries, char *names, size_t names_len,
+                              int *n_entries);
+
+/* Gridder's CUDA stream (cudaStream_t), for callers that time or order work
+ * around the _device entry points. */
+void *wgpu_gridder_stream(wgpu_gridder_t *gridder);
+
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t wgpu_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* Bucketing pass on its own (test hook for bit-exactness)                    */
+/* ------------------------------------------------------------------------ */
+
+/* Runs the GPU bucketing pass for `plan` over host inputs and copies back, in
+ * sorted order, perm (element indices row*n_chan+chan), the footprint corner
+ * (iu, iv, ip), the fractions (fu, fv, fw), and the bucket offsets
+ * (n_tiles*n_planes + 1 entries).  skip_zero selects inversion semantics.
+ * *n_out receives the number of bucketed elements. */
+int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                      const double *uvw, const double *freq, const float *vis,
+                      int skip_zero, uint32_t *perm, int32_t *iu, int32_t *iv,
+                      int32_t *ip, float *fu, float *fv, float *fw,
+                      uint32_t *offsets, int64_t *n_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WGPU_H_ */

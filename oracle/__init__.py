@@ -1,0 +1,201 @@
+"""ctypes wrapper of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+legs import this package, as the checker.  See wgpu_oracle.h for what each
+function restates and its parity status.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+
+class OraclePlan(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("width", "height", "nu", "nv", "support", "tile",
+                                         "n_planes")] + \
+               [(n, C.c_double) for n in ("beta", "dl", "dm", "l_shift", "m_shift", "w0", "dw",
+                                          "nm1_center")]
+
+
+_lib = None
+
+
+def build():
+    r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P, SZ, D, I = C.c_void_p, C.c_size_t, C.c_double, C.c_int
+        L.oracle_dft_invert.argtypes = [SZ, SZ, P, P, P, SZ, SZ, D, D, D, D, P, SZ, I, P]
+        L.oracle_dft_predict.argtypes = [SZ, SZ, P, P, P, SZ, SZ, D, D, D, D, P, SZ, I, P]
+        L.oracle_bucket.restype = C.c_int64
+        L.oracle_bucket.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, P, P, P, P, P,
+                                    P, P, P, P]
+        L.oracle_wgrid_invert.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, P]
+        L.oracle_wgrid_predict.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, P]
+        L.oracle_wgrid_time_parts.restype = D
+        L.oracle_wgrid_time_parts.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, I,
+                                              C.POINTER(D)]
+        L.oracle_es_kernel.restype = D
+        L.oracle_es_kernel.argtypes = [D, D]
+        L.oracle_es_fourier.restype = D
+        L.oracle_es_fourier.argtypes = [D, I, D]
+        L.oracle_apply_gains.restype = I
+        L.oracle_apply_gains.argtypes = [I, SZ, SZ, SZ, P, P, P, P, SZ, SZ, I, P]
+        L.oracle_apply_conjugated_gain.argtypes = [I, P, P, P]
+        L.oracle_apply_gain.argtypes = [I, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def to_oracle_plan(plan):
+    """From a product plan (wsclean_gb300._lib.Plan or dict) to the oracle's."""
+    get = (lambda k: plan[k]) if isinstance(plan, dict) else (lambda k: getattr(plan, k))
+    o = OraclePlan()
+    for k in ("width", "height", "nu", "nv", "support", "tile", "n_planes"):
+        setattr(o, k, int(get(k)))
+    for k in ("beta", "dl", "dm", "l_shift", "m_shift", "w0", "dw"):
+        setattr(o, k, float(get(k)))
+    o.nm1_center = float(get("nm1_center"))
+    return o
+
+
+def dft_invert(uvw, freq, vis, width, height, dl, dm, l_shift=0.0, m_shift=0.0, pixels=None,
+               n_threads=0):
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    vis = np.ascontiguousarray(vis, np.complex64)
+    if pixels is None:
+        pixels = np.arange(width * height, dtype=np.int64)
+    pixels = np.ascontiguousarray(pixels, np.int64)
+    out = np.zeros(pixels.size, np.float64)
+    lib().oracle_dft_invert(uvw.shape[0], freq.size, _p(uvw), _p(freq), _p(vis), width, height,
+                            dl, dm, l_shift, m_shift, _p(pixels), pixels.size, n_threads,
+                            _p(out))
+    return out
+
+
+def dft_predict(uvw, freq, image, width, height, dl, dm, l_shift=0.0, m_shift=0.0,
+                vis_index=None, n_threads=0):
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    image = np.ascontiguousarray(image, np.float64).ravel()
+    n = uvw.shape[0] * freq.size
+    if vis_index is None:
+        vis_index = np.arange(n, dtype=np.int64)
+    vis_index = np.ascontiguousarray(vis_index, np.int64)
+    out = np.zeros(2 * vis_index.size, np.float64)
+    lib().oracle_dft_predict(uvw.shape[0], freq.size, _p(uvw), _p(freq), _p(image), width,
+                             height, dl, dm, l_shift, m_shift, _p(vis_index), vis_index.size,
+                             n_threads, _p(out))
+    return out[0::2] + 1j * out[1::2]
+
+
+def bucket(plan, uvw, freq, vis, skip_zero):
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    vis = None if vis is None else np.ascontiguousarray(vis, np.complex64)
+    op = to_oracle_plan(plan)
+    n = uvw.shape[0] * freq.size
+    perm = np.zeros(n, np.uint32)
+    key = np.zeros(n, np.int64)
+    iu, iv, ip = (np.zeros(n, np.int32) for _ in range(3))
+    fu, fv, fw = (np.zeros(n, np.float32) for _ in range(3))
+    n_keys = (op.nu // op.tile) * (op.nv // op.tile) * op.n_planes
+    off = np.zeros(n_keys + 1, np.int64)
+    k = lib().oracle_bucket(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq), _p(vis),
+                            1 if skip_zero else 0, _p(perm), _p(key), _p(iu), _p(iv), _p(ip),
+                            _p(fu), _p(fv), _p(fw), _p(off))
+    return dict(perm=perm[:k], key=key[:k], iu=iu[:k], iv=iv[:k], ip=ip[:k], fu=fu[:k],
+                fv=fv[:k], fw=fw[:k], offsets=off)
+
+
+def wgrid_invert(plan, uvw, freq, vis, n_threads=0):
+    op = to_oracle_plan(plan)
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    vis = np.ascontiguousarray(vis, np.complex64)
+    out = np.zeros(op.width * op.height, np.float64)
+    r = lib().oracle_wgrid_invert(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq),
+                                  _p(vis), n_threads, _p(out))
+    if r != 0:
+        raise RuntimeError(f"oracle_wgrid_invert failed ({r})")
+    return out
+
+
+def wgrid_predict(plan, uvw, freq, image, n_threads=0):
+    op = to_oracle_plan(plan)
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    image = np.ascontiguousarray(image, np.float64).ravel()
+    out = np.zeros(2 * uvw.shape[0] * freq.size, np.float64)
+    r = lib().oracle_wgrid_predict(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq),
+                                   _p(image), n_threads, _p(out))
+    if r != 0:
+        raise RuntimeError(f"oracle_wgrid_predict failed ({r})")
+    return out[0::2] + 1j * out[1::2]
+
+
+def wgrid_time_parts(plan, uvw, freq, vis, n_threads=0, n_planes_timed=1):
+    op = to_oracle_plan(plan)
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    vis = np.ascontiguousarray(vis, np.complex64)
+    ps = C.c_double()
+    t = lib().oracle_wgrid_time_parts(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq),
+                                      _p(vis), n_threads, n_planes_timed, C.byref(ps))
+    return t, ps.value
+
+
+def es_kernel(beta, z):
+    return lib().oracle_es_kernel(beta, z)
+
+
+def es_fourier(beta, support, f):
+    return lib().oracle_es_fourier(beta, support, f)
+
+
+def apply_gains(mode, n_pol, vis, antenna_pairs, time_offsets, solutions, nparms, n_ant,
+                polarization=0):
+    vis = np.ascontiguousarray(vis, np.complex64)
+    n_rows, n_chan = vis.shape[0], vis.shape[1]
+    ant = np.ascontiguousarray(antenna_pairs, np.uint64)
+    tof = np.ascontiguousarray(time_offsets, np.uint64)
+    sol = np.ascontiguousarray(solutions, np.complex64)
+    out = np.zeros((n_rows, n_chan), np.complex64)
+    r = lib().oracle_apply_gains(mode, n_pol, n_rows, n_chan, _p(vis), _p(ant), _p(tof),
+                                 _p(sol), nparms, n_ant, polarization, _p(out))
+    if r != 0:
+        raise ValueError("invalid gain mode / polarisation combination")
+    return out
+
+
+def apply_conjugated_gain(mode, vis, g1, g2):
+    v = np.ascontiguousarray(vis, np.complex64).copy()
+    a = np.ascontiguousarray(g1, np.complex64)
+    b = np.ascontiguousarray(g2, np.complex64)
+    lib().oracle_apply_conjugated_gain(mode, _p(v), _p(a), _p(b))
+    return v
+
+
+def apply_gain(mode, vis, g1, g2):
+    v = np.ascontiguousarray(vis, np.complex64).copy()
+    a = np.ascontiguousarray(g1, np.complex64)
+    b = np.ascontiguousarray(g2, np.complex64)
+    lib().oracle_apply_gain(mode, _p(v), _p(a), _p(b))
+    return v

@@ -1,0 +1,127 @@
+/*
+ * wgpu oracle -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU (FP64) restatements used to check the GPU w-gridder.  Nothing in the
+ * product links or calls this code; only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py use it, as the checker.
+ *
+ * Parity status:
+ *  - Direct Fourier transform: restates gridding/directmsgridder.cpp (the
+ *    reference's own exact transform).  The reference file cannot be compiled
+ *    here (it needs aocommon, casacore and the MsGridder stack), so the
+ *    restatement is pinned by analytic known-answer tests (point sources on
+ *    pixel centres, constant visibilities) written against the conventions of
+ *    directmsgridder.cpp:56-132,205-229.
+ *  - W-gridder: the reference's arithmetic lives in ducc0 (called from
+ *    wgridder/gridder_simple.h:217-225), which is absent from the reference
+ *    tree.  The FP64 CPU w-gridder below follows the published method (Arras et
+ *    al. 2021; Ye et al. 2021) with the same flags WSClean passes; its parity
+ *    with ducc0 itself is UNPINNED.  It is checked against the DFT.
+ *  - Gains and polarisation collapse: restate gridding/visibilitymodifier.h:
+ *    378-401,538-594 and gridding/msgridderdata.h:36-52, pinned by the
+ *    known-answer constants of tests/gridding/tvisibilitymodifier.cpp.
+ */
+#ifndef WGPU_ORACLE_H_
+#define WGPU_ORACLE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Direct FT inversion (directmsgridder.cpp:92-132): for each selected trimmed
+ * pixel p = x + y*width, out[i] = sum_k Re(V_k exp(-2 pi i (u l + v m + w (n-1))))
+ * with l = (width/2 - x) dl + l_shift, m = (y - height/2) dm + m_shift and
+ * n-1 := 0 beyond the horizon (directmsgridder.cpp:205-229).  uvw in metres,
+ * freq in Hz, vis interleaved complex64 [row][chan].  No 1/ImageWeight. */
+void oracle_dft_invert(size_t n_rows, size_t n_chan, const double *uvw,
+                       const double *freq, const float *vis, size_t width,
+                       size_t height, double dl, double dm, double l_shift,
+                       double m_shift, const int64_t *pixels, size_t n_pixels,
+                       int n_threads, double *out);
+
+/* Adjoint of oracle_dft_invert (prediction): for selected visibility
+ * indices e = row*n_chan + chan, out[2i..2i+1] = sum_p I_p exp(+2 pi i (...)).
+ * image is width*height doubles, row-major [x + y*width]. */
+void oracle_dft_predict(size_t n_rows, size_t n_chan, const double *uvw,
+                        const double *freq, const double *image, size_t width,
+                        size_t height, double dl, double dm, double l_shift,
+                        double m_shift, const int64_t *vis_index, size_t n_sel,
+                        int n_threads, double *out);
+
+/* Parameters of one gridding plan (all produced by the product's planner). */
+typedef struct {
+  int64_t width, height;   /* trimmed image */
+  int64_t nu, nv;          /* padded grid */
+  int64_t support;         /* W */
+  int64_t tile;            /* uv tile edge in cells */
+  int64_t n_planes;        /* w planes */
+  double beta;             /* ES kernel beta */
+  double dl, dm, l_shift, m_shift;
+  double w0, dw;           /* plane p sits at w0 + p dw (lambda) */
+  double nm1_center;       /* c_n: centre of the image's n-1 range */
+} OraclePlan;
+
+/* Bucketing reference: for every included element (inversion: vis != 0;
+ * prediction: all) computes the integer footprint corner, fractions and key
+ * exactly as the GPU pass defines them, then stable counting-sorts by key.
+ * Outputs (n_out elements): perm[s] = element index, key[s], iu/iv/ip, fu/fv/fw.
+ * offsets has n_tiles*n_planes+1 entries.  Returns n_out. */
+int64_t oracle_bucket(const OraclePlan *plan, size_t n_rows, size_t n_chan,
+                      const double *uvw, const double *freq, const float *vis,
+                      int skip_zero, uint32_t *perm, int64_t *key, int32_t *iu,
+                      int32_t *iv, int32_t *ip, float *fu, float *fv,
+                      float *fw, int64_t *offsets);
+
+/* FP64 CPU w-gridder, inversion: dirty[x + y*width] (trimmed, DFT
+ * orientation) = sum over included vis, computed by gridding + FFT + w-screen +
+ * correction.  Returns 0 on success. */
+int oracle_wgrid_invert(const OraclePlan *plan, size_t n_rows, size_t n_chan,
+                        const double *uvw, const double *freq, const float *vis,
+                        int n_threads, double *dirty);
+
+/* FP64 CPU w-gridder, prediction (adjoint): vis_out interleaved complex
+ * doubles [row][chan]. */
+int oracle_wgrid_predict(const OraclePlan *plan, size_t n_rows, size_t n_chan,
+                         const double *uvw, const double *freq,
+                         const double *image, int n_threads, double *vis_out);
+
+/* Timing helper for the CPU baseline: grids (no FFT) the included visibilities
+ * onto the planes they touch, in FP64, and returns seconds spent; and runs
+ * n_planes_timed full plane FFT+screen steps, returning seconds spent in
+ * *plane_seconds. */
+double oracle_wgrid_time_parts(const OraclePlan *plan, size_t n_rows,
+                               size_t n_chan, const double *uvw,
+                               const double *freq, const float *vis,
+                               int n_threads, int n_planes_timed,
+                               double *plane_seconds);
+
+/* ES kernel value at z in [-1,1] and its continuous FT in cell units. */
+double oracle_es_kernel(double beta, double z);
+double oracle_es_fourier(double beta, int support, double f);
+
+/* Gains (visibilitymodifier.h:378-401) applied in conjugate for every row and
+ * channel, followed by the polarisation collapse (msgridderdata.h:36-52).
+ * mode: 0 kXX, 1 kYY, 2 kTrace, 3 k2VisDiagonal, 4 kFull (gainmode.h:16-31).
+ * vis_in: [row][chan][n_pol] complex64; solutions: complex64 with the cached
+ * parm-response layout ((t*n_chan + ch)*n_ant + ant)*nparms; out: collapsed
+ * [row][chan] complex64.  polarization (4-pol collapse): 0 StokesI, 1 Q, 2 U,
+ * 3 V, 4 XX, 5 XY, 6 YX, 7 YY.  Returns 0 on success, -1 on a bad combination. */
+int oracle_apply_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
+                       const float *vis_in, const uint64_t *antenna_pairs,
+                       const uint64_t *time_offsets, const float *solutions,
+                       size_t nparms, size_t n_ant, int polarization,
+                       float *out);
+
+/* Single-visibility-group gain application used by the known-answer tests. */
+void oracle_apply_conjugated_gain(int mode, float *vis, const float *g1,
+                                  const float *g2);
+void oracle_apply_gain(int mode, float *vis, const float *g1, const float *g2);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

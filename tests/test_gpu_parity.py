@@ -1,0 +1,247 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle.
+
+Tolerances: bucketing is bit-exact; images and predicted visibilities must be
+within the requested epsilon (relative L2 against the FP64 direct FT) and within
+max(epsilon/4, 2e-6) of the FP64 CPU w-gridder run on the same plan.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from wsclean_gb300 import _lib, synthetic
+from wsclean_gb300.gridder import WGriddingGridder_Simple, bucket_debug
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+C = 299792458.0
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+def _plan_for(uvw, freq, vis, W, dl, eps, shift=(0.0, 0.0), **kw):
+    wl = uvw[:, 2:3] * (freq / C)[None, :]
+    if vis is not None:
+        wl = wl[vis != 0]
+    return _lib.make_plan(width=W, height=W, dl=dl, dm=dl, l_shift=shift[0], m_shift=shift[1],
+                          epsilon=eps, w_min=float(wl.min()), w_max=float(wl.max()),
+                          n_vis=int(wl.size), **kw)
+
+
+BUCKET_CASES = [
+    dict(W=96, dl=1e-3, rows=700, chan=5, w_scale=1.0, zero=0.2, seed=1, shift=(0, 0), inv=True),
+    dict(W=256, dl=3e-4, rows=3000, chan=8, w_scale=3.0, zero=0.0, seed=2, shift=(0.01, -0.02),
+         inv=False),
+    dict(W=128, dl=5e-4, rows=1500, chan=3, w_scale=0.0, zero=0.1, seed=3, shift=(0, 0), inv=True),
+    dict(W=512, dl=1e-4, rows=5000, chan=16, w_scale=2.0, zero=0.3, seed=4, shift=(0, 0.003),
+         inv=True),
+]
+
+
+@pytest.mark.parametrize("case", BUCKET_CASES)
+def test_bucketing_bit_exact(wgpu_lib, oracle_lib, case):
+    uvw, freq, vis = synthetic.random_points(case["rows"], case["chan"], case["W"], case["dl"],
+                                             case["seed"], w_scale=case["w_scale"],
+                                             frac_zero=case["zero"])
+    if case["seed"] == 2:
+        freq = freq[::-1].copy()  # descending frequencies
+    p = _plan_for(uvw, freq, vis if case["inv"] else None, case["W"], case["dl"], 1e-4,
+                  case["shift"])
+    got = bucket_debug(p, uvw.shape[0], freq.size, uvw, freq, vis if case["inv"] else None,
+                       case["inv"])
+    ref = oracle_lib.bucket(p, uvw, freq, vis if case["inv"] else None, case["inv"])
+    for k in ("perm", "iu", "iv", "ip", "fu", "fv", "fw"):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(got["offsets"].astype(np.int64), ref["offsets"])
+
+
+def test_bucketing_matches_golden_fixture(wgpu_lib):
+    g = np.load(os.path.join(GOLDEN, "bucket_small.npz"))
+    plan = json.loads(str(g["plan"]))
+    p = _lib.Plan()
+    for k, v in plan.items():
+        setattr(p, k, v)
+    got = bucket_debug(p, g["uvw"].shape[0], g["freq"].size, g["uvw"], g["freq"], g["vis"], True)
+    for k in ("perm", "iu", "iv", "ip", "fu", "fv", "fw"):
+        np.testing.assert_array_equal(got[k], g[k], err_msg=k)
+    np.testing.assert_array_equal(got["offsets"].astype(np.int64), g["offsets"])
+
+
+INV_CASES = [
+    dict(W=128, dl=4e-4, eps=1e-4, shift=(0.0, 0.0), num_t=np.float32, w_scale=3.0),
+    dict(W=128, dl=4e-4, eps=1e-5, shift=(0.01, -0.005), num_t=np.float64, w_scale=3.0),
+    dict(W=256, dl=2e-4, eps=1e-5, shift=(0.0, 0.0), num_t=np.float64, w_scale=1.0),
+    dict(W=192, dl=3e-4, eps=1e-3, shift=(-0.004, 0.002), num_t=np.float32, w_scale=0.0),
+]
+
+
+@pytest.mark.parametrize("case", INV_CASES)
+def test_inversion_matches_dft_and_cpu_gridder(wgpu_lib, oracle_lib, case):
+    W, dl, eps = case["W"], case["dl"], case["eps"]
+    uvw, freq, vis = synthetic.random_points(600, 4, W, dl, seed=5, w_scale=case["w_scale"],
+                                             frac_zero=0.1)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, case["shift"][0], case["shift"][1], 1,
+                                epsilon=eps, num_t=case["num_t"])
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    g.FinalizeImage(1.0)
+    img = g.RealImage().astype(np.float64)
+    plan = g.last_plan()
+    ref = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, *case["shift"])
+    assert rel(img, ref) <= eps
+    cpu = oracle_lib.wgrid_invert(plan, uvw, freq, vis)
+    assert rel(img, cpu) <= max(eps / 4, 2e-6)
+    g.close()
+
+
+def test_inversion_in_chunks_with_trim_and_descending_freq(wgpu_lib, oracle_lib):
+    W, Wt, dl = 160, 128, 4e-4
+    uvw, freq, vis = synthetic.random_points(900, 6, Wt, dl, seed=8, w_scale=2.0, frac_zero=0.05)
+    freq = freq[::-1].copy()
+    g = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=1e-4)
+    g.InitializeInversion()
+    for r0 in range(0, 900, 300):
+        g.AddInversionData(300, freq.size, uvw[r0:r0 + 300], freq, vis[r0:r0 + 300])
+    g.FinalizeImage(0.5)
+    full = g.RealImage().reshape(W, W)
+    d = (W - Wt) // 2
+    assert np.all(np.isnan(full[:d, :])) and np.all(np.isnan(full[:, :d]))
+    assert np.all(np.isnan(full[W - d:, :])) and np.all(np.isnan(full[:, W - d:]))
+    img = full[d:d + Wt, d:d + Wt].astype(np.float64).ravel()
+    ref = 0.5 * oracle_lib.dft_invert(uvw, freq, vis, Wt, Wt, dl, dl)
+    assert rel(img, ref) <= 1e-4
+    g.close()
+
+
+PRED_CASES = [
+    dict(W=128, dl=4e-4, eps=1e-4, shift=(0.0, 0.0), w_scale=3.0, n_src=12),
+    dict(W=256, dl=2e-4, eps=1e-5, shift=(0.01, -0.005), w_scale=2.0, n_src=40),
+    dict(W=128, dl=4e-4, eps=1e-5, shift=(0.0, 0.0), w_scale=0.0, n_src=5),
+]
+
+
+@pytest.mark.parametrize("case", PRED_CASES)
+def test_prediction_matches_dft_and_cpu_gridder(wgpu_lib, oracle_lib, case):
+    W, dl, eps = case["W"], case["dl"], case["eps"]
+    uvw, freq, _ = synthetic.random_points(800, 4, W, dl, seed=6, w_scale=case["w_scale"])
+    rng = np.random.default_rng(3)
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, case["n_src"], replace=False)] = rng.uniform(-1, 1, case["n_src"])
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, case["shift"][0], case["shift"][1], 1,
+                                epsilon=eps)
+    g.InitializePrediction(model)
+    pv = g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq)
+    plan = g.last_plan()
+    pr = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl, *case["shift"])
+    assert rel(pv, pr) <= eps
+    cpu = oracle_lib.wgrid_predict(plan, uvw, freq, model)
+    assert rel(pv, cpu) <= max(eps / 4, 2e-6)
+    g.close()
+
+
+def test_prediction_is_adjoint_of_inversion(wgpu_lib):
+    W, dl = 128, 4e-4
+    uvw, freq, vis = synthetic.random_points(700, 4, W, dl, seed=12, w_scale=2.0)
+    rng = np.random.default_rng(5)
+    img = rng.standard_normal(W * W).astype(np.float32)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.003, 0.001, 1, epsilon=1e-5,
+                                num_t=np.float64)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    a = g.RealImage().astype(np.float64)
+    g.InitializePrediction(img)
+    b = g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq).astype(np.complex128)
+    lhs = float(np.dot(a, img))
+    rhs = float(np.real(np.vdot(b, vis.ravel().astype(np.complex128))))
+    assert abs(lhs - rhs) <= 3e-5 * abs(lhs)
+    g.close()
+
+
+def test_golden_dft_fixture_through_gpu(wgpu_lib):
+    gld = np.load(os.path.join(GOLDEN, "dft_small.npz"))
+    W, dl = int(gld["width"]), float(gld["dl"])
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, float(gld["l_shift"]), float(gld["m_shift"]),
+                                1, epsilon=1e-5, num_t=np.float64)
+    g.InitializeInversion()
+    g.AddInversionData(gld["uvw"].shape[0], gld["freq"].size, gld["uvw"], gld["freq"], gld["vis"])
+    assert rel(g.RealImage(), gld["image"]) <= 1e-5
+    g.InitializePrediction(gld["model"].astype(np.float32))
+    pv = g.PredictVisibilities(gld["uvw"].shape[0], gld["freq"].size, gld["uvw"], gld["freq"])
+    assert rel(pv, gld["pred"]) <= 1e-5
+    g.close()
+
+
+def test_empty_and_all_zero_inputs(wgpu_lib):
+    W, dl = 64, 1e-3
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1)
+    g.InitializeInversion()
+    g.AddInversionData(0, 4, np.zeros((0, 3)), np.linspace(1e8, 2e8, 4),
+                       np.zeros((0, 4), np.complex64))
+    g.AddInversionData(10, 2, np.ones((10, 3)), np.array([1e8, 1.1e8]),
+                       np.zeros((10, 2), np.complex64))
+    assert np.all(g.RealImage() == 0)
+    g.close()
+
+
+def test_call_order_errors(wgpu_lib):
+    g = WGriddingGridder_Simple(64, 64, 64, 64, 1e-3, 1e-3, 0, 0, 1)
+    with pytest.raises(_lib.WgpuError) as e:
+        g.AddInversionData(1, 1, np.zeros((1, 3)), np.array([1e8]), np.ones(1, np.complex64))
+    assert e.value.status == _lib.WGPU_ERR_STATE
+    with pytest.raises(_lib.WgpuError) as e:
+        g.PredictVisibilities(1, 1, np.zeros((1, 3)), np.array([1e8]))
+    assert e.value.status == _lib.WGPU_ERR_STATE
+    g.close()
+
+
+MODES = [("xx", 1, 2), ("yy", 1, 4), ("trace", 1, 4), ("diagonal", 2, 2), ("diagonal", 2, 4),
+         ("full", 4, 4)]
+
+
+@pytest.mark.parametrize("mode,n_pol,nparms", MODES)
+def test_corrected_inversion_matches_oracle_gains(wgpu_lib, oracle_lib, mode, n_pol, nparms):
+    from wsclean_gb300.gridder import GainMode
+    W, dl = 128, 4e-4
+    rng = np.random.default_rng(21)
+    n_rows, n_chan, n_ant, n_t = 400, 4, 8, 3
+    uvw, freq, _ = synthetic.random_points(n_rows, n_chan, W, dl, seed=22, w_scale=1.0)
+    vis = (rng.standard_normal((n_rows, n_chan, n_pol)) +
+           1j * rng.standard_normal((n_rows, n_chan, n_pol))).astype(np.complex64)
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)], 1)
+    tof = rng.integers(0, n_t, n_rows)
+    sol = (1 + 0.3 * (rng.standard_normal((n_t, n_chan, n_ant, nparms)) +
+                      1j * rng.standard_normal((n_t, n_chan, n_ant, nparms)))).astype(np.complex64)
+    corrected = oracle_lib.apply_gains(GainMode[mode], n_pol, vis, ant, tof, sol, nparms, n_ant)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=1e-5, num_t=np.float64)
+    g.InitializeInversion()
+    g.AddInversionDataWithCorrectionCallback(mode, n_pol, n_rows, uvw, freq, n_chan, ant, vis,
+                                             tof, sol, nparms, n_t, n_ant)
+    got = g.RealImage().astype(np.float64)
+    g.InitializeInversion()
+    g.AddInversionData(n_rows, n_chan, uvw, freq, corrected)
+    exp = g.RealImage().astype(np.float64)
+    assert rel(got, exp) <= 2e-6
+    ref = oracle_lib.dft_invert(uvw, freq, corrected, W, W, dl, dl)
+    assert rel(got, ref) <= 1e-5
+    g.close()
+
+
+def test_corrected_inversion_rejects_bad_indices(wgpu_lib):
+    W, dl = 64, 1e-3
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1)
+    g.InitializeInversion()
+    uvw, freq, _ = synthetic.random_points(4, 2, W, dl, seed=1)
+    vis = np.ones((4, 2, 1), np.complex64)
+    ant = np.array([[0, 1], [0, 2], [1, 9], [0, 1]])
+    sol = np.ones((1, 2, 3, 2), np.complex64)
+    with pytest.raises(_lib.WgpuError) as e:
+        g.AddInversionDataWithCorrectionCallback("xx", 1, 4, uvw, freq, 2, ant, vis,
+                                                 np.zeros(4, np.uint64), sol, 2, 1, 3)
+    assert e.value.status == _lib.WGPU_ERR_INVALID
+    with pytest.raises(_lib.WgpuError):
+        g.AddInversionDataWithCorrectionCallback("full", 1, 4, uvw, freq, 2, ant, vis,
+                                                 np.zeros(4, np.uint64), sol, 2, 1, 3)
+    g.close()

@@ -1,0 +1,123 @@
+"""ctypes binding of the C ABI declared in include/wgpu.h.
+
+The shared library is the in-tree build wsclean_gb300/_build/libwgpu.so.  There
+is no fallback: if the library is missing or cannot load, every entry point
+raises.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwgpu.so")
+
+WGPU_OK = 0
+WGPU_ERR_INVALID = -1
+WGPU_ERR_CUDA = -2
+WGPU_ERR_NOMEM = -3
+WGPU_ERR_STATE = -4
+WGPU_ERR_TIMEOUT = -5
+
+GAIN_XX, GAIN_YY, GAIN_TRACE, GAIN_2VIS_DIAGONAL, GAIN_FULL = range(5)
+POL_I, POL_Q, POL_U, POL_V, POL_XX, POL_XY, POL_YX, POL_YY = range(8)
+
+
+class WgpuError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"wgpu status {status}: {message}")
+        self.status = status
+
+
+class Plan(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "width", "height", "nu", "nv", "support", "tile", "n_planes", "plane_batch",
+        "fft_n1", "fft_n2")] + [(n, C.c_double) for n in (
+        "sigma", "beta", "dl", "dm", "l_shift", "m_shift", "w0", "dw", "nm1_min",
+        "nm1_max", "nm1_center", "est_error", "est_seconds")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PlanRequest(C.Structure):
+    _fields_ = [("width", C.c_int64), ("height", C.c_int64), ("dl", C.c_double),
+                ("dm", C.c_double), ("l_shift", C.c_double), ("m_shift", C.c_double),
+                ("epsilon", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double),
+                ("n_vis", C.c_int64), ("sigma_min", C.c_double), ("sigma_max", C.c_double),
+                ("force_support", C.c_int64), ("force_sigma", C.c_double),
+                ("force_tile", C.c_int64), ("max_plane_batch", C.c_int64),
+                ("memory_budget_bytes", C.c_double)]
+
+
+_lib = None
+
+P = C.c_void_p
+SZ = C.c_size_t
+D = C.c_double
+I = C.c_int
+
+_PROTOS = {
+    "wgpu_last_error": (C.c_char_p, []),
+    "wgpu_version": (C.c_char_p, []),
+    "wgpu_plan_make": (I, [C.POINTER(PlanRequest), C.POINTER(Plan)]),
+    "wgpu_gridder_create": (I, [SZ, SZ, SZ, SZ, D, D, D, D, SZ, D, SZ, I, I, C.POINTER(P)]),
+    "wgpu_gridder_destroy": (None, [P]),
+    "wgpu_gridder_constant_memory": (SZ, [P]),
+    "wgpu_gridder_per_visibility_memory": (SZ, [P]),
+    "wgpu_gridder_initialize_inversion": (I, [P]),
+    "wgpu_gridder_add_inversion_data": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_add_inversion_data_device": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_add_inversion_data_corrected": (
+        I, [P, I, SZ, SZ, P, P, SZ, P, P, P, P, SZ, SZ, SZ, I]),
+    "wgpu_gridder_finalize_image": (I, [P, D]),
+    "wgpu_gridder_real_image": (I, [P, P]),
+    "wgpu_gridder_initialize_prediction": (I, [P, P]),
+    "wgpu_gridder_predict_visibilities": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_predict_visibilities_device": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_last_plan": (I, [P, C.POINTER(Plan)]),
+    "wgpu_gridder_last_timings": (I, [P, C.POINTER(C.c_double), I, C.c_char_p, SZ,
+                                      C.POINTER(I)]),
+    "wgpu_gridder_stream": (P, [P]),
+    "wgpu_kernel_launch_count": (C.c_uint64, []),
+    "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,
+                              C.POINTER(C.c_int64)]),
+}
+
+
+def lib():
+    """Loads libwgpu.so (building nothing); raises if it is absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise WgpuError(WGPU_ERR_CUDA, f"{LIB_PATH} is missing; run "
+                            "python -m wsclean_gb300.build")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_PROTOS)
+
+
+def check(status):
+    if status != WGPU_OK:
+        msg = lib().wgpu_last_error().decode(errors="replace")
+        raise WgpuError(status, msg)
+
+
+def ptr(a):
+    """Address of a numpy array's data (None for None)."""
+    return None if a is None else a.ctypes.data
+
+
+def make_plan(**kw):
+    r = PlanRequest()
+    for k, v in kw.items():
+        setattr(r, k, v)
+    p = Plan()
+    check(lib().wgpu_plan_make(C.byref(r), C.byref(p)))
+    return p

@@ -1,0 +1,634 @@
+// C-ABI implementation: the gridder object and the inversion / prediction
+// pipelines (host orchestration of the CUDA kernels on one stream).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "wgpu_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &msg) {
+  g_last_error = msg;
+  return status;
+}
+
+template <typename F>
+int guarded(F &&f) {
+  try {
+    g_last_error.clear();
+    f();
+    return WGPU_OK;
+  } catch (const wgpu::Error &e) {
+    return fail(e.status, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(WGPU_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(WGPU_ERR_INVALID, e.what());
+  }
+}
+
+}  // namespace
+
+// Stage timer: events recorded on the gridder stream between launches; the
+// elapsed time of each interval is charged to the stage that opened it.
+struct StageTimer {
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::string> names;
+  size_t used = 0;
+  cudaStream_t stream = nullptr;
+
+  void begin(cudaStream_t s) {
+    stream = s;
+    used = 0;
+    names.clear();
+  }
+  void mark(const char *name) {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      WGPU_CUDA(cudaEventCreate(&e));
+      pool.push_back(e);
+    }
+    WGPU_CUDA(cudaEventRecord(pool[used++], stream));
+    names.push_back(name);
+  }
+  // Returns totals per stage name (last mark is the end marker).
+  std::vector<std::pair<std::string, double>> collect() {
+    std::vector<std::pair<std::string, double>> out;
+    if (used < 2) return out;
+    WGPU_CUDA(cudaEventSynchronize(pool[used - 1]));
+    std::map<std::string, double> acc;
+    std::vector<std::string> order;
+    for (size_t i = 0; i + 1 < used; ++i) {
+      float ms = 0.f;
+      WGPU_CUDA(cudaEventElapsedTime(&ms, pool[i], pool[i + 1]));
+      if (!acc.count(names[i])) order.push_back(names[i]);
+      acc[names[i]] += ms;
+    }
+    for (auto &n : order) out.emplace_back(n, acc[n]);
+    return out;
+  }
+  ~StageTimer() {
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+struct wgpu_gridder {
+  size_t width, height, width_t, height_t, nthreads, verbosity;
+  double dl, dm, l_shift, m_shift, epsilon;
+  bool tuning;
+  int prec;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  wgpu::DeviceArena arena;
+  wgpu::FftTables *fft = nullptr;
+  void *d_img = nullptr;
+  enum class Mode { kNone, kInversion, kPrediction } mode = Mode::kNone;
+  wgpu_plan_t last_plan;
+  StageTimer timer;
+  std::vector<std::pair<std::string, double>> last_timings;
+};
+
+namespace wgpu {
+namespace {
+
+constexpr int kGlNodes = 48;
+
+size_t image_bytes(const wgpu_gridder *g) {
+  return g->width_t * g->height_t * (size_t)g->prec;
+}
+
+void ensure_image(wgpu_gridder *g) {
+  if (!g->d_img) WGPU_CUDA(cudaMalloc(&g->d_img, image_bytes(g)));
+}
+
+// Host-side correction tables for one plan: cx, cy (1/psihat per column/row)
+// and the quadrature nodes (z_q, w_q phi(z_q)) for the per-pixel w factor.
+void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
+                        float **cy, float **gl) {
+  std::vector<float> hx(plan.width), hy(plan.height), hg(2 * kGlNodes);
+  for (int64_t x = 0; x < plan.width; ++x)
+    hx[x] = (float)(1.0 / es_fourier(plan.beta, (int)plan.support,
+                                     (double)(plan.width / 2 - x) / (double)plan.nu));
+  for (int64_t y = 0; y < plan.height; ++y)
+    hy[y] = (float)(1.0 / es_fourier(plan.beta, (int)plan.support,
+                                     (double)(y - plan.height / 2) / (double)plan.nv));
+  // Gauss-Legendre rule of 2*kGlNodes points on [-1, 1], positive half
+  const int n = 2 * kGlNodes;
+  for (int i = 0; i < kGlNodes; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= n; ++k) {
+      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    const double w = 2.0 / ((1.0 - z * z) * dp * dp);
+    hg[2 * i] = (float)z;
+    hg[2 * i + 1] = (float)(w * es_kernel(plan.beta, z));
+  }
+  *cx = (float *)g->arena.get(kSlotCorrX, sizeof(float) * plan.width);
+  *cy = (float *)g->arena.get(kSlotCorrY, sizeof(float) * plan.height);
+  *gl = (float *)g->arena.get(kSlotGl, sizeof(float) * 2 * kGlNodes);
+  WGPU_CUDA(cudaMemcpyAsync(*cx, hx.data(), sizeof(float) * plan.width, cudaMemcpyHostToDevice, g->stream));
+  WGPU_CUDA(cudaMemcpyAsync(*cy, hy.data(), sizeof(float) * plan.height, cudaMemcpyHostToDevice, g->stream));
+  WGPU_CUDA(cudaMemcpyAsync(*gl, hg.data(), sizeof(float) * 2 * kGlNodes, cudaMemcpyHostToDevice, g->stream));
+  // the host vectors die at return: make the copies complete first
+  WGPU_CUDA(cudaStreamSynchronize(g->stream));
+}
+
+wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis) {
+  wgpu_plan_request_t r;
+  std::memset(&r, 0, sizeof(r));
+  r.width = (int64_t)g->width_t;
+  r.height = (int64_t)g->height_t;
+  r.dl = g->dl;
+  r.dm = g->dm;
+  r.l_shift = g->l_shift;
+  r.m_shift = g->m_shift;
+  r.epsilon = g->epsilon;
+  r.w_min = w_min;
+  r.w_max = w_max;
+  r.n_vis = n_vis;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+    r.memory_budget_bytes = std::min(24e9, 0.4 * (double)(free_b + g->arena.total()));
+  }
+  return make_plan(r);
+}
+
+void log_plan(const wgpu_gridder *g, const char *what, const wgpu_plan_t &p,
+              int64_t n_vis) {
+  if (g->verbosity == 0) return;
+  std::fprintf(stderr,
+               "wgpu %s: %lld vis, image %lldx%lld, grid %lldx%lld, W=%lld sigma=%.2f "
+               "beta=%.3f planes=%lld (batch %lld) est.err=%.2e\n",
+               what, (long long)n_vis, (long long)p.width, (long long)p.height,
+               (long long)p.nu, (long long)p.nv, (long long)p.support, p.sigma,
+               p.beta, (long long)p.n_planes, (long long)p.plane_batch,
+               p.est_error);
+}
+
+void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
+                   const double *d_uvw, const double *d_freq, const float *d_vis) {
+  if (g->mode != wgpu_gridder::Mode::kInversion)
+    throw Error(WGPU_ERR_STATE, "AddInversionData before InitializeInversion");
+  if (n_rows == 0 || n_chan == 0) return;
+  cudaStream_t s = g->stream;
+  g->timer.begin(s);
+  g->timer.mark("extent");
+  double w_min, w_max;
+  int64_t count;
+  compute_w_extent(d_uvw, d_freq, d_vis, (int64_t)n_rows, (int64_t)n_chan, true,
+                   &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
+  if (count == 0) {
+    g->timer.mark("end");
+    g->last_timings = g->timer.collect();
+    return;
+  }
+  const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
+  g->last_plan = plan;
+  log_plan(g, "invert", plan, count);
+  const DevPlan dp = to_dev_plan(plan);
+  g->timer.mark("bucket");
+  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis,
+                                             (int64_t)n_rows, (int64_t)n_chan, true, s);
+  g->timer.mark("setup");
+  const int64_t npix = plan.width * plan.height;
+  const int rstride = (int)((plan.width + 31) / 32 * 32);
+  double *nu_w = (double *)g->arena.get(kSlotNuW, sizeof(double) * npix);
+  float2 *acc = (float2 *)g->arena.get(kSlotAcc, sizeof(float2) * npix);
+  const int64_t B = plan.plane_batch;
+  float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
+  float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
+  launch_nu_table(dp, nu_w, s);
+  WGPU_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * npix, s));
+  for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
+    const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+    g->timer.mark("grid");
+    launch_grid(dp, b.records, b.offsets, (int)p0, nb, planes, s);
+    g->timer.mark("fft_rows");
+    launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, s);
+    g->timer.mark("fft_cols_screen");
+    launch_fft_cols_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R,
+                                       rstride, nb, (int)p0, nu_w, acc, s);
+    if (g->verbosity >= 2)
+      std::fprintf(stderr, "wgpu invert: planes %lld..%lld\n", (long long)p0,
+                   (long long)(p0 + nb - 1));
+  }
+  g->timer.mark("finalize");
+  float *cx, *cy, *gl;
+  upload_corrections(g, plan, &cx, &cy, &gl);
+  launch_finalize_add(dp, acc, nu_w, cx, cy, gl, kGlNodes, g->d_img, g->prec, s);
+  g->timer.mark("end");
+  g->last_timings = g->timer.collect();
+}
+
+void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
+                    const double *d_uvw, const double *d_freq, float *d_vis) {
+  if (g->mode != wgpu_gridder::Mode::kPrediction)
+    throw Error(WGPU_ERR_STATE, "PredictVisibilities before InitializePrediction");
+  if (n_rows == 0 || n_chan == 0) return;
+  cudaStream_t s = g->stream;
+  g->timer.begin(s);
+  g->timer.mark("extent");
+  double w_min, w_max;
+  int64_t count;
+  compute_w_extent(d_uvw, d_freq, nullptr, (int64_t)n_rows, (int64_t)n_chan, false,
+                   &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
+  const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
+  g->last_plan = plan;
+  log_plan(g, "predict", plan, count);
+  const DevPlan dp = to_dev_plan(plan);
+  g->timer.mark("bucket");
+  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, nullptr,
+                                             (int64_t)n_rows, (int64_t)n_chan, false, s);
+  g->timer.mark("setup");
+  const int64_t npix = plan.width * plan.height;
+  const int rstride = (int)((plan.width + 31) / 32 * 32);
+  double *nu_w = (double *)g->arena.get(kSlotNuW, sizeof(double) * npix);
+  float *img_corr = (float *)g->arena.get(kSlotImgCorr, sizeof(float) * npix);
+  float2 *vacc = (float2 *)g->arena.get(kSlotVisAcc, sizeof(float2) * (b.n_out + 1));
+  const int64_t B = plan.plane_batch;
+  float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
+  float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
+  launch_nu_table(dp, nu_w, s);
+  float *cx, *cy, *gl;
+  upload_corrections(g, plan, &cx, &cy, &gl);
+  launch_precorrect(dp, g->d_img, g->prec, nu_w, cx, cy, gl, kGlNodes, img_corr, s);
+  WGPU_CUDA(cudaMemsetAsync(vacc, 0, sizeof(float2) * (b.n_out + 1), s));
+  for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
+    const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+    g->timer.mark("fft_cols_screen");
+    launch_fft_cols_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                    img_corr, nu_w, R, rstride, nb, (int)p0, s);
+    g->timer.mark("fft_rows");
+    launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, s);
+    g->timer.mark("degrid");
+    launch_degrid(dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
+  }
+  g->timer.mark("finalize");
+  launch_unpermute_predict(b.records, b.perm, vacc, b.n_out, (float2 *)d_vis, s);
+  g->timer.mark("end");
+  g->last_timings = g->timer.collect();
+}
+
+template <typename T>
+T *upload(wgpu_gridder *g, int slot, const T *h, size_t n) {
+  T *d = (T *)g->arena.get(slot, sizeof(T) * (n ? n : 1));
+  if (n) WGPU_CUDA(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, g->stream));
+  return d;
+}
+
+}  // namespace
+}  // namespace wgpu
+
+using namespace wgpu;
+
+extern "C" {
+
+const char *wgpu_last_error(void) { return g_last_error.c_str(); }
+
+const char *wgpu_version(void) { return "wgpu 0.1 (sm_103a)"; }
+
+int wgpu_plan_make(const wgpu_plan_request_t *request, wgpu_plan_t *plan) {
+  if (!request || !plan) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] { *plan = make_plan(*request); });
+}
+
+int wgpu_gridder_create(size_t width, size_t height, size_t width_t,
+                        size_t height_t, double pixel_size_x,
+                        double pixel_size_y, double l_shift, double m_shift,
+                        size_t nthreads, double epsilon, size_t verbosity,
+                        int tuning, int precision_bytes,
+                        wgpu_gridder_t **gridder) {
+  if (!gridder) return fail(WGPU_ERR_INVALID, "null gridder pointer");
+  *gridder = nullptr;
+  if (verbosity > 2) return fail(WGPU_ERR_INVALID, "verbosity must be 0, 1, or 2");
+  if (precision_bytes != 4 && precision_bytes != 8)
+    return fail(WGPU_ERR_INVALID, "precision_bytes must be 4 or 8");
+  if (width_t > width || height_t > height || width_t == 0 || height_t == 0)
+    return fail(WGPU_ERR_INVALID, "trimmed size must be non-zero and fit the image");
+  if ((width_t & 1) || (height_t & 1))
+    return fail(WGPU_ERR_INVALID, "trimmed image dimensions must be even");
+  if (!(pixel_size_x > 0) || !(pixel_size_y > 0) || !(epsilon > 0))
+    return fail(WGPU_ERR_INVALID, "pixel sizes and epsilon must be positive");
+  return guarded([&] {
+    int n_dev = 0;
+    cudaError_t e = cudaGetDeviceCount(&n_dev);
+    if (e != cudaSuccess || n_dev == 0) {
+      cudaGetLastError();
+      throw Error(WGPU_ERR_CUDA, std::string("no usable CUDA device: ") +
+                                     (e != cudaSuccess ? cudaGetErrorString(e) : "count is 0"));
+    }
+    auto *g = new wgpu_gridder();
+    g->width = width;
+    g->height = height;
+    g->width_t = width_t;
+    g->height_t = height_t;
+    g->dl = pixel_size_x;
+    g->dm = pixel_size_y;
+    g->l_shift = l_shift;
+    g->m_shift = m_shift;
+    g->nthreads = nthreads;
+    g->epsilon = epsilon;
+    g->verbosity = verbosity;
+    g->tuning = tuning != 0;
+    g->prec = precision_bytes;
+    std::memset(&g->last_plan, 0, sizeof(g->last_plan));
+    try {
+      WGPU_CUDA(cudaGetDevice(&g->device));
+      WGPU_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      g->fft = fft_tables_create();
+    } catch (...) {
+      if (g->stream) cudaStreamDestroy(g->stream);
+      delete g;
+      throw;
+    }
+    *gridder = g;
+  });
+}
+
+void wgpu_gridder_destroy(wgpu_gridder_t *g) {
+  if (!g) return;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  g->arena.release();
+  if (g->d_img) cudaFree(g->d_img);
+  fft_tables_destroy(g->fft);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+// gridder_simple_implementation.h:53-61
+size_t wgpu_gridder_constant_memory(const wgpu_gridder_t *g) {
+  if (!g) return 0;
+  const double sigma_max = 2.0;
+  size_t c = (size_t)(sigma_max * sigma_max * g->width_t * g->height_t * 8.0);
+  c += g->width_t * g->height_t * (size_t)g->prec;
+  return c;
+}
+
+// gridder_simple_implementation.h:63-68
+size_t wgpu_gridder_per_visibility_memory(const wgpu_gridder_t *) { return 8; }
+
+int wgpu_gridder_initialize_inversion(wgpu_gridder_t *g) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  return guarded([&] {
+    ensure_image(g);
+    WGPU_CUDA(cudaMemsetAsync(g->d_img, 0, image_bytes(g), g->stream));
+    g->mode = wgpu_gridder::Mode::kInversion;
+  });
+}
+
+int wgpu_gridder_add_inversion_data_device(wgpu_gridder_t *g, size_t n_rows,
+                                           size_t n_chan, const double *d_uvw,
+                                           const double *d_freq,
+                                           const float *d_vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!d_uvw || !d_freq || !d_vis))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] { invert_device(g, n_rows, n_chan, d_uvw, d_freq, d_vis); });
+}
+
+int wgpu_gridder_add_inversion_data(wgpu_gridder_t *g, size_t n_rows,
+                                    size_t n_chan, const double *uvw,
+                                    const double *freq, const float *vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!uvw || !freq || !vis))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kInversion)
+      throw Error(WGPU_ERR_STATE, "AddInversionData before InitializeInversion");
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const float *dv = upload(g, kSlotVis, vis, 2 * n_rows * n_chan);
+    invert_device(g, n_rows, n_chan, du, df, dv);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_add_inversion_data_corrected(
+    wgpu_gridder_t *g, int mode, size_t n_pol, size_t n_rows, const double *uvw,
+    const double *freq, size_t n_chan, const uint64_t *antenna_pairs,
+    const float *vis, const uint64_t *time_offsets, const float *solutions,
+    size_t nparms, size_t n_times, size_t n_ant, int polarization) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if (mode < WGPU_GAIN_XX || mode > WGPU_GAIN_FULL)
+    return fail(WGPU_ERR_INVALID, "invalid gain mode");
+  if (n_pol != 1 && n_pol != 2 && n_pol != 4)
+    return fail(WGPU_ERR_INVALID, "n_polarizations must be 1, 2 or 4");
+  const size_t want = mode == WGPU_GAIN_FULL ? 4 : mode == WGPU_GAIN_2VIS_DIAGONAL ? 2 : 1;
+  if (n_pol != want)
+    return fail(WGPU_ERR_INVALID, "gain mode and n_polarizations do not match");
+  if (nparms != 2 && nparms != 4) return fail(WGPU_ERR_INVALID, "nparms must be 2 or 4");
+  if (polarization < 0 || polarization > 7) return fail(WGPU_ERR_INVALID, "invalid polarization");
+  if ((n_rows && n_chan) && (!uvw || !freq || !vis || !antenna_pairs || !time_offsets || !solutions))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kInversion)
+      throw Error(WGPU_ERR_STATE, "AddInversionData before InitializeInversion");
+    if (n_rows == 0 || n_chan == 0) return;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const float *dv = upload(g, kSlotGainVis, vis, 2 * n_rows * n_chan * n_pol);
+    const uint64_t *da = upload(g, kSlotAnt, antenna_pairs, 2 * n_rows);
+    const uint64_t *dt = upload(g, kSlotTimes, time_offsets, n_rows);
+    const float *ds = upload(g, kSlotSol, solutions, 2 * n_times * n_chan * n_ant * nparms);
+    float2 *dc = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
+    int *err = (int *)g->arena.get(kSlotOutVis, sizeof(int) * 4);
+    WGPU_CUDA(cudaMemsetAsync(err, 0, sizeof(int), g->stream));
+    launch_apply_gains(mode, (int)n_pol, (int64_t)n_rows, (int64_t)n_chan,
+                       (const float2 *)dv, da, dt, (const float2 *)ds, (int)nparms,
+                       (int64_t)n_times, (int64_t)n_ant, polarization, dc, err, g->stream);
+    int herr = 0;
+    WGPU_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    if (herr) throw Error(WGPU_ERR_INVALID, "antenna index or time offset outside the solution table");
+    invert_device(g, n_rows, n_chan, du, df, (const float *)dc);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_finalize_image(wgpu_gridder_t *g, double factor) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  return guarded([&] {
+    if (!g->d_img) throw Error(WGPU_ERR_STATE, "FinalizeImage without an image");
+    launch_scale_image(g->d_img, g->prec, (int64_t)(g->width_t * g->height_t), factor, g->stream);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_real_image(wgpu_gridder_t *g, float *image) {
+  if (!g || !image) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] {
+    if (!g->d_img) throw Error(WGPU_ERR_STATE, "RealImage without an image");
+    const size_t wt = g->width_t, ht = g->height_t;
+    std::vector<char> h(image_bytes(g));
+    WGPU_CUDA(cudaMemcpyAsync(h.data(), g->d_img, h.size(), cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    const size_t dx = (g->width - wt) / 2, dy = (g->height - ht) / 2;
+    const float nan = std::nanf("");
+    for (size_t i = 0; i < g->width * g->height; ++i) image[i] = nan;
+    for (size_t y = 0; y < ht; ++y)
+      for (size_t x = 0; x < wt; ++x) {
+        const size_t i = y * wt + x;
+        const float v = g->prec == 8 ? (float)((const double *)h.data())[i]
+                                     : ((const float *)h.data())[i];
+        image[(x + dx) + (y + dy) * g->width] = v;
+      }
+  });
+}
+
+int wgpu_gridder_initialize_prediction(wgpu_gridder_t *g, const float *image) {
+  if (!g || !image) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] {
+    ensure_image(g);
+    const size_t wt = g->width_t, ht = g->height_t;
+    const size_t dx = (g->width - wt) / 2, dy = (g->height - ht) / 2;
+    std::vector<char> h(image_bytes(g));
+    for (size_t y = 0; y < ht; ++y)
+      for (size_t x = 0; x < wt; ++x) {
+        const float v = image[(x + dx) + (y + dy) * g->width];
+        if (g->prec == 8)
+          ((double *)h.data())[y * wt + x] = v;
+        else
+          ((float *)h.data())[y * wt + x] = v;
+      }
+    WGPU_CUDA(cudaMemcpyAsync(g->d_img, h.data(), h.size(), cudaMemcpyHostToDevice, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    g->mode = wgpu_gridder::Mode::kPrediction;
+  });
+}
+
+int wgpu_gridder_predict_visibilities_device(wgpu_gridder_t *g, size_t n_rows,
+                                             size_t n_chan, const double *d_uvw,
+                                             const double *d_freq, float *d_vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!d_uvw || !d_freq || !d_vis))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] { predict_device(g, n_rows, n_chan, d_uvw, d_freq, d_vis); });
+}
+
+int wgpu_gridder_predict_visibilities(wgpu_gridder_t *g, size_t n_rows,
+                                      size_t n_chan, const double *uvw,
+                                      const double *freq, float *vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!uvw || !freq || !vis))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kPrediction)
+      throw Error(WGPU_ERR_STATE, "PredictVisibilities before InitializePrediction");
+    if (n_rows == 0 || n_chan == 0) return;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    float *dv = (float *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
+    predict_device(g, n_rows, n_chan, du, df, dv);
+    WGPU_CUDA(cudaMemcpyAsync(vis, dv, sizeof(float2) * n_rows * n_chan,
+                              cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_last_plan(const wgpu_gridder_t *g, wgpu_plan_t *plan) {
+  if (!g || !plan) return fail(WGPU_ERR_INVALID, "null argument");
+  *plan = g->last_plan;
+  return WGPU_OK;
+}
+
+int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms,
+                              int max_entries, char *names, size_t names_len,
+                              int *n_entries) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  std::string all;
+  int n = 0;
+  for (const auto &kv : g->last_timings) {
+    if (n < max_entries && ms) ms[n] = kv.second;
+    if (n) all += ";";
+    all += kv.first;
+    ++n;
+  }
+  if (n_entries) *n_entries = n;
+  if (names && names_len) {
+    std::strncpy(names, all.c_str(), names_len - 1);
+    names[names_len - 1] = '\0';
+  }
+  return WGPU_OK;
+}
+
+void *wgpu_gridder_stream(wgpu_gridder_t *g) { return g ? (void *)g->stream : nullptr; }
+
+uint64_t wgpu_kernel_launch_count(void) { return launch_count(); }
+
+int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                      const double *uvw, const double *freq, const float *vis,
+                      int skip_zero, uint32_t *perm, int32_t *iu, int32_t *iv,
+                      int32_t *ip, float *fu, float *fv, float *fw,
+                      uint32_t *offsets, int64_t *n_out) {
+  if (!plan || !uvw || !freq || !n_out) return fail(WGPU_ERR_INVALID, "null argument");
+  if (skip_zero && !vis) return fail(WGPU_ERR_INVALID, "inversion bucketing needs vis");
+  return guarded([&] {
+    int n_dev = 0;
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev == 0) {
+      cudaGetLastError();
+      throw Error(WGPU_ERR_CUDA, "no usable CUDA device");
+    }
+    DeviceArena arena;
+    cudaStream_t s;
+    WGPU_CUDA(cudaStreamCreate(&s));
+    try {
+      const DevPlan dp = to_dev_plan(*plan);
+      double *du = (double *)arena.get(kSlotUvw, sizeof(double) * 3 * n_rows);
+      double *df = (double *)arena.get(kSlotFreq, sizeof(double) * n_chan);
+      float *dv = nullptr;
+      WGPU_CUDA(cudaMemcpyAsync(du, uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
+      WGPU_CUDA(cudaMemcpyAsync(df, freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
+      if (vis) {
+        dv = (float *)arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
+        WGPU_CUDA(cudaMemcpyAsync(dv, vis, sizeof(float2) * n_rows * n_chan, cudaMemcpyHostToDevice, s));
+      }
+      const BucketResult b = bucket_visibilities(arena, dp, du, df, dv, (int64_t)n_rows,
+                                                 (int64_t)n_chan, skip_zero != 0, s);
+      std::vector<VisRecord> rec(b.n_out);
+      if (b.n_out) {
+        WGPU_CUDA(cudaMemcpyAsync(rec.data(), b.records, sizeof(VisRecord) * b.n_out, cudaMemcpyDeviceToHost, s));
+        if (perm) WGPU_CUDA(cudaMemcpyAsync(perm, b.perm, sizeof(uint32_t) * b.n_out, cudaMemcpyDeviceToHost, s));
+      }
+      if (offsets)
+        WGPU_CUDA(cudaMemcpyAsync(offsets, b.offsets, sizeof(uint32_t) * (b.n_keys + 1), cudaMemcpyDeviceToHost, s));
+      WGPU_CUDA(cudaStreamSynchronize(s));
+      for (int64_t k = 0; k < b.n_out; ++k) {
+        if (iu) iu[k] = rec[k].iu;
+        if (iv) iv[k] = rec[k].iv;
+        if (ip) ip[k] = rec[k].ip;
+        if (fu) fu[k] = rec[k].fu;
+        if (fv) fv[k] = rec[k].fv;
+        if (fw) fw[k] = rec[k].fw;
+      }
+      *n_out = b.n_out;
+    } catch (...) {
+      cudaStreamDestroy(s);
+      throw;
+    }
+    cudaStreamDestroy(s);
+  });
+}
+
+}  // extern "C"

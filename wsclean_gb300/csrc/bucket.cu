@@ -1,0 +1,373 @@
+// K1: visibility bucketing.
+//
+// Every visibility (row, chan) gets the corner of its W x W x W footprint on
+// the oversampled (u, v, w-plane) grid, computed in FP64 from uvw x frequency,
+// and a key = (uv tile, first w plane).  A stable LSD radix sort orders the
+// visibilities by key; the bucket offsets come from a key histogram and an
+// exclusive scan; finally one 32-byte record per visibility is written in
+// sorted order, carrying the visibility times its shift phase (inversion) or
+// the phase factor itself (prediction).
+//
+// The footprint arithmetic uses explicitly rounded operations (__dmul_rn,
+// __dsub_rn, never contracted into FMAs) so that the integer corners, the
+// float fractions, the keys and the permutation are bit-identical to the CPU
+// bucketing reference in oracle/wgpu_oracle.c.
+#include <cub/cub.cuh>
+
+#include "wgpu_internal.h"
+
+namespace wgpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct ChannelScale {
+  double su, sv, sw;  // U = uvw_u * su (cells), V = uvw_v * sv, w = uvw_w * sw
+};
+
+__global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
+                                      double gu, double gv,
+                                      ChannelScale *out) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chan) return;
+  const double fl = __ddiv_rn(freq[c], kSpeedOfLight);
+  out[c].su = __dmul_rn(fl, gu);
+  out[c].sv = __dmul_rn(fl, gv);
+  out[c].sw = fl;
+}
+
+struct Footprint {
+  int iu, iv, ip;
+  float fu, fv, fw;
+  uint32_t key;
+};
+
+__device__ __forceinline__ Footprint footprint(const DevPlan &p,
+                                               const double *uvw_row,
+                                               const ChannelScale &cs) {
+  Footprint f;
+  const double half = 0.5 * (double)p.support;
+  const double U = __dmul_rn(uvw_row[0], cs.su);
+  const double V = __dmul_rn(uvw_row[1], cs.sv);
+  const double iu0 = ceil(__dsub_rn(U, half));
+  const double iv0 = ceil(__dsub_rn(V, half));
+  f.fu = __double2float_rn(__dsub_rn(iu0, U));
+  f.fv = __double2float_rn(__dsub_rn(iv0, V));
+  long long iu = (long long)iu0 % p.nu;
+  if (iu < 0) iu += p.nu;
+  long long iv = (long long)iv0 % p.nv;
+  if (iv < 0) iv += p.nv;
+  f.iu = (int)iu;
+  f.iv = (int)iv;
+  if (p.n_planes > 1) {
+    const double wl = __dmul_rn(uvw_row[2], cs.sw);
+    const double Pw = __dmul_rn(__dsub_rn(wl, p.w0), p.inv_dw);
+    double ip0 = ceil(__dsub_rn(Pw, half));
+    const double ip_max = (double)(p.n_planes - p.support);
+    if (ip0 < 0.0) ip0 = 0.0;
+    if (ip0 > ip_max) ip0 = ip_max;
+    f.ip = (int)ip0;
+    f.fw = __double2float_rn(__dsub_rn(ip0, Pw));
+  } else {
+    f.ip = 0;
+    f.fw = 0.0f;
+  }
+  const uint32_t tile = (uint32_t)((f.iv / p.tile) * p.ntu + f.iu / p.tile);
+  f.key = tile * (uint32_t)p.n_planes + (uint32_t)f.ip;
+  return f;
+}
+
+__device__ __forceinline__ bool is_zero(const float2 v) {
+  return v.x == 0.0f && v.y == 0.0f;
+}
+
+// Order-preserving map double -> uint64 for atomic min/max.
+__device__ __forceinline__ unsigned long long dkey(double d) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double dkey_inv(unsigned long long k) {
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & ~0x8000000000000000ull) : ~k;
+  double d;
+  memcpy(&d, &b, sizeof(d));
+  return d;
+}
+
+struct MinOp {
+  __device__ double operator()(double a, double b) const { return fmin(a, b); }
+};
+struct MaxOp {
+  __device__ double operator()(double a, double b) const { return fmax(a, b); }
+};
+
+__global__ void __launch_bounds__(kThreads)
+    w_extent_kernel(const double *uvw, const double *freq, const float2 *vis,
+                    int64_t n_rows, int64_t n_chan, int skip_zero,
+                    unsigned long long *out /*[3]: min key, max key, count*/) {
+  double wmin = 1e300, wmax = -1e300;
+  unsigned long long cnt = 0;
+  const int64_t n = n_rows * n_chan;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (skip_zero && is_zero(vis[e])) continue;
+    const int64_t r = e / n_chan, c = e - r * n_chan;
+    const double fl = __ddiv_rn(freq[c], kSpeedOfLight);
+    const double wl = __dmul_rn(uvw[3 * r + 2], fl);
+    wmin = fmin(wmin, wl);
+    wmax = fmax(wmax, wl);
+    ++cnt;
+  }
+  typedef cub::BlockReduce<double, kThreads> BR;
+  typedef cub::BlockReduce<unsigned long long, kThreads> BRU;
+  __shared__ union {
+    typename BR::TempStorage d;
+    typename BRU::TempStorage u;
+  } tmp;
+  const double bmin = BR(tmp.d).Reduce(wmin, MinOp());
+  __syncthreads();
+  const double bmax = BR(tmp.d).Reduce(wmax, MaxOp());
+  __syncthreads();
+  const unsigned long long bcnt = BRU(tmp.u).Sum(cnt);
+  if (threadIdx.x == 0) {
+    if (bcnt > 0) {
+      atomicMin(&out[0], dkey(bmin));
+      atomicMax(&out[1], dkey(bmax));
+      atomicAdd(&out[2], bcnt);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    key_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
+               const float2 *vis, int64_t n_rows, int64_t n_chan,
+               int skip_zero, uint32_t sentinel, uint32_t *keys,
+               uint32_t *vals, uint32_t *counts) {
+  const int64_t n = n_rows * n_chan;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int64_t r = e / n_chan, c = e - r * n_chan;
+  uint32_t key = sentinel;
+  if (!(skip_zero && is_zero(vis[e]))) {
+    const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
+    key = f.key;
+  }
+  keys[e] = key;
+  vals[e] = (uint32_t)e;
+  if (key != sentinel) {
+    // warp-aggregated histogram update
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, key);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counts[key], __popc(peers));
+  }
+}
+
+// ---------------- stable LSD radix sort, 8-bit digits ----------------------
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kThreads * kSortItems;  // 2048 elements per block
+
+__global__ void __launch_bounds__(kThreads)
+    radix_hist_kernel(const uint32_t *keys, int64_t n, int shift,
+                      uint32_t *hist, int64_t n_blocks) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int64_t i = base + r * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * n_blocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kThreads)
+    radix_scatter_kernel(const uint32_t *keys_in, const uint32_t *vals_in,
+                         int64_t n, int shift, const uint32_t *hist,
+                         int64_t n_blocks, uint32_t *keys_out,
+                         uint32_t *vals_out) {
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t run[256];
+  __shared__ uint32_t wcnt[kThreads / 32][256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  base[threadIdx.x] = hist[(int64_t)threadIdx.x * n_blocks + blockIdx.x];
+  run[threadIdx.x] = 0;
+  const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kSortItems; ++r) {
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t i = tile0 + r * kThreads + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t key = 0, val = 0, d = 256;
+    if (valid) {
+      key = keys_in[i];
+      val = vals_in[i];
+      d = (key >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t acc = run[threadIdx.x];
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) {
+        const uint32_t t = wcnt[w][threadIdx.x];
+        wcnt[w][threadIdx.x] = acc;
+        acc += t;
+      }
+      run[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = base[d] + wcnt[warp][d] + rank;
+      keys_out[pos] = key;
+      vals_out[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    record_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
+                  const float2 *vis, int64_t n_chan, const uint32_t *perm,
+                  int64_t n_out, VisRecord *rec) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_out) return;
+  const uint32_t e = perm[s];
+  const int64_t r = e / n_chan, c = e - r * n_chan;
+  const double *row = uvw + 3 * r;
+  const ChannelScale sc = cs[c];
+  const Footprint f = footprint(p, row, sc);
+  // shift phase theta = u l_shift + v m_shift + w c_n (turns), FP64 argument,
+  // reduced to [-1/2, 1/2] before the FP32 sincos.
+  const double fl = sc.sw;
+  double t = row[0] * fl * p.l_shift + row[1] * fl * p.m_shift +
+             row[2] * fl * p.nm1_center;
+  t -= rint(t);
+  float sn, cn;
+  sincospif(2.0f * (float)t, &sn, &cn);
+  VisRecord o;
+  if (vis) {
+    const float2 v = vis[e];
+    o.re = v.x * cn + v.y * sn;
+    o.im = v.y * cn - v.x * sn;
+  } else {
+    o.re = cn;
+    o.im = -sn;
+  }
+  o.fu = f.fu;
+  o.fv = f.fv;
+  o.fw = f.fw;
+  o.iu = f.iu;
+  o.iv = f.iv;
+  o.ip = f.ip;
+  reinterpret_cast<float4 *>(rec + s)[0] = make_float4(o.re, o.im, o.fu, o.fv);
+  reinterpret_cast<float4 *>(rec + s)[1] =
+      make_float4(o.fw, __int_as_float(o.iu), __int_as_float(o.iv), __int_as_float(o.ip));
+}
+
+unsigned grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+void compute_w_extent(const double *d_uvw, const double *d_freq,
+                      const float *d_vis, int64_t n_rows, int64_t n_chan,
+                      bool skip_zero, double *w_min, double *w_max,
+                      int64_t *count, void *scratch8, cudaStream_t s) {
+  unsigned long long init[3] = {~0ull, 0ull, 0ull};
+  unsigned long long *d = (unsigned long long *)scratch8;
+  WGPU_CUDA(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  const int64_t n = n_rows * n_chan;
+  unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), 152 * 8);
+  w_extent_kernel<<<blocks, kThreads, 0, s>>>(d_uvw, d_freq, (const float2 *)d_vis,
+                                              n_rows, n_chan, skip_zero ? 1 : 0, d);
+  check_launch("w_extent_kernel");
+  unsigned long long out[3];
+  WGPU_CUDA(cudaMemcpyAsync(out, d, sizeof(out), cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  *count = (int64_t)out[2];
+  if (out[2] == 0) {
+    *w_min = *w_max = 0.0;
+  } else {
+    *w_min = dkey_inv(out[0]);
+    *w_max = dkey_inv(out[1]);
+  }
+}
+
+BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
+                                 const double *d_uvw, const double *d_freq,
+                                 const float *d_vis, int64_t n_rows,
+                                 int64_t n_chan, bool skip_zero,
+                                 cudaStream_t s) {
+  const int64_t n = n_rows * n_chan;
+  if (n >= (int64_t)0xFFFFFFFFll)
+    throw Error(WGPU_ERR_INVALID, "more than 2^32-1 visibilities in one call");
+  BucketResult res{};
+  res.n_keys = (int64_t)p.ntu * p.ntv * p.n_planes;
+  if (res.n_keys >= (int64_t)0xFFFFFFFFll)
+    throw Error(WGPU_ERR_INVALID, "too many (tile, plane) buckets");
+  int bits = 1;
+  while (((int64_t)1 << bits) - 1 < res.n_keys) ++bits;
+  const uint32_t sentinel = (uint32_t)(((uint64_t)1 << bits) - 1);
+
+  ChannelScale *cs = (ChannelScale *)arena.get(kSlotExtent, sizeof(ChannelScale) * (n_chan + 1) + 64);
+  uint32_t *keys = (uint32_t *)arena.get(kSlotKeys, sizeof(uint32_t) * (n + 1));
+  uint32_t *keys2 = (uint32_t *)arena.get(kSlotKeysAlt, sizeof(uint32_t) * (n + 1));
+  uint32_t *vals = (uint32_t *)arena.get(kSlotVals, sizeof(uint32_t) * (n + 1));
+  uint32_t *vals2 = (uint32_t *)arena.get(kSlotValsAlt, sizeof(uint32_t) * (n + 1));
+  uint32_t *offsets = (uint32_t *)arena.get(kSlotOffsets, sizeof(uint32_t) * (res.n_keys + 1));
+
+  const double gu = p.dl * (double)p.nu, gv = p.dm * (double)p.nv;
+  channel_scales_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, n_chan, gu, gv, cs);
+  check_launch("channel_scales_kernel");
+  WGPU_CUDA(cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (res.n_keys + 1), s));
+  if (n > 0) {
+    key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
+        p, d_uvw, cs, (const float2 *)d_vis, n_rows, n_chan, skip_zero ? 1 : 0,
+        sentinel, keys, vals, offsets);
+    check_launch("key_kernel");
+  }
+  exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
+
+  // radix sort over the key bits in use
+  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
+  uint32_t *hist = (uint32_t *)arena.get(kSlotHist, sizeof(uint32_t) * (256 * n_blocks + 1));
+  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+  for (int shift = 0; shift < bits && n > 0; shift += 8) {
+    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, n, shift, hist, n_blocks);
+    check_launch("radix_hist_kernel");
+    exclusive_scan_u32(arena, hist, 256 * n_blocks, s);
+    radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, vin, n, shift, hist,
+                                                                 n_blocks, kout, vout);
+    check_launch("radix_scatter_kernel");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  // number of bucketed elements = offsets[n_keys]
+  uint32_t total = 0;
+  WGPU_CUDA(cudaMemcpyAsync(&total, offsets + res.n_keys, sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  res.n_out = total;
+  res.perm = vin;
+  res.offsets = offsets;
+  res.records = (VisRecord *)arena.get(kSlotRecords, sizeof(VisRecord) * (res.n_out + 1));
+  if (res.n_out > 0) {
+    record_kernel<<<grid_for(res.n_out, kThreads), kThreads, 0, s>>>(
+        p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan,
+        res.perm, res.n_out, res.records);
+    check_launch("record_kernel");
+  }
+  return res;
+}
+
+}  // namespace wgpu

@@ -1,0 +1,253 @@
+// K6 grid correction + image accumulation, the per-pixel n-1 table, the
+// prediction pre-correction and output permutation, and K7 gains + collapse.
+#include "wgpu_internal.h"
+
+namespace wgpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+unsigned blocks_for(int64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// n - 1 - c_n per trimmed pixel, FP64.  Pixel (x, y) at l = (width/2 - x) dl +
+// l_shift, m = (y - height/2) dm + m_shift, n - 1 := 0 beyond the horizon
+// (gridding/directmsgridder.cpp:205-229).
+__global__ void nu_table_kernel(DevPlan p, double *nu_w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)p.width * p.height) return;
+  const int x = (int)(i % p.width), y = (int)(i / p.width);
+  const double l = (double)(p.width / 2 - x) * p.dl + p.l_shift;
+  const double m = (double)(y - p.height / 2) * p.dm + p.m_shift;
+  const double r2 = l * l + m * m;
+  const double nm1 = r2 >= 1.0 ? 0.0 : -r2 / (sqrt(1.0 - r2) + 1.0);
+  nu_w[i] = nm1 - p.nm1_center;
+}
+
+// 1 / psihat(dw * nu) by Gauss-Legendre quadrature over the positive half:
+// psihat(f) = W * sum_q g_q cos(pi f W z_q), g_q = w_q phi(z_q).
+__device__ __forceinline__ float w_correction(const DevPlan &p, double nu,
+                                              const float *gl_zw, int n_gl) {
+  if (p.n_planes == 1) return 1.0f;
+  const float a = (float)(M_PI * p.dw * nu * p.support);
+  float acc = 0.0f;
+  for (int q = 0; q < n_gl; ++q) acc += gl_zw[2 * q + 1] * cosf(a * gl_zw[2 * q]);
+  return 1.0f / ((float)p.support * acc);
+}
+
+template <typename NumT>
+__global__ void finalize_add_kernel(DevPlan p, const float2 *acc,
+                                    const double *nu_w, const float *cx,
+                                    const float *cy, const float *gl_zw,
+                                    int n_gl, NumT *img) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)p.width * p.height) return;
+  const int x = (int)(i % p.width), y = (int)(i / p.width);
+  const float2 a = acc[i];
+  const float v = (a.x - a.y) * cx[x] * cy[y] * w_correction(p, nu_w[i], gl_zw, n_gl);
+  img[i] += (NumT)v;
+}
+
+template <typename NumT>
+__global__ void precorrect_kernel(DevPlan p, const NumT *img, const double *nu_w,
+                                  const float *cx, const float *cy,
+                                  const float *gl_zw, int n_gl, float *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)p.width * p.height) return;
+  const int x = (int)(i % p.width), y = (int)(i / p.width);
+  const float v = (float)img[i];
+  out[i] = v == 0.0f ? 0.0f : v * cx[x] * cy[y] * w_correction(p, nu_w[i], gl_zw, n_gl);
+}
+
+__global__ void unpermute_predict_kernel(const VisRecord *rec, const uint32_t *perm,
+                                         const float2 *acc, int64_t n,
+                                         float2 *vis) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 r = __ldg(reinterpret_cast<const float4 *>(rec + s));
+  const float2 a = acc[s];
+  // record holds exp(-2 pi i theta); multiply by its conjugate
+  const float c = r.x, sn = -r.y;
+  vis[perm[s]] = make_float2(a.x * c - a.y * sn, a.x * sn + a.y * c);
+}
+
+// ---- K7: conjugated gains (visibilitymodifier.h:378-401) + collapse -------
+__device__ __forceinline__ float2 cm(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 ca(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cs(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// r = a^H b (row-major 2x2)
+__device__ __forceinline__ void herm_mul(const float2 *a, const float2 *b, float2 *r) {
+  const float2 h[4] = {cj(a[0]), cj(a[2]), cj(a[1]), cj(a[3])};
+  r[0] = ca(cm(h[0], b[0]), cm(h[1], b[2]));
+  r[1] = ca(cm(h[0], b[1]), cm(h[1], b[3]));
+  r[2] = ca(cm(h[2], b[0]), cm(h[3], b[2]));
+  r[3] = ca(cm(h[2], b[1]), cm(h[3], b[3]));
+}
+__device__ __forceinline__ void mat_mul(const float2 *a, const float2 *b, float2 *r) {
+  r[0] = ca(cm(a[0], b[0]), cm(a[1], b[2]));
+  r[1] = ca(cm(a[0], b[1]), cm(a[1], b[3]));
+  r[2] = ca(cm(a[2], b[0]), cm(a[3], b[2]));
+  r[3] = ca(cm(a[2], b[1]), cm(a[3], b[3]));
+}
+
+__device__ __forceinline__ float2 collapse4(const float2 *v, int pol) {
+  switch (pol) {
+    case 0: return cs(ca(v[0], v[3]), 0.5f);
+    case 1: return make_float2(0.5f * (v[0].x - v[3].x), 0.5f * (v[0].y - v[3].y));
+    case 2: return cs(ca(v[1], v[2]), 0.5f);
+    case 3: {
+      const float2 d = make_float2(v[2].x - v[1].x, v[2].y - v[1].y);
+      return make_float2(-0.5f * d.y, 0.5f * d.x);
+    }
+    case 4: return v[0];
+    case 5: return v[1];
+    case 6: return v[2];
+    default: return v[3];
+  }
+}
+
+__global__ void apply_gains_kernel(int mode, int n_pol, int64_t n_rows,
+                                   int64_t n_chan, const float2 *vis_in,
+                                   const uint64_t *ant_pairs,
+                                   const uint64_t *time_offsets,
+                                   const float2 *sol, int nparms,
+                                   int64_t n_times, int64_t n_ant,
+                                   int polarization, float2 *out,
+                                   int *err_flag) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_rows * n_chan) return;
+  const int64_t r = e / n_chan, ch = e - r * n_chan;
+  const uint64_t a1 = ant_pairs[2 * r], a2 = ant_pairs[2 * r + 1];
+  const uint64_t t = time_offsets[r];
+  if (a1 >= (uint64_t)n_ant || a2 >= (uint64_t)n_ant || t >= (uint64_t)n_times) {
+    // out-of-range index: record it and leave the visibility out (zero)
+    atomicOr(err_flag, 1);
+    out[e] = make_float2(0.f, 0.f);
+    return;
+  }
+  const int64_t off = ((int64_t)t * n_chan + ch) * n_ant * nparms;
+  float2 g1[4], g2[4];
+  if (nparms == 2) {
+    g1[0] = sol[off + a1 * 2]; g1[1] = make_float2(0.f, 0.f);
+    g1[2] = make_float2(0.f, 0.f); g1[3] = sol[off + a1 * 2 + 1];
+    g2[0] = sol[off + a2 * 2]; g2[1] = make_float2(0.f, 0.f);
+    g2[2] = make_float2(0.f, 0.f); g2[3] = sol[off + a2 * 2 + 1];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      g1[k] = sol[off + a1 * 4 + k];
+      g2[k] = sol[off + a2 * 4 + k];
+    }
+  }
+  float2 v[4];
+  for (int k = 0; k < n_pol; ++k) v[k] = vis_in[e * n_pol + k];
+  float2 res;
+  switch (mode) {
+    case 0: res = cm(cm(cj(g1[0]), v[0]), g2[0]); break;
+    case 1: res = cm(cm(cj(g1[3]), v[0]), g2[3]); break;
+    case 2: {
+      float2 dd = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) dd = ca(dd, cm(g2[k], cj(g1[k])));
+      res = cm(v[0], cs(dd, 0.5f));
+      break;
+    }
+    case 3: {
+      // second component uses the updated first one, as in
+      // visibilitymodifier.h:393-396
+      const float2 v0 = ca(cm(cm(cj(g1[0]), v[0]), g2[0]), cm(cm(cj(g1[2]), v[1]), g2[2]));
+      const float2 v1 = ca(cm(cm(cj(g1[3]), v[1]), g2[3]), cm(cm(cj(g1[1]), v0), g2[1]));
+      res = ca(v0, v1);  // msgridderdata.h:41-45 collapse: v0 + v1
+      break;
+    }
+    default: {
+      float2 t1[4], t2[4];
+      herm_mul(g1, v, t1);
+      mat_mul(t1, g2, t2);
+      res = collapse4(t2, polarization);
+      break;
+    }
+  }
+  out[e] = res;
+}
+
+}  // namespace
+
+void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s) {
+  const int64_t n = (int64_t)p.width * p.height;
+  nu_table_kernel<<<blocks_for(n), kThreads, 0, s>>>(p, nu_w);
+  check_launch("nu_table_kernel");
+}
+
+void launch_finalize_add(const DevPlan &p, const float2 *acc,
+                         const double *nu_w, const float *cx, const float *cy,
+                         const float *gl_zw, int n_gl, void *img,
+                         int precision_bytes, cudaStream_t s) {
+  const int64_t n = (int64_t)p.width * p.height;
+  if (precision_bytes == 8)
+    finalize_add_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, acc, nu_w, cx, cy, gl_zw, n_gl, (double *)img);
+  else
+    finalize_add_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, acc, nu_w, cx, cy, gl_zw, n_gl, (float *)img);
+  check_launch("finalize_add_kernel");
+}
+
+void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
+                       const double *nu_w, const float *cx, const float *cy,
+                       const float *gl_zw, int n_gl, float *img_corr,
+                       cudaStream_t s) {
+  const int64_t n = (int64_t)p.width * p.height;
+  if (precision_bytes == 8)
+    precorrect_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, (const double *)img, nu_w, cx, cy, gl_zw, n_gl, img_corr);
+  else
+    precorrect_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, (const float *)img, nu_w, cx, cy, gl_zw, n_gl, img_corr);
+  check_launch("precorrect_kernel");
+}
+
+void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
+                              const float2 *acc, int64_t n, float2 *vis,
+                              cudaStream_t s) {
+  if (n <= 0) return;
+  unpermute_predict_kernel<<<blocks_for(n), kThreads, 0, s>>>(rec, perm, acc, n, vis);
+  check_launch("unpermute_predict_kernel");
+}
+
+void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
+                        const float2 *vis_in, const uint64_t *ant_pairs,
+                        const uint64_t *time_offsets, const float2 *sol,
+                        int nparms, int64_t n_times, int64_t n_ant,
+                        int polarization, float2 *out, int *err_flag,
+                        cudaStream_t s) {
+  const int64_t n = n_rows * n_chan;
+  if (n <= 0) return;
+  apply_gains_kernel<<<blocks_for(n), kThreads, 0, s>>>(
+      mode, n_pol, n_rows, n_chan, vis_in, ant_pairs, time_offsets, sol, nparms,
+      n_times, n_ant, polarization, out, err_flag);
+  check_launch("apply_gains_kernel");
+}
+
+}  // namespace wgpu
+
+namespace wgpu {
+namespace {
+template <typename NumT>
+__global__ void scale_kernel(NumT *img, int64_t n, double factor) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) img[i] = (NumT)(img[i] * factor);
+}
+}  // namespace
+
+void launch_scale_image(void *img, int precision_bytes, int64_t n, double factor,
+                        cudaStream_t s) {
+  if (n <= 0) return;
+  const unsigned b = (unsigned)((n + 255) / 256);
+  if (precision_bytes == 8)
+    scale_kernel<double><<<b, 256, 0, s>>>((double *)img, n, factor);
+  else
+    scale_kernel<float><<<b, 256, 0, s>>>((float *)img, n, factor);
+  check_launch("scale_kernel");
+}
+}  // namespace wgpu

@@ -1,0 +1,272 @@
+// Planner: chooses grid size, ES kernel and w-planes for one gridding call.
+//
+// The reference hands epsilon, sigma_min = 1.1 and sigma_max = 2.0 to ducc0
+// (wgridder/gridder_simple.h:57-58, :217-225), which picks the kernel and the
+// plane count internally.  Here the choice is made from the ES-kernel table
+// derived by wsclean_gb300/kernel_table.py and a cost model of the GPU
+// pipeline (cell updates for gridding, bytes moved per w-plane for the FFT
+// passes).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "es_table.h"
+#include "wgpu_internal.h"
+
+namespace wgpu {
+
+namespace {
+
+bool is_smooth235(int64_t k) {
+  for (int p : {2, 3, 5})
+    while (k % p == 0) k /= p;
+  return k == 1;
+}
+
+struct GaussLegendre {
+  static constexpr int kN = 256;  // positive half of a 512-point rule
+  double x[kN], w[kN];
+  GaussLegendre() {
+    const int n = 2 * kN;
+    for (int i = 0; i < kN; ++i) {
+      double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+      double dp = 1.0;
+      for (int it = 0; it < 100; ++it) {
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; ++k) {
+          const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+          p0 = p1;
+          p1 = p2;
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        const double dz = p1 / dp;
+        z -= dz;
+        if (std::fabs(dz) < 1e-16) break;
+      }
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      x[i] = z;
+      w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+  }
+};
+
+const GaussLegendre &gl() {
+  static const GaussLegendre g;
+  return g;
+}
+
+// Throughput constants of the cost model (cell updates/s for the stencil
+// kernels, bytes/s for the FFT passes).  Calibrated against GB300 runs.
+constexpr double kCellRate = 2.0e12;
+constexpr double kByteRate = 4.5e12;
+
+}  // namespace
+
+double es_kernel(double beta, double z) {
+  if (!(std::fabs(z) < 1.0)) return 0.0;
+  return std::exp(beta * (std::sqrt(1.0 - z * z) - 1.0));
+}
+
+double es_fourier(double beta, int support, double f) {
+  const GaussLegendre &g = gl();
+  double acc = 0.0;
+  for (int i = 0; i < GaussLegendre::kN; ++i)
+    acc += g.w[i] * es_kernel(beta, g.x[i]) *
+           std::cos(M_PI * f * support * g.x[i]);
+  return support * acc;
+}
+
+int64_t good_fft_size(int64_t n, int64_t multiple) {
+  int64_t k = (n + multiple - 1) / multiple;
+  if (k < 2) k = 2;
+  while (!is_smooth235(k)) ++k;
+  return k * multiple;
+}
+
+static bool try_decompose(int64_t n, int64_t *n1, int64_t *n2) {
+  // n = n1 * n2 with both factors <= 256, n2 >= n1, as balanced as possible.
+  int64_t best1 = -1;
+  for (int64_t a = 1; a <= 256; ++a) {
+    if (n % a) continue;
+    const int64_t b = n / a;
+    if (b > 256 || b < a) continue;
+    best1 = a;  // increasing a -> more balanced
+  }
+  if (best1 < 0) return false;
+  *n1 = best1;
+  *n2 = n / best1;
+  return true;
+}
+
+void fft_decompose(int64_t n, int64_t *n1, int64_t *n2) {
+  if (!try_decompose(n, n1, n2))
+    throw Error(WGPU_ERR_INVALID, "grid size cannot be split for the column FFT");
+}
+
+void nm1_range(int64_t width, int64_t height, double dl, double dm,
+               double l_shift, double m_shift, double *lo, double *hi) {
+  // Pixel (x, y) sits at l = (width/2 - x) dl + l_shift, m = (y - height/2) dm
+  // + m_shift (gridding/directmsgridder.cpp:113-124 with the wrap of :70-82).
+  const double l_a = (double)(width / 2 - (width - 1)) * dl + l_shift;
+  const double l_b = (double)(width / 2) * dl + l_shift;
+  const double m_a = (double)(-(height / 2)) * dm + m_shift;
+  const double m_b = (double)(height - 1 - height / 2) * dm + m_shift;
+  auto nm1 = [](double l, double m) {
+    const double r2 = l * l + m * m;
+    if (r2 >= 1.0) return -1.0;
+    return -r2 / (std::sqrt(1.0 - r2) + 1.0);
+  };
+  double mn = std::min(std::min(nm1(l_a, m_a), nm1(l_a, m_b)),
+                       std::min(nm1(l_b, m_a), nm1(l_b, m_b)));
+  const double lc = std::min(std::max(0.0, std::min(l_a, l_b)), std::max(l_a, l_b));
+  const double mc = std::min(std::max(0.0, std::min(m_a, m_b)), std::max(m_a, m_b));
+  double mx = nm1(lc, mc);
+  *lo = mn;
+  *hi = mx;
+}
+
+wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
+  if (req.width < 2 || req.height < 2 || (req.width & 1) || (req.height & 1))
+    throw Error(WGPU_ERR_INVALID, "trimmed image dimensions must be even and >= 2");
+  if (!(req.dl > 0.0) || !(req.dm > 0.0))
+    throw Error(WGPU_ERR_INVALID, "pixel sizes must be positive");
+  if (!(req.epsilon > 0.0))
+    throw Error(WGPU_ERR_INVALID, "epsilon must be positive");
+  if (!(req.w_max >= req.w_min))
+    throw Error(WGPU_ERR_INVALID, "w_max < w_min");
+  const double smin = req.sigma_min > 0 ? req.sigma_min : 1.1;
+  const double smax = req.sigma_max > 0 ? req.sigma_max : 2.0;
+
+  double lo, hi;
+  nm1_range(req.width, req.height, req.dl, req.dm, req.l_shift, req.m_shift,
+            &lo, &hi);
+  const double wrange = req.w_max - req.w_min;
+  // w-gridding is skipped only when the whole w spread changes the phase of
+  // any pixel by a negligible fraction of epsilon.
+  const bool use_w = M_PI * wrange * (hi - lo) > 1e-3 * req.epsilon;
+  const double ndim = use_w ? 3.0 : 2.0;
+  const double n_vis = std::max<double>(1.0, (double)req.n_vis);
+
+  wgpu_plan_t best;
+  std::memset(&best, 0, sizeof(best));
+  double best_cost = std::numeric_limits<double>::infinity();
+  double fallback_err = std::numeric_limits<double>::infinity();
+  const EsKernelEntry *fallback = nullptr;
+
+  for (int i = 0; i < kEsKernelTableSize; ++i) {
+    const EsKernelEntry &e = kEsKernelTable[i];
+    if (e.sigma < smin - 1e-9 || e.sigma > smax + 1e-9) continue;
+    if (req.force_support > 0 && e.support != req.force_support) continue;
+    if (req.force_sigma > 0 && std::fabs(e.sigma - req.force_sigma) > 1e-6) continue;
+    // Worst case over the image band (a few point sources near the edge see
+    // the maximum, not the RMS, aliasing error), summed in quadrature over
+    // the gridded dimensions.
+    const double est = std::sqrt(ndim) * e.err_max;
+    if (est < fallback_err) {
+      fallback_err = est;
+      fallback = &e;
+    }
+    if (est > req.epsilon) continue;
+
+    wgpu_plan_t p;
+    std::memset(&p, 0, sizeof(p));
+    p.width = req.width;
+    p.height = req.height;
+    p.support = e.support;
+    p.sigma = e.sigma;
+    p.beta = e.beta;
+    int64_t tile = req.force_tile > 0 ? req.force_tile : 32;
+    int64_t nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
+    int64_t nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
+    if (req.force_tile <= 0 && std::min(nu, nv) < 256) {
+      tile = 16;
+      nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
+      nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
+    }
+    if (e.support > tile) continue;
+    int64_t f1, f2;
+    if (nu > fft_row_max_length() || !try_decompose(nv, &f1, &f2)) continue;
+    p.tile = tile;
+    p.nu = nu;
+    p.nv = nv;
+    p.dl = req.dl;
+    p.dm = req.dm;
+    p.l_shift = req.l_shift;
+    p.m_shift = req.m_shift;
+    p.nm1_min = lo;
+    p.nm1_max = hi;
+    p.nm1_center = 0.5 * (lo + hi);
+    if (use_w) {
+      p.dw = 1.0 / (e.sigma * (hi - lo));
+      p.n_planes = (int64_t)std::ceil(wrange / p.dw) + e.support;
+      p.w0 = req.w_min - 0.5 * (double)e.support * p.dw;
+    } else {
+      p.dw = 1.0;
+      p.n_planes = 1;
+      p.w0 = 0.5 * (req.w_min + req.w_max);
+    }
+    p.est_error = est;
+    const int64_t rstride = (req.width + 31) / 32 * 32;
+    const double w_planes_per_vis = use_w ? (double)e.support : 1.0;
+    const double t_grid = 2.0 * n_vis * e.support * e.support * w_planes_per_vis / kCellRate;
+    const double t_fft = 2.0 * (double)p.n_planes *
+                         (16.0 * nu * nv + 40.0 * nv * rstride) / kByteRate;
+    p.est_seconds = t_grid + t_fft;
+    if (p.est_seconds < best_cost) {
+      best_cost = p.est_seconds;
+      best = p;
+    }
+  }
+  if (!std::isfinite(best_cost)) {
+    if (fallback == nullptr || req.force_support > 0)
+      throw Error(WGPU_ERR_INVALID, "no kernel configuration satisfies the request");
+    // Most accurate entry available: retry pinned to it.
+    wgpu_plan_request_t r2 = req;
+    r2.force_support = fallback->support;
+    r2.force_sigma = fallback->sigma;
+    r2.epsilon = std::max(req.epsilon, fallback_err * 1.0001);
+    return make_plan(r2);
+  }
+  // Planes resident per pipeline step.
+  const int64_t rstride = (best.width + 31) / 32 * 32;
+  const double per_plane = 8.0 * best.nu * best.nv + 8.0 * best.nv * rstride;
+  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 24e9;
+  int64_t batch = (int64_t)std::floor(budget / per_plane);
+  int64_t cap = req.max_plane_batch > 0 ? req.max_plane_batch : 32;
+  batch = std::max<int64_t>(1, std::min<int64_t>(std::min(batch, cap), best.n_planes));
+  best.plane_batch = batch;
+  fft_decompose(best.nv, &best.fft_n1, &best.fft_n2);
+  return best;
+}
+
+DevPlan to_dev_plan(const wgpu_plan_t &p) {
+  DevPlan d;
+  d.nu = (int)p.nu;
+  d.nv = (int)p.nv;
+  d.width = (int)p.width;
+  d.height = (int)p.height;
+  d.support = (int)p.support;
+  d.tile = (int)p.tile;
+  d.ntu = (int)(p.nu / p.tile);
+  d.ntv = (int)(p.nv / p.tile);
+  d.n_planes = (int)p.n_planes;
+  d.beta = (float)p.beta;
+  d.dl = p.dl;
+  d.dm = p.dm;
+  d.l_shift = p.l_shift;
+  d.m_shift = p.m_shift;
+  d.w0 = p.w0;
+  d.dw = p.dw;
+  d.inv_dw = p.n_planes > 1 ? 1.0 / p.dw : 0.0;
+  d.nm1_center = p.nm1_center;
+  return d;
+}
+
+}  // namespace wgpu

@@ -1,0 +1,173 @@
+// Device arena, launch accounting and a device-wide exclusive scan.
+#include <atomic>
+
+#include "wgpu_internal.h"
+
+namespace wgpu {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void count_launch(int n) { g_launches.fetch_add((uint64_t)n); }
+uint64_t launch_count() { return g_launches.load(); }
+
+void check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    throw Error(WGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  count_launch();
+}
+
+DeviceArena::~DeviceArena() { release(); }
+
+void *DeviceArena::get(int slot, size_t bytes) {
+  if (slot < 0 || slot >= kSlots) throw Error(WGPU_ERR_INVALID, "arena slot");
+  if (bytes == 0) bytes = 16;
+  if (size_[slot] >= bytes) return ptr_[slot];
+  if (ptr_[slot]) {
+    cudaFree(ptr_[slot]);
+    ptr_[slot] = nullptr;
+    size_[slot] = 0;
+  }
+  // Round up by 1/8 so that slowly growing chunks do not reallocate each call.
+  size_t want = bytes + bytes / 8;
+  want = (want + 255) & ~size_t(255);
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(WGPU_ERR_NOMEM, "device allocation of " + std::to_string(bytes) +
+                                      " bytes failed: " + cudaGetErrorString(e));
+    }
+    want = bytes;
+  }
+  ptr_[slot] = p;
+  size_[slot] = want;
+  return p;
+}
+
+size_t DeviceArena::total() const {
+  size_t t = 0;
+  for (int i = 0; i < kSlots; ++i) t += size_[i];
+  return t;
+}
+
+void DeviceArena::release() {
+  for (int i = 0; i < kSlots; ++i) {
+    if (ptr_[i]) cudaFree(ptr_[i]);
+    ptr_[i] = nullptr;
+    size_[i] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (uint32, in place).  Three phases: per-chunk sums, scan of
+// the sums (recursively), per-chunk local scan plus the chunk's base.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 16;
+constexpr int kScanChunk = kScanThreads * kScanPerThread;  // 4096
+
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_sums[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < kScanThreads / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < kScanThreads / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const uint32_t warp_base = warp > 0 ? warp_sums[warp - 1] : 0;
+  *total = warp_sums[kScanThreads / 32 - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_chunk_sums(const uint32_t *d, int64_t n, uint32_t *sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  uint32_t s = 0;
+  for (int i = threadIdx.x; i < kScanChunk; i += kScanThreads) {
+    const int64_t k = base + i;
+    if (k < n) s += d[k];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ uint32_t ws[kScanThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_chunk_local(uint32_t *d, int64_t n, const uint32_t *bases) {
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk +
+                       (int64_t)threadIdx.x * kScanPerThread;
+  uint32_t v[kScanPerThread];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanPerThread; ++i) {
+    const int64_t k = base + i;
+    v[i] = k < n ? d[k] : 0u;
+    s += v[i];
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive_scan(s, &total);
+  run += bases ? bases[blockIdx.x] : 0u;
+#pragma unroll
+  for (int i = 0; i < kScanPerThread; ++i) {
+    const int64_t k = base + i;
+    if (k < n) d[k] = run;
+    run += v[i];
+  }
+}
+
+void scan_level(uint32_t *d, int64_t n, uint32_t *tmp, cudaStream_t s) {
+  const int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+  if (nb <= 1) {
+    scan_chunk_local<<<1, kScanThreads, 0, s>>>(d, n, nullptr);
+    check_launch("scan_chunk_local");
+    return;
+  }
+  scan_chunk_sums<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, tmp);
+  check_launch("scan_chunk_sums");
+  scan_level(tmp, nb, tmp + nb, s);
+  scan_chunk_local<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, tmp);
+  check_launch("scan_chunk_local");
+}
+}  // namespace
+
+void exclusive_scan_u32(DeviceArena &arena, uint32_t *d, int64_t n,
+                        cudaStream_t s) {
+  if (n <= 0) return;
+  int64_t need = 0, m = n;
+  while (m > kScanChunk) {
+    m = (m + kScanChunk - 1) / kScanChunk;
+    need += m;
+  }
+  uint32_t *tmp = (uint32_t *)arena.get(kSlotScanTmp, sizeof(uint32_t) * (need + 16));
+  scan_level(d, n, tmp, s);
+}
+
+}  // namespace wgpu

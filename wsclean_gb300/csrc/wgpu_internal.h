@@ -1,0 +1,200 @@
+// Internal declarations shared by the host orchestration and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/wgpu.h"
+
+namespace wgpu {
+
+constexpr double kSpeedOfLight = 299792458.0;
+constexpr int kMaxSupport = 16;
+
+// Exception carrying a C-ABI status; converted at the boundary.
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define WGPU_CUDA(call)                                                      \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      throw ::wgpu::Error(e_ == cudaErrorMemoryAllocation ? WGPU_ERR_NOMEM   \
+                                                          : WGPU_ERR_CUDA,   \
+                          std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void count_launch(int n = 1);
+uint64_t launch_count();
+void check_launch(const char *what);
+
+// One bucketed visibility in sorted order (32 bytes, two 128-bit words).
+// For inversion (re, im) is the visibility times exp(-2 pi i theta); for
+// prediction it is the phase factor exp(-2 pi i theta) itself.
+struct __align__(16) VisRecord {
+  float re, im;
+  float fu, fv;  // footprint corner minus exact position, in cells
+  float fw;      // same along w, in planes
+  int32_t iu, iv;  // wrapped footprint corner
+  int32_t ip;      // first w plane of the footprint
+};
+static_assert(sizeof(VisRecord) == 32, "record layout");
+
+// Plan parameters as the kernels consume them.
+struct DevPlan {
+  int nu, nv, width, height, support, tile, ntu, ntv, n_planes;
+  float beta;
+  double dl, dm, l_shift, m_shift, w0, dw, inv_dw, nm1_center;
+};
+
+DevPlan to_dev_plan(const wgpu_plan_t &p);
+
+// ---- planner (plan.cpp) ----
+wgpu_plan_t make_plan(const wgpu_plan_request_t &req);
+void nm1_range(int64_t width, int64_t height, double dl, double dm,
+               double l_shift, double m_shift, double *lo, double *hi);
+int64_t good_fft_size(int64_t n, int64_t multiple);
+void fft_decompose(int64_t n, int64_t *n1, int64_t *n2);
+// ES kernel FT in cell units (FP64 Gauss-Legendre).
+double es_fourier(double beta, int support, double f);
+double es_kernel(double beta, double z);
+
+// ---- bucketing (bucket.cu) ----
+struct BucketScratch;  // grow-only device buffers
+struct BucketResult {
+  VisRecord *records;   // [n_out]
+  uint32_t *perm;       // [n_out] element index
+  uint32_t *offsets;    // [n_keys + 1]
+  int64_t n_out;
+  int64_t n_keys;
+};
+// Extents of the (non-zero when skip_zero) visibilities: w min/max in
+// wavelengths and the count.
+void compute_w_extent(const double *d_uvw, const double *d_freq,
+                      const float *d_vis, int64_t n_rows, int64_t n_chan,
+                      bool skip_zero, double *w_min, double *w_max,
+                      int64_t *count, void *scratch8, cudaStream_t s);
+
+class DeviceArena;
+BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
+                                 const double *d_uvw, const double *d_freq,
+                                 const float *d_vis, int64_t n_rows,
+                                 int64_t n_chan, bool skip_zero,
+                                 cudaStream_t s);
+
+// ---- gridding (grid.cu) ----
+void launch_grid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                 int p_begin, int n_batch, float2 *planes, cudaStream_t s);
+void launch_degrid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                   int p_begin, int n_batch, const float2 *planes,
+                   float2 *acc, cudaStream_t s);
+int grid_plane_group();
+
+// ---- FFT (fft.cu) ----
+struct FftTables;  // twiddles per length
+const float2 *fft_twiddles(FftTables &t, int n);
+FftTables *fft_tables_create();
+void fft_tables_destroy(FftTables *);
+int fft_row_max_length();
+// Row pass, forward: planes [B][nv][nu] -> R [B][nv][rstride] keeping the
+// trimmed columns.
+void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
+                                  const float2 *planes, float2 *R, int rstride,
+                                  int n_batch, cudaStream_t s);
+// Row pass, backward: R -> planes (full rows).
+void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
+                                  const float2 *R, int rstride, float2 *planes,
+                                  int n_batch, cudaStream_t s);
+// Column passes with the fused w-screen (see fft.cu).
+void launch_fft_cols_forward_accumulate(FftTables &t, const DevPlan &p,
+                                        int n1, int n2, float2 *R, int rstride,
+                                        int n_batch, int p_begin,
+                                        const double *nu_w, float2 *acc,
+                                        cudaStream_t s);
+void launch_fft_cols_backward_screen(FftTables &t, const DevPlan &p, int n1,
+                                     int n2, const float *img_corr,
+                                     const double *nu_w, float2 *R,
+                                     int rstride, int n_batch, int p_begin,
+                                     cudaStream_t s);
+
+// ---- corrections (correct.cu) ----
+void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s);
+// tdirty * corr added into the accumulated image (float or double).
+void launch_finalize_add(const DevPlan &p, const float2 *acc,
+                         const double *nu_w, const float *cx, const float *cy,
+                         const float *gl_zw, int n_gl, void *img,
+                         int precision_bytes, cudaStream_t s);
+// img * corr -> img_corr (prediction pre-correction).
+void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
+                       const double *nu_w, const float *cx, const float *cy,
+                       const float *gl_zw, int n_gl, float *img_corr,
+                       cudaStream_t s);
+void launch_scale_image(void *img, int precision_bytes, int64_t n,
+                        double factor, cudaStream_t s);
+void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
+                              const float2 *acc, int64_t n, float2 *vis,
+                              cudaStream_t s);
+void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
+                        const float2 *vis_in, const uint64_t *ant_pairs,
+                        const uint64_t *time_offsets, const float2 *sol,
+                        int nparms, int64_t n_times, int64_t n_ant,
+                        int polarization, float2 *out, int *err_flag,
+                        cudaStream_t s);
+
+// Grow-only device allocations keyed by slot.
+class DeviceArena {
+ public:
+  DeviceArena() = default;
+  ~DeviceArena();
+  DeviceArena(const DeviceArena &) = delete;
+  DeviceArena &operator=(const DeviceArena &) = delete;
+  void *get(int slot, size_t bytes);
+  size_t total() const;
+  void release();
+
+ private:
+  static constexpr int kSlots = 32;
+  void *ptr_[kSlots] = {};
+  size_t size_[kSlots] = {};
+};
+
+enum ArenaSlot {
+  kSlotKeys = 0,
+  kSlotKeysAlt,
+  kSlotVals,
+  kSlotValsAlt,
+  kSlotHist,
+  kSlotScanTmp,
+  kSlotRecords,
+  kSlotOffsets,
+  kSlotExtent,
+  kSlotPlanes,
+  kSlotRows,
+  kSlotNuW,
+  kSlotAcc,
+  kSlotCorrX,
+  kSlotCorrY,
+  kSlotGl,
+  kSlotVisAcc,
+  kSlotUvw,
+  kSlotFreq,
+  kSlotVis,
+  kSlotGainVis,
+  kSlotAnt,
+  kSlotTimes,
+  kSlotSol,
+  kSlotImgCorr,
+  kSlotErr,
+  kSlotOutVis,
+};
+
+// Exclusive scan of n uint32 values in place (device), returning the total.
+void exclusive_scan_u32(DeviceArena &arena, uint32_t *d, int64_t n,
+                        cudaStream_t s);
+
+}  // namespace wgpu
