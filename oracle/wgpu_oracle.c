@@ -600,8 +600,8 @@ int oracle_wgrid_invert(const OraclePlan *P, size_t n_rows, size_t n_chan,
     const double wp = P->w0 + (double)p * P->dw;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < W * H; ++i) {
-      double s = 0.0, c = 1.0;
-      if (P->n_planes > 1) sincos_turns(wp * nu_w[i], &s, &c);
+      double s, c;
+      sincos_turns(wp * nu_w[i], &s, &c);
       /* Re(F exp(-2 pi i w_p nu)) */
       dirty[i] += img[2 * i] * c + img[2 * i + 1] * s;
     }
@@ -654,8 +654,8 @@ int oracle_wgrid_predict(const OraclePlan *P, size_t n_rows, size_t n_chan,
         memset(col, 0, sizeof(double) * 2 * nv);
         for (int64_t y = 0; y < H; ++y) {
           const int64_t i = x + y * W;
-          double s = 0.0, c = 1.0;
-          if (P->n_planes > 1) sincos_turns(wp * nu_w[i], &s, &c);
+          double s, c;
+          sincos_turns(wp * nu_w[i], &s, &c);
           const int64_t bb = (((y - H / 2) % nv) + nv) % nv;
           col[2 * bb] = corr[i] * c;
           col[2 * bb + 1] = corr[i] * s;

@@ -67,6 +67,11 @@ const GaussLegendre &gl() {
 constexpr double kCellRate = 2.0e12;
 constexpr double kByteRate = 4.5e12;
 
+// Relative FP32 round-off of the gridded planes per unit of correction
+// amplification; measured on GB300 as 2-3e-8 (random visibilities, 2D and 3D
+// plans), rounded up.
+constexpr double kFp32Noise = 5e-8;
+
 }  // namespace
 
 double es_kernel(double beta, double z) {
@@ -165,10 +170,14 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     if (e.sigma < smin - 1e-9 || e.sigma > smax + 1e-9) continue;
     if (req.force_support > 0 && e.support != req.force_support) continue;
     if (req.force_sigma > 0 && std::fabs(e.sigma - req.force_sigma) > 1e-6) continue;
-    // Worst case over the image band (a few point sources near the edge see
-    // the maximum, not the RMS, aliasing error), summed in quadrature over
-    // the gridded dimensions.
-    const double est = std::sqrt(ndim) * e.err_max;
+    // Aliasing: worst case over the image band (a few point sources near the
+    // edge see the maximum, not the RMS, error), summed in quadrature over the
+    // gridded dimensions.  FP32 round-off: the grid and FFT carry white noise
+    // of relative size ~kFp32Noise, which the grid correction magnifies by
+    // amp_rms in every corrected dimension.
+    const double alias = std::sqrt(ndim) * e.err_max;
+    const double fp32 = kFp32Noise * std::pow(e.amp_rms, ndim);
+    const double est = std::sqrt(alias * alias + fp32 * fp32);
     if (est < fallback_err) {
       fallback_err = est;
       fallback = &e;

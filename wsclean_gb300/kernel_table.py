@@ -71,15 +71,25 @@ def best_beta(W, sigma):
             lo = a
     g = 0.5 * (lo + hi)
     rms, mx = alias_error(W, g * base, sigma)
-    return g * base, rms, mx
+    return g * base, rms, mx, amplification(W, g * base, sigma)
+
+
+def amplification(W, beta, sigma, nf=200):
+    """RMS over the band |f| <= 1/(2 sigma) of psihat(0) / psihat(f): the factor
+    by which the grid correction magnifies white round-off noise of the grid
+    and of the FFT.  In FP32 this, raised to the number of corrected
+    dimensions, sets the noise floor of the result."""
+    f = np.linspace(0.0, 0.5 / sigma, nf)
+    a = psihat(0.0, W, beta)[0] / psihat(f, W, beta)
+    return float(np.sqrt(np.mean(a * a)))
 
 
 def build_table():
     rows = []
     for W in W_RANGE:
         for s in SIGMAS:
-            beta, rms, mx = best_beta(W, s)
-            rows.append((W, s, beta, rms, mx))
+            beta, rms, mx, amp = best_beta(W, s)
+            rows.append((W, s, beta, rms, mx, amp))
     return rows
 
 
@@ -87,13 +97,14 @@ def write_header(rows, path):
     with open(path, "w") as fh:
         fh.write("// Generated by wsclean_gb300/kernel_table.py: ES kernel parameters.\n")
         fh.write("// Columns: support W (cells), oversampling sigma, beta, RMS and max\n")
-        fh.write("// one-dimensional relative aliasing error over |f| <= 1/(2 sigma).\n")
+        fh.write("// one-dimensional relative aliasing error over |f| <= 1/(2 sigma), and the\n")
+        fh.write("// RMS correction amplification psihat(0)/psihat(f) over the same band.\n")
         fh.write("#pragma once\n\nnamespace wgpu {\n\n")
         fh.write("struct EsKernelEntry { int support; double sigma; double beta;"
-                 " double err_rms; double err_max; };\n\n")
+                 " double err_rms; double err_max; double amp_rms; };\n\n")
         fh.write("static const EsKernelEntry kEsKernelTable[] = {\n")
-        for W, s, beta, rms, mx in rows:
-            fh.write(f"    {{{W}, {s:.2f}, {beta:.10f}, {rms:.6e}, {mx:.6e}}},\n")
+        for W, s, beta, rms, mx, amp in rows:
+            fh.write(f"    {{{W}, {s:.2f}, {beta:.10f}, {rms:.6e}, {mx:.6e}, {amp:.6e}}},\n")
         fh.write("};\n\n")
         fh.write(f"static const int kEsKernelTableSize = {len(rows)};\n\n}}  // namespace wgpu\n")
 
@@ -101,6 +112,6 @@ def write_header(rows, path):
 if __name__ == "__main__":
     rows = build_table()
     for r in rows:
-        print("W=%2d sigma=%.2f beta=%8.4f rms=%.3e max=%.3e" % r)
+        print("W=%2d sigma=%.2f beta=%8.4f rms=%.3e max=%.3e amp=%.3e" % r)
     here = os.path.dirname(os.path.abspath(__file__))
     write_header(rows, os.path.join(here, "csrc", "es_table.h"))
