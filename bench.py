@@ -1,0 +1,499 @@
+#!/usr/bin/env python
+"""Grid + degrid throughput of the GB300 w-gridder.
+
+One step = one inversion (AddInversionData of the whole visibility set, the
+ms2dirty path behind WGriddingGridder_Simple) followed by one prediction of the
+model image at the same visibilities (PredictVisibilities, the dirty2ms path),
+on the wide-field workload: 8192 x 8192 image, 3" pixels, 256 antennas
+log-radial to 20 km, 32640 baselines x 300 x 8 s, 64 channels 0.9-1.7 GHz,
+500 point sources, epsilon 1e-5 (synthetic data of those shapes).
+
+value  : visibilities per second (Gvis/s) with inputs resident in HBM, through
+         the _device entry points of the C ABI.
+e2e    : the same step through the host-pointer entry points (pinned host
+         buffers; host<->device copies inside the timed region).
+Prints one JSON line (rank 0).  --impl reference times the CPU implementation
+(the oracle's FP64 w-gridder port) on the host cores instead.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD_TEXT = {
+    "wide8192": ("wide-field 8192x8192, 3arcsec pixels, 256 antennas log-radial to 20 km, "
+                 "32640 baselines x 300 x 8 s, 64 channels 0.9-1.7 GHz, 500 sources, eps 1e-5"),
+    "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
+                  "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
+}
+METRIC = "Gvis/s grid+degrid at rel.err <=1e-5 vs FP64 DFT"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------- clocks ---
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- data ---
+def build_data(name, device, seed, max_rows=None):
+    import torch
+    from wsclean_gb300 import synthetic
+    d = synthetic.make_workload(name, seed=seed, max_rows=max_rows, with_model=False)
+    uvw, freq, wts = d["uvw"], d["freq"], d["weights"]
+    cfg = synthetic.WORKLOADS[name]
+    vis = synthetic.model_vis_torch(uvw, freq, d["sources"], device)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    noise = torch.randn(vis.shape, generator=g, dtype=torch.complex64, device=device)
+    d_w = torch.as_tensor(wts, device=device)
+    vis = (vis + cfg["noise"] * math.sqrt(2.0) * noise) * d_w
+    del noise
+    d["d_vis"] = vis.contiguous()
+    d["d_mask"] = (d_w > 0).to(torch.uint8).contiguous()
+    del d_w
+    d["d_uvw"] = torch.as_tensor(uvw, device=device).contiguous()
+    d["d_freq"] = torch.as_tensor(freq, device=device).contiguous()
+    W = d["width"]
+    model = np.zeros(W * W, np.float32)
+    for l, m, s in d["sources"]:
+        x = int(round(W / 2 - l / d["dl"]))
+        y = int(round(m / d["dl"] + W / 2))
+        if 0 <= x < W and 0 <= y < W:
+            model[y * W + x] += s
+    d["model"] = model
+    return d
+
+
+def pinned_copy(t):
+    import torch
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h
+
+
+# ------------------------------------------------------- algorithmic bytes ---
+def stage_bytes(stage, direction, p, n_vis, n_batch_avg):
+    """Minimum HBM bytes of one launch of `stage` (per plane batch)."""
+    nu, nv, W, H = p.nu, p.nv, p.width, p.height
+    rs = (W + 31) // 32 * 32
+    nb = n_batch_avg
+    plane = 8.0 * nu * nv * nb
+    rows = 8.0 * rs * nv * nb
+    touch = 32.0 * n_vis * min(1.0, (nb + p.support - 1) / p.n_planes)
+    if stage == "grid":
+        return plane + touch
+    if stage == "degrid":
+        return plane + touch + 8.0 * n_vis * min(1.0, (nb + p.support - 1) / p.n_planes)
+    if stage == "fft_rows":
+        return plane + rows
+    if stage == "fft_cols_a":
+        return 2 * rows
+    if stage == "fft_cols_b_screen":
+        if direction == "invert":
+            return rows + 8.0 * W * H + 16.0 * W * H
+        return rows + 8.0 * W * H + 4.0 * W * H
+    return None
+
+
+def survey_request_bytes(p, n_vis, n_rows):
+    """Per-request algorithmic bytes: 8 N_vis + 24 N_rows + n_w (40 sigma^2 + 16)
+    Nx Ny + 4 Nx Ny, with sigma^2 Nx Ny the padded grid actually used."""
+    npix = p.width * p.height
+    return 8.0 * n_vis + 24.0 * n_rows + p.n_planes * (40.0 * p.nu * p.nv + 16.0 * npix) + 4.0 * npix
+
+
+# ------------------------------------------------------------ CPU baseline ---
+def cpu_baseline(d, vis_rows, plan, n_vis_total, sample_rows, n_planes_timed, seed=3):
+    """Times the oracle's FP64 CPU w-gridder (all host threads) on a bounded
+    sample: spreading of a random row subset over every plane it touches, and
+    n_planes_timed plane FFT + w-screen passes; extrapolates to the workload.
+    vis_rows(rows) returns the visibilities of the sampled rows."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    n_rows = d["uvw"].shape[0]
+    rows = np.sort(rng.choice(n_rows, size=min(sample_rows, n_rows), replace=False))
+    uvw = d["uvw"][rows]
+    vis = vis_rows(rows)
+    n_sample = int(np.count_nonzero(vis))
+    cores = os.cpu_count()
+    t_vis, t_planes = oracle.wgrid_time_parts(plan, uvw, d["freq"], vis, n_threads=cores,
+                                              n_planes_timed=n_planes_timed)
+    per_vis = t_vis / max(n_sample, 1)
+    per_plane = t_planes / n_planes_timed
+    n_gridded = int(d["n_gridded"])
+    t_grid = per_vis * n_gridded + per_plane * plan.n_planes
+    # the degrid pass moves the same data in the other direction: charged equal
+    t_step = 2.0 * t_grid
+    return dict(value=n_vis_total / t_step / 1e9, unit="Gvis/s", cores=cores, kind="port",
+                sample=(f"FP64 CPU w-gridder (oracle port, {cores} threads): {rows.size} rows "
+                        f"({n_sample} non-zero vis) spread over all their planes in "
+                        f"{t_vis:.2f} s, {n_planes_timed} plane FFT+screen passes of "
+                        f"{plan.nu}x{plan.nv} in {t_planes:.2f} s; extrapolated to "
+                        f"{n_gridded} vis x {plan.n_planes} planes, degrid charged equal "
+                        f"to grid"),
+                seconds_per_step=t_step)
+
+
+def accuracy_check(d, plan, eps, n_rows_sample=400, n_pix=4096, n_pred=4096, seed=4):
+    """GPU result vs the oracle's FP64 DFT on a seeded sample (same plan)."""
+    import oracle
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    rng = np.random.default_rng(seed)
+    W, dl = d["width"], d["dl"]
+    rows = np.sort(rng.choice(d["uvw"].shape[0], size=n_rows_sample, replace=False))
+    uvw, freq, vis = d["uvw"][rows], d["freq"], d["h_vis"][rows]
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=eps, num_t=np.float64)
+    g.pin_plan(plan)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    img = g.RealImage().astype(np.float64)
+    pix = rng.choice(W * W, size=n_pix, replace=False)
+    ref = oracle.dft_invert(uvw, freq, vis, W, W, dl, dl, pixels=pix, n_threads=os.cpu_count())
+    inv_err = float(np.linalg.norm(img[pix] - ref) / np.linalg.norm(ref))
+    mask = (np.abs(vis) > 0).astype(np.uint8).ravel()
+    g.InitializePrediction(d["model"])
+    pv = g.PredictVisibilitiesMasked(uvw.shape[0], freq.size, uvw, freq, mask)
+    sel = np.flatnonzero(mask)
+    sel = rng.choice(sel, size=min(n_pred, sel.size), replace=False)
+    pr = oracle.dft_predict(uvw, freq, d["model"], W, W, dl, dl, vis_index=sel,
+                            n_threads=os.cpu_count())
+    pred_err = float(np.linalg.norm(pv[sel] - pr) / np.linalg.norm(pr))
+    g.close()
+    return {"invert_rel_l2": inv_err, "predict_rel_l2": pred_err,
+            "sample": f"{int(np.count_nonzero(mask))} vis x {n_pix} pixels (invert), "
+                      f"{sel.size} vis (predict), plan pinned to the full-data plan"}
+
+
+# -------------------------------------------------------------- GPU arm -----
+def run_gpu(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from wsclean_gb300 import _lib
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    _lib.lib()
+
+    t0 = time.time()
+    d = build_data(args.workload, dev, seed=2 + rank, max_rows=args.max_rows)
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    n_rows, n_chan = d["uvw"].shape[0], d["freq"].size
+    n_vis = n_rows * n_chan
+    d["n_gridded"] = int(d["d_mask"].sum().item())
+    eps = d["epsilon"]
+    W = d["width"]
+    # the reference picks the double instantiation at this accuracy
+    num_t = np.float64 if eps <= 1.01e-5 else np.float32
+    g = WGriddingGridder_Simple(W, W, W, W, d["dl"], d["dl"], 0.0, 0.0, os.cpu_count(),
+                                epsilon=eps, num_t=num_t)
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+    d_out = torch.empty(n_vis, dtype=torch.complex64, device=dev)
+    inv_weight = 1.0 / d["image_weight"]
+
+    timings = {}
+
+    def step_device():
+        g.InitializeInversion()
+        g.AddInversionDataDevice(n_rows, n_chan, d["d_uvw"].data_ptr(), d["d_freq"].data_ptr(),
+                                 d["d_vis"].data_ptr())
+        timings["invert"] = g.last_timings()
+        g.FinalizeImage(inv_weight)
+        g.InitializePrediction(d["model"])
+        g.PredictVisibilitiesMaskedDevice(n_rows, n_chan, d["d_uvw"].data_ptr(),
+                                          d["d_freq"].data_ptr(), d["d_mask"].data_ptr(),
+                                          d_out.data_ptr())
+        timings["predict"] = g.last_timings()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        launches0 = _lib.lib().wgpu_kernel_launch_count()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        start.record(stream)
+        for _ in range(steps):
+            fn()
+        end.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        ms = start.elapsed_time(end)
+        launches = _lib.lib().wgpu_kernel_launch_count() - launches0
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.barrier()
+            ms = float(t.item())
+        return ms, wall, launches
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, wall, launches = timed(step_device, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_per_step = ms / args.steps
+    value = world * n_vis / (ms_per_step * 1e-3) / 1e9
+
+    # plans of the last step
+    g.InitializeInversion()
+    g.AddInversionDataDevice(n_rows, n_chan, d["d_uvw"].data_ptr(), d["d_freq"].data_ptr(),
+                             d["d_vis"].data_ptr())
+    plan_inv = g.last_plan()
+    inv_stage = g.last_timings()
+    g.InitializePrediction(d["model"])
+    g.PredictVisibilitiesMaskedDevice(n_rows, n_chan, d["d_uvw"].data_ptr(),
+                                      d["d_freq"].data_ptr(), d["d_mask"].data_ptr(),
+                                      d_out.data_ptr())
+    plan_pred = g.last_plan()
+    pred_stage = g.last_timings()
+    torch.cuda.synchronize()
+
+    # ---- roofline of the dominant kernel
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    rows = []
+    for direction, stages, plan in (("invert", inv_stage, plan_inv), ("predict", pred_stage, plan_pred)):
+        n_batches = math.ceil(plan.n_planes / plan.plane_batch)
+        nb_avg = plan.n_planes / n_batches
+        for name, (sms, cnt) in stages.items():
+            b = stage_bytes(name, direction, plan, d["n_gridded"], nb_avg)
+            rows.append(dict(direction=direction, stage=name, ms=sms, launches=cnt,
+                             bytes_per_launch=b))
+    dom = max(rows, key=lambda r: r["ms"])
+    per_launch_ms = dom["ms"] / max(dom["launches"], 1)
+    achieved = (dom["bytes_per_launch"] / (per_launch_ms * 1e-3) / 1e9
+                if dom["bytes_per_launch"] else None)
+    roofline = {"bound": "hbm", "kernel": f"{dom['direction']}:{dom['stage']}",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak if achieved else None), "traffic": None,
+                "peak_source": peak_src,
+                "stages": {f"{r['direction']}:{r['stage']}": round(r["ms"], 3) for r in rows}}
+    if args.traffic:
+        roofline["traffic"] = args.traffic
+
+    # ---- e2e through the host-pointer API (pinned buffers)
+    e2e = None
+    if not args.no_e2e:
+        h_uvw = pinned_copy(d["d_uvw"]).numpy()
+        h_freq = d["freq"]
+        h_vis = pinned_copy(d["d_vis"]).numpy()
+        h_mask = pinned_copy(d["d_mask"]).numpy()
+        h_out = pinned_copy(d_out).numpy()
+
+        def step_host():
+            g.InitializeInversion()
+            g.AddInversionData(n_rows, n_chan, h_uvw, h_freq, h_vis)
+            g.FinalizeImage(inv_weight)
+            g.RealImage()
+            g.InitializePrediction(d["model"])
+            g.PredictVisibilitiesMasked(n_rows, n_chan, h_uvw, h_freq, h_mask, out=h_out)
+
+        e_ms, e_wall, _ = timed(step_host, max(1, args.steps // 2), 1)
+        e_steps = max(1, args.steps // 2)
+        e_ms_step = max(e_ms, e_wall * 1e3) / e_steps
+        h2d = (h_uvw.nbytes * 2 + h_freq.nbytes * 2 + h_vis.nbytes + h_mask.nbytes +
+               d["model"].nbytes)
+        d2h = h_out.nbytes + W * W * 4
+        e2e = {"value": world * n_vis / (e_ms_step * 1e-3) / 1e9, "unit": "Gvis/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": e_ms_step}
+        d["h_vis"] = h_vis.reshape(n_rows, n_chan)
+    else:
+        d["h_vis"] = d["d_vis"].cpu().numpy().reshape(n_rows, n_chan)
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "Gvis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD_TEXT.get(args.workload, args.workload),
+            "n_vis": n_vis, "n_vis_gridded": d["n_gridded"], "n_rows": n_rows,
+            "flagged_fraction": d["flagged_fraction"],
+            "step": "InitializeInversion + AddInversionData + FinalizeImage + "
+                    "InitializePrediction + PredictVisibilities(masked to the gridded set)",
+            "plan_invert": {k: getattr(plan_inv, k) for k in ("nu", "support", "sigma",
+                                                              "n_planes", "plane_batch",
+                                                              "est_error")},
+            "plan_predict": {k: getattr(plan_pred, k) for k in ("nu", "support", "sigma",
+                                                                "n_planes", "plane_batch",
+                                                                "est_error")},
+            "l2": "inputs larger than L2 (visibilities 5 GB, planes 1.2 GB each)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "request_bytes_roofline_frac": None,
+            "datagen_s": round(gen_s, 1),
+        },
+        "roofline": roofline,
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+    }
+    req_bytes = (survey_request_bytes(plan_inv, d["n_gridded"], n_rows) +
+                 survey_request_bytes(plan_pred, d["n_gridded"], n_rows))
+    result["config"]["request_bytes_roofline_frac"] = (req_bytes / (ms_per_step * 1e-3) / 1e9) / peak
+
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(d, lambda r: d["h_vis"][r], plan_inv, n_vis,
+                                              args.cpu_sample_rows, args.cpu_planes)
+        result["cpu_baseline"].pop("seconds_per_step", None)
+        result["config"]["accuracy"] = accuracy_check(d, plan_inv, eps)
+    g.close()
+    return result
+
+
+# ---------------------------------------------------------- reference arm ---
+def run_reference(args):
+    """CPU implementation of the path (the oracle's FP64 w-gridder port; the
+    reference's own wgridder is ducc0, which is absent from the reference tree
+    and cannot be built here), timed on all host cores, each step a bounded
+    sample of the same workload, extrapolated to the metric."""
+    from wsclean_gb300 import _lib, synthetic
+    d = synthetic.make_workload(args.workload, seed=2, max_rows=args.max_rows, with_model=False)
+    n_rows, n_chan = d["uvw"].shape[0], d["freq"].size
+
+    def vis_rows(rows):
+        # random unit-variance visibilities on the non-flagged samples
+        rng = np.random.default_rng(int(rows[0]) + 9)
+        w = d["weights"][rows]
+        v = rng.standard_normal(w.shape) + 1j * rng.standard_normal(w.shape)
+        return np.where(w > 0, v, 0).astype(np.complex64)
+
+    d["n_gridded"] = int(np.count_nonzero(d["weights"]))
+    keep = d["weights"] > 0
+    wl = d["uvw"][:, 2:3] * (d["freq"] / 299792458.0)[None, :]
+    plan = _lib.make_plan(width=d["width"], height=d["height"], dl=d["dl"], dm=d["dl"],
+                          epsilon=d["epsilon"], w_min=float(wl[keep].min()),
+                          w_max=float(wl[keep].max()), n_vis=d["n_gridded"])
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(d, vis_rows, plan, n_rows * n_chan, args.cpu_sample_rows // 2, 1,
+                          seed=100 + i)
+        if i >= args.warmup:
+            vals.append(cb)
+    v = float(np.median([c["value"] for c in vals]))
+    ms = float(np.median([c["seconds_per_step"] for c in vals])) * 1e3
+    cb = vals[-1]
+    cb.pop("seconds_per_step", None)
+    cb["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gvis/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD_TEXT.get(args.workload, args.workload),
+                       "n_vis": n_rows * n_chan, "n_vis_gridded": d["n_gridded"],
+                       "note": "ducc0 (the reference's wgridder) is absent from the reference "
+                               "tree; the FP64 CPU restatement is timed instead"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Gvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="wgpu", choices=["wgpu", "reference"])
+    ap.add_argument("--workload", default="wide8192", choices=sorted(WORKLOAD_TEXT))
+    ap.add_argument("--max-rows", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-rows", type=int, default=200000)
+    ap.add_argument("--cpu-planes", type=int, default=2)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu DRAM bytes per launch of the dominant kernel, if captured")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    res = run_gpu(args, rank, world, local)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

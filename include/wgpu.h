@@ -186,14 +186,36 @@ int wgpu_gridder_predict_visibilities_device(wgpu_gridder_t *gridder,
                                              const double *d_freq,
                                              float *d_vis);
 
+/* PredictVisibilities restricted to the samples whose mask byte is non-zero
+ * ([row * n_chan + chan]); the others are written as 0 and cost nothing.
+ * This answers the open question in gridder_simple.h:181-182 ("how do we
+ * indicate flagged visibilities that do not need to be computed?"); the
+ * reference itself predicts every sample.  d_ variant: device pointers. */
+int wgpu_gridder_predict_visibilities_masked(wgpu_gridder_t *gridder,
+                                             size_t n_rows, size_t n_chan,
+                                             const double *uvw,
+                                             const double *freq,
+                                             const uint8_t *mask, float *vis);
+int wgpu_gridder_predict_visibilities_masked_device(
+    wgpu_gridder_t *gridder, size_t n_rows, size_t n_chan, const double *d_uvw,
+    const double *d_freq, const uint8_t *d_mask, float *d_vis);
+
 /* Plan used by the last inversion/prediction call of this gridder. */
 int wgpu_gridder_last_plan(const wgpu_gridder_t *gridder, wgpu_plan_t *plan);
 
 /* Per-stage device times of the last call (milliseconds, CUDA events on the
- * gridder's stream): names are written as a ';'-separated list. */
+ * gridder's stream) and the number of launches charged to each stage; names
+ * are written as a ';'-separated list. */
 int wgpu_gridder_last_timings(const wgpu_gridder_t *gridder, double *ms,
-                              int max_entries, char *names, size_t names_len,
-                              int *n_entries);
+                              int *counts, int max_entries, char *names,
+                              size_t names_len, int *n_entries);
+
+/* Use `plan` for every following inversion/prediction call instead of
+ * planning per call (NULL returns to per-call planning).  Calls whose data do
+ * not fit the plan's w-planes fail with WGPU_ERR_INVALID.  Keeping one plan
+ * across the major cycles of an imaging run keeps the grids comparable; it
+ * has no counterpart in the reference, where ducc0 plans every call. */
+int wgpu_gridder_pin_plan(wgpu_gridder_t *gridder, const wgpu_plan_t *plan);
 
 /* Gridder's CUDA stream (cudaStream_t), for callers that time or order work
  * around the _device entry points. */

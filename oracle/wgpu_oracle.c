@@ -310,21 +310,36 @@ int64_t oracle_bucket(const OraclePlan *P, size_t n_rows, size_t n_chan,
 typedef struct {
   int n, nf;
   int f[40];
+  double *tw; /* exp(-2 pi i j / n), j < n */
 } FftPlan;
 
 static int fft_plan(int n, FftPlan *p) {
   p->n = n;
   p->nf = 0;
+  p->tw = NULL;
   int m = n;
   while (m % 4 == 0) { p->f[p->nf++] = 4; m /= 4; }
   while (m % 2 == 0) { p->f[p->nf++] = 2; m /= 2; }
   while (m % 3 == 0) { p->f[p->nf++] = 3; m /= 3; }
   while (m % 5 == 0) { p->f[p->nf++] = 5; m /= 5; }
-  return m == 1 ? 0 : -1;
+  if (m != 1) return -1;
+  p->tw = (double *)malloc(sizeof(double) * 2 * n);
+  for (int j = 0; j < n; ++j) {
+    const double a = -TWO_PI * (double)j / (double)n;
+    p->tw[2 * j] = cos(a);
+    p->tw[2 * j + 1] = sin(a);
+  }
+  return 0;
 }
 
-/* One transform of length n; x and y are n complex doubles (interleaved);
- * result ends up in x.  sign = -1 forward, +1 backward (unnormalised). */
+static void fft_free(FftPlan *p) {
+  free(p->tw);
+  p->tw = NULL;
+}
+
+/* One transform of length n (Stockham autosort); x and y are n complex doubles
+ * (interleaved); the result ends up in x.  sign = -1 forward, +1 backward
+ * (unnormalised). */
 static void fft_run(const FftPlan *P, double *x, double *y, int sign) {
   const int n = P->n;
   int p = 1;
@@ -332,14 +347,21 @@ static void fft_run(const FftPlan *P, double *x, double *y, int sign) {
   for (int s = 0; s < P->nf; ++s) {
     const int R = P->f[s];
     const int nR = n / R;
+    const int step = n / (p * R);
+    /* roots of unity of order R */
+    double rr[5], ri[5];
+    for (int q = 0; q < R; ++q) {
+      rr[q] = P->tw[2 * (q * (n / R))];
+      ri[q] = sign * -P->tw[2 * (q * (n / R)) + 1];
+    }
     for (int i = 0; i < nR; ++i) {
       const int k = i % p;
       double ur[5], ui[5];
       for (int t = 0; t < R; ++t) {
         double re = a[2 * (i + t * nR)], im = a[2 * (i + t * nR) + 1];
         if (t > 0 && k > 0) {
-          const double ang = sign * TWO_PI * (double)(t * k) / (double)(p * R);
-          const double c = cos(ang), sn = sin(ang);
+          const int j = t * k * step;
+          const double c = P->tw[2 * j], sn = sign * -P->tw[2 * j + 1];
           const double tr = re * c - im * sn;
           im = re * sn + im * c;
           re = tr;
@@ -347,22 +369,16 @@ static void fft_run(const FftPlan *P, double *x, double *y, int sign) {
         ur[t] = re;
         ui[t] = im;
       }
-      double vr[5], vi[5];
+      const int j = (i - k) * R + k;
       for (int q = 0; q < R; ++q) {
         double sr = 0.0, si = 0.0;
         for (int t = 0; t < R; ++t) {
-          const double ang = sign * TWO_PI * (double)((t * q) % R) / (double)R;
-          const double c = cos(ang), sn = sin(ang);
-          sr += ur[t] * c - ui[t] * sn;
-          si += ur[t] * sn + ui[t] * c;
+          const int e = (t * q) % R;
+          sr += ur[t] * rr[e] - ui[t] * ri[e];
+          si += ur[t] * ri[e] + ui[t] * rr[e];
         }
-        vr[q] = sr;
-        vi[q] = si;
-      }
-      const int j = (i - k) * R + k;
-      for (int q = 0; q < R; ++q) {
-        b[2 * (j + q * p)] = vr[q];
-        b[2 * (j + q * p) + 1] = vi[q];
+        b[2 * (j + q * p)] = sr;
+        b[2 * (j + q * p) + 1] = si;
       }
     }
     p *= R;
@@ -479,10 +495,10 @@ static void correction_table(const OraclePlan *P, const double *nu_w,
 /* grid all vis touching plane p into grid (nv x nu complex doubles). */
 static void grid_plane(const OraclePlan *P, const GridVis *g, size_t n,
                        const size_t *order, const size_t *pstart, int p,
-                       double *grid) {
+                       double *grid, int clear) {
   const int W = (int)P->support, nW = plane_count_w(P);
   const int64_t nu = P->nu, nv = P->nv;
-  memset(grid, 0, sizeof(double) * 2 * nu * nv);
+  if (clear) memset(grid, 0, sizeof(double) * 2 * nu * nv);
   /* vis with ip in [p - nW + 1, p]; grouped by stripe parity for threads */
   const int64_t stripe = 64 > W ? 64 : W;
   const int64_t n_stripes = nv / stripe > 0 ? nv / stripe : 1;
@@ -550,6 +566,8 @@ static void fft_forward_crop(const OraclePlan *P, double *grid, double *img) {
     free(tmp);
     free(col);
   }
+  fft_free(&pu);
+  fft_free(&pv);
 }
 
 static void pixel_nu_table(const OraclePlan *P, double *nu_w) {
@@ -583,6 +601,8 @@ int oracle_wgrid_invert(const OraclePlan *P, size_t n_rows, size_t n_chan,
   if (n_threads > 0) omp_set_num_threads(n_threads);
   FftPlan t1, t2;
   if (fft_plan((int)P->nu, &t1) || fft_plan((int)P->nv, &t2)) return -2;
+  fft_free(&t1);
+  fft_free(&t2);
   GridVis *g;
   size_t n;
   if (prepare_vis(P, n_rows, n_chan, uvw, freq, vis, 1, &g, &n)) return -1;
@@ -595,7 +615,7 @@ int oracle_wgrid_invert(const OraclePlan *P, size_t n_rows, size_t n_chan,
   pixel_nu_table(P, nu_w);
   memset(dirty, 0, sizeof(double) * W * H);
   for (int p = 0; p < P->n_planes; ++p) {
-    grid_plane(P, g, n, order, pstart, p, grid);
+    grid_plane(P, g, n, order, pstart, p, grid, 1);
     fft_forward_crop(P, grid, img);
     const double wp = P->w0 + (double)p * P->dw;
 #pragma omp parallel for schedule(static)
@@ -711,6 +731,8 @@ int oracle_wgrid_predict(const OraclePlan *P, size_t n_rows, size_t n_chan,
   free(order);
   free(pstart);
   free(g);
+  fft_free(&pu);
+  fft_free(&pv);
   return 0;
 }
 
@@ -726,9 +748,11 @@ double oracle_wgrid_time_parts(const OraclePlan *P, size_t n_rows,
   if (prepare_vis(P, n_rows, n_chan, uvw, freq, vis, 1, &g, &n)) return -1.0;
   size_t *order, *pstart;
   sort_by_plane(P, g, n, &order, &pstart);
-  double *grid = malloc(sizeof(double) * 2 * P->nu * P->nv);
+  double *grid = calloc(2 * P->nu * P->nv, sizeof(double));
+  /* spreading cost of every sample over all the planes it touches (the
+   * per-plane clearing is charged to the plane part below) */
   for (int p = 0; p < P->n_planes; ++p)
-    grid_plane(P, g, n, order, pstart, p, grid);
+    grid_plane(P, g, n, order, pstart, p, grid, 0);
   const double t1 = omp_get_wtime();
   const int64_t W = P->width, H = P->height;
   double *img = malloc(sizeof(double) * 2 * W * H);
@@ -737,6 +761,7 @@ double oracle_wgrid_time_parts(const OraclePlan *P, size_t n_rows,
   pixel_nu_table(P, nu_w);
   const double t2 = omp_get_wtime();
   for (int p = 0; p < n_planes_timed; ++p) {
+    memset(grid, 0, sizeof(double) * 2 * P->nu * P->nv);
     fft_forward_crop(P, grid, img);
     const double wp = P->w0 + (double)p * P->dw;
 #pragma omp parallel for schedule(static)

@@ -73,9 +73,12 @@ _PROTOS = {
     "wgpu_gridder_initialize_prediction": (I, [P, P]),
     "wgpu_gridder_predict_visibilities": (I, [P, SZ, SZ, P, P, P]),
     "wgpu_gridder_predict_visibilities_device": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_predict_visibilities_masked": (I, [P, SZ, SZ, P, P, P, P]),
+    "wgpu_gridder_predict_visibilities_masked_device": (I, [P, SZ, SZ, P, P, P, P]),
     "wgpu_gridder_last_plan": (I, [P, C.POINTER(Plan)]),
-    "wgpu_gridder_last_timings": (I, [P, C.POINTER(C.c_double), I, C.c_char_p, SZ,
-                                      C.POINTER(I)]),
+    "wgpu_gridder_last_timings": (I, [P, C.POINTER(C.c_double), C.POINTER(I), I, C.c_char_p,
+                                      SZ, C.POINTER(I)]),
+    "wgpu_gridder_pin_plan": (I, [P, C.POINTER(Plan)]),
     "wgpu_gridder_stream": (P, [P]),
     "wgpu_kernel_launch_count": (C.c_uint64, []),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,

@@ -58,19 +58,28 @@ struct StageTimer {
     names.push_back(name);
   }
   // Returns totals per stage name (last mark is the end marker).
-  std::vector<std::pair<std::string, double>> collect() {
-    std::vector<std::pair<std::string, double>> out;
+  struct Stage {
+    std::string name;
+    double ms;
+    int count;
+  };
+  std::vector<Stage> collect() {
+    std::vector<Stage> out;
     if (used < 2) return out;
     WGPU_CUDA(cudaEventSynchronize(pool[used - 1]));
-    std::map<std::string, double> acc;
-    std::vector<std::string> order;
+    std::map<std::string, size_t> index;
     for (size_t i = 0; i + 1 < used; ++i) {
       float ms = 0.f;
       WGPU_CUDA(cudaEventElapsedTime(&ms, pool[i], pool[i + 1]));
-      if (!acc.count(names[i])) order.push_back(names[i]);
-      acc[names[i]] += ms;
+      auto it = index.find(names[i]);
+      if (it == index.end()) {
+        index[names[i]] = out.size();
+        out.push_back({names[i], 0.0, 0});
+        it = index.find(names[i]);
+      }
+      out[it->second].ms += ms;
+      out[it->second].count += 1;
     }
-    for (auto &n : order) out.emplace_back(n, acc[n]);
     return out;
   }
   ~StageTimer() {
@@ -90,8 +99,10 @@ struct wgpu_gridder {
   void *d_img = nullptr;
   enum class Mode { kNone, kInversion, kPrediction } mode = Mode::kNone;
   wgpu_plan_t last_plan;
+  bool pinned = false;
+  wgpu_plan_t pinned_plan;
   StageTimer timer;
-  std::vector<std::pair<std::string, double>> last_timings;
+  std::vector<StageTimer::Stage> last_timings;
 };
 
 namespace wgpu {
@@ -155,7 +166,30 @@ void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
   WGPU_CUDA(cudaStreamSynchronize(g->stream));
 }
 
+// A pinned plan is used as long as it covers the data: every visibility's w
+// footprint must fall inside its planes (a clamped footprint would be wrong).
+void check_pinned_plan(const wgpu_gridder *g, double w_min, double w_max) {
+  const wgpu_plan_t &p = g->pinned_plan;
+  if (p.width != (int64_t)g->width_t || p.height != (int64_t)g->height_t ||
+      p.dl != g->dl || p.dm != g->dm || p.l_shift != g->l_shift || p.m_shift != g->m_shift)
+    throw Error(WGPU_ERR_INVALID, "pinned plan does not match the gridder geometry");
+  if (p.n_planes > 1) {
+    const double half = 0.5 * (double)p.support;
+    const double lo = p.w0 + (half - 1.0) * p.dw, hi = p.w0 + ((double)p.n_planes - half) * p.dw;
+    if (!(w_min > lo) || !(w_max <= hi))
+      throw Error(WGPU_ERR_INVALID, "data w range exceeds the pinned plan's planes");
+  } else {
+    const double dev = std::max(std::fabs(w_min - p.w0), std::fabs(w_max - p.w0));
+    if (M_PI * dev * (p.nm1_max - p.nm1_min) > 1e-3 * g->epsilon)
+      throw Error(WGPU_ERR_INVALID, "data w range needs w-planes but the pinned plan has one");
+  }
+}
+
 wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis) {
+  if (g->pinned) {
+    check_pinned_plan(g, w_min, w_max);
+    return g->pinned_plan;
+  }
   wgpu_plan_request_t r;
   std::memset(&r, 0, sizeof(r));
   r.width = (int64_t)g->width_t;
@@ -197,7 +231,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->timer.mark("extent");
   double w_min, w_max;
   int64_t count;
-  compute_w_extent(d_uvw, d_freq, d_vis, (int64_t)n_rows, (int64_t)n_chan, true,
+  compute_w_extent(d_uvw, d_freq, d_vis, nullptr, (int64_t)n_rows, (int64_t)n_chan, true,
                    &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
   if (count == 0) {
     g->timer.mark("end");
@@ -209,7 +243,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   log_plan(g, "invert", plan, count);
   const DevPlan dp = to_dev_plan(plan);
   g->timer.mark("bucket");
-  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis,
+  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis, nullptr,
                                              (int64_t)n_rows, (int64_t)n_chan, true, s);
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
@@ -227,9 +261,11 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     launch_grid(dp, b.records, b.offsets, (int)p0, nb, planes, s);
     g->timer.mark("fft_rows");
     launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, s);
-    g->timer.mark("fft_cols_screen");
-    launch_fft_cols_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R,
-                                       rstride, nb, (int)p0, nu_w, acc, s);
+    g->timer.mark("fft_cols_a");
+    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, -1.0f, s);
+    g->timer.mark("fft_cols_b_screen");
+    launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R,
+                                         rstride, nb, (int)p0, nu_w, acc, s);
     if (g->verbosity >= 2)
       std::fprintf(stderr, "wgpu invert: planes %lld..%lld\n", (long long)p0,
                    (long long)(p0 + nb - 1));
@@ -243,7 +279,8 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
 }
 
 void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
-                    const double *d_uvw, const double *d_freq, float *d_vis) {
+                    const double *d_uvw, const double *d_freq,
+                    const uint8_t *d_mask, float *d_vis) {
   if (g->mode != wgpu_gridder::Mode::kPrediction)
     throw Error(WGPU_ERR_STATE, "PredictVisibilities before InitializePrediction");
   if (n_rows == 0 || n_chan == 0) return;
@@ -252,14 +289,22 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->timer.mark("extent");
   double w_min, w_max;
   int64_t count;
-  compute_w_extent(d_uvw, d_freq, nullptr, (int64_t)n_rows, (int64_t)n_chan, false,
+  compute_w_extent(d_uvw, d_freq, nullptr, d_mask, (int64_t)n_rows, (int64_t)n_chan, false,
                    &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
+  if (d_mask) {
+    WGPU_CUDA(cudaMemsetAsync(d_vis, 0, sizeof(float2) * n_rows * n_chan, s));
+    if (count == 0) {
+      g->timer.mark("end");
+      g->last_timings = g->timer.collect();
+      return;
+    }
+  }
   const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
   g->last_plan = plan;
   log_plan(g, "predict", plan, count);
   const DevPlan dp = to_dev_plan(plan);
   g->timer.mark("bucket");
-  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, nullptr,
+  const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, nullptr, d_mask,
                                              (int64_t)n_rows, (int64_t)n_chan, false, s);
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
@@ -277,9 +322,11 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   WGPU_CUDA(cudaMemsetAsync(vacc, 0, sizeof(float2) * (b.n_out + 1), s));
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
-    g->timer.mark("fft_cols_screen");
-    launch_fft_cols_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                    img_corr, nu_w, R, rstride, nb, (int)p0, s);
+    g->timer.mark("fft_cols_b_screen");
+    launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                      img_corr, nu_w, R, rstride, nb, (int)p0, s);
+    g->timer.mark("fft_cols_a");
+    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, +1.0f, s);
     g->timer.mark("fft_rows");
     launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, s);
     g->timer.mark("degrid");
@@ -524,7 +571,38 @@ int wgpu_gridder_predict_visibilities_device(wgpu_gridder_t *g, size_t n_rows,
   if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
   if ((n_rows && n_chan) && (!d_uvw || !d_freq || !d_vis))
     return fail(WGPU_ERR_INVALID, "null data pointer");
-  return guarded([&] { predict_device(g, n_rows, n_chan, d_uvw, d_freq, d_vis); });
+  return guarded([&] { predict_device(g, n_rows, n_chan, d_uvw, d_freq, nullptr, d_vis); });
+}
+
+int wgpu_gridder_predict_visibilities_masked_device(
+    wgpu_gridder_t *g, size_t n_rows, size_t n_chan, const double *d_uvw,
+    const double *d_freq, const uint8_t *d_mask, float *d_vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!d_uvw || !d_freq || !d_vis || !d_mask))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] { predict_device(g, n_rows, n_chan, d_uvw, d_freq, d_mask, d_vis); });
+}
+
+int wgpu_gridder_predict_visibilities_masked(wgpu_gridder_t *g, size_t n_rows,
+                                             size_t n_chan, const double *uvw,
+                                             const double *freq,
+                                             const uint8_t *mask, float *vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if ((n_rows && n_chan) && (!uvw || !freq || !vis || !mask))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kPrediction)
+      throw Error(WGPU_ERR_STATE, "PredictVisibilities before InitializePrediction");
+    if (n_rows == 0 || n_chan == 0) return;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const uint8_t *dm = upload(g, kSlotAnt, mask, n_rows * n_chan);
+    float *dv = (float *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
+    predict_device(g, n_rows, n_chan, du, df, dm, dv);
+    WGPU_CUDA(cudaMemcpyAsync(vis, dv, sizeof(float2) * n_rows * n_chan,
+                              cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
 }
 
 int wgpu_gridder_predict_visibilities(wgpu_gridder_t *g, size_t n_rows,
@@ -540,7 +618,7 @@ int wgpu_gridder_predict_visibilities(wgpu_gridder_t *g, size_t n_rows,
     const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
     const double *df = upload(g, kSlotFreq, freq, n_chan);
     float *dv = (float *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
-    predict_device(g, n_rows, n_chan, du, df, dv);
+    predict_device(g, n_rows, n_chan, du, df, nullptr, dv);
     WGPU_CUDA(cudaMemcpyAsync(vis, dv, sizeof(float2) * n_rows * n_chan,
                               cudaMemcpyDeviceToHost, g->stream));
     WGPU_CUDA(cudaStreamSynchronize(g->stream));
@@ -553,16 +631,34 @@ int wgpu_gridder_last_plan(const wgpu_gridder_t *g, wgpu_plan_t *plan) {
   return WGPU_OK;
 }
 
-int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms,
+int wgpu_gridder_pin_plan(wgpu_gridder_t *g, const wgpu_plan_t *plan) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if (!plan) {
+    g->pinned = false;
+    return WGPU_OK;
+  }
+  if (plan->support < 2 || plan->support > kMaxSupport || plan->n_planes < 1 ||
+      (plan->tile != 16 && plan->tile != 32) || plan->nu % plan->tile || plan->nv % plan->tile ||
+      plan->nu < 2 * plan->tile || plan->nv < 2 * plan->tile || plan->support > plan->tile ||
+      plan->plane_batch < 1 || plan->fft_n1 * plan->fft_n2 != plan->nv ||
+      (plan->n_planes > 1 && plan->n_planes < plan->support))
+    return fail(WGPU_ERR_INVALID, "pinned plan is not self-consistent");
+  g->pinned_plan = *plan;
+  g->pinned = true;
+  return WGPU_OK;
+}
+
+int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms, int *counts,
                               int max_entries, char *names, size_t names_len,
                               int *n_entries) {
   if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
   std::string all;
   int n = 0;
-  for (const auto &kv : g->last_timings) {
-    if (n < max_entries && ms) ms[n] = kv.second;
+  for (const auto &st : g->last_timings) {
+    if (n < max_entries && ms) ms[n] = st.ms;
+    if (n < max_entries && counts) counts[n] = st.count;
     if (n) all += ";";
-    all += kv.first;
+    all += st.name;
     ++n;
   }
   if (n_entries) *n_entries = n;
@@ -604,7 +700,7 @@ int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
         dv = (float *)arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
         WGPU_CUDA(cudaMemcpyAsync(dv, vis, sizeof(float2) * n_rows * n_chan, cudaMemcpyHostToDevice, s));
       }
-      const BucketResult b = bucket_visibilities(arena, dp, du, df, dv, (int64_t)n_rows,
+      const BucketResult b = bucket_visibilities(arena, dp, du, df, dv, nullptr, (int64_t)n_rows,
                                                  (int64_t)n_chan, skip_zero != 0, s);
       std::vector<VisRecord> rec(b.n_out);
       if (b.n_out) {

@@ -82,6 +82,18 @@ __device__ __forceinline__ bool is_zero(const float2 v) {
   return v.x == 0.0f && v.y == 0.0f;
 }
 
+// Which samples take part: inversion skips zero visibilities
+// (gridder_simple.h:111); a prediction mask skips samples whose byte is 0.
+struct Selector {
+  const float2 *vis;     // non-null: skip samples equal to 0
+  const uint8_t *mask;   // non-null: skip samples with mask 0
+  __device__ __forceinline__ bool operator()(int64_t e) const {
+    if (vis && is_zero(vis[e])) return false;
+    if (mask && mask[e] == 0) return false;
+    return true;
+  }
+};
+
 // Order-preserving map double -> uint64 for atomic min/max.
 __device__ __forceinline__ unsigned long long dkey(double d) {
   unsigned long long b = (unsigned long long)__double_as_longlong(d);
@@ -102,15 +114,15 @@ struct MaxOp {
 };
 
 __global__ void __launch_bounds__(kThreads)
-    w_extent_kernel(const double *uvw, const double *freq, const float2 *vis,
-                    int64_t n_rows, int64_t n_chan, int skip_zero,
+    w_extent_kernel(const double *uvw, const double *freq, Selector sel,
+                    int64_t n_rows, int64_t n_chan,
                     unsigned long long *out /*[3]: min key, max key, count*/) {
   double wmin = 1e300, wmax = -1e300;
   unsigned long long cnt = 0;
   const int64_t n = n_rows * n_chan;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
-    if (skip_zero && is_zero(vis[e])) continue;
+    if (!sel(e)) continue;
     const int64_t r = e / n_chan, c = e - r * n_chan;
     const double fl = __ddiv_rn(freq[c], kSpeedOfLight);
     const double wl = __dmul_rn(uvw[3 * r + 2], fl);
@@ -140,15 +152,15 @@ __global__ void __launch_bounds__(kThreads)
 
 __global__ void __launch_bounds__(kThreads)
     key_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
-               const float2 *vis, int64_t n_rows, int64_t n_chan,
-               int skip_zero, uint32_t sentinel, uint32_t *keys,
+               Selector sel, int64_t n_rows, int64_t n_chan,
+               uint32_t sentinel, uint32_t *keys,
                uint32_t *vals, uint32_t *counts) {
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const int64_t r = e / n_chan, c = e - r * n_chan;
   uint32_t key = sentinel;
-  if (!(skip_zero && is_zero(vis[e]))) {
+  if (sel(e)) {
     const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
     key = f.key;
   }
@@ -280,16 +292,17 @@ unsigned grid_for(int64_t n, int threads) {
 }  // namespace
 
 void compute_w_extent(const double *d_uvw, const double *d_freq,
-                      const float *d_vis, int64_t n_rows, int64_t n_chan,
-                      bool skip_zero, double *w_min, double *w_max,
-                      int64_t *count, void *scratch8, cudaStream_t s) {
+                      const float *d_vis, const uint8_t *d_mask, int64_t n_rows,
+                      int64_t n_chan, bool skip_zero, double *w_min,
+                      double *w_max, int64_t *count, void *scratch8,
+                      cudaStream_t s) {
   unsigned long long init[3] = {~0ull, 0ull, 0ull};
   unsigned long long *d = (unsigned long long *)scratch8;
   WGPU_CUDA(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, s));
   const int64_t n = n_rows * n_chan;
   unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), 152 * 8);
-  w_extent_kernel<<<blocks, kThreads, 0, s>>>(d_uvw, d_freq, (const float2 *)d_vis,
-                                              n_rows, n_chan, skip_zero ? 1 : 0, d);
+  const Selector sel{skip_zero ? (const float2 *)d_vis : nullptr, d_mask};
+  w_extent_kernel<<<blocks, kThreads, 0, s>>>(d_uvw, d_freq, sel, n_rows, n_chan, d);
   check_launch("w_extent_kernel");
   unsigned long long out[3];
   WGPU_CUDA(cudaMemcpyAsync(out, d, sizeof(out), cudaMemcpyDeviceToHost, s));
@@ -305,8 +318,8 @@ void compute_w_extent(const double *d_uvw, const double *d_freq,
 
 BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  const double *d_uvw, const double *d_freq,
-                                 const float *d_vis, int64_t n_rows,
-                                 int64_t n_chan, bool skip_zero,
+                                 const float *d_vis, const uint8_t *d_mask,
+                                 int64_t n_rows, int64_t n_chan, bool skip_zero,
                                  cudaStream_t s) {
   const int64_t n = n_rows * n_chan;
   if (n >= (int64_t)0xFFFFFFFFll)
@@ -332,8 +345,8 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   WGPU_CUDA(cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (res.n_keys + 1), s));
   if (n > 0) {
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
-        p, d_uvw, cs, (const float2 *)d_vis, n_rows, n_chan, skip_zero ? 1 : 0,
-        sentinel, keys, vals, offsets);
+        p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
+        n_rows, n_chan, sentinel, keys, vals, offsets);
     check_launch("key_kernel");
   }
   exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);

@@ -472,21 +472,25 @@ void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
   check_launch("fft_rows_backward_pad_kernel");
 }
 
-void launch_fft_cols_forward_accumulate(FftTables &t, const DevPlan &p,
-                                        int n1, int n2, float2 *R, int rstride,
-                                        int n_batch, int p_begin,
-                                        const double *nu_w, float2 *acc,
-                                        cudaStream_t s) {
+void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
+                       int rstride, int n_batch, float sign, cudaStream_t s) {
+  if (n1 <= 1) return;
   const int ncg = rstride / kPanel;
-  if (n1 > 1) {
-    const FftDesc d1 = make_desc(n1);
-    const size_t smem = sizeof(float2) * n1 * kPanel;
-    set_smem((const void *)fft_cols_pass_a_kernel, smem);
-    dim3 grid(ncg, n2, n_batch);
-    fft_cols_pass_a_kernel<<<grid, kColThreads, smem, s>>>(
-        d1, R, rstride, p.nv, n2, -1.0f, fft_twiddles(t, n1), fft_twiddles(t, p.nv));
-    check_launch("fft_cols_pass_a_kernel");
-  }
+  const FftDesc d1 = make_desc(n1);
+  const size_t smem = sizeof(float2) * n1 * kPanel;
+  set_smem((const void *)fft_cols_pass_a_kernel, smem);
+  dim3 grid(ncg, n2, n_batch);
+  fft_cols_pass_a_kernel<<<grid, kColThreads, smem, s>>>(
+      d1, R, rstride, p.nv, n2, sign, fft_twiddles(t, n1), fft_twiddles(t, p.nv));
+  check_launch("fft_cols_pass_a_kernel");
+}
+
+void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1,
+                                          int n2, float2 *R, int rstride,
+                                          int n_batch, int p_begin,
+                                          const double *nu_w, float2 *acc,
+                                          cudaStream_t s) {
+  const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
   const size_t smem = sizeof(float2) * n2 * kPanel;
   set_smem((const void *)fft_cols_forward_accumulate_kernel, smem);
@@ -496,31 +500,20 @@ void launch_fft_cols_forward_accumulate(FftTables &t, const DevPlan &p,
   check_launch("fft_cols_forward_accumulate_kernel");
 }
 
-void launch_fft_cols_backward_screen(FftTables &t, const DevPlan &p, int n1,
-                                     int n2, const float *img_corr,
-                                     const double *nu_w, float2 *R,
-                                     int rstride, int n_batch, int p_begin,
-                                     cudaStream_t s) {
+void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
+                                       int n2, const float *img_corr,
+                                       const double *nu_w, float2 *R,
+                                       int rstride, int n_batch, int p_begin,
+                                       cudaStream_t s) {
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
-  {
-    const size_t smem = sizeof(float2) * n2 * kPanel;
-    set_smem((const void *)fft_cols_backward_screen_kernel, smem);
-    dim3 grid(ncg, n1);
-    fft_cols_backward_screen_kernel<<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin,
-        fft_twiddles(t, n2), fft_twiddles(t, p.nv));
-    check_launch("fft_cols_backward_screen_kernel");
-  }
-  if (n1 > 1) {
-    const FftDesc d1 = make_desc(n1);
-    const size_t smem = sizeof(float2) * n1 * kPanel;
-    set_smem((const void *)fft_cols_pass_a_kernel, smem);
-    dim3 grid(ncg, n2, n_batch);
-    fft_cols_pass_a_kernel<<<grid, kColThreads, smem, s>>>(
-        d1, R, rstride, p.nv, n2, +1.0f, fft_twiddles(t, n1), fft_twiddles(t, p.nv));
-    check_launch("fft_cols_pass_a_kernel");
-  }
+  const size_t smem = sizeof(float2) * n2 * kPanel;
+  set_smem((const void *)fft_cols_backward_screen_kernel, smem);
+  dim3 grid(ncg, n1);
+  fft_cols_backward_screen_kernel<<<grid, kColThreads, smem, s>>>(
+      d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin,
+      fft_twiddles(t, n2), fft_twiddles(t, p.nv));
+  check_launch("fft_cols_backward_screen_kernel");
 }
 
 }  // namespace wgpu

@@ -76,15 +76,16 @@ struct BucketResult {
 // Extents of the (non-zero when skip_zero) visibilities: w min/max in
 // wavelengths and the count.
 void compute_w_extent(const double *d_uvw, const double *d_freq,
-                      const float *d_vis, int64_t n_rows, int64_t n_chan,
-                      bool skip_zero, double *w_min, double *w_max,
-                      int64_t *count, void *scratch8, cudaStream_t s);
+                      const float *d_vis, const uint8_t *d_mask, int64_t n_rows,
+                      int64_t n_chan, bool skip_zero, double *w_min,
+                      double *w_max, int64_t *count, void *scratch8,
+                      cudaStream_t s);
 
 class DeviceArena;
 BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  const double *d_uvw, const double *d_freq,
-                                 const float *d_vis, int64_t n_rows,
-                                 int64_t n_chan, bool skip_zero,
+                                 const float *d_vis, const uint8_t *d_mask,
+                                 int64_t n_rows, int64_t n_chan, bool skip_zero,
                                  cudaStream_t s);
 
 // ---- gridding (grid.cu) ----
@@ -110,17 +111,21 @@ void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
 void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
                                   const float2 *R, int rstride, float2 *planes,
                                   int n_batch, cudaStream_t s);
-// Column passes with the fused w-screen (see fft.cu).
-void launch_fft_cols_forward_accumulate(FftTables &t, const DevPlan &p,
-                                        int n1, int n2, float2 *R, int rstride,
-                                        int n_batch, int p_begin,
-                                        const double *nu_w, float2 *acc,
-                                        cudaStream_t s);
-void launch_fft_cols_backward_screen(FftTables &t, const DevPlan &p, int n1,
-                                     int n2, const float *img_corr,
-                                     const double *nu_w, float2 *R,
-                                     int rstride, int n_batch, int p_begin,
-                                     cudaStream_t s);
+// Column passes (four-step split nv = n1 * n2, see fft.cu): pass A over
+// strided length-n1 transforms, pass B over contiguous length-n2 transforms
+// with the fused w-screen.
+void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
+                       int rstride, int n_batch, float sign, cudaStream_t s);
+void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1,
+                                          int n2, float2 *R, int rstride,
+                                          int n_batch, int p_begin,
+                                          const double *nu_w, float2 *acc,
+                                          cudaStream_t s);
+void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
+                                       int n2, const float *img_corr,
+                                       const double *nu_w, float2 *R,
+                                       int rstride, int n_batch, int p_begin,
+                                       cudaStream_t s);
 
 // ---- corrections (correct.cu) ----
 void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s);

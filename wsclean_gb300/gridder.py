@@ -125,6 +125,21 @@ class WGriddingGridder_Simple:
                                                       ptr(freq), ptr(out)))
         return out
 
+    def PredictVisibilitiesMasked(self, n_rows, n_chan, uvw, freq, mask, out=None):
+        """PredictVisibilities for the samples with mask != 0 (others -> 0)."""
+        uvw, freq = _f64(uvw), _f64(freq)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        assert mask.size == n_rows * n_chan
+        if out is None:
+            out = np.empty(n_rows * n_chan, dtype=np.complex64)
+        check(lib().wgpu_gridder_predict_visibilities_masked(
+            self._h, n_rows, n_chan, ptr(uvw), ptr(freq), ptr(mask), ptr(out)))
+        return out
+
+    def PredictVisibilitiesMaskedDevice(self, n_rows, n_chan, d_uvw, d_freq, d_mask, d_vis):
+        check(lib().wgpu_gridder_predict_visibilities_masked_device(
+            self._h, n_rows, n_chan, d_uvw, d_freq, d_mask, d_vis))
+
     def PredictVisibilitiesDevice(self, n_rows, n_chan, d_uvw, d_freq, d_vis):
         check(lib().wgpu_gridder_predict_visibilities_device(self._h, n_rows, n_chan, d_uvw,
                                                              d_freq, d_vis))
@@ -136,12 +151,18 @@ class WGriddingGridder_Simple:
         return p
 
     def last_timings(self):
+        """{stage: (milliseconds, launches)} of the last call."""
         ms = (C.c_double * 64)()
+        cnt = (C.c_int * 64)()
         names = C.create_string_buffer(4096)
         n = C.c_int()
-        check(lib().wgpu_gridder_last_timings(self._h, ms, 64, names, 4096, C.byref(n)))
+        check(lib().wgpu_gridder_last_timings(self._h, ms, cnt, 64, names, 4096, C.byref(n)))
         keys = names.value.decode().split(";") if n.value else []
-        return {k: ms[i] for i, k in enumerate(keys)}
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(keys)}
+
+    def pin_plan(self, plan):
+        """Use `plan` (a Plan from last_plan()) for following calls; None unpins."""
+        check(lib().wgpu_gridder_pin_plan(self._h, None if plan is None else C.byref(plan)))
 
     def stream(self):
         return lib().wgpu_gridder_stream(self._h)
