@@ -2,6 +2,7 @@
 // pipelines (host orchestration of the CUDA kernels on one stream).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -206,6 +207,11 @@ wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis)
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
     r.memory_budget_bytes = std::min(24e9, 0.4 * (double)(free_b + g->arena.total()));
   }
+  // WGPU_PLANE_BUDGET_GB caps the plane-batch memory (profiling small cases)
+  if (const char *env = std::getenv("WGPU_PLANE_BUDGET_GB")) {
+    const double gb = std::atof(env);
+    if (gb > 0) r.memory_budget_bytes = gb * 1e9;
+  }
   return make_plan(r);
 }
 
@@ -258,7 +264,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
     g->timer.mark("grid");
-    launch_grid(dp, b.records, b.offsets, (int)p0, nb, planes, s);
+    launch_grid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, s);
     g->timer.mark("fft_rows");
     launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, s);
     g->timer.mark("fft_cols_a");
@@ -330,7 +336,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     g->timer.mark("fft_rows");
     launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, s);
     g->timer.mark("degrid");
-    launch_degrid(dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
+    launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
   }
   g->timer.mark("finalize");
   launch_unpermute_predict(b.records, b.perm, vacc, b.n_out, (float2 *)d_vis, s);

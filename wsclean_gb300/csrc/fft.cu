@@ -29,8 +29,8 @@
 
 namespace wgpu {
 
-constexpr int kFftMaxRow = 16384;
-constexpr int kMaxElemsPerThread = 32;
+constexpr int kFftMaxRow = 12288;  // two row buffers fit in 227 KB of shared memory
+constexpr int kMaxElemsPerThread = 16;  // complex values a thread holds per stage
 constexpr int kMaxStages = 20;
 
 int fft_row_max_length() { return kFftMaxRow; }
@@ -39,6 +39,7 @@ struct FftDesc {
   int L;
   int n_stages;
   int radix[kMaxStages];
+  unsigned magic[kMaxStages];  // ceil(2^32 / p) for the stage's p
 };
 
 struct FftTables {
@@ -81,6 +82,11 @@ static FftDesc make_desc(int L) {
   while (m % 5 == 0) { d.radix[d.n_stages++] = 5; m /= 5; }
   if (m != 1 || d.n_stages > kMaxStages)
     throw Error(WGPU_ERR_INVALID, "FFT length " + std::to_string(L) + " is not 2^a 3^b 5^c");
+  unsigned long long p = 1;
+  for (int st = 0; st < d.n_stages; ++st) {
+    d.magic[st] = (unsigned)(((1ull << 32) + p - 1) / p);
+    p *= (unsigned long long)d.radix[st];
+  }
   return d;
 }
 
@@ -166,65 +172,70 @@ __device__ __forceinline__ void dft<5>(float2 *x, float s) {
   x[3] = csub(r2, i2);
 }
 
-// One Stockham stage over nb interleaved transforms of length L stored as
-// s[k * ks + b * bs].  p = product of the radices of the earlier stages.
-template <int R>
-__device__ __forceinline__ void stage(float2 *s, int L, int nb, int ks, int bs,
-                                      int p, float sign, const float2 *__restrict__ tw) {
-  constexpr int NB = (kMaxElemsPerThread + R - 1) / R;
-  const int nbut = (L / R) * nb;
+// Layout of the transforms a CTA holds in shared memory.
+//   kRow:   one transform, element k at s[k].
+//   kPanel: 32 interleaved transforms (one per column of a panel), element k
+//           of transform b at s[k * 32 + b].
+enum Layout { kRow = 0, kPanelLayout = 1 };
+
+// One Stockham radix-R stage, out of place (src -> dst).  p = product of the
+// radices of the earlier stages; p_magic = ceil(2^32 / p) gives i / p exactly
+// for i < 2^14 (transform lengths here are at most 12288).
+template <int R, Layout LAY>
+__device__ __forceinline__ void stage(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                      int L, int p, unsigned p_magic, float sign,
+                                      const float2 *__restrict__ tw) {
+  constexpr int NB = LAY == kPanelLayout ? 32 : 1;
   const int LR = L / R;
+  const int nbut = LR * NB;
   const int tw_step = L / (p * R);
-  float2 v[NB][R];
+  for (int u = threadIdx.x; u < nbut; u += blockDim.x) {
+    const int b = LAY == kPanelLayout ? (u & 31) : 0;
+    const int i = LAY == kPanelLayout ? (u >> 5) : u;
+    const int k = p == 1 ? 0 : i - p * (int)__umulhi((unsigned)i, p_magic);
+    float2 v[R];
 #pragma unroll
-  for (int c = 0; c < NB; ++c) {
-    const int u = threadIdx.x + c * blockDim.x;
-    if (u < nbut) {
-      const int b = u % nb, i = u / nb;
-      const int k = i % p;
+    for (int t = 0; t < R; ++t) v[t] = src[(i + t * LR) * NB + b];
+    if (k > 0) {
 #pragma unroll
-      for (int t = 0; t < R; ++t) v[c][t] = s[(i + t * LR) * ks + b * bs];
-      if (k > 0) {
-#pragma unroll
-        for (int t = 1; t < R; ++t) {
-          float2 w = __ldg(tw + t * k * tw_step);
-          w.y *= -sign;  // table holds exp(-2 pi i j / L); sign +1 conjugates
-          v[c][t] = cmul(v[c][t], w);
-        }
+      for (int t = 1; t < R; ++t) {
+        float2 w = __ldg(tw + t * k * tw_step);
+        w.y *= -sign;  // table holds exp(-2 pi i j / L); sign +1 conjugates
+        v[t] = cmul(v[t], w);
       }
-      dft<R>(v[c], sign);
     }
-  }
-  __syncthreads();
+    dft<R>(v, sign);
+    const int j = (i - k) * R + k;
 #pragma unroll
-  for (int c = 0; c < NB; ++c) {
-    const int u = threadIdx.x + c * blockDim.x;
-    if (u < nbut) {
-      const int b = u % nb, i = u / nb;
-      const int k = i % p;
-      const int j = (i - k) * R + k;
-#pragma unroll
-      for (int q = 0; q < R; ++q) s[(j + q * p) * ks + b * bs] = v[c][q];
-    }
+    for (int q = 0; q < R; ++q) dst[(j + q * p) * NB + b] = v[q];
   }
   __syncthreads();
 }
 
-// Full transform; sign -1 forward, +1 backward (unnormalised).
-__device__ void fft_smem(float2 *s, const FftDesc &d, int nb, int ks, int bs,
-                         float sign, const float2 *__restrict__ tw) {
+// Full transform of the data in buf[0]; buf[1] is scratch of the same size.
+// sign -1 forward, +1 backward (unnormalised).  Returns the buffer holding the
+// result.  The caller has synchronised after filling buf[0].
+template <Layout LAY>
+__device__ __forceinline__ float2 *fft_smem(float2 *buf0, float2 *buf1, const FftDesc &d,
+                                            float sign, const float2 *__restrict__ tw) {
+  float2 *src = buf0, *dst = buf1;
   int p = 1;
   for (int st = 0; st < d.n_stages; ++st) {
     const int R = d.radix[st];
+    const unsigned m = d.magic[st];
     switch (R) {
-      case 8: stage<8>(s, d.L, nb, ks, bs, p, sign, tw); break;
-      case 4: stage<4>(s, d.L, nb, ks, bs, p, sign, tw); break;
-      case 2: stage<2>(s, d.L, nb, ks, bs, p, sign, tw); break;
-      case 3: stage<3>(s, d.L, nb, ks, bs, p, sign, tw); break;
-      default: stage<5>(s, d.L, nb, ks, bs, p, sign, tw); break;
+      case 8: stage<8, LAY>(src, dst, d.L, p, m, sign, tw); break;
+      case 4: stage<4, LAY>(src, dst, d.L, p, m, sign, tw); break;
+      case 2: stage<2, LAY>(src, dst, d.L, p, m, sign, tw); break;
+      case 3: stage<3, LAY>(src, dst, d.L, p, m, sign, tw); break;
+      default: stage<5, LAY>(src, dst, d.L, p, m, sign, tw); break;
     }
     p *= R;
+    float2 *t = src;
+    src = dst;
+    dst = t;
   }
+  return src;
 }
 
 __device__ __forceinline__ int wrap(int a, int n) {
@@ -233,7 +244,7 @@ __device__ __forceinline__ int wrap(int a, int n) {
 }
 
 // ---------------------------------------------------------------- rows ----
-__global__ void fft_rows_forward_crop_kernel(FftDesc d, const float2 *__restrict__ planes,
+__global__ void __launch_bounds__(1024) fft_rows_forward_crop_kernel(FftDesc d, const float2 *__restrict__ planes,
                                              float2 *__restrict__ R, int rstride,
                                              int nv, int width,
                                              const float2 *__restrict__ tw) {
@@ -244,16 +255,16 @@ __global__ void fft_rows_forward_crop_kernel(FftDesc d, const float2 *__restrict
   for (int k = threadIdx.x; k < L / 2; k += blockDim.x)
     reinterpret_cast<float4 *>(s)[k] = __ldg(reinterpret_cast<const float4 *>(src) + k);
   __syncthreads();
-  fft_smem(s, d, 1, 1, 0, -1.0f, tw);
+  const float2 *res = fft_smem<kRow>(s, s + L, d, -1.0f, tw);
   float2 *dst = R + row * (size_t)rstride;
   for (int x = threadIdx.x; x < rstride; x += blockDim.x) {
     float2 v = make_float2(0.f, 0.f);
-    if (x < width) v = s[wrap(width / 2 - x, L)];
+    if (x < width) v = res[wrap(width / 2 - x, L)];
     dst[x] = v;
   }
 }
 
-__global__ void fft_rows_backward_pad_kernel(FftDesc d, const float2 *__restrict__ R,
+__global__ void __launch_bounds__(1024) fft_rows_backward_pad_kernel(FftDesc d, const float2 *__restrict__ R,
                                              int rstride, float2 *__restrict__ planes,
                                              int nv, int width,
                                              const float2 *__restrict__ tw) {
@@ -265,14 +276,14 @@ __global__ void fft_rows_backward_pad_kernel(FftDesc d, const float2 *__restrict
   const float2 *src = R + row * (size_t)rstride;
   for (int x = threadIdx.x; x < width; x += blockDim.x) s[wrap(width / 2 - x, L)] = src[x];
   __syncthreads();
-  fft_smem(s, d, 1, 1, 0, +1.0f, tw);
+  const float2 *res = fft_smem<kRow>(s, s + L, d, +1.0f, tw);
   float2 *dst = planes + row * (size_t)L;
   for (int k = threadIdx.x; k < L / 2; k += blockDim.x)
-    reinterpret_cast<float4 *>(dst)[k] = reinterpret_cast<const float4 *>(s)[k];
+    reinterpret_cast<float4 *>(dst)[k] = reinterpret_cast<const float4 *>(res)[k];
 }
 
 // ------------------------------------------------------------- columns ----
-constexpr int kColThreads = 256;
+constexpr int kColThreads = 512;
 constexpr int kPanel = 32;  // columns per panel
 
 // Pass A (forward) / A' (backward): strided length-n1 transforms.
@@ -289,21 +300,13 @@ __global__ void __launch_bounds__(kColThreads)
     s[e] = base[(size_t)(r2 + n2 * r1) * rstride + c];
   }
   __syncthreads();
-  if (sign > 0) {
-    // backward: this pass runs last; no twiddle here (applied in pass B')
-    fft_smem(s, d1, kPanel, kPanel, 1, sign, tw1);
-  } else {
-    fft_smem(s, d1, kPanel, kPanel, 1, sign, tw1);
-    for (int e = threadIdx.x; e < n1 * kPanel; e += blockDim.x) {
-      const int k1 = e / kPanel;
-      const int j = (int)(((long long)r2 * k1) % nv);
-      s[e] = cmul(s[e], __ldg(twN + j));
-    }
-    __syncthreads();
-  }
+  // backward: this pass runs last and the twiddle was applied in pass B'
+  const float2 *res = fft_smem<kPanelLayout>(s, s + n1 * kPanel, d1, sign, tw1);
   for (int e = threadIdx.x; e < n1 * kPanel; e += blockDim.x) {
     const int k1 = e / kPanel, c = e % kPanel;
-    base[(size_t)(r2 + n2 * k1) * rstride + c] = s[e];
+    float2 v = res[e];
+    if (sign < 0) v = cmul(v, __ldg(twN + (int)(((long long)r2 * k1) % nv)));
+    base[(size_t)(r2 + n2 * k1) * rstride + c] = v;
   }
 }
 
@@ -345,7 +348,7 @@ __global__ void __launch_bounds__(kColThreads)
       s[e] = base[(size_t)r2 * rstride + c];
     }
     __syncthreads();
-    fft_smem(s, d2, kPanel, kPanel, 1, -1.0f, tw2);
+    const float2 *res = fft_smem<kPanelLayout>(s, s + n2 * kPanel, d2, -1.0f, tw2);
     const double wq = p.w0 + (double)(p_begin + b) * p.dw;
 #pragma unroll
     for (int c = 0; c < NE; ++c) {
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(kColThreads)
         const int x = cg * kPanel + col;
         const int y = image_row_of(k1 + n1 * k2, nv, p.height);
         if (x < p.width && y >= 0) {
-          const float2 v = s[e];
+          const float2 v = res[e];
           float sn, cs;
           screen(wq, __ldg(nu_w + (size_t)y * p.width + x), &sn, &cs);
           // Re(v exp(-2 pi i t)) = v.re cos + v.im sin
@@ -419,11 +422,11 @@ __global__ void __launch_bounds__(kColThreads)
       s[e] = v;
     }
     __syncthreads();
-    fft_smem(s, d2, kPanel, kPanel, 1, +1.0f, tw2);
+    const float2 *res = fft_smem<kPanelLayout>(s, s + n2 * kPanel, d2, +1.0f, tw2);
     float2 *base = R + (size_t)b * nv * rstride + (size_t)n2 * k1 * rstride + cg * kPanel;
     for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
       const int r2 = e / kPanel, c = e % kPanel;
-      float2 v = s[e];
+      float2 v = res[e];
       if (n1 > 1) {
         float2 w = __ldg(twN + (int)(((long long)r2 * k1) % nv));
         w.y = -w.y;  // exp(+2 pi i r2 k1 / nv)
@@ -435,11 +438,10 @@ __global__ void __launch_bounds__(kColThreads)
   }
 }
 
+// Threads for a row transform of length L (about L/8 butterflies per stage).
 int row_threads(int L) {
-  int t = 64;
-  while (t * kMaxElemsPerThread < L) t *= 2;
-  if (t < 128 && L >= 2048) t = 128;
-  return t;
+  int t = (L / 8 + 31) / 32 * 32;
+  return t < 64 ? 64 : (t > 1024 ? 1024 : t);
 }
 
 void set_smem(const void *fn, size_t bytes) {
@@ -453,7 +455,7 @@ void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
                                   int n_batch, cudaStream_t s) {
   const FftDesc d = make_desc(p.nu);
   const float2 *tw = fft_twiddles(t, p.nu);
-  const size_t smem = sizeof(float2) * p.nu;
+  const size_t smem = 2 * sizeof(float2) * p.nu;
   set_smem((const void *)fft_rows_forward_crop_kernel, smem);
   fft_rows_forward_crop_kernel<<<(unsigned)((size_t)n_batch * p.nv), row_threads(p.nu), smem, s>>>(
       d, planes, R, rstride, p.nv, p.width, tw);
@@ -465,7 +467,7 @@ void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
                                   int n_batch, cudaStream_t s) {
   const FftDesc d = make_desc(p.nu);
   const float2 *tw = fft_twiddles(t, p.nu);
-  const size_t smem = sizeof(float2) * p.nu;
+  const size_t smem = 2 * sizeof(float2) * p.nu;
   set_smem((const void *)fft_rows_backward_pad_kernel, smem);
   fft_rows_backward_pad_kernel<<<(unsigned)((size_t)n_batch * p.nv), row_threads(p.nu), smem, s>>>(
       d, R, rstride, planes, p.nv, p.width, tw);
@@ -477,7 +479,7 @@ void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R
   if (n1 <= 1) return;
   const int ncg = rstride / kPanel;
   const FftDesc d1 = make_desc(n1);
-  const size_t smem = sizeof(float2) * n1 * kPanel;
+  const size_t smem = 2 * sizeof(float2) * n1 * kPanel;
   set_smem((const void *)fft_cols_pass_a_kernel, smem);
   dim3 grid(ncg, n2, n_batch);
   fft_cols_pass_a_kernel<<<grid, kColThreads, smem, s>>>(
@@ -492,7 +494,7 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
                                           cudaStream_t s) {
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
-  const size_t smem = sizeof(float2) * n2 * kPanel;
+  const size_t smem = 2 * sizeof(float2) * n2 * kPanel;
   set_smem((const void *)fft_cols_forward_accumulate_kernel, smem);
   dim3 grid(ncg, n1);
   fft_cols_forward_accumulate_kernel<<<grid, kColThreads, smem, s>>>(
@@ -507,7 +509,7 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        cudaStream_t s) {
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
-  const size_t smem = sizeof(float2) * n2 * kPanel;
+  const size_t smem = 2 * sizeof(float2) * n2 * kPanel;
   set_smem((const void *)fft_cols_backward_screen_kernel, smem);
   dim3 grid(ncg, n1);
   fft_cols_backward_screen_kernel<<<grid, kColThreads, smem, s>>>(

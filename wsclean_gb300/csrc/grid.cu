@@ -1,18 +1,24 @@
 // K2 gridding and K3 degridding over (uv tile, w-plane group) work units.
 //
-// Gridding: one CTA owns a T x T tile of G consecutive w planes.  It reads the
-// visibilities bucketed in its own tile and in the three neighbouring tiles
-// whose footprints can spill into it (left, below, below-left; the footprint
-// corner decides the bucket), restricted by key range to the first planes that
-// reach the group.  A chunk of records at a time is spread into a shared-
-// memory copy of the tile with shared-memory atomics; after each chunk the
-// partial tile is folded into per-thread Kahan-compensated accumulators and
-// cleared, so long buckets do not lose FP32 precision.  Each tile cell is
-// finally written once to HBM (no global atomics, no memset of the planes).
+// Work unit = (uv tile T x T, group of G consecutive w planes).  A gridding
+// unit reads the visibilities bucketed in its own tile and in the three
+// neighbouring tiles whose footprints can spill into it (left, below,
+// below-left; the footprint corner decides the bucket), restricted by key
+// range to the first planes that reach the group.  Units are split into work
+// items of at most kItemVis visibility reads, and one persistent launch works
+// through the items of a plane batch from a device counter, so that the
+// crowded tiles of a dense uv core are shared by many CTAs.
 //
-// Degridding: one CTA loads its tile plus a (W-1)-cell halo of G planes into
-// shared memory and gathers, for every visibility of its own bucket, the
-// W x W x (planes in the group) weighted sum; results are added to the
+// Gridding item: records are staged kChunk at a time in shared memory and
+// spread into a shared copy of the tile with shared-memory atomics; every
+// kFoldEvery rounds the partial tile is folded into per-thread
+// Kahan-compensated accumulators and cleared, so long lists keep FP32
+// precision.  A unit made of one item writes each cell once to HBM; the items
+// of a split unit add into cells that a planning pass zeroed.
+//
+// Degridding item: loads its tile plus a (W-1)-cell halo of G planes into
+// shared memory and gathers, for each visibility of its slice of the own
+// bucket, the W x W x (planes in the group) weighted sum, added to the
 // per-visibility accumulator.
 #include "wgpu_internal.h"
 
@@ -21,9 +27,9 @@ namespace wgpu {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kChunk = 64;  // records staged per round
-constexpr int kCells = 4096;  // G * T * T cells per gridding CTA
-constexpr int kCellsPerThread = kCells / kThreads;
+constexpr int kChunk = 64;       // records staged in shared memory per round
+constexpr int kFoldEvery = 4;    // rounds between two Kahan folds
+constexpr uint32_t kItemVis = 2048;  // visibility reads per work item
 
 __device__ __forceinline__ float es_eval(float beta, float z) {
   const float t = 1.0f - z * z;
@@ -45,251 +51,429 @@ __device__ __forceinline__ VisRecord load_record(const VisRecord *r) {
   return o;
 }
 
+// The key ranges of the visibilities that can reach unit (tile, q0..q1-1):
+// own tile and the three neighbours (dtu, dtv in {0, 1}).
+__device__ __forceinline__ void unit_range(const DevPlan &p, const uint32_t *off, int tile,
+                                           int q0, int q1, int nb, uint32_t *s0,
+                                           uint32_t *s1) {
+  const int tu = tile % p.ntu, tv = tile / p.ntu;
+  const int dtu = nb & 1, dtv = nb >> 1;
+  const int stu = (tu - dtu + p.ntu) % p.ntu;
+  const int stv = (tv - dtv + p.ntv) % p.ntv;
+  const int plo = max(q0 - p.support + 1, 0);
+  const int phi = min(q1 - 1, p.n_planes - 1);
+  const uint32_t key0 = (uint32_t)(stv * p.ntu + stu) * (uint32_t)p.n_planes;
+  *s0 = off[key0 + plo];
+  *s1 = off[key0 + phi + 1];
+}
+
+// Planning pass: one warp per unit counts the unit's visibility reads and its
+// work items; the cells of split units are zeroed here.
+template <int T, int G>
+__global__ void __launch_bounds__(kThreads)
+    grid_plan_kernel(DevPlan p, const uint32_t *__restrict__ off, int p_begin, int n_batch,
+                     int n_units, int degrid, uint32_t *__restrict__ items,
+                     float2 *__restrict__ planes) {
+  const int unit = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (unit >= n_units) return;
+  const int n_tiles = p.ntu * p.ntv;
+  const int tile = unit % n_tiles, group = unit / n_tiles;
+  const int q0 = p_begin + group * G;
+  const int q1 = min(q0 + G, p_begin + n_batch);
+  uint32_t cnt = 0;
+  if (lane < (degrid ? 1 : 4)) {
+    uint32_t a, b;
+    unit_range(p, off, tile, q0, q1, lane, &a, &b);
+    cnt = b - a;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  const uint32_t n_items = cnt <= kItemVis ? 1u : (cnt + kItemVis - 1) / kItemVis;
+  if (degrid && cnt == 0) {
+    if (lane == 0) items[unit] = 0;
+    return;
+  }
+  if (lane == 0) items[unit] = n_items;
+  if (!degrid && n_items > 1) {
+    const int tu = tile % p.ntu, tv = tile / p.ntu;
+    const size_t plane_elems = (size_t)p.nu * p.nv;
+    for (int c = lane; c < (q1 - q0) * T * T; c += 32) {
+      const int pq = c / (T * T), rem = c - pq * T * T;
+      const int row = rem / T, col = rem - row * T;
+      planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
+             tu * T + col] = make_float2(0.f, 0.f);
+    }
+  }
+}
+
+// Item -> unit: last unit whose first item is <= item.
+__device__ __forceinline__ int find_unit(const uint32_t *item_off, int n_units, uint32_t item) {
+  int lo = 0, hi = n_units;  // item_off[lo] <= item < item_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (item_off[mid] <= item) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 template <int T, int G>
 __global__ void __launch_bounds__(kThreads)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
-                const uint32_t *__restrict__ off, int p_begin, int n_batch,
+                const uint32_t *__restrict__ off, int p_begin, int n_batch, int n_units,
+                const uint32_t *__restrict__ item_off, uint32_t *__restrict__ counter,
                 float2 *__restrict__ planes) {
-  static_assert(G * T * T == kCells, "cells per CTA");
+  constexpr int kCellsPerThread = G * T * T / kThreads;  // cells a thread folds
+  static_assert(kCellsPerThread * kThreads == G * T * T, "cells per work item");
   constexpr int TS = T + 1;  // padded row stride (float2 units)
   __shared__ float2 buf[G * T * TS];
   __shared__ float kval[kChunk][3][kMaxSupport];
   __shared__ float2 cvis[kChunk];
-  __shared__ int cpos[kChunk][3];  // iu_rel, iv_rel, ip
+  __shared__ int cpos[kChunk][3];     // iu_rel, iv_rel, ip
   __shared__ float cfrac[kChunk][3];  // fu, fv, fw
+  __shared__ uint32_t sh_item;
+  __shared__ int sh_unit;
+  __shared__ uint32_t sh_s0[4], sh_s1[4];
 
   const int W = p.support;
   const float inv_half = 2.0f / (float)W;
-  const int tile = blockIdx.x;
-  const int tu = tile % p.ntu, tv = tile / p.ntu;
-  const int q0 = p_begin + blockIdx.y * G;
-  const int q1 = min(q0 + G, p_begin + n_batch);
+  const int n_tiles = p.ntu * p.ntv;
+  const uint32_t total = item_off[n_units];
+  const size_t plane_elems = (size_t)p.nu * p.nv;
 
   for (int c = threadIdx.x; c < G * T * TS; c += kThreads) buf[c] = make_float2(0.f, 0.f);
-  float2 sum[kCellsPerThread], comp[kCellsPerThread];
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    sum[k] = make_float2(0.f, 0.f);
-    comp[k] = make_float2(0.f, 0.f);
-  }
-  __syncthreads();
 
-  const int plo = max(q0 - W + 1, 0);
-  const int phi = min(q1 - 1, p.n_planes - 1);
-  for (int nb = 0; nb < 4; ++nb) {
-    const int dtu = nb & 1, dtv = nb >> 1;
-    const int stu = (tu - dtu + p.ntu) % p.ntu;
-    const int stv = (tv - dtv + p.ntv) % p.ntv;
-    const uint32_t key0 = (uint32_t)(stv * p.ntu + stu) * (uint32_t)p.n_planes;
-    const uint32_t s0 = off[key0 + plo];
-    const uint32_t s1 = off[key0 + phi + 1];
-    for (uint32_t sb = s0; sb < s1; sb += kChunk) {
-      const int m_count = (int)min((uint32_t)kChunk, s1 - sb);
-      if (threadIdx.x < m_count) {
-        const VisRecord r = load_record(rec + sb + threadIdx.x);
-        int iu_rel = r.iu - tu * T;
-        if (iu_rel >= T) iu_rel -= p.nu;
-        int iv_rel = r.iv - tv * T;
-        if (iv_rel >= T) iv_rel -= p.nv;
-        cvis[threadIdx.x] = make_float2(r.re, r.im);
-        cpos[threadIdx.x][0] = iu_rel;
-        cpos[threadIdx.x][1] = iv_rel;
-        cpos[threadIdx.x][2] = r.ip;
-        cfrac[threadIdx.x][0] = r.fu;
-        cfrac[threadIdx.x][1] = r.fv;
-        cfrac[threadIdx.x][2] = r.fw;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t it = atomicAdd(counter, 1u);
+      sh_item = it;
+      if (it < total) {
+        const int u = find_unit(item_off, n_units, it);
+        sh_unit = u;
+        const int tile = u % n_tiles, group = u / n_tiles;
+        const int q0 = p_begin + group * G;
+        const int q1 = min(q0 + G, p_begin + n_batch);
+        for (int nb = 0; nb < 4; ++nb) unit_range(p, off, tile, q0, q1, nb, &sh_s0[nb], &sh_s1[nb]);
       }
-      __syncthreads();
-      // kernel values: (m, dim, j) -> phi((f + j) / half)
-      for (int idx = threadIdx.x; idx < m_count * 3 * kMaxSupport; idx += kThreads) {
-        const int j = idx % kMaxSupport;
-        const int d = (idx / kMaxSupport) % 3;
-        const int m = idx / (3 * kMaxSupport);
-        if (j >= W) continue;
-        float v;
-        if (d == 2 && p.n_planes == 1)
-          v = (j == 0) ? 1.0f : 0.0f;
-        else
-          v = es_eval(p.beta, (cfrac[m][d] + (float)j) * inv_half);
-        kval[m][d][j] = v;
-      }
-      __syncthreads();
-      // spread: units (m, j) = one footprint row of one visibility
-      for (int u = threadIdx.x; u < m_count * W; u += kThreads) {
-        const int m = u / W, j = u - m * W;
-        const int row = cpos[m][1] + j;
-        if (row < 0 || row >= T) continue;
-        const int ip = cpos[m][2];
-        const int pa = max(ip, q0), pb = min(ip + W - 1, q1 - 1);
-        if (pa > pb) continue;
-        const int iu_rel = cpos[m][0];
-        const int ia = max(0, -iu_rel), ib = min(W - 1, T - 1 - iu_rel);
-        const float ky = kval[m][1][j];
-        const float2 v = cvis[m];
-        for (int q = pa; q <= pb; ++q) {
-          const float wy = ky * kval[m][2][q - ip];
-          float2 *brow = buf + ((q - q0) * T + row) * TS + iu_rel;
-          for (int i = ia; i <= ib; ++i) {
-            const float wt = wy * kval[m][0][i];
-            atomicAdd(&brow[i].x, wt * v.x);
-            atomicAdd(&brow[i].y, wt * v.y);
+    }
+    __syncthreads();
+    const uint32_t item = sh_item;
+    if (item >= total) break;
+    const int unit = sh_unit;
+    const int tile = unit % n_tiles, group = unit / n_tiles;
+    const int tu = tile % p.ntu, tv = tile / p.ntu;
+    const int q0 = p_begin + group * G;
+    const int q1 = min(q0 + G, p_begin + n_batch);
+    const uint32_t first = item_off[unit];
+    const uint32_t n_items = item_off[unit + 1] - first;
+    const uint32_t lo = (item - first) * kItemVis, hi = lo + kItemVis;
+
+    float2 sum[kCellsPerThread], comp[kCellsPerThread];
+#pragma unroll
+    for (int k = 0; k < kCellsPerThread; ++k) {
+      sum[k] = make_float2(0.f, 0.f);
+      comp[k] = make_float2(0.f, 0.f);
+    }
+    int rounds = 0;
+    uint32_t base = 0;  // position of range nb in the unit's concatenated list
+    for (int nb = 0; nb < 4; ++nb) {
+      const uint32_t s0 = sh_s0[nb], s1 = sh_s1[nb];
+      const uint32_t len = s1 - s0;
+      const uint32_t a = max(lo, base), b = min(hi, base + len);
+      base += len;
+      if (a >= b) continue;
+      for (uint32_t sb = s0 + (a - (base - len)); sb < s0 + (b - (base - len)); sb += kChunk) {
+        const int m_count = (int)min((uint32_t)kChunk, s0 + (b - (base - len)) - sb);
+        if (threadIdx.x < m_count) {
+          const VisRecord r = load_record(rec + sb + threadIdx.x);
+          int iu_rel = r.iu - tu * T;
+          if (iu_rel >= T) iu_rel -= p.nu;
+          int iv_rel = r.iv - tv * T;
+          if (iv_rel >= T) iv_rel -= p.nv;
+          cvis[threadIdx.x] = make_float2(r.re, r.im);
+          cpos[threadIdx.x][0] = iu_rel;
+          cpos[threadIdx.x][1] = iv_rel;
+          cpos[threadIdx.x][2] = r.ip;
+          cfrac[threadIdx.x][0] = r.fu;
+          cfrac[threadIdx.x][1] = r.fv;
+          cfrac[threadIdx.x][2] = r.fw;
+        }
+        __syncthreads();
+        // kernel values: (m, dim, j) -> phi((f + j) / half)
+        for (int idx = threadIdx.x; idx < m_count * 3 * kMaxSupport; idx += kThreads) {
+          const int j = idx % kMaxSupport;
+          const int d = (idx / kMaxSupport) % 3;
+          const int m = idx / (3 * kMaxSupport);
+          if (j >= W) continue;
+          float v;
+          if (d == 2 && p.n_planes == 1)
+            v = (j == 0) ? 1.0f : 0.0f;
+          else
+            v = es_eval(p.beta, (cfrac[m][d] + (float)j) * inv_half);
+          kval[m][d][j] = v;
+        }
+        __syncthreads();
+        // spread: units (m, j) = one footprint row of one visibility
+        for (int u = threadIdx.x; u < m_count * W; u += kThreads) {
+          const int m = u / W, j = u - m * W;
+          const int row = cpos[m][1] + j;
+          if (row < 0 || row >= T) continue;
+          const int ip = cpos[m][2];
+          const int pa = max(ip, q0), pb = min(ip + W - 1, q1 - 1);
+          if (pa > pb) continue;
+          const int iu_rel = cpos[m][0];
+          const int ia = max(0, -iu_rel), ib = min(W - 1, T - 1 - iu_rel);
+          const float ky = kval[m][1][j];
+          const float2 v = cvis[m];
+          for (int q = pa; q <= pb; ++q) {
+            const float wy = ky * kval[m][2][q - ip];
+            float2 *brow = buf + ((q - q0) * T + row) * TS + iu_rel;
+            for (int i = ia; i <= ib; ++i) {
+              const float wt = wy * kval[m][0][i];
+              atomicAdd(&brow[i].x, wt * v.x);
+              atomicAdd(&brow[i].y, wt * v.y);
+            }
           }
         }
-      }
-      __syncthreads();
-      // fold the chunk into the compensated accumulators
+        __syncthreads();
+        if (++rounds == kFoldEvery) {
+          rounds = 0;
 #pragma unroll
-      for (int k = 0; k < kCellsPerThread; ++k) {
-        const int c = threadIdx.x + k * kThreads;
-        const int pq = c / (T * T), rem = c - pq * T * T;
-        const int row = rem / T, col = rem - row * T;
-        float2 *cell = buf + (pq * T + row) * TS + col;
-        const float2 x = *cell;
-        *cell = make_float2(0.f, 0.f);
-        // Kahan (Neumaier form) per component
-        float y = x.x - comp[k].x;
-        float t = sum[k].x + y;
-        comp[k].x = (t - sum[k].x) - y;
-        sum[k].x = t;
-        y = x.y - comp[k].y;
-        t = sum[k].y + y;
-        comp[k].y = (t - sum[k].y) - y;
-        sum[k].y = t;
+          for (int k = 0; k < kCellsPerThread; ++k) {
+            const int c = threadIdx.x + k * kThreads;
+            const int pq = c / (T * T), rem = c - pq * T * T;
+            const int row = rem / T, col = rem - row * T;
+            float2 *cell = buf + (pq * T + row) * TS + col;
+            const float2 x = *cell;
+            *cell = make_float2(0.f, 0.f);
+            float y = x.x - comp[k].x;
+            float t = sum[k].x + y;
+            comp[k].x = (t - sum[k].x) - y;
+            sum[k].x = t;
+            y = x.y - comp[k].y;
+            t = sum[k].y + y;
+            comp[k].y = (t - sum[k].y) - y;
+            sum[k].y = t;
+          }
+          __syncthreads();
+        }
       }
-      __syncthreads();
     }
-  }
-  // write the tile of each plane in the group
-  const size_t plane_elems = (size_t)p.nu * p.nv;
+    // final fold and write
 #pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int c = threadIdx.x + k * kThreads;
-    const int pq = c / (T * T), rem = c - pq * T * T;
-    const int row = rem / T, col = rem - row * T;
-    const int q = q0 + pq;
-    if (q < q1) {
-      planes[(size_t)(q - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
-             tu * T + col] = sum[k];
+    for (int k = 0; k < kCellsPerThread; ++k) {
+      const int c = threadIdx.x + k * kThreads;
+      const int pq = c / (T * T), rem = c - pq * T * T;
+      const int row = rem / T, col = rem - row * T;
+      float2 *cell = buf + (pq * T + row) * TS + col;
+      const float2 x = *cell;
+      *cell = make_float2(0.f, 0.f);
+      float y = x.x - comp[k].x;
+      float t = sum[k].x + y;
+      comp[k].x = (t - sum[k].x) - y;
+      sum[k].x = t;
+      y = x.y - comp[k].y;
+      t = sum[k].y + y;
+      comp[k].y = (t - sum[k].y) - y;
+      sum[k].y = t;
+      const int q = q0 + pq;
+      if (q < q1) {
+        float2 *dst = planes + (size_t)(q - p_begin) * plane_elems +
+                      (size_t)(tv * T + row) * p.nu + tu * T + col;
+        if (n_items == 1)
+          *dst = sum[k];
+        else
+          atomicAdd(dst, sum[k]);
+      }
     }
+    __syncthreads();
   }
 }
 
 template <int T, int G>
 __global__ void __launch_bounds__(kThreads)
     degrid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
-                  const uint32_t *__restrict__ off, int p_begin, int n_batch,
+                  const uint32_t *__restrict__ off, int p_begin, int n_batch, int n_units,
+                  const uint32_t *__restrict__ item_off, uint32_t *__restrict__ counter,
                   const float2 *__restrict__ planes, float2 *__restrict__ acc) {
   extern __shared__ float2 region[];  // [G][R][RS]
+  __shared__ uint32_t sh_item;
+  __shared__ int sh_unit;
   const int W = p.support;
   const int R = T + W - 1;
   const int RS = R + 1;
-  const float half = 0.5f * (float)W;
-  const float inv_half = 1.0f / half;
-  const int tile = blockIdx.x;
-  const int tu = tile % p.ntu, tv = tile / p.ntu;
-  const int q0 = p_begin + blockIdx.y * G;
-  const int q1 = min(q0 + G, p_begin + n_batch);
-  const int plo = max(q0 - W + 1, 0);
-  const int phi = min(q1 - 1, p.n_planes - 1);
-  const uint32_t key0 = (uint32_t)tile * (uint32_t)p.n_planes;
-  const uint32_t s0 = off[key0 + plo];
-  const uint32_t s1 = off[key0 + phi + 1];
-  if (s0 == s1) return;  // uniform across the CTA
-
+  const float inv_half = 2.0f / (float)W;
+  const int n_tiles = p.ntu * p.ntv;
+  const uint32_t total = item_off[n_units];
   const size_t plane_elems = (size_t)p.nu * p.nv;
-  const int nq = q1 - q0;
-  for (int idx = threadIdx.x; idx < nq * R * R; idx += blockDim.x) {
-    const int pq = idx / (R * R), rem = idx - pq * R * R;
-    const int r = rem / R, c = rem - r * R;
-    int gv = tv * T + r;
-    if (gv >= p.nv) gv -= p.nv;
-    int gu = tu * T + c;
-    if (gu >= p.nu) gu -= p.nu;
-    region[(pq * R + r) * RS + c] =
-        planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu];
-  }
-  __syncthreads();
 
-  for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-    const VisRecord r = load_record(rec + s);
-    float kx[kMaxSupport], ky[kMaxSupport];
-#pragma unroll
-    for (int j = 0; j < kMaxSupport; ++j) {
-      kx[j] = j < W ? es_eval(p.beta, (r.fu + (float)j) * inv_half) : 0.0f;
-      ky[j] = j < W ? es_eval(p.beta, (r.fv + (float)j) * inv_half) : 0.0f;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t it = atomicAdd(counter, 1u);
+      sh_item = it;
+      if (it < total) sh_unit = find_unit(item_off, n_units, it);
     }
-    const int iu_rel = r.iu - tu * T;
-    const int iv_rel = r.iv - tv * T;
-    const int pa = max(r.ip, q0), pb = min(r.ip + W - 1, q1 - 1);
-    float sr = 0.f, si = 0.f;
-    for (int q = pa; q <= pb; ++q) {
-      const float kw = p.n_planes == 1 ? 1.0f
-                                       : es_eval(p.beta, (r.fw + (float)(q - r.ip)) * inv_half);
-      const float2 *base = region + ((q - q0) * R + iv_rel) * RS + iu_rel;
-      float pr = 0.f, pi = 0.f;
-      for (int j = 0; j < W; ++j) {
-        const float2 *rowp = base + j * RS;
-        float rr = 0.f, ri = 0.f;
+    __syncthreads();
+    const uint32_t item = sh_item;
+    if (item >= total) break;
+    const int unit = sh_unit;
+    const int tile = unit % n_tiles, group = unit / n_tiles;
+    const int tu = tile % p.ntu, tv = tile / p.ntu;
+    const int q0 = p_begin + group * G;
+    const int q1 = min(q0 + G, p_begin + n_batch);
+    uint32_t s0, s1;
+    unit_range(p, off, tile, q0, q1, 0, &s0, &s1);
+    const uint32_t lo = s0 + (item - item_off[unit]) * kItemVis;
+    const uint32_t hi = min(s1, lo + kItemVis);
+
+    const int nq = q1 - q0;
+    for (int idx = threadIdx.x; idx < nq * R * R; idx += blockDim.x) {
+      const int pq = idx / (R * R), rem = idx - pq * R * R;
+      const int r = rem / R, c = rem - r * R;
+      int gv = tv * T + r;
+      if (gv >= p.nv) gv -= p.nv;
+      int gu = tu * T + c;
+      if (gu >= p.nu) gu -= p.nu;
+      region[(pq * R + r) * RS + c] =
+          planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu];
+    }
+    __syncthreads();
+
+    for (uint32_t s = lo + threadIdx.x; s < hi; s += blockDim.x) {
+      const VisRecord r = load_record(rec + s);
+      float kx[kMaxSupport], ky[kMaxSupport];
 #pragma unroll
-        for (int i = 0; i < kMaxSupport; ++i) {
-          if (i < W) {
-            const float2 g = rowp[i];
-            rr += kx[i] * g.x;
-            ri += kx[i] * g.y;
+      for (int j = 0; j < kMaxSupport; ++j) {
+        kx[j] = j < W ? es_eval(p.beta, (r.fu + (float)j) * inv_half) : 0.0f;
+        ky[j] = j < W ? es_eval(p.beta, (r.fv + (float)j) * inv_half) : 0.0f;
+      }
+      const int iu_rel = r.iu - tu * T;
+      const int iv_rel = r.iv - tv * T;
+      const int pa = max(r.ip, q0), pb = min(r.ip + W - 1, q1 - 1);
+      float sr = 0.f, si = 0.f;
+      for (int q = pa; q <= pb; ++q) {
+        const float kw = p.n_planes == 1 ? 1.0f
+                                         : es_eval(p.beta, (r.fw + (float)(q - r.ip)) * inv_half);
+        const float2 *bp = region + ((q - q0) * R + iv_rel) * RS + iu_rel;
+        float pr = 0.f, pi = 0.f;
+#pragma unroll
+        for (int j = 0; j < kMaxSupport; ++j) {
+          if (j < W) {
+            const float2 *rowp = bp + j * RS;
+            float rr = 0.f, ri = 0.f;
+#pragma unroll
+            for (int i = 0; i < kMaxSupport; ++i) {
+              if (i < W) {
+                const float2 g = rowp[i];
+                rr += kx[i] * g.x;
+                ri += kx[i] * g.y;
+              }
+            }
+            pr += ky[j] * rr;
+            pi += ky[j] * ri;
           }
         }
-        pr += ky[j] * rr;
-        pi += ky[j] * ri;
+        sr += kw * pr;
+        si += kw * pi;
       }
-      sr += kw * pr;
-      si += kw * pi;
+      atomicAdd(&acc[s], make_float2(sr, si));
     }
-    atomicAdd(&acc[s], make_float2(sr, si));
+    __syncthreads();
   }
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    WGPU_CUDA(cudaGetDevice(&dev));
+    WGPU_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+// Plans the work items of one batch: returns the scanned item offsets
+// (n_units + 1 entries) in `item_off`.
+template <int T, int G>
+void plan_items(DeviceArena &arena, const DevPlan &p, const uint32_t *off, int p_begin,
+                int n_batch, bool degrid, float2 *planes, uint32_t **item_off,
+                int *n_units, cudaStream_t s) {
+  const int n_groups = (n_batch + G - 1) / G;
+  *n_units = p.ntu * p.ntv * n_groups;
+  *item_off = (uint32_t *)arena.get(kSlotItems, sizeof(uint32_t) * (*n_units + 2));
+  const int warps_per_block = kThreads / 32;
+  const unsigned blocks = (unsigned)((*n_units + warps_per_block - 1) / warps_per_block);
+  grid_plan_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, off, p_begin, n_batch, *n_units,
+                                                     degrid ? 1 : 0, *item_off, planes);
+  check_launch("grid_plan_kernel");
+  WGPU_CUDA(cudaMemsetAsync(*item_off + *n_units, 0, sizeof(uint32_t), s));
+  exclusive_scan_u32(arena, *item_off, *n_units + 1, s);
+}
+
+template <int T, int G>
+void grid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                const uint32_t *off, int p_begin, int n_batch, float2 *planes,
+                cudaStream_t s) {
+  uint32_t *item_off;
+  int n_units;
+  plan_items<T, G>(arena, p, off, p_begin, n_batch, false, planes, &item_off, &n_units, s);
+  uint32_t *counter = (uint32_t *)arena.get(kSlotCounter, 64);
+  WGPU_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), s));
+  int per_sm = 0;
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G>, kThreads, 0));
+  const int blocks = sm_count() * std::max(per_sm, 1);
+  grid_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, rec, off, p_begin, n_batch, n_units,
+                                                item_off, counter, planes);
+  check_launch("grid_kernel");
+}
+
+template <int T, int G>
+void degrid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                  const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
+                  float2 *acc, cudaStream_t s) {
+  uint32_t *item_off;
+  int n_units;
+  plan_items<T, G>(arena, p, off, p_begin, n_batch, true, nullptr, &item_off, &n_units, s);
+  uint32_t *counter = (uint32_t *)arena.get(kSlotCounter, 64);
+  WGPU_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), s));
+  const int R = T + p.support - 1;
+  const size_t smem = sizeof(float2) * G * R * (R + 1);
+  WGPU_CUDA(cudaFuncSetAttribute(degrid_kernel<T, G>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G>,
+                                                          kThreads, smem));
+  const int blocks = sm_count() * std::max(per_sm, 1);
+  degrid_kernel<T, G><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, n_units,
+                                                     item_off, counter, planes, acc);
+  check_launch("degrid_kernel");
 }
 
 }  // namespace
 
 int grid_plane_group() { return 4; }
 
-void launch_grid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
-                 int p_begin, int n_batch, float2 *planes, cudaStream_t s) {
-  const int n_tiles = p.ntu * p.ntv;
-  if (p.tile == 32) {
-    constexpr int G = 4;
-    dim3 grid(n_tiles, (n_batch + G - 1) / G);
-    grid_kernel<32, G><<<grid, kThreads, 0, s>>>(p, rec, off, p_begin, n_batch, planes);
-  } else if (p.tile == 16) {
-    constexpr int G = 16;
-    dim3 grid(n_tiles, (n_batch + G - 1) / G);
-    grid_kernel<16, G><<<grid, kThreads, 0, s>>>(p, rec, off, p_begin, n_batch, planes);
-  } else {
+void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                 const uint32_t *off, int p_begin, int n_batch, float2 *planes,
+                 cudaStream_t s) {
+  if (p.tile == 32)
+    grid_batch<32, 4>(arena, p, rec, off, p_begin, n_batch, planes, s);
+  else if (p.tile == 16)
+    grid_batch<16, 8>(arena, p, rec, off, p_begin, n_batch, planes, s);
+  else
     throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
-  }
-  check_launch("grid_kernel");
 }
 
-void launch_degrid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
-                   int p_begin, int n_batch, const float2 *planes, float2 *acc,
-                   cudaStream_t s) {
-  const int n_tiles = p.ntu * p.ntv;
-  const int R = p.tile + p.support - 1;
-  if (p.tile == 32) {
-    constexpr int G = 4;
-    const size_t smem = sizeof(float2) * G * R * (R + 1);
-    cudaFuncSetAttribute(degrid_kernel<32, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(n_tiles, (n_batch + G - 1) / G);
-    degrid_kernel<32, G><<<grid, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, planes, acc);
-  } else if (p.tile == 16) {
-    constexpr int G = 8;
-    const size_t smem = sizeof(float2) * G * R * (R + 1);
-    cudaFuncSetAttribute(degrid_kernel<16, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(n_tiles, (n_batch + G - 1) / G);
-    degrid_kernel<16, G><<<grid, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, planes, acc);
-  } else {
+void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                   const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
+                   float2 *acc, cudaStream_t s) {
+  if (p.tile == 32)
+    degrid_batch<32, 4>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+  else if (p.tile == 16)
+    degrid_batch<16, 8>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+  else
     throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
-  }
-  check_launch("degrid_kernel");
 }
 
 }  // namespace wgpu

@@ -89,11 +89,13 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  cudaStream_t s);
 
 // ---- gridding (grid.cu) ----
-void launch_grid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
-                 int p_begin, int n_batch, float2 *planes, cudaStream_t s);
-void launch_degrid(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
-                   int p_begin, int n_batch, const float2 *planes,
-                   float2 *acc, cudaStream_t s);
+class DeviceArena;
+void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                 const uint32_t *off, int p_begin, int n_batch, float2 *planes,
+                 cudaStream_t s);
+void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                   const uint32_t *off, int p_begin, int n_batch,
+                   const float2 *planes, float2 *acc, cudaStream_t s);
 int grid_plane_group();
 
 // ---- FFT (fft.cu) ----
@@ -196,6 +198,8 @@ enum ArenaSlot {
   kSlotImgCorr,
   kSlotErr,
   kSlotOutVis,
+  kSlotItems,
+  kSlotCounter,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
