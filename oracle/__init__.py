@@ -116,7 +116,7 @@ def bucket(plan, uvw, freq, vis, skip_zero):
     key = np.zeros(n, np.int64)
     iu, iv, ip = (np.zeros(n, np.int32) for _ in range(3))
     fu, fv, fw = (np.zeros(n, np.float32) for _ in range(3))
-    n_keys = (op.nu // op.tile) * (op.nv // op.tile) * op.n_planes
+    n_keys = (op.nu // op.tile) * (op.nv // op.tile) * 4 * op.n_planes
     off = np.zeros(n_keys + 1, np.int64)
     k = lib().oracle_bucket(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq), _p(vis),
                             1 if skip_zero else 0, _p(perm), _p(key), _p(iu), _p(iv), _p(ip),

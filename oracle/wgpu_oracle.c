@@ -232,7 +232,11 @@ static void footprint(const OraclePlan *P, const double *scale_u,
   }
   const int64_t ntu = P->nu / P->tile;
   const int64_t tile = (iv / P->tile) * ntu + iu / P->tile;
-  f->key = tile * P->n_planes + f->ip;
+  /* spill class: does the footprint reach the tile to the right / above */
+  const int right = (iu % P->tile) > P->tile - P->support;
+  const int up = (iv % P->tile) > P->tile - P->support;
+  const int64_t cls = right ? (up ? 2 : 1) : (up ? 3 : 0);
+  f->key = (tile * 4 + cls) * P->n_planes + f->ip;
 }
 
 static void channel_scales(const OraclePlan *P, size_t n_chan,
@@ -258,7 +262,7 @@ int64_t oracle_bucket(const OraclePlan *P, size_t n_rows, size_t n_chan,
   channel_scales(P, n_chan, freq, su, sv, sw);
   const double inv_dw = P->n_planes > 1 ? 1.0 / P->dw : 0.0;
   const int64_t n_keys =
-      (P->nu / P->tile) * (P->nv / P->tile) * P->n_planes;
+      (P->nu / P->tile) * (P->nv / P->tile) * 4 * P->n_planes;
   const size_t n_el = n_rows * n_chan;
   int64_t *ekey = malloc(sizeof(int64_t) * (n_el + 1));
   memset(offsets, 0, sizeof(int64_t) * (n_keys + 1));

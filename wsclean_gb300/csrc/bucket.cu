@@ -37,6 +37,20 @@ __global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
   out[c].sw = fl;
 }
 
+}  // namespace
+
+// Which neighbouring tiles a footprint with corner (iu_local, iv_local) in
+// its tile spills into: 0 none, 1 right only, 2 right and up, 3 up only.  The
+// order lets the left neighbour read classes [1, 2], the lower neighbour
+// [2, 3] and the diagonal one [2, 2] as contiguous key ranges.
+__host__ __device__ inline int spill_class(int iu_local, int iv_local, int tile, int support) {
+  const bool right = iu_local > tile - support;
+  const bool up = iv_local > tile - support;
+  return right ? (up ? 2 : 1) : (up ? 3 : 0);
+}
+
+namespace {
+
 struct Footprint {
   int iu, iv, ip;
   float fu, fv, fw;
@@ -74,7 +88,9 @@ __device__ __forceinline__ Footprint footprint(const DevPlan &p,
     f.fw = 0.0f;
   }
   const uint32_t tile = (uint32_t)((f.iv / p.tile) * p.ntu + f.iu / p.tile);
-  f.key = tile * (uint32_t)p.n_planes + (uint32_t)f.ip;
+  f.key = (tile * 4u + (uint32_t)spill_class(f.iu % p.tile, f.iv % p.tile, p.tile, p.support)) *
+              (uint32_t)p.n_planes +
+          (uint32_t)f.ip;
   return f;
 }
 
@@ -325,7 +341,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   if (n >= (int64_t)0xFFFFFFFFll)
     throw Error(WGPU_ERR_INVALID, "more than 2^32-1 visibilities in one call");
   BucketResult res{};
-  res.n_keys = (int64_t)p.ntu * p.ntv * p.n_planes;
+  res.n_keys = (int64_t)p.ntu * p.ntv * 4 * p.n_planes;
   if (res.n_keys >= (int64_t)0xFFFFFFFFll)
     throw Error(WGPU_ERR_INVALID, "too many (tile, plane) buckets");
   int bits = 1;

@@ -54,6 +54,7 @@ struct DevPlan {
 
 DevPlan to_dev_plan(const wgpu_plan_t &p);
 
+
 // ---- planner (plan.cpp) ----
 wgpu_plan_t make_plan(const wgpu_plan_request_t &req);
 void nm1_range(int64_t width, int64_t height, double dl, double dm,
@@ -200,6 +201,7 @@ enum ArenaSlot {
   kSlotOutVis,
   kSlotItems,
   kSlotCounter,
+  kSlotItemDesc,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.

@@ -180,7 +180,7 @@ def bucket_debug(plan, n_rows, n_chan, uvw, freq, vis, skip_zero):
     fu = np.zeros(n, np.float32)
     fv = np.zeros(n, np.float32)
     fw = np.zeros(n, np.float32)
-    n_keys = (plan.nu // plan.tile) * (plan.nv // plan.tile) * plan.n_planes
+    n_keys = (plan.nu // plan.tile) * (plan.nv // plan.tile) * 4 * plan.n_planes
     off = np.zeros(n_keys + 1, np.uint32)
     n_out = C.c_int64()
     check(lib().wgpu_bucket_debug(C.byref(plan), n_rows, n_chan, ptr(uvw), ptr(freq), ptr(vis),
