@@ -104,6 +104,7 @@ struct wgpu_gridder {
   wgpu_plan_t pinned_plan;
   StageTimer timer;
   std::vector<StageTimer::Stage> last_timings;
+  std::string corr_key;  // geometry of the correction tables in the arena
 };
 
 namespace wgpu {
@@ -123,6 +124,18 @@ void ensure_image(wgpu_gridder *g) {
 // and the quadrature nodes (z_q, w_q phi(z_q)) for the per-pixel w factor.
 void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
                         float **cy, float **gl) {
+  // The tables depend on the kernel and grid geometry only: reuse them while
+  // the plan keeps those.
+  char key[256];
+  std::snprintf(key, sizeof(key), "%.17g/%lld/%lld/%lld/%lld/%lld", plan.beta,
+                (long long)plan.support, (long long)plan.nu, (long long)plan.nv,
+                (long long)plan.width, (long long)plan.height);
+  if (g->corr_key == key) {
+    *cx = (float *)g->arena.get(kSlotCorrX, sizeof(float) * plan.width);
+    *cy = (float *)g->arena.get(kSlotCorrY, sizeof(float) * plan.height);
+    *gl = (float *)g->arena.get(kSlotGl, sizeof(float) * 2 * kGlNodes);
+    return;
+  }
   std::vector<float> hx(plan.width), hy(plan.height), hg(2 * kGlNodes);
   for (int64_t x = 0; x < plan.width; ++x)
     hx[x] = (float)(1.0 / es_fourier(plan.beta, (int)plan.support,
@@ -165,6 +178,7 @@ void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
   WGPU_CUDA(cudaMemcpyAsync(*gl, hg.data(), sizeof(float) * 2 * kGlNodes, cudaMemcpyHostToDevice, g->stream));
   // the host vectors die at return: make the copies complete first
   WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  g->corr_key = key;
 }
 
 // A pinned plan is used as long as it covers the data: every visibility's w

@@ -27,8 +27,6 @@ namespace wgpu {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kChunk = 64;       // records staged in shared memory per round
-constexpr int kFoldEvery = 4;    // rounds between two Kahan folds
 constexpr uint32_t kItemVis = 2048;  // visibility reads per work item
 
 // ES kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)), 0 outside |z| < 1, with the
@@ -128,7 +126,22 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
   for (uint32_t i = a; i < b; ++i) desc[i] = (uint32_t)unit | flag;
 }
 
-template <int T, int G>
+// Shared-memory row stride for a tile (or halo region) of `rows` cells: the
+// lanes of a warp cover footprint rows of W cells, so the stride is chosen
+// congruent to 8 (W <= 8, four rows per warp instruction) or 16 (two rows)
+// modulo 32 banks; re and im live in separate arrays so one atomic or load per
+// lane touches one bank.
+__host__ __device__ constexpr int padded_stride(int rows, int W) {
+  return ((rows + 31 - (W <= 8 ? 8 : 16)) / 32) * 32 + (W <= 8 ? 8 : 16);
+}
+
+// Gridding of one plane batch, one warp per visibility: lanes own footprint
+// cells (c = lane + 32 k, i = c % W, j = c / W), the W kernel values of each
+// dimension are evaluated by W lanes and broadcast by shuffles, and each cell
+// is added into the shared tile with one atomic per component.  Every 256
+// visibilities of an item the partial tile is folded into per-thread
+// Kahan-compensated sums.
+template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                 const uint32_t *__restrict__ off, int p_begin, int n_batch,
@@ -136,22 +149,24 @@ __global__ void __launch_bounds__(kThreads)
                 uint32_t total, float2 *__restrict__ planes) {
   constexpr int kCellsPerThread = G * T * T / kThreads;  // cells a thread folds
   static_assert(kCellsPerThread * kThreads == G * T * T, "cells per work item");
-  constexpr int TS = T + 1;  // padded row stride (float2 units)
-  __shared__ float2 buf[G * T * TS];
-  __shared__ float kval[kChunk][3][kMaxSupport];
-  __shared__ float2 cvis[kChunk];
-  __shared__ int cpos[kChunk][3];     // iu_rel, iv_rel, ip
-  __shared__ float cfrac[kChunk][3];  // fu, fv, fw
+  constexpr int TS = padded_stride(T, W);
+  constexpr int kPlane = T * TS;            // floats per plane in each array
+  constexpr int kFoot = W * W;
+  constexpr int kLaneCells = (kFoot + 31) / 32;
+  constexpr int kRound = kThreads;          // visibilities between two folds
+  extern __shared__ float smem[];
+  float *bre = smem;                  // [G][T][TS]
+  float *bim = smem + G * kPlane;     // [G][T][TS]
+  __shared__ uint32_t rs0[9], rcum[10];
 
-  const int W = p.support;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
 
-  for (int c = threadIdx.x; c < G * T * TS; c += kThreads) buf[c] = make_float2(0.f, 0.f);
+  for (int c = threadIdx.x; c < 2 * G * kPlane; c += kThreads) smem[c] = 0.f;
   __syncthreads();
 
-  // static round-robin over the work items: no shared fetch, no barrier
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     const uint32_t d = __ldg(desc + item);
     const int unit = (int)(d & 0x7fffffffu);
@@ -171,7 +186,20 @@ __global__ void __launch_bounds__(kThreads)
     }
     const uint32_t first = __ldg(item_off + unit);
     const uint32_t n_items = __ldg(item_off + unit + 1) - first;
-    const uint32_t lo = (item - first) * kItemVis, hi = lo + kItemVis;
+    if (threadIdx.x < 9) {
+      uint32_t a, b;
+      unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
+      rs0[threadIdx.x] = a;
+      rcum[threadIdx.x + 1] = b - a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      rcum[0] = 0;
+      for (int r = 0; r < 9; ++r) rcum[r + 1] += rcum[r];
+    }
+    __syncthreads();
+    const uint32_t lo = (item - first) * kItemVis;
+    const uint32_t hi = min(lo + kItemVis, rcum[9]);
 
     float2 sum[kCellsPerThread], comp[kCellsPerThread];
 #pragma unroll
@@ -179,111 +207,80 @@ __global__ void __launch_bounds__(kThreads)
       sum[k] = make_float2(0.f, 0.f);
       comp[k] = make_float2(0.f, 0.f);
     }
-    int rounds = 0;
-    uint32_t base = 0;  // position of range r in the unit's concatenated list
-    for (int r = 0; r < 9; ++r) {
-      uint32_t s0, s1;
-      unit_range(p, off, tile, q0, q1, r, &s0, &s1);
-      const uint32_t len = s1 - s0;
-      const uint32_t a = max(lo, base), b = min(hi, base + len);
-      const uint32_t start = base;
-      base += len;
-      if (a >= b) continue;
-      const uint32_t e0 = s0 + (a - start), e1 = s0 + (b - start);
-      for (uint32_t sb = e0; sb < e1; sb += kChunk) {
-        const int m_count = (int)min((uint32_t)kChunk, e1 - sb);
-        if (threadIdx.x < m_count) {
-          const VisRecord rr = load_record(rec + sb + threadIdx.x);
-          int iu_rel = rr.iu - tu * T;
-          if (iu_rel >= T) iu_rel -= p.nu;
-          int iv_rel = rr.iv - tv * T;
-          if (iv_rel >= T) iv_rel -= p.nv;
-          cvis[threadIdx.x] = make_float2(rr.re, rr.im);
-          cpos[threadIdx.x][0] = iu_rel;
-          cpos[threadIdx.x][1] = iv_rel;
-          cpos[threadIdx.x][2] = rr.ip;
-          cfrac[threadIdx.x][0] = rr.fu;
-          cfrac[threadIdx.x][1] = rr.fv;
-          cfrac[threadIdx.x][2] = rr.fw;
+    for (uint32_t rb = lo; rb < hi; rb += kRound) {
+      const uint32_t we = min(hi, rb + (uint32_t)(warp + 1) * 32u);
+      int r = 0;
+      for (uint32_t pos = rb + (uint32_t)warp * 32u; pos < we; ++pos) {
+        while (pos >= rcum[r + 1]) ++r;
+        const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
+        int iu_rel = v.iu - tu * T;
+        if (iu_rel >= T) iu_rel -= p.nu;
+        int iv_rel = v.iv - tv * T;
+        if (iv_rel >= T) iv_rel -= p.nv;
+        const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
+        if (pa > pb) continue;  // uniform in the warp
+        // lanes 0..W-1: kx, W..2W-1: ky (first value); lanes 0..W-1: kw
+        float k1 = 0.f, k2 = 0.f;
+        if (lane < W)
+          k1 = es_eval(p.beta, (v.fu + (float)lane) * inv_half);
+        else if (lane < 2 * W)
+          k1 = es_eval(p.beta, (v.fv + (float)(lane - W)) * inv_half);
+        if (lane < W)
+          k2 = p.n_planes == 1 ? (lane == 0 ? 1.0f : 0.0f)
+                               : es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+        float wgt[kLaneCells];
+        int idx[kLaneCells];
+#pragma unroll
+        for (int k = 0; k < kLaneCells; ++k) {
+          const int c = lane + 32 * k;
+          const int i = c % W, j = c / W;
+          const float kx = __shfl_sync(0xffffffffu, k1, i);
+          const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
+          const int row = iv_rel + j, col = iu_rel + i;
+          const bool in = c < kFoot && row >= 0 && row < T && col >= 0 && col < T;
+          wgt[k] = in ? kx * ky : 0.f;
+          idx[k] = in ? row * TS + col : -1;
         }
-        __syncthreads();
-        // kernel values: (m, dim, j) -> phi((f + j) / half)
-        for (int idx = threadIdx.x; idx < m_count * 3 * kMaxSupport; idx += kThreads) {
-          const int j = idx % kMaxSupport;
-          const int dd = (idx / kMaxSupport) % 3;
-          const int m = idx / (3 * kMaxSupport);
-          if (j >= W) continue;
-          float v;
-          if (dd == 2 && p.n_planes == 1)
-            v = (j == 0) ? 1.0f : 0.0f;
-          else
-            v = es_eval(p.beta, (cfrac[m][dd] + (float)j) * inv_half);
-          kval[m][dd][j] = v;
-        }
-        __syncthreads();
-        // spread: units (m, j) = one footprint row of one visibility
-        for (int u = threadIdx.x; u < m_count * W; u += kThreads) {
-          const int m = u / W, j = u - m * W;
-          const int row = cpos[m][1] + j;
-          if (row < 0 || row >= T) continue;
-          const int ip = cpos[m][2];
-          const int pa = max(ip, q0), pb = min(ip + W - 1, q1 - 1);
-          if (pa > pb) continue;
-          const int iu_rel = cpos[m][0];
-          const int ia = max(0, -iu_rel), ib = min(W - 1, T - 1 - iu_rel);
-          const float ky = kval[m][1][j];
-          const float2 v = cvis[m];
-          for (int q = pa; q <= pb; ++q) {
-            const float wy = ky * kval[m][2][q - ip];
-            float2 *brow = buf + ((q - q0) * T + row) * TS + iu_rel;
-            for (int i = ia; i <= ib; ++i) {
-              const float wt = wy * kval[m][0][i];
-              atomicAdd(&brow[i].x, wt * v.x);
-              atomicAdd(&brow[i].y, wt * v.y);
+        for (int q = pa; q <= pb; ++q) {
+          const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
+          const float vr = v.re * kw, vi = v.im * kw;
+          float *pre = bre + (q - q0) * kPlane, *pim = bim + (q - q0) * kPlane;
+#pragma unroll
+          for (int k = 0; k < kLaneCells; ++k) {
+            if (idx[k] >= 0) {
+              atomicAdd(pre + idx[k], wgt[k] * vr);
+              atomicAdd(pim + idx[k], wgt[k] * vi);
             }
           }
         }
-        __syncthreads();
-        if (++rounds == kFoldEvery) {
-          rounds = 0;
-#pragma unroll
-          for (int k = 0; k < kCellsPerThread; ++k) {
-            const int c = threadIdx.x + k * kThreads;
-            const int pq = c / (T * T), rem = c - pq * T * T;
-            const int row = rem / T, col = rem - row * T;
-            float2 *cell = buf + (pq * T + row) * TS + col;
-            const float2 x = *cell;
-            *cell = make_float2(0.f, 0.f);
-            float y = x.x - comp[k].x;
-            float t = sum[k].x + y;
-            comp[k].x = (t - sum[k].x) - y;
-            sum[k].x = t;
-            y = x.y - comp[k].y;
-            t = sum[k].y + y;
-            comp[k].y = (t - sum[k].y) - y;
-            sum[k].y = t;
-          }
-          __syncthreads();
-        }
       }
+      __syncthreads();
+      // fold the round into the compensated sums
+#pragma unroll
+      for (int k = 0; k < kCellsPerThread; ++k) {
+        const int c = threadIdx.x + k * kThreads;
+        const int pq = c / (T * T), rem = c - pq * T * T;
+        const int row = rem / T, col = rem - row * T;
+        const int o = pq * kPlane + row * TS + col;
+        const float xr = bre[o], xi = bim[o];
+        bre[o] = 0.f;
+        bim[o] = 0.f;
+        float y = xr - comp[k].x;
+        float t = sum[k].x + y;
+        comp[k].x = (t - sum[k].x) - y;
+        sum[k].x = t;
+        y = xi - comp[k].y;
+        t = sum[k].y + y;
+        comp[k].y = (t - sum[k].y) - y;
+        sum[k].y = t;
+      }
+      __syncthreads();
     }
-    // final fold and write
 #pragma unroll
     for (int k = 0; k < kCellsPerThread; ++k) {
       const int c = threadIdx.x + k * kThreads;
       const int pq = c / (T * T), rem = c - pq * T * T;
       const int row = rem / T, col = rem - row * T;
-      float2 *cell = buf + (pq * T + row) * TS + col;
-      const float2 x = *cell;
-      *cell = make_float2(0.f, 0.f);
-      float y = x.x - comp[k].x;
-      float t = sum[k].x + y;
-      comp[k].x = (t - sum[k].x) - y;
-      sum[k].x = t;
-      y = x.y - comp[k].y;
-      t = sum[k].y + y;
-      comp[k].y = (t - sum[k].y) - y;
-      sum[k].y = t;
       const int q = q0 + pq;
       if (q < q1) {
         float2 *dst = planes + (size_t)(q - p_begin) * plane_elems +
@@ -294,21 +291,29 @@ __global__ void __launch_bounds__(kThreads)
           atomicAdd(dst, sum[k]);
       }
     }
-    __syncthreads();
   }
 }
 
-template <int T, int G>
+// Degridding of one plane batch, one warp per visibility: lanes own footprint
+// cells, each lane accumulates its cells over the planes of the group from the
+// shared halo region, and a warp-level shuffle reduction forms the sum.
+template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     degrid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                   const uint32_t *__restrict__ off, int p_begin, int n_batch,
                   const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
                   uint32_t total, const float2 *__restrict__ planes,
                   float2 *__restrict__ acc) {
-  extern __shared__ float2 region[];  // [G][R][RS]
-  const int W = p.support;
-  const int R = T + W - 1;
-  const int RS = R + 1;
+  constexpr int R = T + W - 1;
+  constexpr int RS = padded_stride(R, W);
+  constexpr int kPlane = R * RS;
+  constexpr int kFoot = W * W;
+  constexpr int kLaneCells = (kFoot + 31) / 32;
+  extern __shared__ float smem[];
+  float *gre = smem;               // [G][R][RS]
+  float *gim = smem + G * kPlane;  // [G][R][RS]
+  __shared__ uint32_t rs0[4], rcum[5];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
@@ -319,7 +324,7 @@ __global__ void __launch_bounds__(kThreads)
     const int tu = tile % p.ntu, tv = tile / p.ntu;
     const int q0 = p_begin + group * G;
     const int q1 = min(q0 + G, p_begin + n_batch);
-    const uint32_t lo = (item - __ldg(item_off + unit)) * kItemVis, hi = lo + kItemVis;
+    const uint32_t lo = (item - __ldg(item_off + unit)) * kItemVis;
 
     const int nq = q1 - q0;
     for (int idx = threadIdx.x; idx < nq * R * R; idx += blockDim.x) {
@@ -329,59 +334,72 @@ __global__ void __launch_bounds__(kThreads)
       if (gv >= p.nv) gv -= p.nv;
       int gu = tu * T + c;
       if (gu >= p.nu) gu -= p.nu;
-      region[(pq * R + r) * RS + c] =
+      const float2 g =
           planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu];
+      gre[pq * kPlane + r * RS + c] = g.x;
+      gim[pq * kPlane + r * RS + c] = g.y;
+    }
+    if (threadIdx.x < 4) {
+      uint32_t a, b;
+      unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
+      rs0[threadIdx.x] = a;
+      rcum[threadIdx.x + 1] = b - a;
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+      rcum[0] = 0;
+      for (int r = 0; r < 4; ++r) rcum[r + 1] += rcum[r];
+    }
+    __syncthreads();
+    const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
-    uint32_t base = 0;
-    for (int rg = 0; rg < 4; ++rg) {  // own tile, classes 0..3
-      uint32_t s0, s1;
-      unit_range(p, off, tile, q0, q1, rg, &s0, &s1);
-      const uint32_t len = s1 - s0;
-      const uint32_t a = max(lo, base), b = min(hi, base + len);
-      const uint32_t start = base;
-      base += len;
-      if (a >= b) continue;
-      for (uint32_t s = s0 + (a - start) + threadIdx.x; s < s0 + (b - start); s += blockDim.x) {
-        const VisRecord r = load_record(rec + s);
-        float kx[kMaxSupport], ky[kMaxSupport];
+    int r = 0;
+    for (uint32_t pos = lo + warp; pos < hi; pos += kThreads / 32) {
+      while (pos >= rcum[r + 1]) ++r;
+      const uint32_t s = rs0[r] + (pos - rcum[r]);
+      const VisRecord v = load_record(rec + s);
+      const int iu_rel = v.iu - tu * T;
+      const int iv_rel = v.iv - tv * T;
+      const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
+      if (pa > pb) continue;  // uniform in the warp
+      float k1 = 0.f, k2 = 0.f;
+      if (lane < W)
+        k1 = es_eval(p.beta, (v.fu + (float)lane) * inv_half);
+      else if (lane < 2 * W)
+        k1 = es_eval(p.beta, (v.fv + (float)(lane - W)) * inv_half);
+      if (lane < W)
+        k2 = p.n_planes == 1 ? (lane == 0 ? 1.0f : 0.0f)
+                             : es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+      float wgt[kLaneCells];
+      int idx[kLaneCells];
 #pragma unroll
-        for (int j = 0; j < kMaxSupport; ++j) {
-          kx[j] = j < W ? es_eval(p.beta, (r.fu + (float)j) * inv_half) : 0.0f;
-          ky[j] = j < W ? es_eval(p.beta, (r.fv + (float)j) * inv_half) : 0.0f;
-        }
-        const int iu_rel = r.iu - tu * T;
-        const int iv_rel = r.iv - tv * T;
-        const int pa = max(r.ip, q0), pb = min(r.ip + W - 1, q1 - 1);
-        float sr = 0.f, si = 0.f;
-        for (int q = pa; q <= pb; ++q) {
-          const float kw = p.n_planes == 1 ? 1.0f
-                                           : es_eval(p.beta, (r.fw + (float)(q - r.ip)) * inv_half);
-          const float2 *bp = region + ((q - q0) * R + iv_rel) * RS + iu_rel;
-          float pr = 0.f, pi = 0.f;
-#pragma unroll
-          for (int j = 0; j < kMaxSupport; ++j) {
-            if (j < W) {
-              const float2 *rowp = bp + j * RS;
-              float rr = 0.f, ri = 0.f;
-#pragma unroll
-              for (int i = 0; i < kMaxSupport; ++i) {
-                if (i < W) {
-                  const float2 g = rowp[i];
-                  rr += kx[i] * g.x;
-                  ri += kx[i] * g.y;
-                }
-              }
-              pr += ky[j] * rr;
-              pi += ky[j] * ri;
-            }
-          }
-          sr += kw * pr;
-          si += kw * pi;
-        }
-        atomicAdd(&acc[s], make_float2(sr, si));
+      for (int k = 0; k < kLaneCells; ++k) {
+        const int c = lane + 32 * k;
+        const int i = c % W, j = c / W;
+        const float kx = __shfl_sync(0xffffffffu, k1, i);
+        const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
+        wgt[k] = c < kFoot ? kx * ky : 0.f;
+        idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : 0;
       }
+      float sr = 0.f, si = 0.f;
+      for (int q = pa; q <= pb; ++q) {
+        const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
+        const float *pre = gre + (q - q0) * kPlane, *pim = gim + (q - q0) * kPlane;
+        float pr = 0.f, pi = 0.f;
+#pragma unroll
+        for (int k = 0; k < kLaneCells; ++k) {
+          pr += wgt[k] * pre[idx[k]];
+          pi += wgt[k] * pim[idx[k]];
+        }
+        sr += kw * pr;
+        si += kw * pi;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+      }
+      if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
     }
     __syncthreads();
   }
@@ -415,19 +433,17 @@ uint32_t plan_items(DeviceArena &arena, const DevPlan &p, const uint32_t *off, i
   check_launch("grid_plan_kernel");
   WGPU_CUDA(cudaMemsetAsync(*item_off + n_units, 0, sizeof(uint32_t), s));
   exclusive_scan_u32(arena, *item_off, n_units + 1, s);
-  uint32_t *pinned = (uint32_t *)arena.get(kSlotCounter, 64);
   uint32_t total = 0;
   WGPU_CUDA(cudaMemcpyAsync(&total, *item_off + n_units, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
-  (void)pinned;
   *desc = (uint32_t *)arena.get(kSlotItemDesc, sizeof(uint32_t) * ((size_t)total + 1));
   fill_items_kernel<<<(n_units + 255) / 256, 256, 0, s>>>(*item_off, counts, n_units, *desc);
   check_launch("fill_items_kernel");
   return total;
 }
 
-template <int T, int G>
+template <int T, int G, int W>
 void grid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                 const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                 cudaStream_t s) {
@@ -435,15 +451,19 @@ void grid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
   const uint32_t total =
       plan_items<T, G>(arena, p, off, p_begin, n_batch, false, planes, &item_off, &desc, s);
   if (total == 0) return;
+  const size_t smem = sizeof(float) * 2 * G * T * padded_stride(T, W);
+  WGPU_CUDA(cudaFuncSetAttribute(grid_kernel<T, G, W>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G>, kThreads, 0));
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G, W>,
+                                                          kThreads, smem));
   const uint32_t blocks = std::min<uint32_t>(total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
-  grid_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, rec, off, p_begin, n_batch, item_off, desc,
-                                                total, planes);
+  grid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, item_off,
+                                                      desc, total, planes);
   check_launch("grid_kernel");
 }
 
-template <int T, int G>
+template <int T, int G, int W>
 void degrid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                   const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
                   float2 *acc, cudaStream_t s) {
@@ -451,17 +471,46 @@ void degrid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
   const uint32_t total =
       plan_items<T, G>(arena, p, off, p_begin, n_batch, true, nullptr, &item_off, &desc, s);
   if (total == 0) return;
-  const int R = T + p.support - 1;
-  const size_t smem = sizeof(float2) * G * R * (R + 1);
-  WGPU_CUDA(cudaFuncSetAttribute(degrid_kernel<T, G>,
+  constexpr int R = T + W - 1;
+  const size_t smem = sizeof(float) * 2 * G * R * padded_stride(R, W);
+  WGPU_CUDA(cudaFuncSetAttribute(degrid_kernel<T, G, W>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G>,
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G, W>,
                                                           kThreads, smem));
   const uint32_t blocks = std::min<uint32_t>(total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
-  degrid_kernel<T, G><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, item_off,
-                                                     desc, total, planes, acc);
+  degrid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch,
+                                                        item_off, desc, total, planes, acc);
   check_launch("degrid_kernel");
+}
+
+// Dispatch over the kernel support (4..16) for one tile shape.
+template <int T, int G, int W = 4>
+void grid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                   const uint32_t *off, int p_begin, int n_batch, float2 *planes,
+                   cudaStream_t s) {
+  if constexpr (W > kMaxSupport) {
+    throw Error(WGPU_ERR_INVALID, "kernel support out of range");
+  } else {
+    if (support == W)
+      grid_batch<T, G, W>(arena, p, rec, off, p_begin, n_batch, planes, s);
+    else
+      grid_dispatch<T, G, W + 1>(support, arena, p, rec, off, p_begin, n_batch, planes, s);
+  }
+}
+
+template <int T, int G, int W = 4>
+void degrid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
+                     const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
+                     float2 *acc, cudaStream_t s) {
+  if constexpr (W > kMaxSupport) {
+    throw Error(WGPU_ERR_INVALID, "kernel support out of range");
+  } else {
+    if (support == W)
+      degrid_batch<T, G, W>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+    else
+      degrid_dispatch<T, G, W + 1>(support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+  }
 }
 
 }  // namespace
@@ -471,10 +520,12 @@ int grid_plane_group() { return 4; }
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s) {
+  if (p.support < 4 || p.support > kMaxSupport)
+    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
   if (p.tile == 32)
-    grid_batch<32, 4>(arena, p, rec, off, p_begin, n_batch, planes, s);
+    grid_dispatch<32, 4>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
   else if (p.tile == 16)
-    grid_batch<16, 8>(arena, p, rec, off, p_begin, n_batch, planes, s);
+    grid_dispatch<16, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
   else
     throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
 }
@@ -482,10 +533,12 @@ void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
 void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                    const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
                    float2 *acc, cudaStream_t s) {
+  if (p.support < 4 || p.support > kMaxSupport)
+    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
   if (p.tile == 32)
-    degrid_batch<32, 4>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+    degrid_dispatch<32, 4>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
   else if (p.tile == 16)
-    degrid_batch<16, 8>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+    degrid_dispatch<16, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
   else
     throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
 }
