@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kThreads)
   float *bre = smem;                  // [G][T][TS]
   float *bim = smem + G * kPlane;     // [G][T][TS]
   __shared__ uint32_t rs0[9], rcum[10];
+  __shared__ float4 stage[kRound][2];  // the round's records, loaded coalesced
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_half = 2.0f / (float)W;
@@ -208,11 +209,25 @@ __global__ void __launch_bounds__(kThreads)
       comp[k] = make_float2(0.f, 0.f);
     }
     for (uint32_t rb = lo; rb < hi; rb += kRound) {
-      const uint32_t we = min(hi, rb + (uint32_t)(warp + 1) * 32u);
-      int r = 0;
-      for (uint32_t pos = rb + (uint32_t)warp * 32u; pos < we; ++pos) {
-        while (pos >= rcum[r + 1]) ++r;
-        const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
+      {
+        const uint32_t pos = rb + threadIdx.x;
+        if (pos < hi) {
+          int r = 0;
+          while (pos >= rcum[r + 1]) ++r;
+          const float4 *src = reinterpret_cast<const float4 *>(rec + rs0[r] + (pos - rcum[r]));
+          stage[threadIdx.x][0] = __ldg(src);
+          stage[threadIdx.x][1] = __ldg(src + 1);
+        }
+      }
+      __syncthreads();
+      const int n_round = (int)min((uint32_t)kRound, hi - rb);
+      for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
+        VisRecord v;
+        {
+          const float4 a = stage[m][0], b = stage[m][1];
+          v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
+          v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
+        }
         int iu_rel = v.iu - tu * T;
         if (iu_rel >= T) iu_rel -= p.nu;
         int iv_rel = v.iv - tv * T;
@@ -313,6 +328,8 @@ __global__ void __launch_bounds__(kThreads)
   float *gre = smem;               // [G][R][RS]
   float *gim = smem + G * kPlane;  // [G][R][RS]
   __shared__ uint32_t rs0[4], rcum[5];
+  __shared__ float4 stage[kThreads][2];
+  __shared__ uint32_t stage_s[kThreads];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
@@ -353,11 +370,29 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
     const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
-    int r = 0;
-    for (uint32_t pos = lo + warp; pos < hi; pos += kThreads / 32) {
-      while (pos >= rcum[r + 1]) ++r;
-      const uint32_t s = rs0[r] + (pos - rcum[r]);
-      const VisRecord v = load_record(rec + s);
+    for (uint32_t rb = lo; rb < hi; rb += kThreads) {
+     {
+      const uint32_t pos = rb + threadIdx.x;
+      if (pos < hi) {
+        int r = 0;
+        while (pos >= rcum[r + 1]) ++r;
+        const uint32_t s = rs0[r] + (pos - rcum[r]);
+        const float4 *src = reinterpret_cast<const float4 *>(rec + s);
+        stage[threadIdx.x][0] = __ldg(src);
+        stage[threadIdx.x][1] = __ldg(src + 1);
+        stage_s[threadIdx.x] = s;
+      }
+     }
+     __syncthreads();
+     const int n_round = (int)min((uint32_t)kThreads, hi - rb);
+     for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
+      const uint32_t s = stage_s[m];
+      VisRecord v;
+      {
+        const float4 a = stage[m][0], b = stage[m][1];
+        v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
+        v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
+      }
       const int iu_rel = v.iu - tu * T;
       const int iv_rel = v.iv - tv * T;
       const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
@@ -400,8 +435,9 @@ __global__ void __launch_bounds__(kThreads)
         si += __shfl_xor_sync(0xffffffffu, si, o);
       }
       if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
+     }
+     __syncthreads();
     }
-    __syncthreads();
   }
 }
 
