@@ -219,7 +219,7 @@ wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis)
   r.n_vis = n_vis;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-    r.memory_budget_bytes = std::min(24e9, 0.4 * (double)(free_b + g->arena.total()));
+    r.memory_budget_bytes = std::min(40e9, 0.4 * (double)(free_b + g->arena.total()));
   }
   // WGPU_PLANE_BUDGET_GB caps the plane-batch memory (profiling small cases)
   if (const char *env = std::getenv("WGPU_PLANE_BUDGET_GB")) {

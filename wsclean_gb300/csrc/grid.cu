@@ -28,6 +28,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kItemVis = 2048;  // visibility reads per work item
+constexpr int kTile = 16;            // uv tile edge (cells)
+constexpr int kGridPlanes = 16;      // w planes per gridding work unit
 
 // ES kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)), 0 outside |z| < 1, with the
 // fast intrinsics: their relative error (~1e-7 where phi is large) is white
@@ -132,7 +134,8 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
 // modulo 32 banks; re and im live in separate arrays so one atomic or load per
 // lane touches one bank.
 __host__ __device__ constexpr int padded_stride(int rows, int W) {
-  return ((rows + 31 - (W <= 8 ? 8 : 16)) / 32) * 32 + (W <= 8 ? 8 : 16);
+  return W <= 8 ? (((rows + 7) / 16) * 16 + 8)    // 8 or 24 (mod 32)
+                : (((rows + 15) / 32) * 32 + 16);  // 16 (mod 32)
 }
 
 // Gridding of one plane batch, one warp per visibility: lanes own footprint
@@ -235,14 +238,13 @@ __global__ void __launch_bounds__(kThreads)
         const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
         if (pa > pb) continue;  // uniform in the warp
         // lanes 0..W-1: kx, W..2W-1: ky (first value); lanes 0..W-1: kw
-        float k1 = 0.f, k2 = 0.f;
-        if (lane < W)
-          k1 = es_eval(p.beta, (v.fu + (float)lane) * inv_half);
-        else if (lane < 2 * W)
-          k1 = es_eval(p.beta, (v.fv + (float)(lane - W)) * inv_half);
-        if (lane < W)
-          k2 = p.n_planes == 1 ? (lane == 0 ? 1.0f : 0.0f)
-                               : es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+        // lanes 0..W-1 hold kx, W..2W-1 hold ky (k1); lanes 0..W-1 hold kw (k2)
+        const bool lx = lane < W;
+        const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
+        float k1 = es_eval(p.beta, f1 * inv_half);
+        k1 = lane < 2 * W ? k1 : 0.f;
+        float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+        if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
         float wgt[kLaneCells];
         int idx[kLaneCells];
 #pragma unroll
@@ -397,14 +399,12 @@ __global__ void __launch_bounds__(kThreads)
       const int iv_rel = v.iv - tv * T;
       const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
       if (pa > pb) continue;  // uniform in the warp
-      float k1 = 0.f, k2 = 0.f;
-      if (lane < W)
-        k1 = es_eval(p.beta, (v.fu + (float)lane) * inv_half);
-      else if (lane < 2 * W)
-        k1 = es_eval(p.beta, (v.fv + (float)(lane - W)) * inv_half);
-      if (lane < W)
-        k2 = p.n_planes == 1 ? (lane == 0 ? 1.0f : 0.0f)
-                             : es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+      const bool lx = lane < W;
+      const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
+      float k1 = es_eval(p.beta, f1 * inv_half);
+      k1 = lane < 2 * W ? k1 : 0.f;
+      float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+      if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
       float wgt[kLaneCells];
       int idx[kLaneCells];
 #pragma unroll
@@ -539,7 +539,7 @@ template <int T, int G, int W = 4>
 void degrid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                      const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
                      float2 *acc, cudaStream_t s) {
-  if constexpr (W > kMaxSupport) {
+  if constexpr (W > kMaxSupport || (G > 8 && W > 8)) {
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
@@ -551,19 +551,15 @@ void degrid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const Vi
 
 }  // namespace
 
-int grid_plane_group() { return 4; }
+int grid_plane_group() { return kGridPlanes; }
 
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s) {
   if (p.support < 4 || p.support > kMaxSupport)
     throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
-  if (p.tile == 32)
-    grid_dispatch<32, 4>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
-  else if (p.tile == 16)
-    grid_dispatch<16, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
-  else
-    throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
+  if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
+  grid_dispatch<kTile, kGridPlanes>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
 }
 
 void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
@@ -571,12 +567,11 @@ void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                    float2 *acc, cudaStream_t s) {
   if (p.support < 4 || p.support > kMaxSupport)
     throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
-  if (p.tile == 32)
-    degrid_dispatch<32, 4>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
-  else if (p.tile == 16)
-    degrid_dispatch<16, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+  if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
+  if (p.support <= 8)
+    degrid_dispatch<kTile, 16>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
   else
-    throw Error(WGPU_ERR_INVALID, "tile must be 16 or 32");
+    degrid_dispatch<kTile, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
 }
 
 }  // namespace wgpu

@@ -191,14 +191,12 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     p.support = e.support;
     p.sigma = e.sigma;
     p.beta = e.beta;
-    int64_t tile = req.force_tile > 0 ? req.force_tile : 32;
-    int64_t nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
-    int64_t nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
-    if (req.force_tile <= 0 && std::min(nu, nv) < 256) {
-      tile = 16;
-      nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
-      nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
-    }
+    // uv tiles of 16 x 16 cells (the gridding work units pair them with 16
+    // w planes); the grid spans at least two tiles per axis
+    const int64_t tile = 16;
+    if (req.force_tile > 0 && req.force_tile != tile) continue;
+    const int64_t nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
+    const int64_t nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
     if (e.support > tile) continue;
     int64_t f1, f2;
     if (nu > fft_row_max_length() || !try_decompose(nv, &f1, &f2)) continue;
@@ -246,10 +244,13 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
   // Planes resident per pipeline step.
   const int64_t rstride = (best.width + 31) / 32 * 32;
   const double per_plane = 8.0 * best.nu * best.nv + 8.0 * best.nv * rstride;
-  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 24e9;
+  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 40e9;
   int64_t batch = (int64_t)std::floor(budget / per_plane);
   int64_t cap = req.max_plane_batch > 0 ? req.max_plane_batch : 32;
   batch = std::max<int64_t>(1, std::min<int64_t>(std::min(batch, cap), best.n_planes));
+  // whole 16-plane gridding groups where the batch allows it
+  const int64_t group = grid_plane_group();
+  if (batch > group && batch < best.n_planes) batch -= batch % group;
   best.plane_batch = batch;
   fft_decompose(best.nv, &best.fft_n1, &best.fft_n2);
   return best;
