@@ -141,22 +141,20 @@ __host__ __device__ constexpr int padded_stride(int rows, int W) {
 // Gridding of one plane batch, one warp per visibility: lanes own footprint
 // cells (c = lane + 32 k, i = c % W, j = c / W), the W kernel values of each
 // dimension are evaluated by W lanes and broadcast by shuffles, and each cell
-// is added into the shared tile with one atomic per component.  Every 256
-// visibilities of an item the partial tile is folded into per-thread
-// Kahan-compensated sums.
+// is added into the shared tile with one atomic per component.  A work item
+// holds at most kItemVis visibility reads, which bounds the FP32 accumulation
+// chain of every cell; the item's tile is flushed to HBM once at its end.
 template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                 const uint32_t *__restrict__ off, int p_begin, int n_batch,
                 const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
                 uint32_t total, float2 *__restrict__ planes) {
-  constexpr int kCellsPerThread = G * T * T / kThreads;  // cells a thread folds
-  static_assert(kCellsPerThread * kThreads == G * T * T, "cells per work item");
   constexpr int TS = padded_stride(T, W);
   constexpr int kPlane = T * TS;            // floats per plane in each array
   constexpr int kFoot = W * W;
   constexpr int kLaneCells = (kFoot + 31) / 32;
-  constexpr int kRound = kThreads;          // visibilities between two folds
+  constexpr int kRound = kThreads;          // records staged per round
   extern __shared__ float smem[];
   float *bre = smem;                  // [G][T][TS]
   float *bim = smem + G * kPlane;     // [G][T][TS]
@@ -205,12 +203,6 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t lo = (item - first) * kItemVis;
     const uint32_t hi = min(lo + kItemVis, rcum[9]);
 
-    float2 sum[kCellsPerThread], comp[kCellsPerThread];
-#pragma unroll
-    for (int k = 0; k < kCellsPerThread; ++k) {
-      sum[k] = make_float2(0.f, 0.f);
-      comp[k] = make_float2(0.f, 0.f);
-    }
     for (uint32_t rb = lo; rb < hi; rb += kRound) {
       {
         const uint32_t pos = rb + threadIdx.x;
@@ -237,7 +229,6 @@ __global__ void __launch_bounds__(kThreads)
         if (iv_rel >= T) iv_rel -= p.nv;
         const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
         if (pa > pb) continue;  // uniform in the warp
-        // lanes 0..W-1: kx, W..2W-1: ky (first value); lanes 0..W-1: kw
         // lanes 0..W-1 hold kx, W..2W-1 hold ky (k1); lanes 0..W-1 hold kw (k2)
         const bool lx = lane < W;
         const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
@@ -272,42 +263,26 @@ __global__ void __launch_bounds__(kThreads)
         }
       }
       __syncthreads();
-      // fold the round into the compensated sums
-#pragma unroll
-      for (int k = 0; k < kCellsPerThread; ++k) {
-        const int c = threadIdx.x + k * kThreads;
-        const int pq = c / (T * T), rem = c - pq * T * T;
-        const int row = rem / T, col = rem - row * T;
-        const int o = pq * kPlane + row * TS + col;
-        const float xr = bre[o], xi = bim[o];
-        bre[o] = 0.f;
-        bim[o] = 0.f;
-        float y = xr - comp[k].x;
-        float t = sum[k].x + y;
-        comp[k].x = (t - sum[k].x) - y;
-        sum[k].x = t;
-        y = xi - comp[k].y;
-        t = sum[k].y + y;
-        comp[k].y = (t - sum[k].y) - y;
-        sum[k].y = t;
-      }
-      __syncthreads();
     }
-#pragma unroll
-    for (int k = 0; k < kCellsPerThread; ++k) {
-      const int c = threadIdx.x + k * kThreads;
+    // flush the tile (a split unit adds into cells zeroed by the planner)
+    for (int c = threadIdx.x; c < G * T * T; c += kThreads) {
       const int pq = c / (T * T), rem = c - pq * T * T;
       const int row = rem / T, col = rem - row * T;
+      const int o = pq * kPlane + row * TS + col;
+      const float2 val = make_float2(bre[o], bim[o]);
+      bre[o] = 0.f;
+      bim[o] = 0.f;
       const int q = q0 + pq;
       if (q < q1) {
         float2 *dst = planes + (size_t)(q - p_begin) * plane_elems +
                       (size_t)(tv * T + row) * p.nu + tu * T + col;
         if (n_items == 1)
-          *dst = sum[k];
+          *dst = val;
         else
-          atomicAdd(dst, sum[k]);
+          atomicAdd(dst, val);
       }
     }
+    __syncthreads();
   }
 }
 
