@@ -1,0 +1,196 @@
+/*
+ * wsclean::WGriddingGridder_Simple<NumT> on the GB300 w-gridder.
+ *
+ * A header-only C++ class with the interface of wgridder/gridder_simple.h
+ * (WGriddingGridderBase, :19-41, and WGriddingGridder_Simple, :54-245), written
+ * on the C ABI in wgpu.h.  WSClean's WGriddingMSGridder (MakeGridder,
+ * wgriddingmsgridder.cpp:41-54) constructs it exactly as it constructs the
+ * ducc0-backed class.  Errors from the C ABI are rethrown as
+ * std::runtime_error, as the reference's MR_assert / exceptions are.
+ *
+ * Standalone use: define nothing; GainMode, BandData and MsGridder are
+ * declared here.  Inside WSClean: define WGPU_WITH_WSCLEAN before including, so
+ * that WSClean's own GainMode / aocommon::BandData / MsGridder are used and the
+ * correction callback reads the gridder's cached solution table (see
+ * INTEGRATION.md for the accessor it needs).
+ */
+#ifndef WGPU_GRIDDER_H_
+#define WGPU_GRIDDER_H_
+
+#include <complex>
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "wgpu.h"
+
+#ifdef WGPU_WITH_WSCLEAN
+#include <aocommon/banddata.h>
+#include "../gridding/gainmode.h"
+#include "../gridding/msgridder.h"
+#else
+namespace aocommon {
+class BandData;
+}
+namespace wsclean {
+/* gridding/gainmode.h:16-31 */
+enum class GainMode { kXX, kYY, kTrace, k2VisDiagonal, kFull };
+class MsGridder;
+}  // namespace wsclean
+#endif
+
+namespace wsclean {
+
+/* The cached parm-response table a correction callback needs on the device:
+ * complex64 solutions indexed ((t * n_chan + ch) * n_ant + ant) * nparms
+ * (visibilitymodifier.h:547-551). */
+struct GpuCorrectionTable {
+  const std::complex<float> *solutions = nullptr;
+  size_t n_times = 0;
+  size_t nparms = 2;
+  int polarization = WGPU_POL_STOKES_I;
+};
+
+/* gridder_simple.h:19-41 */
+class WGriddingGridderBase {
+ public:
+  virtual ~WGriddingGridderBase() = default;
+  virtual size_t ConstantMemoryUsage() const = 0;
+  virtual size_t PerVisibilityMemoryUsage() const = 0;
+  virtual void InitializeInversion() = 0;
+  virtual void AddInversionData(size_t n_rows, size_t n_chan, const double *uvw,
+                                const double *freq,
+                                const std::complex<float> *vis) = 0;
+  virtual void AddInversionDataWithCorrectionCallback(
+      GainMode mode, size_t n_polarizations, size_t n_rows, const double *uvws,
+      const double *frequencies, size_t n_channels,
+      const aocommon::BandData &selected_band,
+      const std::pair<size_t, size_t> *antennas,
+      const std::complex<float> *visibilities, const size_t *time_offsets,
+      MsGridder *gridder, size_t n_antenna) = 0;
+  virtual void FinalizeImage(double multiplicationFactor) = 0;
+  virtual std::vector<float> RealImage() = 0;
+  virtual void InitializePrediction(const float *image_data) = 0;
+  virtual void PredictVisibilities(size_t n_rows, size_t n_chan,
+                                   const double *uvw, const double *freq,
+                                   std::complex<float> *vis) const = 0;
+};
+
+namespace wgpu_detail {
+inline void check(int status) {
+  if (status != WGPU_OK)
+    throw std::runtime_error(std::string("wgpu: ") + wgpu_last_error());
+}
+}  // namespace wgpu_detail
+
+template <typename NumT>
+class WGriddingGridder_Simple final : public WGriddingGridderBase {
+  static_assert(sizeof(NumT) == 4 || sizeof(NumT) == 8, "float or double");
+
+ public:
+  static constexpr double sigma_min = 1.1;  // gridder_simple.h:57
+  static constexpr double sigma_max = 2.0;  // gridder_simple.h:58
+
+  /* gridder_simple.h:84-88; nthreads is accepted and not used (one GPU). */
+  WGriddingGridder_Simple(size_t width, size_t height, size_t width_t,
+                          size_t height_t, double pixelSizeX, double pixelSizeY,
+                          double l_shift, double m_shift, size_t nthreads,
+                          double epsilon = 1e-4, size_t verbosity = 0,
+                          bool tuning = false) {
+    wgpu_detail::check(wgpu_gridder_create(
+        width, height, width_t, height_t, pixelSizeX, pixelSizeY, l_shift, m_shift,
+        nthreads, epsilon, verbosity, tuning ? 1 : 0, (int)sizeof(NumT), &g_));
+    width_ = width;
+    height_ = height;
+  }
+  ~WGriddingGridder_Simple() override { wgpu_gridder_destroy(g_); }
+  WGriddingGridder_Simple(const WGriddingGridder_Simple &) = delete;
+  WGriddingGridder_Simple &operator=(const WGriddingGridder_Simple &) = delete;
+
+  size_t ConstantMemoryUsage() const override { return wgpu_gridder_constant_memory(g_); }
+  size_t PerVisibilityMemoryUsage() const override {
+    return wgpu_gridder_per_visibility_memory(g_);
+  }
+  void InitializeInversion() override {
+    wgpu_detail::check(wgpu_gridder_initialize_inversion(g_));
+  }
+  void AddInversionData(size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+                        const std::complex<float> *vis) override {
+    wgpu_detail::check(wgpu_gridder_add_inversion_data(
+        g_, n_rows, n_chan, uvw, freq, reinterpret_cast<const float *>(vis)));
+  }
+
+  /* gridder_simple_implementation.h:92-110.  The device cannot call back into
+   * MsGridder, so the gridder's cached solution table is read once and the
+   * per-row corrections run on the GPU (kernel K7). */
+  void AddInversionDataWithCorrectionCallback(
+      GainMode mode, size_t n_polarizations, size_t n_rows, const double *uvws,
+      const double *frequencies, size_t n_channels,
+      const aocommon::BandData &selected_band,
+      const std::pair<size_t, size_t> *antennas,
+      const std::complex<float> *visibilities, const size_t *time_offsets,
+      MsGridder *gridder, size_t n_antenna) override {
+    (void)selected_band;
+#ifdef WGPU_WITH_WSCLEAN
+    const GpuCorrectionTable table = gridder->GpuCorrections();
+    AddInversionDataWithCorrections(mode, n_polarizations, n_rows, uvws, frequencies,
+                                    n_channels, antennas, visibilities, time_offsets, table,
+                                    n_antenna);
+#else
+    (void)mode; (void)n_polarizations; (void)n_rows; (void)uvws; (void)frequencies;
+    (void)n_channels; (void)antennas; (void)visibilities; (void)time_offsets;
+    (void)gridder; (void)n_antenna;
+    throw std::runtime_error(
+        "wgpu: the correction callback needs WSClean's MsGridder (build with "
+        "WGPU_WITH_WSCLEAN) or AddInversionDataWithCorrections with a solution table");
+#endif
+  }
+
+  /* The same with the solution table passed explicitly. */
+  void AddInversionDataWithCorrections(GainMode mode, size_t n_polarizations, size_t n_rows,
+                                       const double *uvws, const double *frequencies,
+                                       size_t n_channels,
+                                       const std::pair<size_t, size_t> *antennas,
+                                       const std::complex<float> *visibilities,
+                                       const size_t *time_offsets,
+                                       const GpuCorrectionTable &table, size_t n_antenna) {
+    static_assert(sizeof(std::pair<size_t, size_t>) == 2 * sizeof(uint64_t),
+                  "antenna pairs are passed as two 64-bit indices");
+    wgpu_detail::check(wgpu_gridder_add_inversion_data_corrected(
+        g_, static_cast<int>(mode), n_polarizations, n_rows, uvws, frequencies, n_channels,
+        reinterpret_cast<const uint64_t *>(antennas),
+        reinterpret_cast<const float *>(visibilities),
+        reinterpret_cast<const uint64_t *>(time_offsets),
+        reinterpret_cast<const float *>(table.solutions), table.nparms, table.n_times,
+        n_antenna, table.polarization));
+  }
+
+  void FinalizeImage(double multiplicationFactor) override {
+    wgpu_detail::check(wgpu_gridder_finalize_image(g_, multiplicationFactor));
+  }
+  std::vector<float> RealImage() override {
+    std::vector<float> image(width_ * height_);
+    wgpu_detail::check(wgpu_gridder_real_image(g_, image.data()));
+    return image;
+  }
+  void InitializePrediction(const float *image_data) override {
+    wgpu_detail::check(wgpu_gridder_initialize_prediction(g_, image_data));
+  }
+  void PredictVisibilities(size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+                           std::complex<float> *vis) const override {
+    wgpu_detail::check(wgpu_gridder_predict_visibilities(g_, n_rows, n_chan, uvw, freq,
+                                                         reinterpret_cast<float *>(vis)));
+  }
+
+  wgpu_gridder_t *handle() const { return g_; }
+
+ private:
+  wgpu_gridder_t *g_ = nullptr;
+  size_t width_ = 0, height_ = 0;
+};
+
+}  // namespace wsclean
+
+#endif  // WGPU_GRIDDER_H_

@@ -1,0 +1,79 @@
+// Drives the C++ drop-in class (include/wgpu_gridder.h) the way WSClean's
+// WGriddingMSGridder does: construct, InitializeInversion, AddInversionData
+// in chunks, FinalizeImage, RealImage, InitializePrediction,
+// PredictVisibilities.  Inputs are read from and outputs written to raw
+// binary files given on the command line; the Python test compares them with
+// the oracle.
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "wgpu_gridder.h"
+
+template <typename T>
+static std::vector<T> read_file(const char *path, size_t n) {
+  std::vector<T> v(n);
+  FILE *f = std::fopen(path, "rb");
+  if (!f || std::fread(v.data(), sizeof(T), n, f) != n) {
+    std::fprintf(stderr, "cannot read %s\n", path);
+    std::exit(2);
+  }
+  std::fclose(f);
+  return v;
+}
+
+template <typename T>
+static void write_file(const std::string &path, const std::vector<T> &v) {
+  FILE *f = std::fopen(path.c_str(), "wb");
+  std::fwrite(v.data(), sizeof(T), v.size(), f);
+  std::fclose(f);
+}
+
+int main(int argc, char **argv) {
+  if (argc != 12) {
+    std::fprintf(stderr,
+                 "usage: adapter_test width width_t n_rows n_chan dl eps uvw freq vis model out_prefix\n");
+    return 2;
+  }
+  const size_t W = std::atoi(argv[1]), Wt = std::atoi(argv[2]);
+  const size_t n_rows = std::atoi(argv[3]), n_chan = std::atoi(argv[4]);
+  const double dl = std::atof(argv[5]), eps = std::atof(argv[6]);
+  auto uvw = read_file<double>(argv[7], 3 * n_rows);
+  auto freq = read_file<double>(argv[8], n_chan);
+  auto vis = read_file<std::complex<float>>(argv[9], n_rows * n_chan);
+  auto model = read_file<float>(argv[10], W * W);
+  std::string prefix = argv[11];
+  try {
+    wsclean::WGriddingGridder_Simple<double> g(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 4, eps);
+    wsclean::WGriddingGridderBase &base = g;
+    base.InitializeInversion();
+    const size_t half = n_rows / 2;
+    base.AddInversionData(half, n_chan, uvw.data(), freq.data(), vis.data());
+    base.AddInversionData(n_rows - half, n_chan, uvw.data() + 3 * half, freq.data(),
+                          vis.data() + half * n_chan);
+    base.FinalizeImage(1.0);
+    write_file(prefix + "image.bin", base.RealImage());
+    base.InitializePrediction(model.data());
+    std::vector<std::complex<float>> pred(n_rows * n_chan);
+    base.PredictVisibilities(n_rows, n_chan, uvw.data(), freq.data(), pred.data());
+    write_file(prefix + "pred.bin", pred);
+    // bad argument -> std::runtime_error, as the reference's MR_assert throws
+    bool threw = false;
+    try {
+      wsclean::WGriddingGridder_Simple<float> bad(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, eps, 3);
+    } catch (const std::runtime_error &) {
+      threw = true;
+    }
+    if (!threw) {
+      std::fprintf(stderr, "verbosity 3 was accepted\n");
+      return 1;
+    }
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    return 1;
+  }
+  std::printf("adapter ok\n");
+  return 0;
+}

@@ -1,0 +1,54 @@
+"""The C++ drop-in class (include/wgpu_gridder.h) compiled with g++ against
+the library and driven like WSClean drives WGriddingGridder_Simple."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from wsclean_gb300 import synthetic
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "adapter_test.cpp")
+
+
+def _build(tmp_path, wgpu_lib):
+    exe = str(tmp_path / "adapter_test")
+    lib_dir = os.path.join(ROOT, "wsclean_gb300", "_build")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
+           "-L", lib_dir, "-lwgpu", f"-Wl,-rpath,{lib_dir}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def test_adapter_compiles(tmp_path, wgpu_lib):
+    assert os.path.exists(_build(tmp_path, wgpu_lib))
+
+
+@pytest.mark.gpu
+def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
+    exe = _build(tmp_path, wgpu_lib)
+    W, Wt, dl, eps = 160, 128, 4e-4, 1e-5
+    uvw, freq, vis = synthetic.random_points(600, 4, Wt, dl, seed=41, w_scale=2.0,
+                                             frac_zero=0.05)
+    model = np.zeros((W, W), np.float32)
+    model[70, 60] = 1.0
+    model[90, 100] = -0.5
+    files = {}
+    for name, arr in dict(uvw=uvw, freq=freq, vis=vis.astype(np.complex64), model=model).items():
+        files[name] = str(tmp_path / f"{name}.bin")
+        np.ascontiguousarray(arr).tofile(files[name])
+    prefix = str(tmp_path / "out_")
+    r = subprocess.run([exe, str(W), str(Wt), str(uvw.shape[0]), str(freq.size), repr(dl),
+                        repr(eps), files["uvw"], files["freq"], files["vis"], files["model"],
+                        prefix], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    img = np.fromfile(prefix + "image.bin", np.float32).reshape(W, W)
+    d = (W - Wt) // 2
+    ref = oracle_lib.dft_invert(uvw, freq, vis, Wt, Wt, dl, dl).reshape(Wt, Wt)
+    got = img[d:d + Wt, d:d + Wt].astype(np.float64)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= eps
+    pred = np.fromfile(prefix + "pred.bin", np.complex64)
+    trimmed = model[d:d + Wt, d:d + Wt].ravel()
+    pr = oracle_lib.dft_predict(uvw, freq, trimmed, Wt, Wt, dl, dl)
+    assert np.linalg.norm(pred - pr) / np.linalg.norm(pr) <= eps
