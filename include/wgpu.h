@@ -239,6 +239,50 @@ int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
                       int32_t *ip, float *fu, float *fv, float *fw,
                       uint32_t *offsets, int64_t *n_out);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free bucketing                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference (ducc0 does its indexing internally).
+ *
+ * The bucketing pass of wgpu_bucket_debug for callers that cannot allocate
+ * device memory while calling into this library: for example a host that owns
+ * all device memory through its own pool, or a pipeline that must not trigger
+ * the device-wide synchronisation that cudaMalloc / cudaFree can cause.  The
+ * caller passes device inputs and device outputs; the scratch (sort keys,
+ * histograms, scan sums) lives in a static device array of
+ * wgpu_bucket_noalloc_scratch_bytes() bytes (about 17 MB) that every GPU
+ * loading the library holds until the process exits.  No cudaMalloc, cudaFree
+ * or allocating library routine is called.
+ *
+ * Limits: at most WGPU_NOALLOC_MAX_VISIBILITIES samples (n_rows * n_chan),
+ * WGPU_NOALLOC_MAX_CHANNELS channels and 2^26 (tile, plane) buckets; larger
+ * requests fail with WGPU_ERR_INVALID.
+ *
+ * Outputs: d_records receives one 32-byte record per bucketed sample in sorted
+ * order: float re, im (visibility times its shift phase, or the phase factor
+ * for prediction), float fu, fv, fw (footprint corner minus exact position),
+ * int32 iu, iv (wrapped footprint corner), int32 ip (first w plane); d_perm the
+ * element index (row * n_chan + chan) of each record; d_offsets the
+ * n_tiles * 4 * n_planes + 1 bucket offsets.  Size d_records and d_perm for
+ * n_rows * n_chan entries; *n_out receives the number written.
+ *
+ * The first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.  All calls
+ * share the array and it keeps the last call's contents: calls whose work
+ * overlaps on the GPU (different streams or host threads) race and must be
+ * serialised by the caller.  stream may be NULL (the legacy default stream). */
+#define WGPU_NOALLOC_MAX_VISIBILITIES (1 << 20)
+#define WGPU_NOALLOC_MAX_CHANNELS 4096
+
+int wgpu_bucket_noalloc(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                        const double *d_uvw, const double *d_freq,
+                        const float *d_vis, int skip_zero, void *d_records,
+                        uint32_t *d_perm, uint32_t *d_offsets, void *stream,
+                        int64_t *n_out);
+
+size_t wgpu_bucket_noalloc_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,9 @@ WGPU_ERR_NOMEM = -3
 WGPU_ERR_STATE = -4
 WGPU_ERR_TIMEOUT = -5
 
+NOALLOC_MAX_VISIBILITIES = 1 << 20
+NOALLOC_MAX_CHANNELS = 4096
+
 GAIN_XX, GAIN_YY, GAIN_TRACE, GAIN_2VIS_DIAGONAL, GAIN_FULL = range(5)
 POL_I, POL_Q, POL_U, POL_V, POL_XX, POL_XY, POL_YX, POL_YY = range(8)
 
@@ -83,6 +86,9 @@ _PROTOS = {
     "wgpu_kernel_launch_count": (C.c_uint64, []),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,
                               C.POINTER(C.c_int64)]),
+    "wgpu_bucket_noalloc": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P,
+                                C.POINTER(C.c_int64)]),
+    "wgpu_bucket_noalloc_scratch_bytes": (SZ, []),
 }
 
 

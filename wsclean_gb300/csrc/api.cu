@@ -748,3 +748,27 @@ int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
 }
 
 }  // extern "C"
+
+extern "C" {
+
+size_t wgpu_bucket_noalloc_scratch_bytes(void) { return bucket_noalloc_scratch_bytes(); }
+
+int wgpu_bucket_noalloc(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                        const double *d_uvw, const double *d_freq, const float *d_vis,
+                        int skip_zero, void *d_records, uint32_t *d_perm, uint32_t *d_offsets,
+                        void *stream, int64_t *n_out) {
+  if (!plan || !n_out) return fail(WGPU_ERR_INVALID, "null argument");
+  if ((n_rows && n_chan) && (!d_uvw || !d_freq || !d_records || !d_perm))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  if (!d_offsets) return fail(WGPU_ERR_INVALID, "null offsets pointer");
+  if (skip_zero && !d_vis && n_rows && n_chan)
+    return fail(WGPU_ERR_INVALID, "inversion bucketing needs the visibilities");
+  return guarded([&] {
+    const DevPlan dp = to_dev_plan(*plan);
+    *n_out = bucket_visibilities_noalloc(dp, d_uvw, d_freq, d_vis, (int64_t)n_rows,
+                                         (int64_t)n_chan, skip_zero != 0, (VisRecord *)d_records,
+                                         d_perm, d_offsets, (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"

@@ -14,6 +14,8 @@
 // bucketing reference in oracle/wgpu_oracle.c.
 #include <cub/cub.cuh>
 
+#include <mutex>
+
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -397,6 +399,135 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     check_launch("record_kernel");
   }
   return res;
+}
+
+
+// ---------------------------------------------------------------------------
+// Allocation-free bucketing.
+//
+// Some callers cannot allocate device memory while they call this library: a
+// host that owns the whole device memory through its own pool, code running
+// under a memory budget that forbids new allocations, or a pipeline that must
+// not trigger the device-wide synchronisation a cudaMalloc / cudaFree may
+// cause.  For them the bucketing pass keeps its scratch (sort keys and values
+// in two copies, per-block digit histograms, scan partial sums, channel
+// scales) in the file-scope device array below, sized for at most
+// kNoallocMaxVis visibilities and kNoallocMaxChan channels.  Every GPU that
+// loads the library holds this array until the process exits.  Its address is
+// looked up once per device (cudaGetSymbolAddress, with that device current)
+// on the first call made on the device.  All calls share the array and it keeps
+// the contents of the last call: calls whose work overlaps on the GPU (other
+// streams, other host threads) race with each other and must be serialised by
+// the caller.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int64_t kNoallocMaxVis = WGPU_NOALLOC_MAX_VISIBILITIES;
+constexpr int64_t kNoallocMaxChan = WGPU_NOALLOC_MAX_CHANNELS;
+constexpr int64_t kNoallocMaxKeys = (int64_t)1 << 26;
+constexpr int64_t kNoallocBlocks = (kNoallocMaxVis + kSortTile - 1) / kSortTile;
+constexpr size_t kNoallocScanWords = ((kNoallocMaxKeys + 1) / 4096 + 64 + 255) / 256 * 256;
+constexpr size_t kNoallocSortBytes = 4 * sizeof(uint32_t) * kNoallocMaxVis;
+constexpr size_t kNoallocHistBytes = sizeof(uint32_t) * 256 * kNoallocBlocks;
+constexpr size_t kNoallocScanBytes = sizeof(uint32_t) * kNoallocScanWords;
+constexpr size_t kNoallocScaleBytes = (sizeof(ChannelScale) * kNoallocMaxChan + 255) / 256 * 256;
+constexpr size_t kNoallocBytes =
+    kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes + kNoallocScaleBytes;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_bucket_scratch[kNoallocBytes];
+
+size_t bucket_noalloc_scratch_bytes() { return kNoallocBytes; }
+
+// Device address of g_bucket_scratch for the current device, looked up once.
+static unsigned char *bucket_scratch_address() {
+  static std::mutex mu;
+  static unsigned char *addr[256] = {};
+  int dev = 0;
+  WGPU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) throw Error(WGPU_ERR_CUDA, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_bucket_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      throw Error(WGPU_ERR_CUDA, std::string("cudaGetSymbolAddress of the bucketing scratch: ") +
+                                     cudaGetErrorString(e));
+    }
+    addr[dev] = (unsigned char *)p;
+  }
+  return addr[dev];
+}
+
+int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const double *d_freq,
+                                    const float *d_vis, int64_t n_rows, int64_t n_chan,
+                                    bool skip_zero, VisRecord *d_records, uint32_t *d_perm,
+                                    uint32_t *d_offsets, cudaStream_t s) {
+  const int64_t n = n_rows * n_chan;
+  if (n > kNoallocMaxVis)
+    throw Error(WGPU_ERR_INVALID, "allocation-free bucketing takes at most " +
+                                      std::to_string(kNoallocMaxVis) + " visibilities, got " +
+                                      std::to_string(n));
+  if (n_chan > kNoallocMaxChan)
+    throw Error(WGPU_ERR_INVALID, "allocation-free bucketing takes at most " +
+                                      std::to_string(kNoallocMaxChan) + " channels");
+  const int64_t n_keys = (int64_t)p.ntu * p.ntv * 4 * p.n_planes;
+  if (n_keys > kNoallocMaxKeys)
+    throw Error(WGPU_ERR_INVALID, "plan has too many (tile, plane) buckets for the "
+                                  "allocation-free bucketing");
+  int bits = 1;
+  while (((int64_t)1 << bits) - 1 < n_keys) ++bits;
+  const uint32_t sentinel = (uint32_t)(((uint64_t)1 << bits) - 1);
+
+  unsigned char *base = bucket_scratch_address();
+  uint32_t *keys = (uint32_t *)base;
+  uint32_t *keys2 = keys + kNoallocMaxVis;
+  uint32_t *vals = keys2 + kNoallocMaxVis;
+  uint32_t *vals2 = vals + kNoallocMaxVis;
+  uint32_t *hist = (uint32_t *)(base + kNoallocSortBytes);
+  uint32_t *scan_tmp = (uint32_t *)(base + kNoallocSortBytes + kNoallocHistBytes);
+  ChannelScale *cs =
+      (ChannelScale *)(base + kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes);
+
+  const double gu = p.dl * (double)p.nu, gv = p.dm * (double)p.nv;
+  if (n_chan > 0) {
+    channel_scales_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, n_chan, gu, gv, cs);
+    check_launch("channel_scales_kernel");
+  }
+  // the histogram accumulates into the caller's offsets: start from zero
+  WGPU_CUDA(cudaMemsetAsync(d_offsets, 0, sizeof(uint32_t) * (n_keys + 1), s));
+  if (n > 0) {
+    key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
+        p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, nullptr}, n_rows,
+        n_chan, sentinel, keys, vals, d_offsets);
+    check_launch("key_kernel");
+  }
+  exclusive_scan_u32_scratch(d_offsets, n_keys + 1, scan_tmp, s);
+  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
+  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+  for (int shift = 0; shift < bits && n > 0; shift += 8) {
+    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, n, shift, hist, n_blocks);
+    check_launch("radix_hist_kernel");
+    exclusive_scan_u32_scratch(hist, 256 * n_blocks, scan_tmp, s);
+    radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, vin, n, shift, hist,
+                                                                 n_blocks, kout, vout);
+    check_launch("radix_scatter_kernel");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  uint32_t total = 0;
+  WGPU_CUDA(cudaMemcpyAsync(&total, d_offsets + n_keys, sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  if (total > 0) {
+    WGPU_CUDA(cudaMemcpyAsync(d_perm, vin, sizeof(uint32_t) * total, cudaMemcpyDeviceToDevice, s));
+    record_kernel<<<grid_for(total, kThreads), kThreads, 0, s>>>(
+        p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan, vin, total,
+        d_records);
+    check_launch("record_kernel");
+  }
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  return total;
 }
 
 }  // namespace wgpu

@@ -170,4 +170,18 @@ void exclusive_scan_u32(DeviceArena &arena, uint32_t *d, int64_t n,
   scan_level(d, n, tmp, s);
 }
 
+int64_t exclusive_scan_scratch_words(int64_t n) {
+  int64_t need = 0, m = n;
+  while (m > kScanChunk) {
+    m = (m + kScanChunk - 1) / kScanChunk;
+    need += m;
+  }
+  return need + 16;
+}
+
+void exclusive_scan_u32_scratch(uint32_t *d, int64_t n, uint32_t *tmp, cudaStream_t s) {
+  if (n <= 0) return;
+  scan_level(d, n, tmp, s);
+}
+
 }  // namespace wgpu

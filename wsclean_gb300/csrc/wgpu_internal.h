@@ -89,6 +89,13 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  int64_t n_rows, int64_t n_chan, bool skip_zero,
                                  cudaStream_t s);
 
+// Bucketing with scratch in a static device array (no device allocation).
+size_t bucket_noalloc_scratch_bytes();
+int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const double *d_freq,
+                                    const float *d_vis, int64_t n_rows, int64_t n_chan,
+                                    bool skip_zero, VisRecord *d_records, uint32_t *d_perm,
+                                    uint32_t *d_offsets, cudaStream_t s);
+
 // ---- gridding (grid.cu) ----
 class DeviceArena;
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
@@ -207,5 +214,9 @@ enum ArenaSlot {
 // Exclusive scan of n uint32 values in place (device), returning the total.
 void exclusive_scan_u32(DeviceArena &arena, uint32_t *d, int64_t n,
                         cudaStream_t s);
+// Same with caller-provided scratch of exclusive_scan_scratch_words(n) words.
+int64_t exclusive_scan_scratch_words(int64_t n);
+void exclusive_scan_u32_scratch(uint32_t *d, int64_t n, uint32_t *tmp,
+                                cudaStream_t s);
 
 }  // namespace wgpu
