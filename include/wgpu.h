@@ -200,6 +200,34 @@ int wgpu_gridder_predict_visibilities_masked_device(
     wgpu_gridder_t *gridder, size_t n_rows, size_t n_chan, const double *d_uvw,
     const double *d_freq, const uint8_t *d_mask, float *d_vis);
 
+/* ------------------------------------------------------------------------ */
+/* Bound visibility sets: state kept on the device across major cycles        */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference, where every AddInversionData /
+ * PredictVisibilities call re-plans and re-indexes its data inside ducc0.
+ * WSClean's major cycles grid and predict the same rows (same uvw, same
+ * flags) again and again; bind copies uvw / freq / mask to the device once,
+ * plans, buckets, lays out the work items and captures the inversion and the
+ * prediction pipelines in CUDA graphs.  Each later cycle only moves the
+ * visibilities and replays a graph.  mask ([row * n_chan + chan], may be
+ * NULL = every sample) selects the samples that take part; unselected samples
+ * are predicted as 0 and ignored by the inversion.  The bound set lives until
+ * unbind, a new bind or destroy.
+ *   invert_bound:  adds the dirty image of `vis` to the accumulated image
+ *                  (after InitializeInversion), like AddInversionData.
+ *   predict_bound: predicts the bound samples from the image set by
+ *                  InitializePrediction, like PredictVisibilities. */
+int wgpu_gridder_bind(wgpu_gridder_t *gridder, size_t n_rows, size_t n_chan,
+                      const double *uvw, const double *freq,
+                      const uint8_t *mask);
+int wgpu_gridder_unbind(wgpu_gridder_t *gridder);
+int wgpu_gridder_invert_bound(wgpu_gridder_t *gridder, const float *vis);
+int wgpu_gridder_invert_bound_device(wgpu_gridder_t *gridder,
+                                     const float *d_vis);
+int wgpu_gridder_predict_bound(wgpu_gridder_t *gridder, float *vis);
+int wgpu_gridder_predict_bound_device(wgpu_gridder_t *gridder, float *d_vis);
+
 /* Plan used by the last inversion/prediction call of this gridder. */
 int wgpu_gridder_last_plan(const wgpu_gridder_t *gridder, wgpu_plan_t *plan);
 

@@ -246,3 +246,62 @@ def test_corrected_inversion_rejects_bad_indices(wgpu_lib):
         g.AddInversionDataWithCorrectionCallback("full", 1, 4, uvw, freq, 2, ant, vis,
                                                  np.zeros(4, np.uint64), sol, 2, 1, 3)
     g.close()
+
+
+def test_bound_cycles_match_unbound_calls(wgpu_lib, oracle_lib):
+    """Device-resident state across major cycles: bind once, then grid and
+    predict twice through the captured graphs; each result equals the plain
+    per-call path (same plan) and the DFT within epsilon."""
+    W, dl, eps = 192, 3e-4, 1e-5
+    uvw, freq, vis1 = synthetic.random_points(900, 6, W, dl, seed=51, w_scale=2.0)
+    _, _, vis2 = synthetic.random_points(900, 6, W, dl, seed=52, w_scale=2.0)
+    rng = np.random.default_rng(9)
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, 25, replace=False)] = rng.uniform(-1, 1, 25)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.002, -0.001, 1, epsilon=eps,
+                                num_t=np.float64)
+    g.Bind(uvw.shape[0], freq.size, uvw, freq)
+    bound_plan = g.last_plan()
+    ref_g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.002, -0.001, 1, epsilon=eps,
+                                    num_t=np.float64)
+    ref_g.pin_plan(bound_plan)
+    for cycle, vis in enumerate((vis1, vis2, vis1)):
+        g.InitializeInversion()
+        g.InvertBound(vis)
+        img = g.RealImage().astype(np.float64)
+        ref_g.InitializeInversion()
+        ref_g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+        assert rel(img, ref_g.RealImage()) <= 2e-6, cycle
+        if cycle < 2:
+            dft = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, 0.002, -0.001)
+            assert rel(img, dft) <= eps
+        g.InitializePrediction(model)
+        pv = g.PredictBound()
+        ref_g.InitializePrediction(model)
+        pr = ref_g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq)
+        assert rel(pv, pr) <= 2e-6, cycle
+    g.close()
+    ref_g.close()
+
+
+def test_bound_mask_selects_samples(wgpu_lib):
+    W, dl = 128, 4e-4
+    uvw, freq, vis = synthetic.random_points(500, 4, W, dl, seed=53, w_scale=1.0)
+    mask = (np.random.default_rng(2).uniform(size=vis.shape) > 0.3).astype(np.uint8)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=1e-4)
+    g.Bind(uvw.shape[0], freq.size, uvw, freq, mask)
+    g.InitializeInversion()
+    g.InvertBound(vis)
+    img = g.RealImage()
+    g.pin_plan(g.last_plan())
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, np.where(mask > 0, vis, 0))
+    assert rel(img, g.RealImage()) <= 2e-6
+    model = np.zeros(W * W, np.float32)
+    model[1234] = 1.0
+    g.InitializePrediction(model)
+    pv = g.PredictBound().reshape(vis.shape)
+    assert np.all(pv[mask == 0] == 0)
+    pm = g.PredictVisibilitiesMasked(uvw.shape[0], freq.size, uvw, freq, mask).reshape(vis.shape)
+    assert rel(pv, pm) <= 2e-6
+    g.close()

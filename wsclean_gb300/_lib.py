@@ -82,6 +82,12 @@ _PROTOS = {
     "wgpu_gridder_last_timings": (I, [P, C.POINTER(C.c_double), C.POINTER(I), I, C.c_char_p,
                                       SZ, C.POINTER(I)]),
     "wgpu_gridder_pin_plan": (I, [P, C.POINTER(Plan)]),
+    "wgpu_gridder_bind": (I, [P, SZ, SZ, P, P, P]),
+    "wgpu_gridder_unbind": (I, [P]),
+    "wgpu_gridder_invert_bound": (I, [P, P]),
+    "wgpu_gridder_invert_bound_device": (I, [P, P]),
+    "wgpu_gridder_predict_bound": (I, [P, P]),
+    "wgpu_gridder_predict_bound_device": (I, [P, P]),
     "wgpu_gridder_stream": (P, [P]),
     "wgpu_kernel_launch_count": (C.c_uint64, []),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,

@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,41 @@ struct StageTimer {
   }
 };
 
+// Device-resident state of a bound visibility set (see wgpu_gridder_bind):
+// bucketing, work items, buffers and the captured inversion / prediction
+// graphs, all owned here so that later unbound calls cannot move them.
+struct BoundState {
+  wgpu_plan_t plan;
+  wgpu::DevPlan dp;
+  int64_t n_rows = 0, n_chan = 0, n_out = 0;
+  std::vector<void *> owned;
+  double *uvw = nullptr, *freq = nullptr, *nu_w = nullptr;
+  uint8_t *mask = nullptr;
+  wgpu::VisRecord *geom = nullptr, *work = nullptr;
+  uint32_t *perm = nullptr, *offsets = nullptr;
+  float2 *vis_in = nullptr, *vis_out = nullptr, *vacc = nullptr;
+  float2 *planes = nullptr, *rows = nullptr, *acc = nullptr;
+  float *img_corr = nullptr, *cx = nullptr, *cy = nullptr, *gl = nullptr;
+  std::vector<wgpu::WorkItems> gitems, ditems;
+  cudaGraph_t ginv = nullptr, gpred = nullptr;
+  cudaGraphExec_t xinv = nullptr, xpred = nullptr;
+  uint64_t inv_kernels = 0, pred_kernels = 0;
+
+  void *alloc(size_t bytes) {
+    void *p = nullptr;
+    WGPU_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+    owned.push_back(p);
+    return p;
+  }
+  ~BoundState() {
+    if (xinv) cudaGraphExecDestroy(xinv);
+    if (xpred) cudaGraphExecDestroy(xpred);
+    if (ginv) cudaGraphDestroy(ginv);
+    if (gpred) cudaGraphDestroy(gpred);
+    for (void *p : owned) cudaFree(p);
+  }
+};
+
 struct wgpu_gridder {
   size_t width, height, width_t, height_t, nthreads, verbosity;
   double dl, dm, l_shift, m_shift, epsilon;
@@ -105,6 +141,7 @@ struct wgpu_gridder {
   StageTimer timer;
   std::vector<StageTimer::Stage> last_timings;
   std::string corr_key;  // geometry of the correction tables in the arena
+  std::unique_ptr<BoundState> bound;
 };
 
 namespace wgpu {
@@ -358,6 +395,178 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->last_timings = g->timer.collect();
 }
 
+// ---- bound visibility sets: plan and bucket once, replay captured graphs ----
+
+void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const double *h_uvw,
+                       const double *h_freq, const uint8_t *h_mask) {
+  g->bound.reset();
+  if (n_rows == 0 || n_chan == 0) throw Error(WGPU_ERR_INVALID, "empty visibility set");
+  cudaStream_t s = g->stream;
+  ensure_image(g);
+  auto b = std::make_unique<BoundState>();
+  const int64_t n = (int64_t)(n_rows * n_chan);
+  b->n_rows = (int64_t)n_rows;
+  b->n_chan = (int64_t)n_chan;
+  b->uvw = (double *)b->alloc(sizeof(double) * 3 * n_rows);
+  b->freq = (double *)b->alloc(sizeof(double) * n_chan);
+  WGPU_CUDA(cudaMemcpyAsync(b->uvw, h_uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(b->freq, h_freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
+  if (h_mask) {
+    b->mask = (uint8_t *)b->alloc((size_t)n);
+    WGPU_CUDA(cudaMemcpyAsync(b->mask, h_mask, (size_t)n, cudaMemcpyHostToDevice, s));
+  }
+  double w_min, w_max;
+  int64_t count;
+  compute_w_extent(b->uvw, b->freq, nullptr, b->mask, b->n_rows, b->n_chan, false, &w_min,
+                   &w_max, &count, g->arena.get(kSlotErr, 64), s);
+  if (count == 0) throw Error(WGPU_ERR_INVALID, "the mask selects no visibility");
+  b->plan = plan_for(g, w_min, w_max, count);
+  g->last_plan = b->plan;
+  log_plan(g, "bind", b->plan, count);
+  const wgpu_plan_t &plan = b->plan;
+  b->dp = to_dev_plan(plan);
+  const DevPlan &dp = b->dp;
+  const BucketResult br = bucket_visibilities(g->arena, dp, b->uvw, b->freq, nullptr, b->mask,
+                                              b->n_rows, b->n_chan, false, s);
+  b->n_out = br.n_out;
+  b->geom = (VisRecord *)b->alloc(sizeof(VisRecord) * (br.n_out + 1));
+  b->work = (VisRecord *)b->alloc(sizeof(VisRecord) * (br.n_out + 1));
+  b->perm = (uint32_t *)b->alloc(sizeof(uint32_t) * (br.n_out + 1));
+  b->offsets = (uint32_t *)b->alloc(sizeof(uint32_t) * (br.n_keys + 1));
+  WGPU_CUDA(cudaMemcpyAsync(b->geom, br.records, sizeof(VisRecord) * br.n_out,
+                            cudaMemcpyDeviceToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(b->perm, br.perm, sizeof(uint32_t) * br.n_out,
+                            cudaMemcpyDeviceToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(b->offsets, br.offsets, sizeof(uint32_t) * (br.n_keys + 1),
+                            cudaMemcpyDeviceToDevice, s));
+  const int64_t npix = plan.width * plan.height;
+  const int rstride = (int)((plan.width + 31) / 32 * 32);
+  const int64_t B = plan.plane_batch;
+  b->vis_in = (float2 *)b->alloc(sizeof(float2) * n);
+  b->vis_out = (float2 *)b->alloc(sizeof(float2) * n);
+  b->vacc = (float2 *)b->alloc(sizeof(float2) * (br.n_out + 1));
+  b->planes = (float2 *)b->alloc(sizeof(float2) * B * plan.nu * plan.nv);
+  b->rows = (float2 *)b->alloc(sizeof(float2) * B * plan.nv * rstride);
+  b->acc = (float2 *)b->alloc(sizeof(float2) * npix);
+  b->nu_w = (double *)b->alloc(sizeof(double) * npix);
+  b->img_corr = (float *)b->alloc(sizeof(float) * npix);
+  b->cx = (float *)b->alloc(sizeof(float) * plan.width);
+  b->cy = (float *)b->alloc(sizeof(float) * plan.height);
+  b->gl = (float *)b->alloc(sizeof(float) * 2 * kGlNodes);
+  launch_nu_table(dp, b->nu_w, s);
+  float *cx, *cy, *gl;
+  upload_corrections(g, plan, &cx, &cy, &gl);
+  WGPU_CUDA(cudaMemcpyAsync(b->cx, cx, sizeof(float) * plan.width, cudaMemcpyDeviceToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(b->cy, cy, sizeof(float) * plan.height, cudaMemcpyDeviceToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(b->gl, gl, sizeof(float) * 2 * kGlNodes, cudaMemcpyDeviceToDevice, s));
+  // twiddle tables are created outside the capture (they are copied synchronously)
+  fft_twiddles(*g->fft, (int)plan.nu);
+  fft_twiddles(*g->fft, (int)plan.nv);
+  fft_twiddles(*g->fft, (int)plan.fft_n1);
+  fft_twiddles(*g->fft, (int)plan.fft_n2);
+  BoundState *bp = b.get();
+  const ItemAlloc own = [bp](int, size_t bytes) -> void * { return bp->alloc(bytes); };
+  for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
+    const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+    b->gitems.push_back(plan_grid_items(dp, b->offsets, (int)p0, nb, nullptr, own, s));
+    b->ditems.push_back(plan_degrid_items(dp, b->offsets, (int)p0, nb, own, s));
+  }
+  WGPU_CUDA(cudaStreamSynchronize(s));
+
+  // inversion graph: records from the new visibilities, then the batches
+  uint64_t k0 = launch_count();
+  WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    launch_restamp(b->geom, b->perm, b->vis_in, b->n_out, b->work, s);
+    WGPU_CUDA(cudaMemsetAsync(b->acc, 0, sizeof(float2) * npix, s));
+    for (size_t i = 0; i < b->gitems.size(); ++i) {
+      const int p0 = (int)(i * B);
+      const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+      launch_zero_split_units(dp, b->gitems[i], p0, nb, b->planes, s);
+      launch_grid_items(dp, b->work, b->offsets, p0, nb, b->gitems[i], b->planes, s);
+      launch_fft_rows_forward_crop(*g->fft, dp, b->planes, b->rows, rstride, nb, s);
+      launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
+                        -1.0f, s);
+      launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                           b->rows, rstride, nb, p0, b->nu_w, b->acc, s);
+    }
+    launch_finalize_add(dp, b->acc, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, g->d_img, g->prec, s);
+  } catch (...) {
+    cudaGraph_t junk;
+    cudaStreamEndCapture(s, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
+  WGPU_CUDA(cudaStreamEndCapture(s, &b->ginv));
+  WGPU_CUDA(cudaGraphInstantiate(&b->xinv, b->ginv, 0));
+  b->inv_kernels = launch_count() - k0;
+  count_launch(-(int)b->inv_kernels);  // captured, not run
+
+  // prediction graph: pre-correction, the batches, un-permute
+  k0 = launch_count();
+  WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    launch_precorrect(dp, g->d_img, g->prec, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, b->img_corr, s);
+    WGPU_CUDA(cudaMemsetAsync(b->vacc, 0, sizeof(float2) * (b->n_out + 1), s));
+    for (size_t i = 0; i < b->ditems.size(); ++i) {
+      const int p0 = (int)(i * B);
+      const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+      launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                        b->img_corr, b->nu_w, b->rows, rstride, nb, p0, s);
+      launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
+                        +1.0f, s);
+      launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, s);
+      launch_degrid_items(dp, b->geom, b->offsets, p0, nb, b->ditems[i], b->planes, b->vacc, s);
+    }
+    WGPU_CUDA(cudaMemsetAsync(b->vis_out, 0, sizeof(float2) * n, s));
+    launch_unpermute_predict(b->geom, b->perm, b->vacc, b->n_out, b->vis_out, s);
+  } catch (...) {
+    cudaGraph_t junk;
+    cudaStreamEndCapture(s, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
+  WGPU_CUDA(cudaStreamEndCapture(s, &b->gpred));
+  WGPU_CUDA(cudaGraphInstantiate(&b->xpred, b->gpred, 0));
+  b->pred_kernels = launch_count() - k0;
+  count_launch(-(int)b->pred_kernels);
+  g->bound = std::move(b);
+}
+
+void invert_bound(wgpu_gridder *g, const float *vis, bool device) {
+  if (!g->bound) throw Error(WGPU_ERR_STATE, "no bound visibility set");
+  if (g->mode != wgpu_gridder::Mode::kInversion)
+    throw Error(WGPU_ERR_STATE, "bound inversion before InitializeInversion");
+  BoundState &b = *g->bound;
+  cudaStream_t s = g->stream;
+  g->timer.begin(s);
+  g->timer.mark("bound_invert");
+  WGPU_CUDA(cudaMemcpyAsync(b.vis_in, vis, sizeof(float2) * b.n_rows * b.n_chan,
+                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaGraphLaunch(b.xinv, s));
+  count_launch((int)b.inv_kernels);
+  g->timer.mark("end");
+  g->last_timings = g->timer.collect();
+  g->last_plan = b.plan;
+}
+
+void predict_bound(wgpu_gridder *g, float *vis, bool device) {
+  if (!g->bound) throw Error(WGPU_ERR_STATE, "no bound visibility set");
+  if (g->mode != wgpu_gridder::Mode::kPrediction)
+    throw Error(WGPU_ERR_STATE, "bound prediction before InitializePrediction");
+  BoundState &b = *g->bound;
+  cudaStream_t s = g->stream;
+  g->timer.begin(s);
+  g->timer.mark("bound_predict");
+  WGPU_CUDA(cudaGraphLaunch(b.xpred, s));
+  count_launch((int)b.pred_kernels);
+  WGPU_CUDA(cudaMemcpyAsync(vis, b.vis_out, sizeof(float2) * b.n_rows * b.n_chan,
+                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  g->timer.mark("end");
+  g->last_timings = g->timer.collect();
+  g->last_plan = b.plan;
+}
+
 template <typename T>
 T *upload(wgpu_gridder *g, int slot, const T *h, size_t n) {
   T *d = (T *)g->arena.get(slot, sizeof(T) * (n ? n : 1));
@@ -437,6 +646,7 @@ int wgpu_gridder_create(size_t width, size_t height, size_t width_t,
 void wgpu_gridder_destroy(wgpu_gridder_t *g) {
   if (!g) return;
   if (g->stream) cudaStreamSynchronize(g->stream);
+  g->bound.reset();
   g->arena.release();
   if (g->d_img) cudaFree(g->d_img);
   fft_tables_destroy(g->fft);
@@ -692,6 +902,47 @@ int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms, int *counts,
 void *wgpu_gridder_stream(wgpu_gridder_t *g) { return g ? (void *)g->stream : nullptr; }
 
 uint64_t wgpu_kernel_launch_count(void) { return launch_count(); }
+
+int wgpu_gridder_bind(wgpu_gridder_t *g, size_t n_rows, size_t n_chan, const double *uvw,
+                      const double *freq, const uint8_t *mask) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if (!uvw || !freq) return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] { bind_visibilities(g, n_rows, n_chan, uvw, freq, mask); });
+}
+
+int wgpu_gridder_unbind(wgpu_gridder_t *g) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  return guarded([&] {
+    if (g->stream) WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    g->bound.reset();
+  });
+}
+
+int wgpu_gridder_invert_bound(wgpu_gridder_t *g, const float *vis) {
+  if (!g || !vis) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] {
+    invert_bound(g, vis, false);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_invert_bound_device(wgpu_gridder_t *g, const float *d_vis) {
+  if (!g || !d_vis) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] { invert_bound(g, d_vis, true); });
+}
+
+int wgpu_gridder_predict_bound(wgpu_gridder_t *g, float *vis) {
+  if (!g || !vis) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] {
+    predict_bound(g, vis, false);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int wgpu_gridder_predict_bound_device(wgpu_gridder_t *g, float *d_vis) {
+  if (!g || !d_vis) return fail(WGPU_ERR_INVALID, "null argument");
+  return guarded([&] { predict_bound(g, d_vis, true); });
+}
 
 int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
                       const double *uvw, const double *freq, const float *vis,

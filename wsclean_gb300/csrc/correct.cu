@@ -251,3 +251,33 @@ void launch_scale_image(void *img, int precision_bytes, int64_t n, double factor
   check_launch("scale_kernel");
 }
 }  // namespace wgpu
+
+namespace wgpu {
+namespace {
+// Inversion records from stored prediction records: the geometry is kept and
+// (re, im) becomes visibility x phase factor, the product the bucketing pass
+// forms for inversion.
+__global__ void restamp_kernel(const VisRecord *__restrict__ geom,
+                               const uint32_t *__restrict__ perm,
+                               const float2 *__restrict__ vis, int64_t n,
+                               VisRecord *__restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(geom + s));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(geom + s) + 1);
+  const float2 v = __ldg(vis + perm[s]);
+  // phase factor (a.x, a.y) = exp(-2 pi i theta)
+  const float re = v.x * a.x - v.y * a.y;
+  const float im = v.x * a.y + v.y * a.x;
+  reinterpret_cast<float4 *>(out + s)[0] = make_float4(re, im, a.z, a.w);
+  reinterpret_cast<float4 *>(out + s)[1] = b;
+}
+}  // namespace
+
+void launch_restamp(const VisRecord *geom, const uint32_t *perm, const float2 *vis, int64_t n,
+                    VisRecord *out, cudaStream_t s) {
+  if (n <= 0) return;
+  restamp_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(geom, perm, vis, n, out);
+  check_launch("restamp_kernel");
+}
+}  // namespace wgpu

@@ -20,6 +20,8 @@
 // shared memory and gathers, for each visibility of its slice of the own
 // bucket, the W x W x (planes in the group) weighted sum, added to the
 // per-visibility accumulator.
+#include <algorithm>
+
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -426,62 +428,84 @@ int sm_count() {
   return n;
 }
 
-// Plans the work items of one batch: scanned item offsets (n_units + 1) and
-// the item -> unit descriptors.  Returns the number of items (one small
-// device-to-host read that sizes the launch).
+// Zeroes the cells of the gridding units that are split into several items
+// (their items add into the planes); one warp per unit.
 template <int T, int G>
-uint32_t plan_items(DeviceArena &arena, const DevPlan &p, const uint32_t *off, int p_begin,
-                    int n_batch, bool degrid, float2 *planes, uint32_t **item_off,
-                    uint32_t **desc, cudaStream_t s) {
+__global__ void __launch_bounds__(kThreads)
+    zero_split_units_kernel(DevPlan p, const uint32_t *__restrict__ item_off, int p_begin,
+                            int n_batch, int n_units, float2 *__restrict__ planes) {
+  const int unit = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (unit >= n_units) return;
+  if (item_off[unit + 1] - item_off[unit] <= 1) return;
+  const int n_tiles = p.ntu * p.ntv;
+  const int tile = unit % n_tiles, group = unit / n_tiles;
+  const int tu = tile % p.ntu, tv = tile / p.ntu;
+  const int q0 = p_begin + group * G;
+  const int q1 = min(q0 + G, p_begin + n_batch);
+  const size_t plane_elems = (size_t)p.nu * p.nv;
+  for (int c = lane; c < (q1 - q0) * T * T; c += 32) {
+    const int pq = c / (T * T), rem = c - pq * T * T;
+    const int row = rem / T, col = rem - row * T;
+    planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
+           tu * T + col] = make_float2(0.f, 0.f);
+  }
+}
+
+// Plans the work items of one batch: scanned item offsets (n_units + 1) and
+// the item -> unit descriptors, in buffers from `alloc`.  The number of items
+// sizes the launch (one small device-to-host read).  With `planes` the split
+// gridding units are zeroed as well.
+template <int T, int G>
+WorkItems plan_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
+                     bool degrid, float2 *planes, const ItemAlloc &alloc, cudaStream_t s) {
+  WorkItems wi;
   const int n_groups = (n_batch + G - 1) / G;
-  const int n_units = p.ntu * p.ntv * n_groups;
-  *item_off = (uint32_t *)arena.get(kSlotItems, sizeof(uint32_t) * (2 * (size_t)n_units + 4));
-  uint32_t *counts = *item_off + n_units + 2;
+  wi.n_units = p.ntu * p.ntv * n_groups;
+  wi.item_off = (uint32_t *)alloc(0, sizeof(uint32_t) * (2 * (size_t)wi.n_units + 4));
+  uint32_t *counts = wi.item_off + wi.n_units + 2;
   const int warps_per_block = kThreads / 32;
-  const unsigned blocks = (unsigned)((n_units + warps_per_block - 1) / warps_per_block);
-  grid_plan_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, off, p_begin, n_batch, n_units,
-                                                     degrid ? 1 : 0, *item_off, counts, planes);
+  const unsigned blocks = (unsigned)((wi.n_units + warps_per_block - 1) / warps_per_block);
+  grid_plan_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, off, p_begin, n_batch, wi.n_units,
+                                                     degrid ? 1 : 0, wi.item_off, counts,
+                                                     planes);
   check_launch("grid_plan_kernel");
-  WGPU_CUDA(cudaMemsetAsync(*item_off + n_units, 0, sizeof(uint32_t), s));
-  exclusive_scan_u32(arena, *item_off, n_units + 1, s);
+  WGPU_CUDA(cudaMemsetAsync(wi.item_off + wi.n_units, 0, sizeof(uint32_t), s));
+  uint32_t *tmp = (uint32_t *)alloc(2, sizeof(uint32_t) * exclusive_scan_scratch_words(wi.n_units + 1));
+  exclusive_scan_u32_scratch(wi.item_off, wi.n_units + 1, tmp, s);
   uint32_t total = 0;
-  WGPU_CUDA(cudaMemcpyAsync(&total, *item_off + n_units, sizeof(uint32_t),
+  WGPU_CUDA(cudaMemcpyAsync(&total, wi.item_off + wi.n_units, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
-  *desc = (uint32_t *)arena.get(kSlotItemDesc, sizeof(uint32_t) * ((size_t)total + 1));
-  fill_items_kernel<<<(n_units + 255) / 256, 256, 0, s>>>(*item_off, counts, n_units, *desc);
+  wi.total = total;
+  wi.desc = (uint32_t *)alloc(1, sizeof(uint32_t) * ((size_t)total + 1));
+  fill_items_kernel<<<(wi.n_units + 255) / 256, 256, 0, s>>>(wi.item_off, counts, wi.n_units,
+                                                              wi.desc);
   check_launch("fill_items_kernel");
-  return total;
+  return wi;
 }
 
 template <int T, int G, int W>
-void grid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
-                const uint32_t *off, int p_begin, int n_batch, float2 *planes,
-                cudaStream_t s) {
-  uint32_t *item_off, *desc;
-  const uint32_t total =
-      plan_items<T, G>(arena, p, off, p_begin, n_batch, false, planes, &item_off, &desc, s);
-  if (total == 0) return;
+void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
+                int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
+  if (wi.total == 0) return;
   const size_t smem = sizeof(float) * 2 * G * T * padded_stride(T, W);
   WGPU_CUDA(cudaFuncSetAttribute(grid_kernel<T, G, W>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G, W>,
                                                           kThreads, smem));
-  const uint32_t blocks = std::min<uint32_t>(total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
-  grid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch, item_off,
-                                                      desc, total, planes);
+  const uint32_t blocks = std::min<uint32_t>(wi.total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
+  grid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch,
+                                                      wi.item_off, wi.desc, wi.total, planes);
   check_launch("grid_kernel");
 }
 
 template <int T, int G, int W>
-void degrid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
-                  const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
-                  float2 *acc, cudaStream_t s) {
-  uint32_t *item_off, *desc;
-  const uint32_t total =
-      plan_items<T, G>(arena, p, off, p_begin, n_batch, true, nullptr, &item_off, &desc, s);
-  if (total == 0) return;
+void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
+                  int n_batch, const WorkItems &wi, const float2 *planes, float2 *acc,
+                  cudaStream_t s) {
+  if (wi.total == 0) return;
   constexpr int R = T + W - 1;
   const size_t smem = sizeof(float) * 2 * G * R * padded_stride(R, W);
   WGPU_CUDA(cudaFuncSetAttribute(degrid_kernel<T, G, W>,
@@ -489,64 +513,112 @@ void degrid_batch(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G, W>,
                                                           kThreads, smem));
-  const uint32_t blocks = std::min<uint32_t>(total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
+  const uint32_t blocks = std::min<uint32_t>(wi.total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
   degrid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch,
-                                                        item_off, desc, total, planes, acc);
+                                                        wi.item_off, wi.desc, wi.total, planes,
+                                                        acc);
   check_launch("degrid_kernel");
 }
 
-// Dispatch over the kernel support (4..16) for one tile shape.
+// Dispatch over the kernel support (4..16).
 template <int T, int G, int W = 4>
-void grid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
-                   const uint32_t *off, int p_begin, int n_batch, float2 *planes,
+void grid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                   int p_begin, int n_batch, const WorkItems &wi, float2 *planes,
                    cudaStream_t s) {
   if constexpr (W > kMaxSupport) {
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
-      grid_batch<T, G, W>(arena, p, rec, off, p_begin, n_batch, planes, s);
+      grid_items<T, G, W>(p, rec, off, p_begin, n_batch, wi, planes, s);
     else
-      grid_dispatch<T, G, W + 1>(support, arena, p, rec, off, p_begin, n_batch, planes, s);
+      grid_dispatch<T, G, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, s);
   }
 }
 
 template <int T, int G, int W = 4>
-void degrid_dispatch(int support, DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
-                     const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
+void degrid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                     int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
                      float2 *acc, cudaStream_t s) {
   if constexpr (W > kMaxSupport || (G > 8 && W > 8)) {
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
-      degrid_batch<T, G, W>(arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+      degrid_items<T, G, W>(p, rec, off, p_begin, n_batch, wi, planes, acc, s);
     else
-      degrid_dispatch<T, G, W + 1>(support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+      degrid_dispatch<T, G, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
   }
 }
+
+void check_plan(const DevPlan &p) {
+  if (p.support < 4 || p.support > kMaxSupport)
+    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
+  if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
+}
+
+int degrid_group(const DevPlan &p) { return p.support <= 8 ? 16 : 8; }
 
 }  // namespace
 
 int grid_plane_group() { return kGridPlanes; }
 
+WorkItems plan_grid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
+                          float2 *planes, const ItemAlloc &alloc, cudaStream_t s) {
+  check_plan(p);
+  return plan_items<kTile, kGridPlanes>(p, off, p_begin, n_batch, false, planes, alloc, s);
+}
+
+WorkItems plan_degrid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
+                            const ItemAlloc &alloc, cudaStream_t s) {
+  check_plan(p);
+  if (degrid_group(p) == 16)
+    return plan_items<kTile, 16>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
+  return plan_items<kTile, 8>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
+}
+
+void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
+                             float2 *planes, cudaStream_t s) {
+  const int warps_per_block = kThreads / 32;
+  const unsigned blocks = (unsigned)((wi.n_units + warps_per_block - 1) / warps_per_block);
+  zero_split_units_kernel<kTile, kGridPlanes><<<blocks, kThreads, 0, s>>>(
+      p, wi.item_off, p_begin, n_batch, wi.n_units, planes);
+  check_launch("zero_split_units_kernel");
+}
+
+void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
+                       int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
+  check_plan(p);
+  grid_dispatch<kTile, kGridPlanes>(p.support, p, rec, off, p_begin, n_batch, wi, planes, s);
+}
+
+void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                         int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
+                         float2 *acc, cudaStream_t s) {
+  check_plan(p);
+  if (degrid_group(p) == 16)
+    degrid_dispatch<kTile, 16>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+  else
+    degrid_dispatch<kTile, 8>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+}
+
+static ItemAlloc arena_alloc(DeviceArena &arena) {
+  return [&arena](int which, size_t bytes) -> void * {
+    const int slot = which == 0 ? kSlotItems : which == 1 ? kSlotItemDesc : kSlotScanTmp;
+    return arena.get(slot, bytes);
+  };
+}
+
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s) {
-  if (p.support < 4 || p.support > kMaxSupport)
-    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
-  if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
-  grid_dispatch<kTile, kGridPlanes>(p.support, arena, p, rec, off, p_begin, n_batch, planes, s);
+  const WorkItems wi = plan_grid_items(p, off, p_begin, n_batch, planes, arena_alloc(arena), s);
+  launch_grid_items(p, rec, off, p_begin, n_batch, wi, planes, s);
 }
 
 void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                    const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
                    float2 *acc, cudaStream_t s) {
-  if (p.support < 4 || p.support > kMaxSupport)
-    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
-  if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
-  if (p.support <= 8)
-    degrid_dispatch<kTile, 16>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
-  else
-    degrid_dispatch<kTile, 8>(p.support, arena, p, rec, off, p_begin, n_batch, planes, acc, s);
+  const WorkItems wi = plan_degrid_items(p, off, p_begin, n_batch, arena_alloc(arena), s);
+  launch_degrid_items(p, rec, off, p_begin, n_batch, wi, planes, acc, s);
 }
 
 }  // namespace wgpu

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 
@@ -98,6 +99,28 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
 
 // ---- gridding (grid.cu) ----
 class DeviceArena;
+// Work items of one plane batch (see grid.cu): scanned item offsets per
+// (tile, plane group) unit and the item -> unit descriptors.
+struct WorkItems {
+  uint32_t *item_off = nullptr;
+  uint32_t *desc = nullptr;
+  uint32_t total = 0;
+  int n_units = 0;
+};
+// Buffer provider for planning: which = 0 item offsets, 1 descriptors, 2 scan
+// scratch.
+using ItemAlloc = std::function<void *(int which, size_t bytes)>;
+WorkItems plan_grid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
+                          float2 *planes, const ItemAlloc &alloc, cudaStream_t s);
+WorkItems plan_degrid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
+                            const ItemAlloc &alloc, cudaStream_t s);
+void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
+                             float2 *planes, cudaStream_t s);
+void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
+                       int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s);
+void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
+                         int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
+                         float2 *acc, cudaStream_t s);
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s);
@@ -151,6 +174,8 @@ void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
                        cudaStream_t s);
 void launch_scale_image(void *img, int precision_bytes, int64_t n,
                         double factor, cudaStream_t s);
+void launch_restamp(const VisRecord *geom, const uint32_t *perm, const float2 *vis,
+                    int64_t n, VisRecord *out, cudaStream_t s);
 void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
                               const float2 *acc, int64_t n, float2 *vis,
                               cudaStream_t s);

@@ -144,6 +144,34 @@ class WGriddingGridder_Simple:
         check(lib().wgpu_gridder_predict_visibilities_device(self._h, n_rows, n_chan, d_uvw,
                                                              d_freq, d_vis))
 
+    # device-resident state across major cycles
+    def Bind(self, n_rows, n_chan, uvw, freq, mask=None):
+        """Plan and bucket this visibility set once; later cycles replay graphs."""
+        uvw, freq = _f64(uvw), _f64(freq)
+        self._bound_n = n_rows * n_chan
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        check(lib().wgpu_gridder_bind(self._h, n_rows, n_chan, ptr(uvw), ptr(freq), ptr(m)))
+
+    def Unbind(self):
+        check(lib().wgpu_gridder_unbind(self._h))
+
+    def InvertBound(self, vis):
+        vis = _c64(vis)
+        assert vis.size == self._bound_n
+        check(lib().wgpu_gridder_invert_bound(self._h, ptr(vis)))
+
+    def InvertBoundDevice(self, d_vis):
+        check(lib().wgpu_gridder_invert_bound_device(self._h, d_vis))
+
+    def PredictBound(self, out=None):
+        if out is None:
+            out = np.empty(self._bound_n, dtype=np.complex64)
+        check(lib().wgpu_gridder_predict_bound(self._h, ptr(out)))
+        return out
+
+    def PredictBoundDevice(self, d_vis):
+        check(lib().wgpu_gridder_predict_bound_device(self._h, d_vis))
+
     # diagnostics
     def last_plan(self):
         p = _lib.Plan()
