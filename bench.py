@@ -405,6 +405,13 @@ def run_gpu(args, rank, world, local):
                  survey_request_bytes(plan_pred, d["n_gridded"], n_rows))
     result["config"]["request_bytes_roofline_frac"] = (req_bytes / (ms_per_step * 1e-3) / 1e9) / peak
 
+    if args.serve_requests > 0:
+        g.close()  # release the wide-field gridder's planes before serving
+        del d_out
+        d.pop("d_vis", None)
+        torch.cuda.empty_cache()
+        free_b, _ = torch.cuda.mem_get_info()
+        result["serving"] = run_serving(args, 0.7 * free_b)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(d, lambda r: d["h_vis"][r], plan_inv, n_vis,
                                               args.cpu_sample_rows, args.cpu_planes)
@@ -412,6 +419,52 @@ def run_gpu(args, rank, world, local):
         result["config"]["accuracy"] = accuracy_check(d, plan_inv, eps)
     g.close()
     return result
+
+
+# ---------------------------------------------------------------- serving ---
+def run_serving(args, device_bytes):
+    """Mixed-size request stream through the request server (scaled serving
+    workload): the plain one-request-at-a-time path, the saturated server and
+    Poisson arrivals at 0.8 of the saturated capacity."""
+    from wsclean_gb300 import serving
+    t0 = time.time()
+    pool = serving.make_pool(args.serve_max_vis)
+    pool_rows = pool["uvw"].shape[0]
+    reqs = serving.make_stream(args.serve_requests, vis_range=(1e5, args.serve_max_vis),
+                               side_range=(512, args.serve_max_side), pool_rows=pool_rows,
+                               cycles=args.serve_cycles)
+    gen_s = time.time() - t0
+    keep = tuple(r["id"] for r in reqs[:6])
+    planes = device_bytes / (2.0 * args.serve_slots)
+    plain, kept_plain = serving.one_at_a_time(pool, reqs, device_bytes, planes, keep)
+    sat, kept_sat = serving.saturated(pool, reqs, device_bytes, planes, args.serve_slots, keep)
+    rate = 0.8 * len(reqs) / sat["wall_s"]
+    poi = serving.poisson(pool, reqs, device_bytes, planes, args.serve_slots, rate)
+    # served (mixed) against one-at-a-time (alone) results of the same requests:
+    # the runs differ only in the order of the float atomic additions
+    same, same_eps = 0.0, 0.0
+    eps_of = {r["id"]: r["eps"] for r in reqs}
+    for i in keep:
+        a, b = kept_plain[i], kept_sat[i]
+        e = float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-30))
+        same, same_eps = max(same, e), max(same_eps, e / eps_of[i])
+    sides = [r["side"] for r in reqs]
+    nvis = [r["rows"] * serving.N_CHAN for r in reqs]
+    return {
+        "workload": (f"{len(reqs)} requests ({sum(r['kind'] == 'invert' for r in reqs)} grid / "
+                     f"{sum(r['kind'] == 'predict' for r in reqs)} degrid), image side log-uniform "
+                     f"512-{args.serve_max_side} (drawn {min(sides)}-{max(sides)}), N_vis "
+                     f"log-uniform 1e5-{args.serve_max_vis:.0e} (drawn {min(nvis)}-{max(nvis)}) "
+                     f"from the 64-antenna 3 km array, eps 1e-4/1e-5, {args.serve_cycles} major "
+                     f"cycles per request with state resident"),
+        "slots": args.serve_slots, "device_budget_gb": device_bytes / 1e9,
+        "visibilities": serving.total_vis(reqs),
+        "one_at_a_time": plain, "saturated": sat, "poisson": poi,
+        "served_over_plain": sat["gvis_s"] / plain["gvis_s"],
+        "alone_vs_mixed_max_rel_l2": same, "alone_vs_mixed_max_over_eps": same_eps,
+        "alone_vs_mixed_tolerance": "relative L2 <= the request's epsilon",
+        "datagen_s": round(gen_s, 1),
+    }
 
 
 # ---------------------------------------------------------- reference arm ---
@@ -472,6 +525,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=200000)
     ap.add_argument("--cpu-planes", type=int, default=2)
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests in the serving stream (0 skips it)")
+    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-cycles", type=int, default=5)
+    ap.add_argument("--serve-max-vis", type=float, default=1e7)
+    ap.add_argument("--serve-max-side", type=int, default=4096)
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving stream and print its JSON")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes per launch of the dominant kernel, if captured")
     args = ap.parse_args()
@@ -481,6 +542,12 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.serve_only:
+        import torch
+        torch.cuda.set_device(local)
+        free_b, _ = torch.cuda.mem_get_info()
+        print(json.dumps(run_serving(args, 0.7 * free_b)), flush=True)
         return
     if world > 1:
         import torch

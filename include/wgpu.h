@@ -245,6 +245,11 @@ int wgpu_gridder_last_timings(const wgpu_gridder_t *gridder, double *ms,
  * has no counterpart in the reference, where ducc0 plans every call. */
 int wgpu_gridder_pin_plan(wgpu_gridder_t *gridder, const wgpu_plan_t *plan);
 
+/* Cap, in bytes, on the device memory of the w-plane batch that this
+ * gridder's plans keep resident (0 = 40% of free device memory, at most 40 GB).
+ * Lets several gridders share one GPU; no counterpart in the reference. */
+int wgpu_gridder_set_plane_budget(wgpu_gridder_t *gridder, double bytes);
+
 /* Gridder's CUDA stream (cudaStream_t), for callers that time or order work
  * around the _device entry points. */
 void *wgpu_gridder_stream(wgpu_gridder_t *gridder);
@@ -310,6 +315,73 @@ int wgpu_bucket_noalloc(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
                         int64_t *n_out);
 
 size_t wgpu_bucket_noalloc_scratch_bytes(void);
+
+/* ------------------------------------------------------------------------ */
+/* Request server: continuous batching of gridding requests on one GPU        */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces, for this path, GriddingTaskManager / ThreadedScheduler
+ * (scheduling/griddingtaskmanager.cpp:26-103, threadedscheduler.cpp:12-228),
+ * which run gridding tasks on a pool of CPU threads.  Requests are queued in
+ * arrival order and run by `max_active` worker slots, each with its own CUDA
+ * stream, so admitted requests overlap on the device.  A request is admitted
+ * when a slot is free and its estimated device memory fits what is left of
+ * `device_bytes` (one that is larger than the whole budget runs alone);
+ * admission is first-come first-served, except that a request whose session is
+ * running waits without holding back the requests behind it.  Requests with
+ * the same non-zero `session` share one gridder bound to the first request's
+ * uvw / freq / mask (wgpu_gridder_bind): later requests of the session reuse
+ * that device state and replay its graphs, and must carry the same geometry
+ * and sample set.  A session's device memory is held until
+ * wgpu_server_close_session.  Requests of one session run in submission
+ * order.  Every pointer in a request must stay valid until its wait returns. */
+#define WGPU_REQUEST_INVERT 1  /* vis -> image_out (FinalizeImage(image_factor)) */
+#define WGPU_REQUEST_PREDICT 2 /* model -> vis_out */
+
+typedef struct wgpu_request {
+  int kind;
+  uint64_t session;
+  size_t width, height, width_t, height_t; /* as wgpu_gridder_create */
+  double pixel_size_x, pixel_size_y, l_shift, m_shift, epsilon;
+  size_t n_rows, n_chan;
+  const double *uvw, *freq;
+  const uint8_t *mask;  /* optional sample selection ([row * n_chan + chan]) */
+  const float *vis;     /* inversion input, complex64 */
+  double image_factor;  /* inversion: FinalizeImage factor */
+  float *image_out;     /* inversion output, width * height */
+  const float *model;   /* prediction input, width * height */
+  float *vis_out;       /* prediction output, complex64 */
+} wgpu_request_t;
+
+typedef struct wgpu_server_stats {
+  uint64_t completed, failed, queued, running;
+  uint64_t peak_running;      /* most requests that ran at once */
+  double device_bytes_in_use; /* admitted requests + resident sessions */
+  double peak_device_bytes;   /* largest device_bytes_in_use */
+  double visibilities;        /* n_rows * n_chan of completed requests */
+  double elapsed_s;           /* first submission to last completion */
+} wgpu_server_stats_t;
+
+typedef struct wgpu_server wgpu_server_t;
+
+/* plane_budget_bytes caps the w-plane batch of each request's plan
+ * (0 = device_bytes / (2 * max_active)). */
+int wgpu_server_create(double device_bytes, int max_active,
+                       double plane_budget_bytes, wgpu_server_t **server);
+/* Queue a request; *ticket identifies it for wgpu_server_wait. */
+int wgpu_server_submit(wgpu_server_t *server, const wgpu_request_t *request,
+                       uint64_t *ticket);
+/* Block until the request has finished; returns its status (its message via
+ * wgpu_last_error) and, if non-NULL, its latency (submission to completion)
+ * and queueing time in milliseconds.  A ticket can be waited for once. */
+int wgpu_server_wait(wgpu_server_t *server, uint64_t ticket,
+                     double *latency_ms, double *queue_ms);
+/* Release a session's gridder and device memory (WGPU_ERR_STATE while one of
+ * its requests is queued or running). */
+int wgpu_server_close_session(wgpu_server_t *server, uint64_t session);
+int wgpu_server_stats(wgpu_server_t *server, wgpu_server_stats_t *stats);
+/* Finishes the queued requests, then stops the workers and frees everything. */
+void wgpu_server_destroy(wgpu_server_t *server);
 
 #ifdef __cplusplus
 }

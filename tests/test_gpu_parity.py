@@ -305,3 +305,41 @@ def test_bound_mask_selects_samples(wgpu_lib):
     pm = g.PredictVisibilitiesMasked(uvw.shape[0], freq.size, uvw, freq, mask).reshape(vis.shape)
     assert rel(pv, pm) <= 2e-6
     g.close()
+
+
+def test_bound_split_units_over_plane_batches(wgpu_lib, oracle_lib):
+    """Dense set over two plane batches in which 72 gridding units need more
+    than one work item (more than 2048 visibility reads): the bound graphs
+    equal the plain path with the same plan, and the DFT within epsilon."""
+    W, dl, eps = 64, 5e-3, 1e-4
+    uvw, freq, vis = synthetic.random_points(8000, 32, W, dl, seed=71, w_scale=3.0)
+    plan = _plan_for(uvw, freq, None, W, dl, eps, max_plane_batch=16)
+    assert plan.n_planes > plan.plane_batch
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=eps)
+    g.pin_plan(plan)
+    g.Bind(uvw.shape[0], freq.size, uvw, freq)
+    ref_g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=eps)
+    ref_g.pin_plan(plan)
+    rng = np.random.default_rng(12)
+    for cycle in range(2):
+        g.InitializeInversion()
+        g.InvertBound(vis)
+        img = g.RealImage().astype(np.float64)
+        ref_g.InitializeInversion()
+        ref_g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+        assert rel(img, ref_g.RealImage()) <= 2e-6, cycle
+    pix = rng.choice(W * W, 512, replace=False)
+    dft = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, pixels=pix)
+    assert rel(img[pix], dft) <= eps
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, 10, replace=False)] = rng.uniform(-1, 1, 10)
+    g.InitializePrediction(model)
+    pv = g.PredictBound()
+    ref_g.InitializePrediction(model)
+    pr = ref_g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq)
+    assert rel(pv, pr) <= 2e-6
+    sel = rng.choice(pv.size, 4096, replace=False)
+    pd = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl, vis_index=sel)
+    assert rel(pv[sel], pd) <= eps
+    g.close()
+    ref_g.close()

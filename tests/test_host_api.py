@@ -118,6 +118,18 @@ def test_no_device_fails_loudly(wgpu_lib):
     with pytest.raises(_lib.WgpuError):
         from wsclean_gb300.gridder import bucket_debug
         bucket_debug(p, 1, 1, uvw, np.array([1e8]), np.ones(1, np.complex64), True)
+    from wsclean_gb300.server import GriddingServer
+    with pytest.raises(_lib.WgpuError) as e:
+        GriddingServer(1e9, max_active=2)
+    assert e.value.status == _lib.WGPU_ERR_CUDA
+
+
+def test_server_validates_arguments(wgpu_lib):
+    from wsclean_gb300.server import GriddingServer
+    for args in ((0.0, 2), (1e9, 0), (1e9, 65), (-1.0, 1)):
+        with pytest.raises(_lib.WgpuError) as e:
+            GriddingServer(*args)
+        assert e.value.status == _lib.WGPU_ERR_INVALID
 
 
 def test_constant_memory_formula_matches_reference():

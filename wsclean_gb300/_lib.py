@@ -51,6 +51,29 @@ class PlanRequest(C.Structure):
                 ("memory_budget_bytes", C.c_double)]
 
 
+class Request(C.Structure):
+    """wgpu_request_t: one inversion or prediction request for the server."""
+    _fields_ = [("kind", C.c_int), ("session", C.c_uint64),
+                ("width", C.c_size_t), ("height", C.c_size_t),
+                ("width_t", C.c_size_t), ("height_t", C.c_size_t),
+                ("pixel_size_x", C.c_double), ("pixel_size_y", C.c_double),
+                ("l_shift", C.c_double), ("m_shift", C.c_double), ("epsilon", C.c_double),
+                ("n_rows", C.c_size_t), ("n_chan", C.c_size_t),
+                ("uvw", C.c_void_p), ("freq", C.c_void_p), ("mask", C.c_void_p),
+                ("vis", C.c_void_p), ("image_factor", C.c_double),
+                ("image_out", C.c_void_p), ("model", C.c_void_p), ("vis_out", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_uint64),
+                ("running", C.c_uint64), ("peak_running", C.c_uint64),
+                ("device_bytes_in_use", C.c_double), ("peak_device_bytes", C.c_double),
+                ("visibilities", C.c_double), ("elapsed_s", C.c_double)]
+
+
+REQUEST_INVERT = 1
+REQUEST_PREDICT = 2
+
 _lib = None
 
 P = C.c_void_p
@@ -88,6 +111,7 @@ _PROTOS = {
     "wgpu_gridder_invert_bound_device": (I, [P, P]),
     "wgpu_gridder_predict_bound": (I, [P, P]),
     "wgpu_gridder_predict_bound_device": (I, [P, P]),
+    "wgpu_gridder_set_plane_budget": (I, [P, D]),
     "wgpu_gridder_stream": (P, [P]),
     "wgpu_kernel_launch_count": (C.c_uint64, []),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,
@@ -95,6 +119,12 @@ _PROTOS = {
     "wgpu_bucket_noalloc": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P,
                                 C.POINTER(C.c_int64)]),
     "wgpu_bucket_noalloc_scratch_bytes": (SZ, []),
+    "wgpu_server_create": (I, [D, I, D, C.POINTER(P)]),
+    "wgpu_server_submit": (I, [P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "wgpu_server_wait": (I, [P, C.c_uint64, C.POINTER(D), C.POINTER(D)]),
+    "wgpu_server_close_session": (I, [P, C.c_uint64]),
+    "wgpu_server_stats": (I, [P, C.POINTER(ServerStats)]),
+    "wgpu_server_destroy": (None, [P]),
 }
 
 

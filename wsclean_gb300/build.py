@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwgpu.so")
 
-SOURCES = ["api.cu", "bucket.cu", "grid.cu", "fft.cu", "correct.cu", "util.cu", "plan.cpp"]
+SOURCES = ["api.cu", "bucket.cu", "grid.cu", "fft.cu", "correct.cu", "util.cu", "server.cu",
+           "plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -37,6 +37,11 @@ int guarded(F &&f) {
 
 }  // namespace
 
+namespace wgpu {
+int report_failure(int status, const std::string &msg) { return fail(status, msg); }
+void clear_failure() { g_last_error.clear(); }
+}  // namespace wgpu
+
 // Stage timer: events recorded on the gridder stream between launches; the
 // elapsed time of each interval is charged to the stage that opened it.
 struct StageTimer {
@@ -142,6 +147,7 @@ struct wgpu_gridder {
   std::vector<StageTimer::Stage> last_timings;
   std::string corr_key;  // geometry of the correction tables in the arena
   std::unique_ptr<BoundState> bound;
+  double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
 };
 
 namespace wgpu {
@@ -258,6 +264,7 @@ wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis)
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
     r.memory_budget_bytes = std::min(40e9, 0.4 * (double)(free_b + g->arena.total()));
   }
+  if (g->plane_budget > 0) r.memory_budget_bytes = g->plane_budget;
   // WGPU_PLANE_BUDGET_GB caps the plane-batch memory (profiling small cases)
   if (const char *env = std::getenv("WGPU_PLANE_BUDGET_GB")) {
     const double gb = std::atof(env);
@@ -474,7 +481,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   WGPU_CUDA(cudaStreamSynchronize(s));
 
   // inversion graph: records from the new visibilities, then the batches
-  uint64_t k0 = launch_count();
+  uint64_t k0 = thread_launch_count();
   WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   try {
     launch_restamp(b->geom, b->perm, b->vis_in, b->n_out, b->work, s);
@@ -499,11 +506,11 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   }
   WGPU_CUDA(cudaStreamEndCapture(s, &b->ginv));
   WGPU_CUDA(cudaGraphInstantiate(&b->xinv, b->ginv, 0));
-  b->inv_kernels = launch_count() - k0;
+  b->inv_kernels = thread_launch_count() - k0;
   count_launch(-(int)b->inv_kernels);  // captured, not run
 
   // prediction graph: pre-correction, the batches, un-permute
-  k0 = launch_count();
+  k0 = thread_launch_count();
   WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   try {
     launch_precorrect(dp, g->d_img, g->prec, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, b->img_corr, s);
@@ -528,7 +535,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   }
   WGPU_CUDA(cudaStreamEndCapture(s, &b->gpred));
   WGPU_CUDA(cudaGraphInstantiate(&b->xpred, b->gpred, 0));
-  b->pred_kernels = launch_count() - k0;
+  b->pred_kernels = thread_launch_count() - k0;
   count_launch(-(int)b->pred_kernels);
   g->bound = std::move(b);
 }
@@ -902,6 +909,14 @@ int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms, int *counts,
 void *wgpu_gridder_stream(wgpu_gridder_t *g) { return g ? (void *)g->stream : nullptr; }
 
 uint64_t wgpu_kernel_launch_count(void) { return launch_count(); }
+
+int wgpu_gridder_set_plane_budget(wgpu_gridder_t *g, double bytes) {
+  return guarded([&] {
+    if (!g) throw Error(WGPU_ERR_INVALID, "null gridder");
+    if (!(bytes >= 0)) throw Error(WGPU_ERR_INVALID, "negative plane budget");
+    g->plane_budget = bytes;
+  });
+}
 
 int wgpu_gridder_bind(wgpu_gridder_t *g, size_t n_rows, size_t n_chan, const double *uvw,
                       const double *freq, const uint8_t *mask) {

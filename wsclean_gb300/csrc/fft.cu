@@ -444,9 +444,7 @@ int row_threads(int L) {
   return t < 64 ? 64 : (t > 1024 ? 1024 : t);
 }
 
-void set_smem(const void *fn, size_t bytes) {
-  WGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-}
+void set_smem(const void *fn, size_t bytes) { ensure_dynamic_smem(fn, bytes); }
 
 }  // namespace
 

@@ -107,7 +107,9 @@ __global__ void __launch_bounds__(kThreads)
     items[unit] = n_items;
     counts[unit] = cnt;
   }
-  if (!degrid && n_items > 1) {
+  // planes is null when the items are planned ahead of the gridding (bound
+  // sets); zero_split_units_kernel then clears these cells before each pass.
+  if (!degrid && planes != nullptr && n_items > 1) {
     const int tu = tile % p.ntu, tv = tile / p.ntu;
     const size_t plane_elems = (size_t)p.nu * p.nv;
     for (int c = lane; c < (q1 - q0) * T * T; c += 32) {
@@ -419,12 +421,13 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
+  // initialised once, thread-safely (gridders run on several host threads)
+  static const int n = [] {
+    int dev = 0, v = 0;
     WGPU_CUDA(cudaGetDevice(&dev));
-    WGPU_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-  }
+    WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
   return n;
 }
 
@@ -490,8 +493,7 @@ void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int
                 int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
   if (wi.total == 0) return;
   const size_t smem = sizeof(float) * 2 * G * T * padded_stride(T, W);
-  WGPU_CUDA(cudaFuncSetAttribute(grid_kernel<T, G, W>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)grid_kernel<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G, W>,
                                                           kThreads, smem));
@@ -508,8 +510,7 @@ void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, i
   if (wi.total == 0) return;
   constexpr int R = T + W - 1;
   const size_t smem = sizeof(float) * 2 * G * R * padded_stride(R, W);
-  WGPU_CUDA(cudaFuncSetAttribute(degrid_kernel<T, G, W>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)degrid_kernel<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G, W>,
                                                           kThreads, smem));

@@ -1,5 +1,8 @@
 // Device arena, launch accounting and a device-wide exclusive scan.
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "wgpu_internal.h"
 
@@ -7,10 +10,31 @@ namespace wgpu {
 
 namespace {
 std::atomic<uint64_t> g_launches{0};
+thread_local uint64_t t_launches = 0;  // this thread's share (graph capture)
 }
 
-void count_launch(int n) { g_launches.fetch_add((uint64_t)n); }
+void count_launch(int n) {
+  g_launches.fetch_add((uint64_t)n);
+  t_launches += (uint64_t)n;
+}
 uint64_t launch_count() { return g_launches.load(); }
+uint64_t thread_launch_count() { return t_launches; }
+
+// Raises the kernel's dynamic shared-memory cap to at least `bytes`, never
+// lowering it: gridders on several host threads launch the same kernels with
+// different sizes, and a cap lowered by one thread would make another thread's
+// launch (or graph instantiation) fail.
+void ensure_dynamic_smem(const void *fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> caps;
+  int dev = 0;
+  WGPU_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cap = caps[{dev, fn}];
+  if (bytes <= cap) return;
+  WGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cap = bytes;
+}
 
 void check_launch(const char *what) {
   cudaError_t e = cudaGetLastError();

@@ -32,7 +32,14 @@ struct Error : std::runtime_error {
 
 void count_launch(int n = 1);
 uint64_t launch_count();
+uint64_t thread_launch_count();  // launches issued by the calling thread
+
+// Sets the calling thread's wgpu_last_error message; returns status.
+int report_failure(int status, const std::string &msg);
+void clear_failure();
 void check_launch(const char *what);
+// Raises (never lowers) a kernel's dynamic shared-memory cap; thread-safe.
+void ensure_dynamic_smem(const void *fn, size_t bytes);
 
 // One bucketed visibility in sorted order (32 bytes, two 128-bit words).
 // For inversion (re, im) is the visibility times exp(-2 pi i theta); for

@@ -135,14 +135,17 @@ def model_vis_torch(uvw, freq, sources, device, chunk_rows=1 << 16):
 
 
 def make_workload(name, seed=1, max_rows=None, with_model=True, device=None,
-                  n_src=None):
+                  n_src=None, n_t=None):
     """Builds the named workload.  Returns a dict with uvw [rows,3] f64, freq f64,
     vis [rows, chan] complex64 (weighted, Nyquist-guarded), image/pixel geometry,
     the sources and the sum of weights (ImageWeight).  max_rows keeps a
-    leading subset of rows (all baselines of the first time steps)."""
+    leading subset of rows (all baselines of the first time steps); n_t
+    overrides the number of time steps."""
     cfg = dict(WORKLOADS[name])
     if n_src is not None:
         cfg["n_src"] = n_src
+    if n_t is not None:
+        cfg["n_t"] = int(n_t)
     rng = np.random.default_rng(seed)
     enu = antenna_enu(cfg["n_ant"], cfg["layout"], cfg["radius_m"], rng)
     bxyz, a1, a2 = baselines_xyz(enu)
