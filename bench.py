@@ -32,6 +32,8 @@ sys.path.insert(0, ROOT)
 WORKLOAD_TEXT = {
     "wide8192": ("wide-field 8192x8192, 3arcsec pixels, 256 antennas log-radial to 20 km, "
                  "32640 baselines x 300 x 8 s, 64 channels 0.9-1.7 GHz, 500 sources, eps 1e-5"),
+    "wide2048": ("profiling-size wide field: the wide-field array, 3arcsec pixels and band on "
+                 "a 2048x2048 image, 32640 baselines x 8 x 8 s, 64 channels, eps 1e-5"),
     "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
                   "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
 }

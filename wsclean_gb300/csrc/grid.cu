@@ -142,35 +142,64 @@ __host__ __device__ constexpr int padded_stride(int rows, int W) {
                 : (((rows + 15) / 32) * 32 + 16);  // 16 (mod 32)
 }
 
-// Gridding of one plane batch, one warp per visibility: lanes own footprint
-// cells (c = lane + 32 k, i = c % W, j = c / W), the W kernel values of each
-// dimension are evaluated by W lanes and broadcast by shuffles, and each cell
-// is added into the shared tile with one atomic per component.  A work item
-// holds at most kItemVis visibility reads, which bounds the FP32 accumulation
-// chain of every cell; the item's tile is flushed to HBM once at its end.
+// Shared-memory layout of the gridding kernel: the tile's float2 cells
+// [G][T][T], then the staged round: five meta arrays [5][kGridRound] (re, im,
+// u and v corner relative to the tile, first plane relative to the group) and
+// the kernel values [kGridRound][kw] with kw = 3W rounded up to an odd count
+// (kx[W], ky[W], kz[W] per record; the odd stride keeps the stores of a warp
+// on distinct banks).
+constexpr int kGridRound = 128;  // records staged per round
+__host__ __device__ constexpr int grid_weight_stride(int W) { return (3 * W) | 1; }
+template <int T, int G, int W>
+constexpr size_t grid_smem_bytes() {
+  return sizeof(float2) * G * T * T +
+         sizeof(float) * kGridRound * (5 + grid_weight_stride(W));
+}
+
+// Gridding of one plane batch.  The block owns one unit (a T x T tile over G
+// planes) per work item and keeps its cells in shared memory.  Warp k owns
+// rows 2k and 2k+1 of every plane, so a cell is only ever updated by one warp:
+// plain load-multiply-add-store, no atomics.  Each round stages up to
+// kGridRound visibility reads with their kernel values (evaluated once per
+// read); every warp scans the round and adds the part of each footprint that
+// falls on its two rows: lanes cover (footprint column, row of the pair,
+// plane parity) and step through the footprint's planes.  Columns are
+// XOR-swizzled by row parity so that the 64-bit accesses of a half-warp (two
+// rows x eight columns) fall on distinct banks.  A work item holds at most
+// kItemVis reads, which bounds the FP32 accumulation chain of every cell; the
+// tile is flushed to HBM once at the item's end.
 template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                 const uint32_t *__restrict__ off, int p_begin, int n_batch,
                 const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
                 uint32_t total, float2 *__restrict__ planes) {
-  constexpr int TS = padded_stride(T, W);
-  constexpr int kPlane = T * TS;            // floats per plane in each array
-  constexpr int kFoot = W * W;
-  constexpr int kLaneCells = (kFoot + 31) / 32;
-  constexpr int kRound = kThreads;          // records staged per round
-  extern __shared__ float smem[];
-  float *bre = smem;                  // [G][T][TS]
-  float *bim = smem + G * kPlane;     // [G][T][TS]
+  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+  constexpr int kCols = W <= 8 ? 8 : 16;            // lanes across footprint columns
+  constexpr int kPlaneLanes = 32 / (2 * kCols);     // 2 (W <= 8) or 1
+  constexpr int kSteps = (W + kPlaneLanes - 1) / kPlaneLanes;
+  constexpr int kWS = grid_weight_stride(W);
+  constexpr int kCells = T * T;
+  extern __shared__ float4 smem4[];
+  float2 *cells = reinterpret_cast<float2 *>(smem4);  // [G][T][T], swizzled columns
+  float *m_re = reinterpret_cast<float *>(cells + G * kCells);
+  float *m_im = m_re + kGridRound;
+  int *m_iu = reinterpret_cast<int *>(m_im + kGridRound);
+  int *m_iv = m_iu + kGridRound;
+  int *m_ip = m_iv + kGridRound;
+  float *wts = reinterpret_cast<float *>(m_ip + kGridRound);  // [kGridRound][kWS]
   __shared__ uint32_t rs0[9], rcum[10];
-  __shared__ float4 stage[kRound][2];  // the round's records, loaded coalesced
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ci = lane % kCols;              // footprint column offset
+  const int row = 2 * warp + ((lane / kCols) & 1);
+  const int pj = lane / (2 * kCols);        // plane parity (W <= 8)
+  const int swz = (row & 1) << 3;
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
 
-  for (int c = threadIdx.x; c < 2 * G * kPlane; c += kThreads) smem[c] = 0.f;
+  for (int c = threadIdx.x; c < G * kCells; c += kThreads) cells[c] = make_float2(0.f, 0.f);
   __syncthreads();
 
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
@@ -180,13 +209,14 @@ __global__ void __launch_bounds__(kThreads)
     const int tu = tile % p.ntu, tv = tile / p.ntu;
     const int q0 = p_begin + group * G;
     const int q1 = min(q0 + G, p_begin + n_batch);
+    const int nq = q1 - q0;
     if (d & 0x80000000u) {
       // no visibility reaches this unit: its cells are zero
-      for (int c = threadIdx.x; c < (q1 - q0) * T * T; c += kThreads) {
-        const int pq = c / (T * T), rem = c - pq * T * T;
-        const int row = rem / T, col = rem - row * T;
-        planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
-               tu * T + col] = make_float2(0.f, 0.f);
+      for (int c = threadIdx.x; c < nq * kCells; c += kThreads) {
+        const int pq = c / kCells, rem = c - pq * kCells;
+        const int rr = rem / T, cc = rem - rr * T;
+        planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
+               tu * T + cc] = make_float2(0.f, 0.f);
       }
       continue;
     }
@@ -207,79 +237,81 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t lo = (item - first) * kItemVis;
     const uint32_t hi = min(lo + kItemVis, rcum[9]);
 
-    for (uint32_t rb = lo; rb < hi; rb += kRound) {
+    for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
+      // stage: threads t and t + kGridRound share read t; the first evaluates
+      // kx and ky, the second kz and the meta data
       {
-        const uint32_t pos = rb + threadIdx.x;
+        const int t = threadIdx.x % kGridRound;
+        const bool second = threadIdx.x >= kGridRound;
+        const uint32_t pos = rb + (uint32_t)t;
         if (pos < hi) {
           int r = 0;
           while (pos >= rcum[r + 1]) ++r;
-          const float4 *src = reinterpret_cast<const float4 *>(rec + rs0[r] + (pos - rcum[r]));
-          stage[threadIdx.x][0] = __ldg(src);
-          stage[threadIdx.x][1] = __ldg(src + 1);
-        }
-      }
-      __syncthreads();
-      const int n_round = (int)min((uint32_t)kRound, hi - rb);
-      for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
-        VisRecord v;
-        {
-          const float4 a = stage[m][0], b = stage[m][1];
-          v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
-          v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
-        }
-        int iu_rel = v.iu - tu * T;
-        if (iu_rel >= T) iu_rel -= p.nu;
-        int iv_rel = v.iv - tv * T;
-        if (iv_rel >= T) iv_rel -= p.nv;
-        const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
-        if (pa > pb) continue;  // uniform in the warp
-        // lanes 0..W-1 hold kx, W..2W-1 hold ky (k1); lanes 0..W-1 hold kw (k2)
-        const bool lx = lane < W;
-        const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
-        float k1 = es_eval(p.beta, f1 * inv_half);
-        k1 = lane < 2 * W ? k1 : 0.f;
-        float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
-        if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
-        float wgt[kLaneCells];
-        int idx[kLaneCells];
+          const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
+          float *w = wts + t * kWS;
+          if (!second) {
 #pragma unroll
-        for (int k = 0; k < kLaneCells; ++k) {
-          const int c = lane + 32 * k;
-          const int i = c % W, j = c / W;
-          const float kx = __shfl_sync(0xffffffffu, k1, i);
-          const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
-          const int row = iv_rel + j, col = iu_rel + i;
-          const bool in = c < kFoot && row >= 0 && row < T && col >= 0 && col < T;
-          wgt[k] = in ? kx * ky : 0.f;
-          idx[k] = in ? row * TS + col : -1;
-        }
-        for (int q = pa; q <= pb; ++q) {
-          const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
-          const float vr = v.re * kw, vi = v.im * kw;
-          float *pre = bre + (q - q0) * kPlane, *pim = bim + (q - q0) * kPlane;
-#pragma unroll
-          for (int k = 0; k < kLaneCells; ++k) {
-            if (idx[k] >= 0) {
-              atomicAdd(pre + idx[k], wgt[k] * vr);
-              atomicAdd(pim + idx[k], wgt[k] * vi);
+            for (int k = 0; k < W; ++k) {
+              w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
+              w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
             }
+          } else {
+#pragma unroll
+            for (int k = 0; k < W; ++k)
+              w[2 * W + k] = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
+                                             : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+            int iu_rel = v.iu - tu * T;
+            if (iu_rel >= T) iu_rel -= p.nu;
+            int iv_rel = v.iv - tv * T;
+            if (iv_rel >= T) iv_rel -= p.nv;
+            m_re[t] = v.re;
+            m_im[t] = v.im;
+            m_iu[t] = iu_rel;
+            m_iv[t] = iv_rel;
+            m_ip[t] = v.ip - q0;
           }
         }
       }
       __syncthreads();
+      const int n_round = (int)min((uint32_t)kGridRound, hi - rb);
+      for (int m = 0; m < n_round; ++m) {
+        const int ivr = m_iv[m];
+        if (ivr > 2 * warp + 1 || ivr + W <= 2 * warp) continue;  // uniform in the warp
+        const int col = m_iu[m] + ci;
+        const int dv = row - ivr;
+        if (ci < W && col >= 0 && col < T && dv >= 0 && dv < W) {
+          const float *w = wts + m * kWS;
+          const int ipr = m_ip[m];
+          const float re = m_re[m], im = m_im[m];
+          const float wuv = w[ci] * w[W + dv];
+          float2 *cb = cells + row * T + (col ^ swz);
+#pragma unroll
+          for (int s = 0; s < kSteps; ++s) {
+            const int dz = s * kPlaneLanes + pj;
+            const int q = ipr + dz;
+            if (dz < W && q >= 0 && q < nq) {
+              const float t = wuv * w[2 * W + dz];
+              float2 c = cb[q * kCells];
+              c.x = fmaf(t, re, c.x);
+              c.y = fmaf(t, im, c.y);
+              cb[q * kCells] = c;
+            }
+          }
+        }
+        __syncwarp();  // the next read's lanes may update the same cells
+      }
+      __syncthreads();
     }
-    // flush the tile (a split unit adds into cells zeroed by the planner)
-    for (int c = threadIdx.x; c < G * T * T; c += kThreads) {
-      const int pq = c / (T * T), rem = c - pq * T * T;
-      const int row = rem / T, col = rem - row * T;
-      const int o = pq * kPlane + row * TS + col;
-      const float2 val = make_float2(bre[o], bim[o]);
-      bre[o] = 0.f;
-      bim[o] = 0.f;
-      const int q = q0 + pq;
-      if (q < q1) {
-        float2 *dst = planes + (size_t)(q - p_begin) * plane_elems +
-                      (size_t)(tv * T + row) * p.nu + tu * T + col;
+    // flush the tile (a split unit adds into cells zeroed beforehand)
+    for (int c = threadIdx.x; c < G * kCells; c += kThreads) {
+      const int pq = c / kCells, rem = c - pq * kCells;
+      const int rr = rem / T, cc = rem - rr * T;
+      float2 *src = cells + pq * kCells + rr * T + (cc ^ ((rr & 1) << 3));
+      const float2 val = *src;
+      *src = make_float2(0.f, 0.f);
+      if (pq < nq) {
+        float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
+                      (size_t)(tv * T + rr) * p.nu + tu * T + cc;
         if (n_items == 1)
           *dst = val;
         else
@@ -492,7 +524,7 @@ template <int T, int G, int W>
 void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
                 int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
   if (wi.total == 0) return;
-  const size_t smem = sizeof(float) * 2 * G * T * padded_stride(T, W);
+  const size_t smem = grid_smem_bytes<T, G, W>();
   ensure_dynamic_smem((const void *)grid_kernel<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G, W>,

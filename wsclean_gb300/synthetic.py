@@ -36,6 +36,14 @@ WORKLOADS = {
                      n_t=300, dt=8.0, n_chan=64, f0=0.9e9, f1=1.7e9, n_src=500,
                      flux="powerlaw", fmin=1e-3, fmax=5.0, noise=0.01, weights="uniform",
                      dec_deg=45.0, epsilon=1e-5),
+    # Profiling-size wide field: the 8192^2 workload's array, pixels and band
+    # on a 2048^2 image over 8 time steps; each 16x16-cell x 16-plane gridding
+    # unit reads about as many visibilities (~190) as in the full workload
+    # (~180), within a few GB of device memory.
+    "wide2048": dict(npix=2048, pix_arcsec=3.0, n_ant=256, layout="lograd", radius_m=20000.0,
+                     n_t=8, dt=8.0, n_chan=64, f0=0.9e9, f1=1.7e9, n_src=500,
+                     flux="powerlaw", fmin=1e-3, fmax=5.0, noise=0.01, weights="uniform",
+                     dec_deg=45.0, epsilon=1e-5),
     # 4096^2 full polarisation with the 3 km array, 32 channels.
     "fullpol4096": dict(npix=4096, pix_arcsec=10.0, n_ant=64, layout="disk", radius_m=1500.0,
                         n_t=60, dt=10.0, n_chan=32, f0=120e6, f1=180e6, n_src=20,
