@@ -148,12 +148,30 @@ struct wgpu_gridder {
   std::string corr_key;  // geometry of the correction tables in the arena
   std::unique_ptr<BoundState> bound;
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
+  unsigned *d_flags = nullptr;  // device: expired bounded waits
+  unsigned *h_flags = nullptr;  // pinned host copy, read after each call
 };
 
 namespace wgpu {
 namespace {
 
 constexpr int kGlNodes = 48;
+
+// Ends a pipeline: the device flag word is copied behind the last launch, the
+// end event is recorded and waited for, and an expired bounded wait is
+// reported as WGPU_ERR_TIMEOUT.
+void end_call(wgpu_gridder *g) {
+  WGPU_CUDA(cudaMemcpyAsync(g->h_flags, g->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            g->stream));
+  g->timer.mark("end");
+  g->last_timings = g->timer.collect();
+  if (*g->h_flags != 0) {
+    *g->h_flags = 0;
+    WGPU_CUDA(cudaMemsetAsync(g->d_flags, 0, sizeof(unsigned), g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (row transform prefetch)");
+  }
+}
 
 size_t image_bytes(const wgpu_gridder *g) {
   return g->width_t * g->height_t * (size_t)g->prec;
@@ -298,8 +316,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   compute_w_extent(d_uvw, d_freq, d_vis, nullptr, (int64_t)n_rows, (int64_t)n_chan, true,
                    &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
   if (count == 0) {
-    g->timer.mark("end");
-    g->last_timings = g->timer.collect();
+    end_call(g);
     return;
   }
   const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
@@ -324,7 +341,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     g->timer.mark("grid");
     launch_grid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, s);
     g->timer.mark("fft_rows");
-    launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, s);
+    launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, g->d_flags, s);
     g->timer.mark("fft_cols_a");
     launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, -1.0f, s);
     g->timer.mark("fft_cols_b_screen");
@@ -338,8 +355,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   float *cx, *cy, *gl;
   upload_corrections(g, plan, &cx, &cy, &gl);
   launch_finalize_add(dp, acc, nu_w, cx, cy, gl, kGlNodes, g->d_img, g->prec, s);
-  g->timer.mark("end");
-  g->last_timings = g->timer.collect();
+  end_call(g);
 }
 
 void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
@@ -358,8 +374,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   if (d_mask) {
     WGPU_CUDA(cudaMemsetAsync(d_vis, 0, sizeof(float2) * n_rows * n_chan, s));
     if (count == 0) {
-      g->timer.mark("end");
-      g->last_timings = g->timer.collect();
+      end_call(g);
       return;
     }
   }
@@ -392,14 +407,13 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     g->timer.mark("fft_cols_a");
     launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, +1.0f, s);
     g->timer.mark("fft_rows");
-    launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, s);
+    launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, g->d_flags, s);
     g->timer.mark("degrid");
     launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
   }
   g->timer.mark("finalize");
   launch_unpermute_predict(b.records, b.perm, vacc, b.n_out, (float2 *)d_vis, s);
-  g->timer.mark("end");
-  g->last_timings = g->timer.collect();
+  end_call(g);
 }
 
 // ---- bound visibility sets: plan and bucket once, replay captured graphs ----
@@ -471,6 +485,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   fft_twiddles(*g->fft, (int)plan.nv);
   fft_twiddles(*g->fft, (int)plan.fft_n1);
   fft_twiddles(*g->fft, (int)plan.fft_n2);
+  fft_prepare_rows(*g->fft, (int)plan.nu);
   BoundState *bp = b.get();
   const ItemAlloc own = [bp](int, size_t bytes) -> void * { return bp->alloc(bytes); };
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
@@ -491,7 +506,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
       launch_zero_split_units(dp, b->gitems[i], p0, nb, b->planes, s);
       launch_grid_items(dp, b->work, b->offsets, p0, nb, b->gitems[i], b->planes, s);
-      launch_fft_rows_forward_crop(*g->fft, dp, b->planes, b->rows, rstride, nb, s);
+      launch_fft_rows_forward_crop(*g->fft, dp, b->planes, b->rows, rstride, nb, g->d_flags, s);
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
                         -1.0f, s);
       launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
@@ -522,7 +537,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                                         b->img_corr, b->nu_w, b->rows, rstride, nb, p0, s);
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
                         +1.0f, s);
-      launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, s);
+      launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, g->d_flags, s);
       launch_degrid_items(dp, b->geom, b->offsets, p0, nb, b->ditems[i], b->planes, b->vacc, s);
     }
     WGPU_CUDA(cudaMemsetAsync(b->vis_out, 0, sizeof(float2) * n, s));
@@ -552,8 +567,7 @@ void invert_bound(wgpu_gridder *g, const float *vis, bool device) {
                             device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   WGPU_CUDA(cudaGraphLaunch(b.xinv, s));
   count_launch((int)b.inv_kernels);
-  g->timer.mark("end");
-  g->last_timings = g->timer.collect();
+  end_call(g);
   g->last_plan = b.plan;
 }
 
@@ -569,8 +583,7 @@ void predict_bound(wgpu_gridder *g, float *vis, bool device) {
   count_launch((int)b.pred_kernels);
   WGPU_CUDA(cudaMemcpyAsync(vis, b.vis_out, sizeof(float2) * b.n_rows * b.n_chan,
                             device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
-  g->timer.mark("end");
-  g->last_timings = g->timer.collect();
+  end_call(g);
   g->last_plan = b.plan;
 }
 
@@ -640,8 +653,14 @@ int wgpu_gridder_create(size_t width, size_t height, size_t width_t,
     try {
       WGPU_CUDA(cudaGetDevice(&g->device));
       WGPU_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      WGPU_CUDA(cudaMalloc(&g->d_flags, sizeof(unsigned)));
+      WGPU_CUDA(cudaMemset(g->d_flags, 0, sizeof(unsigned)));
+      WGPU_CUDA(cudaMallocHost(&g->h_flags, sizeof(unsigned)));
+      *g->h_flags = 0;
       g->fft = fft_tables_create();
     } catch (...) {
+      if (g->d_flags) cudaFree(g->d_flags);
+      if (g->h_flags) cudaFreeHost(g->h_flags);
       if (g->stream) cudaStreamDestroy(g->stream);
       delete g;
       throw;
@@ -656,6 +675,8 @@ void wgpu_gridder_destroy(wgpu_gridder_t *g) {
   g->bound.reset();
   g->arena.release();
   if (g->d_img) cudaFree(g->d_img);
+  if (g->d_flags) cudaFree(g->d_flags);
+  if (g->h_flags) cudaFreeHost(g->h_flags);
   fft_tables_destroy(g->fft);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;

@@ -44,9 +44,11 @@ struct FftDesc {
 
 struct FftTables {
   std::mutex mu;
-  std::map<int, float2 *> tables;
+  std::map<int, float2 *> tables;      // exp(-2 pi i j / n), j < n
+  std::map<int, float2 *> row_tables;  // per-stage tables of row schedules
   ~FftTables() {
     for (auto &kv : tables) cudaFree(kv.second);
+    for (auto &kv : row_tables) cudaFree(kv.second);
   }
 };
 
@@ -70,11 +72,16 @@ const float2 *fft_twiddles(FftTables &t, int n) {
   return d;
 }
 
-static FftDesc make_desc(int L) {
+// Radix schedule for length L: radix 16 first where allowed (row transforms;
+// the later strides are then multiples of 16, which with the row swizzle
+// keeps every stage free of bank conflicts), then 8, 4, 2, 3, 5.
+static FftDesc make_desc(int L, bool radix16 = false) {
   FftDesc d;
   d.L = L;
   d.n_stages = 0;
   int m = L;
+  if (radix16)
+    while (m % 16 == 0) { d.radix[d.n_stages++] = 16; m /= 16; }
   while (m % 8 == 0) { d.radix[d.n_stages++] = 8; m /= 8; }
   while (m % 4 == 0) { d.radix[d.n_stages++] = 4; m /= 4; }
   while (m % 2 == 0) { d.radix[d.n_stages++] = 2; m /= 2; }
@@ -142,6 +149,44 @@ __device__ __forceinline__ void dft<8>(float2 *x, float s) {
   }
 }
 
+// 16 = 4 x 4: DFT4 over n1 of x[4 n1 + n2], twiddle w16^(n2 k1), DFT4 over
+// n2; output k1 + 4 k2.
+template <>
+__device__ __forceinline__ void dft<16>(float2 *x, float s) {
+  constexpr float c8 = 0.92387953251128675613f;  // cos(pi / 8)
+  constexpr float s8 = 0.38268343236508977173f;  // sin(pi / 8)
+  constexpr float r = 0.70710678118654752440f;
+  float2 y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) y[n2][n1] = x[4 * n1 + n2];
+    dft<4>(y[n2], s);
+  }
+  // w16^e = exp(s 2 pi i e / 16) for e = n2 k1
+  const float2 w1 = make_float2(c8, s * s8), w2 = make_float2(r, s * r),
+               w3 = make_float2(s8, s * c8), w6 = make_float2(-r, s * r),
+               w9 = make_float2(-c8, -s * s8);
+  y[1][1] = cmul(y[1][1], w1);
+  y[1][2] = cmul(y[1][2], w2);
+  y[1][3] = cmul(y[1][3], w3);
+  y[2][1] = cmul(y[2][1], w2);
+  y[2][2] = mul_si(y[2][2], s);
+  y[2][3] = cmul(y[2][3], w6);
+  y[3][1] = cmul(y[3][1], w3);
+  y[3][2] = cmul(y[3][2], w6);
+  y[3][3] = cmul(y[3][3], w9);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 z[4];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) z[n2] = y[n2][k1];
+    dft<4>(z, s);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) x[k1 + 4 * k2] = z[k2];
+  }
+}
+
 template <>
 __device__ __forceinline__ void dft<3>(float2 *x, float s) {
   constexpr float h = 0.86602540378443864676f;
@@ -173,10 +218,16 @@ __device__ __forceinline__ void dft<5>(float2 *x, float s) {
 }
 
 // Layout of the transforms a CTA holds in shared memory.
-//   kRow:   one transform, element k at s[k].
+//   kRow:   one transform, element k at s[row_slot(k)]: the low four bits of
+//           k are XORed with bits 4-7, which puts the strided accesses of
+//           every stage (and the natural-order fill and read-out) on distinct
+//           banks.  Buffers are rounded up to a multiple of 16 elements.
 //   kPanel: 32 interleaved transforms (one per column of a panel), element k
 //           of transform b at s[k * 32 + b].
 enum Layout { kRow = 0, kPanelLayout = 1 };
+
+__device__ __forceinline__ int row_slot(int k) { return k ^ ((k >> 4) & 15); }
+__host__ __device__ constexpr int row_buffer(int L) { return (L + 15) & ~15; }
 
 // One Stockham radix-R stage, out of place (src -> dst).  p = product of the
 // radices of the earlier stages; p_magic = ceil(2^32 / p) gives i / p exactly
@@ -195,7 +246,8 @@ __device__ __forceinline__ void stage(const float2 *__restrict__ src, float2 *__
     const int k = p == 1 ? 0 : i - p * (int)__umulhi((unsigned)i, p_magic);
     float2 v[R];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = src[(i + t * LR) * NB + b];
+    for (int t = 0; t < R; ++t)
+      v[t] = LAY == kRow ? src[row_slot(i + t * LR)] : src[(i + t * LR) * NB + b];
     if (k > 0) {
 #pragma unroll
       for (int t = 1; t < R; ++t) {
@@ -207,7 +259,12 @@ __device__ __forceinline__ void stage(const float2 *__restrict__ src, float2 *__
     dft<R>(v, sign);
     const int j = (i - k) * R + k;
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[(j + q * p) * NB + b] = v[q];
+    for (int q = 0; q < R; ++q) {
+      if (LAY == kRow)
+        dst[row_slot(j + q * p)] = v[q];
+      else
+        dst[(j + q * p) * NB + b] = v[q];
+    }
   }
   __syncthreads();
 }
@@ -224,6 +281,9 @@ __device__ __forceinline__ float2 *fft_smem(float2 *buf0, float2 *buf1, const Ff
     const int R = d.radix[st];
     const unsigned m = d.magic[st];
     switch (R) {
+      case 16:
+        if constexpr (LAY == kRow) stage<16, LAY>(src, dst, d.L, p, m, sign, tw);
+        break;
       case 8: stage<8, LAY>(src, dst, d.L, p, m, sign, tw); break;
       case 4: stage<4, LAY>(src, dst, d.L, p, m, sign, tw); break;
       case 2: stage<2, LAY>(src, dst, d.L, p, m, sign, tw); break;
@@ -244,42 +304,305 @@ __device__ __forceinline__ int wrap(int a, int n) {
 }
 
 // ---------------------------------------------------------------- rows ----
-__global__ void __launch_bounds__(1024) fft_rows_forward_crop_kernel(FftDesc d, const float2 *__restrict__ planes,
-                                             float2 *__restrict__ R, int rstride,
-                                             int nv, int width,
-                                             const float2 *__restrict__ tw) {
-  extern __shared__ float2 s[];
-  const int L = d.L;
-  const size_t row = blockIdx.x;  // plane * nv + b
-  const float2 *src = planes + row * (size_t)L;
-  for (int k = threadIdx.x; k < L / 2; k += blockDim.x)
-    reinterpret_cast<float4 *>(s)[k] = __ldg(reinterpret_cast<const float4 *>(src) + k);
+// Row transforms (length L = nu, a multiple of 16) use radix 16 first and the
+// swizzled row layout; twiddles come from per-stage tables laid out
+// [t - 1][k] (exp(-2 pi i t k / (p R))), so the lanes of a warp (consecutive
+// k) read consecutive entries.  Two kernels:
+//  * rows longer than kRowPingPongMax (8192, 10240, 12288): a persistent
+//    kernel, one CTA per SM looping over rows; the transform runs in place in
+//    one buffer (each thread holds the inputs of its butterflies in registers
+//    across a barrier) while a TMA bulk copy (cp.async.bulk, completion on an
+//    mbarrier) brings the next row into the other buffer.
+//  * shorter rows: one CTA per row, Stockham stages ping-ponging between two
+//    buffers, L / 16 threads, several CTAs per SM.
+
+constexpr int kRowPingPongMax = 6912;
+constexpr int kRowIn = 0;      // stage input: natural order as copied
+constexpr int kRowInPad = 1;   // natural order of the zero-padded, re-centred row
+constexpr int kRowInSlot = 2;  // swizzled layout written by an earlier stage
+
+struct RowStages {
+  int tw_off[kMaxStages];  // offset of each stage's table in the row table
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Waits for the phase of `parity` with a deadline of about two seconds;
+// returns false if it expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  const long long deadline = clock64() + (4ll << 30);
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() > deadline) return false;
+  return true;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Loads element a of the stage input.
+template <int IN>
+__device__ __forceinline__ float2 row_in(const float2 *buf, int a, int L, int width) {
+  if (IN == kRowIn) return buf[a];
+  if (IN == kRowInPad) {
+    const int x = wrap(width / 2 - a, L);
+    return x < width ? buf[x] : make_float2(0.f, 0.f);
+  }
+  return buf[row_slot(a)];
+}
+
+// Stockham butterfly i of a radix-R stage: twiddle, DFT, outputs in v.
+template <int R>
+__device__ __forceinline__ int row_butterfly(float2 *v, int i, int p, unsigned p_magic, float sign,
+                                             const float2 *__restrict__ tws) {
+  const int k = p == 1 ? 0 : i - p * (int)__umulhi((unsigned)i, p_magic);
+  if (k > 0) {
+#pragma unroll
+    for (int t = 1; t < R; ++t) {
+      float2 w = __ldg(tws + (t - 1) * p + k);
+      w.y *= -sign;  // tables hold exp(-2 pi i t k / (p R)); sign +1 conjugates
+      v[t] = cmul(v[t], w);
+    }
+  }
+  dft<R>(v, sign);
+  return (i - k) * R + k;  // outputs go to j + q p
+}
+
+// One in-place Stockham stage of radix R over buf (length L).  blockDim.x >=
+// L / 16, so a thread holds at most ceil(16 / R) butterflies.
+template <int R, int IN>
+__device__ __forceinline__ void row_stage_inplace(float2 *buf, int L, int p, unsigned p_magic,
+                                                  float sign, const float2 *__restrict__ tws,
+                                                  int width) {
+  constexpr int KMAX = (16 + R - 1) / R;
+  const int LR = L / R;
+  float2 v[KMAX][R];
+#pragma unroll
+  for (int kk = 0; kk < KMAX; ++kk) {
+    const int i = threadIdx.x + kk * blockDim.x;
+    if (i < LR) {
+#pragma unroll
+      for (int t = 0; t < R; ++t) v[kk][t] = row_in<IN>(buf, i + t * LR, L, width);
+    }
+  }
   __syncthreads();
-  const float2 *res = fft_smem<kRow>(s, s + L, d, -1.0f, tw);
-  float2 *dst = R + row * (size_t)rstride;
-  for (int x = threadIdx.x; x < rstride; x += blockDim.x) {
-    float2 v = make_float2(0.f, 0.f);
-    if (x < width) v = res[wrap(width / 2 - x, L)];
-    dst[x] = v;
+#pragma unroll
+  for (int kk = 0; kk < KMAX; ++kk) {
+    const int i = threadIdx.x + kk * blockDim.x;
+    if (i < LR) {
+      const int j = row_butterfly<R>(v[kk], i, p, p_magic, sign, tws);
+#pragma unroll
+      for (int q = 0; q < R; ++q) buf[row_slot(j + q * p)] = v[kk][q];
+    }
+  }
+  __syncthreads();
+}
+
+// Last stage (p R = L): each butterfly writes the addresses it read, so
+// threads work through their butterflies one at a time.
+template <int R>
+__device__ __forceinline__ void row_stage_last(float2 *buf, int L, int p, float sign,
+                                               const float2 *__restrict__ tws) {
+  const int LR = L / R;  // == p
+  for (int i = threadIdx.x; i < LR; i += blockDim.x) {
+    float2 v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = buf[row_slot(i + t * LR)];
+    if (i > 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) {
+        float2 w = __ldg(tws + (t - 1) * p + i);
+        w.y *= -sign;
+        v[t] = cmul(v[t], w);
+      }
+    }
+    dft<R>(v, sign);
+#pragma unroll
+    for (int q = 0; q < R; ++q) buf[row_slot(i + q * LR)] = v[q];
+  }
+  __syncthreads();
+}
+
+// Writes the transformed row: FWD crops the `width` kept columns (re-centred)
+// into out (out_stride entries), !FWD writes the L entries in natural order.
+template <bool FWD>
+__device__ __forceinline__ void row_out(const float2 *res, float2 *__restrict__ out,
+                                        int out_stride, int L, int width) {
+  float4 *dst = reinterpret_cast<float4 *>(out);
+  if (FWD) {
+    for (int x2 = threadIdx.x; x2 < out_stride / 2; x2 += blockDim.x) {
+      const int x = 2 * x2;
+      const float2 a = x < width ? res[row_slot(wrap(width / 2 - x, L))] : make_float2(0.f, 0.f);
+      const float2 c =
+          x + 1 < width ? res[row_slot(wrap(width / 2 - x - 1, L))] : make_float2(0.f, 0.f);
+      dst[x2] = make_float4(a.x, a.y, c.x, c.y);
+    }
+  } else {
+    for (int k2 = threadIdx.x; k2 < L / 2; k2 += blockDim.x) {
+      const float2 a = res[row_slot(2 * k2)], c = res[row_slot(2 * k2 + 1)];
+      dst[k2] = make_float4(a.x, a.y, c.x, c.y);
+    }
   }
 }
 
-__global__ void __launch_bounds__(1024) fft_rows_backward_pad_kernel(FftDesc d, const float2 *__restrict__ R,
-                                             int rstride, float2 *__restrict__ planes,
-                                             int nv, int width,
-                                             const float2 *__restrict__ tw) {
+constexpr int kRowThreadsMax = kFftMaxRow / 16;  // 768: one radix-16 butterfly each
+
+// Persistent row kernel.  Schedule: radix 16, (n_stages - 2 - MID8) radix-16
+// stages, one radix-8 stage if MID8, and a last stage of radix LAST.
+// FWD: plane rows (length L) -> forward FFT -> cropped rows of R.
+// !FWD: rows of R (width valid entries) -> zero padding, re-centring ->
+//      backward FFT -> plane rows.  buf_elems >= max(L, in_stride); in_bytes
+// is the size of one input row.
+template <bool FWD, int LAST, bool MID8>
+__global__ void __launch_bounds__(kRowThreadsMax, 1)
+    fft_rows_persistent_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
+                               const float2 *__restrict__ in, int in_stride, uint32_t in_bytes,
+                               float2 *__restrict__ out, int out_stride, int n_rows, int width,
+                               int buf_elems, unsigned *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char row_smem[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(row_smem);  // two mbarriers
+  float2 *bufs = reinterpret_cast<float2 *>(row_smem + 128);
+  const int L = d.L;
+  const float sign = FWD ? -1.0f : 1.0f;
+  const int G = gridDim.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0]);
+    mbar_init(&bar[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_proxy_async();
+  }
+  __syncthreads();
+  int row = blockIdx.x;
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar[0], in_bytes);
+    bulk_copy_g2s(bufs, in + (size_t)row * in_stride, in_bytes, &bar[0]);
+  }
+  uint32_t phase0 = 0, phase1 = 0;
+  for (int it = 0; row < n_rows; ++it, row += G) {
+    const int b = it & 1;
+    float2 *buf = bufs + (size_t)b * buf_elems;
+    const int next = row + G;
+    if (next < n_rows && threadIdx.x == 0) {
+      mbar_expect_tx(&bar[b ^ 1], in_bytes);
+      bulk_copy_g2s(bufs + (size_t)(b ^ 1) * buf_elems, in + (size_t)next * in_stride, in_bytes,
+                    &bar[b ^ 1]);
+    }
+    const bool ok = mbar_wait_bounded(&bar[b], b == 0 ? phase0 : phase1);
+    if (__syncthreads_or(!ok)) {
+      // a copy did not complete in time: record it, wait once more (bounded)
+      // for the copies still in flight, and leave
+      if (threadIdx.x == 0) atomicAdd(err, 1u);
+      mbar_wait_bounded(&bar[b], b == 0 ? phase0 : phase1);
+      if (next < n_rows) mbar_wait_bounded(&bar[b ^ 1], b == 0 ? phase1 : phase0);
+      return;
+    }
+    if (b == 0) phase0 ^= 1; else phase1 ^= 1;
+    row_stage_inplace<16, FWD ? kRowIn : kRowInPad>(buf, L, 1, d.magic[0], sign,
+                                                     tws + st.tw_off[0], width);
+    int p = 16, s = 1;
+    const int n_mid16 = d.n_stages - 2 - (MID8 ? 1 : 0);
+    for (int m = 0; m < n_mid16; ++m, ++s) {
+      row_stage_inplace<16, kRowInSlot>(buf, L, p, d.magic[s], sign, tws + st.tw_off[s], width);
+      p *= 16;
+    }
+    if (MID8) {
+      row_stage_inplace<8, kRowInSlot>(buf, L, p, d.magic[s], sign, tws + st.tw_off[s], width);
+      p *= 8;
+      ++s;
+    }
+    row_stage_last<LAST>(buf, L, p, sign, tws + st.tw_off[s]);
+    row_out<FWD>(buf, out + (size_t)row * out_stride, out_stride, L, width);
+    // generic accesses to this buffer end here; the bulk copy issued into it
+    // at the next iteration is ordered after them
+    fence_proxy_async();
+    __syncthreads();
+  }
+}
+
+// Out-of-place Stockham stage over the swizzled row layout.
+template <int R>
+__device__ __forceinline__ void row_stage_pp(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                             int L, int p, unsigned p_magic, float sign,
+                                             const float2 *__restrict__ tws) {
+  const int LR = L / R;
+  for (int i = threadIdx.x; i < LR; i += blockDim.x) {
+    float2 v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = src[row_slot(i + t * LR)];
+    const int j = row_butterfly<R>(v, i, p, p_magic, sign, tws);
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[row_slot(j + q * p)] = v[q];
+  }
+  __syncthreads();
+}
+
+// Ping-pong row kernel, one CTA per row (rows up to kRowPingPongMax).
+template <bool FWD>
+__global__ void __launch_bounds__(kRowPingPongMax / 16, 2)
+    fft_rows_pingpong_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
+                             const float2 *__restrict__ in, int in_stride,
+                             float2 *__restrict__ out, int out_stride, int width) {
   extern __shared__ float2 s[];
   const int L = d.L;
+  const float sign = FWD ? -1.0f : 1.0f;
   const size_t row = blockIdx.x;
-  for (int k = threadIdx.x; k < L; k += blockDim.x) s[k] = make_float2(0.f, 0.f);
+  float2 *buf0 = s, *buf1 = s + row_buffer(L);
+  if (FWD) {
+    const float4 *src = reinterpret_cast<const float4 *>(in + row * in_stride);
+    for (int k = threadIdx.x; k < L / 2; k += blockDim.x) {
+      const float4 v = __ldg(src + k);
+      buf0[row_slot(2 * k)] = make_float2(v.x, v.y);
+      buf0[row_slot(2 * k + 1)] = make_float2(v.z, v.w);
+    }
+  } else {
+    for (int k = threadIdx.x; k < L; k += blockDim.x) buf0[k] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const float2 *src = in + row * in_stride;
+    for (int x = threadIdx.x; x < width; x += blockDim.x)
+      buf0[row_slot(wrap(width / 2 - x, L))] = __ldg(src + x);
+  }
   __syncthreads();
-  const float2 *src = R + row * (size_t)rstride;
-  for (int x = threadIdx.x; x < width; x += blockDim.x) s[wrap(width / 2 - x, L)] = src[x];
-  __syncthreads();
-  const float2 *res = fft_smem<kRow>(s, s + L, d, +1.0f, tw);
-  float2 *dst = planes + row * (size_t)L;
-  for (int k = threadIdx.x; k < L / 2; k += blockDim.x)
-    reinterpret_cast<float4 *>(dst)[k] = reinterpret_cast<const float4 *>(res)[k];
+  float2 *a = buf0, *b = buf1;
+  int p = 1;
+  for (int st_i = 0; st_i < d.n_stages; ++st_i) {
+    const float2 *tw = tws + st.tw_off[st_i];
+    switch (d.radix[st_i]) {
+      case 16: row_stage_pp<16>(a, b, L, p, d.magic[st_i], sign, tw); break;
+      case 8: row_stage_pp<8>(a, b, L, p, d.magic[st_i], sign, tw); break;
+      case 4: row_stage_pp<4>(a, b, L, p, d.magic[st_i], sign, tw); break;
+      case 2: row_stage_pp<2>(a, b, L, p, d.magic[st_i], sign, tw); break;
+      case 3: row_stage_pp<3>(a, b, L, p, d.magic[st_i], sign, tw); break;
+      default: row_stage_pp<5>(a, b, L, p, d.magic[st_i], sign, tw); break;
+    }
+    p *= d.radix[st_i];
+    float2 *t = a;
+    a = b;
+    b = t;
+  }
+  row_out<FWD>(a, out + row * out_stride, out_stride, L, width);
 }
 
 // ------------------------------------------------------------- columns ----
@@ -438,38 +761,148 @@ __global__ void __launch_bounds__(kColThreads)
   }
 }
 
-// Threads for a row transform of length L (about L/8 butterflies per stage).
-int row_threads(int L) {
-  int t = (L / 8 + 31) / 32 * 32;
-  return t < 64 ? 64 : (t > 1024 ? 1024 : t);
-}
-
 void set_smem(const void *fn, size_t bytes) { ensure_dynamic_smem(fn, bytes); }
+
+int sm_count_fft() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    WGPU_CUDA(cudaGetDevice(&dev));
+    WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
+  return n;
+}
 
 }  // namespace
 
+// Per-stage twiddle tables of the row schedule of length L (cached).
+static const float2 *row_stage_twiddles(FftTables &t, const FftDesc &d, RowStages *st) {
+  std::lock_guard<std::mutex> lock(t.mu);
+  int p = 1, off = 0;
+  for (int s = 0; s < d.n_stages; ++s) {
+    st->tw_off[s] = off;
+    off += p * (d.radix[s] - 1);
+    p *= d.radix[s];
+  }
+  auto it = t.row_tables.find(d.L);
+  if (it != t.row_tables.end()) return it->second;
+  std::vector<float2> h((size_t)std::max(off, 1));
+  p = 1;
+  for (int s = 0; s < d.n_stages; ++s) {
+    const int R = d.radix[s];
+    for (int tt = 1; tt < R; ++tt)
+      for (int k = 0; k < p; ++k) {
+        // exp(-2 pi i t k / (p R)), argument reduced exactly in FP64
+        const long long num = (long long)tt * k % ((long long)p * R);
+        const double a = -2.0 * M_PI * (double)num / ((double)p * R);
+        h[st->tw_off[s] + (tt - 1) * p + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
+    p *= R;
+  }
+  float2 *dd = nullptr;
+  WGPU_CUDA(cudaMalloc(&dd, sizeof(float2) * h.size()));
+  WGPU_CUDA(cudaMemcpy(dd, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
+  t.row_tables[d.L] = dd;
+  return dd;
+}
+
+// Row lengths the persistent kernel handles (radix 16, radix-16 stages, an
+// optional radix-8 stage, one last stage of radix 2, 3 or 5).
+static bool persistent_schedule(const FftDesc &d, int *last, bool *mid8) {
+  if (d.n_stages < 2 || d.radix[0] != 16) return false;
+  *last = d.radix[d.n_stages - 1];
+  *mid8 = false;
+  for (int s = 1; s + 1 < d.n_stages; ++s) {
+    if (d.radix[s] == 16 && !*mid8) continue;
+    if (d.radix[s] == 8 && s + 2 == d.n_stages) { *mid8 = true; continue; }
+    return false;
+  }
+  return (*last == 2 && !*mid8) || (*last == 3 && !*mid8) || (*last == 5 && *mid8);
+}
+
+bool fft_row_length_supported(int L) {
+  if (L % 16 || L > kFftMaxRow) return false;
+  if (L <= kRowPingPongMax) return true;
+  FftDesc d;
+  try {
+    d = make_desc(L, true);
+  } catch (const Error &) {
+    return false;
+  }
+  int last;
+  bool mid8;
+  return persistent_schedule(d, &last, &mid8);
+}
+
+void fft_prepare_rows(FftTables &t, int L) {
+  RowStages st;
+  row_stage_twiddles(t, make_desc(L, true), &st);
+}
+
+template <bool FWD, int LAST, bool MID8>
+static void launch_persistent(const FftDesc &d, const RowStages &st, const float2 *tws,
+                              const DevPlan &p, const float2 *in, int in_stride, float2 *out,
+                              int out_stride, int n_rows, unsigned *err, cudaStream_t s) {
+  const int buf_elems = std::max(p.nu, in_stride);
+  const uint32_t in_bytes = (uint32_t)(sizeof(float2) * (FWD ? p.nu : in_stride));
+  if ((in_bytes & 15) || (buf_elems & 1))
+    throw Error(WGPU_ERR_INVALID, "row transform sizes must be multiples of 16 bytes");
+  const int threads = std::min(kRowThreadsMax, (p.nu / 16 + 31) / 32 * 32);
+  const size_t smem = 128 + 2 * sizeof(float2) * (size_t)buf_elems;
+  auto kern = fft_rows_persistent_kernel<FWD, LAST, MID8>;
+  set_smem((const void *)kern, smem);
+  int per_sm = 0;
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  if (per_sm < 1) throw Error(WGPU_ERR_INVALID, "row transform does not fit on an SM");
+  const int blocks = std::min(n_rows, sm_count_fft() * per_sm);
+  kern<<<blocks, threads, smem, s>>>(d, st, tws, in, in_stride, in_bytes, out, out_stride,
+                                      n_rows, p.width, buf_elems, err);
+  check_launch(FWD ? "fft_rows_persistent_kernel<forward>"
+                   : "fft_rows_persistent_kernel<backward>");
+}
+
+template <bool FWD>
+static void launch_rows(FftTables &t, const DevPlan &p, const float2 *in, int in_stride,
+                        float2 *out, int out_stride, int n_rows, unsigned *err,
+                        cudaStream_t s) {
+  if (n_rows <= 0) return;
+  if (p.nu % 16 || p.nu > kFftMaxRow)
+    throw Error(WGPU_ERR_INVALID, "row transform length must be a multiple of 16 up to 12288");
+  const FftDesc d = make_desc(p.nu, true);
+  RowStages st;
+  const float2 *tws = row_stage_twiddles(t, d, &st);
+  if (p.nu > kRowPingPongMax) {
+    int last;
+    bool mid8;
+    if (!persistent_schedule(d, &last, &mid8))
+      throw Error(WGPU_ERR_INVALID, "row length " + std::to_string(p.nu) +
+                                        " has no row transform schedule");
+    if (last == 2)
+      launch_persistent<FWD, 2, false>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+    else if (last == 3)
+      launch_persistent<FWD, 3, false>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+    else
+      launch_persistent<FWD, 5, true>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+    return;
+  }
+  const int threads = std::max(64, (p.nu / 16 + 31) / 32 * 32);
+  const size_t smem = 2 * sizeof(float2) * (size_t)row_buffer(p.nu);
+  set_smem((const void *)fft_rows_pingpong_kernel<FWD>, smem);
+  fft_rows_pingpong_kernel<FWD><<<(unsigned)n_rows, threads, smem, s>>>(
+      d, st, tws, in, in_stride, out, out_stride, p.width);
+  check_launch(FWD ? "fft_rows_pingpong_kernel<forward>" : "fft_rows_pingpong_kernel<backward>");
+}
+
 void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
                                   const float2 *planes, float2 *R, int rstride,
-                                  int n_batch, cudaStream_t s) {
-  const FftDesc d = make_desc(p.nu);
-  const float2 *tw = fft_twiddles(t, p.nu);
-  const size_t smem = 2 * sizeof(float2) * p.nu;
-  set_smem((const void *)fft_rows_forward_crop_kernel, smem);
-  fft_rows_forward_crop_kernel<<<(unsigned)((size_t)n_batch * p.nv), row_threads(p.nu), smem, s>>>(
-      d, planes, R, rstride, p.nv, p.width, tw);
-  check_launch("fft_rows_forward_crop_kernel");
+                                  int n_batch, unsigned *err, cudaStream_t s) {
+  launch_rows<true>(t, p, planes, p.nu, R, rstride, n_batch * p.nv, err, s);
 }
 
 void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
                                   const float2 *R, int rstride, float2 *planes,
-                                  int n_batch, cudaStream_t s) {
-  const FftDesc d = make_desc(p.nu);
-  const float2 *tw = fft_twiddles(t, p.nu);
-  const size_t smem = 2 * sizeof(float2) * p.nu;
-  set_smem((const void *)fft_rows_backward_pad_kernel, smem);
-  fft_rows_backward_pad_kernel<<<(unsigned)((size_t)n_batch * p.nv), row_threads(p.nu), smem, s>>>(
-      d, R, rstride, planes, p.nv, p.width, tw);
-  check_launch("fft_rows_backward_pad_kernel");
+                                  int n_batch, unsigned *err, cudaStream_t s) {
+  launch_rows<false>(t, p, R, rstride, planes, p.nu, n_batch * p.nv, err, s);
 }
 
 void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,

@@ -195,7 +195,10 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     // w planes); the grid spans at least two tiles per axis
     const int64_t tile = 16;
     if (req.force_tile > 0 && req.force_tile != tile) continue;
-    const int64_t nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
+    // row length: the next size with a row-transform schedule
+    int64_t nu = good_fft_size((int64_t)std::ceil(e.sigma * req.width), tile);
+    while (nu <= fft_row_max_length() && !fft_row_length_supported((int)nu))
+      nu = good_fft_size(nu + 1, tile);
     const int64_t nv = good_fft_size((int64_t)std::ceil(e.sigma * req.height), tile);
     if (e.support > tile) continue;
     int64_t f1, f2;

@@ -142,15 +142,22 @@ const float2 *fft_twiddles(FftTables &t, int n);
 FftTables *fft_tables_create();
 void fft_tables_destroy(FftTables *);
 int fft_row_max_length();
+// Whether the row transform supports length L (multiples of 16; above 6912
+// only 8192, 10240 and 12288).
+bool fft_row_length_supported(int L);
 // Row pass, forward: planes [B][nv][nu] -> R [B][nv][rstride] keeping the
 // trimmed columns.
-void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
-                                  const float2 *planes, float2 *R, int rstride,
-                                  int n_batch, cudaStream_t s);
+// Row transforms (persistent, TMA-prefetched).  err counts bounded waits that
+// expired (a device word the caller checks after the call).
+void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p, const float2 *planes,
+                                  float2 *R, int rstride, int n_batch, unsigned *err,
+                                  cudaStream_t s);
 // Row pass, backward: R -> planes (full rows).
-void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
-                                  const float2 *R, int rstride, float2 *planes,
-                                  int n_batch, cudaStream_t s);
+void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p, const float2 *R,
+                                  int rstride, float2 *planes, int n_batch, unsigned *err,
+                                  cudaStream_t s);
+// Creates the row-transform tables of length L (before a graph capture).
+void fft_prepare_rows(FftTables &t, int L);
 // Column passes (four-step split nv = n1 * n2, see fft.cu): pass A over
 // strided length-n1 transforms, pass B over contiguous length-n2 transforms
 // with the fused w-screen.
