@@ -642,14 +642,59 @@ __device__ __forceinline__ int image_row_of(int k, int nv, int height) {
   return -1;
 }
 
-__device__ __forceinline__ void screen(double wq, double nu, float *s, float *c) {
-  double t = wq * nu;
-  t -= rint(t);
-  sincospif(2.0f * (float)t, s, c);
+// Phase of the w-screen for the planes b of a batch: t_b = (wq0 + b dw) nu
+// turns.  The FP64 products wq0 nu and dw nu are reduced modulo 1 once per
+// pixel; dw nu is split into a head with 16 fractional bits, for which b * head
+// is exact in FP32 (b < 256), and a tail below 2^-17.  The FP32 sum then
+// carries an error of about 1e-7 turns.
+constexpr float kNoPixel = 8.0f;  // phase marker of panel elements outside the image
+__device__ __forceinline__ void screen_phase(double wq0, double dw, double nu, float *a,
+                                             float *bh, float *bl) {
+  double ta = wq0 * nu;
+  ta -= rint(ta);
+  double tb = dw * nu;
+  tb -= rint(tb);
+  const double h = rint(tb * 65536.0) * (1.0 / 65536.0);
+  *a = (float)ta;
+  *bh = (float)h;
+  *bl = (float)(tb - h);
+}
+__device__ __forceinline__ void screen_b(float a, float bh, float bl, int b, float *sn,
+                                         float *cs) {
+  float h = (float)b * bh;  // exact
+  h -= rintf(h);
+  float t = a + h + (float)b * bl;
+  t -= rintf(t);
+  sincospif(2.0f * t, sn, cs);
 }
 
-// Pass B (forward) with the fused w-screen and accumulation over the batch.
-__global__ void __launch_bounds__(kColThreads)
+// Shared layout of the column-B kernels: the two FFT buffers (n2 * kPanel
+// each), then the per-element phase terms a, bh, bl (n2 * kPanel each).
+__host__ __device__ constexpr size_t cols_b_smem(int n2) {
+  return (size_t)n2 * kPanel * (2 * sizeof(float2) + 3 * sizeof(float));
+}
+
+// Phase terms of the panel elements of this block (kNoPixel outside the image).
+__device__ __forceinline__ void cols_b_phases(const DevPlan &p, int n1, int n2, int cg, int k1,
+                                              int p_begin, const double *__restrict__ nu_w,
+                                              float *pa, float *pbh, float *pbl) {
+  const double wq0 = p.w0 + (double)p_begin * p.dw;
+  for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
+    const int k2 = e / kPanel, col = e % kPanel;
+    const int x = cg * kPanel + col;
+    const int y = image_row_of(k1 + n1 * k2, p.nv, p.height);
+    if (x < p.width && y >= 0) {
+      screen_phase(wq0, p.dw, __ldg(nu_w + (size_t)y * p.width + x), &pa[e], &pbh[e], &pbl[e]);
+    } else {
+      pa[e] = kNoPixel;
+    }
+  }
+}
+
+// Pass B (forward) with the fused w-screen and accumulation over the batch;
+// NE >= n2 * kPanel / blockDim.x accumulators per thread.
+template <int NE>
+__global__ void __launch_bounds__(kColThreads, 2)
     fft_cols_forward_accumulate_kernel(FftDesc d2, DevPlan p, int n1,
                                        float2 *__restrict__ R, int rstride,
                                        int n_batch, int p_begin,
@@ -660,30 +705,30 @@ __global__ void __launch_bounds__(kColThreads)
   const int n2 = d2.L;
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
-  constexpr int NE = kMaxElemsPerThread;
+  const int ne = n2 * kPanel;
+  float *pa = reinterpret_cast<float *>(s + 2 * ne);
+  float *pbh = pa + ne, *pbl = pbh + ne;
+  cols_b_phases(p, n1, n2, cg, k1, p_begin, nu_w, pa, pbh, pbl);
   float part[NE];
 #pragma unroll
   for (int c = 0; c < NE; ++c) part[c] = 0.f;
   for (int b = 0; b < n_batch; ++b) {
     const float2 *base = R + (size_t)b * nv * rstride + (size_t)n2 * k1 * rstride + cg * kPanel;
-    for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
       const int r2 = e / kPanel, c = e % kPanel;
       s[e] = base[(size_t)r2 * rstride + c];
     }
     __syncthreads();
-    const float2 *res = fft_smem<kPanelLayout>(s, s + n2 * kPanel, d2, -1.0f, tw2);
-    const double wq = p.w0 + (double)(p_begin + b) * p.dw;
+    const float2 *res = fft_smem<kPanelLayout>(s, s + ne, d2, -1.0f, tw2);
 #pragma unroll
     for (int c = 0; c < NE; ++c) {
       const int e = threadIdx.x + c * blockDim.x;
-      if (e < n2 * kPanel) {
-        const int k2 = e / kPanel, col = e % kPanel;
-        const int x = cg * kPanel + col;
-        const int y = image_row_of(k1 + n1 * k2, nv, p.height);
-        if (x < p.width && y >= 0) {
+      if (e < ne) {
+        const float a = pa[e];
+        if (a != kNoPixel) {
           const float2 v = res[e];
           float sn, cs;
-          screen(wq, __ldg(nu_w + (size_t)y * p.width + x), &sn, &cs);
+          screen_b(a, pbh[e], pbl[e], b, &sn, &cs);
           // Re(v exp(-2 pi i t)) = v.re cos + v.im sin
           part[c] += v.x * cs + v.y * sn;
         }
@@ -694,26 +739,25 @@ __global__ void __launch_bounds__(kColThreads)
 #pragma unroll
   for (int c = 0; c < NE; ++c) {
     const int e = threadIdx.x + c * blockDim.x;
-    if (e < n2 * kPanel) {
+    if (e < ne && pa[e] != kNoPixel) {
       const int k2 = e / kPanel, col = e % kPanel;
       const int x = cg * kPanel + col;
       const int y = image_row_of(k1 + n1 * k2, nv, p.height);
-      if (x < p.width && y >= 0) {
-        float2 *a = acc + (size_t)y * p.width + x;
-        float2 sc = *a;  // (sum, compensation)
-        const float yv = part[c] - sc.y;
-        const float t = sc.x + yv;
-        sc.y = (t - sc.x) - yv;
-        sc.x = t;
-        *a = sc;
-      }
+      float2 *a = acc + (size_t)y * p.width + x;
+      float2 sc = *a;  // (sum, compensation)
+      const float yv = part[c] - sc.y;
+      const float t = sc.x + yv;
+      sc.y = (t - sc.x) - yv;
+      sc.x = t;
+      *a = sc;
     }
   }
 }
 
 // Pass B' (backward): screened, pre-corrected image rows -> length-n2
 // backward transforms -> twiddle -> R rows n2*k1 + r2.
-__global__ void __launch_bounds__(kColThreads)
+template <int NE>
+__global__ void __launch_bounds__(kColThreads, 2)
     fft_cols_backward_screen_kernel(FftDesc d2, DevPlan p, int n1,
                                     const float *__restrict__ img_corr,
                                     const double *__restrict__ nu_w,
@@ -725,29 +769,41 @@ __global__ void __launch_bounds__(kColThreads)
   const int n2 = d2.L;
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
-  for (int b = 0; b < n_batch; ++b) {
-    const double wq = p.w0 + (double)(p_begin + b) * p.dw;
-    for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
+  const int ne = n2 * kPanel;
+  float *pa = reinterpret_cast<float *>(s + 2 * ne);
+  float *pbh = pa + ne, *pbl = pbh + ne;
+  cols_b_phases(p, n1, n2, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  float val[NE];  // pre-corrected image value of each element
+#pragma unroll
+  for (int c = 0; c < NE; ++c) {
+    const int e = threadIdx.x + c * blockDim.x;
+    val[c] = 0.f;
+    if (e < ne) {
       const int k2 = e / kPanel, col = e % kPanel;
       const int x = cg * kPanel + col;
       const int y = image_row_of(k1 + n1 * k2, nv, p.height);
-      float2 v = make_float2(0.f, 0.f);
-      if (x < p.width && y >= 0) {
-        const size_t i = (size_t)y * p.width + x;
-        const float a = __ldg(img_corr + i);
-        if (a != 0.0f) {
+      if (x < p.width && y >= 0) val[c] = __ldg(img_corr + (size_t)y * p.width + x);
+    }
+  }
+  __syncthreads();
+  for (int b = 0; b < n_batch; ++b) {
+#pragma unroll
+    for (int c = 0; c < NE; ++c) {
+      const int e = threadIdx.x + c * blockDim.x;
+      if (e < ne) {
+        float2 v = make_float2(0.f, 0.f);
+        if (val[c] != 0.0f) {
           float sn, cs;
-          screen(wq, __ldg(nu_w + i), &sn, &cs);
-          // a exp(+2 pi i t)
-          v = make_float2(a * cs, a * sn);
+          screen_b(pa[e], pbh[e], pbl[e], b, &sn, &cs);
+          v = make_float2(val[c] * cs, val[c] * sn);  // a exp(+2 pi i t)
         }
+        s[e] = v;
       }
-      s[e] = v;
     }
     __syncthreads();
-    const float2 *res = fft_smem<kPanelLayout>(s, s + n2 * kPanel, d2, +1.0f, tw2);
+    const float2 *res = fft_smem<kPanelLayout>(s, s + ne, d2, +1.0f, tw2);
     float2 *base = R + (size_t)b * nv * rstride + (size_t)n2 * k1 * rstride + cg * kPanel;
-    for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
       const int r2 = e / kPanel, c = e % kPanel;
       float2 v = res[e];
       if (n1 > 1) {
@@ -925,11 +981,18 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
                                           cudaStream_t s) {
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
-  const size_t smem = 2 * sizeof(float2) * n2 * kPanel;
-  set_smem((const void *)fft_cols_forward_accumulate_kernel, smem);
+  const size_t smem = cols_b_smem(n2);
   dim3 grid(ncg, n1);
-  fft_cols_forward_accumulate_kernel<<<grid, kColThreads, smem, s>>>(
-      d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, fft_twiddles(t, n2));
+  const float2 *tw = fft_twiddles(t, n2);
+  if (n2 * kPanel <= 8 * kColThreads) {
+    set_smem((const void *)fft_cols_forward_accumulate_kernel<8>, smem);
+    fft_cols_forward_accumulate_kernel<8><<<grid, kColThreads, smem, s>>>(
+        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw);
+  } else {
+    set_smem((const void *)fft_cols_forward_accumulate_kernel<16>, smem);
+    fft_cols_forward_accumulate_kernel<16><<<grid, kColThreads, smem, s>>>(
+        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw);
+  }
   check_launch("fft_cols_forward_accumulate_kernel");
 }
 
@@ -940,12 +1003,18 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        cudaStream_t s) {
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
-  const size_t smem = 2 * sizeof(float2) * n2 * kPanel;
-  set_smem((const void *)fft_cols_backward_screen_kernel, smem);
+  const size_t smem = cols_b_smem(n2);
   dim3 grid(ncg, n1);
-  fft_cols_backward_screen_kernel<<<grid, kColThreads, smem, s>>>(
-      d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin,
-      fft_twiddles(t, n2), fft_twiddles(t, p.nv));
+  const float2 *tw = fft_twiddles(t, n2), *twN = fft_twiddles(t, p.nv);
+  if (n2 * kPanel <= 8 * kColThreads) {
+    set_smem((const void *)fft_cols_backward_screen_kernel<8>, smem);
+    fft_cols_backward_screen_kernel<8><<<grid, kColThreads, smem, s>>>(
+        d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN);
+  } else {
+    set_smem((const void *)fft_cols_backward_screen_kernel<16>, smem);
+    fft_cols_backward_screen_kernel<16><<<grid, kColThreads, smem, s>>>(
+        d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN);
+  }
   check_launch("fft_cols_backward_screen_kernel");
 }
 
