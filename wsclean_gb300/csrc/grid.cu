@@ -322,9 +322,18 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Degridding of one plane batch, one warp per visibility: lanes own footprint
-// cells, each lane accumulates its cells over the planes of the group from the
-// shared halo region, and a warp-level shuffle reduction forms the sum.
+// Degridding of one plane batch, one warp per visibility: the block loads
+// its unit's halo region (the tile plus W - 1 cells, G planes) into shared
+// memory as float2 cells with a row stride of T + W rounded to 8 mod 16 (a
+// half-warp's two rows x eight columns then fall on distinct bank pairs);
+// lanes own footprint cells, accumulate their cells over the planes of the
+// group, and a warp-level shuffle reduction forms the sum.
+__host__ __device__ constexpr int degrid_row_stride(int R) { return (R + 7) / 16 * 16 + 8; }
+template <int T, int G, int W>
+constexpr size_t degrid_smem_bytes() {
+  return sizeof(float2) * G * (T + W - 1) * degrid_row_stride(T + W - 1);
+}
+
 template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     degrid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
@@ -333,13 +342,11 @@ __global__ void __launch_bounds__(kThreads)
                   uint32_t total, const float2 *__restrict__ planes,
                   float2 *__restrict__ acc) {
   constexpr int R = T + W - 1;
-  constexpr int RS = padded_stride(R, W);
+  constexpr int RS = degrid_row_stride(R);
   constexpr int kPlane = R * RS;
   constexpr int kFoot = W * W;
   constexpr int kLaneCells = (kFoot + 31) / 32;
-  extern __shared__ float smem[];
-  float *gre = smem;               // [G][R][RS]
-  float *gim = smem + G * kPlane;  // [G][R][RS]
+  extern __shared__ float2 halo[];  // [G][R][RS]
   __shared__ uint32_t rs0[4], rcum[5];
   __shared__ float4 stage[kThreads][2];
   __shared__ uint32_t stage_s[kThreads];
@@ -364,10 +371,8 @@ __global__ void __launch_bounds__(kThreads)
       if (gv >= p.nv) gv -= p.nv;
       int gu = tu * T + c;
       if (gu >= p.nu) gu -= p.nu;
-      const float2 g =
-          planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu];
-      gre[pq * kPlane + r * RS + c] = g.x;
-      gim[pq * kPlane + r * RS + c] = g.y;
+      halo[pq * kPlane + r * RS + c] =
+          __ldg(planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu);
     }
     if (threadIdx.x < 4) {
       uint32_t a, b;
@@ -384,70 +389,71 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
     for (uint32_t rb = lo; rb < hi; rb += kThreads) {
-     {
-      const uint32_t pos = rb + threadIdx.x;
-      if (pos < hi) {
-        int r = 0;
-        while (pos >= rcum[r + 1]) ++r;
-        const uint32_t s = rs0[r] + (pos - rcum[r]);
-        const float4 *src = reinterpret_cast<const float4 *>(rec + s);
-        stage[threadIdx.x][0] = __ldg(src);
-        stage[threadIdx.x][1] = __ldg(src + 1);
-        stage_s[threadIdx.x] = s;
-      }
-     }
-     __syncthreads();
-     const int n_round = (int)min((uint32_t)kThreads, hi - rb);
-     for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
-      const uint32_t s = stage_s[m];
-      VisRecord v;
       {
-        const float4 a = stage[m][0], b = stage[m][1];
-        v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
-        v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
+        const uint32_t pos = rb + threadIdx.x;
+        if (pos < hi) {
+          int r = 0;
+          while (pos >= rcum[r + 1]) ++r;
+          const uint32_t s = rs0[r] + (pos - rcum[r]);
+          const float4 *src = reinterpret_cast<const float4 *>(rec + s);
+          stage[threadIdx.x][0] = __ldg(src);
+          stage[threadIdx.x][1] = __ldg(src + 1);
+          stage_s[threadIdx.x] = s;
+        }
       }
-      const int iu_rel = v.iu - tu * T;
-      const int iv_rel = v.iv - tv * T;
-      const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
-      if (pa > pb) continue;  // uniform in the warp
-      const bool lx = lane < W;
-      const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
-      float k1 = es_eval(p.beta, f1 * inv_half);
-      k1 = lane < 2 * W ? k1 : 0.f;
-      float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
-      if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
-      float wgt[kLaneCells];
-      int idx[kLaneCells];
-#pragma unroll
-      for (int k = 0; k < kLaneCells; ++k) {
-        const int c = lane + 32 * k;
-        const int i = c % W, j = c / W;
-        const float kx = __shfl_sync(0xffffffffu, k1, i);
-        const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
-        wgt[k] = c < kFoot ? kx * ky : 0.f;
-        idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : 0;
-      }
-      float sr = 0.f, si = 0.f;
-      for (int q = pa; q <= pb; ++q) {
-        const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
-        const float *pre = gre + (q - q0) * kPlane, *pim = gim + (q - q0) * kPlane;
-        float pr = 0.f, pi = 0.f;
+      __syncthreads();
+      const int n_round = (int)min((uint32_t)kThreads, hi - rb);
+      for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
+        const uint32_t s = stage_s[m];
+        VisRecord v;
+        {
+          const float4 a = stage[m][0], b = stage[m][1];
+          v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
+          v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
+        }
+        const int iu_rel = v.iu - tu * T;
+        const int iv_rel = v.iv - tv * T;
+        const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
+        if (pa > pb) continue;  // uniform in the warp
+        const bool lx = lane < W;
+        const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
+        float k1 = es_eval(p.beta, f1 * inv_half);
+        k1 = lane < 2 * W ? k1 : 0.f;
+        float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+        if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
+        float wgt[kLaneCells];
+        int idx[kLaneCells];
 #pragma unroll
         for (int k = 0; k < kLaneCells; ++k) {
-          pr += wgt[k] * pre[idx[k]];
-          pi += wgt[k] * pim[idx[k]];
+          const int c = lane + 32 * k;
+          const int i = c % W, j = c / W;
+          const float kx = __shfl_sync(0xffffffffu, k1, i);
+          const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
+          wgt[k] = c < kFoot ? kx * ky : 0.f;
+          idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : 0;
         }
-        sr += kw * pr;
-        si += kw * pi;
-      }
+        float sr = 0.f, si = 0.f;
+        for (int q = pa; q <= pb; ++q) {
+          const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
+          const float2 *pl = halo + (q - q0) * kPlane;
+          float pr = 0.f, pi = 0.f;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(0xffffffffu, sr, o);
-        si += __shfl_xor_sync(0xffffffffu, si, o);
+          for (int k = 0; k < kLaneCells; ++k) {
+            const float2 g = pl[idx[k]];
+            pr = fmaf(wgt[k], g.x, pr);
+            pi = fmaf(wgt[k], g.y, pi);
+          }
+          sr = fmaf(kw, pr, sr);
+          si = fmaf(kw, pi, si);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sr += __shfl_xor_sync(0xffffffffu, sr, o);
+          si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
       }
-      if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
-     }
-     __syncthreads();
+      __syncthreads();
     }
   }
 }
@@ -540,8 +546,7 @@ void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, i
                   int n_batch, const WorkItems &wi, const float2 *planes, float2 *acc,
                   cudaStream_t s) {
   if (wi.total == 0) return;
-  constexpr int R = T + W - 1;
-  const size_t smem = sizeof(float) * 2 * G * R * padded_stride(R, W);
+  const size_t smem = degrid_smem_bytes<T, G, W>();
   ensure_dynamic_smem((const void *)degrid_kernel<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degrid_kernel<T, G, W>,
@@ -588,7 +593,10 @@ void check_plan(const DevPlan &p) {
   if (p.tile != kTile) throw Error(WGPU_ERR_INVALID, "uv tile must be 16 cells");
 }
 
-int degrid_group(const DevPlan &p) { return p.support <= 8 ? 16 : 8; }
+// w planes per degridding unit: 8 keeps the halo region of a 16x16 tile at
+// ~35 KB (W = 8), five blocks per SM; 16 planes halve the record reads but
+// allow only two blocks per SM, which measured 1.3x slower.
+constexpr int kDegridPlanes = 8;
 
 }  // namespace
 
@@ -603,9 +611,7 @@ WorkItems plan_grid_items(const DevPlan &p, const uint32_t *off, int p_begin, in
 WorkItems plan_degrid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
                             const ItemAlloc &alloc, cudaStream_t s) {
   check_plan(p);
-  if (degrid_group(p) == 16)
-    return plan_items<kTile, 16>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
-  return plan_items<kTile, 8>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
+  return plan_items<kTile, kDegridPlanes>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
 }
 
 void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
@@ -627,10 +633,8 @@ void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t 
                          int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
                          float2 *acc, cudaStream_t s) {
   check_plan(p);
-  if (degrid_group(p) == 16)
-    degrid_dispatch<kTile, 16>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
-  else
-    degrid_dispatch<kTile, 8>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+  degrid_dispatch<kTile, kDegridPlanes>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc,
+                                        s);
 }
 
 static ItemAlloc arena_alloc(DeviceArena &arena) {
