@@ -34,6 +34,10 @@ WORKLOAD_TEXT = {
                  "32640 baselines x 300 x 8 s, 64 channels 0.9-1.7 GHz, 500 sources, eps 1e-5"),
     "wide2048": ("profiling-size wide field: the wide-field array, 3arcsec pixels and band on "
                  "a 2048x2048 image, 32640 baselines x 8 x 8 s, 64 channels, eps 1e-5"),
+    "fullpol4096": ("full polarisation 4096x4096, 10arcsec pixels, 64 antennas in a 3 km disk, "
+                    "2016 baselines x 60 x 10 s, 32 channels 120-180 MHz, XX/XY/YX/YY from 20 "
+                    "sources with random Stokes Q, U, V (|pol frac| <= 0.3), per-antenna full "
+                    "Jones solutions per time step and channel, eps 1e-4"),
     "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
                   "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
 }
@@ -434,6 +438,118 @@ def run_gpu(args, rank, world, local):
     return result
 
 
+# ------------------------------------------------------- full polarisation ---
+def run_fullpol(args):
+    """Corrected inversion (full-Jones gains applied on the device, collapsed to
+    Stokes I) followed by prediction of the model image, through the host API;
+    accuracy against the oracle's gain application and FP64 DFT on a sample."""
+    import torch
+    import oracle
+    from wsclean_gb300 import synthetic
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    d = synthetic.make_workload("fullpol4096", seed=3, with_model=False)
+    vis4, ant, tof, sol, n_t = synthetic.full_polarisation(d, dev)
+    gen_s = time.time() - t0
+    n_rows, n_chan, n_ant = d["uvw"].shape[0], d["freq"].size, d["n_ant"]
+    W, dl, eps = d["width"], d["dl"], d["epsilon"]
+    model = np.zeros(W * W, np.float32)
+    for l, m, sflux in d["sources"]:
+        x, y = int(round(W / 2 - l / dl)), int(round(m / dl + W / 2))
+        if 0 <= x < W and 0 <= y < W:
+            model[y * W + x] += sflux
+    uvw = pinned_copy(torch.as_tensor(d["uvw"])).numpy()
+    freq = d["freq"]
+    vis_p = pinned_copy(torch.as_tensor(vis4)).numpy()
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, os.cpu_count(), epsilon=eps)
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+    out = {}
+
+    def step():
+        g.InitializeInversion()
+        g.AddInversionDataWithCorrectionCallback("full", 4, n_rows, uvw, freq, n_chan, ant, vis_p,
+                                                 tof, sol, 4, n_t, n_ant)
+        g.FinalizeImage(1.0)
+        out["img"] = g.RealImage()
+        g.InitializePrediction(model)
+        out["pv"] = g.PredictVisibilities(n_rows, n_chan, uvw, freq)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    launches = _lib_launches() - l0
+    ms = max(start.elapsed_time(end), wall * 1e3) / args.steps
+    n_vis = n_rows * n_chan
+    plan = g.last_plan()
+    # accuracy on a seeded row sample, with the full-data plan pinned
+    rng = np.random.default_rng(7)
+    rows = np.sort(rng.choice(n_rows, 300, replace=False))
+    corrected = oracle.apply_gains(4, 4, vis4[rows], ant[rows], tof[rows], sol, 4, n_ant)
+    gs = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=eps)
+    gs.pin_plan(plan)
+    gs.InitializeInversion()
+    gs.AddInversionDataWithCorrectionCallback("full", 4, rows.size, d["uvw"][rows], freq, n_chan,
+                                              ant[rows], vis4[rows], tof[rows], sol, 4, n_t,
+                                              n_ant)
+    img = gs.RealImage().astype(np.float64)
+    pix = rng.choice(W * W, 4096, replace=False)
+    ref = oracle.dft_invert(d["uvw"][rows], freq, corrected, W, W, dl, dl, pixels=pix,
+                            n_threads=os.cpu_count())
+    inv_err = float(np.linalg.norm(img[pix] - ref) / np.linalg.norm(ref))
+    gs.InitializePrediction(model)
+    pv = gs.PredictVisibilities(rows.size, n_chan, d["uvw"][rows], freq)
+    sel = rng.choice(pv.size, 4096, replace=False)
+    pr = oracle.dft_predict(d["uvw"][rows], freq, model, W, W, dl, dl, vis_index=sel,
+                            n_threads=os.cpu_count())
+    pred_err = float(np.linalg.norm(pv[sel] - pr) / np.linalg.norm(pr))
+    gs.close()
+    g.close()
+    value = n_vis / (ms * 1e-3) / 1e9
+    h2d = uvw.nbytes * 2 + freq.nbytes * 2 + vis_p.nbytes + ant.nbytes + tof.nbytes + sol.nbytes + model.nbytes
+    d2h = n_vis * 8 + W * W * 4
+    return {
+        "metric": "Gvis/s corrected inversion + prediction (full-Jones gains, Stokes I)",
+        "value": value, "unit": "Gvis/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT["fullpol4096"], "n_rows": n_rows,
+                   "n_vis": n_vis, "correlations_per_vis": 4,
+                   "step": "InitializeInversion + AddInversionDataWithCorrectionCallback(full, "
+                           "4 pol, Stokes I) + FinalizeImage + RealImage + InitializePrediction "
+                           "+ PredictVisibilities, host buffers",
+                   "plan": {k: getattr(plan, k) for k in ("nu", "support", "sigma", "n_planes",
+                                                          "plane_batch", "est_error")},
+                   "accuracy": {"invert_rel_l2": inv_err, "predict_rel_l2": pred_err,
+                                "sample": "300 rows x 32 channels: oracle gains + FP64 DFT on "
+                                          "4096 pixels (invert), 4096 vis (predict)"},
+                   "datagen_s": round(gen_s, 1)},
+        "clocks": clk,
+        "e2e": {"value": value, "unit": "Gvis/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+    }
+
+
+def _lib_launches():
+    from wsclean_gb300 import _lib
+    return _lib.lib().wgpu_kernel_launch_count()
+
+
 # ---------------------------------------------------------------- serving ---
 def run_serving(args, device_bytes):
     """Mixed-size request stream through the request server (scaled serving
@@ -555,6 +671,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.workload == "fullpol4096":
+        print(json.dumps(run_fullpol(args)), flush=True)
         return
     if args.serve_only:
         import torch

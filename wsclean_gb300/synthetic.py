@@ -217,3 +217,42 @@ def random_points(n_rows, n_chan, width, dl, seed, w_scale=1.0, f0=1e8, f1=2e8,
     if frac_zero > 0:
         vis[rng.uniform(size=vis.shape) < frac_zero] = 0
     return uvw, freq, vis
+
+
+def full_polarisation(d, device, seed=3, pol_fraction=0.3, gain_scatter=0.1, n_times=None):
+    """Four-correlation visibilities (XX, XY, YX, YY) of the workload's sources
+    with random Stokes Q, U, V (|pol fraction| <= pol_fraction) for linear
+    feeds: XX = I + Q, XY = U + iV, YX = U - iV, YY = I - Q; plus per-antenna
+    full-Jones solutions (identity + complex Gaussian scatter) per time step and
+    channel, indexed ((t * n_chan + ch) * n_ant + ant) * 4 + parm.  Returns
+    (vis [rows, chan, 4] complex64 on the host, antennas [rows, 2] u64, time
+    offsets [rows] u64, solutions, n_times)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    src = d["sources"]
+    n = src.shape[0]
+    frac = rng.uniform(-pol_fraction, pol_fraction, (n, 3)) / np.sqrt(3.0)
+    stokes = {"I": src[:, 2], "Q": src[:, 2] * frac[:, 0], "U": src[:, 2] * frac[:, 1],
+              "V": src[:, 2] * frac[:, 2]}
+    parts = {}
+    for k, s in stokes.items():
+        srck = src.copy()
+        srck[:, 2] = s
+        parts[k] = model_vis_torch(d["uvw"], d["freq"], srck, device)
+    vis = torch.stack([parts["I"] + parts["Q"], parts["U"] + 1j * parts["V"],
+                       parts["U"] - 1j * parts["V"], parts["I"] - parts["Q"]], dim=-1)
+    del parts
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    vis = vis + 0.01 * np.sqrt(2.0) * torch.randn(vis.shape, generator=g, dtype=vis.dtype,
+                                                  device=device)
+    vis = vis.cpu().numpy().astype(np.complex64)
+    n_t = int(d["n_t"]) if n_times is None else int(n_times)
+    n_ant, n_chan = int(d["n_ant"]), d["freq"].size
+    eye = np.array([1, 0, 0, 1], np.complex64)
+    sol = (eye[None, None, None, :] + gain_scatter * (
+        rng.standard_normal((n_t, n_chan, n_ant, 4)) +
+        1j * rng.standard_normal((n_t, n_chan, n_ant, 4)))).astype(np.complex64)
+    ant = np.stack([d["ant1"], d["ant2"]], axis=1).astype(np.uint64)
+    tof = (d["time_index"] % n_t).astype(np.uint64)
+    return np.ascontiguousarray(vis), ant, tof, sol, n_t
