@@ -383,6 +383,56 @@ int wgpu_server_stats(wgpu_server_t *server, wgpu_server_stats_t *stats);
 /* Finishes the queued requests, then stops the workers and frees everything. */
 void wgpu_server_destroy(wgpu_server_t *server);
 
+/* ------------------------------------------------------------------------ */
+/* Batched facets: many gridding jobs in one launch per wave                  */
+/* ------------------------------------------------------------------------ */
+
+/* Counterpart of MSGridderManager::BatchInvert with shared reads
+ * (gridding/msgriddermanager.cpp:118-396): one visibility set imaged into
+ * many facets (own size, pixel size and phase-centre shift, as
+ * GriddingTaskFactory sets them, scheduling/griddingtaskfactory.cpp:24-34),
+ * each for every output-channel group.  A job is (facet, channel group),
+ * numbered group * n_facets + facet.
+ *   create: channel_groups holds n_groups + 1 increasing channel boundaries.
+ *   bind:   uploads uvw / freq once, plans every job with one kernel support
+ *           width (the width with the lowest summed cost-model time), buckets
+ *           every job, packs the jobs' 16-plane batches into waves under
+ *           plane_budget_bytes (0 = 40 GB) and captures the whole inversion
+ *           in one CUDA graph: per wave, one persistent gridding launch over
+ *           all the wave's jobs, then each job's FFT passes.
+ *   invert: visibilities [row][chan] complex64 in, and the dirty images of
+ *           all jobs out, concatenated in job order, each width * height
+ *           float row-major [x + y * width] (not divided by any weight).
+ * The whole visibility set and every job's sorted records stay on the device
+ * until destroy; size the set to fit. */
+typedef struct wgpu_facet {
+  size_t width, height;           /* even */
+  double pixel_size_x, pixel_size_y;
+  double l_shift, m_shift;        /* facet centre relative to the phase centre */
+} wgpu_facet_t;
+
+typedef struct wgpu_facets_info {
+  uint64_t n_jobs, n_waves, support, graph_kernels, image_elems;
+  double job_visibilities; /* samples gridded over all jobs per inversion */
+  double last_ms;          /* device time of the last inversion, incl. copies */
+} wgpu_facets_info_t;
+
+typedef struct wgpu_facets wgpu_facets_t;
+
+int wgpu_facets_create(const wgpu_facet_t *facets, size_t n_facets,
+                       const size_t *channel_groups, size_t n_groups,
+                       double epsilon, double plane_budget_bytes,
+                       wgpu_facets_t **facets_out);
+int wgpu_facets_bind(wgpu_facets_t *facets, size_t n_rows, size_t n_chan,
+                     const double *uvw, const double *freq);
+int wgpu_facets_invert(wgpu_facets_t *facets, const float *vis, float *images);
+int wgpu_facets_invert_device(wgpu_facets_t *facets, const float *d_vis,
+                              float *d_images);
+int wgpu_facets_info(const wgpu_facets_t *facets, wgpu_facets_info_t *info);
+int wgpu_facets_job_plan(const wgpu_facets_t *facets, size_t job, wgpu_plan_t *plan);
+void *wgpu_facets_stream(wgpu_facets_t *facets);
+void wgpu_facets_destroy(wgpu_facets_t *facets);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,19 @@ class ServerStats(C.Structure):
                 ("visibilities", C.c_double), ("elapsed_s", C.c_double)]
 
 
+class Facet(C.Structure):
+    """wgpu_facet_t: one facet of a facet batch."""
+    _fields_ = [("width", C.c_size_t), ("height", C.c_size_t),
+                ("pixel_size_x", C.c_double), ("pixel_size_y", C.c_double),
+                ("l_shift", C.c_double), ("m_shift", C.c_double)]
+
+
+class FacetsInfo(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("n_jobs", "n_waves", "support", "graph_kernels",
+                                           "image_elems")] + \
+               [("job_visibilities", C.c_double), ("last_ms", C.c_double)]
+
+
 REQUEST_INVERT = 1
 REQUEST_PREDICT = 2
 
@@ -125,6 +138,14 @@ _PROTOS = {
     "wgpu_server_close_session": (I, [P, C.c_uint64]),
     "wgpu_server_stats": (I, [P, C.POINTER(ServerStats)]),
     "wgpu_server_destroy": (None, [P]),
+    "wgpu_facets_create": (I, [C.POINTER(Facet), SZ, C.POINTER(SZ), SZ, D, D, C.POINTER(P)]),
+    "wgpu_facets_bind": (I, [P, SZ, SZ, P, P]),
+    "wgpu_facets_invert": (I, [P, P, P]),
+    "wgpu_facets_invert_device": (I, [P, P, P]),
+    "wgpu_facets_info": (I, [P, C.POINTER(FacetsInfo)]),
+    "wgpu_facets_job_plan": (I, [P, SZ, C.POINTER(Plan)]),
+    "wgpu_facets_stream": (P, [P]),
+    "wgpu_facets_destroy": (None, [P]),
 }
 
 

@@ -1,0 +1,514 @@
+// Batched facets: many gridding jobs (facets of their own size and phase
+// centre, times output-channel groups) on one visibility set.
+//
+// This is the GPU counterpart of WSClean's shared-read batch inversion
+// (MSGridderManager::BatchInvert / ReadChunkForInvertImplementation,
+// gridding/msgriddermanager.cpp:118-396), which runs one gridder per facet on
+// the same chunk of rows, and of the per-facet l/m shifts of
+// GriddingTaskFactory (scheduling/griddingtaskfactory.cpp:24-34).
+//
+// bind: the rows are uploaded once; each job is planned with a support width
+// common to all jobs (chosen by summing the cost model over the jobs for every
+// candidate width), bucketed into its own records, and given the work items of
+// each of its plane batches.  The (job, plane batch) pairs are packed into
+// waves that fit the plane-memory budget.  The whole inversion is captured in
+// one CUDA graph: per job the visibilities are stamped into its records; per
+// wave ONE persistent gridding launch works through the items of every pair in
+// the wave, then each pair's FFT passes accumulate into its job's image; per
+// job the grid correction finishes the image.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "wgpu_internal.h"
+
+namespace wgpu {
+namespace {
+
+constexpr int kFacetThreads = 256;
+
+// records of a job from the visibilities of its channel range [c0, c0 + nch)
+__global__ void restamp_channels_kernel(const VisRecord *__restrict__ geom,
+                                        const uint32_t *__restrict__ perm,
+                                        const float2 *__restrict__ vis, int64_t n, int nch,
+                                        int n_chan, int c0, VisRecord *__restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(geom + s));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(geom + s) + 1);
+  const uint32_t e = __ldg(perm + s);
+  const uint32_t row = e / (uint32_t)nch, ch = e - row * (uint32_t)nch;
+  const float2 v = __ldg(vis + (size_t)row * n_chan + c0 + ch);
+  // (a.x, a.y) is the sample's phase factor exp(-2 pi i theta)
+  reinterpret_cast<float4 *>(out + s)[0] =
+      make_float4(v.x * a.x - v.y * a.y, v.x * a.y + v.y * a.x, a.z, a.w);
+  reinterpret_cast<float4 *>(out + s)[1] = b;
+}
+
+struct Job {
+  wgpu_facet_t facet;
+  int c0 = 0, nch = 0;
+  double w_min = 0, w_max = 0;
+  int64_t count = 0;
+  wgpu_plan_t plan;
+  DevPlan dp;
+  int64_t n_out = 0;
+  int64_t n_keys = 0;
+  VisRecord *geom = nullptr, *work = nullptr;
+  uint32_t *perm = nullptr, *offsets = nullptr;
+  float2 *acc = nullptr;
+  double *nu_w = nullptr;
+  float *cx = nullptr, *cy = nullptr, *gl = nullptr;
+  float *img = nullptr;  // width * height, row-major
+  std::vector<WorkItems> items;  // per plane batch
+  int rstride = 0;
+};
+
+struct Slot {
+  int job, batch, p0, nb;
+  size_t planes_off, rows_off;  // in float2 elements of the pool
+};
+
+}  // namespace
+}  // namespace wgpu
+
+using namespace wgpu;
+
+struct wgpu_facets {
+  std::vector<wgpu_facet_t> facets;
+  std::vector<size_t> groups;  // channel boundaries, n_groups + 1
+  double epsilon = 1e-4;
+  double plane_budget = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  FftTables *fft = nullptr;
+  std::vector<void *> owned;
+  std::vector<Job> jobs;
+  size_t n_rows = 0, n_chan = 0;
+  double *d_uvw = nullptr, *d_freq = nullptr;
+  float2 *d_vis = nullptr;
+  float *d_images = nullptr;
+  size_t image_elems = 0;
+  float2 *pool = nullptr;
+  std::vector<std::vector<Slot>> waves;
+  int support = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t graph_kernels = 0;
+  unsigned *d_flags = nullptr, *h_flags = nullptr;
+  bool bound = false;
+  double last_ms = 0;
+
+  void *alloc(size_t bytes) {
+    void *p = nullptr;
+    WGPU_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+    owned.push_back(p);
+    return p;
+  }
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    for (void *p : owned) cudaFree(p);
+    owned.clear();
+    jobs.clear();
+    waves.clear();
+    bound = false;
+  }
+  ~wgpu_facets() {
+    if (stream) cudaStreamSynchronize(stream);
+    release();
+    if (d_flags) cudaFree(d_flags);
+    if (h_flags) cudaFreeHost(h_flags);
+    if (fft) fft_tables_destroy(fft);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+wgpu_plan_request_t job_request(const wgpu_facets &f, const Job &j, int64_t force_support) {
+  wgpu_plan_request_t r;
+  std::memset(&r, 0, sizeof(r));
+  r.width = (int64_t)j.facet.width;
+  r.height = (int64_t)j.facet.height;
+  r.dl = j.facet.pixel_size_x;
+  r.dm = j.facet.pixel_size_y;
+  r.l_shift = j.facet.l_shift;
+  r.m_shift = j.facet.m_shift;
+  r.epsilon = f.epsilon;
+  r.w_min = j.w_min;
+  r.w_max = j.w_max;
+  r.n_vis = j.count;
+  r.force_support = force_support;
+  r.max_plane_batch = grid_plane_group();  // one gridding group per batch
+  r.memory_budget_bytes = 1e15;
+  return r;
+}
+
+void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw,
+                 const double *freq) {
+  f->release();
+  cudaStream_t s = f->stream;
+  if (n_rows == 0 || n_chan == 0) throw Error(WGPU_ERR_INVALID, "empty visibility set");
+  if (f->groups.back() > n_chan) throw Error(WGPU_ERR_INVALID, "channel group beyond n_chan");
+  f->n_rows = n_rows;
+  f->n_chan = n_chan;
+  f->d_uvw = (double *)f->alloc(sizeof(double) * 3 * n_rows);
+  f->d_freq = (double *)f->alloc(sizeof(double) * n_chan);
+  f->d_vis = (float2 *)f->alloc(sizeof(float2) * n_rows * n_chan);
+  WGPU_CUDA(cudaMemcpyAsync(f->d_uvw, uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->d_freq, freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
+  DeviceArena arena;  // bucketing scratch, released at return
+
+  // jobs: group-major (job = group * n_facets + facet); w extent per group
+  const size_t n_groups = f->groups.size() - 1;
+  for (size_t gi = 0; gi < n_groups; ++gi) {
+    const int c0 = (int)f->groups[gi], nch = (int)(f->groups[gi + 1] - f->groups[gi]);
+    double w_min, w_max;
+    int64_t count;
+    compute_w_extent(f->d_uvw, f->d_freq + c0, nullptr, nullptr, (int64_t)n_rows, nch, false,
+                     &w_min, &w_max, &count, arena.get(kSlotErr, 64), s);
+    for (const wgpu_facet_t &fc : f->facets) {
+      Job j;
+      j.facet = fc;
+      j.c0 = c0;
+      j.nch = nch;
+      j.w_min = w_min;
+      j.w_max = w_max;
+      j.count = count;
+      f->jobs.push_back(j);
+    }
+  }
+  // support width common to all jobs: the candidate with the lowest summed
+  // cost-model time among the widths the jobs would pick on their own
+  int64_t w_lo = 64, w_hi = 0;
+  for (Job &j : f->jobs) {
+    const wgpu_plan_t p = make_plan(job_request(*f, j, 0));
+    w_lo = std::min(w_lo, p.support);
+    w_hi = std::max(w_hi, p.support);
+  }
+  double best = 1e300;
+  int64_t best_w = w_hi;
+  for (int64_t w = w_lo; w <= w_hi; ++w) {
+    double total = 0;
+    try {
+      for (Job &j : f->jobs) total += make_plan(job_request(*f, j, w)).est_seconds;
+    } catch (const Error &) {
+      continue;  // some job cannot reach epsilon with this width
+    }
+    if (total < best) {
+      best = total;
+      best_w = w;
+    }
+  }
+  f->support = (int)best_w;
+  for (Job &j : f->jobs) {
+    j.plan = make_plan(job_request(*f, j, best_w));
+    j.dp = to_dev_plan(j.plan);
+    j.rstride = (int)((j.plan.width + 31) / 32 * 32);
+  }
+
+  // per job: bucketing into owned buffers, tables, work items
+  f->image_elems = 0;
+  for (Job &j : f->jobs) f->image_elems += j.facet.width * j.facet.height;
+  f->d_images = (float *)f->alloc(sizeof(float) * f->image_elems);
+  size_t img_off = 0;
+  for (Job &j : f->jobs) {
+    const BucketResult br = bucket_visibilities(arena, j.dp, f->d_uvw, f->d_freq + j.c0, nullptr,
+                                                nullptr, (int64_t)n_rows, j.nch, false, s);
+    j.n_out = br.n_out;
+    j.n_keys = br.n_keys;
+    j.geom = (VisRecord *)f->alloc(sizeof(VisRecord) * (br.n_out + 1));
+    j.work = (VisRecord *)f->alloc(sizeof(VisRecord) * (br.n_out + 1));
+    j.perm = (uint32_t *)f->alloc(sizeof(uint32_t) * (br.n_out + 1));
+    j.offsets = (uint32_t *)f->alloc(sizeof(uint32_t) * (br.n_keys + 1));
+    WGPU_CUDA(cudaMemcpyAsync(j.geom, br.records, sizeof(VisRecord) * br.n_out,
+                              cudaMemcpyDeviceToDevice, s));
+    WGPU_CUDA(cudaMemcpyAsync(j.perm, br.perm, sizeof(uint32_t) * br.n_out,
+                              cudaMemcpyDeviceToDevice, s));
+    WGPU_CUDA(cudaMemcpyAsync(j.offsets, br.offsets, sizeof(uint32_t) * (br.n_keys + 1),
+                              cudaMemcpyDeviceToDevice, s));
+    const int64_t npix = j.plan.width * j.plan.height;
+    j.acc = (float2 *)f->alloc(sizeof(float2) * npix);
+    j.nu_w = (double *)f->alloc(sizeof(double) * npix);
+    launch_nu_table(j.dp, j.nu_w, s);
+    std::vector<float> hx, hy, hg;
+    correction_tables(j.plan, hx, hy, hg);
+    j.cx = (float *)f->alloc(sizeof(float) * hx.size());
+    j.cy = (float *)f->alloc(sizeof(float) * hy.size());
+    j.gl = (float *)f->alloc(sizeof(float) * hg.size());
+    WGPU_CUDA(cudaMemcpyAsync(j.cx, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice, s));
+    WGPU_CUDA(cudaMemcpyAsync(j.cy, hy.data(), sizeof(float) * hy.size(), cudaMemcpyHostToDevice, s));
+    WGPU_CUDA(cudaMemcpyAsync(j.gl, hg.data(), sizeof(float) * hg.size(), cudaMemcpyHostToDevice, s));
+    WGPU_CUDA(cudaStreamSynchronize(s));  // host tables die at the end of the iteration
+    j.img = f->d_images + img_off;
+    img_off += j.facet.width * j.facet.height;
+    wgpu_facets *fp = f;
+    const ItemAlloc own = [fp](int, size_t bytes) -> void * { return fp->alloc(bytes); };
+    const int B = (int)j.plan.plane_batch;
+    for (int p0 = 0; p0 < j.plan.n_planes; p0 += B) {
+      const int nb = (int)std::min<int64_t>(B, j.plan.n_planes - p0);
+      j.items.push_back(plan_grid_items(j.dp, j.offsets, p0, nb, nullptr, own, s));
+    }
+    fft_twiddles(*f->fft, (int)j.plan.nu);
+    fft_twiddles(*f->fft, (int)j.plan.nv);
+    fft_twiddles(*f->fft, (int)j.plan.fft_n1);
+    fft_twiddles(*f->fft, (int)j.plan.fft_n2);
+    fft_prepare_rows(*f->fft, (int)j.plan.nu);
+  }
+  arena.release();
+
+  // waves of (job, plane batch) pairs within the plane budget
+  std::vector<Slot> pending;
+  for (int ji = 0; ji < (int)f->jobs.size(); ++ji) {
+    const Job &j = f->jobs[ji];
+    for (int b = 0; b < (int)j.items.size(); ++b) {
+      Slot sl;
+      sl.job = ji;
+      sl.batch = b;
+      sl.p0 = b * (int)j.plan.plane_batch;
+      sl.nb = (int)std::min<int64_t>(j.plan.plane_batch, j.plan.n_planes - sl.p0);
+      pending.push_back(sl);
+    }
+  }
+  size_t pool_elems = 0;
+  std::vector<Slot> wave;
+  size_t used = 0;
+  auto close_wave = [&] {
+    if (wave.empty()) return;
+    pool_elems = std::max(pool_elems, used);
+    f->waves.push_back(wave);
+    wave.clear();
+    used = 0;
+  };
+  for (Slot sl : pending) {
+    const Job &j = f->jobs[sl.job];
+    const size_t pe = (size_t)sl.nb * j.plan.nu * j.plan.nv;
+    const size_t re = (size_t)sl.nb * j.plan.nv * j.rstride;
+    if (!wave.empty() && (double)(used + pe + re) * sizeof(float2) > f->plane_budget) close_wave();
+    sl.planes_off = used;
+    sl.rows_off = used + pe;
+    used += pe + re;
+    wave.push_back(sl);
+  }
+  close_wave();
+  f->pool = (float2 *)f->alloc(sizeof(float2) * pool_elems);
+
+  // job tables of each wave's gridding launch
+  std::vector<GridJob *> d_jobs;
+  std::vector<uint32_t *> d_base;
+  std::vector<uint32_t> totals;
+  for (const auto &w : f->waves) {
+    std::vector<GridJob> hj;
+    std::vector<uint32_t> hb;
+    uint32_t total = 0;
+    for (const Slot &sl : w) {
+      const Job &j = f->jobs[sl.job];
+      const WorkItems &wi = j.items[sl.batch];
+      GridJob g;
+      g.p = j.dp;
+      g.rec = j.work;
+      g.off = j.offsets;
+      g.item_off = wi.item_off;
+      g.desc = wi.desc;
+      g.planes = f->pool + sl.planes_off;
+      g.p_begin = sl.p0;
+      g.n_batch = sl.nb;
+      hj.push_back(g);
+      hb.push_back(total);
+      total += wi.total;
+    }
+    GridJob *dj = (GridJob *)f->alloc(sizeof(GridJob) * hj.size());
+    uint32_t *db = (uint32_t *)f->alloc(sizeof(uint32_t) * hb.size());
+    WGPU_CUDA(cudaMemcpyAsync(dj, hj.data(), sizeof(GridJob) * hj.size(), cudaMemcpyHostToDevice, s));
+    WGPU_CUDA(cudaMemcpyAsync(db, hb.data(), sizeof(uint32_t) * hb.size(), cudaMemcpyHostToDevice, s));
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    d_jobs.push_back(dj);
+    d_base.push_back(db);
+    totals.push_back(total);
+  }
+
+  // one graph for the whole inversion
+  prepare_grid_items_multi(f->support);
+  const uint64_t k0 = thread_launch_count();
+  WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (Job &j : f->jobs) {
+      const int64_t n = j.n_out;
+      if (n > 0) {
+        restamp_channels_kernel<<<(unsigned)((n + kFacetThreads - 1) / kFacetThreads),
+                                  kFacetThreads, 0, s>>>(j.geom, j.perm, f->d_vis, n, j.nch,
+                                                         (int)f->n_chan, j.c0, j.work);
+        check_launch("restamp_channels_kernel");
+      }
+      WGPU_CUDA(cudaMemsetAsync(j.acc, 0, sizeof(float2) * j.plan.width * j.plan.height, s));
+    }
+    WGPU_CUDA(cudaMemsetAsync(f->d_images, 0, sizeof(float) * f->image_elems, s));
+    for (size_t wi = 0; wi < f->waves.size(); ++wi) {
+      for (const Slot &sl : f->waves[wi]) {
+        const Job &j = f->jobs[sl.job];
+        launch_zero_split_units(j.dp, j.items[sl.batch], sl.p0, sl.nb, f->pool + sl.planes_off, s);
+      }
+      launch_grid_items_multi(f->support, d_jobs[wi], d_base[wi], (int)f->waves[wi].size(),
+                              totals[wi], s);
+      for (const Slot &sl : f->waves[wi]) {
+        const Job &j = f->jobs[sl.job];
+        float2 *planes = f->pool + sl.planes_off, *rows = f->pool + sl.rows_off;
+        launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, f->d_flags, s);
+        launch_fft_cols_a(*f->fft, j.dp, (int)j.plan.fft_n1, (int)j.plan.fft_n2, rows, j.rstride,
+                          sl.nb, -1.0f, s);
+        launch_fft_cols_b_forward_accumulate(*f->fft, j.dp, (int)j.plan.fft_n1,
+                                             (int)j.plan.fft_n2, rows, j.rstride, sl.nb, sl.p0,
+                                             j.nu_w, j.acc, s);
+      }
+    }
+    for (Job &j : f->jobs)
+      launch_finalize_add(j.dp, j.acc, j.nu_w, j.cx, j.cy, j.gl, kCorrGlNodes, j.img, 4, s);
+  } catch (...) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(s, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    throw;
+  }
+  WGPU_CUDA(cudaStreamEndCapture(s, &f->graph));
+  WGPU_CUDA(cudaGraphInstantiate(&f->exec, f->graph, 0));
+  f->graph_kernels = thread_launch_count() - k0;
+  count_launch(-(int)f->graph_kernels);  // captured, not run
+  f->bound = true;
+}
+
+void invert_facets(wgpu_facets *f, const float *vis, bool device, float *images) {
+  if (!f->bound) throw Error(WGPU_ERR_STATE, "no bound visibility set");
+  cudaStream_t s = f->stream;
+  cudaEvent_t e0, e1;
+  WGPU_CUDA(cudaEventCreate(&e0));
+  WGPU_CUDA(cudaEventCreate(&e1));
+  WGPU_CUDA(cudaEventRecord(e0, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->d_vis, vis, sizeof(float2) * f->n_rows * f->n_chan,
+                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaGraphLaunch(f->exec, s));
+  count_launch((int)f->graph_kernels);
+  if (images)
+    WGPU_CUDA(cudaMemcpyAsync(images, f->d_images, sizeof(float) * f->image_elems,
+                              device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->h_flags, f->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaEventRecord(e1, s));
+  WGPU_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  f->last_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (*f->h_flags != 0) {
+    *f->h_flags = 0;
+    WGPU_CUDA(cudaMemsetAsync(f->d_flags, 0, sizeof(unsigned), s));
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (row transform prefetch)");
+  }
+}
+
+template <typename F>
+int facets_guarded(F &&fn) {
+  try {
+    clear_failure();
+    fn();
+    return WGPU_OK;
+  } catch (const Error &e) {
+    return report_failure(e.status, e.what());
+  } catch (const std::bad_alloc &) {
+    return report_failure(WGPU_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return report_failure(WGPU_ERR_INVALID, e.what());
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int wgpu_facets_create(const wgpu_facet_t *facets, size_t n_facets, const size_t *channel_groups,
+                       size_t n_groups, double epsilon, double plane_budget_bytes,
+                       wgpu_facets_t **out) {
+  if (!facets || !channel_groups || !out || n_facets == 0 || n_groups == 0)
+    return report_failure(WGPU_ERR_INVALID, "null or empty facet batch");
+  if (!(epsilon > 0) || !(plane_budget_bytes >= 0))
+    return report_failure(WGPU_ERR_INVALID, "invalid epsilon or plane budget");
+  for (size_t i = 0; i < n_groups; ++i)
+    if (channel_groups[i + 1] <= channel_groups[i])
+      return report_failure(WGPU_ERR_INVALID, "channel groups must be increasing");
+  for (size_t i = 0; i < n_facets; ++i)
+    if (facets[i].width == 0 || facets[i].height == 0 || facets[i].width % 2 ||
+        facets[i].height % 2 || !(facets[i].pixel_size_x > 0) || !(facets[i].pixel_size_y > 0))
+      return report_failure(WGPU_ERR_INVALID, "facet sizes must be even and pixel sizes positive");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return report_failure(WGPU_ERR_CUDA, "no usable CUDA device");
+  }
+  return facets_guarded([&] {
+    auto f = std::make_unique<wgpu_facets>();
+    f->facets.assign(facets, facets + n_facets);
+    f->groups.assign(channel_groups, channel_groups + n_groups + 1);
+    f->epsilon = epsilon;
+    f->plane_budget = plane_budget_bytes > 0 ? plane_budget_bytes : 40e9;
+    WGPU_CUDA(cudaGetDevice(&f->device));
+    WGPU_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+    WGPU_CUDA(cudaMalloc(&f->d_flags, sizeof(unsigned)));
+    WGPU_CUDA(cudaMemset(f->d_flags, 0, sizeof(unsigned)));
+    WGPU_CUDA(cudaMallocHost(&f->h_flags, sizeof(unsigned)));
+    *f->h_flags = 0;
+    f->fft = fft_tables_create();
+    *out = f.release();
+  });
+}
+
+int wgpu_facets_bind(wgpu_facets_t *f, size_t n_rows, size_t n_chan, const double *uvw,
+                     const double *freq) {
+  if (!f || !uvw || !freq) return report_failure(WGPU_ERR_INVALID, "null argument");
+  return facets_guarded([&] {
+    WGPU_CUDA(cudaSetDevice(f->device));
+    bind_facets(f, n_rows, n_chan, uvw, freq);
+  });
+}
+
+int wgpu_facets_invert(wgpu_facets_t *f, const float *vis, float *images) {
+  if (!f || !vis) return report_failure(WGPU_ERR_INVALID, "null argument");
+  return facets_guarded([&] { invert_facets(f, vis, false, images); });
+}
+
+int wgpu_facets_invert_device(wgpu_facets_t *f, const float *d_vis, float *d_images) {
+  if (!f || !d_vis) return report_failure(WGPU_ERR_INVALID, "null argument");
+  return facets_guarded([&] { invert_facets(f, d_vis, true, d_images); });
+}
+
+int wgpu_facets_info(const wgpu_facets_t *f, wgpu_facets_info_t *info) {
+  if (!f || !info) return report_failure(WGPU_ERR_INVALID, "null argument");
+  info->n_jobs = f->jobs.size();
+  info->n_waves = f->waves.size();
+  info->support = f->support;
+  info->graph_kernels = f->graph_kernels;
+  info->image_elems = f->image_elems;
+  double vis = 0;
+  for (const Job &j : f->jobs) vis += (double)j.n_out;
+  info->job_visibilities = vis;
+  info->last_ms = f->last_ms;
+  return WGPU_OK;
+}
+
+int wgpu_facets_job_plan(const wgpu_facets_t *f, size_t job, wgpu_plan_t *plan) {
+  if (!f || !plan) return report_failure(WGPU_ERR_INVALID, "null argument");
+  if (job >= f->jobs.size()) return report_failure(WGPU_ERR_INVALID, "job index out of range");
+  *plan = f->jobs[job].plan;
+  return WGPU_OK;
+}
+
+void *wgpu_facets_stream(wgpu_facets_t *f) { return f ? (void *)f->stream : nullptr; }
+
+void wgpu_facets_destroy(wgpu_facets_t *f) { delete f; }
+
+}  // extern "C"

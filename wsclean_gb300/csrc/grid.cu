@@ -9,12 +9,12 @@
 // through the items of a plane batch from a device counter, so that the
 // crowded tiles of a dense uv core are shared by many CTAs.
 //
-// Gridding item: records are staged kChunk at a time in shared memory and
-// spread into a shared copy of the tile with shared-memory atomics; every
-// kFoldEvery rounds the partial tile is folded into per-thread
-// Kahan-compensated accumulators and cleared, so long lists keep FP32
-// precision.  A unit made of one item writes each cell once to HBM; the items
-// of a split unit add into cells that a planning pass zeroed.
+// Gridding item: a block keeps the unit's cells in shared memory; each warp
+// owns two rows of every plane and adds the footprints of the staged records
+// with plain read-add-writes; the tile is written to HBM once per item (a
+// unit split into several items adds into cells zeroed beforehand).  One
+// launch can also serve many jobs (facets x channel groups), each with its own
+// plan, records and planes (grid_kernel_multi).
 //
 // Degridding item: loads its tile plus a (W-1)-cell halo of G planes into
 // shared memory and gathers, for each visibility of its slice of the own
@@ -132,16 +132,6 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
   for (uint32_t i = a; i < b; ++i) desc[i] = (uint32_t)unit | flag;
 }
 
-// Shared-memory row stride for a tile (or halo region) of `rows` cells: the
-// lanes of a warp cover footprint rows of W cells, so the stride is chosen
-// congruent to 8 (W <= 8, four rows per warp instruction) or 16 (two rows)
-// modulo 32 banks; re and im live in separate arrays so one atomic or load per
-// lane touches one bank.
-__host__ __device__ constexpr int padded_stride(int rows, int W) {
-  return W <= 8 ? (((rows + 7) / 16) * 16 + 8)    // 8 or 24 (mod 32)
-                : (((rows + 15) / 32) * 32 + 16);  // 16 (mod 32)
-}
-
 // Shared-memory layout of the gridding kernel: the tile's float2 cells
 // [G][T][T], then the staged round: five meta arrays [5][kGridRound] (re, im,
 // u and v corner relative to the tile, first plane relative to the group) and
@@ -168,28 +158,50 @@ constexpr size_t grid_smem_bytes() {
 // rows x eight columns) fall on distinct banks.  A work item holds at most
 // kItemVis reads, which bounds the FP32 accumulation chain of every cell; the
 // tile is flushed to HBM once at the item's end.
+
+// Shared memory of the gridding kernels (see grid_smem_bytes).
+struct GridSmem {
+  float2 *cells;
+  float *m_re, *m_im;
+  int *m_iu, *m_iv, *m_ip;
+  float *wts;
+  uint32_t *rs0, *rcum;
+};
+
 template <int T, int G, int W>
-__global__ void __launch_bounds__(kThreads)
-    grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
-                const uint32_t *__restrict__ off, int p_begin, int n_batch,
-                const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
-                uint32_t total, float2 *__restrict__ planes) {
-  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+__device__ __forceinline__ GridSmem grid_smem(float4 *smem4, uint32_t *rs0, uint32_t *rcum) {
+  constexpr int kCells = T * T;
+  GridSmem sm;
+  sm.cells = reinterpret_cast<float2 *>(smem4);  // [G][T][T], swizzled columns
+  sm.m_re = reinterpret_cast<float *>(sm.cells + G * kCells);
+  sm.m_im = sm.m_re + kGridRound;
+  sm.m_iu = reinterpret_cast<int *>(sm.m_im + kGridRound);
+  sm.m_iv = sm.m_iu + kGridRound;
+  sm.m_ip = sm.m_iv + kGridRound;
+  sm.wts = reinterpret_cast<float *>(sm.m_ip + kGridRound);  // [kGridRound][kWS]
+  sm.rs0 = rs0;
+  sm.rcum = rcum;
+  return sm;
+}
+
+// One work item (descriptor d, item index `item` of its plane batch).  The
+// tile cells are zero on entry and on return; ends with a block barrier
+// unless the unit has no visibilities.
+template <int T, int G, int W>
+__device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__restrict__ rec,
+                                          const uint32_t *__restrict__ off, int p_begin,
+                                          int n_batch, const uint32_t *__restrict__ item_off,
+                                          uint32_t d, uint32_t item,
+                                          float2 *__restrict__ planes, const GridSmem &sm) {
   constexpr int kCols = W <= 8 ? 8 : 16;            // lanes across footprint columns
   constexpr int kPlaneLanes = 32 / (2 * kCols);     // 2 (W <= 8) or 1
   constexpr int kSteps = (W + kPlaneLanes - 1) / kPlaneLanes;
   constexpr int kWS = grid_weight_stride(W);
   constexpr int kCells = T * T;
-  extern __shared__ float4 smem4[];
-  float2 *cells = reinterpret_cast<float2 *>(smem4);  // [G][T][T], swizzled columns
-  float *m_re = reinterpret_cast<float *>(cells + G * kCells);
-  float *m_im = m_re + kGridRound;
-  int *m_iu = reinterpret_cast<int *>(m_im + kGridRound);
-  int *m_iv = m_iu + kGridRound;
-  int *m_ip = m_iv + kGridRound;
-  float *wts = reinterpret_cast<float *>(m_ip + kGridRound);  // [kGridRound][kWS]
-  __shared__ uint32_t rs0[9], rcum[10];
-
+  float2 *cells = sm.cells;
+  float *m_re = sm.m_re, *m_im = sm.m_im, *wts = sm.wts;
+  int *m_iu = sm.m_iu, *m_iv = sm.m_iv, *m_ip = sm.m_ip;
+  uint32_t *rs0 = sm.rs0, *rcum = sm.rcum;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ci = lane % kCols;              // footprint column offset
   const int row = 2 * warp + ((lane / kCols) & 1);
@@ -198,127 +210,173 @@ __global__ void __launch_bounds__(kThreads)
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
-
-  for (int c = threadIdx.x; c < G * kCells; c += kThreads) cells[c] = make_float2(0.f, 0.f);
-  __syncthreads();
-
-  for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
-    const uint32_t d = __ldg(desc + item);
-    const int unit = (int)(d & 0x7fffffffu);
-    const int tile = unit % n_tiles, group = unit / n_tiles;
-    const int tu = tile % p.ntu, tv = tile / p.ntu;
-    const int q0 = p_begin + group * G;
-    const int q1 = min(q0 + G, p_begin + n_batch);
-    const int nq = q1 - q0;
-    if (d & 0x80000000u) {
-      // no visibility reaches this unit: its cells are zero
-      for (int c = threadIdx.x; c < nq * kCells; c += kThreads) {
-        const int pq = c / kCells, rem = c - pq * kCells;
-        const int rr = rem / T, cc = rem - rr * T;
-        planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
-               tu * T + cc] = make_float2(0.f, 0.f);
-      }
-      continue;
-    }
-    const uint32_t first = __ldg(item_off + unit);
-    const uint32_t n_items = __ldg(item_off + unit + 1) - first;
-    if (threadIdx.x < 9) {
-      uint32_t a, b;
-      unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
-      rs0[threadIdx.x] = a;
-      rcum[threadIdx.x + 1] = b - a;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      rcum[0] = 0;
-      for (int r = 0; r < 9; ++r) rcum[r + 1] += rcum[r];
-    }
-    __syncthreads();
-    const uint32_t lo = (item - first) * kItemVis;
-    const uint32_t hi = min(lo + kItemVis, rcum[9]);
-
-    for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
-      // stage: threads t and t + kGridRound share read t; the first evaluates
-      // kx and ky, the second kz and the meta data
-      {
-        const int t = threadIdx.x % kGridRound;
-        const bool second = threadIdx.x >= kGridRound;
-        const uint32_t pos = rb + (uint32_t)t;
-        if (pos < hi) {
-          int r = 0;
-          while (pos >= rcum[r + 1]) ++r;
-          const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
-          float *w = wts + t * kWS;
-          if (!second) {
-#pragma unroll
-            for (int k = 0; k < W; ++k) {
-              w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
-              w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
-            }
-          } else {
-#pragma unroll
-            for (int k = 0; k < W; ++k)
-              w[2 * W + k] = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
-                                             : es_eval(p.beta, (v.fw + (float)k) * inv_half);
-            int iu_rel = v.iu - tu * T;
-            if (iu_rel >= T) iu_rel -= p.nu;
-            int iv_rel = v.iv - tv * T;
-            if (iv_rel >= T) iv_rel -= p.nv;
-            m_re[t] = v.re;
-            m_im[t] = v.im;
-            m_iu[t] = iu_rel;
-            m_iv[t] = iv_rel;
-            m_ip[t] = v.ip - q0;
-          }
-        }
-      }
-      __syncthreads();
-      const int n_round = (int)min((uint32_t)kGridRound, hi - rb);
-      for (int m = 0; m < n_round; ++m) {
-        const int ivr = m_iv[m];
-        if (ivr > 2 * warp + 1 || ivr + W <= 2 * warp) continue;  // uniform in the warp
-        const int col = m_iu[m] + ci;
-        const int dv = row - ivr;
-        if (ci < W && col >= 0 && col < T && dv >= 0 && dv < W) {
-          const float *w = wts + m * kWS;
-          const int ipr = m_ip[m];
-          const float re = m_re[m], im = m_im[m];
-          const float wuv = w[ci] * w[W + dv];
-          float2 *cb = cells + row * T + (col ^ swz);
-#pragma unroll
-          for (int s = 0; s < kSteps; ++s) {
-            const int dz = s * kPlaneLanes + pj;
-            const int q = ipr + dz;
-            if (dz < W && q >= 0 && q < nq) {
-              const float t = wuv * w[2 * W + dz];
-              float2 c = cb[q * kCells];
-              c.x = fmaf(t, re, c.x);
-              c.y = fmaf(t, im, c.y);
-              cb[q * kCells] = c;
-            }
-          }
-        }
-        __syncwarp();  // the next read's lanes may update the same cells
-      }
-      __syncthreads();
-    }
-    // flush the tile (a split unit adds into cells zeroed beforehand)
-    for (int c = threadIdx.x; c < G * kCells; c += kThreads) {
+  const int unit = (int)(d & 0x7fffffffu);
+  const int tile = unit % n_tiles, group = unit / n_tiles;
+  const int tu = tile % p.ntu, tv = tile / p.ntu;
+  const int q0 = p_begin + group * G;
+  const int q1 = min(q0 + G, p_begin + n_batch);
+  const int nq = q1 - q0;
+  if (d & 0x80000000u) {
+    // no visibility reaches this unit: its cells are zero
+    for (int c = threadIdx.x; c < nq * kCells; c += kThreads) {
       const int pq = c / kCells, rem = c - pq * kCells;
       const int rr = rem / T, cc = rem - rr * T;
-      float2 *src = cells + pq * kCells + rr * T + (cc ^ ((rr & 1) << 3));
-      const float2 val = *src;
-      *src = make_float2(0.f, 0.f);
-      if (pq < nq) {
-        float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
-                      (size_t)(tv * T + rr) * p.nu + tu * T + cc;
-        if (n_items == 1)
-          *dst = val;
-        else
-          atomicAdd(dst, val);
+      planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
+             tu * T + cc] = make_float2(0.f, 0.f);
+    }
+    return;
+  }
+  const uint32_t first = __ldg(item_off + unit);
+  const uint32_t n_items = __ldg(item_off + unit + 1) - first;
+  if (threadIdx.x < 9) {
+    uint32_t a, b;
+    unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
+    rs0[threadIdx.x] = a;
+    rcum[threadIdx.x + 1] = b - a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    rcum[0] = 0;
+    for (int r = 0; r < 9; ++r) rcum[r + 1] += rcum[r];
+  }
+  __syncthreads();
+  const uint32_t lo = (item - first) * kItemVis;
+  const uint32_t hi = min(lo + kItemVis, rcum[9]);
+
+  for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
+    // stage: threads t and t + kGridRound share read t; the first evaluates
+    // kx and ky, the second kz and the meta data
+    {
+      const int t = threadIdx.x % kGridRound;
+      const bool second = threadIdx.x >= kGridRound;
+      const uint32_t pos = rb + (uint32_t)t;
+      if (pos < hi) {
+        int r = 0;
+        while (pos >= rcum[r + 1]) ++r;
+        const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
+        float *w = wts + t * kWS;
+        if (!second) {
+#pragma unroll
+          for (int k = 0; k < W; ++k) {
+            w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
+            w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < W; ++k)
+            w[2 * W + k] = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
+                                           : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+          int iu_rel = v.iu - tu * T;
+          if (iu_rel >= T) iu_rel -= p.nu;
+          int iv_rel = v.iv - tv * T;
+          if (iv_rel >= T) iv_rel -= p.nv;
+          m_re[t] = v.re;
+          m_im[t] = v.im;
+          m_iu[t] = iu_rel;
+          m_iv[t] = iv_rel;
+          m_ip[t] = v.ip - q0;
+        }
       }
     }
     __syncthreads();
+    const int n_round = (int)min((uint32_t)kGridRound, hi - rb);
+    for (int m = 0; m < n_round; ++m) {
+      const int ivr = m_iv[m];
+      if (ivr > 2 * warp + 1 || ivr + W <= 2 * warp) continue;  // uniform in the warp
+      const int col = m_iu[m] + ci;
+      const int dv = row - ivr;
+      if (ci < W && col >= 0 && col < T && dv >= 0 && dv < W) {
+        const float *w = wts + m * kWS;
+        const int ipr = m_ip[m];
+        const float re = m_re[m], im = m_im[m];
+        const float wuv = w[ci] * w[W + dv];
+        float2 *cb = cells + row * T + (col ^ swz);
+#pragma unroll
+        for (int s = 0; s < kSteps; ++s) {
+          const int dz = s * kPlaneLanes + pj;
+          const int q = ipr + dz;
+          if (dz < W && q >= 0 && q < nq) {
+            const float t = wuv * w[2 * W + dz];
+            float2 c = cb[q * kCells];
+            c.x = fmaf(t, re, c.x);
+            c.y = fmaf(t, im, c.y);
+            cb[q * kCells] = c;
+          }
+        }
+      }
+      __syncwarp();  // the next read's lanes may update the same cells
+    }
+    __syncthreads();
+  }
+  // flush the tile (a split unit adds into cells zeroed beforehand)
+  for (int c = threadIdx.x; c < G * kCells; c += kThreads) {
+    const int pq = c / kCells, rem = c - pq * kCells;
+    const int rr = rem / T, cc = rem - rr * T;
+    float2 *src = cells + pq * kCells + rr * T + (cc ^ ((rr & 1) << 3));
+    const float2 val = *src;
+    *src = make_float2(0.f, 0.f);
+    if (pq < nq) {
+      float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
+                    (size_t)(tv * T + rr) * p.nu + tu * T + cc;
+      if (n_items == 1)
+        *dst = val;
+      else
+        atomicAdd(dst, val);
+    }
+  }
+  __syncthreads();
+}
+
+template <int T, int G, int W>
+__global__ void __launch_bounds__(kThreads)
+    grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
+                const uint32_t *__restrict__ off, int p_begin, int n_batch,
+                const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
+                uint32_t total, float2 *__restrict__ planes) {
+  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+  extern __shared__ float4 smem4[];
+  __shared__ uint32_t rs0[9], rcum[10];
+  const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
+  for (int c = threadIdx.x; c < G * T * T; c += kThreads) sm.cells[c] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (uint32_t item = blockIdx.x; item < total; item += gridDim.x)
+    grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, __ldg(desc + item), item, planes,
+                       sm);
+}
+
+// Several gridding jobs (facets x channel groups, each with its own plan,
+// records and planes but the same kernel support) in one persistent launch:
+// item i belongs to the job j with job_base[j] <= i < job_base[j + 1]; the
+// block keeps the current job's description in shared memory.
+template <int T, int G, int W>
+__global__ void __launch_bounds__(kThreads)
+    grid_kernel_multi(const GridJob *__restrict__ jobs, const uint32_t *__restrict__ job_base,
+                      int n_jobs, uint32_t total) {
+  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+  static_assert(sizeof(GridJob) % 8 == 0, "job copied in 8-byte words");
+  extern __shared__ float4 smem4[];
+  __shared__ uint32_t rs0[9], rcum[10];
+  __shared__ GridJob job;
+  const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
+  for (int c = threadIdx.x; c < G * T * T; c += kThreads) sm.cells[c] = make_float2(0.f, 0.f);
+  int cur = -1;
+  for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+    int lo = 0, hi = n_jobs - 1;  // last job whose base is <= item
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(job_base + mid) <= item) lo = mid; else hi = mid - 1;
+    }
+    if (lo != cur) {
+      __syncthreads();  // nobody reads the previous job any more
+      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs + lo);
+      unsigned long long *dst = reinterpret_cast<unsigned long long *>(&job);
+      for (int k = threadIdx.x; k < (int)(sizeof(GridJob) / 8); k += kThreads) dst[k] = __ldg(src + k);
+      cur = lo;
+    }
+    __syncthreads();
+    const uint32_t local = item - __ldg(job_base + lo);
+    grid_item<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off,
+                       __ldg(job.desc + local), local, job.planes, sm);
   }
 }
 
@@ -558,6 +616,33 @@ void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, i
   check_launch("degrid_kernel");
 }
 
+template <int T, int G, int W>
+void grid_items_multi(const GridJob *d_jobs, const uint32_t *d_base, int n_jobs, uint32_t total,
+                      cudaStream_t s) {
+  if (total == 0) return;
+  const size_t smem = grid_smem_bytes<T, G, W>();
+  ensure_dynamic_smem((const void *)grid_kernel_multi<T, G, W>, smem);
+  int per_sm = 0;
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel_multi<T, G, W>,
+                                                          kThreads, smem));
+  const uint32_t blocks = std::min<uint32_t>(total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
+  grid_kernel_multi<T, G, W><<<blocks, kThreads, smem, s>>>(d_jobs, d_base, n_jobs, total);
+  check_launch("grid_kernel_multi");
+}
+
+template <int T, int G, int W = 4>
+void grid_multi_dispatch(int support, const GridJob *d_jobs, const uint32_t *d_base, int n_jobs,
+                         uint32_t total, cudaStream_t s) {
+  if constexpr (W > kMaxSupport) {
+    throw Error(WGPU_ERR_INVALID, "kernel support out of range");
+  } else {
+    if (support == W)
+      grid_items_multi<T, G, W>(d_jobs, d_base, n_jobs, total, s);
+    else
+      grid_multi_dispatch<T, G, W + 1>(support, d_jobs, d_base, n_jobs, total, s);
+  }
+}
+
 // Dispatch over the kernel support (4..16).
 template <int T, int G, int W = 4>
 void grid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const uint32_t *off,
@@ -627,6 +712,27 @@ void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *o
                        int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
   check_plan(p);
   grid_dispatch<kTile, kGridPlanes>(p.support, p, rec, off, p_begin, n_batch, wi, planes, s);
+}
+
+template <int T, int G, int W = 4>
+void grid_multi_prepare(int support) {
+  if constexpr (W <= kMaxSupport) {
+    if (support == W)
+      ensure_dynamic_smem((const void *)grid_kernel_multi<T, G, W>, grid_smem_bytes<T, G, W>());
+    else
+      grid_multi_prepare<T, G, W + 1>(support);
+  }
+}
+
+void prepare_grid_items_multi(int support) {
+  grid_multi_prepare<kTile, kGridPlanes>(support);
+}
+
+void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
+                             int n_jobs, uint32_t total, cudaStream_t s) {
+  if (support < 4 || support > kMaxSupport)
+    throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
+  grid_multi_dispatch<kTile, kGridPlanes>(support, d_jobs, d_base, n_jobs, total, s);
 }
 
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,

@@ -7,6 +7,7 @@
 #include <functional>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../include/wgpu.h"
 
@@ -61,6 +62,23 @@ struct DevPlan {
 };
 
 DevPlan to_dev_plan(const wgpu_plan_t &p);
+
+// One gridding job of a multi-job launch: its plan, bucketed records and
+// offsets, the work items of its current plane batch and the planes they
+// fill.
+struct GridJob {
+  DevPlan p;
+  const VisRecord *rec;
+  const uint32_t *off;
+  const uint32_t *item_off;
+  const uint32_t *desc;
+  float2 *planes;
+  int p_begin, n_batch;
+};
+
+constexpr int kCorrGlNodes = 48;  // Gauss-Legendre nodes (positive half) of the w correction
+void correction_tables(const wgpu_plan_t &plan, std::vector<float> &hx, std::vector<float> &hy,
+                       std::vector<float> &hg);
 
 
 // ---- planner (plan.cpp) ----
@@ -125,6 +143,12 @@ void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin,
                              float2 *planes, cudaStream_t s);
 void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
                        int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s);
+// All jobs' items in one persistent launch (items of job j start at
+// d_base[j]); every job has kernel support `support`.
+// Sets the multi-job kernel's shared-memory cap (before a graph capture).
+void prepare_grid_items_multi(int support);
+void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
+                             int n_jobs, uint32_t total, cudaStream_t s);
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                          int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
                          float2 *acc, cudaStream_t s);
