@@ -38,6 +38,10 @@ WORKLOAD_TEXT = {
                     "2016 baselines x 60 x 10 s, 32 channels 120-180 MHz, XX/XY/YX/YY from 20 "
                     "sources with random Stokes Q, U, V (|pol frac| <= 0.3), per-antenna full "
                     "Jones solutions per time step and channel, eps 1e-4"),
+    "facets": ("batched facets: 37 facets of 512-3072 pixels (multiples of 4), 10arcsec "
+               "pixels, centres within a 6 deg field, x 8 output channels of 2 channels; "
+               "64 antennas in a 3 km disk, 2016 baselines x 620 x 10 s (scaled from 6200), "
+               "16 channels 120-180 MHz, 20 sources, eps 1e-4"),
     "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
                   "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
 }
@@ -545,6 +549,153 @@ def run_fullpol(args):
     }
 
 
+def run_facets(args):
+    """Batched facet inversion (all facet x channel jobs, one multi-job gridding
+    launch per wave, one CUDA graph) against the same jobs run one at a time
+    through the plain per-call path."""
+    import torch
+    import oracle
+    from wsclean_gb300 import synthetic
+    from wsclean_gb300.facets import FacetBatch
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(4)
+    t0 = time.time()
+    d = synthetic.make_workload("plain1024", seed=4, with_model=False, n_t=args.facet_times)
+    vis = synthetic.model_vis_torch(d["uvw"], d["freq"], d["sources"], dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    vis = vis + 0.01 * math.sqrt(2.0) * torch.randn(vis.shape, generator=g, dtype=vis.dtype,
+                                                    device=dev)
+    d_vis = vis.contiguous()
+    h_vis = pinned_copy(d_vis).numpy()
+    gen_s = time.time() - t0
+    dl = d["dl"]
+    half = math.radians(3.0)
+    facets = []
+    for _ in range(37):
+        side = int(rng.uniform(512, 3072)) // 4 * 4
+        facets.append(dict(width=side, height=side, dl=dl, dm=dl,
+                           l_shift=float(rng.uniform(-half, half)),
+                           m_shift=float(rng.uniform(-half, half))))
+    groups = list(range(0, 17, 2))
+    n_rows, n_chan = d["uvw"].shape[0], d["freq"].size
+    eps = 1e-4
+    t0 = time.time()
+    fb = FacetBatch(facets, groups, epsilon=eps)
+    fb.bind(d["uvw"], d["freq"])
+    torch.cuda.synchronize()
+    bind_s = time.time() - t0
+    info = fb.info()
+    out = torch.empty(int(info["image_elems"]), dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(fb.stream(), device=dev)
+
+    def step():
+        fb.invert_device(d_vis.data_ptr(), out.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = _lib_launches() - l0
+    ms = start.elapsed_time(end) / args.steps
+    job_vis = float(info["job_visibilities"])
+    # end to end: host visibilities in, host images out
+    h_img = np.empty(int(info["image_elems"]), np.float32)
+    w0 = time.perf_counter()
+    e_steps = max(1, args.steps // 2)
+    for _ in range(e_steps):
+        fb.invert(h_vis)
+    e_ms = (time.perf_counter() - w0) * 1e3 / e_steps
+    # the same jobs one at a time through the plain per-call path
+    per_group = [d_vis[:, c0:c0 + 2].contiguous() for c0 in groups[:-1]]
+    d_uvw = torch.as_tensor(d["uvw"], device=dev)
+    d_freq = torch.as_tensor(d["freq"], device=dev)
+    gp = {}
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    images_plain = {}
+    for gi in range(len(groups) - 1):
+        c0 = groups[gi]
+        for fi, f in enumerate(facets):
+            key = fi
+            if key not in gp:
+                gp[key] = WGriddingGridder_Simple(f["width"], f["height"], f["width"], f["height"],
+                                                  dl, dl, f["l_shift"], f["m_shift"], 1,
+                                                  epsilon=eps)
+            gg = gp[key]
+            gg.InitializeInversion()
+            gg.AddInversionDataDevice(n_rows, 2, d_uvw.data_ptr(), d_freq[c0:c0 + 2].data_ptr(),
+                                      per_group[gi].data_ptr())
+            gg.FinalizeImage(1.0)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - w0
+    # accuracy: two jobs against the plain path on the job's plan, one against the DFT
+    images = out.cpu().numpy()
+    offs = np.cumsum([0] + [f["width"] * f["height"] for f in facets] * (len(groups) - 1))
+    checks = {}
+    for job in (0, len(facets) * 3 + 5):
+        gi, fi = divmod(job, len(facets))
+        f, c0 = facets[fi], groups[gi]
+        img = images[offs[job]:offs[job + 1]].astype(np.float64)
+        gg = WGriddingGridder_Simple(f["width"], f["height"], f["width"], f["height"], dl, dl,
+                                     f["l_shift"], f["m_shift"], 1, epsilon=eps)
+        gg.pin_plan(fb.job_plan(job))
+        gg.InitializeInversion()
+        gg.AddInversionDataDevice(n_rows, 2, d_uvw.data_ptr(), d_freq[c0:c0 + 2].data_ptr(),
+                                  per_group[gi].data_ptr())
+        gg.FinalizeImage(1.0)
+        ref = gg.RealImage().astype(np.float64)
+        gg.close()
+        checks[f"job{job}_vs_plain_rel_l2"] = float(np.linalg.norm(img - ref) / np.linalg.norm(ref))
+        if job == 0:
+            pix = rng.choice(f["width"] * f["height"], 64, replace=False)
+            hv = h_vis[:, c0:c0 + 2]
+            dft = oracle.dft_invert(d["uvw"], d["freq"][c0:c0 + 2], hv, f["width"], f["height"],
+                                    dl, dl, f["l_shift"], f["m_shift"], pixels=pix,
+                                    n_threads=os.cpu_count())
+            checks["job0_vs_dft_rel_l2_64px"] = float(np.linalg.norm(img[pix] - dft) /
+                                                      np.linalg.norm(dft))
+    for gg in gp.values():
+        gg.close()
+    fb.close()
+    value = job_vis / (ms * 1e-3) / 1e9
+    plain_value = job_vis / plain_s / 1e9
+    sides = [f["width"] for f in facets]
+    return {
+        "metric": "Gvis/s batched facet inversion (job-samples: facets x channel groups)",
+        "value": value, "unit": "Gvis/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT["facets"], "n_rows": n_rows, "n_chan": n_chan,
+                   "facet_sides": [min(sides), max(sides)], "jobs": int(info["n_jobs"]),
+                   "waves": int(info["n_waves"]), "support": int(info["support"]),
+                   "graph_kernels_per_inversion": int(info["graph_kernels"]),
+                   "job_samples": job_vis, "bind_s": round(bind_s, 2),
+                   "plain_one_at_a_time_gvis_s": plain_value,
+                   "batched_over_plain": value / plain_value,
+                   "checks": checks, "datagen_s": round(gen_s, 1),
+                   "step": "one inversion of every facet x channel job (graph replay), device "
+                           "visibilities in, device images out"},
+        "clocks": clk,
+        "e2e": {"value": job_vis / (e_ms * 1e-3) / 1e9, "unit": "Gvis/s",
+                "h2d_bytes_per_step": int(h_vis.nbytes),
+                "d2h_bytes_per_step": int(h_img.nbytes), "ms_per_step": e_ms},
+        "gpu_launches": int(launches),
+    }
+
+
 def _lib_launches():
     from wsclean_gb300 import _lib
     return _lib.lib().wgpu_kernel_launch_count()
@@ -654,6 +805,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=200000)
     ap.add_argument("--cpu-planes", type=int, default=2)
+    ap.add_argument("--facet-times", type=int, default=620,
+                    help="time steps of the facet workload (6200 in the full workload)")
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests in the serving stream (0 skips it)")
     ap.add_argument("--serve-slots", type=int, default=8)
@@ -671,6 +824,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.workload == "facets":
+        print(json.dumps(run_facets(args)), flush=True)
         return
     if args.workload == "fullpol4096":
         print(json.dumps(run_fullpol(args)), flush=True)

@@ -14,8 +14,9 @@
 // waves that fit the plane-memory budget.  The whole inversion is captured in
 // one CUDA graph: per job the visibilities are stamped into its records; per
 // wave ONE persistent gridding launch works through the items of every pair in
-// the wave, then each pair's FFT passes accumulate into its job's image; per
-// job the grid correction finishes the image.
+// the wave, then each pair's FFT passes accumulate into its job's image (the
+// pairs' FFT chains spread over four streams, joined before the next wave);
+// per job the grid correction finishes the image.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -84,6 +85,9 @@ struct wgpu_facets {
   double plane_budget = 0;
   int device = 0;
   cudaStream_t stream = nullptr;
+  static constexpr int kSide = 4;  // streams of the per-job FFT chains
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t ev_grid = nullptr, ev_side[kSide] = {};
   FftTables *fft = nullptr;
   std::vector<void *> owned;
   std::vector<Job> jobs;
@@ -125,6 +129,11 @@ struct wgpu_facets {
     if (d_flags) cudaFree(d_flags);
     if (h_flags) cudaFreeHost(h_flags);
     if (fft) fft_tables_destroy(fft);
+    for (int k = 0; k < kSide; ++k) {
+      if (side[k]) cudaStreamDestroy(side[k]);
+      if (ev_side[k]) cudaEventDestroy(ev_side[k]);
+    }
+    if (ev_grid) cudaEventDestroy(ev_grid);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -356,15 +365,25 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
       }
       launch_grid_items_multi(f->support, d_jobs[wi], d_base[wi], (int)f->waves[wi].size(),
                               totals[wi], s);
+      // the FFT chains of the wave's pairs on side streams (a job's pairs
+      // stay on one stream: they accumulate into the same image)
+      WGPU_CUDA(cudaEventRecord(f->ev_grid, s));
+      for (int k = 0; k < wgpu_facets::kSide; ++k)
+        WGPU_CUDA(cudaStreamWaitEvent(f->side[k], f->ev_grid, 0));
       for (const Slot &sl : f->waves[wi]) {
         const Job &j = f->jobs[sl.job];
+        cudaStream_t ss = f->side[sl.job % wgpu_facets::kSide];
         float2 *planes = f->pool + sl.planes_off, *rows = f->pool + sl.rows_off;
-        launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, f->d_flags, s);
+        launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, f->d_flags, ss);
         launch_fft_cols_a(*f->fft, j.dp, (int)j.plan.fft_n1, (int)j.plan.fft_n2, rows, j.rstride,
-                          sl.nb, -1.0f, s);
+                          sl.nb, -1.0f, ss);
         launch_fft_cols_b_forward_accumulate(*f->fft, j.dp, (int)j.plan.fft_n1,
                                              (int)j.plan.fft_n2, rows, j.rstride, sl.nb, sl.p0,
-                                             j.nu_w, j.acc, s);
+                                             j.nu_w, j.acc, ss);
+      }
+      for (int k = 0; k < wgpu_facets::kSide; ++k) {
+        WGPU_CUDA(cudaEventRecord(f->ev_side[k], f->side[k]));
+        WGPU_CUDA(cudaStreamWaitEvent(s, f->ev_side[k], 0));
       }
     }
     for (Job &j : f->jobs)
@@ -458,6 +477,11 @@ int wgpu_facets_create(const wgpu_facet_t *facets, size_t n_facets, const size_t
     f->plane_budget = plane_budget_bytes > 0 ? plane_budget_bytes : 40e9;
     WGPU_CUDA(cudaGetDevice(&f->device));
     WGPU_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+    for (int k = 0; k < wgpu_facets::kSide; ++k) {
+      WGPU_CUDA(cudaStreamCreateWithFlags(&f->side[k], cudaStreamNonBlocking));
+      WGPU_CUDA(cudaEventCreateWithFlags(&f->ev_side[k], cudaEventDisableTiming));
+    }
+    WGPU_CUDA(cudaEventCreateWithFlags(&f->ev_grid, cudaEventDisableTiming));
     WGPU_CUDA(cudaMalloc(&f->d_flags, sizeof(unsigned)));
     WGPU_CUDA(cudaMemset(f->d_flags, 0, sizeof(unsigned)));
     WGPU_CUDA(cudaMallocHost(&f->h_flags, sizeof(unsigned)));
