@@ -138,7 +138,7 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
 // the kernel values [kGridRound][kw] with kw = 3W rounded up to an odd count
 // (kx[W], ky[W], kz[W] per record; the odd stride keeps the stores of a warp
 // on distinct banks).
-constexpr int kGridRound = 128;  // records staged per round
+constexpr int kGridRound = 64;  // records staged per round (four threads stage each)
 __host__ __device__ constexpr int grid_weight_stride(int W) { return (3 * W) | 1; }
 template <int T, int G, int W>
 constexpr size_t grid_smem_bytes() {
@@ -244,28 +244,29 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   const uint32_t hi = min(lo + kItemVis, rcum[9]);
 
   for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
-    // stage: threads t and t + kGridRound share read t; the first evaluates
-    // kx and ky, the second kz and the meta data
+    // stage: four threads share read t (role 0: kx, 1: ky, 2: kz, 3: meta)
     {
+      static_assert(kThreads == 4 * kGridRound, "four staging roles");
       const int t = threadIdx.x % kGridRound;
-      const bool second = threadIdx.x >= kGridRound;
+      const int role = threadIdx.x / kGridRound;
       const uint32_t pos = rb + (uint32_t)t;
       if (pos < hi) {
         int r = 0;
         while (pos >= rcum[r + 1]) ++r;
         const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
         float *w = wts + t * kWS;
-        if (!second) {
+        if (role == 0) {
 #pragma unroll
-          for (int k = 0; k < W; ++k) {
-            w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
-            w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
-          }
-        } else {
+          for (int k = 0; k < W; ++k) w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
+        } else if (role == 1) {
+#pragma unroll
+          for (int k = 0; k < W; ++k) w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
+        } else if (role == 2) {
 #pragma unroll
           for (int k = 0; k < W; ++k)
             w[2 * W + k] = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
                                            : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+        } else {
           int iu_rel = v.iu - tu * T;
           if (iu_rel >= T) iu_rel -= p.nu;
           int iv_rel = v.iv - tv * T;
