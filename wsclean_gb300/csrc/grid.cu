@@ -138,7 +138,7 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
 // the kernel values [kGridRound][kw] with kw = 3W rounded up to an odd count
 // (kx[W], ky[W], kz[W] per record; the odd stride keeps the stores of a warp
 // on distinct banks).
-constexpr int kGridRound = 64;  // records staged per round (four threads stage each)
+constexpr int kGridRound = 32;  // records staged per round (eight threads stage each)
 __host__ __device__ constexpr int grid_weight_stride(int W) { return (3 * W) | 1; }
 template <int T, int G, int W>
 constexpr size_t grid_smem_bytes() {
@@ -244,28 +244,30 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   const uint32_t hi = min(lo + kItemVis, rcum[9]);
 
   for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
-    // stage: four threads share read t (role 0: kx, 1: ky, 2: kz, 3: meta)
+    // stage: eight threads share read t; roles 0-5 evaluate half of kx, ky
+    // or kz each, role 6 writes the meta data
     {
-      static_assert(kThreads == 4 * kGridRound, "four staging roles");
+      static_assert(kThreads == 8 * kGridRound, "eight staging roles");
+      constexpr int kHalf = (W + 1) / 2;
       const int t = threadIdx.x % kGridRound;
       const int role = threadIdx.x / kGridRound;
       const uint32_t pos = rb + (uint32_t)t;
-      if (pos < hi) {
+      if (pos < hi && role < 7) {
         int r = 0;
         while (pos >= rcum[r + 1]) ++r;
         const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
         float *w = wts + t * kWS;
-        if (role == 0) {
+        if (role < 6) {
+          const int dim = role >> 1, k0 = (role & 1) * kHalf;
+          const float f = dim == 0 ? v.fu : (dim == 1 ? v.fv : v.fw);
 #pragma unroll
-          for (int k = 0; k < W; ++k) w[k] = es_eval(p.beta, (v.fu + (float)k) * inv_half);
-        } else if (role == 1) {
-#pragma unroll
-          for (int k = 0; k < W; ++k) w[W + k] = es_eval(p.beta, (v.fv + (float)k) * inv_half);
-        } else if (role == 2) {
-#pragma unroll
-          for (int k = 0; k < W; ++k)
-            w[2 * W + k] = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
-                                           : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+          for (int kk = 0; kk < kHalf; ++kk) {
+            const int k = k0 + kk;
+            if (k < W)
+              w[dim * W + k] = (dim == 2 && p.n_planes == 1)
+                                   ? (k == 0 ? 1.0f : 0.0f)
+                                   : es_eval(p.beta, (f + (float)k) * inv_half);
+          }
         } else {
           int iu_rel = v.iu - tu * T;
           if (iu_rel >= T) iu_rel -= p.nu;
