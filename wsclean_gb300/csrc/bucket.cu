@@ -131,10 +131,20 @@ struct MaxOp {
   __device__ double operator()(double a, double b) const { return fmax(a, b); }
 };
 
+// With TABLE the block first divides each channel's frequency by c into
+// shared memory (n_chan doubles), instead of dividing once per sample; the
+// quotients are the same correctly rounded values either way.
+template <bool TABLE>
 __global__ void __launch_bounds__(kThreads)
     w_extent_kernel(const double *uvw, const double *freq, Selector sel,
                     int64_t n_rows, int64_t n_chan,
                     unsigned long long *out /*[3]: min key, max key, count*/) {
+  extern __shared__ double fl_tab[];
+  if (TABLE) {
+    for (int64_t c = threadIdx.x; c < n_chan; c += blockDim.x)
+      fl_tab[c] = __ddiv_rn(freq[c], kSpeedOfLight);
+    __syncthreads();
+  }
   double wmin = 1e300, wmax = -1e300;
   unsigned long long cnt = 0;
   const int64_t n = n_rows * n_chan;
@@ -142,7 +152,7 @@ __global__ void __launch_bounds__(kThreads)
        e += (int64_t)gridDim.x * blockDim.x) {
     if (!sel(e)) continue;
     const int64_t r = e / n_chan, c = e - r * n_chan;
-    const double fl = __ddiv_rn(freq[c], kSpeedOfLight);
+    const double fl = TABLE ? fl_tab[c] : __ddiv_rn(freq[c], kSpeedOfLight);
     const double wl = __dmul_rn(uvw[3 * r + 2], fl);
     wmin = fmin(wmin, wl);
     wmax = fmax(wmax, wl);
@@ -320,7 +330,12 @@ void compute_w_extent(const double *d_uvw, const double *d_freq,
   const int64_t n = n_rows * n_chan;
   unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), 152 * 8);
   const Selector sel{skip_zero ? (const float2 *)d_vis : nullptr, d_mask};
-  w_extent_kernel<<<blocks, kThreads, 0, s>>>(d_uvw, d_freq, sel, n_rows, n_chan, d);
+  if (n_chan <= 4096) {
+    w_extent_kernel<true><<<blocks, kThreads, sizeof(double) * n_chan, s>>>(d_uvw, d_freq, sel,
+                                                                           n_rows, n_chan, d);
+  } else {
+    w_extent_kernel<false><<<blocks, kThreads, 0, s>>>(d_uvw, d_freq, sel, n_rows, n_chan, d);
+  }
   check_launch("w_extent_kernel");
   unsigned long long out[3];
   WGPU_CUDA(cudaMemcpyAsync(out, d, sizeof(out), cudaMemcpyDeviceToHost, s));

@@ -382,7 +382,7 @@ __device__ __forceinline__ int row_butterfly(float2 *v, int i, int p, unsigned p
   if (k > 0) {
 #pragma unroll
     for (int t = 1; t < R; ++t) {
-      float2 w = __ldg(tws + (t - 1) * p + k);
+      float2 w = tws[(t - 1) * p + k];  // shared or read-only global table
       w.y *= -sign;  // tables hold exp(-2 pi i t k / (p R)); sign +1 conjugates
       v[t] = cmul(v[t], w);
     }
@@ -481,10 +481,13 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
     fft_rows_persistent_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
                                const float2 *__restrict__ in, int in_stride, uint32_t in_bytes,
                                float2 *__restrict__ out, int out_stride, int n_rows, int width,
-                               int buf_elems, unsigned *__restrict__ err) {
+                               int buf_elems, int mid_tab, unsigned *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char row_smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(row_smem);  // two mbarriers
   float2 *bufs = reinterpret_cast<float2 *>(row_smem + 128);
+  // twiddles of the middle stages (mid_tab entries from stage 1 on), copied
+  // once per CTA when they fit; otherwise read from global memory
+  float2 *tab = bufs + 2 * (size_t)buf_elems;
   const int L = d.L;
   const float sign = FWD ? -1.0f : 1.0f;
   const int G = gridDim.x;
@@ -494,6 +497,7 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_proxy_async();
   }
+  for (int i = threadIdx.x; i < mid_tab; i += blockDim.x) tab[i] = __ldg(tws + st.tw_off[1] + i);
   __syncthreads();
   int row = blockIdx.x;
   if (threadIdx.x == 0) {
@@ -525,11 +529,13 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
     int p = 16, s = 1;
     const int n_mid16 = d.n_stages - 2 - (MID8 ? 1 : 0);
     for (int m = 0; m < n_mid16; ++m, ++s) {
-      row_stage_inplace<16, kRowInSlot>(buf, L, p, d.magic[s], sign, tws + st.tw_off[s], width);
+      const float2 *tw = mid_tab ? tab + (st.tw_off[s] - st.tw_off[1]) : tws + st.tw_off[s];
+      row_stage_inplace<16, kRowInSlot>(buf, L, p, d.magic[s], sign, tw, width);
       p *= 16;
     }
     if (MID8) {
-      row_stage_inplace<8, kRowInSlot>(buf, L, p, d.magic[s], sign, tws + st.tw_off[s], width);
+      const float2 *tw = mid_tab ? tab + (st.tw_off[s] - st.tw_off[1]) : tws + st.tw_off[s];
+      row_stage_inplace<8, kRowInSlot>(buf, L, p, d.magic[s], sign, tw, width);
       p *= 8;
       ++s;
     }
@@ -904,7 +910,16 @@ static void launch_persistent(const FftDesc &d, const RowStages &st, const float
   if ((in_bytes & 15) || (buf_elems & 1))
     throw Error(WGPU_ERR_INVALID, "row transform sizes must be multiples of 16 bytes");
   const int threads = std::min(kRowThreadsMax, (p.nu / 16 + 31) / 32 * 32);
-  const size_t smem = 128 + 2 * sizeof(float2) * (size_t)buf_elems;
+  size_t smem = 128 + 2 * sizeof(float2) * (size_t)buf_elems;
+  // middle-stage twiddles (stages 1 .. n-2) into shared memory when they fit
+  int mid_tab = d.n_stages > 2 ? st.tw_off[d.n_stages - 1] - st.tw_off[1] : 0;
+  int dev = 0, smem_max = 0;
+  WGPU_CUDA(cudaGetDevice(&dev));
+  WGPU_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem + sizeof(float2) * (size_t)mid_tab <= (size_t)smem_max)
+    smem += sizeof(float2) * (size_t)mid_tab;
+  else
+    mid_tab = 0;
   auto kern = fft_rows_persistent_kernel<FWD, LAST, MID8>;
   set_smem((const void *)kern, smem);
   int per_sm = 0;
@@ -912,7 +927,7 @@ static void launch_persistent(const FftDesc &d, const RowStages &st, const float
   if (per_sm < 1) throw Error(WGPU_ERR_INVALID, "row transform does not fit on an SM");
   const int blocks = std::min(n_rows, sm_count_fft() * per_sm);
   kern<<<blocks, threads, smem, s>>>(d, st, tws, in, in_stride, in_bytes, out, out_stride,
-                                      n_rows, p.width, buf_elems, err);
+                                      n_rows, p.width, buf_elems, mid_tab, err);
   check_launch(FWD ? "fft_rows_persistent_kernel<forward>"
                    : "fft_rows_persistent_kernel<backward>");
 }
