@@ -615,8 +615,30 @@ __global__ void __launch_bounds__(kRowPingPongMax / 16, 2)
 constexpr int kColThreads = 512;
 constexpr int kPanel = 32;  // columns per panel
 
+// Loads a panel of n_rows x kPanel elements (row r at src + r * row_stride)
+// into shared memory, issuing all of a thread's loads before the stores so
+// that enough bytes are in flight to cover the HBM latency.
+__device__ __forceinline__ void load_panel(float2 *__restrict__ s, const float2 *__restrict__ src,
+                                           size_t row_stride, int n_rows) {
+  constexpr int kBatch = 8;  // loads in flight per thread
+  const int n_el = n_rows * kPanel;
+  for (int e0 = threadIdx.x; e0 < n_el; e0 += kBatch * blockDim.x) {
+    float2 tmp[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k) {
+      const int e = e0 + k * blockDim.x;
+      if (e < n_el) tmp[k] = __ldg(src + (size_t)(e / kPanel) * row_stride + (e % kPanel));
+    }
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k) {
+      const int e = e0 + k * blockDim.x;
+      if (e < n_el) s[e] = tmp[k];
+    }
+  }
+}
+
 // Pass A (forward) / A' (backward): strided length-n1 transforms.
-__global__ void __launch_bounds__(kColThreads)
+__global__ void __launch_bounds__(kColThreads, 3)
     fft_cols_pass_a_kernel(FftDesc d1, float2 *__restrict__ R, int rstride, int nv,
                            int n2, float sign, const float2 *__restrict__ tw1,
                            const float2 *__restrict__ twN) {
@@ -624,10 +646,7 @@ __global__ void __launch_bounds__(kColThreads)
   const int n1 = d1.L;
   const int cg = blockIdx.x, r2 = blockIdx.y;
   float2 *base = R + (size_t)blockIdx.z * nv * rstride + cg * kPanel;
-  for (int e = threadIdx.x; e < n1 * kPanel; e += blockDim.x) {
-    const int r1 = e / kPanel, c = e % kPanel;
-    s[e] = base[(size_t)(r2 + n2 * r1) * rstride + c];
-  }
+  load_panel(s, base + (size_t)r2 * rstride, (size_t)n2 * rstride, n1);
   __syncthreads();
   // backward: this pass runs last and the twiddle was applied in pass B'
   const float2 *res = fft_smem<kPanelLayout>(s, s + n1 * kPanel, d1, sign, tw1);
@@ -720,10 +739,7 @@ __global__ void __launch_bounds__(kColThreads, 2)
   for (int c = 0; c < NE; ++c) part[c] = 0.f;
   for (int b = 0; b < n_batch; ++b) {
     const float2 *base = R + (size_t)b * nv * rstride + (size_t)n2 * k1 * rstride + cg * kPanel;
-    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-      const int r2 = e / kPanel, c = e % kPanel;
-      s[e] = base[(size_t)r2 * rstride + c];
-    }
+    load_panel(s, base, (size_t)rstride, n2);
     __syncthreads();
     const float2 *res = fft_smem<kPanelLayout>(s, s + ne, d2, -1.0f, tw2);
 #pragma unroll
