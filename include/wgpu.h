@@ -257,6 +257,13 @@ void *wgpu_gridder_stream(wgpu_gridder_t *gridder);
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t wgpu_kernel_launch_count(void);
 
+/* Failure-detection self-test (no counterpart in the reference): one CTA
+ * waits, with the bounded mbarrier wait the row transforms use, on a barrier
+ * that nothing arrives at.  The wait must expire after timeout_ms (at most
+ * 10 s) and be reported; returns WGPU_ERR_TIMEOUT in that case, WGPU_OK if
+ * the wait did not expire.  The device stays usable afterwards. */
+int wgpu_selftest_bounded_wait(double timeout_ms);
+
 /* ------------------------------------------------------------------------ */
 /* Bucketing pass on its own (test hook for bit-exactness)                    */
 /* ------------------------------------------------------------------------ */

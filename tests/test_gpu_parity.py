@@ -343,3 +343,18 @@ def test_bound_split_units_over_plane_batches(wgpu_lib, oracle_lib):
     assert rel(pv[sel], pd) <= eps
     g.close()
     ref_g.close()
+
+
+def test_bounded_wait_expires_and_device_stays_usable(wgpu_lib):
+    """A bounded device wait on a barrier that nothing arrives at expires,
+    is reported as WGPU_ERR_TIMEOUT, and later work runs normally."""
+    st = wgpu_lib.wgpu_selftest_bounded_wait(50.0)
+    assert st == _lib.WGPU_ERR_TIMEOUT
+    assert b"expired" in wgpu_lib.wgpu_last_error()
+    W, dl = 64, 1e-3
+    uvw, freq, vis = synthetic.random_points(100, 2, W, dl, seed=91)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=1e-4)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    assert np.isfinite(g.RealImage()).all()
+    g.close()

@@ -127,6 +127,7 @@ _PROTOS = {
     "wgpu_gridder_set_plane_budget": (I, [P, D]),
     "wgpu_gridder_stream": (P, [P]),
     "wgpu_kernel_launch_count": (C.c_uint64, []),
+    "wgpu_selftest_bounded_wait": (I, [D]),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,
                               C.POINTER(C.c_int64)]),
     "wgpu_bucket_noalloc": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P,

@@ -944,6 +944,21 @@ void *wgpu_gridder_stream(wgpu_gridder_t *g) { return g ? (void *)g->stream : nu
 
 uint64_t wgpu_kernel_launch_count(void) { return launch_count(); }
 
+int wgpu_selftest_bounded_wait(double timeout_ms) {
+  if (!(timeout_ms > 0) || timeout_ms > 10000)
+    return fail(WGPU_ERR_INVALID, "timeout must be in (0, 10000] ms");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(WGPU_ERR_CUDA, "no usable CUDA device");
+  }
+  int st = WGPU_OK;
+  const int g = guarded([&] { st = bounded_wait_selftest(timeout_ms); });
+  if (g != WGPU_OK) return g;
+  if (st == WGPU_ERR_TIMEOUT) return fail(st, "bounded device wait expired (self-test)");
+  return st;
+}
+
 int wgpu_gridder_set_plane_budget(wgpu_gridder_t *g, double bytes) {
   return guarded([&] {
     if (!g) throw Error(WGPU_ERR_INVALID, "null gridder");

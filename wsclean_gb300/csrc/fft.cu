@@ -351,13 +351,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
   return ok != 0;
 }
-// Waits for the phase of `parity` with a deadline of about two seconds;
-// returns false if it expired.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  const long long deadline = clock64() + (4ll << 30);
+// Waits for the phase of `parity` for at most `cycles` SM clock cycles (the
+// row kernels give about two seconds); returns false if the wait expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  long long cycles = 4ll << 30) {
+  const long long deadline = clock64() + cycles;
   while (!mbar_try_wait(bar, parity))
     if (clock64() > deadline) return false;
   return true;
+}
+
+// Self-test of the bounded wait: waits on an mbarrier that nothing arrives
+// at, so the wait must expire; records the expiry and returns.
+__global__ void bounded_wait_selftest_kernel(long long cycles, unsigned *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar);
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0, cycles);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicAdd(err, 1u);
 }
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -1047,6 +1058,29 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
         d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN);
   }
   check_launch("fft_cols_backward_screen_kernel");
+}
+
+// Runs the bounded-wait self-test on the current device; returns
+// WGPU_ERR_TIMEOUT when the wait expired and reported it (the expected
+// outcome), WGPU_OK if it did not.
+int bounded_wait_selftest(double timeout_ms) {
+  int dev = 0, khz = 0;
+  WGPU_CUDA(cudaGetDevice(&dev));
+  WGPU_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+  const long long cycles = (long long)(timeout_ms * (double)khz);
+  unsigned *d_err = nullptr, h_err = 0;
+  WGPU_CUDA(cudaMalloc(&d_err, sizeof(unsigned)));
+  cudaError_t e = cudaMemset(d_err, 0, sizeof(unsigned));
+  if (e == cudaSuccess) {
+    bounded_wait_selftest_kernel<<<1, 64>>>(cycles, d_err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaFree(d_err);
+  if (e != cudaSuccess) throw Error(WGPU_ERR_CUDA, cudaGetErrorString(e));
+  count_launch();
+  return h_err ? WGPU_ERR_TIMEOUT : WGPU_OK;
 }
 
 }  // namespace wgpu

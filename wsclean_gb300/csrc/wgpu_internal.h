@@ -182,6 +182,8 @@ void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p, const float2 *
                                   cudaStream_t s);
 // Creates the row-transform tables of length L (before a graph capture).
 void fft_prepare_rows(FftTables &t, int L);
+// Bounded-wait self-test (fft.cu): WGPU_ERR_TIMEOUT when the wait expired.
+int bounded_wait_selftest(double timeout_ms);
 // Column passes (four-step split nv = n1 * n2, see fft.cu): pass A over
 // strided length-n1 transforms, pass B over contiguous length-n2 transforms
 // with the fused w-screen.
