@@ -246,7 +246,7 @@ int wgpu_gridder_last_timings(const wgpu_gridder_t *gridder, double *ms,
 int wgpu_gridder_pin_plan(wgpu_gridder_t *gridder, const wgpu_plan_t *plan);
 
 /* Cap, in bytes, on the device memory of the w-plane batch that this
- * gridder's plans keep resident (0 = 40% of free device memory, at most 40 GB).
+ * gridder's plans keep resident (0 = 40% of free device memory, at most 64 GB).
  * Lets several gridders share one GPU; no counterpart in the reference. */
 int wgpu_gridder_set_plane_budget(wgpu_gridder_t *gridder, double bytes);
 
@@ -403,8 +403,9 @@ void wgpu_server_destroy(wgpu_server_t *server);
  *   create: channel_groups holds n_groups + 1 increasing channel boundaries.
  *   bind:   uploads uvw / freq once, plans every job with one kernel support
  *           width (the width with the lowest summed cost-model time), buckets
- *           every job, packs the jobs' 16-plane batches into waves under
- *           plane_budget_bytes (0 = 40 GB) and captures the whole inversion
+ *           every job, packs the jobs' 16-plane batches (planes, rows and
+ *           gridding spill) into waves under plane_budget_bytes (0 = 40 GB)
+ *           and captures the whole inversion
  *           in one CUDA graph: per wave, one persistent gridding launch over
  *           all the wave's jobs, then each job's FFT passes.
  *   invert: visibilities [row][chan] complex64 in, and the dirty images of

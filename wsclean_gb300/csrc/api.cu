@@ -293,7 +293,7 @@ wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis)
   r.n_vis = n_vis;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-    r.memory_budget_bytes = std::min(40e9, 0.4 * (double)(free_b + g->arena.total()));
+    r.memory_budget_bytes = std::min(64e9, 0.4 * (double)(free_b + g->arena.total()));
   }
   if (g->plane_budget > 0) r.memory_budget_bytes = g->plane_budget;
   // WGPU_PLANE_BUDGET_GB caps the plane-batch memory (profiling small cases)
@@ -503,7 +503,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   const ItemAlloc own = [bp](int, size_t bytes) -> void * { return bp->alloc(bytes); };
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
-    b->gitems.push_back(plan_grid_items(dp, b->offsets, (int)p0, nb, nullptr, own, s));
+    b->gitems.push_back(plan_grid_items(dp, b->offsets, (int)p0, nb, own, s));
     b->ditems.push_back(plan_degrid_items(dp, b->offsets, (int)p0, nb, own, s));
   }
   WGPU_CUDA(cudaStreamSynchronize(s));

@@ -70,7 +70,7 @@ struct Job {
 
 struct Slot {
   int job, batch, p0, nb;
-  size_t planes_off, rows_off;  // in float2 elements of the pool
+  size_t planes_off, rows_off, spill_off;  // in float2 elements of the pool
 };
 
 }  // namespace
@@ -258,11 +258,14 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     j.img = f->d_images + img_off;
     img_off += j.facet.width * j.facet.height;
     wgpu_facets *fp = f;
-    const ItemAlloc own = [fp](int, size_t bytes) -> void * { return fp->alloc(bytes); };
+    // spill slots come from the wave pool (set when the waves are packed)
+    const ItemAlloc own = [fp](int which, size_t bytes) -> void * {
+      return which == 3 ? nullptr : fp->alloc(bytes);
+    };
     const int B = (int)j.plan.plane_batch;
     for (int p0 = 0; p0 < j.plan.n_planes; p0 += B) {
       const int nb = (int)std::min<int64_t>(B, j.plan.n_planes - p0);
-      j.items.push_back(plan_grid_items(j.dp, j.offsets, p0, nb, nullptr, own, s));
+      j.items.push_back(plan_grid_items(j.dp, j.offsets, p0, nb, own, s));
     }
     fft_twiddles(*f->fft, (int)j.plan.nu);
     fft_twiddles(*f->fft, (int)j.plan.nv);
@@ -299,14 +302,21 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     const Job &j = f->jobs[sl.job];
     const size_t pe = (size_t)sl.nb * j.plan.nu * j.plan.nv;
     const size_t re = (size_t)sl.nb * j.plan.nv * j.rstride;
-    if (!wave.empty() && (double)(used + pe + re) * sizeof(float2) > f->plane_budget) close_wave();
+    // every region starts on a 512-byte boundary: the row transforms read
+    // planes with 16-byte bulk copies and vector loads
+    const size_t se = (grid_spill_elems(j.dp, j.items[sl.batch]) + 63) / 64 * 64;
+    if (!wave.empty() && (double)(used + pe + re + se) * sizeof(float2) > f->plane_budget)
+      close_wave();
     sl.planes_off = used;
     sl.rows_off = used + pe;
-    used += pe + re;
+    sl.spill_off = used + pe + re;
+    used += pe + re + se;
     wave.push_back(sl);
   }
   close_wave();
   f->pool = (float2 *)f->alloc(sizeof(float2) * pool_elems);
+  for (const auto &w : f->waves)
+    for (const Slot &sl : w) f->jobs[sl.job].items[sl.batch].spill = f->pool + sl.spill_off;
 
   // job tables of each wave's gridding launch
   std::vector<GridJob *> d_jobs;
@@ -325,6 +335,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
       g.off = j.offsets;
       g.item_off = wi.item_off;
       g.desc = wi.desc;
+      g.slot = wi.slot;
+      g.spill = wi.spill;
       g.planes = f->pool + sl.planes_off;
       g.p_begin = sl.p0;
       g.n_batch = sl.nb;
@@ -374,6 +386,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
         const Job &j = f->jobs[sl.job];
         cudaStream_t ss = f->side[sl.job % wgpu_facets::kSide];
         float2 *planes = f->pool + sl.planes_off, *rows = f->pool + sl.rows_off;
+        launch_spill_fixup(j.dp, j.items[sl.batch], sl.p0, sl.nb, planes, ss);
         launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, f->d_flags, ss);
         launch_fft_cols_a(*f->fft, j.dp, (int)j.plan.fft_n1, (int)j.plan.fft_n2, rows, j.rstride,
                           sl.nb, -1.0f, ss);

@@ -1,20 +1,21 @@
 // K2 gridding and K3 degridding over (uv tile, w-plane group) work units.
 //
-// Work unit = (uv tile T x T, group of G consecutive w planes).  A gridding
-// unit reads the visibilities bucketed in its own tile and in the three
-// neighbouring tiles whose footprints can spill into it (left, below,
-// below-left; the footprint corner decides the bucket), restricted by key
-// range to the first planes that reach the group.  Units are split into work
-// items of at most kItemVis visibility reads, and one persistent launch works
-// through the items of a plane batch from a device counter, so that the
-// crowded tiles of a dense uv core are shared by many CTAs.
+// Work unit = (uv tile T x T, group of G consecutive w planes).  A unit reads
+// the visibilities bucketed in its own tile (footprint corner in the tile;
+// the key's class says which neighbours the footprint reaches), restricted by
+// key range to the first planes that reach the group.  Units are split into
+// work items of at most kItemVis visibility reads, and one persistent launch
+// works through the items of a plane batch, so that the crowded tiles of a
+// dense uv core are shared by many CTAs.
 //
-// Gridding item: a block keeps the unit's cells in shared memory; each warp
-// owns two rows of every plane and adds the footprints of the staged records
-// with plain read-add-writes; the tile is written to HBM once per item (a
-// unit split into several items adds into cells zeroed beforehand).  One
-// launch can also serve many jobs (facets x channel groups), each with its own
-// plan, records and planes (grid_kernel_multi).
+// Gridding item: a block accumulates whole footprints into the unit's halo
+// region (the tile plus W - 1 cells to the right and up, G planes) in shared
+// memory; warp k owns the halo rows congruent to k modulo 8, so every row of a
+// footprint has one owner and cells are updated with plain read-add-writes.
+// The tile's own cells are written to the planes once per item; the border
+// cells go to the unit's spill slot and a fix-up pass adds them into the
+// neighbouring tiles.  One launch can also serve many jobs (facets x channel
+// groups), each with its own plan, records and planes (grid_kernel_multi).
 //
 // Degridding item: loads its tile plus a (W-1)-cell halo of G planes into
 // shared memory and gathers, for each visibility of its slice of the own
@@ -79,13 +80,13 @@ __device__ __forceinline__ void unit_range(const DevPlan &p, const uint32_t *off
   *s1 = __ldg(off + key0 + phi + 1);
 }
 
-// Planning pass: one warp per unit counts the unit's visibility reads and its
-// work items; the cells of split gridding units are zeroed here.
+// Planning pass: one warp per unit counts the reads of the unit (the four
+// classes of its own tile) and its work items.
 template <int T, int G>
 __global__ void __launch_bounds__(kThreads)
     grid_plan_kernel(DevPlan p, const uint32_t *__restrict__ off, int p_begin, int n_batch,
                      int n_units, int degrid, uint32_t *__restrict__ items,
-                     uint32_t *__restrict__ counts, float2 *__restrict__ planes) {
+                     uint32_t *__restrict__ counts) {
   const int unit = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (unit >= n_units) return;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(kThreads)
   const int q0 = p_begin + group * G;
   const int q1 = min(q0 + G, p_begin + n_batch);
   uint32_t cnt = 0;
-  if (lane < (degrid ? 4 : 9)) {
+  if (lane < 4) {
     uint32_t a, b;
     unit_range(p, off, tile, q0, q1, lane, &a, &b);
     cnt = b - a;
@@ -107,18 +108,20 @@ __global__ void __launch_bounds__(kThreads)
     items[unit] = n_items;
     counts[unit] = cnt;
   }
-  // planes is null when the items are planned ahead of the gridding (bound
-  // sets); zero_split_units_kernel then clears these cells before each pass.
-  if (!degrid && planes != nullptr && n_items > 1) {
-    const int tu = tile % p.ntu, tv = tile / p.ntu;
-    const size_t plane_elems = (size_t)p.nu * p.nv;
-    for (int c = lane; c < (q1 - q0) * T * T; c += 32) {
-      const int pq = c / (T * T), rem = c - pq * T * T;
-      const int row = rem / T, col = rem - row * T;
-      planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
-             tu * T + col] = make_float2(0.f, 0.f);
-    }
-  }
+}
+
+// Spill slots: flags of the units with visibilities (scanned afterwards), then
+// slot = scanned index for those units and -1 for the others.
+__global__ void slot_flags_kernel(const uint32_t *__restrict__ counts, int n_units,
+                                  uint32_t *__restrict__ flags) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < n_units) flags[u] = counts[u] > 0 ? 1u : 0u;
+  if (u == n_units) flags[u] = 0u;
+}
+__global__ void slot_final_kernel(const uint32_t *__restrict__ counts, int n_units,
+                                  int *__restrict__ slot) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < n_units && counts[u] == 0) slot[u] = -1;
 }
 
 // item -> unit descriptors (bit 31 marks a unit without visibilities).
@@ -132,81 +135,87 @@ __global__ void fill_items_kernel(const uint32_t *__restrict__ item_off,
   for (uint32_t i = a; i < b; ++i) desc[i] = (uint32_t)unit | flag;
 }
 
-// Shared-memory layout of the gridding kernel: the tile's float2 cells
-// [G][T][T], then the staged round: five meta arrays [5][kGridRound] (re, im,
-// u and v corner relative to the tile, first plane relative to the group) and
-// the kernel values [kGridRound][kw] with kw = 3W rounded up to an odd count
-// (kx[W], ky[W], kz[W] per record; the odd stride keeps the stores of a warp
-// on distinct banks).
+// Geometry of the gridding halo region: R = T + W - 1 rows and columns; the
+// plane stride is padded to 8 modulo 16 float2 for W <= 8 (a half-warp then
+// covers eight columns of two planes on distinct bank pairs); G planes per
+// unit (16 for W <= 8, 8 above, to keep the region near 70 KB).
+__host__ __device__ constexpr int grid_group(int W) { return W <= 8 ? 16 : 8; }
+__host__ __device__ constexpr int halo_rows(int T, int W) { return T + W - 1; }
+__host__ __device__ constexpr int halo_plane(int T, int W) {
+  return W <= 8 ? ((halo_rows(T, W) * halo_rows(T, W) + 15) / 16 * 16 + 8)
+                : ((halo_rows(T, W) * halo_rows(T, W) + 15) / 16 * 16);
+}
+// Border cells of a unit (outside its tile): the right strip (columns T..R-1,
+// all R rows), then the top strip (rows T..R-1, columns 0..T-1).
+__host__ __device__ constexpr int spill_cells(int T, int W) {
+  return (W - 1) * halo_rows(T, W) + (W - 1) * T;
+}
+__host__ __device__ __forceinline__ int border_index(int T, int W, int r, int c) {
+  return c >= T ? r * (W - 1) + (c - T) : (W - 1) * halo_rows(T, W) + (r - T) * T + c;
+}
+
+// Shared-memory layout of the gridding kernels: the halo cells [G][plane],
+// then the staged round: the meta data of each read (int4: u and v corner
+// relative to the tile, first plane relative to the group), its weighted
+// visibility (float2), and the kernel values [kGridRound][kw] with kw = 3W
+// rounded up to an odd count (kx[W], ky[W], kz[W] per read; the odd stride
+// keeps the stores of a warp on distinct banks).
 constexpr int kGridRound = 32;  // records staged per round (eight threads stage each)
 __host__ __device__ constexpr int grid_weight_stride(int W) { return (3 * W) | 1; }
 template <int T, int G, int W>
 constexpr size_t grid_smem_bytes() {
-  return sizeof(float2) * G * T * T +
-         sizeof(float) * kGridRound * (5 + grid_weight_stride(W));
+  return sizeof(float2) * G * halo_plane(T, W) +
+         (size_t)kGridRound * (sizeof(int4) + sizeof(float2) + sizeof(float) * grid_weight_stride(W));
 }
-
-// Gridding of one plane batch.  The block owns one unit (a T x T tile over G
-// planes) per work item and keeps its cells in shared memory.  Warp k owns
-// rows 2k and 2k+1 of every plane, so a cell is only ever updated by one warp:
-// plain load-multiply-add-store, no atomics.  Each round stages up to
-// kGridRound visibility reads with their kernel values (evaluated once per
-// read); every warp scans the round and adds the part of each footprint that
-// falls on its two rows: lanes cover (footprint column, row of the pair,
-// plane parity) and step through the footprint's planes.  Columns are
-// XOR-swizzled by row parity so that the 64-bit accesses of a half-warp (two
-// rows x eight columns) fall on distinct banks.  A work item holds at most
-// kItemVis reads, which bounds the FP32 accumulation chain of every cell; the
-// tile is flushed to HBM once at the item's end.
 
 // Shared memory of the gridding kernels (see grid_smem_bytes).
 struct GridSmem {
-  float2 *cells;
-  float *m_re, *m_im;
-  int *m_iu, *m_iv, *m_ip;
-  float *wts;
+  float2 *cells;  // [G][halo plane]
+  int4 *meta;     // (iu_rel, iv_rel, ip_rel, -) per staged read
+  float2 *vis;    // weighted visibility per staged read
+  float *wts;     // [kGridRound][kw]
   uint32_t *rs0, *rcum;
 };
 
 template <int T, int G, int W>
 __device__ __forceinline__ GridSmem grid_smem(float4 *smem4, uint32_t *rs0, uint32_t *rcum) {
-  constexpr int kCells = T * T;
   GridSmem sm;
-  sm.cells = reinterpret_cast<float2 *>(smem4);  // [G][T][T], swizzled columns
-  sm.m_re = reinterpret_cast<float *>(sm.cells + G * kCells);
-  sm.m_im = sm.m_re + kGridRound;
-  sm.m_iu = reinterpret_cast<int *>(sm.m_im + kGridRound);
-  sm.m_iv = sm.m_iu + kGridRound;
-  sm.m_ip = sm.m_iv + kGridRound;
-  sm.wts = reinterpret_cast<float *>(sm.m_ip + kGridRound);  // [kGridRound][kWS]
+  sm.cells = reinterpret_cast<float2 *>(smem4);
+  sm.meta = reinterpret_cast<int4 *>(sm.cells + G * halo_plane(T, W));
+  sm.vis = reinterpret_cast<float2 *>(sm.meta + kGridRound);
+  sm.wts = reinterpret_cast<float *>(sm.vis + kGridRound);
   sm.rs0 = rs0;
   sm.rcum = rcum;
   return sm;
 }
 
-// One work item (descriptor d, item index `item` of its plane batch).  The
-// tile cells are zero on entry and on return; ends with a block barrier
-// unless the unit has no visibilities.
+// One gridding work item (descriptor d, item index `item` of its batch).  The
+// halo cells are zero on entry and on return; ends with a block barrier
+// unless the unit has no visibilities.  Reads are staged in rounds of
+// kGridRound with their kernel values (evaluated once per read by eight
+// threads); every warp then adds, for every read of the round, the footprint
+// row it owns (rows congruent to the warp index modulo 8): lanes cover
+// (footprint column, plane lane) and step through the footprint's planes.
 template <int T, int G, int W>
 __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__restrict__ rec,
                                           const uint32_t *__restrict__ off, int p_begin,
                                           int n_batch, const uint32_t *__restrict__ item_off,
+                                          const int *__restrict__ slots, float2 *__restrict__ spill,
                                           uint32_t d, uint32_t item,
                                           float2 *__restrict__ planes, const GridSmem &sm) {
-  constexpr int kCols = W <= 8 ? 8 : 16;            // lanes across footprint columns
-  constexpr int kPlaneLanes = 32 / (2 * kCols);     // 2 (W <= 8) or 1
+  constexpr int kCols = W <= 8 ? 8 : 16;          // lanes across footprint columns
+  constexpr int kPlaneLanes = 32 / kCols;         // 4 (W <= 8) or 2
   constexpr int kSteps = (W + kPlaneLanes - 1) / kPlaneLanes;
   constexpr int kWS = grid_weight_stride(W);
-  constexpr int kCells = T * T;
+  constexpr int R = halo_rows(T, W);
+  constexpr int PS = halo_plane(T, W);
+  constexpr int B = spill_cells(T, W);
   float2 *cells = sm.cells;
-  float *m_re = sm.m_re, *m_im = sm.m_im, *wts = sm.wts;
-  int *m_iu = sm.m_iu, *m_iv = sm.m_iv, *m_ip = sm.m_ip;
+  float *wts = sm.wts;
   uint32_t *rs0 = sm.rs0, *rcum = sm.rcum;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ci = lane % kCols;              // footprint column offset
-  const int row = 2 * warp + ((lane / kCols) & 1);
-  const int pj = lane / (2 * kCols);        // plane parity (W <= 8)
-  const int swz = (row & 1) << 3;
+  const int ci = lane % kCols;       // footprint column offset
+  const int pl = lane / kCols;       // plane lane
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
@@ -217,9 +226,9 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   const int q1 = min(q0 + G, p_begin + n_batch);
   const int nq = q1 - q0;
   if (d & 0x80000000u) {
-    // no visibility reaches this unit: its cells are zero
-    for (int c = threadIdx.x; c < nq * kCells; c += kThreads) {
-      const int pq = c / kCells, rem = c - pq * kCells;
+    // no visibility reaches this unit: its own cells are zero
+    for (int c = threadIdx.x; c < nq * T * T; c += kThreads) {
+      const int pq = c / (T * T), rem = c - pq * (T * T);
       const int rr = rem / T, cc = rem - rr * T;
       planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
              tu * T + cc] = make_float2(0.f, 0.f);
@@ -228,7 +237,7 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   }
   const uint32_t first = __ldg(item_off + unit);
   const uint32_t n_items = __ldg(item_off + unit + 1) - first;
-  if (threadIdx.x < 9) {
+  if (threadIdx.x < 4) {
     uint32_t a, b;
     unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
     rs0[threadIdx.x] = a;
@@ -237,11 +246,11 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   __syncthreads();
   if (threadIdx.x == 0) {
     rcum[0] = 0;
-    for (int r = 0; r < 9; ++r) rcum[r + 1] += rcum[r];
+    for (int r = 0; r < 4; ++r) rcum[r + 1] += rcum[r];
   }
   __syncthreads();
   const uint32_t lo = (item - first) * kItemVis;
-  const uint32_t hi = min(lo + kItemVis, rcum[9]);
+  const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
   for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
     // stage: eight threads share read t; roles 0-5 evaluate half of kx, ky
@@ -269,41 +278,35 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
                                    : es_eval(p.beta, (f + (float)k) * inv_half);
           }
         } else {
-          int iu_rel = v.iu - tu * T;
-          if (iu_rel >= T) iu_rel -= p.nu;
-          int iv_rel = v.iv - tv * T;
-          if (iv_rel >= T) iv_rel -= p.nv;
-          m_re[t] = v.re;
-          m_im[t] = v.im;
-          m_iu[t] = iu_rel;
-          m_iv[t] = iv_rel;
-          m_ip[t] = v.ip - q0;
+          // own-tile records: the corner lies in the tile (0 <= rel < T)
+          sm.meta[t] = make_int4(v.iu - tu * T, v.iv - tv * T, v.ip - q0, 0);
+          sm.vis[t] = make_float2(v.re, v.im);
         }
       }
     }
     __syncthreads();
     const int n_round = (int)min((uint32_t)kGridRound, hi - rb);
     for (int m = 0; m < n_round; ++m) {
-      const int ivr = m_iv[m];
-      if (ivr > 2 * warp + 1 || ivr + W <= 2 * warp) continue;  // uniform in the warp
-      const int col = m_iu[m] + ci;
-      const int dv = row - ivr;
-      if (ci < W && col >= 0 && col < T && dv >= 0 && dv < W) {
-        const float *w = wts + m * kWS;
-        const int ipr = m_ip[m];
-        const float re = m_re[m], im = m_im[m];
-        const float wuv = w[ci] * w[W + dv];
-        float2 *cb = cells + row * T + (col ^ swz);
+      const int4 mt = sm.meta[m];  // (iu_rel, iv_rel, ip_rel)
+      const float *w = wts + m * kWS;
+      const float2 vv = sm.vis[m];
+      const int col = mt.x + ci;
+      // footprint rows owned by this warp: dv = (warp - iv_rel) mod 8, + 8
+      for (int dv = (warp - mt.y) & 7; dv < W; dv += 8) {
+        if (ci < W) {
+          const float wuv = w[ci] * w[W + dv];
+          float2 *cb = cells + (mt.y + dv) * R + col;
 #pragma unroll
-        for (int s = 0; s < kSteps; ++s) {
-          const int dz = s * kPlaneLanes + pj;
-          const int q = ipr + dz;
-          if (dz < W && q >= 0 && q < nq) {
-            const float t = wuv * w[2 * W + dz];
-            float2 c = cb[q * kCells];
-            c.x = fmaf(t, re, c.x);
-            c.y = fmaf(t, im, c.y);
-            cb[q * kCells] = c;
+          for (int s = 0; s < kSteps; ++s) {
+            const int dz = s * kPlaneLanes + pl;
+            const int q = mt.z + dz;
+            if (dz < W && q >= 0 && q < nq) {
+              const float t = wuv * w[2 * W + dz];
+              float2 c = cb[q * PS];
+              c.x = fmaf(t, vv.x, c.x);
+              c.y = fmaf(t, vv.y, c.y);
+              cb[q * PS] = c;
+            }
           }
         }
       }
@@ -311,21 +314,26 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
     }
     __syncthreads();
   }
-  // flush the tile (a split unit adds into cells zeroed beforehand)
-  for (int c = threadIdx.x; c < G * kCells; c += kThreads) {
-    const int pq = c / kCells, rem = c - pq * kCells;
-    const int rr = rem / T, cc = rem - rr * T;
-    float2 *src = cells + pq * kCells + rr * T + (cc ^ ((rr & 1) << 3));
+  // flush: the tile's cells to the planes (a split unit adds into cells
+  // zeroed beforehand), the border cells to the unit's spill slot
+  const int slot = __ldg(slots + unit);
+  float2 *sp = spill + (size_t)slot * G * B;
+  for (int c = threadIdx.x; c < nq * R * R; c += kThreads) {
+    const int pq = c / (R * R), rem = c - pq * (R * R);
+    const int rr = rem / R, cc = rem - rr * R;
+    float2 *src = cells + pq * PS + rr * R + cc;
     const float2 val = *src;
     *src = make_float2(0.f, 0.f);
-    if (pq < nq) {
-      float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
-                    (size_t)(tv * T + rr) * p.nu + tu * T + cc;
-      if (n_items == 1)
-        *dst = val;
-      else
-        atomicAdd(dst, val);
-    }
+    float2 *dst;
+    if (rr < T && cc < T)
+      dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
+            tu * T + cc;
+    else
+      dst = sp + (size_t)pq * B + border_index(T, W, rr, cc);
+    if (n_items == 1)
+      *dst = val;
+    else
+      atomicAdd(dst, val);
   }
   __syncthreads();
 }
@@ -335,16 +343,18 @@ __global__ void __launch_bounds__(kThreads)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                 const uint32_t *__restrict__ off, int p_begin, int n_batch,
                 const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
+                const int *__restrict__ slots, float2 *__restrict__ spill,
                 uint32_t total, float2 *__restrict__ planes) {
-  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+  static_assert(kThreads == 256, "eight warps own the halo rows modulo 8");
   extern __shared__ float4 smem4[];
-  __shared__ uint32_t rs0[9], rcum[10];
+  __shared__ uint32_t rs0[4], rcum[5];
   const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
-  for (int c = threadIdx.x; c < G * T * T; c += kThreads) sm.cells[c] = make_float2(0.f, 0.f);
+  for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
+    sm.cells[c] = make_float2(0.f, 0.f);
   __syncthreads();
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x)
-    grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, __ldg(desc + item), item, planes,
-                       sm);
+    grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill,
+                       __ldg(desc + item), item, planes, sm);
 }
 
 // Several gridding jobs (facets x channel groups, each with its own plan,
@@ -355,13 +365,14 @@ template <int T, int G, int W>
 __global__ void __launch_bounds__(kThreads)
     grid_kernel_multi(const GridJob *__restrict__ jobs, const uint32_t *__restrict__ job_base,
                       int n_jobs, uint32_t total) {
-  static_assert(T == 16 && kThreads == 256, "eight warps own two tile rows each");
+  static_assert(kThreads == 256, "eight warps own the halo rows modulo 8");
   static_assert(sizeof(GridJob) % 8 == 0, "job copied in 8-byte words");
   extern __shared__ float4 smem4[];
-  __shared__ uint32_t rs0[9], rcum[10];
+  __shared__ uint32_t rs0[4], rcum[5];
   __shared__ GridJob job;
   const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
-  for (int c = threadIdx.x; c < G * T * T; c += kThreads) sm.cells[c] = make_float2(0.f, 0.f);
+  for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
+    sm.cells[c] = make_float2(0.f, 0.f);
   int cur = -1;
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     int lo = 0, hi = n_jobs - 1;  // last job whose base is <= item
@@ -378,8 +389,62 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     const uint32_t local = item - __ldg(job_base + lo);
-    grid_item<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off,
-                       __ldg(job.desc + local), local, job.planes, sm);
+    grid_item<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off, job.slot,
+                       job.spill, __ldg(job.desc + local), local, job.planes, sm);
+  }
+}
+
+// Fix-up after a gridding pass: every tile cell within W - 1 of the tile's
+// left or lower edge receives the border cells that its left, lower and
+// lower-left neighbours spilled (one block per unit, one thread per cell).
+__global__ void __launch_bounds__(kThreads)
+    spill_fixup_kernel(DevPlan p, int G, int p_begin, int n_batch, int n_units,
+                       const int *__restrict__ slots, const float2 *__restrict__ spill,
+                       float2 *__restrict__ planes) {
+  constexpr int T = kTile;
+  const int W = p.support, B = (W - 1) * (T + W - 1) + (W - 1) * T;
+  const int n_tiles = p.ntu * p.ntv;
+  const size_t plane_elems = (size_t)p.nu * p.nv;
+  for (int unit = blockIdx.x; unit < n_units; unit += gridDim.x) {
+    const int tile = unit % n_tiles, group = unit / n_tiles;
+    const int tu = tile % p.ntu, tv = tile / p.ntu;
+    const int q0 = p_begin + group * G;
+    const int nq = min(q0 + G, p_begin + n_batch) - q0;
+    const int tl = (tu + p.ntu - 1) % p.ntu, tb = (tv + p.ntv - 1) % p.ntv;
+    const int base = group * n_tiles;
+    const int s_left = __ldg(slots + base + tv * p.ntu + tl);
+    const int s_low = __ldg(slots + base + tb * p.ntu + tu);
+    const int s_diag = __ldg(slots + base + tb * p.ntu + tl);
+    if (s_left < 0 && s_low < 0 && s_diag < 0) continue;
+    for (int c = threadIdx.x; c < nq * T * T; c += blockDim.x) {
+      const int pq = c / (T * T), rem = c - pq * (T * T);
+      const int r = rem / T, col = rem - r * T;
+      const bool from_left = col < W - 1, from_low = r < W - 1;
+      if (!from_left && !from_low) continue;
+      float2 add = make_float2(0.f, 0.f);
+      if (from_left && s_left >= 0) {
+        const float2 v = __ldg(spill + ((size_t)s_left * G + pq) * B + border_index(T, W, r, col + T));
+        add.x += v.x;
+        add.y += v.y;
+      }
+      if (from_low && s_low >= 0) {
+        const float2 v = __ldg(spill + ((size_t)s_low * G + pq) * B + border_index(T, W, r + T, col));
+        add.x += v.x;
+        add.y += v.y;
+      }
+      if (from_left && from_low && s_diag >= 0) {
+        const float2 v =
+            __ldg(spill + ((size_t)s_diag * G + pq) * B + border_index(T, W, r + T, col + T));
+        add.x += v.x;
+        add.y += v.y;
+      }
+      float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
+                    (size_t)(tv * T + r) * p.nu + tu * T + col;
+      float2 g = *dst;
+      g.x += add.x;
+      g.y += add.y;
+      *dst = g;
+    }
   }
 }
 
@@ -531,11 +596,13 @@ int sm_count() {
 }
 
 // Zeroes the cells of the gridding units that are split into several items
-// (their items add into the planes); one warp per unit.
+// (their items add into the planes and into the unit's spill slot); one warp
+// per unit.
 template <int T, int G>
 __global__ void __launch_bounds__(kThreads)
     zero_split_units_kernel(DevPlan p, const uint32_t *__restrict__ item_off, int p_begin,
-                            int n_batch, int n_units, float2 *__restrict__ planes) {
+                            int n_batch, int n_units, const int *__restrict__ slots,
+                            float2 *__restrict__ spill, float2 *__restrict__ planes) {
   const int unit = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (unit >= n_units) return;
@@ -552,38 +619,62 @@ __global__ void __launch_bounds__(kThreads)
     planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + row) * p.nu +
            tu * T + col] = make_float2(0.f, 0.f);
   }
+  const int slot = slots[unit];
+  if (slot >= 0) {
+    const int B = (p.support - 1) * (T + p.support - 1) + (p.support - 1) * T;
+    float2 *sp = spill + (size_t)slot * G * B;
+    for (int c = lane; c < (q1 - q0) * B; c += 32) sp[c] = make_float2(0.f, 0.f);
+  }
 }
 
 // Plans the work items of one batch: scanned item offsets (n_units + 1) and
-// the item -> unit descriptors, in buffers from `alloc`.  The number of items
-// sizes the launch (one small device-to-host read).  With `planes` the split
-// gridding units are zeroed as well.
+// the item -> unit descriptors, in buffers from `alloc`; for gridding also the
+// units' spill slots and the spill buffer.  The numbers of items and slots
+// size the launches (one small device-to-host read).
 template <int T, int G>
 WorkItems plan_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
-                     bool degrid, float2 *planes, const ItemAlloc &alloc, cudaStream_t s) {
+                     bool degrid, const ItemAlloc &alloc, cudaStream_t s) {
   WorkItems wi;
   const int n_groups = (n_batch + G - 1) / G;
   wi.n_units = p.ntu * p.ntv * n_groups;
-  wi.item_off = (uint32_t *)alloc(0, sizeof(uint32_t) * (2 * (size_t)wi.n_units + 4));
+  // [item_off: n_units + 2][counts: n_units + 2][slots: n_units + 2]
+  const size_t words = 3 * ((size_t)wi.n_units + 2);
+  wi.item_off = (uint32_t *)alloc(0, sizeof(uint32_t) * words);
   uint32_t *counts = wi.item_off + wi.n_units + 2;
+  uint32_t *slots = counts + wi.n_units + 2;
   const int warps_per_block = kThreads / 32;
   const unsigned blocks = (unsigned)((wi.n_units + warps_per_block - 1) / warps_per_block);
   grid_plan_kernel<T, G><<<blocks, kThreads, 0, s>>>(p, off, p_begin, n_batch, wi.n_units,
-                                                     degrid ? 1 : 0, wi.item_off, counts,
-                                                     planes);
+                                                     degrid ? 1 : 0, wi.item_off, counts);
   check_launch("grid_plan_kernel");
   WGPU_CUDA(cudaMemsetAsync(wi.item_off + wi.n_units, 0, sizeof(uint32_t), s));
   uint32_t *tmp = (uint32_t *)alloc(2, sizeof(uint32_t) * exclusive_scan_scratch_words(wi.n_units + 1));
   exclusive_scan_u32_scratch(wi.item_off, wi.n_units + 1, tmp, s);
-  uint32_t total = 0;
-  WGPU_CUDA(cudaMemcpyAsync(&total, wi.item_off + wi.n_units, sizeof(uint32_t),
+  if (!degrid) {
+    slot_flags_kernel<<<(wi.n_units + 256) / 256, 256, 0, s>>>(counts, wi.n_units, slots);
+    check_launch("slot_flags_kernel");
+    exclusive_scan_u32_scratch(slots, wi.n_units + 1, tmp, s);
+  }
+  uint32_t totals[2] = {0, 0};
+  WGPU_CUDA(cudaMemcpyAsync(&totals[0], wi.item_off + wi.n_units, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
+  if (!degrid)
+    WGPU_CUDA(cudaMemcpyAsync(&totals[1], slots + wi.n_units, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
-  wi.total = total;
-  wi.desc = (uint32_t *)alloc(1, sizeof(uint32_t) * ((size_t)total + 1));
+  wi.total = totals[0];
+  wi.desc = (uint32_t *)alloc(1, sizeof(uint32_t) * ((size_t)wi.total + 1));
   fill_items_kernel<<<(wi.n_units + 255) / 256, 256, 0, s>>>(wi.item_off, counts, wi.n_units,
                                                               wi.desc);
   check_launch("fill_items_kernel");
+  if (!degrid) {
+    slot_final_kernel<<<(wi.n_units + 255) / 256, 256, 0, s>>>(counts, wi.n_units, (int *)slots);
+    check_launch("slot_final_kernel");
+    wi.slot = (int *)slots;
+    wi.n_slots = (int)totals[1];
+    const size_t B = (size_t)spill_cells(T, p.support);
+    wi.spill = (float2 *)alloc(3, sizeof(float2) * ((size_t)wi.n_slots * G * B + 1));
+  }
   return wi;
 }
 
@@ -598,7 +689,8 @@ void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int
                                                           kThreads, smem));
   const uint32_t blocks = std::min<uint32_t>(wi.total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
   grid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch,
-                                                      wi.item_off, wi.desc, wi.total, planes);
+                                                      wi.item_off, wi.desc, wi.slot, wi.spill,
+                                                      wi.total, planes);
   check_launch("grid_kernel");
 }
 
@@ -633,21 +725,21 @@ void grid_items_multi(const GridJob *d_jobs, const uint32_t *d_base, int n_jobs,
   check_launch("grid_kernel_multi");
 }
 
-template <int T, int G, int W = 4>
+template <int T, int W = 4>
 void grid_multi_dispatch(int support, const GridJob *d_jobs, const uint32_t *d_base, int n_jobs,
                          uint32_t total, cudaStream_t s) {
   if constexpr (W > kMaxSupport) {
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
-      grid_items_multi<T, G, W>(d_jobs, d_base, n_jobs, total, s);
+      grid_items_multi<T, grid_group(W), W>(d_jobs, d_base, n_jobs, total, s);
     else
-      grid_multi_dispatch<T, G, W + 1>(support, d_jobs, d_base, n_jobs, total, s);
+      grid_multi_dispatch<T, W + 1>(support, d_jobs, d_base, n_jobs, total, s);
   }
 }
 
-// Dispatch over the kernel support (4..16).
-template <int T, int G, int W = 4>
+// Dispatch over the kernel support (4..16); the plane group follows W.
+template <int T, int W = 4>
 void grid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                    int p_begin, int n_batch, const WorkItems &wi, float2 *planes,
                    cudaStream_t s) {
@@ -655,9 +747,9 @@ void grid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const ui
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
-      grid_items<T, G, W>(p, rec, off, p_begin, n_batch, wi, planes, s);
+      grid_items<T, grid_group(W), W>(p, rec, off, p_begin, n_batch, wi, planes, s);
     else
-      grid_dispatch<T, G, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, s);
+      grid_dispatch<T, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, s);
   }
 }
 
@@ -691,51 +783,72 @@ constexpr int kDegridPlanes = 8;
 int grid_plane_group() { return kGridPlanes; }
 
 WorkItems plan_grid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
-                          float2 *planes, const ItemAlloc &alloc, cudaStream_t s) {
+                          const ItemAlloc &alloc, cudaStream_t s) {
   check_plan(p);
-  return plan_items<kTile, kGridPlanes>(p, off, p_begin, n_batch, false, planes, alloc, s);
+  if (p.support <= 8)
+    return plan_items<kTile, grid_group(8)>(p, off, p_begin, n_batch, false, alloc, s);
+  return plan_items<kTile, grid_group(16)>(p, off, p_begin, n_batch, false, alloc, s);
 }
 
 WorkItems plan_degrid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
                             const ItemAlloc &alloc, cudaStream_t s) {
   check_plan(p);
-  return plan_items<kTile, kDegridPlanes>(p, off, p_begin, n_batch, true, nullptr, alloc, s);
+  return plan_items<kTile, kDegridPlanes>(p, off, p_begin, n_batch, true, alloc, s);
 }
 
 void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
                              float2 *planes, cudaStream_t s) {
   const int warps_per_block = kThreads / 32;
   const unsigned blocks = (unsigned)((wi.n_units + warps_per_block - 1) / warps_per_block);
-  zero_split_units_kernel<kTile, kGridPlanes><<<blocks, kThreads, 0, s>>>(
-      p, wi.item_off, p_begin, n_batch, wi.n_units, planes);
+  if (p.support <= 8)
+    zero_split_units_kernel<kTile, grid_group(8)><<<blocks, kThreads, 0, s>>>(
+        p, wi.item_off, p_begin, n_batch, wi.n_units, wi.slot, wi.spill, planes);
+  else
+    zero_split_units_kernel<kTile, grid_group(16)><<<blocks, kThreads, 0, s>>>(
+        p, wi.item_off, p_begin, n_batch, wi.n_units, wi.slot, wi.spill, planes);
   check_launch("zero_split_units_kernel");
+}
+
+size_t grid_spill_elems(const DevPlan &p, const WorkItems &wi) {
+  const int G = p.support <= 8 ? grid_group(8) : grid_group(16);
+  return (size_t)wi.n_slots * G * spill_cells(kTile, p.support);
+}
+
+void launch_spill_fixup(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
+                        float2 *planes, cudaStream_t s) {
+  if (wi.n_slots == 0 || p.support < 2) return;
+  const int G = p.support <= 8 ? grid_group(8) : grid_group(16);
+  const unsigned blocks = (unsigned)std::min<int64_t>(wi.n_units, (int64_t)sm_count() * 8);
+  spill_fixup_kernel<<<blocks, kThreads, 0, s>>>(p, G, p_begin, n_batch, wi.n_units, wi.slot,
+                                                  wi.spill, planes);
+  check_launch("spill_fixup_kernel");
 }
 
 void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
                        int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
   check_plan(p);
-  grid_dispatch<kTile, kGridPlanes>(p.support, p, rec, off, p_begin, n_batch, wi, planes, s);
+  grid_dispatch<kTile>(p.support, p, rec, off, p_begin, n_batch, wi, planes, s);
+  launch_spill_fixup(p, wi, p_begin, n_batch, planes, s);
 }
 
-template <int T, int G, int W = 4>
+template <int T, int W = 4>
 void grid_multi_prepare(int support) {
   if constexpr (W <= kMaxSupport) {
     if (support == W)
-      ensure_dynamic_smem((const void *)grid_kernel_multi<T, G, W>, grid_smem_bytes<T, G, W>());
+      ensure_dynamic_smem((const void *)grid_kernel_multi<T, grid_group(W), W>,
+                          grid_smem_bytes<T, grid_group(W), W>());
     else
-      grid_multi_prepare<T, G, W + 1>(support);
+      grid_multi_prepare<T, W + 1>(support);
   }
 }
 
-void prepare_grid_items_multi(int support) {
-  grid_multi_prepare<kTile, kGridPlanes>(support);
-}
+void prepare_grid_items_multi(int support) { grid_multi_prepare<kTile>(support); }
 
 void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
                              int n_jobs, uint32_t total, cudaStream_t s) {
   if (support < 4 || support > kMaxSupport)
     throw Error(WGPU_ERR_INVALID, "kernel support must be 4..16");
-  grid_multi_dispatch<kTile, kGridPlanes>(support, d_jobs, d_base, n_jobs, total, s);
+  grid_multi_dispatch<kTile>(support, d_jobs, d_base, n_jobs, total, s);
 }
 
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
@@ -748,7 +861,10 @@ void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t 
 
 static ItemAlloc arena_alloc(DeviceArena &arena) {
   return [&arena](int which, size_t bytes) -> void * {
-    const int slot = which == 0 ? kSlotItems : which == 1 ? kSlotItemDesc : kSlotScanTmp;
+    const int slot = which == 0   ? kSlotItems
+                     : which == 1 ? kSlotItemDesc
+                     : which == 2 ? kSlotScanTmp
+                                  : kSlotSpill;
     return arena.get(slot, bytes);
   };
 }
@@ -756,7 +872,8 @@ static ItemAlloc arena_alloc(DeviceArena &arena) {
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s) {
-  const WorkItems wi = plan_grid_items(p, off, p_begin, n_batch, planes, arena_alloc(arena), s);
+  const WorkItems wi = plan_grid_items(p, off, p_begin, n_batch, arena_alloc(arena), s);
+  launch_zero_split_units(p, wi, p_begin, n_batch, planes, s);
   launch_grid_items(p, rec, off, p_begin, n_batch, wi, planes, s);
 }
 

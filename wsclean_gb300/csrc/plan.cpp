@@ -248,8 +248,12 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
   }
   // Planes resident per pipeline step.
   const int64_t rstride = (best.width + 31) / 32 * 32;
-  const double per_plane = 8.0 * best.nu * best.nv + 8.0 * best.nv * rstride;
-  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 40e9;
+  // plane + cropped rows + the gridding units' spilled border cells (at most
+  // (W - 1)(2T + W - 1) cells per T x T tile)
+  const double spill = (double)(best.support - 1) * (2.0 * best.tile + best.support - 1) /
+                       ((double)best.tile * best.tile);
+  const double per_plane = 8.0 * best.nu * best.nv * (1.0 + spill) + 8.0 * best.nv * rstride;
+  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 64e9;
   int64_t batch = (int64_t)std::floor(budget / per_plane);
   int64_t cap = req.max_plane_batch > 0 ? req.max_plane_batch : 32;
   batch = std::max<int64_t>(1, std::min<int64_t>(std::min(batch, cap), best.n_planes));

@@ -86,7 +86,9 @@ double estimate_bytes(const wgpu_request_t &r, double plane_budget) {
   q.memory_budget_bytes = plane_budget;
   const wgpu_plan_t p = wgpu::make_plan(q);
   const double n = (double)r.n_rows * (double)r.n_chan;
-  const double planes = (double)p.plane_batch * 8.0 * (double)p.nu * (double)p.nv;
+  const double spill = (double)(p.support - 1) * (2.0 * p.tile + p.support - 1) /
+                       ((double)p.tile * p.tile);
+  const double planes = (double)p.plane_batch * 8.0 * (double)p.nu * (double)p.nv * (1.0 + spill);
   const double rows = (double)p.plane_batch * 8.0 * (double)p.nv * (double)((p.width + 31) / 32 * 32);
   const double img = 24.0 * (double)r.width * (double)r.height;
   const double keys = 4.0 * (double)(p.nu / p.tile) * (double)(p.nv / p.tile) * 4.0 * (double)p.n_planes;

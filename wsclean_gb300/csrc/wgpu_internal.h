@@ -72,6 +72,8 @@ struct GridJob {
   const uint32_t *off;
   const uint32_t *item_off;
   const uint32_t *desc;
+  const int *slot;
+  float2 *spill;
   float2 *planes;
   int p_begin, n_batch;
 };
@@ -131,12 +133,17 @@ struct WorkItems {
   uint32_t *desc = nullptr;
   uint32_t total = 0;
   int n_units = 0;
+  // gridding only: spill slot of each unit (-1 for a unit without
+  // visibilities) and the slots' border cells
+  int *slot = nullptr;
+  float2 *spill = nullptr;
+  int n_slots = 0;
 };
-// Buffer provider for planning: which = 0 item offsets, 1 descriptors, 2 scan
-// scratch.
+// Buffer provider for planning: which = 0 item offsets (and unit tables),
+// 1 descriptors, 2 scan scratch, 3 spill slots.
 using ItemAlloc = std::function<void *(int which, size_t bytes)>;
 WorkItems plan_grid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
-                          float2 *planes, const ItemAlloc &alloc, cudaStream_t s);
+                          const ItemAlloc &alloc, cudaStream_t s);
 WorkItems plan_degrid_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_batch,
                             const ItemAlloc &alloc, cudaStream_t s);
 void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
@@ -145,6 +152,13 @@ void launch_grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *o
                        int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s);
 // All jobs' items in one persistent launch (items of job j start at
 // d_base[j]); every job has kernel support `support`.
+// float2 elements of a gridding batch's spill slots (an allocator that
+// returns null for `which` 3 leaves WorkItems::spill for the caller to set).
+size_t grid_spill_elems(const DevPlan &p, const WorkItems &wi);
+// Adds the units' spilled border cells into the neighbouring tiles' cells;
+// runs after the gridding of a plane batch (launch_grid_items does it).
+void launch_spill_fixup(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
+                        float2 *planes, cudaStream_t s);
 // Sets the multi-job kernel's shared-memory cap (before a graph capture).
 void prepare_grid_items_multi(int support);
 void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
@@ -274,6 +288,7 @@ enum ArenaSlot {
   kSlotItems,
   kSlotCounter,
   kSlotItemDesc,
+  kSlotSpill,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
