@@ -151,6 +151,7 @@ struct BoundState {
   uint8_t *mask = nullptr;
   wgpu::VisRecord *geom = nullptr, *work = nullptr;
   uint32_t *perm = nullptr, *offsets = nullptr;
+  wgpu::RowOccupancy rows_occ;  // rows the bound set's footprints touch
   float2 *vis_in = nullptr, *vis_out = nullptr, *vacc = nullptr;
   float2 *planes = nullptr, *rows = nullptr, *acc = nullptr;
   float *img_corr = nullptr, *cx = nullptr, *cy = nullptr, *gl = nullptr;
@@ -354,12 +355,14 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     g->timer.mark("grid");
     launch_grid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, s);
     g->timer.mark("fft_rows");
-    launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, g->d_flags, s);
+    const RowSel sel = row_sel(b.rows, (int)p0);
+    launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, sel, g->d_flags, s);
     g->timer.mark("fft_cols_a");
-    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, -1.0f, s);
+    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, -1.0f,
+                      sel, s);
     g->timer.mark("fft_cols_b_screen");
     launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R,
-                                         rstride, nb, (int)p0, nu_w, acc, s);
+                                         rstride, nb, (int)p0, nu_w, acc, sel, s);
     if (g->verbosity >= 2)
       std::fprintf(stderr, "wgpu invert: planes %lld..%lld\n", (long long)p0,
                    (long long)(p0 + nb - 1));
@@ -418,9 +421,11 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
                                       img_corr, nu_w, R, rstride, nb, (int)p0, s);
     g->timer.mark("fft_cols_a");
-    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, +1.0f, s);
+    const RowSel sel = row_sel(b.rows, (int)p0);
+    launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, +1.0f,
+                      sel, s);
     g->timer.mark("fft_rows");
-    launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, g->d_flags, s);
+    launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, sel, g->d_flags, s);
     g->timer.mark("degrid");
     launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
   }
@@ -473,6 +478,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                             cudaMemcpyDeviceToDevice, s));
   WGPU_CUDA(cudaMemcpyAsync(b->offsets, br.offsets, sizeof(uint32_t) * (br.n_keys + 1),
                             cudaMemcpyDeviceToDevice, s));
+  b->rows_occ = copy_row_occupancy(br.rows, b->alloc(br.rows.bytes()), s);
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
   const int64_t B = plan.plane_batch;
@@ -519,11 +525,13 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
       launch_zero_split_units(dp, b->gitems[i], p0, nb, b->planes, s);
       launch_grid_items(dp, b->work, b->offsets, p0, nb, b->gitems[i], b->planes, s);
-      launch_fft_rows_forward_crop(*g->fft, dp, b->planes, b->rows, rstride, nb, g->d_flags, s);
+      const RowSel sel = row_sel(b->rows_occ, p0);
+      launch_fft_rows_forward_crop(*g->fft, dp, b->planes, b->rows, rstride, nb, sel, g->d_flags,
+                                   s);
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
-                        -1.0f, s);
+                        -1.0f, sel, s);
       launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                           b->rows, rstride, nb, p0, b->nu_w, b->acc, s);
+                                           b->rows, rstride, nb, p0, b->nu_w, b->acc, sel, s);
     }
     launch_finalize_add(dp, b->acc, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, g->d_img, g->prec, s);
   } catch (...) {
@@ -548,9 +556,11 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
       launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
                                         b->img_corr, b->nu_w, b->rows, rstride, nb, p0, s);
+      const RowSel sel = row_sel(b->rows_occ, p0);
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
-                        +1.0f, s);
-      launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, g->d_flags, s);
+                        +1.0f, sel, s);
+      launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, sel, g->d_flags,
+                                   s);
       launch_degrid_items(dp, b->geom, b->offsets, p0, nb, b->ditems[i], b->planes, b->vacc, s);
     }
     WGPU_CUDA(cudaMemsetAsync(b->vis_out, 0, sizeof(float2) * n, s));

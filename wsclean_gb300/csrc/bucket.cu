@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(kThreads)
     key_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
                Selector sel, int64_t n_rows, int64_t n_chan,
                uint32_t sentinel, uint32_t *keys,
-               uint32_t *vals, uint32_t *counts) {
+               uint32_t *vals, uint32_t *counts, uint8_t *corners) {
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(kThreads)
   if (sel(e)) {
     const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
     key = f.key;
+    if (corners) corners[(size_t)f.ip * p.nv + f.iv] = 1;
   }
   keys[e] = key;
   vals[e] = (uint32_t)e;
@@ -311,6 +312,93 @@ __global__ void __launch_bounds__(kThreads)
       make_float4(o.fw, __int_as_float(o.iu), __int_as_float(o.iv), __int_as_float(o.ip));
 }
 
+// ---------------- row occupancy ----------------------------------------------
+constexpr int kOccThreads = 1024;
+
+// Plane q's rows covered by a footprint: a footprint with corner (ip, iv)
+// covers planes ip .. ip + W - 1 and rows iv .. iv + W - 1 (cyclically), so
+// row r of plane q is covered when a corner lies on one of the planes
+// q - W + 1 .. q and rows r - W + 1 .. r.  One block per plane.
+__global__ void __launch_bounds__(kOccThreads)
+    row_flags_kernel(const uint8_t *__restrict__ corners, int nv, int W,
+                     uint8_t *__restrict__ flags, uint32_t *__restrict__ counts) {
+  extern __shared__ uint8_t any_plane[];  // [nv]: corners of planes q - W + 1 .. q
+  __shared__ uint32_t total;
+  const int q = blockIdx.x;
+  if (threadIdx.x == 0) total = 0;
+  for (int r = threadIdx.x; r < nv; r += blockDim.x) {
+    uint8_t a = 0;
+    for (int k = 0; k < W && k <= q; ++k) a |= corners[(size_t)(q - k) * nv + r];
+    any_plane[r] = a;
+  }
+  __syncthreads();
+  uint32_t cnt = 0;
+  for (int r = threadIdx.x; r < nv; r += blockDim.x) {
+    uint8_t f = 0;
+    for (int k = 0; k < W; ++k) {
+      int rr = r - k;
+      while (rr < 0) rr += nv;
+      f |= any_plane[rr];
+    }
+    flags[(size_t)q * nv + r] = f ? 1 : 0;
+    cnt += f ? 1u : 0u;
+  }
+  if (cnt) atomicAdd(&total, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[q] = total;
+}
+
+// Compacts plane q's flagged rows into list[start[q] ..], in row order;
+// start[q] is the sum of the earlier planes' counts.  One block per plane.
+__global__ void __launch_bounds__(kOccThreads)
+    row_list_kernel(const uint8_t *__restrict__ flags, const uint32_t *__restrict__ counts,
+                    int n_planes, int nv, uint32_t *__restrict__ start,
+                    uint32_t *__restrict__ list) {
+  __shared__ uint32_t s_base;
+  __shared__ uint32_t warp_tot[kOccThreads / 32];
+  const int q = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  uint32_t part = 0;
+  for (int k = threadIdx.x; k < q; k += blockDim.x) part += counts[k];
+  if (part) atomicAdd(&s_base, part);
+  __syncthreads();
+  uint32_t base = s_base;
+  if (threadIdx.x == 0) {
+    start[q] = base;
+    if (q == n_planes - 1) start[n_planes] = base + counts[q];
+  }
+  for (int r0 = 0; r0 < nv; r0 += blockDim.x) {
+    const int r = r0 + threadIdx.x;
+    const bool f = r < nv && flags[(size_t)q * nv + r] != 0;
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) warp_tot[warp] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (int w = 0; w < n_warps; ++w) {
+      const uint32_t t = warp_tot[w];
+      before += w < warp ? t : 0u;
+      all += t;
+    }
+    if (f) list[base + before + __popc(m & ((1u << lane) - 1u))] = (uint32_t)q * (uint32_t)nv + r;
+    base += all;
+    __syncthreads();
+  }
+}
+
+// Flags, counts, starts and the row list from the corners key_kernel marked.
+void build_row_occupancy(const RowOccupancy &o, int W, cudaStream_t s) {
+  if (o.n_planes == 0) return;
+  ensure_dynamic_smem((const void *)row_flags_kernel, (size_t)o.nv);
+  row_flags_kernel<<<o.n_planes, kOccThreads, o.nv, s>>>(o.corners(), o.nv, W, o.flags(),
+                                                          o.counts());
+  check_launch("row_flags_kernel");
+  row_list_kernel<<<o.n_planes, kOccThreads, 0, s>>>(o.flags(), o.counts(), o.n_planes, o.nv,
+                                                      o.start(), o.list());
+  check_launch("row_list_kernel");
+}
+
 unsigned grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -318,6 +406,14 @@ unsigned grid_for(int64_t n, int threads) {
 }
 
 }  // namespace
+
+RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_t s) {
+  RowOccupancy o = rows;
+  if (!rows.buf) return o;
+  o.buf = (uint8_t *)dst;
+  WGPU_CUDA(cudaMemcpyAsync(o.buf, rows.buf, rows.bytes(), cudaMemcpyDeviceToDevice, s));
+  return o;
+}
 
 void compute_w_extent(const double *d_uvw, const double *d_freq,
                       const float *d_vis, const uint8_t *d_mask, int64_t n_rows,
@@ -376,12 +472,19 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   channel_scales_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, n_chan, gu, gv, cs);
   check_launch("channel_scales_kernel");
   WGPU_CUDA(cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (res.n_keys + 1), s));
+  if ((uint64_t)p.n_planes * (uint64_t)p.nv >= 0xFFFFFFFFull)
+    throw Error(WGPU_ERR_INVALID, "too many (plane, row) pairs");
+  res.rows.n_planes = p.n_planes;
+  res.rows.nv = p.nv;
+  res.rows.buf = (uint8_t *)arena.get(kSlotRowOcc, RowOccupancy{nullptr, p.n_planes, p.nv}.bytes());
+  WGPU_CUDA(cudaMemsetAsync(res.rows.corners(), 0, res.rows.cells(), s));
   if (n > 0) {
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
-        n_rows, n_chan, sentinel, keys, vals, offsets);
+        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners());
     check_launch("key_kernel");
   }
+  build_row_occupancy(res.rows, p.support, s);
   exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
 
   // radix sort over the key bits in use
@@ -514,7 +617,7 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
   if (n > 0) {
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, nullptr}, n_rows,
-        n_chan, sentinel, keys, vals, d_offsets);
+        n_chan, sentinel, keys, vals, d_offsets, nullptr);
     check_launch("key_kernel");
   }
   exclusive_scan_u32_scratch(d_offsets, n_keys + 1, scan_tmp, s);

@@ -60,6 +60,7 @@ struct Job {
   int64_t n_keys = 0;
   VisRecord *geom = nullptr, *work = nullptr;
   uint32_t *perm = nullptr, *offsets = nullptr;
+  RowOccupancy rows_occ;  // plane rows the job's footprints touch
   float2 *acc = nullptr;
   double *nu_w = nullptr;
   float *cx = nullptr, *cy = nullptr, *gl = nullptr;
@@ -242,6 +243,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
                               cudaMemcpyDeviceToDevice, s));
     WGPU_CUDA(cudaMemcpyAsync(j.offsets, br.offsets, sizeof(uint32_t) * (br.n_keys + 1),
                               cudaMemcpyDeviceToDevice, s));
+    j.rows_occ = copy_row_occupancy(br.rows, f->alloc(br.rows.bytes()), s);
     const int64_t npix = j.plan.width * j.plan.height;
     j.acc = (float2 *)f->alloc(sizeof(float2) * npix);
     j.nu_w = (double *)f->alloc(sizeof(double) * npix);
@@ -387,12 +389,14 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
         cudaStream_t ss = f->side[sl.job % wgpu_facets::kSide];
         float2 *planes = f->pool + sl.planes_off, *rows = f->pool + sl.rows_off;
         launch_spill_fixup(j.dp, j.items[sl.batch], sl.p0, sl.nb, planes, ss);
-        launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, f->d_flags, ss);
+        const RowSel sel = row_sel(j.rows_occ, sl.p0);
+        launch_fft_rows_forward_crop(*f->fft, j.dp, planes, rows, j.rstride, sl.nb, sel,
+                                     f->d_flags, ss);
         launch_fft_cols_a(*f->fft, j.dp, (int)j.plan.fft_n1, (int)j.plan.fft_n2, rows, j.rstride,
-                          sl.nb, -1.0f, ss);
+                          sl.nb, -1.0f, sel, ss);
         launch_fft_cols_b_forward_accumulate(*f->fft, j.dp, (int)j.plan.fft_n1,
                                              (int)j.plan.fft_n2, rows, j.rstride, sl.nb, sl.p0,
-                                             j.nu_w, j.acc, ss);
+                                             j.nu_w, j.acc, sel, ss);
       }
       for (int k = 0; k < wgpu_facets::kSide; ++k) {
         WGPU_CUDA(cudaEventRecord(f->ev_side[k], f->side[k]));

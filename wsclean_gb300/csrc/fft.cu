@@ -487,12 +487,23 @@ constexpr int kRowThreadsMax = kFftMaxRow / 16;  // 768: one radix-16 butterfly 
 // !FWD: rows of R (width valid entries) -> zero padding, re-centring ->
 //      backward FFT -> plane rows.  buf_elems >= max(L, in_stride); in_bytes
 // is the size of one input row.
+// Number of rows a row launch transforms, and the batch row index of its
+// item idx (see RowSel).
+__device__ __forceinline__ int sel_rows(const RowSel &sel, int n_batch, int nv) {
+  return sel.list ? (int)(__ldg(sel.start + n_batch) - __ldg(sel.start)) : n_batch * nv;
+}
+__device__ __forceinline__ int sel_row(const RowSel &sel, int idx, int nv) {
+  return sel.list ? (int)(__ldg(sel.list + __ldg(sel.start) + idx) - (uint32_t)sel.p_begin * nv)
+                  : idx;
+}
+
 template <bool FWD, int LAST, bool MID8>
 __global__ void __launch_bounds__(kRowThreadsMax, 1)
     fft_rows_persistent_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
                                const float2 *__restrict__ in, int in_stride, uint32_t in_bytes,
-                               float2 *__restrict__ out, int out_stride, int n_rows, int width,
-                               int buf_elems, int mid_tab, unsigned *__restrict__ err) {
+                               float2 *__restrict__ out, int out_stride, int n_batch, int nv,
+                               RowSel sel, int width, int buf_elems, int mid_tab,
+                               unsigned *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char row_smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(row_smem);  // two mbarriers
   float2 *bufs = reinterpret_cast<float2 *>(row_smem + 128);
@@ -510,20 +521,22 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
   }
   for (int i = threadIdx.x; i < mid_tab; i += blockDim.x) tab[i] = __ldg(tws + st.tw_off[1] + i);
   __syncthreads();
-  int row = blockIdx.x;
-  if (threadIdx.x == 0) {
+  const int n_items = sel_rows(sel, n_batch, nv);
+  int item = blockIdx.x;
+  if (threadIdx.x == 0 && item < n_items) {
     mbar_expect_tx(&bar[0], in_bytes);
-    bulk_copy_g2s(bufs, in + (size_t)row * in_stride, in_bytes, &bar[0]);
+    bulk_copy_g2s(bufs, in + (size_t)sel_row(sel, item, nv) * in_stride, in_bytes, &bar[0]);
   }
   uint32_t phase0 = 0, phase1 = 0;
-  for (int it = 0; row < n_rows; ++it, row += G) {
+  for (int it = 0; item < n_items; ++it, item += G) {
     const int b = it & 1;
     float2 *buf = bufs + (size_t)b * buf_elems;
-    const int next = row + G;
-    if (next < n_rows && threadIdx.x == 0) {
+    const int row = sel_row(sel, item, nv);
+    const int next = item + G;
+    if (next < n_items && threadIdx.x == 0) {
       mbar_expect_tx(&bar[b ^ 1], in_bytes);
-      bulk_copy_g2s(bufs + (size_t)(b ^ 1) * buf_elems, in + (size_t)next * in_stride, in_bytes,
-                    &bar[b ^ 1]);
+      bulk_copy_g2s(bufs + (size_t)(b ^ 1) * buf_elems,
+                    in + (size_t)sel_row(sel, next, nv) * in_stride, in_bytes, &bar[b ^ 1]);
     }
     const bool ok = mbar_wait_bounded(&bar[b], b == 0 ? phase0 : phase1);
     if (__syncthreads_or(!ok)) {
@@ -531,7 +544,7 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
       // for the copies still in flight, and leave
       if (threadIdx.x == 0) atomicAdd(err, 1u);
       mbar_wait_bounded(&bar[b], b == 0 ? phase0 : phase1);
-      if (next < n_rows) mbar_wait_bounded(&bar[b ^ 1], b == 0 ? phase1 : phase0);
+      if (next < n_items) mbar_wait_bounded(&bar[b ^ 1], b == 0 ? phase1 : phase0);
       return;
     }
     if (b == 0) phase0 ^= 1; else phase1 ^= 1;
@@ -581,11 +594,13 @@ template <bool FWD>
 __global__ void __launch_bounds__(kRowPingPongMax / 16, 2)
     fft_rows_pingpong_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
                              const float2 *__restrict__ in, int in_stride,
-                             float2 *__restrict__ out, int out_stride, int width) {
+                             float2 *__restrict__ out, int out_stride, int n_batch, int nv,
+                             RowSel sel, int width) {
   extern __shared__ float2 s[];
   const int L = d.L;
   const float sign = FWD ? -1.0f : 1.0f;
-  const size_t row = blockIdx.x;
+  if ((int)blockIdx.x >= sel_rows(sel, n_batch, nv)) return;  // whole block
+  const size_t row = (size_t)sel_row(sel, blockIdx.x, nv);
   float2 *buf0 = s, *buf1 = s + row_buffer(L);
   if (FWD) {
     const float4 *src = reinterpret_cast<const float4 *>(in + row * in_stride);
@@ -629,8 +644,12 @@ constexpr int kPanel = 32;  // columns per panel
 // Loads a panel of n_rows x kPanel elements (row r at src + r * row_stride)
 // into shared memory, issuing all of a thread's loads before the stores so
 // that enough bytes are in flight to cover the HBM latency.
+// With row_flags, panel row r is read only where row_flags[r * flag_stride]
+// is set and is zero elsewhere.
 __device__ __forceinline__ void load_panel(float2 *__restrict__ s, const float2 *__restrict__ src,
-                                           size_t row_stride, int n_rows) {
+                                           size_t row_stride, int n_rows,
+                                           const uint8_t *__restrict__ row_flags = nullptr,
+                                           int flag_stride = 0) {
   constexpr int kBatch = 8;  // loads in flight per thread
   const int n_el = n_rows * kPanel;
   for (int e0 = threadIdx.x; e0 < n_el; e0 += kBatch * blockDim.x) {
@@ -638,7 +657,12 @@ __device__ __forceinline__ void load_panel(float2 *__restrict__ s, const float2 
 #pragma unroll
     for (int k = 0; k < kBatch; ++k) {
       const int e = e0 + k * blockDim.x;
-      if (e < n_el) tmp[k] = __ldg(src + (size_t)(e / kPanel) * row_stride + (e % kPanel));
+      if (e < n_el) {
+        const int r = e / kPanel;
+        tmp[k] = (!row_flags || __ldg(row_flags + (size_t)r * flag_stride))
+                     ? __ldg(src + (size_t)r * row_stride + (e % kPanel))
+                     : make_float2(0.f, 0.f);
+      }
     }
 #pragma unroll
     for (int k = 0; k < kBatch; ++k) {
@@ -652,12 +676,18 @@ __device__ __forceinline__ void load_panel(float2 *__restrict__ s, const float2 
 __global__ void __launch_bounds__(kColThreads, 3)
     fft_cols_pass_a_kernel(FftDesc d1, float2 *__restrict__ R, int rstride, int nv,
                            int n2, float sign, const float2 *__restrict__ tw1,
-                           const float2 *__restrict__ twN) {
+                           const float2 *__restrict__ twN, const uint8_t *__restrict__ flags) {
   extern __shared__ float2 s[];
   const int n1 = d1.L;
   const int cg = blockIdx.x, r2 = blockIdx.y;
   float2 *base = R + (size_t)blockIdx.z * nv * rstride + cg * kPanel;
-  load_panel(s, base + (size_t)r2 * rstride, (size_t)n2 * rstride, n1);
+  // flags of this plane's rows (null: every row carries data)
+  const uint8_t *fl = flags ? flags + (size_t)blockIdx.z * nv : nullptr;
+  if (sign < 0)
+    load_panel(s, base + (size_t)r2 * rstride, (size_t)n2 * rstride, n1, fl ? fl + r2 : nullptr,
+               n2);
+  else
+    load_panel(s, base + (size_t)r2 * rstride, (size_t)n2 * rstride, n1);
   __syncthreads();
   // backward: this pass runs last and the twiddle was applied in pass B'
   const float2 *res = fft_smem<kPanelLayout>(s, s + n1 * kPanel, d1, sign, tw1);
@@ -665,7 +695,8 @@ __global__ void __launch_bounds__(kColThreads, 3)
     const int k1 = e / kPanel, c = e % kPanel;
     float2 v = res[e];
     if (sign < 0) v = cmul(v, __ldg(twN + (int)(((long long)r2 * k1) % nv)));
-    base[(size_t)(r2 + n2 * k1) * rstride + c] = v;
+    // backward: rows no visibility reads are not written
+    if (sign < 0 || !fl || __ldg(fl + r2 + n2 * k1)) base[(size_t)(r2 + n2 * k1) * rstride + c] = v;
   }
 }
 
@@ -736,7 +767,8 @@ __global__ void __launch_bounds__(kColThreads, 2)
                                        int n_batch, int p_begin,
                                        const double *__restrict__ nu_w,
                                        float2 *__restrict__ acc,
-                                       const float2 *__restrict__ tw2) {
+                                       const float2 *__restrict__ tw2,
+                                       const uint8_t *__restrict__ flags) {
   extern __shared__ float2 s[];
   const int n2 = d2.L;
   const int nv = p.nv;
@@ -750,7 +782,9 @@ __global__ void __launch_bounds__(kColThreads, 2)
   for (int c = 0; c < NE; ++c) part[c] = 0.f;
   for (int b = 0; b < n_batch; ++b) {
     const float2 *base = R + (size_t)b * nv * rstride + (size_t)n2 * k1 * rstride + cg * kPanel;
-    load_panel(s, base, (size_t)rstride, n2);
+    // flags (set only when no pass A ran before): unflagged rows read as zeros
+    load_panel(s, base, (size_t)rstride, n2,
+               flags ? flags + (size_t)b * nv + (size_t)n2 * k1 : nullptr, 1);
     __syncthreads();
     const float2 *res = fft_smem<kPanelLayout>(s, s + ne, d2, -1.0f, tw2);
 #pragma unroll
@@ -931,7 +965,9 @@ void fft_prepare_rows(FftTables &t, int L) {
 template <bool FWD, int LAST, bool MID8>
 static void launch_persistent(const FftDesc &d, const RowStages &st, const float2 *tws,
                               const DevPlan &p, const float2 *in, int in_stride, float2 *out,
-                              int out_stride, int n_rows, unsigned *err, cudaStream_t s) {
+                              int out_stride, int n_batch, const RowSel &sel, unsigned *err,
+                              cudaStream_t s) {
+  const int n_rows = n_batch * p.nv;
   const int buf_elems = std::max(p.nu, in_stride);
   const uint32_t in_bytes = (uint32_t)(sizeof(float2) * (FWD ? p.nu : in_stride));
   if ((in_bytes & 15) || (buf_elems & 1))
@@ -954,15 +990,16 @@ static void launch_persistent(const FftDesc &d, const RowStages &st, const float
   if (per_sm < 1) throw Error(WGPU_ERR_INVALID, "row transform does not fit on an SM");
   const int blocks = std::min(n_rows, sm_count_fft() * per_sm);
   kern<<<blocks, threads, smem, s>>>(d, st, tws, in, in_stride, in_bytes, out, out_stride,
-                                      n_rows, p.width, buf_elems, mid_tab, err);
+                                      n_batch, p.nv, sel, p.width, buf_elems, mid_tab, err);
   check_launch(FWD ? "fft_rows_persistent_kernel<forward>"
                    : "fft_rows_persistent_kernel<backward>");
 }
 
 template <bool FWD>
 static void launch_rows(FftTables &t, const DevPlan &p, const float2 *in, int in_stride,
-                        float2 *out, int out_stride, int n_rows, unsigned *err,
-                        cudaStream_t s) {
+                        float2 *out, int out_stride, int n_batch, const RowSel &sel,
+                        unsigned *err, cudaStream_t s) {
+  const int n_rows = n_batch * p.nv;
   if (n_rows <= 0) return;
   if (p.nu % 16 || p.nu > kFftMaxRow)
     throw Error(WGPU_ERR_INVALID, "row transform length must be a multiple of 16 up to 12288");
@@ -976,35 +1013,41 @@ static void launch_rows(FftTables &t, const DevPlan &p, const float2 *in, int in
       throw Error(WGPU_ERR_INVALID, "row length " + std::to_string(p.nu) +
                                         " has no row transform schedule");
     if (last == 2)
-      launch_persistent<FWD, 2, false>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+      launch_persistent<FWD, 2, false>(d, st, tws, p, in, in_stride, out, out_stride, n_batch, sel,
+                                       err, s);
     else if (last == 3)
-      launch_persistent<FWD, 3, false>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+      launch_persistent<FWD, 3, false>(d, st, tws, p, in, in_stride, out, out_stride, n_batch, sel,
+                                       err, s);
     else
-      launch_persistent<FWD, 5, true>(d, st, tws, p, in, in_stride, out, out_stride, n_rows, err, s);
+      launch_persistent<FWD, 5, true>(d, st, tws, p, in, in_stride, out, out_stride, n_batch, sel,
+                                       err, s);
     return;
   }
   const int threads = std::max(64, (p.nu / 16 + 31) / 32 * 32);
   const size_t smem = 2 * sizeof(float2) * (size_t)row_buffer(p.nu);
   set_smem((const void *)fft_rows_pingpong_kernel<FWD>, smem);
   fft_rows_pingpong_kernel<FWD><<<(unsigned)n_rows, threads, smem, s>>>(
-      d, st, tws, in, in_stride, out, out_stride, p.width);
+      d, st, tws, in, in_stride, out, out_stride, n_batch, p.nv, sel, p.width);
   check_launch(FWD ? "fft_rows_pingpong_kernel<forward>" : "fft_rows_pingpong_kernel<backward>");
 }
 
 void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p,
                                   const float2 *planes, float2 *R, int rstride,
-                                  int n_batch, unsigned *err, cudaStream_t s) {
-  launch_rows<true>(t, p, planes, p.nu, R, rstride, n_batch * p.nv, err, s);
+                                  int n_batch, const RowSel &sel, unsigned *err,
+                                  cudaStream_t s) {
+  launch_rows<true>(t, p, planes, p.nu, R, rstride, n_batch, sel, err, s);
 }
 
 void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
                                   const float2 *R, int rstride, float2 *planes,
-                                  int n_batch, unsigned *err, cudaStream_t s) {
-  launch_rows<false>(t, p, R, rstride, planes, p.nu, n_batch * p.nv, err, s);
+                                  int n_batch, const RowSel &sel, unsigned *err,
+                                  cudaStream_t s) {
+  launch_rows<false>(t, p, R, rstride, planes, p.nu, n_batch, sel, err, s);
 }
 
 void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
-                       int rstride, int n_batch, float sign, cudaStream_t s) {
+                       int rstride, int n_batch, float sign, const RowSel &sel,
+                       cudaStream_t s) {
   if (n1 <= 1) return;
   const int ncg = rstride / kPanel;
   const FftDesc d1 = make_desc(n1);
@@ -1012,7 +1055,7 @@ void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R
   set_smem((const void *)fft_cols_pass_a_kernel, smem);
   dim3 grid(ncg, n2, n_batch);
   fft_cols_pass_a_kernel<<<grid, kColThreads, smem, s>>>(
-      d1, R, rstride, p.nv, n2, sign, fft_twiddles(t, n1), fft_twiddles(t, p.nv));
+      d1, R, rstride, p.nv, n2, sign, fft_twiddles(t, n1), fft_twiddles(t, p.nv), sel.flags);
   check_launch("fft_cols_pass_a_kernel");
 }
 
@@ -1020,7 +1063,10 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
                                           int n2, float2 *R, int rstride,
                                           int n_batch, int p_begin,
                                           const double *nu_w, float2 *acc,
-                                          cudaStream_t s) {
+                                          const RowSel &sel, cudaStream_t s) {
+  // after a pass A every row of R holds data; without one, R is as the row
+  // transforms left it
+  const uint8_t *flags = n1 <= 1 ? sel.flags : nullptr;
   const int ncg = rstride / kPanel;
   const FftDesc d2 = make_desc(n2);
   const size_t smem = cols_b_smem(n2);
@@ -1029,11 +1075,11 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
   if (n2 * kPanel <= 8 * kColThreads) {
     set_smem((const void *)fft_cols_forward_accumulate_kernel<8>, smem);
     fft_cols_forward_accumulate_kernel<8><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw);
+        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags);
   } else {
     set_smem((const void *)fft_cols_forward_accumulate_kernel<16>, smem);
     fft_cols_forward_accumulate_kernel<16><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw);
+        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags);
   }
   check_launch("fft_cols_forward_accumulate_kernel");
 }

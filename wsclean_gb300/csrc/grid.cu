@@ -555,8 +555,11 @@ __global__ void __launch_bounds__(kThreads)
           const int i = c % W, j = c / W;
           const float kx = __shfl_sync(0xffffffffu, k1, i);
           const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
+          // lanes past the footprint read its corner cell with weight 0 (a
+          // footprint cell: planes rows outside every footprint are never
+          // written in prediction and may hold anything)
           wgt[k] = c < kFoot ? kx * ky : 0.f;
-          idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : 0;
+          idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : iv_rel * RS + iu_rel;
         }
         float sr = 0.f, si = 0.f;
         for (int q = pa; q <= pb; ++q) {

@@ -94,6 +94,54 @@ double es_fourier(double beta, int support, double f);
 double es_kernel(double beta, double z);
 
 // ---- bucketing (bucket.cu) ----
+// Which (w-plane, grid row) pairs some visibility footprint touches.  A row
+// that no footprint touches holds zeros after gridding and is read by no
+// visibility in degridding, so the row transforms skip it.  One device
+// allocation of bytes() bytes:
+//   corners [n_planes][nv] u8   1 where a footprint has its corner (ip, iv)
+//   flags   [n_planes][nv] u8   1 where a footprint covers the row
+//   counts  [n_planes]     u32  flagged rows per plane
+//   start   [n_planes + 1] u32  first list entry of each plane
+//   list    [sum counts]   u32  flagged rows as q * nv + row, by plane then row
+struct RowOccupancy {
+  uint8_t *buf = nullptr;
+  int n_planes = 0;
+  int nv = 0;
+  static size_t r256(size_t b) { return (b + 255) / 256 * 256; }
+  size_t cells() const { return (size_t)n_planes * (size_t)nv; }
+  uint8_t *corners() const { return buf; }
+  uint8_t *flags() const { return buf + r256(cells()); }
+  uint32_t *counts() const { return (uint32_t *)(buf + 2 * r256(cells())); }
+  uint32_t *start() const {
+    return (uint32_t *)(buf + 2 * r256(cells()) + r256(4 * (size_t)n_planes));
+  }
+  uint32_t *list() const {
+    return (uint32_t *)(buf + 2 * r256(cells()) + r256(4 * (size_t)n_planes) +
+                        r256(4 * ((size_t)n_planes + 1)));
+  }
+  size_t bytes() const { return (size_t)((uint8_t *)list() - buf) + 4 * cells(); }
+};
+
+// Rows of one plane batch for the row transforms and column pass A: all rows
+// when list is null; otherwise the batch's rows are the list entries
+// start[0] .. start[n_batch] - 1 (entry - p_begin * nv is the row's index in
+// the batch) and flags[b * nv + row] marks the rows of batch plane b.
+struct RowSel {
+  const uint8_t *flags = nullptr;
+  const uint32_t *start = nullptr;
+  const uint32_t *list = nullptr;
+  int p_begin = 0;
+};
+inline RowSel row_sel(const RowOccupancy &o, int p_begin) {
+  RowSel r;
+  if (!o.buf) return r;
+  r.flags = o.flags() + (size_t)p_begin * o.nv;
+  r.start = o.start() + p_begin;
+  r.list = o.list();
+  r.p_begin = p_begin;
+  return r;
+}
+
 struct BucketScratch;  // grow-only device buffers
 struct BucketResult {
   VisRecord *records;   // [n_out]
@@ -101,7 +149,11 @@ struct BucketResult {
   uint32_t *offsets;    // [n_keys + 1]
   int64_t n_out;
   int64_t n_keys;
+  RowOccupancy rows;    // in the arena's occupancy slot
 };
+// Copies the occupancy data into dst (rows.bytes() bytes of device memory)
+// and returns the view on the copy.
+RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_t s);
 // Extents of the (non-zero when skip_zero) visibilities: w min/max in
 // wavelengths and the count.
 void compute_w_extent(const double *d_uvw, const double *d_freq,
@@ -187,13 +239,15 @@ bool fft_row_length_supported(int L);
 // trimmed columns.
 // Row transforms (persistent, TMA-prefetched).  err counts bounded waits that
 // expired (a device word the caller checks after the call).
+// Only the rows `sel` names are transformed: the other rows of R are left
+// as they are (column pass A reads them as zeros through the same flags).
 void launch_fft_rows_forward_crop(FftTables &t, const DevPlan &p, const float2 *planes,
-                                  float2 *R, int rstride, int n_batch, unsigned *err,
-                                  cudaStream_t s);
-// Row pass, backward: R -> planes (full rows).
+                                  float2 *R, int rstride, int n_batch, const RowSel &sel,
+                                  unsigned *err, cudaStream_t s);
+// Row pass, backward: R -> planes (full rows), only the rows `sel` names.
 void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p, const float2 *R,
-                                  int rstride, float2 *planes, int n_batch, unsigned *err,
-                                  cudaStream_t s);
+                                  int rstride, float2 *planes, int n_batch, const RowSel &sel,
+                                  unsigned *err, cudaStream_t s);
 // Creates the row-transform tables of length L (before a graph capture).
 void fft_prepare_rows(FftTables &t, int L);
 // Bounded-wait self-test (fft.cu): WGPU_ERR_TIMEOUT when the wait expired.
@@ -201,13 +255,17 @@ int bounded_wait_selftest(double timeout_ms);
 // Column passes (four-step split nv = n1 * n2, see fft.cu): pass A over
 // strided length-n1 transforms, pass B over contiguous length-n2 transforms
 // with the fused w-screen.
+// Pass A with sel.flags: forward reads unflagged rows of R as zeros, backward
+// writes only the flagged rows.
 void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
-                       int rstride, int n_batch, float sign, cudaStream_t s);
+                       int rstride, int n_batch, float sign, const RowSel &sel,
+                       cudaStream_t s);
+// sel: the rows the forward row transforms wrote (read when n1 <= 1).
 void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1,
                                           int n2, float2 *R, int rstride,
                                           int n_batch, int p_begin,
                                           const double *nu_w, float2 *acc,
-                                          cudaStream_t s);
+                                          const RowSel &sel, cudaStream_t s);
 void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        int n2, const float *img_corr,
                                        const double *nu_w, float2 *R,
@@ -252,7 +310,7 @@ class DeviceArena {
   void release();
 
  private:
-  static constexpr int kSlots = 32;
+  static constexpr int kSlots = 40;
   void *ptr_[kSlots] = {};
   size_t size_[kSlots] = {};
 };
@@ -289,6 +347,7 @@ enum ArenaSlot {
   kSlotCounter,
   kSlotItemDesc,
   kSlotSpill,
+  kSlotRowOcc,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
