@@ -529,7 +529,9 @@ __global__ void __launch_bounds__(kThreads)
       }
       __syncthreads();
       const int n_round = (int)min((uint32_t)kThreads, hi - rb);
-      for (int m = warp * 32; m < min(n_round, warp * 32 + 32); ++m) {
+      // the round's records dealt round-robin over the warps (a unit's plane
+      // group often holds fewer records than a round)
+      for (int m = warp; m < n_round; m += kThreads / 32) {
         const uint32_t s = stage_s[m];
         VisRecord v;
         {
@@ -541,12 +543,22 @@ __global__ void __launch_bounds__(kThreads)
         const int iv_rel = v.iv - tv * T;
         const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
         if (pa > pb) continue;  // uniform in the warp
-        const bool lx = lane < W;
-        const float f1 = (lx ? v.fu : v.fv) + (float)(lx ? lane : lane - W);
-        float k1 = es_eval(p.beta, f1 * inv_half);
-        k1 = lane < 2 * W ? k1 : 0.f;
-        float k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
-        if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
+        // kernel weights: lanes [0, W) along u, [W, 2W) along v; along w
+        // lanes [2W, 3W) of k1 when 3W <= 32, else lanes [0, W) of k2
+        constexpr bool kOneEval = 3 * W <= 32;
+        constexpr int kW0 = kOneEval ? 2 * W : 0;
+        const int sec = lane < W ? 0 : (lane < 2 * W ? 1 : 2);
+        float k1, k2 = 0.f;
+        if (kOneEval) {
+          const float f1 = (sec == 0 ? v.fu : sec == 1 ? v.fv : v.fw) + (float)(lane - sec * W);
+          k1 = lane < 3 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
+          if (p.n_planes == 1 && sec == 2) k1 = lane == 2 * W ? 1.0f : 0.0f;
+        } else {
+          const float f1 = (sec == 0 ? v.fu : v.fv) + (float)(sec == 0 ? lane : lane - W);
+          k1 = lane < 2 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
+          k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+          if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
+        }
         float wgt[kLaneCells];
         int idx[kLaneCells];
 #pragma unroll
@@ -563,7 +575,7 @@ __global__ void __launch_bounds__(kThreads)
         }
         float sr = 0.f, si = 0.f;
         for (int q = pa; q <= pb; ++q) {
-          const float kw = __shfl_sync(0xffffffffu, k2, q - v.ip);
+          const float kw = __shfl_sync(0xffffffffu, kOneEval ? k1 : k2, kW0 + q - v.ip);
           const float2 *pl = halo + (q - q0) * kPlane;
           float pr = 0.f, pi = 0.f;
 #pragma unroll
