@@ -96,6 +96,80 @@ __device__ __forceinline__ Footprint footprint(const DevPlan &p,
   return f;
 }
 
+// ---- FP32 decision of the integer footprint --------------------------------
+// The corners are ceilings of FP64 values: x = (a * s) - h for u and v, and
+// y = ((w * sw - w0) * inv_dw) - h for w.  The same chains in FP32 (inputs
+// rounded to float, each operation rounded) differ from the FP64 values by at
+// most 2^-24 times a few times the magnitudes involved (bounds below, with a
+// factor 4 where 3.0001 suffices); where the FP32 value lies farther than that
+// from every integer, its ceiling is the FP64 ceiling.  Otherwise the sample is
+// left to the FP64 pass.
+constexpr float kTwoM22 = 2.384185791015625e-07f;  // 2^-22
+
+// ceil of x = fl64(fl64(a * s) - h), or false when the FP32 value is too
+// close to an integer (or out of int range) to decide.
+__device__ __forceinline__ bool ceil_decided(double a, double s, float h, int *c) {
+  const float x = __fsub_rn(__fmul_rn(__double2float_rn(a), __double2float_rn(s)), h);
+  const float eb = kTwoM22 * (fabsf(x) + h) + 1e-6f;
+  if (!(fabsf(x) < 1.0e9f)) return false;
+  const float fx = floorf(x);
+  const float lo = x - fx;  // exact
+  if (!(lo > eb && lo < 1.0f - eb)) return false;
+  *c = (int)fx + 1;
+  return true;
+}
+
+// Wraps a corner into [0, n) as the FP64 path does ((c mod n) + n mod n),
+// for corners within one period of the grid.
+__device__ __forceinline__ bool wrap_decided(int c, int n, int *out) {
+  if (c < -n || c >= 2 * n) return false;
+  *out = c < 0 ? c + n : (c >= n ? c - n : c);
+  return true;
+}
+
+// Key (and corner row / first plane) of a sample decided in FP32; false
+// when any of the three corners needs the FP64 footprint.
+__device__ __forceinline__ bool key_decided(const DevPlan &p, const double *uvw_row,
+                                            const ChannelScale &cs, uint32_t *key, int *iv_out,
+                                            int *ip_out) {
+  const float half = 0.5f * (float)p.support;
+  int iu0, iv0, iu, iv, ip = 0;
+  if (!ceil_decided(uvw_row[0], cs.su, half, &iu0) || !ceil_decided(uvw_row[1], cs.sv, half, &iv0))
+    return false;
+  if (!wrap_decided(iu0, p.nu, &iu) || !wrap_decided(iv0, p.nv, &iv)) return false;
+  if (p.n_planes > 1) {
+    const float wl = __fmul_rn(__double2float_rn(uvw_row[2]), __double2float_rn(cs.sw));
+    const float w0 = __double2float_rn(p.w0), idw = __double2float_rn(p.inv_dw);
+    const float d = __fsub_rn(wl, w0);
+    const float pw = __fmul_rn(d, idw);
+    const float y = __fsub_rn(pw, half);
+    const float eb =
+        kTwoM22 * (fabsf(idw) * (fabsf(wl) + fabsf(w0) + fabsf(d)) + fabsf(pw) + fabsf(y)) + 1e-6f;
+    const int ip_max = p.n_planes - p.support;
+    if (!(fabsf(y) < 1.0e9f)) return false;
+    if (y + eb <= 0.0f) {
+      ip = 0;  // ceil(y) <= 0
+    } else if (y - eb > (float)(ip_max - 1)) {
+      ip = ip_max;  // ceil(y) >= ip_max
+    } else {
+      const float fy = floorf(y);
+      const float lo = y - fy;
+      if (!(lo > eb && lo < 1.0f - eb)) return false;
+      ip = min(max((int)fy + 1, 0), ip_max);
+    }
+  }
+  const int tu = p.tile == 16 ? iu >> 4 : iu / p.tile;
+  const int tv = p.tile == 16 ? iv >> 4 : iv / p.tile;
+  const uint32_t tile = (uint32_t)(tv * p.ntu + tu);
+  *key = (tile * 4u + (uint32_t)spill_class(iu - tu * p.tile, iv - tv * p.tile, p.tile,
+                                            p.support)) *
+             (uint32_t)p.n_planes +
+         (uint32_t)ip;
+  *iv_out = iv;
+  *ip_out = ip;
+  return true;
+}
+
 __device__ __forceinline__ bool is_zero(const float2 v) {
   return v.x == 0.0f && v.y == 0.0f;
 }
@@ -182,16 +256,33 @@ __global__ void __launch_bounds__(kThreads)
     key_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
                Selector sel, int64_t n_rows, int64_t n_chan,
                uint32_t sentinel, uint32_t *keys,
-               uint32_t *vals, uint32_t *counts, uint8_t *corners) {
+               uint32_t *vals, uint32_t *counts, uint8_t *corners,
+               uint32_t *pending, uint32_t *n_pending) {
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const int64_t r = e / n_chan, c = e - r * n_chan;
   uint32_t key = sentinel;
+  bool defer = false;
   if (sel(e)) {
-    const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
-    key = f.key;
-    if (corners) corners[(size_t)f.ip * p.nv + f.iv] = 1;
+    int iv, ip;
+    if (key_decided(p, uvw + 3 * r, cs[c], &key, &iv, &ip)) {
+      if (corners) corners[(size_t)ip * p.nv + iv] = 1;
+    } else {
+      defer = true;
+    }
+  }
+  {
+    // samples the FP32 test cannot decide go to the FP64 pass (key_fix_kernel)
+    const unsigned dm = __ballot_sync(__activemask(), defer);
+    if (dm) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(dm) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(n_pending, (uint32_t)__popc(dm));
+      base = __shfl_sync(__activemask(), base, leader);
+      if (defer) pending[base + __popc(dm & ((1u << lane) - 1u))] = (uint32_t)e;
+    }
   }
   keys[e] = key;
   vals[e] = (uint32_t)e;
@@ -201,6 +292,23 @@ __global__ void __launch_bounds__(kThreads)
     const unsigned peers = __match_any_sync(active, key);
     const int leader = __ffs(peers) - 1;
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counts[key], __popc(peers));
+  }
+}
+
+// FP64 footprints of the samples key_kernel deferred: key, corner mark and
+// histogram count.
+__global__ void __launch_bounds__(kThreads)
+    key_fix_kernel(DevPlan p, const double *uvw, const ChannelScale *cs, int64_t n_chan,
+                   const uint32_t *__restrict__ pending, const uint32_t *__restrict__ n_pending,
+                   uint32_t *keys, uint32_t *counts, uint8_t *corners) {
+  const uint32_t n = *n_pending;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t e = pending[i];
+    const int64_t r = e / n_chan, c = e - r * n_chan;
+    const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
+    keys[e] = f.key;
+    if (corners) corners[(size_t)f.ip * p.nv + f.iv] = 1;
+    atomicAdd(&counts[f.key], 1u);
   }
 }
 
@@ -273,6 +381,67 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Footprint of a record: corners decided in FP32 where possible (see
+// key_decided), fractions from the FP64 coordinates; identical to footprint().
+__device__ __forceinline__ Footprint record_footprint(const DevPlan &p, const double *row,
+                                                      const ChannelScale &cs, double *wl_out) {
+  const float half = 0.5f * (float)p.support;
+  int iu0, iv0, iu, iv;
+  bool ok = ceil_decided(row[0], cs.su, half, &iu0) && ceil_decided(row[1], cs.sv, half, &iv0) &&
+            wrap_decided(iu0, p.nu, &iu) && wrap_decided(iv0, p.nv, &iv);
+  Footprint f;
+  double wl = 0.0, pw = 0.0;
+  int ip = 0;
+  if (ok && p.n_planes > 1) {
+    wl = __dmul_rn(row[2], cs.sw);
+    pw = __dmul_rn(__dsub_rn(wl, p.w0), p.inv_dw);
+    const float wlf = __fmul_rn(__double2float_rn(row[2]), __double2float_rn(cs.sw));
+    const float w0 = __double2float_rn(p.w0), idw = __double2float_rn(p.inv_dw);
+    const float d = __fsub_rn(wlf, w0);
+    const float pwf = __fmul_rn(d, idw);
+    const float y = __fsub_rn(pwf, half);
+    const float eb =
+        kTwoM22 * (fabsf(idw) * (fabsf(wlf) + fabsf(w0) + fabsf(d)) + fabsf(pwf) + fabsf(y)) +
+        1e-6f;
+    const int ip_max = p.n_planes - p.support;
+    if (!(fabsf(y) < 1.0e9f)) {
+      ok = false;
+    } else if (y + eb <= 0.0f) {
+      ip = 0;
+    } else if (y - eb > (float)(ip_max - 1)) {
+      ip = ip_max;
+    } else {
+      const float fy = floorf(y);
+      const float lo = y - fy;
+      if (lo > eb && lo < 1.0f - eb)
+        ip = min(max((int)fy + 1, 0), ip_max);
+      else
+        ok = false;
+    }
+  }
+  if (!ok) {
+    *wl_out = __dmul_rn(row[2], cs.sw);
+    return footprint(p, row, cs);
+  }
+  f.iu = iu;
+  f.iv = iv;
+  f.fu = __double2float_rn(__dsub_rn((double)iu0, __dmul_rn(row[0], cs.su)));
+  f.fv = __double2float_rn(__dsub_rn((double)iv0, __dmul_rn(row[1], cs.sv)));
+  if (p.n_planes > 1) {
+    f.ip = ip;
+    f.fw = __double2float_rn(__dsub_rn((double)ip, pw));
+  } else {
+    f.ip = 0;
+    f.fw = 0.0f;
+    wl = __dmul_rn(row[2], cs.sw);
+  }
+  f.key = 0;  // not needed for records
+  *wl_out = wl;
+  return f;
+}
+
+// SHIFT: the image has an l or m shift (else the phase needs only w).
+template <bool SHIFT>
 __global__ void __launch_bounds__(kThreads)
     record_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
                   const float2 *vis, int64_t n_chan, const uint32_t *perm,
@@ -283,12 +452,18 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t r = e / n_chan, c = e - r * n_chan;
   const double *row = uvw + 3 * r;
   const ChannelScale sc = cs[c];
-  const Footprint f = footprint(p, row, sc);
+  double wl;
+  const Footprint f = record_footprint(p, row, sc, &wl);
   // shift phase theta = u l_shift + v m_shift + w c_n (turns), FP64 argument,
-  // reduced to [-1/2, 1/2] before the FP32 sincos.
-  const double fl = sc.sw;
-  double t = row[0] * fl * p.l_shift + row[1] * fl * p.m_shift +
-             row[2] * fl * p.nm1_center;
+  // reduced to [-1/2, 1/2] before the FP32 sincos.  Without shifts the first
+  // two terms are zero and theta = fl(w f / c) c_n, the same value.
+  double t;
+  if (SHIFT) {
+    const double fl = sc.sw;
+    t = row[0] * fl * p.l_shift + row[1] * fl * p.m_shift + row[2] * fl * p.nm1_center;
+  } else {
+    t = __dmul_rn(wl, p.nm1_center);
+  }
   t -= rint(t);
   float sn, cn;
   sincospif(2.0f * (float)t, &sn, &cn);
@@ -479,10 +654,17 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   res.rows.buf = (uint8_t *)arena.get(kSlotRowOcc, RowOccupancy{nullptr, p.n_planes, p.nv}.bytes());
   WGPU_CUDA(cudaMemsetAsync(res.rows.corners(), 0, res.rows.cells(), s));
   if (n > 0) {
+    // deferred samples listed in keys2 (free until the first radix pass),
+    // their count in the word after the channel scales
+    uint32_t *n_pending = (uint32_t *)(cs + n_chan + 1);
+    WGPU_CUDA(cudaMemsetAsync(n_pending, 0, sizeof(uint32_t), s));
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
-        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners());
+        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners(), keys2, n_pending);
     check_launch("key_kernel");
+    key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, n_pending,
+                                                        keys, offsets, res.rows.corners());
+    check_launch("key_fix_kernel");
   }
   build_row_occupancy(res.rows, p.support, s);
   exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
@@ -511,7 +693,9 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   res.offsets = offsets;
   res.records = (VisRecord *)arena.get(kSlotRecords, sizeof(VisRecord) * (res.n_out + 1));
   if (res.n_out > 0) {
-    record_kernel<<<grid_for(res.n_out, kThreads), kThreads, 0, s>>>(
+    const bool shift = p.l_shift != 0.0 || p.m_shift != 0.0;
+    (shift ? record_kernel<true> : record_kernel<false>)<<<grid_for(res.n_out, kThreads),
+                                                          kThreads, 0, s>>>(
         p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan,
         res.perm, res.n_out, res.records);
     check_launch("record_kernel");
@@ -615,10 +799,16 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
   // the histogram accumulates into the caller's offsets: start from zero
   WGPU_CUDA(cudaMemsetAsync(d_offsets, 0, sizeof(uint32_t) * (n_keys + 1), s));
   if (n > 0) {
+    // deferred samples listed in keys2, their count in vals2[0] (both free
+    // until the first radix pass)
+    WGPU_CUDA(cudaMemsetAsync(vals2, 0, sizeof(uint32_t), s));
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, nullptr}, n_rows,
-        n_chan, sentinel, keys, vals, d_offsets, nullptr);
+        n_chan, sentinel, keys, vals, d_offsets, nullptr, keys2, vals2);
     check_launch("key_kernel");
+    key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, vals2, keys,
+                                                        d_offsets, nullptr);
+    check_launch("key_fix_kernel");
   }
   exclusive_scan_u32_scratch(d_offsets, n_keys + 1, scan_tmp, s);
   const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
@@ -639,7 +829,9 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
   WGPU_CUDA(cudaStreamSynchronize(s));
   if (total > 0) {
     WGPU_CUDA(cudaMemcpyAsync(d_perm, vin, sizeof(uint32_t) * total, cudaMemcpyDeviceToDevice, s));
-    record_kernel<<<grid_for(total, kThreads), kThreads, 0, s>>>(
+    const bool shift = p.l_shift != 0.0 || p.m_shift != 0.0;
+    (shift ? record_kernel<true> : record_kernel<false>)<<<grid_for(total, kThreads), kThreads,
+                                                          0, s>>>(
         p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan, vin, total,
         d_records);
     check_launch("record_kernel");

@@ -30,7 +30,6 @@
 namespace wgpu {
 
 constexpr int kFftMaxRow = 12288;  // two row buffers fit in 227 KB of shared memory
-constexpr int kMaxElemsPerThread = 16;  // complex values a thread holds per stage
 constexpr int kMaxStages = 20;
 
 int fft_row_max_length() { return kFftMaxRow; }
@@ -694,7 +693,8 @@ __global__ void __launch_bounds__(kColThreads, 3)
   for (int e = threadIdx.x; e < n1 * kPanel; e += blockDim.x) {
     const int k1 = e / kPanel, c = e % kPanel;
     float2 v = res[e];
-    if (sign < 0) v = cmul(v, __ldg(twN + (int)(((long long)r2 * k1) % nv)));
+    // r2 < n2 and k1 < n1, so r2 k1 < nv indexes the table directly
+    if (sign < 0) v = cmul(v, __ldg(twN + r2 * k1));
     // backward: rows no visibility reads are not written
     if (sign < 0 || !fl || __ldg(fl + r2 + n2 * k1)) base[(size_t)(r2 + n2 * k1) * rstride + c] = v;
   }
@@ -874,7 +874,7 @@ __global__ void __launch_bounds__(kColThreads, 2)
       const int r2 = e / kPanel, c = e % kPanel;
       float2 v = res[e];
       if (n1 > 1) {
-        float2 w = __ldg(twN + (int)(((long long)r2 * k1) % nv));
+        float2 w = __ldg(twN + r2 * k1);  // r2 < n2, k1 < n1: r2 k1 < nv
         w.y = -w.y;  // exp(+2 pi i r2 k1 / nv)
         v = cmul(v, w);
       }

@@ -599,17 +599,6 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-int sm_count() {
-  // initialised once, thread-safely (gridders run on several host threads)
-  static const int n = [] {
-    int dev = 0, v = 0;
-    WGPU_CUDA(cudaGetDevice(&dev));
-    WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-    return v;
-  }();
-  return n;
-}
-
 // Zeroes the cells of the gridding units that are split into several items
 // (their items add into the planes and into the unit's spill slot); one warp
 // per unit.

@@ -45,6 +45,17 @@ void check_launch(const char *what) {
 
 DeviceArena::~DeviceArena() { release(); }
 
+int sm_count() {
+  // initialised once, thread-safely (gridders run on several host threads)
+  static const int n = [] {
+    int dev = 0, v = 0;
+    WGPU_CUDA(cudaGetDevice(&dev));
+    WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
+  return n;
+}
+
 void *DeviceArena::get(int slot, size_t bytes) {
   if (slot < 0 || slot >= kSlots) throw Error(WGPU_ERR_INVALID, "arena slot");
   if (bytes == 0) bytes = 16;

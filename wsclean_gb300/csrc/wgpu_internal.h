@@ -32,6 +32,7 @@ struct Error : std::runtime_error {
   } while (0)
 
 void count_launch(int n = 1);
+int sm_count();  // multiprocessors of the current device (first call's device)
 uint64_t launch_count();
 uint64_t thread_launch_count();  // launches issued by the calling thread
 
