@@ -448,12 +448,13 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Degridding of one plane batch, one warp per visibility: the block loads
-// its unit's halo region (the tile plus W - 1 cells, G planes) into shared
-// memory as float2 cells with a row stride of T + W rounded to 8 mod 16 (a
-// half-warp's two rows x eight columns then fall on distinct bank pairs);
-// lanes own footprint cells, accumulate their cells over the planes of the
-// group, and a warp-level shuffle reduction forms the sum.
+// Degridding of one plane batch: the block loads its unit's halo region (the
+// tile plus W - 1 cells, G planes) into shared memory as float2 cells with a
+// row stride of T + W rounded to 8 mod 16, stages the unit's records in rounds
+// and works through them.  W <= 8: groups of eight lanes take one record
+// each (lane i sums footprint column i over the rows and planes, a three-step
+// shuffle reduction forms the record's sum).  W > 8: one warp per record,
+// lanes own footprint cells and a warp-wide reduction forms the sum.
 __host__ __device__ constexpr int degrid_row_stride(int R) { return (R + 7) / 16 * 16 + 8; }
 template <int T, int G, int W>
 constexpr size_t degrid_smem_bytes() {
@@ -529,70 +530,132 @@ __global__ void __launch_bounds__(kThreads)
       }
       __syncthreads();
       const int n_round = (int)min((uint32_t)kThreads, hi - rb);
-      // the round's records dealt round-robin over the warps (a unit's plane
-      // group often holds fewer records than a round)
-      for (int m = warp; m < n_round; m += kThreads / 32) {
-        const uint32_t s = stage_s[m];
-        VisRecord v;
-        {
-          const float4 a = stage[m][0], b = stage[m][1];
-          v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
-          v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
-        }
-        const int iu_rel = v.iu - tu * T;
-        const int iv_rel = v.iv - tv * T;
-        const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
-        if (pa > pb) continue;  // uniform in the warp
-        // kernel weights: lanes [0, W) along u, [W, 2W) along v; along w
-        // lanes [2W, 3W) of k1 when 3W <= 32, else lanes [0, W) of k2
-        constexpr bool kOneEval = 3 * W <= 32;
-        constexpr int kW0 = kOneEval ? 2 * W : 0;
-        const int sec = lane < W ? 0 : (lane < 2 * W ? 1 : 2);
-        float k1, k2 = 0.f;
-        if (kOneEval) {
-          const float f1 = (sec == 0 ? v.fu : sec == 1 ? v.fv : v.fw) + (float)(lane - sec * W);
-          k1 = lane < 3 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
-          if (p.n_planes == 1 && sec == 2) k1 = lane == 2 * W ? 1.0f : 0.0f;
-        } else {
-          const float f1 = (sec == 0 ? v.fu : v.fv) + (float)(sec == 0 ? lane : lane - W);
-          k1 = lane < 2 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
-          k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
-          if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
-        }
-        float wgt[kLaneCells];
-        int idx[kLaneCells];
-#pragma unroll
-        for (int k = 0; k < kLaneCells; ++k) {
-          const int c = lane + 32 * k;
-          const int i = c % W, j = c / W;
-          const float kx = __shfl_sync(0xffffffffu, k1, i);
-          const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
-          // lanes past the footprint read its corner cell with weight 0 (a
-          // footprint cell: planes rows outside every footprint are never
-          // written in prediction and may hold anything)
-          wgt[k] = c < kFoot ? kx * ky : 0.f;
-          idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : iv_rel * RS + iu_rel;
-        }
-        float sr = 0.f, si = 0.f;
-        for (int q = pa; q <= pb; ++q) {
-          const float kw = __shfl_sync(0xffffffffu, kOneEval ? k1 : k2, kW0 + q - v.ip);
-          const float2 *pl = halo + (q - q0) * kPlane;
-          float pr = 0.f, pi = 0.f;
-#pragma unroll
-          for (int k = 0; k < kLaneCells; ++k) {
-            const float2 g = pl[idx[k]];
-            pr = fmaf(wgt[k], g.x, pr);
-            pi = fmaf(wgt[k], g.y, pi);
+      if constexpr (W <= 8) {
+        // groups of eight lanes, one record each: lane i of a group owns
+        // footprint column i and sums its W rows over the record's planes; a
+        // warp takes four consecutive records per step (records of a class
+        // range are ordered by first plane, so the four mostly share planes)
+        const int g = lane >> 3, i = lane & 7;
+        const int gbase = lane & ~7;
+        for (int m0 = warp * 4; m0 < n_round; m0 += kThreads / 8) {
+          const int m = m0 + g;
+          const bool valid = m < n_round;
+          const int mm = valid ? m : m0;
+          const float4 a = stage[mm][0], b = stage[mm][1];
+          const uint32_t s = stage_s[mm];
+          const int iu_rel = __float_as_int(b.y) - tu * T;
+          const int iv_rel = __float_as_int(b.z) - tv * T;
+          const int ip = __float_as_int(b.w);
+          int pa = max(ip, q0), pb = min(ip + W - 1, q1 - 1);
+          if (!valid) pa = pb + 1;
+          // kernel values at index i along u, v and w
+          float ku = 0.f, kv = 0.f, kw = 0.f;
+          if (i < W) {
+            ku = es_eval(p.beta, (a.z + (float)i) * inv_half);
+            kv = es_eval(p.beta, (a.w + (float)i) * inv_half);
+            kw = p.n_planes == 1 ? (i == 0 ? 1.0f : 0.0f)
+                                 : es_eval(p.beta, (b.x + (float)i) * inv_half);
           }
-          sr = fmaf(kw, pr, sr);
-          si = fmaf(kw, pi, si);
-        }
+          float kvj[W];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          sr += __shfl_xor_sync(0xffffffffu, sr, o);
-          si += __shfl_xor_sync(0xffffffffu, si, o);
+          for (int j = 0; j < W; ++j) kvj[j] = __shfl_sync(0xffffffffu, kv, gbase + j);
+          // the union of the four records' planes; each group reads only its
+          // own footprint cells (rows outside every footprint may hold
+          // anything in prediction)
+          const int qa = __reduce_min_sync(0xffffffffu, pa <= pb ? pa : 0x7fffffff);
+          const int qb = __reduce_max_sync(0xffffffffu, pa <= pb ? pb : -0x7fffffff);
+          const float2 *col = halo + iv_rel * RS + iu_rel + i;
+          float sr = 0.f, si = 0.f;
+          for (int q = qa; q <= qb; ++q) {
+            const int dz = q - ip;
+            const float kwq = __shfl_sync(0xffffffffu, kw, gbase + min(max(dz, 0), 7));
+            if (q >= pa && q <= pb && i < W) {
+              const float2 *c = col + (q - q0) * kPlane;
+              float cr = 0.f, cim = 0.f;
+#pragma unroll
+              for (int j = 0; j < W; ++j) {
+                const float2 gv = c[j * RS];
+                cr = fmaf(kvj[j], gv.x, cr);
+                cim = fmaf(kvj[j], gv.y, cim);
+              }
+              sr = fmaf(kwq, cr, sr);
+              si = fmaf(kwq, cim, si);
+            }
+          }
+          sr *= ku;
+          si *= ku;
+#pragma unroll
+          for (int o = 4; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+          }
+          if (i == 0 && pa <= pb) atomicAdd(&acc[s], make_float2(sr, si));
         }
-        if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
+      } else {
+        // one warp per record (W > 8): lanes own footprint cells
+        for (int m = warp; m < n_round; m += kThreads / 32) {
+          const uint32_t s = stage_s[m];
+          VisRecord v;
+          {
+            const float4 a = stage[m][0], b = stage[m][1];
+            v.re = a.x; v.im = a.y; v.fu = a.z; v.fv = a.w; v.fw = b.x;
+            v.iu = __float_as_int(b.y); v.iv = __float_as_int(b.z); v.ip = __float_as_int(b.w);
+          }
+          const int iu_rel = v.iu - tu * T;
+          const int iv_rel = v.iv - tv * T;
+          const int pa = max(v.ip, q0), pb = min(v.ip + W - 1, q1 - 1);
+          if (pa > pb) continue;  // uniform in the warp
+          // kernel weights: lanes [0, W) along u, [W, 2W) along v; along w
+          // lanes [2W, 3W) of k1 when 3W <= 32, else lanes [0, W) of k2
+          constexpr bool kOneEval = 3 * W <= 32;
+          constexpr int kW0 = kOneEval ? 2 * W : 0;
+          const int sec = lane < W ? 0 : (lane < 2 * W ? 1 : 2);
+          float k1, k2 = 0.f;
+          if (kOneEval) {
+            const float f1 = (sec == 0 ? v.fu : sec == 1 ? v.fv : v.fw) + (float)(lane - sec * W);
+            k1 = lane < 3 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
+            if (p.n_planes == 1 && sec == 2) k1 = lane == 2 * W ? 1.0f : 0.0f;
+          } else {
+            const float f1 = (sec == 0 ? v.fu : v.fv) + (float)(sec == 0 ? lane : lane - W);
+            k1 = lane < 2 * W ? es_eval(p.beta, f1 * inv_half) : 0.f;
+            k2 = es_eval(p.beta, (v.fw + (float)lane) * inv_half);
+            if (p.n_planes == 1) k2 = lane == 0 ? 1.0f : 0.0f;
+          }
+          float wgt[kLaneCells];
+          int idx[kLaneCells];
+  #pragma unroll
+          for (int k = 0; k < kLaneCells; ++k) {
+            const int c = lane + 32 * k;
+            const int i = c % W, j = c / W;
+            const float kx = __shfl_sync(0xffffffffu, k1, i);
+            const float ky = __shfl_sync(0xffffffffu, k1, W + (j < W ? j : 0));
+            // lanes past the footprint read its corner cell with weight 0 (a
+            // footprint cell: planes rows outside every footprint are never
+            // written in prediction and may hold anything)
+            wgt[k] = c < kFoot ? kx * ky : 0.f;
+            idx[k] = c < kFoot ? (iv_rel + j) * RS + iu_rel + i : iv_rel * RS + iu_rel;
+          }
+          float sr = 0.f, si = 0.f;
+          for (int q = pa; q <= pb; ++q) {
+            const float kw = __shfl_sync(0xffffffffu, kOneEval ? k1 : k2, kW0 + q - v.ip);
+            const float2 *pl = halo + (q - q0) * kPlane;
+            float pr = 0.f, pi = 0.f;
+  #pragma unroll
+            for (int k = 0; k < kLaneCells; ++k) {
+              const float2 g = pl[idx[k]];
+              pr = fmaf(wgt[k], g.x, pr);
+              pi = fmaf(wgt[k], g.y, pi);
+            }
+            sr = fmaf(kw, pr, sr);
+            si = fmaf(kw, pi, si);
+          }
+  #pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+          }
+          if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
+        }
       }
       __syncthreads();
     }
