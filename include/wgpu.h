@@ -279,6 +279,19 @@ int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
                       int32_t *ip, float *fu, float *fv, float *fw,
                       uint32_t *offsets, int64_t *n_out);
 
+/* No counterpart in the reference (a test hook of this library).
+ *
+ * The same bucketing pass, returning which (w plane, grid row) pairs a
+ * footprint touches: row_flags [n_planes * nv] (1 where a footprint with
+ * corner (ip, iv) covers plane q = ip .. ip + W - 1 and row iv .. iv + W - 1,
+ * cyclically), row_start [n_planes + 1] (first list entry of each plane) and
+ * row_list [n_planes * nv] (the flagged rows as q * nv + row, by plane then
+ * row; row_start[n_planes] entries are written).  Null outputs are skipped. */
+int wgpu_bucket_debug_rows(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                           const double *uvw, const double *freq, const float *vis,
+                           int skip_zero, uint8_t *row_flags, uint32_t *row_start,
+                           uint32_t *row_list);
+
 /* ------------------------------------------------------------------------ */
 /* Allocation-free bucketing                                                  */
 /* ------------------------------------------------------------------------ */

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from wsclean_gb300 import _lib, synthetic
-from wsclean_gb300.gridder import WGriddingGridder_Simple, bucket_debug
+from wsclean_gb300.gridder import WGriddingGridder_Simple, bucket_debug, bucket_debug_rows
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -69,6 +69,68 @@ def test_bucketing_matches_golden_fixture(wgpu_lib):
     for k in ("perm", "iu", "iv", "ip", "fu", "fv", "fw"):
         np.testing.assert_array_equal(got[k], g[k], err_msg=k)
     np.testing.assert_array_equal(got["offsets"].astype(np.int64), g["offsets"])
+
+
+def _footprint_rows(iv, ip, n_planes, nv, W):
+    """(plane, row) pairs the footprints with corners (ip, iv) cover: planes
+    ip .. ip + W - 1 (one plane without w stacking), rows iv .. iv + W - 1
+    cyclically."""
+    corner = np.zeros((n_planes, nv), bool)
+    corner[ip, iv] = True
+    occ = np.zeros_like(corner)
+    for a in range(W if n_planes > 1 else 1):
+        for b in range(W):
+            occ[a:] |= np.roll(corner, b, axis=1)[:n_planes - a]
+    return occ
+
+
+@pytest.mark.parametrize("case", BUCKET_CASES)
+def test_row_occupancy_matches_oracle_footprints(wgpu_lib, oracle_lib, case):
+    """The rows the row transforms process are exactly the (plane, row) pairs
+    that the oracle's footprints cover, listed in plane-then-row order."""
+    uvw, freq, vis = synthetic.random_points(case["rows"], case["chan"], case["W"], case["dl"],
+                                             case["seed"], w_scale=case["w_scale"],
+                                             frac_zero=case["zero"])
+    v = vis if case["inv"] else None
+    p = _plan_for(uvw, freq, v, case["W"], case["dl"], 1e-4, case["shift"])
+    ref = oracle_lib.bucket(p, uvw, freq, v, case["inv"])
+    got = bucket_debug_rows(p, uvw.shape[0], freq.size, uvw, freq, v, case["inv"])
+    occ = _footprint_rows(np.asarray(ref["iv"]), np.asarray(ref["ip"]), p.n_planes, p.nv,
+                          p.support)
+    np.testing.assert_array_equal(got["flags"].astype(bool), occ)
+    np.testing.assert_array_equal(got["list"], np.flatnonzero(occ.ravel()).astype(np.uint32))
+    np.testing.assert_array_equal(got["start"].astype(np.int64),
+                                  np.concatenate([[0], np.cumsum(occ.sum(axis=1))]))
+
+
+def test_bucketing_bit_exact_near_cell_edges(wgpu_lib, oracle_lib):
+    """Footprint corners within 1e-9 cells (or planes) of an integer: the FP32
+    test cannot decide these samples and leaves them to the FP64 pass, whose
+    corners and fractions must still equal the oracle's."""
+    rng = np.random.default_rng(7)
+    W, dl, n = 256, 3e-4, 4000
+    uvw, freq, _ = synthetic.random_points(n, 1, W, dl, 7, w_scale=2.0)
+    p = _plan_for(uvw, freq, None, W, dl, 1e-4)
+    fl = freq[0] / C
+    su, sv = fl * dl * p.nu, fl * dl * p.nv
+    half = 0.5 * p.support
+    wl = uvw[:, 2] * fl
+    inner = np.ones(n, bool)
+    inner[[int(np.argmin(wl)), int(np.argmax(wl))]] = False  # keep the w range
+    d = rng.choice([-1e-9, 0.0, 1e-9], size=(n, 3))
+    u = (np.round(uvw[:, 0] * su - half) + half + d[:, 0]) / su
+    v = (np.round(uvw[:, 1] * sv - half) + half + d[:, 1]) / sv
+    uvw[inner, 0] = u[inner]
+    uvw[inner, 1] = v[inner]
+    assert p.n_planes > 1
+    q = np.round((wl - p.w0) / p.dw - half)
+    w = ((q + half + d[:, 2]) * p.dw + p.w0) / fl
+    uvw[inner, 2] = w[inner]
+    got = bucket_debug(p, n, 1, uvw, freq, None, False)
+    ref = oracle_lib.bucket(p, uvw, freq, None, False)
+    for k in ("perm", "iu", "iv", "ip", "fu", "fv", "fw"):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(got["offsets"].astype(np.int64), ref["offsets"])
 
 
 INV_CASES = [

@@ -130,6 +130,7 @@ _PROTOS = {
     "wgpu_selftest_bounded_wait": (I, [D]),
     "wgpu_bucket_debug": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P, P, P, P, P,
                               C.POINTER(C.c_int64)]),
+    "wgpu_bucket_debug_rows": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P]),
     "wgpu_bucket_noalloc": (I, [C.POINTER(Plan), SZ, SZ, P, P, P, I, P, P, P, P,
                                 C.POINTER(C.c_int64)]),
     "wgpu_bucket_noalloc_scratch_bytes": (SZ, []),

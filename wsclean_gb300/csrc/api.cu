@@ -1018,12 +1018,13 @@ int wgpu_gridder_predict_bound_device(wgpu_gridder_t *g, float *d_vis) {
   return guarded([&] { predict_bound(g, d_vis, true); });
 }
 
-int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
-                      const double *uvw, const double *freq, const float *vis,
-                      int skip_zero, uint32_t *perm, int32_t *iu, int32_t *iv,
-                      int32_t *ip, float *fu, float *fv, float *fw,
-                      uint32_t *offsets, int64_t *n_out) {
-  if (!plan || !uvw || !freq || !n_out) return fail(WGPU_ERR_INVALID, "null argument");
+static int bucket_debug_impl(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                             const double *uvw, const double *freq, const float *vis,
+                             int skip_zero, uint32_t *perm, int32_t *iu, int32_t *iv,
+                             int32_t *ip, float *fu, float *fv, float *fw, uint32_t *offsets,
+                             int64_t *n_out, uint8_t *row_flags, uint32_t *row_start,
+                             uint32_t *row_list) {
+  if (!plan || !uvw || !freq) return fail(WGPU_ERR_INVALID, "null argument");
   if (skip_zero && !vis) return fail(WGPU_ERR_INVALID, "inversion bucketing needs vis");
   return guarded([&] {
     int n_dev = 0;
@@ -1063,13 +1064,44 @@ int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
         if (fv) fv[k] = rec[k].fv;
         if (fw) fw[k] = rec[k].fw;
       }
-      *n_out = b.n_out;
+      const RowOccupancy &o = b.rows;
+      if (row_flags)
+        WGPU_CUDA(cudaMemcpy(row_flags, o.flags(), o.cells(), cudaMemcpyDeviceToHost));
+      std::vector<uint32_t> st((size_t)o.n_planes + 1, 0);
+      if (o.n_planes > 0)
+        WGPU_CUDA(cudaMemcpy(st.data(), o.start(), sizeof(uint32_t) * st.size(),
+                             cudaMemcpyDeviceToHost));
+      if (row_start) std::copy(st.begin(), st.end(), row_start);
+      if (row_list && st.back() > 0)
+        WGPU_CUDA(cudaMemcpy(row_list, o.list(), sizeof(uint32_t) * st.back(),
+                             cudaMemcpyDeviceToHost));
+      if (n_out) *n_out = b.n_out;
     } catch (...) {
       cudaStreamDestroy(s);
       throw;
     }
     cudaStreamDestroy(s);
   });
+}
+
+
+int wgpu_bucket_debug(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                      const double *uvw, const double *freq, const float *vis,
+                      int skip_zero, uint32_t *perm, int32_t *iu, int32_t *iv,
+                      int32_t *ip, float *fu, float *fv, float *fw,
+                      uint32_t *offsets, int64_t *n_out) {
+  if (!n_out) return fail(WGPU_ERR_INVALID, "null argument");
+  return bucket_debug_impl(plan, n_rows, n_chan, uvw, freq, vis, skip_zero, perm, iu, iv, ip,
+                           fu, fv, fw, offsets, n_out, nullptr, nullptr, nullptr);
+}
+
+int wgpu_bucket_debug_rows(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
+                           const double *uvw, const double *freq, const float *vis,
+                           int skip_zero, uint8_t *row_flags, uint32_t *row_start,
+                           uint32_t *row_list) {
+  return bucket_debug_impl(plan, n_rows, n_chan, uvw, freq, vis, skip_zero, nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                           row_flags, row_start, row_list);
 }
 
 }  // extern "C"

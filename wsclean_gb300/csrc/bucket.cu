@@ -26,6 +26,7 @@ constexpr int kThreads = 256;
 
 struct ChannelScale {
   double su, sv, sw;  // U = uvw_u * su (cells), V = uvw_v * sv, w = uvw_w * sw
+  float fsu, fsv, fsw, pad;  // the same rounded to float (FP32 footprint tests)
 };
 
 __global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
@@ -37,6 +38,26 @@ __global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
   out[c].su = __dmul_rn(fl, gu);
   out[c].sv = __dmul_rn(fl, gv);
   out[c].sw = fl;
+  out[c].fsu = __double2float_rn(out[c].su);
+  out[c].fsv = __double2float_rn(out[c].sv);
+  out[c].fsw = __double2float_rn(fl);
+  out[c].pad = 0.f;
+}
+
+// uvw rows rounded to float (FP32 footprint tests), one float4 per row.
+__global__ void uvw_float_kernel(const double *__restrict__ uvw, int64_t n_rows,
+                                 float4 *__restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  out[r] = make_float4(__double2float_rn(uvw[3 * r]), __double2float_rn(uvw[3 * r + 1]),
+                       __double2float_rn(uvw[3 * r + 2]), 0.f);
+}
+
+// The float row of sample row r: from the table when there is one.
+__device__ __forceinline__ float4 row_float(const float4 *uvwf, const double *uvw, int64_t r) {
+  if (uvwf) return __ldg(uvwf + r);
+  return make_float4(__double2float_rn(uvw[3 * r]), __double2float_rn(uvw[3 * r + 1]),
+                     __double2float_rn(uvw[3 * r + 2]), 0.f);
 }
 
 }  // namespace
@@ -106,10 +127,11 @@ __device__ __forceinline__ Footprint footprint(const DevPlan &p,
 // left to the FP64 pass.
 constexpr float kTwoM22 = 2.384185791015625e-07f;  // 2^-22
 
-// ceil of x = fl64(fl64(a * s) - h), or false when the FP32 value is too
-// close to an integer (or out of int range) to decide.
-__device__ __forceinline__ bool ceil_decided(double a, double s, float h, int *c) {
-  const float x = __fsub_rn(__fmul_rn(__double2float_rn(a), __double2float_rn(s)), h);
+// ceil of x = fl64(fl64(a * s) - h) from a and s rounded to float, or false
+// when the FP32 value is too close to an integer (or out of int range) to
+// decide.
+__device__ __forceinline__ bool ceil_decided(float a, float s, float h, int *c) {
+  const float x = __fsub_rn(__fmul_rn(a, s), h);
   const float eb = kTwoM22 * (fabsf(x) + h) + 1e-6f;
   if (!(fabsf(x) < 1.0e9f)) return false;
   const float fx = floorf(x);
@@ -129,17 +151,17 @@ __device__ __forceinline__ bool wrap_decided(int c, int n, int *out) {
 
 // Key (and corner row / first plane) of a sample decided in FP32; false
 // when any of the three corners needs the FP64 footprint.
-__device__ __forceinline__ bool key_decided(const DevPlan &p, const double *uvw_row,
+__device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
                                             const ChannelScale &cs, uint32_t *key, int *iv_out,
                                             int *ip_out) {
   const float half = 0.5f * (float)p.support;
   int iu0, iv0, iu, iv, ip = 0;
-  if (!ceil_decided(uvw_row[0], cs.su, half, &iu0) || !ceil_decided(uvw_row[1], cs.sv, half, &iv0))
+  if (!ceil_decided(rf.x, cs.fsu, half, &iu0) || !ceil_decided(rf.y, cs.fsv, half, &iv0))
     return false;
   if (!wrap_decided(iu0, p.nu, &iu) || !wrap_decided(iv0, p.nv, &iv)) return false;
   if (p.n_planes > 1) {
-    const float wl = __fmul_rn(__double2float_rn(uvw_row[2]), __double2float_rn(cs.sw));
-    const float w0 = __double2float_rn(p.w0), idw = __double2float_rn(p.inv_dw);
+    const float wl = __fmul_rn(rf.z, cs.fsw);
+    const float w0 = p.w0f, idw = p.inv_dwf;
     const float d = __fsub_rn(wl, w0);
     const float pw = __fmul_rn(d, idw);
     const float y = __fsub_rn(pw, half);
@@ -257,7 +279,7 @@ __global__ void __launch_bounds__(kThreads)
                Selector sel, int64_t n_rows, int64_t n_chan,
                uint32_t sentinel, uint32_t *keys,
                uint32_t *vals, uint32_t *counts, uint8_t *corners,
-               uint32_t *pending, uint32_t *n_pending) {
+               uint32_t *pending, uint32_t *n_pending, const float4 *__restrict__ uvwf) {
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
@@ -266,7 +288,7 @@ __global__ void __launch_bounds__(kThreads)
   bool defer = false;
   if (sel(e)) {
     int iv, ip;
-    if (key_decided(p, uvw + 3 * r, cs[c], &key, &iv, &ip)) {
+    if (key_decided(p, row_float(uvwf, uvw, r), cs[c], &key, &iv, &ip)) {
       if (corners) corners[(size_t)ip * p.nv + iv] = 1;
     } else {
       defer = true;
@@ -384,10 +406,11 @@ __global__ void __launch_bounds__(kThreads)
 // Footprint of a record: corners decided in FP32 where possible (see
 // key_decided), fractions from the FP64 coordinates; identical to footprint().
 __device__ __forceinline__ Footprint record_footprint(const DevPlan &p, const double *row,
-                                                      const ChannelScale &cs, double *wl_out) {
+                                                      const float4 rf, const ChannelScale &cs,
+                                                      double *wl_out) {
   const float half = 0.5f * (float)p.support;
   int iu0, iv0, iu, iv;
-  bool ok = ceil_decided(row[0], cs.su, half, &iu0) && ceil_decided(row[1], cs.sv, half, &iv0) &&
+  bool ok = ceil_decided(rf.x, cs.fsu, half, &iu0) && ceil_decided(rf.y, cs.fsv, half, &iv0) &&
             wrap_decided(iu0, p.nu, &iu) && wrap_decided(iv0, p.nv, &iv);
   Footprint f;
   double wl = 0.0, pw = 0.0;
@@ -395,8 +418,8 @@ __device__ __forceinline__ Footprint record_footprint(const DevPlan &p, const do
   if (ok && p.n_planes > 1) {
     wl = __dmul_rn(row[2], cs.sw);
     pw = __dmul_rn(__dsub_rn(wl, p.w0), p.inv_dw);
-    const float wlf = __fmul_rn(__double2float_rn(row[2]), __double2float_rn(cs.sw));
-    const float w0 = __double2float_rn(p.w0), idw = __double2float_rn(p.inv_dw);
+    const float wlf = __fmul_rn(rf.z, cs.fsw);
+    const float w0 = p.w0f, idw = p.inv_dwf;
     const float d = __fsub_rn(wlf, w0);
     const float pwf = __fmul_rn(d, idw);
     const float y = __fsub_rn(pwf, half);
@@ -445,7 +468,7 @@ template <bool SHIFT>
 __global__ void __launch_bounds__(kThreads)
     record_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
                   const float2 *vis, int64_t n_chan, const uint32_t *perm,
-                  int64_t n_out, VisRecord *rec) {
+                  int64_t n_out, VisRecord *rec, const float4 *__restrict__ uvwf) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_out) return;
   const uint32_t e = perm[s];
@@ -453,7 +476,7 @@ __global__ void __launch_bounds__(kThreads)
   const double *row = uvw + 3 * r;
   const ChannelScale sc = cs[c];
   double wl;
-  const Footprint f = record_footprint(p, row, sc, &wl);
+  const Footprint f = record_footprint(p, row, row_float(uvwf, uvw, r), sc, &wl);
   // shift phase theta = u l_shift + v m_shift + w c_n (turns), FP64 argument,
   // reduced to [-1/2, 1/2] before the FP32 sincos.  Without shifts the first
   // two terms are zero and theta = fl(w f / c) c_n, the same value.
@@ -637,6 +660,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   const uint32_t sentinel = (uint32_t)(((uint64_t)1 << bits) - 1);
 
   ChannelScale *cs = (ChannelScale *)arena.get(kSlotExtent, sizeof(ChannelScale) * (n_chan + 1) + 64);
+  float4 *uvwf = (float4 *)arena.get(kSlotUvwF32, sizeof(float4) * (n_rows + 1));
   uint32_t *keys = (uint32_t *)arena.get(kSlotKeys, sizeof(uint32_t) * (n + 1));
   uint32_t *keys2 = (uint32_t *)arena.get(kSlotKeysAlt, sizeof(uint32_t) * (n + 1));
   uint32_t *vals = (uint32_t *)arena.get(kSlotVals, sizeof(uint32_t) * (n + 1));
@@ -658,9 +682,12 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     // their count in the word after the channel scales
     uint32_t *n_pending = (uint32_t *)(cs + n_chan + 1);
     WGPU_CUDA(cudaMemsetAsync(n_pending, 0, sizeof(uint32_t), s));
+    uvw_float_kernel<<<grid_for(n_rows, kThreads), kThreads, 0, s>>>(d_uvw, n_rows, uvwf);
+    check_launch("uvw_float_kernel");
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
-        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners(), keys2, n_pending);
+        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners(), keys2, n_pending,
+        uvwf);
     check_launch("key_kernel");
     key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, n_pending,
                                                         keys, offsets, res.rows.corners());
@@ -697,7 +724,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     (shift ? record_kernel<true> : record_kernel<false>)<<<grid_for(res.n_out, kThreads),
                                                           kThreads, 0, s>>>(
         p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan,
-        res.perm, res.n_out, res.records);
+        res.perm, res.n_out, res.records, uvwf);
     check_launch("record_kernel");
   }
   return res;
@@ -804,7 +831,7 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
     WGPU_CUDA(cudaMemsetAsync(vals2, 0, sizeof(uint32_t), s));
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, nullptr}, n_rows,
-        n_chan, sentinel, keys, vals, d_offsets, nullptr, keys2, vals2);
+        n_chan, sentinel, keys, vals, d_offsets, nullptr, keys2, vals2, nullptr);
     check_launch("key_kernel");
     key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, vals2, keys,
                                                         d_offsets, nullptr);
@@ -833,7 +860,7 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
     (shift ? record_kernel<true> : record_kernel<false>)<<<grid_for(total, kThreads), kThreads,
                                                           0, s>>>(
         p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan, vin, total,
-        d_records);
+        d_records, nullptr);
     check_launch("record_kernel");
   }
   WGPU_CUDA(cudaStreamSynchronize(s));

@@ -285,6 +285,8 @@ DevPlan to_dev_plan(const wgpu_plan_t &p) {
   d.dw = p.dw;
   d.inv_dw = p.n_planes > 1 ? 1.0 / p.dw : 0.0;
   d.nm1_center = p.nm1_center;
+  d.w0f = (float)d.w0;
+  d.inv_dwf = (float)d.inv_dw;
   return d;
 }
 

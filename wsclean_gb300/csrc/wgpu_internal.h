@@ -59,6 +59,7 @@ static_assert(sizeof(VisRecord) == 32, "record layout");
 struct DevPlan {
   int nu, nv, width, height, support, tile, ntu, ntv, n_planes;
   float beta;
+  float w0f, inv_dwf;  // w0 and inv_dw rounded to float (FP32 footprint tests)
   double dl, dm, l_shift, m_shift, w0, dw, inv_dw, nm1_center;
 };
 
@@ -349,6 +350,7 @@ enum ArenaSlot {
   kSlotItemDesc,
   kSlotSpill,
   kSlotRowOcc,
+  kSlotUvwF32,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.

@@ -217,3 +217,21 @@ def bucket_debug(plan, n_rows, n_chan, uvw, freq, vis, skip_zero):
     k = n_out.value
     return dict(perm=perm[:k], iu=iu[:k], iv=iv[:k], ip=ip[:k], fu=fu[:k], fv=fv[:k],
                 fw=fw[:k], offsets=off)
+
+
+def bucket_debug_rows(plan, n_rows, n_chan, uvw, freq, vis, skip_zero):
+    """Row occupancy of the bucketing pass (wgpu_bucket_debug_rows): flags
+    [n_planes, nv] uint8, start [n_planes + 1] and the row list."""
+    uvw = _f64(uvw)
+    freq = _f64(freq)
+    if vis is not None:
+        vis = _c64(vis)
+    cells = int(plan.n_planes) * int(plan.nv)
+    flags = np.zeros(cells, np.uint8)
+    start = np.zeros(int(plan.n_planes) + 1, np.uint32)
+    rows = np.zeros(cells, np.uint32)
+    check(lib().wgpu_bucket_debug_rows(C.byref(plan), n_rows, n_chan, ptr(uvw), ptr(freq),
+                                       ptr(vis), 1 if skip_zero else 0, ptr(flags), ptr(start),
+                                       ptr(rows)))
+    return dict(flags=flags.reshape(int(plan.n_planes), int(plan.nv)), start=start,
+                list=rows[:int(start[-1])])
