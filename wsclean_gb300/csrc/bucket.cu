@@ -354,29 +354,59 @@ __global__ void __launch_bounds__(kThreads)
   hist[(int64_t)threadIdx.x * n_blocks + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable scatter of one 8-bit digit.  Each block first orders its tile of
+// kSortTile elements by digit in shared memory (stable: rank by round, warp
+// and lane), then writes each digit's run to its global range, so that
+// consecutive threads write consecutive addresses.  hist holds the exclusive
+// scan of the per-(digit, block) counts (digit-major); a tile's own count of
+// digit d is the difference to the next entry (n after the last).
 __global__ void __launch_bounds__(kThreads)
     radix_scatter_kernel(const uint32_t *keys_in, const uint32_t *vals_in,
                          int64_t n, int shift, const uint32_t *hist,
                          int64_t n_blocks, uint32_t *keys_out,
                          uint32_t *vals_out) {
-  __shared__ uint32_t base[256];
-  __shared__ uint32_t run[256];
+  __shared__ uint32_t base[256];    // global position of the tile's first element of digit d
+  __shared__ uint32_t tstart[256];  // first position of digit d in the tile's sorted order
+  __shared__ uint32_t run[256];     // elements of digit d placed by earlier rounds
   __shared__ uint32_t wcnt[kThreads / 32][256];
+  __shared__ uint32_t wsum[kThreads / 32];
+  __shared__ uint32_t skey[kSortTile], sval[kSortTile];
+  static_assert(kThreads == 256, "one thread per digit");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  base[threadIdx.x] = hist[(int64_t)threadIdx.x * n_blocks + blockIdx.x];
-  run[threadIdx.x] = 0;
   const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
+  const int tile_n = (int)min((int64_t)kSortTile, n - tile0);
+  {
+    const int64_t at = (int64_t)threadIdx.x * n_blocks + blockIdx.x;
+    const uint32_t b0 = hist[at];
+    const uint32_t b1 = (threadIdx.x == 255 && blockIdx.x == n_blocks - 1) ? (uint32_t)n
+                                                                           : hist[at + 1];
+    base[threadIdx.x] = b0;
+    run[threadIdx.x] = 0;
+    // exclusive scan of the tile's digit counts (one digit per thread)
+    const uint32_t cnt = b1 - b0;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    tstart[threadIdx.x] = before + x - cnt;
+  }
   const unsigned lt_mask = (1u << lane) - 1u;
   for (int r = 0; r < kSortItems; ++r) {
 #pragma unroll
     for (int w = 0; w < kThreads / 32; ++w) wcnt[w][threadIdx.x] = 0;
     __syncthreads();
-    const int64_t i = tile0 + r * kThreads + threadIdx.x;
-    const bool valid = i < n;
+    const int t = r * kThreads + threadIdx.x;
+    const bool valid = t < tile_n;
     uint32_t key = 0, val = 0, d = 256;
     if (valid) {
-      key = keys_in[i];
-      val = vals_in[i];
+      key = keys_in[tile0 + t];
+      val = vals_in[tile0 + t];
       d = (key >> shift) & 255u;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -387,19 +417,26 @@ __global__ void __launch_bounds__(kThreads)
       uint32_t acc = run[threadIdx.x];
 #pragma unroll
       for (int w = 0; w < kThreads / 32; ++w) {
-        const uint32_t t = wcnt[w][threadIdx.x];
+        const uint32_t c = wcnt[w][threadIdx.x];
         wcnt[w][threadIdx.x] = acc;
-        acc += t;
+        acc += c;
       }
       run[threadIdx.x] = acc;
     }
     __syncthreads();
     if (valid) {
-      const uint32_t pos = base[d] + wcnt[warp][d] + rank;
-      keys_out[pos] = key;
-      vals_out[pos] = val;
+      const uint32_t pos = tstart[d] + wcnt[warp][d] + rank;
+      skey[pos] = key;
+      sval[pos] = val;
     }
-    __syncthreads();
+    __syncthreads();  // wcnt is cleared for the next round
+  }
+  for (int j = threadIdx.x; j < tile_n; j += kThreads) {
+    const uint32_t key = skey[j];
+    const uint32_t d = (key >> shift) & 255u;
+    const uint32_t out = base[d] + ((uint32_t)j - tstart[d]);
+    keys_out[out] = key;
+    vals_out[out] = sval[j];
   }
 }
 
