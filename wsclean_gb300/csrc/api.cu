@@ -192,6 +192,7 @@ struct wgpu_gridder {
   StageTimer timer;
   std::vector<StageTimer::Stage> last_timings;
   std::string corr_key;  // geometry of the correction tables in the arena
+  std::string nuw_key;   // geometry (and buffer) of the n - 1 table in the arena
   std::unique_ptr<BoundState> bound;
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
   unsigned *d_flags = nullptr;  // device: expired bounded waits
@@ -254,6 +255,21 @@ void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
   // the host vectors die at return: make the copies complete first
   WGPU_CUDA(cudaStreamSynchronize(g->stream));
   g->corr_key = key;
+}
+
+// Per-pixel n - 1 - c_n table (FP64) of the plan's image geometry, in the
+// arena; recomputed only when that geometry or the buffer changes.
+double *nu_table_for(wgpu_gridder *g, const wgpu_plan_t &plan, const DevPlan &dp) {
+  double *nu_w = (double *)g->arena.get(kSlotNuW, sizeof(double) * plan.width * plan.height);
+  char key[320];
+  std::snprintf(key, sizeof(key), "%p/%lld/%lld/%.17g/%.17g/%.17g/%.17g/%.17g", (void *)nu_w,
+                (long long)plan.width, (long long)plan.height, plan.dl, plan.dm, plan.l_shift,
+                plan.m_shift, plan.nm1_center);
+  if (g->nuw_key != key) {
+    launch_nu_table(dp, nu_w, g->stream);
+    g->nuw_key = key;
+  }
+  return nu_w;
 }
 
 // A pinned plan is used as long as it covers the data: every visibility's w
@@ -343,12 +359,11 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
-  double *nu_w = (double *)g->arena.get(kSlotNuW, sizeof(double) * npix);
+  double *nu_w = nu_table_for(g, plan, dp);
   float2 *acc = (float2 *)g->arena.get(kSlotAcc, sizeof(float2) * npix);
   const int64_t B = plan.plane_batch;
   float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
   float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
-  launch_nu_table(dp, nu_w, s);
   WGPU_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * npix, s));
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
@@ -404,13 +419,12 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
-  double *nu_w = (double *)g->arena.get(kSlotNuW, sizeof(double) * npix);
+  double *nu_w = nu_table_for(g, plan, dp);
   float *img_corr = (float *)g->arena.get(kSlotImgCorr, sizeof(float) * npix);
   float2 *vacc = (float2 *)g->arena.get(kSlotVisAcc, sizeof(float2) * (b.n_out + 1));
   const int64_t B = plan.plane_batch;
   float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
   float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
-  launch_nu_table(dp, nu_w, s);
   float *cx, *cy, *gl;
   upload_corrections(g, plan, &cx, &cy, &gl);
   launch_precorrect(dp, g->d_img, g->prec, nu_w, cx, cy, gl, kGlNodes, img_corr, s);
