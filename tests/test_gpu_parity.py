@@ -179,6 +179,46 @@ def test_inversion_in_chunks_with_trim_and_descending_freq(wgpu_lib, oracle_lib)
     g.close()
 
 
+# Grid sizes whose column split n1 x n2 uses the two-stage panel transforms
+# (lengths 16 R2, R2 in 2, 3, 4, 5, 6, 8), with sigma pinned to 1.5.
+PANEL_CASES = [
+    dict(W=1024, dl=6e-5, split=(32, 48)),
+    dict(W=2048, dl=3e-5, split=(48, 64)),
+    dict(W=5120, dl=1.2e-5, split=(80, 96)),
+    dict(W=8192, dl=8e-6, split=(96, 128)),
+]
+
+
+@pytest.mark.parametrize("case", PANEL_CASES)
+def test_two_stage_column_transforms_match_dft(wgpu_lib, oracle_lib, case):
+    """Inversion and prediction through the two-stage column passes against the
+    FP64 direct transform (sampled pixels and visibilities), eps = 1e-5."""
+    W, dl, eps = case["W"], case["dl"], 1e-5
+    uvw, freq, vis = synthetic.random_points(800, 4, W, dl, seed=9, w_scale=0.5)
+    wl = uvw[:, 2:3] * (freq / C)[None, :]
+    p = _lib.make_plan(width=W, height=W, dl=dl, dm=dl, epsilon=eps, w_min=float(wl.min()),
+                       w_max=float(wl.max()), n_vis=int(wl.size), force_sigma=1.5)
+    assert (p.fft_n1, p.fft_n2) == case["split"]
+    rng = np.random.default_rng(11)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=eps, num_t=np.float64)
+    g.pin_plan(p)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    g.FinalizeImage(1.0)
+    img = g.RealImage().astype(np.float64).ravel()
+    pix = rng.choice(W * W, size=4096, replace=False)
+    ref = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, pixels=pix)
+    assert rel(img[pix], ref) <= eps
+    model = np.zeros(W * W, np.float32)
+    src = rng.choice(W * W, size=6, replace=False)
+    model[src] = rng.uniform(-1, 1, 6)
+    g.InitializePrediction(model)
+    pv = g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq).ravel()
+    pr = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl)
+    assert rel(pv, np.asarray(pr).ravel()) <= eps
+    g.close()
+
+
 PRED_CASES = [
     dict(W=128, dl=4e-4, eps=1e-4, shift=(0.0, 0.0), w_scale=3.0, n_src=12),
     dict(W=256, dl=2e-4, eps=1e-5, shift=(0.01, -0.005), w_scale=2.0, n_src=40),

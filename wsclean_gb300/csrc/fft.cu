@@ -216,6 +216,24 @@ __device__ __forceinline__ void dft<5>(float2 *x, float s) {
   x[3] = csub(r2, i2);
 }
 
+// 6 = 2 x 3: E = DFT3 of the even inputs, O of the odd ones; X[k] = E[k] +
+// w6^k O[k], X[k + 3] = E[k] - w6^k O[k] (k < 3), w6 = exp(s 2 pi i / 6).
+template <>
+__device__ __forceinline__ void dft<6>(float2 *x, float s) {
+  constexpr float h = 0.86602540378443864676f;  // sin(pi / 3)
+  float2 e[3] = {x[0], x[2], x[4]}, o[3] = {x[1], x[3], x[5]};
+  dft<3>(e, s);
+  dft<3>(o, s);
+  const float2 o1 = make_float2(0.5f * o[1].x - s * h * o[1].y, 0.5f * o[1].y + s * h * o[1].x);
+  const float2 o2 = make_float2(-0.5f * o[2].x - s * h * o[2].y, -0.5f * o[2].y + s * h * o[2].x);
+  x[0] = cadd(e[0], o[0]);
+  x[3] = csub(e[0], o[0]);
+  x[1] = cadd(e[1], o1);
+  x[4] = csub(e[1], o1);
+  x[2] = cadd(e[2], o2);
+  x[5] = csub(e[2], o2);
+}
+
 // Layout of the transforms a CTA holds in shared memory.
 //   kRow:   one transform, element k at s[row_slot(k)]: the low four bits of
 //           k are XORed with bits 4-7, which puts the strided accesses of
@@ -884,6 +902,205 @@ __global__ void __launch_bounds__(kColThreads, 2)
   }
 }
 
+// ---------------------------------------------- two-stage panel transforms ----
+// Column transforms of length N = 16 R2 (R2 <= 8) over a panel of 32 columns,
+// in two Stockham stages and one shared-memory round trip:
+//   stage 1, radix 16 (p = 1): butterfly (i < R2, column b) takes panel rows
+//     i + t R2 (t < 16) straight from `load` into registers and writes its
+//     outputs to s[(16 i + q) * 32 + b];
+//   stage 2, radix R2 (p = 16): butterfly (i < 16, b) reads s[(i + 16 t) * 32 +
+//     b], twiddles by exp(sign 2 pi i t i / N), and hands output row i + 16 q
+//     (natural order) to `store`.
+// kPanelThreads threads: stage 1 has R2 * 32 <= 256 butterflies, stage 2 has
+// 512, two per thread (slot = it * R2 + q numbers a thread's outputs).
+constexpr int kPanelThreads = 256;
+
+template <int R2, class Load, class Store>
+__device__ __forceinline__ void panel_fft(float2 *__restrict__ s, float sign,
+                                          const float2 *__restrict__ tw, Load load, Store store) {
+  const int b = threadIdx.x & 31;
+  if (threadIdx.x < R2 * 32) {
+    const int i = threadIdx.x >> 5;
+    float2 v[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) v[t] = load(t, i + t * R2, b);
+    dft<16>(v, sign);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) s[(16 * i + q) * 32 + b] = v[q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const int i = (threadIdx.x >> 5) + 8 * it;
+    float2 v[R2];
+#pragma unroll
+    for (int t = 0; t < R2; ++t) v[t] = s[(i + 16 * t) * 32 + b];
+    if (i > 0) {
+#pragma unroll
+      for (int t = 1; t < R2; ++t) {
+        float2 w = __ldg(tw + t * i);  // exp(-2 pi i t i / N)
+        w.y *= -sign;
+        v[t] = cmul(v[t], w);
+      }
+    }
+    dft<R2>(v, sign);
+#pragma unroll
+    for (int q = 0; q < R2; ++q) store(it * R2 + q, i + 16 * q, b, v[q]);
+  }
+}
+
+// Pass A / A' with the two-stage panel transform (n1 = 16 R2): panel row e is
+// row r2 + n2 e of plane blockIdx.z; forward reads unflagged rows as zeros and
+// applies the four-step twiddle w_nv^(r2 k1), backward writes flagged rows only.
+template <int R2>
+__global__ void __launch_bounds__(kPanelThreads)
+    fft_cols_pass_a16_kernel(float2 *__restrict__ R, int rstride, int nv, int n2, float sign,
+                             const float2 *__restrict__ tw1, const float2 *__restrict__ twN,
+                             const uint8_t *__restrict__ flags) {
+  __shared__ float2 s[16 * R2 * 32];
+  const int cg = blockIdx.x, r2 = blockIdx.y;
+  float2 *base = R + (size_t)blockIdx.z * nv * rstride + cg * kPanel;
+  const uint8_t *fl = flags ? flags + (size_t)blockIdx.z * nv : nullptr;
+  const bool fwd = sign < 0;
+  auto load = [&](int, int e, int c) -> float2 {
+    const int row = r2 + n2 * e;
+    if (fwd && fl && !__ldg(fl + row)) return make_float2(0.f, 0.f);
+    return __ldg(base + (size_t)row * rstride + c);
+  };
+  auto store = [&](int, int k1, int c, float2 v) {
+    const int row = r2 + n2 * k1;
+    if (fwd) {
+      v = cmul(v, __ldg(twN + r2 * k1));  // r2 k1 < nv
+      base[(size_t)row * rstride + c] = v;
+    } else if (!fl || __ldg(fl + row)) {
+      base[(size_t)row * rstride + c] = v;
+    }
+  };
+  panel_fft<R2>(s, sign, tw1, load, store);
+}
+
+// Shared bytes of the two-stage pass B kernels: the FFT buffer (n2 * kPanel
+// float2) and the phase terms a, bh, bl (n2 * kPanel floats each).
+__host__ __device__ constexpr size_t cols_b16_smem(int n2) {
+  return (size_t)n2 * kPanel * (sizeof(float2) + 3 * sizeof(float));
+}
+
+// Pass B (forward, n2 = 16 R2) with the fused w-screen: a thread's stage-2
+// outputs (slot it R2 + q: row (tid >> 5) + 8 it + 16 q, column tid & 31) are
+// the same for every plane, so their screened real parts sum over the batch in
+// registers and go once into the image accumulator (Kahan).  flags (set only
+// when no pass A ran before): unflagged rows of R read as zeros.
+template <int R2>
+__global__ void __launch_bounds__(kPanelThreads, 2)
+    fft_cols_forward_accumulate16_kernel(DevPlan p, int n1, float2 *__restrict__ R, int rstride,
+                                         int n_batch, int p_begin,
+                                         const double *__restrict__ nu_w,
+                                         float2 *__restrict__ acc,
+                                         const float2 *__restrict__ tw2,
+                                         const uint8_t *__restrict__ flags) {
+  extern __shared__ float2 s[];
+  constexpr int N = 16 * R2, ne = N * kPanel;
+  const int nv = p.nv;
+  const int cg = blockIdx.x, k1 = blockIdx.y;
+  float *pa = reinterpret_cast<float *>(s + ne);
+  float *pbh = pa + ne, *pbl = pbh + ne;
+  cols_b_phases(p, n1, N, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  float part[2 * R2];
+#pragma unroll
+  for (int c = 0; c < 2 * R2; ++c) part[c] = 0.f;
+  for (int b = 0; b < n_batch; ++b) {
+    const float2 *base = R + (size_t)b * nv * rstride + (size_t)N * k1 * rstride + cg * kPanel;
+    const uint8_t *fl = flags ? flags + (size_t)b * nv + (size_t)N * k1 : nullptr;
+    auto load = [&](int, int e, int c) -> float2 {
+      if (fl && !__ldg(fl + e)) return make_float2(0.f, 0.f);
+      return __ldg(base + (size_t)e * rstride + c);
+    };
+    auto store = [&](int slot, int k2, int c, float2 v) {
+      const int e = k2 * kPanel + c;
+      const float a = pa[e];
+      if (a != kNoPixel) {
+        float sn, cs;
+        screen_b(a, pbh[e], pbl[e], b, &sn, &cs);
+        // Re(v exp(-2 pi i t)) = v.re cos + v.im sin
+        part[slot] += v.x * cs + v.y * sn;
+      }
+    };
+    panel_fft<R2>(s, -1.0f, tw2, load, store);
+    __syncthreads();  // the next plane's stage 1 rewrites s
+  }
+  const int col = threadIdx.x & 31;
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+#pragma unroll
+    for (int q = 0; q < R2; ++q) {
+      const int k2 = (threadIdx.x >> 5) + 8 * it + 16 * q;
+      const int e = k2 * kPanel + col;
+      if (pa[e] != kNoPixel) {
+        const int x = cg * kPanel + col;
+        const int y = image_row_of(k1 + n1 * k2, nv, p.height);
+        float2 *a = acc + (size_t)y * p.width + x;
+        float2 sc = *a;  // (sum, compensation)
+        const float yv = part[it * R2 + q] - sc.y;
+        const float t = sc.x + yv;
+        sc.y = (t - sc.x) - yv;
+        sc.x = t;
+        *a = sc;
+      }
+    }
+  }
+}
+
+// Pass B' (backward, n2 = 16 R2): screened, pre-corrected image rows -> length
+// n2 backward transforms -> twiddle -> R rows n2 k1 + r2.  A stage-1 thread
+// keeps the 16 image values it feeds (rows i + t R2 of its column).
+template <int R2>
+__global__ void __launch_bounds__(kPanelThreads, 2)
+    fft_cols_backward_screen16_kernel(DevPlan p, int n1, const float *__restrict__ img_corr,
+                                      const double *__restrict__ nu_w, float2 *__restrict__ R,
+                                      int rstride, int n_batch, int p_begin,
+                                      const float2 *__restrict__ tw2,
+                                      const float2 *__restrict__ twN) {
+  extern __shared__ float2 s[];
+  constexpr int N = 16 * R2, ne = N * kPanel;
+  const int nv = p.nv;
+  const int cg = blockIdx.x, k1 = blockIdx.y;
+  float *pa = reinterpret_cast<float *>(s + ne);
+  float *pbh = pa + ne, *pbl = pbh + ne;
+  cols_b_phases(p, n1, N, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  const int col = threadIdx.x & 31, i1 = threadIdx.x >> 5;
+  float val[16];
+#pragma unroll
+  for (int t = 0; t < 16; ++t) {
+    val[t] = 0.f;
+    if (i1 < R2) {
+      const int x = cg * kPanel + col;
+      const int y = image_row_of(k1 + n1 * (i1 + t * R2), nv, p.height);
+      if (x < p.width && y >= 0) val[t] = __ldg(img_corr + (size_t)y * p.width + x);
+    }
+  }
+  __syncthreads();  // phase terms
+  for (int b = 0; b < n_batch; ++b) {
+    float2 *base = R + (size_t)b * nv * rstride + (size_t)N * k1 * rstride + cg * kPanel;
+    auto load = [&](int t, int e, int c) -> float2 {
+      if (val[t] == 0.0f) return make_float2(0.f, 0.f);
+      const int idx = e * kPanel + c;
+      float sn, cs;
+      screen_b(pa[idx], pbh[idx], pbl[idx], b, &sn, &cs);
+      return make_float2(val[t] * cs, val[t] * sn);  // a exp(+2 pi i t)
+    };
+    auto store = [&](int, int r2, int c, float2 v) {
+      if (n1 > 1) {
+        float2 w = __ldg(twN + r2 * k1);  // r2 < n2, k1 < n1: r2 k1 < nv
+        w.y = -w.y;                        // exp(+2 pi i r2 k1 / nv)
+        v = cmul(v, w);
+      }
+      base[(size_t)r2 * rstride + c] = v;
+    };
+    panel_fft<R2>(s, +1.0f, tw2, load, store);
+    __syncthreads();
+  }
+}
+
 void set_smem(const void *fn, size_t bytes) { ensure_dynamic_smem(fn, bytes); }
 
 int sm_count_fft() {
@@ -1045,11 +1262,40 @@ void launch_fft_rows_backward_pad(FftTables &t, const DevPlan &p,
   launch_rows<false>(t, p, R, rstride, planes, p.nu, n_batch, sel, err, s);
 }
 
+// R2 of the two-stage panel transform of length n, or 0 when n is not 16 R2
+// for R2 in {2, 3, 4, 5, 6, 8} (other lengths use the generic Stockham panel
+// kernels).
+static int panel_r2(int n) {
+  const int r = n % 16 == 0 ? n / 16 : 0;
+  return (r >= 2 && r <= 8 && r != 7) ? r : 0;  // radices with a butterfly: 2, 3, 4, 5, 6, 8
+}
+
+#define WGPU_PANEL_SWITCH(r2, CALL) \
+  switch (r2) {                     \
+    case 2: CALL(2); break;         \
+    case 3: CALL(3); break;         \
+    case 4: CALL(4); break;         \
+    case 5: CALL(5); break;         \
+    case 6: CALL(6); break;         \
+    default: CALL(8); break;        \
+  }
+
 void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
                        int rstride, int n_batch, float sign, const RowSel &sel,
                        cudaStream_t s) {
   if (n1 <= 1) return;
   const int ncg = rstride / kPanel;
+  if (const int r2p = panel_r2(n1)) {
+    dim3 grid(ncg, n2, n_batch);
+    const float2 *tw1 = fft_twiddles(t, n1), *twN = fft_twiddles(t, p.nv);
+#define WGPU_PASS_A16(X)                                                                     \
+  fft_cols_pass_a16_kernel<X><<<grid, kPanelThreads, 0, s>>>(R, rstride, p.nv, n2, sign, tw1, \
+                                                             twN, sel.flags)
+    WGPU_PANEL_SWITCH(r2p, WGPU_PASS_A16)
+#undef WGPU_PASS_A16
+    check_launch("fft_cols_pass_a16_kernel");
+    return;
+  }
   const FftDesc d1 = make_desc(n1);
   const size_t smem = 2 * sizeof(float2) * n1 * kPanel;
   set_smem((const void *)fft_cols_pass_a_kernel, smem);
@@ -1068,6 +1314,19 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
   // transforms left it
   const uint8_t *flags = n1 <= 1 ? sel.flags : nullptr;
   const int ncg = rstride / kPanel;
+  if (const int r2p = panel_r2(n2)) {
+    dim3 grid(ncg, n1);
+    const float2 *tw = fft_twiddles(t, n2);
+    const size_t smem = cols_b16_smem(n2);
+#define WGPU_PASS_B16(X)                                                                  \
+  set_smem((const void *)fft_cols_forward_accumulate16_kernel<X>, smem);                  \
+  fft_cols_forward_accumulate16_kernel<X><<<grid, kPanelThreads, smem, s>>>(              \
+      p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags)
+    WGPU_PANEL_SWITCH(r2p, WGPU_PASS_B16)
+#undef WGPU_PASS_B16
+    check_launch("fft_cols_forward_accumulate16_kernel");
+    return;
+  }
   const FftDesc d2 = make_desc(n2);
   const size_t smem = cols_b_smem(n2);
   dim3 grid(ncg, n1);
@@ -1090,6 +1349,19 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        int rstride, int n_batch, int p_begin,
                                        cudaStream_t s) {
   const int ncg = rstride / kPanel;
+  if (const int r2p = panel_r2(n2)) {
+    dim3 grid(ncg, n1);
+    const float2 *tw = fft_twiddles(t, n2), *twN = fft_twiddles(t, p.nv);
+    const size_t smem = cols_b16_smem(n2);
+#define WGPU_PASS_B16B(X)                                                                 \
+  set_smem((const void *)fft_cols_backward_screen16_kernel<X>, smem);                     \
+  fft_cols_backward_screen16_kernel<X><<<grid, kPanelThreads, smem, s>>>(                 \
+      p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN)
+    WGPU_PANEL_SWITCH(r2p, WGPU_PASS_B16B)
+#undef WGPU_PASS_B16B
+    check_launch("fft_cols_backward_screen16_kernel");
+    return;
+  }
   const FftDesc d2 = make_desc(n2);
   const size_t smem = cols_b_smem(n2);
   dim3 grid(ncg, n1);
