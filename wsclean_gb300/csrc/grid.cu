@@ -156,24 +156,27 @@ __host__ __device__ __forceinline__ int border_index(int T, int W, int r, int c)
 
 // Shared-memory layout of the gridding kernels: the halo cells [G][plane],
 // then the staged round: the meta data of each read (int4: u and v corner
-// relative to the tile, first plane relative to the group), its weighted
-// visibility (float2), and the kernel values [kGridRound][kw] with kw = 3W
-// rounded up to an odd count (kx[W], ky[W], kz[W] per read; the odd stride
-// keeps the stores of a warp on distinct banks).
+// relative to the tile, first plane relative to the group, and the range
+// [lo, hi) of footprint planes inside the group as lo | hi << 8), the
+// visibility times the w kernel value of each footprint plane
+// ([kGridRound][W] float2), and the u, v kernel values [kGridRound][kw] with
+// kw = 2W rounded up to an odd count (the odd stride keeps the stores of a warp
+// on distinct banks).
 constexpr int kGridRound = 32;  // records staged per round (eight threads stage each)
-__host__ __device__ constexpr int grid_weight_stride(int W) { return (3 * W) | 1; }
+__host__ __device__ constexpr int grid_weight_stride(int W) { return (2 * W) | 1; }
 template <int T, int G, int W>
 constexpr size_t grid_smem_bytes() {
   return sizeof(float2) * G * halo_plane(T, W) +
-         (size_t)kGridRound * (sizeof(int4) + sizeof(float2) + sizeof(float) * grid_weight_stride(W));
+         (size_t)kGridRound * (sizeof(int4) + sizeof(float2) * W +
+                               sizeof(float) * grid_weight_stride(W));
 }
 
 // Shared memory of the gridding kernels (see grid_smem_bytes).
 struct GridSmem {
   float2 *cells;  // [G][halo plane]
-  int4 *meta;     // (iu_rel, iv_rel, ip_rel, -) per staged read
-  float2 *vis;    // weighted visibility per staged read
-  float *wts;     // [kGridRound][kw]
+  int4 *meta;     // (iu_rel, iv_rel, ip_rel, lo | hi << 8) per staged read
+  float2 *vz;     // [kGridRound][W]: visibility times kz[dz]
+  float *wts;     // [kGridRound][kw]: kx[W], ky[W]
   uint32_t *rs0, *rcum;
 };
 
@@ -182,8 +185,8 @@ __device__ __forceinline__ GridSmem grid_smem(float4 *smem4, uint32_t *rs0, uint
   GridSmem sm;
   sm.cells = reinterpret_cast<float2 *>(smem4);
   sm.meta = reinterpret_cast<int4 *>(sm.cells + G * halo_plane(T, W));
-  sm.vis = reinterpret_cast<float2 *>(sm.meta + kGridRound);
-  sm.wts = reinterpret_cast<float *>(sm.vis + kGridRound);
+  sm.vz = reinterpret_cast<float2 *>(sm.meta + kGridRound);
+  sm.wts = reinterpret_cast<float *>(sm.vz + kGridRound * W);
   sm.rs0 = rs0;
   sm.rcum = rcum;
   return sm;
@@ -253,8 +256,9 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
   for (uint32_t rb = lo; rb < hi; rb += kGridRound) {
-    // stage: eight threads share read t; roles 0-5 evaluate half of kx, ky
-    // or kz each, role 6 writes the meta data
+    // stage: eight threads share read t; roles 0-3 evaluate half of kx or ky
+    // each, roles 4-5 half of the visibility times kz, role 6 writes the meta
+    // data
     {
       static_assert(kThreads == 8 * kGridRound, "eight staging roles");
       constexpr int kHalf = (W + 1) / 2;
@@ -266,31 +270,45 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
         while (pos >= rcum[r + 1]) ++r;
         const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
         float *w = wts + t * kWS;
-        if (role < 6) {
+        if (role < 4) {
           const int dim = role >> 1, k0 = (role & 1) * kHalf;
-          const float f = dim == 0 ? v.fu : (dim == 1 ? v.fv : v.fw);
+          const float f = dim == 0 ? v.fu : v.fv;
 #pragma unroll
           for (int kk = 0; kk < kHalf; ++kk) {
             const int k = k0 + kk;
-            if (k < W)
-              w[dim * W + k] = (dim == 2 && p.n_planes == 1)
-                                   ? (k == 0 ? 1.0f : 0.0f)
-                                   : es_eval(p.beta, (f + (float)k) * inv_half);
+            if (k < W) w[dim * W + k] = es_eval(p.beta, (f + (float)k) * inv_half);
+          }
+        } else if (role < 6) {
+          const int k0 = (role & 1) * kHalf;
+          float2 *vz = sm.vz + t * W;
+#pragma unroll
+          for (int kk = 0; kk < kHalf; ++kk) {
+            const int k = k0 + kk;
+            if (k < W) {
+              const float kz = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
+                                               : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+              vz[k] = make_float2(v.re * kz, v.im * kz);
+            }
           }
         } else {
-          // own-tile records: the corner lies in the tile (0 <= rel < T)
-          sm.meta[t] = make_int4(v.iu - tu * T, v.iv - tv * T, v.ip - q0, 0);
-          sm.vis[t] = make_float2(v.re, v.im);
+          // own-tile records: the corner lies in the tile (0 <= rel < T);
+          // footprint planes dz in [lo, hi) fall inside the group
+          const int ip_rel = v.ip - q0;
+          const int lo = max(0, -ip_rel), hi = min(W, nq - ip_rel);
+          sm.meta[t] = make_int4(v.iu - tu * T, v.iv - tv * T, ip_rel, lo | (hi << 8));
         }
       }
     }
     __syncthreads();
     const int n_round = (int)min((uint32_t)kGridRound, hi - rb);
     for (int m = 0; m < n_round; ++m) {
-      const int4 mt = sm.meta[m];  // (iu_rel, iv_rel, ip_rel)
+      const int4 mt = sm.meta[m];  // (iu_rel, iv_rel, ip_rel, lo | hi << 8)
       const float *w = wts + m * kWS;
-      const float2 vv = sm.vis[m];
-      const int col = mt.x + ci;
+      const float2 *vz = sm.vz + m * W;
+      const int lo = mt.w & 255, n_dz = (mt.w >> 8) - lo;
+      // the footprint's cells of plane ip_rel (dz = 0); the range test keeps
+      // every access inside the group's planes
+      const int col = mt.z * PS + mt.x + ci;
       // footprint rows owned by this warp: dv = (warp - iv_rel) mod 8, + 8
       for (int dv = (warp - mt.y) & 7; dv < W; dv += 8) {
         if (ci < W) {
@@ -299,13 +317,12 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
 #pragma unroll
           for (int s = 0; s < kSteps; ++s) {
             const int dz = s * kPlaneLanes + pl;
-            const int q = mt.z + dz;
-            if (dz < W && q >= 0 && q < nq) {
-              const float t = wuv * w[2 * W + dz];
-              float2 c = cb[q * PS];
-              c.x = fmaf(t, vv.x, c.x);
-              c.y = fmaf(t, vv.y, c.y);
-              cb[q * PS] = c;
+            if ((unsigned)(dz - lo) < (unsigned)n_dz) {
+              const float2 z = vz[dz];
+              float2 c = cb[dz * PS];
+              c.x = fmaf(wuv, z.x, c.x);
+              c.y = fmaf(wuv, z.y, c.y);
+              cb[dz * PS] = c;
             }
           }
         }
