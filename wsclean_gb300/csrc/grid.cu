@@ -59,9 +59,10 @@ __device__ __forceinline__ VisRecord load_record(const VisRecord *r) {
 
 // Key layout (bucket.cu): key = ((tile * 4 + class) * n_planes + first plane),
 // class = which neighbours a footprint spills into (0 none, 1 right, 2 right
-// and up, 3 up).  A gridding unit reads its own tile (all classes), the left
-// tile (classes 1-2), the lower tile (2-3) and the lower-left tile (2): nine
-// key ranges, each restricted to first planes that reach the plane group.
+// and up, 3 up).  A unit reads the four class ranges of its own tile (entries
+// 0-3 below), each restricted to first planes that reach the plane group; the
+// remaining entries name the left, lower and lower-left neighbours' ranges
+// that reach a tile.
 __constant__ int kRangeDtu[9] = {0, 0, 0, 0, 1, 1, 0, 0, 1};
 __constant__ int kRangeDtv[9] = {0, 0, 0, 0, 0, 0, 1, 1, 1};
 __constant__ int kRangeCls[9] = {0, 1, 2, 3, 1, 2, 2, 3, 2};
@@ -478,8 +479,10 @@ constexpr size_t degrid_smem_bytes() {
   return sizeof(float2) * G * (T + W - 1) * degrid_row_stride(T + W - 1);
 }
 
+// Blocks per SM that the shared memory allows (five for W <= 8, three above);
+// the register cap keeps them
 template <int T, int G, int W>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
     degrid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                   const uint32_t *__restrict__ off, int p_begin, int n_batch,
                   const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
@@ -508,15 +511,30 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t lo = (item - __ldg(item_off + unit)) * kItemVis;
 
     const int nq = q1 - q0;
-    for (int idx = threadIdx.x; idx < nq * R * R; idx += blockDim.x) {
-      const int pq = idx / (R * R), rem = idx - pq * R * R;
-      const int r = rem / R, c = rem - r * R;
-      int gv = tv * T + r;
-      if (gv >= p.nv) gv -= p.nv;
-      int gu = tu * T + c;
-      if (gu >= p.nu) gu -= p.nu;
-      halo[pq * kPlane + r * RS + c] =
-          __ldg(planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu);
+    // halo load, four loads in flight per thread before their stores
+    const int n_halo = nq * R * R;
+    for (int i0 = threadIdx.x; i0 < n_halo; i0 += 4 * kThreads) {
+      float2 tmp[4];
+      int dst[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int idx = i0 + k * kThreads;
+        dst[k] = -1;
+        if (idx < n_halo) {
+          const int pq = idx / (R * R), rem = idx - pq * R * R;
+          const int r = rem / R, c = rem - r * R;
+          int gv = tv * T + r;
+          if (gv >= p.nv) gv -= p.nv;
+          int gu = tu * T + c;
+          if (gu >= p.nu) gu -= p.nu;
+          tmp[k] = __ldg(planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu +
+                         gu);
+          dst[k] = pq * kPlane + r * RS + c;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (dst[k] >= 0) halo[dst[k]] = tmp[k];
     }
     if (threadIdx.x < 4) {
       uint32_t a, b;
