@@ -373,13 +373,15 @@ def run_gpu(args, rank, world, local):
         h_vis = pinned_copy(d["d_vis"]).numpy()
         h_mask = pinned_copy(d["d_mask"]).numpy()
         h_out = pinned_copy(d_out).numpy()
+        h_model = pinned_copy(torch.from_numpy(d["model"])).numpy()
+        h_img = torch.empty(W * W, dtype=torch.float32, pin_memory=True).numpy()
 
         def step_host():
             g.InitializeInversion()
             g.AddInversionData(n_rows, n_chan, h_uvw, h_freq, h_vis)
             g.FinalizeImage(inv_weight)
-            g.RealImage()
-            g.InitializePrediction(d["model"])
+            g.RealImage(out=h_img)
+            g.InitializePrediction(h_model)
             g.PredictVisibilitiesMasked(n_rows, n_chan, h_uvw, h_freq, h_mask, out=h_out)
 
         e_ms, e_wall, _ = timed(step_host, max(1, args.steps // 2), 1)

@@ -197,6 +197,8 @@ struct wgpu_gridder {
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
   unsigned *d_flags = nullptr;  // device: expired bounded waits
   unsigned *h_flags = nullptr;  // pinned host copy, read after each call
+  void *stage_buf[2] = {};      // page-locked staging chunks for pageable caller memory
+  cudaEvent_t stage_ev[2] = {};
 };
 
 namespace wgpu {
@@ -226,6 +228,109 @@ size_t image_bytes(const wgpu_gridder *g) {
 
 void ensure_image(wgpu_gridder *g) {
   if (!g->d_img) WGPU_CUDA(cudaMalloc(&g->d_img, image_bytes(g)));
+}
+
+// ---- copies between caller host memory and the device ------------------------
+// Page-locked caller memory (pinned or registered) and small buffers are
+// copied directly.  Pageable memory goes through two page-locked staging
+// chunks of the gridder: the device copy of one chunk runs while the host
+// copies the next, instead of the driver's slower pageable path.
+constexpr size_t kStageChunk = 16ull << 20;
+constexpr size_t kDirectCopyMax = 4ull << 20;
+
+bool host_is_pinned(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+void ensure_staging(wgpu_gridder *g) {
+  for (int k = 0; k < 2; ++k) {
+    if (!g->stage_buf[k])
+      WGPU_CUDA(cudaHostAlloc(&g->stage_buf[k], kStageChunk, cudaHostAllocDefault));
+    if (!g->stage_ev[k])
+      WGPU_CUDA(cudaEventCreateWithFlags(&g->stage_ev[k], cudaEventDisableTiming));
+  }
+}
+
+// Host to device on the gridder stream; returns once the caller's memory has
+// been read (the device copy may still be running).
+void copy_to_device(wgpu_gridder *g, void *d, const void *h, size_t bytes) {
+  if (bytes == 0) return;
+  if (bytes <= kDirectCopyMax || host_is_pinned(h)) {
+    WGPU_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream));
+    return;
+  }
+  ensure_staging(g);
+  int k = 0;
+  for (size_t off = 0; off < bytes; off += kStageChunk, k ^= 1) {
+    const size_t n = std::min(kStageChunk, bytes - off);
+    WGPU_CUDA(cudaEventSynchronize(g->stage_ev[k]));  // the chunk's previous copy is done
+    std::memcpy(g->stage_buf[k], (const char *)h + off, n);
+    WGPU_CUDA(cudaMemcpyAsync((char *)d + off, g->stage_buf[k], n, cudaMemcpyHostToDevice,
+                              g->stream));
+    WGPU_CUDA(cudaEventRecord(g->stage_ev[k], g->stream));
+  }
+}
+
+// Device to host after the work queued on the gridder stream; returns when
+// the caller's memory holds the data.
+void copy_to_host(wgpu_gridder *g, void *h, const void *d, size_t bytes) {
+  if (bytes == 0) return;
+  if (bytes <= kDirectCopyMax || host_is_pinned(h)) {
+    WGPU_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    return;
+  }
+  ensure_staging(g);
+  const size_t n_chunks = (bytes + kStageChunk - 1) / kStageChunk;
+  auto issue = [&](size_t c) {
+    const size_t off = c * kStageChunk, n = std::min(kStageChunk, bytes - off);
+    WGPU_CUDA(cudaMemcpyAsync(g->stage_buf[c & 1], (const char *)d + off, n,
+                              cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaEventRecord(g->stage_ev[c & 1], g->stream));
+  };
+  issue(0);
+  if (n_chunks > 1) issue(1);
+  for (size_t c = 0; c < n_chunks; ++c) {
+    WGPU_CUDA(cudaEventSynchronize(g->stage_ev[c & 1]));
+    const size_t off = c * kStageChunk, n = std::min(kStageChunk, bytes - off);
+    std::memcpy((char *)h + off, g->stage_buf[c & 1], n);
+    if (c + 2 < n_chunks) issue(c + 2);  // into the chunk just emptied
+  }
+}
+
+// The caller's float image (width x height) from the gridder's image (trimmed
+// width_t x height_t, float or double): NaN outside the trimmed region.
+__global__ void image_out_kernel(const void *__restrict__ img, int prec, int64_t wt, int64_t ht,
+                                 int64_t w, int64_t h, float *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w * h) return;
+  const int64_t x = i % w, y = i / w;
+  const int64_t xs = x - (w - wt) / 2, ys = y - (h - ht) / 2;
+  float v = __int_as_float(0x7fc00000);  // quiet NaN
+  if (xs >= 0 && xs < wt && ys >= 0 && ys < ht) {
+    const int64_t j = ys * wt + xs;
+    v = prec == 8 ? __double2float_rn(((const double *)img)[j]) : ((const float *)img)[j];
+  }
+  out[i] = v;
+}
+
+// The gridder's image (trimmed region, float or double) from the caller's
+// float image.
+__global__ void image_in_kernel(const float *__restrict__ in, int prec, int64_t wt, int64_t ht,
+                                int64_t w, int64_t h, void *__restrict__ img) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= wt * ht) return;
+  const int64_t xs = i % wt, ys = i / wt;
+  const float v = in[(xs + (w - wt) / 2) + (ys + (h - ht) / 2) * w];
+  if (prec == 8)
+    ((double *)img)[i] = (double)v;
+  else
+    ((float *)img)[i] = v;
 }
 
 // Host-side correction tables for one plan: cx, cy (1/psihat per column/row)
@@ -462,11 +567,11 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   b->n_chan = (int64_t)n_chan;
   b->uvw = (double *)b->alloc(sizeof(double) * 3 * n_rows);
   b->freq = (double *)b->alloc(sizeof(double) * n_chan);
-  WGPU_CUDA(cudaMemcpyAsync(b->uvw, h_uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
-  WGPU_CUDA(cudaMemcpyAsync(b->freq, h_freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
+  copy_to_device(g, b->uvw, h_uvw, sizeof(double) * 3 * n_rows);
+  copy_to_device(g, b->freq, h_freq, sizeof(double) * n_chan);
   if (h_mask) {
     b->mask = (uint8_t *)b->alloc((size_t)n);
-    WGPU_CUDA(cudaMemcpyAsync(b->mask, h_mask, (size_t)n, cudaMemcpyHostToDevice, s));
+    copy_to_device(g, b->mask, h_mask, (size_t)n);
   }
   double w_min, w_max;
   int64_t count;
@@ -600,8 +705,11 @@ void invert_bound(wgpu_gridder *g, const float *vis, bool device) {
   cudaStream_t s = g->stream;
   g->timer.begin(s);
   g->timer.mark("bound_invert");
-  WGPU_CUDA(cudaMemcpyAsync(b.vis_in, vis, sizeof(float2) * b.n_rows * b.n_chan,
-                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  if (device)
+    WGPU_CUDA(cudaMemcpyAsync(b.vis_in, vis, sizeof(float2) * b.n_rows * b.n_chan,
+                              cudaMemcpyDeviceToDevice, s));
+  else
+    copy_to_device(g, b.vis_in, vis, sizeof(float2) * b.n_rows * b.n_chan);
   WGPU_CUDA(cudaGraphLaunch(b.xinv, s));
   count_launch((int)b.inv_kernels);
   end_call(g);
@@ -618,8 +726,11 @@ void predict_bound(wgpu_gridder *g, float *vis, bool device) {
   g->timer.mark("bound_predict");
   WGPU_CUDA(cudaGraphLaunch(b.xpred, s));
   count_launch((int)b.pred_kernels);
-  WGPU_CUDA(cudaMemcpyAsync(vis, b.vis_out, sizeof(float2) * b.n_rows * b.n_chan,
-                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  if (device)
+    WGPU_CUDA(cudaMemcpyAsync(vis, b.vis_out, sizeof(float2) * b.n_rows * b.n_chan,
+                              cudaMemcpyDeviceToDevice, s));
+  else
+    copy_to_host(g, vis, b.vis_out, sizeof(float2) * b.n_rows * b.n_chan);
   end_call(g);
   g->last_plan = b.plan;
 }
@@ -627,7 +738,7 @@ void predict_bound(wgpu_gridder *g, float *vis, bool device) {
 template <typename T>
 T *upload(wgpu_gridder *g, int slot, const T *h, size_t n) {
   T *d = (T *)g->arena.get(slot, sizeof(T) * (n ? n : 1));
-  if (n) WGPU_CUDA(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, g->stream));
+  copy_to_device(g, d, h, sizeof(T) * n);
   return d;
 }
 
@@ -714,6 +825,10 @@ void wgpu_gridder_destroy(wgpu_gridder_t *g) {
   if (g->d_img) cudaFree(g->d_img);
   if (g->d_flags) cudaFree(g->d_flags);
   if (g->h_flags) cudaFreeHost(g->h_flags);
+  for (int k = 0; k < 2; ++k) {
+    if (g->stage_buf[k]) cudaFreeHost(g->stage_buf[k]);
+    if (g->stage_ev[k]) cudaEventDestroy(g->stage_ev[k]);
+  }
   fft_tables_destroy(g->fft);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -822,20 +937,15 @@ int wgpu_gridder_real_image(wgpu_gridder_t *g, float *image) {
   if (!g || !image) return fail(WGPU_ERR_INVALID, "null argument");
   return guarded([&] {
     if (!g->d_img) throw Error(WGPU_ERR_STATE, "RealImage without an image");
-    const size_t wt = g->width_t, ht = g->height_t;
-    std::vector<char> h(image_bytes(g));
-    WGPU_CUDA(cudaMemcpyAsync(h.data(), g->d_img, h.size(), cudaMemcpyDeviceToHost, g->stream));
-    WGPU_CUDA(cudaStreamSynchronize(g->stream));
-    const size_t dx = (g->width - wt) / 2, dy = (g->height - ht) / 2;
-    const float nan = std::nanf("");
-    for (size_t i = 0; i < g->width * g->height; ++i) image[i] = nan;
-    for (size_t y = 0; y < ht; ++y)
-      for (size_t x = 0; x < wt; ++x) {
-        const size_t i = y * wt + x;
-        const float v = g->prec == 8 ? (float)((const double *)h.data())[i]
-                                     : ((const float *)h.data())[i];
-        image[(x + dx) + (y + dy) * g->width] = v;
-      }
+    // trimmed image -> full float image with NaN borders on the device, then
+    // one copy to the caller
+    const int64_t n = (int64_t)(g->width * g->height);
+    float *d_out = (float *)g->arena.get(kSlotImgIO, sizeof(float) * (size_t)n);
+    image_out_kernel<<<(unsigned)((n + 255) / 256), 256, 0, g->stream>>>(
+        g->d_img, g->prec, (int64_t)g->width_t, (int64_t)g->height_t, (int64_t)g->width,
+        (int64_t)g->height, d_out);
+    check_launch("image_out_kernel");
+    copy_to_host(g, image, d_out, sizeof(float) * (size_t)n);
   });
 }
 
@@ -843,18 +953,16 @@ int wgpu_gridder_initialize_prediction(wgpu_gridder_t *g, const float *image) {
   if (!g || !image) return fail(WGPU_ERR_INVALID, "null argument");
   return guarded([&] {
     ensure_image(g);
-    const size_t wt = g->width_t, ht = g->height_t;
-    const size_t dx = (g->width - wt) / 2, dy = (g->height - ht) / 2;
-    std::vector<char> h(image_bytes(g));
-    for (size_t y = 0; y < ht; ++y)
-      for (size_t x = 0; x < wt; ++x) {
-        const float v = image[(x + dx) + (y + dy) * g->width];
-        if (g->prec == 8)
-          ((double *)h.data())[y * wt + x] = v;
-        else
-          ((float *)h.data())[y * wt + x] = v;
-      }
-    WGPU_CUDA(cudaMemcpyAsync(g->d_img, h.data(), h.size(), cudaMemcpyHostToDevice, g->stream));
+    // the caller's float image to the device, then its trimmed region into
+    // the gridder's image (float or double)
+    const int64_t n = (int64_t)(g->width * g->height);
+    float *d_in = (float *)g->arena.get(kSlotImgIO, sizeof(float) * (size_t)n);
+    copy_to_device(g, d_in, image, sizeof(float) * (size_t)n);
+    const int64_t nt = (int64_t)(g->width_t * g->height_t);
+    image_in_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, g->stream>>>(
+        d_in, g->prec, (int64_t)g->width_t, (int64_t)g->height_t, (int64_t)g->width,
+        (int64_t)g->height, g->d_img);
+    check_launch("image_in_kernel");
     WGPU_CUDA(cudaStreamSynchronize(g->stream));
     g->mode = wgpu_gridder::Mode::kPrediction;
   });
@@ -894,9 +1002,7 @@ int wgpu_gridder_predict_visibilities_masked(wgpu_gridder_t *g, size_t n_rows,
     const uint8_t *dm = upload(g, kSlotAnt, mask, n_rows * n_chan);
     float *dv = (float *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
     predict_device(g, n_rows, n_chan, du, df, dm, dv);
-    WGPU_CUDA(cudaMemcpyAsync(vis, dv, sizeof(float2) * n_rows * n_chan,
-                              cudaMemcpyDeviceToHost, g->stream));
-    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    copy_to_host(g, vis, dv, sizeof(float2) * n_rows * n_chan);
   });
 }
 
@@ -914,9 +1020,7 @@ int wgpu_gridder_predict_visibilities(wgpu_gridder_t *g, size_t n_rows,
     const double *df = upload(g, kSlotFreq, freq, n_chan);
     float *dv = (float *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
     predict_device(g, n_rows, n_chan, du, df, nullptr, dv);
-    WGPU_CUDA(cudaMemcpyAsync(vis, dv, sizeof(float2) * n_rows * n_chan,
-                              cudaMemcpyDeviceToHost, g->stream));
-    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    copy_to_host(g, vis, dv, sizeof(float2) * n_rows * n_chan);
   });
 }
 

@@ -509,8 +509,8 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_out) return;
   const uint32_t e = perm[s];
-  const int64_t r = e / n_chan, c = e - r * n_chan;
-  const double *row = uvw + 3 * r;
+  const uint32_t r = e / (uint32_t)n_chan, c = e - r * (uint32_t)n_chan;  // e < 2^32
+  const double *row = uvw + 3 * (size_t)r;
   const ChannelScale sc = cs[c];
   double wl;
   const Footprint f = record_footprint(p, row, row_float(uvwf, uvw, r), sc, &wl);

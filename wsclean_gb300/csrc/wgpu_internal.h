@@ -351,6 +351,7 @@ enum ArenaSlot {
   kSlotSpill,
   kSlotRowOcc,
   kSlotUvwF32,
+  kSlotImgIO,
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.

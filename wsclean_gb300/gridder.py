@@ -108,8 +108,14 @@ class WGriddingGridder_Simple:
     def FinalizeImage(self, multiplication_factor):
         check(lib().wgpu_gridder_finalize_image(self._h, float(multiplication_factor)))
 
-    def RealImage(self):
-        out = np.empty(self.width * self.height, dtype=np.float32)
+    def RealImage(self, out=None):
+        """The image as float32 (width * height); `out` (contiguous float32 of
+        that size, e.g. pinned host memory) receives it when given."""
+        if out is None:
+            out = np.empty(self.width * self.height, dtype=np.float32)
+        else:
+            assert out.dtype == np.float32 and out.flags.c_contiguous
+            assert out.size == self.width * self.height
         check(lib().wgpu_gridder_real_image(self._h, ptr(out)))
         return out
 
