@@ -340,7 +340,7 @@ constexpr int kSortTile = kThreads * kSortItems;  // 2048 elements per block
 
 __global__ void __launch_bounds__(kThreads)
     radix_hist_kernel(const uint32_t *keys, int64_t n, int shift,
-                      uint32_t *hist, int64_t n_blocks) {
+                      uint32_t *hist, int64_t n_blocks, bool drop, uint32_t drop_key) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -348,7 +348,10 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const int64_t i = base + r * kThreads + threadIdx.x;
-    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    if (i < n) {
+      const uint32_t k = keys[i];
+      if (!(drop && k == drop_key)) atomicAdd(&h[(k >> shift) & 255u], 1u);
+    }
   }
   __syncthreads();
   hist[(int64_t)threadIdx.x * n_blocks + blockIdx.x] = h[threadIdx.x];
@@ -359,17 +362,20 @@ __global__ void __launch_bounds__(kThreads)
 // and lane), then writes each digit's run to its global range, so that
 // consecutive threads write consecutive addresses.  hist holds the exclusive
 // scan of the per-(digit, block) counts (digit-major); a tile's own count of
-// digit d is the difference to the next entry (n after the last).
+// digit d is the difference to the next entry (n_kept after the last).  With
+// drop, elements whose key is drop_key take no part (the histogram skipped
+// them too) and n_kept elements come out.
 __global__ void __launch_bounds__(kThreads)
     radix_scatter_kernel(const uint32_t *keys_in, const uint32_t *vals_in,
                          int64_t n, int shift, const uint32_t *hist,
                          int64_t n_blocks, uint32_t *keys_out,
-                         uint32_t *vals_out) {
+                         uint32_t *vals_out, bool drop, uint32_t drop_key, uint32_t n_kept) {
   __shared__ uint32_t base[256];    // global position of the tile's first element of digit d
   __shared__ uint32_t tstart[256];  // first position of digit d in the tile's sorted order
   __shared__ uint32_t run[256];     // elements of digit d placed by earlier rounds
   __shared__ uint32_t wcnt[kThreads / 32][256];
   __shared__ uint32_t wsum[kThreads / 32];
+  __shared__ uint32_t tile_kept;
   __shared__ uint32_t skey[kSortTile], sval[kSortTile];
   static_assert(kThreads == 256, "one thread per digit");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -378,7 +384,7 @@ __global__ void __launch_bounds__(kThreads)
   {
     const int64_t at = (int64_t)threadIdx.x * n_blocks + blockIdx.x;
     const uint32_t b0 = hist[at];
-    const uint32_t b1 = (threadIdx.x == 255 && blockIdx.x == n_blocks - 1) ? (uint32_t)n
+    const uint32_t b1 = (threadIdx.x == 255 && blockIdx.x == n_blocks - 1) ? n_kept
                                                                            : hist[at + 1];
     base[threadIdx.x] = b0;
     run[threadIdx.x] = 0;
@@ -395,6 +401,7 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t before = 0;
     for (int w = 0; w < warp; ++w) before += wsum[w];
     tstart[threadIdx.x] = before + x - cnt;
+    if (threadIdx.x == 255) tile_kept = before + x;
   }
   const unsigned lt_mask = (1u << lane) - 1u;
   for (int r = 0; r < kSortItems; ++r) {
@@ -402,12 +409,16 @@ __global__ void __launch_bounds__(kThreads)
     for (int w = 0; w < kThreads / 32; ++w) wcnt[w][threadIdx.x] = 0;
     __syncthreads();
     const int t = r * kThreads + threadIdx.x;
-    const bool valid = t < tile_n;
+    bool valid = t < tile_n;
     uint32_t key = 0, val = 0, d = 256;
     if (valid) {
       key = keys_in[tile0 + t];
       val = vals_in[tile0 + t];
       d = (key >> shift) & 255u;
+      if (drop && key == drop_key) {
+        valid = false;
+        d = 256;
+      }
     }
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const uint32_t rank = __popc(peers & lt_mask);
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();  // wcnt is cleared for the next round
   }
-  for (int j = threadIdx.x; j < tile_n; j += kThreads) {
+  for (int j = threadIdx.x; j < (int)tile_kept; j += kThreads) {
     const uint32_t key = skey[j];
     const uint32_t d = (key >> shift) & 255u;
     const uint32_t out = base[d] + ((uint32_t)j - tstart[d]);
@@ -642,6 +653,33 @@ unsigned grid_for(int64_t n, int threads) {
 
 }  // namespace
 
+namespace {
+// Stable LSD radix sort of (key, value) pairs over `bits` key bits.  The first
+// pass drops the elements whose key is `sentinel` (samples that take no part),
+// so the n_kept others come out; kin / vin end up naming the sorted buffers.
+// scan(d, n) is an exclusive scan of n uint32 values in place.
+template <class Scan>
+void radix_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *&vout,
+                     int64_t n, uint32_t n_kept, int bits, uint32_t sentinel, uint32_t *hist,
+                     Scan scan, cudaStream_t s) {
+  int64_t cur = n;
+  for (int shift = 0; shift < bits && cur > 0 && n_kept > 0; shift += 8) {
+    const bool drop = shift == 0;
+    const int64_t n_blocks = (cur + kSortTile - 1) / kSortTile;
+    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, cur, shift, hist, n_blocks,
+                                                              drop, sentinel);
+    check_launch("radix_hist_kernel");
+    scan(hist, 256 * n_blocks);
+    radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(
+        kin, vin, cur, shift, hist, n_blocks, kout, vout, drop, sentinel, n_kept);
+    check_launch("radix_scatter_kernel");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+    cur = n_kept;
+  }
+}
+}  // namespace
+
 RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_t s) {
   RowOccupancy o = rows;
   if (!rows.buf) return o;
@@ -733,25 +771,17 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   build_row_occupancy(res.rows, p.support, s);
   exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
 
-  // radix sort over the key bits in use
-  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
-  uint32_t *hist = (uint32_t *)arena.get(kSlotHist, sizeof(uint32_t) * (256 * n_blocks + 1));
-  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  for (int shift = 0; shift < bits && n > 0; shift += 8) {
-    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, n, shift, hist, n_blocks);
-    check_launch("radix_hist_kernel");
-    exclusive_scan_u32(arena, hist, 256 * n_blocks, s);
-    radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, vin, n, shift, hist,
-                                                                 n_blocks, kout, vout);
-    check_launch("radix_scatter_kernel");
-    std::swap(kin, kout);
-    std::swap(vin, vout);
-  }
   // number of bucketed elements = offsets[n_keys]
   uint32_t total = 0;
   WGPU_CUDA(cudaMemcpyAsync(&total, offsets + res.n_keys, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
+  // radix sort over the key bits in use, the unselected samples dropped
+  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
+  uint32_t *hist = (uint32_t *)arena.get(kSlotHist, sizeof(uint32_t) * (256 * n_blocks + 1));
+  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+  radix_sort_kept(kin, vin, kout, vout, n, total, bits, sentinel, hist,
+                  [&](uint32_t *d, int64_t m) { exclusive_scan_u32(arena, d, m, s); }, s);
   res.n_out = total;
   res.perm = vin;
   res.offsets = offsets;
@@ -875,22 +905,14 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
     check_launch("key_fix_kernel");
   }
   exclusive_scan_u32_scratch(d_offsets, n_keys + 1, scan_tmp, s);
-  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
-  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  for (int shift = 0; shift < bits && n > 0; shift += 8) {
-    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, n, shift, hist, n_blocks);
-    check_launch("radix_hist_kernel");
-    exclusive_scan_u32_scratch(hist, 256 * n_blocks, scan_tmp, s);
-    radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, vin, n, shift, hist,
-                                                                 n_blocks, kout, vout);
-    check_launch("radix_scatter_kernel");
-    std::swap(kin, kout);
-    std::swap(vin, vout);
-  }
   uint32_t total = 0;
   WGPU_CUDA(cudaMemcpyAsync(&total, d_offsets + n_keys, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
+  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+  radix_sort_kept(kin, vin, kout, vout, n, total, bits, sentinel, hist,
+                  [&](uint32_t *d, int64_t m) { exclusive_scan_u32_scratch(d, m, scan_tmp, s); },
+                  s);
   if (total > 0) {
     WGPU_CUDA(cudaMemcpyAsync(d_perm, vin, sizeof(uint32_t) * total, cudaMemcpyDeviceToDevice, s));
     const bool shift = p.l_shift != 0.0 || p.m_shift != 0.0;
