@@ -474,6 +474,46 @@ __device__ __forceinline__ void row_stage_last(float2 *buf, int L, int p, float 
   __syncthreads();
 }
 
+// Last stage with its outputs written straight to the output row (no
+// shared-memory write and read-out): output k goes to column
+// x = (width/2 - k) mod L when x < width (FWD: the kept, re-centred columns;
+// columns width .. out_stride - 1 are zero) or to position k (!FWD).
+template <int R, bool FWD>
+__device__ __forceinline__ void row_stage_last_out(const float2 *buf, int L, int p, float sign,
+                                                   const float2 *__restrict__ tws,
+                                                   float2 *__restrict__ out, int out_stride,
+                                                   int width) {
+  const int LR = L / R;  // == p
+  for (int i = threadIdx.x; i < LR; i += blockDim.x) {
+    float2 v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = buf[row_slot(i + t * LR)];
+    if (i > 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) {
+        float2 w = __ldg(tws + (t - 1) * p + i);
+        w.y *= -sign;
+        v[t] = cmul(v[t], w);
+      }
+    }
+    dft<R>(v, sign);
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int k = i + q * LR;
+      if (FWD) {
+        int x = width / 2 - k;
+        if (x < 0) x += L;
+        if (x < width) out[x] = v[q];
+      } else {
+        out[k] = v[q];
+      }
+    }
+  }
+  if (FWD)
+    for (int x = width + threadIdx.x; x < out_stride; x += blockDim.x)
+      out[x] = make_float2(0.f, 0.f);
+}
+
 // Writes the transformed row: FWD crops the `width` kept columns (re-centred)
 // into out (out_stride entries), !FWD writes the L entries in natural order.
 template <bool FWD>
@@ -580,8 +620,8 @@ __global__ void __launch_bounds__(kRowThreadsMax, 1)
       p *= 8;
       ++s;
     }
-    row_stage_last<LAST>(buf, L, p, sign, tws + st.tw_off[s]);
-    row_out<FWD>(buf, out + (size_t)row * out_stride, out_stride, L, width);
+    row_stage_last_out<LAST, FWD>(buf, L, p, sign, tws + st.tw_off[s],
+                                  out + (size_t)row * out_stride, out_stride, width);
     // generic accesses to this buffer end here; the bulk copy issued into it
     // at the next iteration is ordered after them
     fence_proxy_async();
