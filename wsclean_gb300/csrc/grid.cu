@@ -511,30 +511,19 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
     const uint32_t lo = (item - __ldg(item_off + unit)) * kItemVis;
 
     const int nq = q1 - q0;
-    // halo load, four loads in flight per thread before their stores
+    // halo load: asynchronous 8-byte copies straight into shared memory
+    // (cp.async), each thread waiting for its own before the barrier below
     const int n_halo = nq * R * R;
-    for (int i0 = threadIdx.x; i0 < n_halo; i0 += 4 * kThreads) {
-      float2 tmp[4];
-      int dst[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int idx = i0 + k * kThreads;
-        dst[k] = -1;
-        if (idx < n_halo) {
-          const int pq = idx / (R * R), rem = idx - pq * R * R;
-          const int r = rem / R, c = rem - r * R;
-          int gv = tv * T + r;
-          if (gv >= p.nv) gv -= p.nv;
-          int gu = tu * T + c;
-          if (gu >= p.nu) gu -= p.nu;
-          tmp[k] = __ldg(planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu +
-                         gu);
-          dst[k] = pq * kPlane + r * RS + c;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (dst[k] >= 0) halo[dst[k]] = tmp[k];
+    for (int idx = threadIdx.x; idx < n_halo; idx += kThreads) {
+      const int pq = idx / (R * R), rem = idx - pq * R * R;
+      const int r = rem / R, c = rem - r * R;
+      int gv = tv * T + r;
+      if (gv >= p.nv) gv -= p.nv;
+      int gu = tu * T + c;
+      if (gu >= p.nu) gu -= p.nu;
+      const float2 *src = planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(halo + pq * kPlane + r * RS + c);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
     }
     if (threadIdx.x < 4) {
       uint32_t a, b;
@@ -542,6 +531,7 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
       rs0[threadIdx.x] = a;
       rcum[threadIdx.x + 1] = b - a;
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     if (threadIdx.x == 0) {
       rcum[0] = 0;
