@@ -547,11 +547,16 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
           int r = 0;
           while (pos >= rcum[r + 1]) ++r;
           const uint32_t s = rs0[r] + (pos - rcum[r]);
-          const float4 *src = reinterpret_cast<const float4 *>(rec + s);
-          stage[threadIdx.x][0] = __ldg(src);
-          stage[threadIdx.x][1] = __ldg(src + 1);
+          // the 32-byte record into the stage with two 16-byte cp.async copies
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&stage[threadIdx.x][0]);
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(rec + s)
+                       : "memory");
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u),
+                       "l"(reinterpret_cast<const float4 *>(rec + s) + 1)
+                       : "memory");
           stage_s[threadIdx.x] = s;
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
       }
       __syncthreads();
       const int n_round = (int)min((uint32_t)kThreads, hi - rb);
