@@ -311,22 +311,26 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
       // every access inside the group's planes
       const int col = mt.z * PS + mt.x + ci;
       // footprint rows owned by this warp: dv = (warp - iv_rel) mod 8, + 8
-      for (int dv = (warp - mt.y) & 7; dv < W; dv += 8) {
-        if (ci < W) {
-          const float wuv = w[ci] * w[W + dv];
-          float2 *cb = cells + (mt.y + dv) * R + col;
+      auto add_row = [&](int dv) {
+        const float wuv = w[ci] * w[W + dv];
+        float2 *cb = cells + (mt.y + dv) * R + col;
 #pragma unroll
-          for (int s = 0; s < kSteps; ++s) {
-            const int dz = s * kPlaneLanes + pl;
-            if ((unsigned)(dz - lo) < (unsigned)n_dz) {
-              const float2 z = vz[dz];
-              float2 c = cb[dz * PS];
-              c.x = fmaf(wuv, z.x, c.x);
-              c.y = fmaf(wuv, z.y, c.y);
-              cb[dz * PS] = c;
-            }
+        for (int s = 0; s < kSteps; ++s) {
+          const int dz = s * kPlaneLanes + pl;
+          if ((unsigned)(dz - lo) < (unsigned)n_dz) {
+            const float2 z = vz[dz];
+            float2 c = cb[dz * PS];
+            c.x = fmaf(wuv, z.x, c.x);
+            c.y = fmaf(wuv, z.y, c.y);
+            cb[dz * PS] = c;
           }
         }
+      };
+      if constexpr (W == 8) {
+        add_row((warp - mt.y) & 7);  // one row per warp, every lane's column inside
+      } else {
+        for (int dv = (warp - mt.y) & 7; dv < W; dv += 8)
+          if (ci < W) add_row(dv);
       }
       __syncwarp();  // the next read's lanes may update the same cells
     }
