@@ -288,7 +288,10 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
             if (k < W) {
               const float kz = p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
                                                : es_eval(p.beta, (v.fw + (float)k) * inv_half);
-              vz[k] = make_float2(v.re * kz, v.im * kz);
+              // W = 8: plane k = s * 4 + pl at (pl, s), so that a lane's two
+              // planes are one 16-byte load
+              const int at = W == 8 ? ((k & 3) * 2 + (k >> 2)) : k;
+              vz[at] = make_float2(v.re * kz, v.im * kz);
             }
           }
         } else {
@@ -314,15 +317,31 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
       auto add_row = [&](int dv) {
         const float wuv = w[ci] * w[W + dv];
         float2 *cb = cells + (mt.y + dv) * R + col;
+        if constexpr (W == 8) {
+          // planes pl and pl + 4 of this lane in one load
+          const float4 z2 = reinterpret_cast<const float4 *>(vz)[pl];
 #pragma unroll
-        for (int s = 0; s < kSteps; ++s) {
-          const int dz = s * kPlaneLanes + pl;
-          if ((unsigned)(dz - lo) < (unsigned)n_dz) {
-            const float2 z = vz[dz];
-            float2 c = cb[dz * PS];
-            c.x = fmaf(wuv, z.x, c.x);
-            c.y = fmaf(wuv, z.y, c.y);
-            cb[dz * PS] = c;
+          for (int s = 0; s < 2; ++s) {
+            const int dz = s * 4 + pl;
+            if ((unsigned)(dz - lo) < (unsigned)n_dz) {
+              const float zx = s == 0 ? z2.x : z2.z, zy = s == 0 ? z2.y : z2.w;
+              float2 c = cb[dz * PS];
+              c.x = fmaf(wuv, zx, c.x);
+              c.y = fmaf(wuv, zy, c.y);
+              cb[dz * PS] = c;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int s = 0; s < kSteps; ++s) {
+            const int dz = s * kPlaneLanes + pl;
+            if ((unsigned)(dz - lo) < (unsigned)n_dz) {
+              const float2 z = vz[dz];
+              float2 c = cb[dz * PS];
+              c.x = fmaf(wuv, z.x, c.x);
+              c.y = fmaf(wuv, z.y, c.y);
+              cb[dz * PS] = c;
+            }
           }
         }
       };
