@@ -372,6 +372,9 @@ def run_gpu(args, rank, world, local):
                 roofline["traffic_unit"] = "GB per launch"
                 roofline["achieved_bytes_per_launch_gb"] = dom["bytes_per_launch"] / 1e9
                 roofline["traffic_source"] = t["how"]
+                if "shared_pipe_frac" in t:
+                    roofline["shared_pipe_frac"] = t["shared_pipe_frac"]
+                    roofline["shared_pipe_source"] = t["shared_pipe_how"]
 
     # ---- e2e through the host-pointer API (pinned buffers)
     e2e = None
