@@ -2,9 +2,10 @@
 // column passes.
 //
 // A plane batch lives in HBM as [B][nv][nu] complex64.  Inversion runs
-//   rows:    forward FFT of every row (length nu, one row per CTA, whole row in
-//            shared memory), keeping only the `width` trimmed columns, written
-//            to R = [B][nv][rstride];
+//   rows:    forward FFT of every row that some footprint touches (the row
+//            list of the bucketing pass; length nu, whole row in shared
+//            memory), keeping only the `width` trimmed columns, written to
+//            R = [B][nv][rstride];
 //   cols A:  four-step split nv = n1 * n2: panels of 32 columns x n1 rows at
 //            stride n2, forward FFT of length n1, twiddle w_nv^(r2 k1);
 //   cols B:  panels of 32 columns x n2 consecutive rows, forward FFT of length
@@ -16,10 +17,12 @@
 // Prediction runs the adjoint passes in the opposite order (cols B', cols A',
 // rows) with the opposite sign, zero padding instead of cropping.
 //
-// The FFT engine is a Stockham autosort with radices 2, 3, 4, 5 and 8.  Each
-// stage reads every butterfly input into registers, synchronises, and writes
-// the outputs in place.  Twiddles come from tables computed in FP64 on the
-// host and rounded to FP32 once.
+// The FFT engine is a Stockham autosort with radices 2, 3, 4, 5, 6, 8 and 16.
+// Row stages read every butterfly input into registers, synchronise, and write
+// the outputs in place.  Column transforms of length 16 R2 (R2 in 2, 3, 4, 5,
+// 6, 8) take two stages with one shared-memory round trip (panel_fft); other
+// lengths use the generic stage loop.  Twiddles come from tables computed in
+// FP64 on the host and rounded to FP32 once.
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -449,31 +452,6 @@ __device__ __forceinline__ void row_stage_inplace(float2 *buf, int L, int p, uns
   __syncthreads();
 }
 
-// Last stage (p R = L): each butterfly writes the addresses it read, so
-// threads work through their butterflies one at a time.
-template <int R>
-__device__ __forceinline__ void row_stage_last(float2 *buf, int L, int p, float sign,
-                                               const float2 *__restrict__ tws) {
-  const int LR = L / R;  // == p
-  for (int i = threadIdx.x; i < LR; i += blockDim.x) {
-    float2 v[R];
-#pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = buf[row_slot(i + t * LR)];
-    if (i > 0) {
-#pragma unroll
-      for (int t = 1; t < R; ++t) {
-        float2 w = __ldg(tws + (t - 1) * p + i);
-        w.y *= -sign;
-        v[t] = cmul(v[t], w);
-      }
-    }
-    dft<R>(v, sign);
-#pragma unroll
-    for (int q = 0; q < R; ++q) buf[row_slot(i + q * LR)] = v[q];
-  }
-  __syncthreads();
-}
-
 // Last stage with its outputs written straight to the output row (no
 // shared-memory write and read-out): output k goes to column
 // x = (width/2 - k) mod L when x < width (FWD: the kept, re-centred columns;
@@ -538,12 +516,6 @@ __device__ __forceinline__ void row_out(const float2 *res, float2 *__restrict__ 
 
 constexpr int kRowThreadsMax = kFftMaxRow / 16;  // 768: one radix-16 butterfly each
 
-// Persistent row kernel.  Schedule: radix 16, (n_stages - 2 - MID8) radix-16
-// stages, one radix-8 stage if MID8, and a last stage of radix LAST.
-// FWD: plane rows (length L) -> forward FFT -> cropped rows of R.
-// !FWD: rows of R (width valid entries) -> zero padding, re-centring ->
-//      backward FFT -> plane rows.  buf_elems >= max(L, in_stride); in_bytes
-// is the size of one input row.
 // Number of rows a row launch transforms, and the batch row index of its
 // item idx (see RowSel).
 __device__ __forceinline__ int sel_rows(const RowSel &sel, int n_batch, int nv) {
@@ -554,6 +526,13 @@ __device__ __forceinline__ int sel_row(const RowSel &sel, int idx, int nv) {
                   : idx;
 }
 
+// Persistent row kernel.  Schedule: radix 16, (n_stages - 2 - MID8) radix-16
+// stages, one radix-8 stage if MID8, and a last stage of radix LAST that
+// writes straight to the output row.
+// FWD: plane rows (length L) -> forward FFT -> cropped rows of R.
+// !FWD: rows of R (width valid entries) -> zero padding, re-centring ->
+//      backward FFT -> plane rows.  buf_elems >= max(L, in_stride); in_bytes
+// is the size of one input row.  Only the rows `sel` names are transformed.
 template <bool FWD, int LAST, bool MID8>
 __global__ void __launch_bounds__(kRowThreadsMax, 1)
     fft_rows_persistent_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
