@@ -163,6 +163,23 @@ int wgpu_gridder_add_inversion_data_corrected(
     const uint64_t *time_offsets, const float *solutions, size_t nparms,
     size_t n_times, size_t n_ant, int polarization);
 
+/* The prediction write-back of WSClean for corrected (facet / h5parm)
+ * prediction: PredictVisibilities (gridder_simple_implementation.h:170-196)
+ * followed by what MsGridderData::WriteCollapsedVisibilities and
+ * WriteInstrumentalVisibilities do per row on the host (msgridderdata.h:180-202,
+ * 943-1003): the predicted value expanded to n_pol correlations (duplicated
+ * for 2, Stokes -> linear for 4 with `polarization` as in the corrected
+ * inversion) and multiplied by the forward gains G1 V G2^H of the row's
+ * antennas (VisibilityModifier::ApplyParmResponse, visibilitymodifier.cpp:
+ * 196-228, and ApplyGain, visibilitymodifier.h:345-370), all on the device.
+ * Layouts as in wgpu_gridder_add_inversion_data_corrected; the output vis is
+ * [row][chan][n_pol] complex64. */
+int wgpu_gridder_predict_visibilities_corrected(
+    wgpu_gridder_t *gridder, int mode, size_t n_pol, size_t n_rows, const double *uvw,
+    const double *freq, size_t n_chan, const uint64_t *antenna_pairs,
+    const uint64_t *time_offsets, const float *solutions, size_t nparms, size_t n_times,
+    size_t n_ant, int polarization, float *vis);
+
 /* gridder_simple_implementation.h:142-145. */
 int wgpu_gridder_finalize_image(wgpu_gridder_t *gridder, double factor);
 

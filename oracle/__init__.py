@@ -53,6 +53,8 @@ def lib():
         L.oracle_es_fourier.argtypes = [D, I, D]
         L.oracle_apply_gains.restype = I
         L.oracle_apply_gains.argtypes = [I, SZ, SZ, SZ, P, P, P, P, SZ, SZ, I, P]
+        L.oracle_forward_gains.restype = I
+        L.oracle_forward_gains.argtypes = [I, SZ, SZ, SZ, P, P, P, P, SZ, SZ, I, P]
         L.oracle_apply_conjugated_gain.argtypes = [I, P, P, P]
         L.oracle_apply_gain.argtypes = [I, P, P, P]
         _lib = L
@@ -180,6 +182,23 @@ def apply_gains(mode, n_pol, vis, antenna_pairs, time_offsets, solutions, nparms
     out = np.zeros((n_rows, n_chan), np.complex64)
     r = lib().oracle_apply_gains(mode, n_pol, n_rows, n_chan, _p(vis), _p(ant), _p(tof),
                                  _p(sol), nparms, n_ant, polarization, _p(out))
+    if r != 0:
+        raise ValueError("invalid gain mode / polarisation combination")
+    return out
+
+
+def forward_gains(mode, n_pol, vis, antenna_pairs, time_offsets, solutions, nparms, n_ant,
+                  polarization=0):
+    """Prediction write-back: predicted [row][chan] values expanded to n_pol
+    correlations and multiplied by the forward gains; [row][chan][n_pol]."""
+    vis = np.ascontiguousarray(vis, np.complex64)
+    n_rows, n_chan = vis.shape[0], vis.shape[1]
+    ant = np.ascontiguousarray(antenna_pairs, np.uint64)
+    tof = np.ascontiguousarray(time_offsets, np.uint64)
+    sol = np.ascontiguousarray(solutions, np.complex64)
+    out = np.zeros((n_rows, n_chan, n_pol), np.complex64)
+    r = lib().oracle_forward_gains(mode, n_pol, n_rows, n_chan, _p(vis), _p(ant), _p(tof),
+                                   _p(sol), nparms, n_ant, polarization, _p(out))
     if r != 0:
         raise ValueError("invalid gain mode / polarisation combination")
     return out

@@ -951,6 +951,66 @@ static cf collapse4(const float *v, int pol) {
   }
 }
 
+/* Stokes parameter `pol` (or linear correlation 4-7) of value s as linear
+ * correlations (XX, XY, YX, YY): the inverse of collapse4, i.e. XX = I + Q,
+ * YY = I - Q, XY = U + iV, YX = U - iV.  This restates the 4-polarisation
+ * branch of ExpandData (msgridderdata.h:63-68), whose converter
+ * (aocommon::Polarization::ConvertToLinear) is absent from the reference tree:
+ * the convention is the one of collapse4 above, unpinned. */
+static void expand4(cf s, int pol, float *v) {
+  cf z = {0.0f, 0.0f}, o[4] = {z, z, z, z};
+  switch (pol) {
+    case 0: o[0] = s; o[3] = s; break;
+    case 1: { cf m = {-s.re, -s.im}; o[0] = s; o[3] = m; break; }
+    case 2: o[1] = s; o[2] = s; break;
+    case 3: { cf is = {-s.im, s.re}, mis = {s.im, -s.re}; o[1] = is; o[2] = mis; break; }
+    case 4: o[0] = s; break;
+    case 5: o[1] = s; break;
+    case 6: o[2] = s; break;
+    default: o[3] = s; break;
+  }
+  for (int i = 0; i < 4; ++i) st(v, i, o[i]);
+}
+
+int oracle_forward_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
+                         const float *vis_in, const uint64_t *antenna_pairs,
+                         const uint64_t *time_offsets, const float *solutions,
+                         size_t nparms, size_t n_ant, int polarization, float *out) {
+  if (mode_npol(mode) != (int)n_pol) return -1;
+  if (nparms != 2 && nparms != 4) return -1;
+  for (size_t r = 0; r < n_rows; ++r) {
+    const uint64_t a1 = antenna_pairs[2 * r], a2 = antenna_pairs[2 * r + 1];
+    const uint64_t t = time_offsets[r];
+    for (size_t ch = 0; ch < n_chan; ++ch) {
+      /* visibilitymodifier.cpp:205-227 indexing */
+      const size_t off = (t * n_chan + ch) * n_ant * nparms;
+      const float *s1 = solutions + 2 * (off + a1 * nparms);
+      const float *s2 = solutions + 2 * (off + a2 * nparms);
+      float g1[8] = {0}, g2[8] = {0};
+      if (nparms == 2) {
+        g1[0] = s1[0]; g1[1] = s1[1]; g1[6] = s1[2]; g1[7] = s1[3];
+        g2[0] = s2[0]; g2[1] = s2[1]; g2[6] = s2[2]; g2[7] = s2[3];
+      } else {
+        memcpy(g1, s1, sizeof(float) * 8);
+        memcpy(g2, s2, sizeof(float) * 8);
+      }
+      const cf sv = ld(vis_in + 2 * (r * n_chan + ch), 0);
+      float v[8];
+      if (n_pol == 1) {
+        st(v, 0, sv);
+      } else if (n_pol == 2) { /* ExpandData<2>, msgridderdata.h:58-62 */
+        st(v, 0, sv);
+        st(v, 1, sv);
+      } else {
+        expand4(sv, polarization, v);
+      }
+      oracle_apply_gain(mode, v, g1, g2); /* ApplyParmResponse -> ApplyGain */
+      memcpy(out + 2 * ((r * n_chan + ch) * n_pol), v, sizeof(float) * 2 * n_pol);
+    }
+  }
+  return 0;
+}
+
 int oracle_apply_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
                        const float *vis_in, const uint64_t *antenna_pairs,
                        const uint64_t *time_offsets, const float *solutions,

@@ -109,6 +109,16 @@ double oracle_es_fourier(double beta, int support, double f);
  * parm-response layout ((t*n_chan + ch)*n_ant + ant)*nparms; out: collapsed
  * [row][chan] complex64.  polarization (4-pol collapse): 0 StokesI, 1 Q, 2 U,
  * 3 V, 4 XX, 5 XY, 6 YX, 7 YY.  Returns 0 on success, -1 on a bad combination. */
+/* Prediction write-back: predicted [row][chan] complex64 values expanded to
+ * n_pol correlations (1: as is; 2: duplicated, msgridderdata.h:58-62; 4:
+ * Stokes -> linear, the inverse of the collapse above) and multiplied by the
+ * forward gains (visibilitymodifier.h:345-370 through visibilitymodifier.cpp:
+ * 196-228).  out: [row][chan][n_pol] complex64.  Same layouts and return
+ * values as oracle_apply_gains. */
+int oracle_forward_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
+                         const float *vis_in, const uint64_t *antenna_pairs,
+                         const uint64_t *time_offsets, const float *solutions,
+                         size_t nparms, size_t n_ant, int polarization, float *out);
 int oracle_apply_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
                        const float *vis_in, const uint64_t *antenna_pairs,
                        const uint64_t *time_offsets, const float *solutions,

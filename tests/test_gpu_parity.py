@@ -332,6 +332,36 @@ def test_corrected_inversion_matches_oracle_gains(wgpu_lib, oracle_lib, mode, n_
     g.close()
 
 
+@pytest.mark.parametrize("mode,n_pol,nparms", MODES)
+def test_corrected_prediction_matches_oracle_gains(wgpu_lib, oracle_lib, mode, n_pol, nparms):
+    """Prediction write-back on the device (expansion + forward gains) against
+    the oracle's write-back of the same predicted values and of the FP64
+    direct prediction."""
+    from wsclean_gb300.gridder import GainMode
+    W, dl = 128, 4e-4
+    rng = np.random.default_rng(23)
+    n_rows, n_chan, n_ant, n_t = 400, 4, 8, 3
+    uvw, freq, _ = synthetic.random_points(n_rows, n_chan, W, dl, seed=24, w_scale=1.0)
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)], 1)
+    tof = rng.integers(0, n_t, n_rows)
+    sol = (1 + 0.3 * (rng.standard_normal((n_t, n_chan, n_ant, nparms)) +
+                      1j * rng.standard_normal((n_t, n_chan, n_ant, nparms)))).astype(np.complex64)
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, 8, replace=False)] = rng.uniform(-1, 1, 8)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1, epsilon=1e-5, num_t=np.float64)
+    g.InitializePrediction(model)
+    got = g.PredictVisibilitiesWithCorrection(mode, n_pol, n_rows, uvw, freq, n_chan, ant, tof,
+                                              sol, nparms, n_t, n_ant)
+    got = got.reshape(n_rows, n_chan, n_pol)
+    plain = g.PredictVisibilities(n_rows, n_chan, uvw, freq).reshape(n_rows, n_chan)
+    exp = oracle_lib.forward_gains(GainMode[mode], n_pol, plain, ant, tof, sol, nparms, n_ant)
+    assert rel(got, exp) <= 1e-6
+    dft = np.asarray(oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl)).reshape(n_rows, n_chan)
+    ref = oracle_lib.forward_gains(GainMode[mode], n_pol, dft, ant, tof, sol, nparms, n_ant)
+    assert rel(got, ref) <= 1e-5
+    g.close()
+
+
 def test_corrected_inversion_rejects_bad_indices(wgpu_lib):
     W, dl = 64, 1e-3
     g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0, 0, 1)

@@ -78,6 +78,43 @@ def test_gains_table_layout_and_collapse(oracle_lib):
         oracle_lib.apply_gains(0, 2, vis2, ant, tof, sol2, 2, n_ant)
 
 
+def test_forward_gains_expand_and_match_matrix_algebra(oracle_lib):
+    """Prediction write-back: with identity gains the 4-correlation expansion
+    collapses back to the predicted value for every polarisation; with random
+    gains each mode equals its matrix form (G1 V G2^H on the expanded value)."""
+    rng = np.random.default_rng(9)
+    n_rows, n_chan, n_ant, n_t = 5, 3, 4, 2
+    vis = (rng.standard_normal((n_rows, n_chan)) +
+           1j * rng.standard_normal((n_rows, n_chan))).astype(np.complex64)
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)], 1)
+    tof = rng.integers(0, n_t, n_rows)
+    eye = np.zeros((n_t, n_chan, n_ant, 4), np.complex64)
+    eye[..., 0] = eye[..., 3] = 1
+    for pol in range(8):
+        lin = oracle_lib.forward_gains(4, 4, vis, ant, tof, eye, 4, n_ant, polarization=pol)
+        back = oracle_lib.apply_gains(4, 4, lin, ant, tof, eye, 4, n_ant, polarization=pol)
+        np.testing.assert_allclose(back, vis, rtol=1e-6, atol=1e-6)
+    sol = (rng.standard_normal((n_t, n_chan, n_ant, 4)) +
+           1j * rng.standard_normal((n_t, n_chan, n_ant, 4))).astype(np.complex64)
+    full = oracle_lib.forward_gains(4, 4, vis, ant, tof, sol, 4, n_ant, polarization=0)
+    xx = oracle_lib.forward_gains(0, 1, vis, ant, tof, sol, 4, n_ant)
+    dg = oracle_lib.forward_gains(3, 2, vis, ant, tof, sol, 4, n_ant)
+    for r in range(n_rows):
+        for c in range(n_chan):
+            g1 = sol[tof[r], c, ant[r, 0]].astype(np.complex128).reshape(2, 2)
+            g2 = sol[tof[r], c, ant[r, 1]].astype(np.complex128).reshape(2, 2)
+            v = vis[r, c]
+            want = g1 @ np.array([[v, 0], [0, v]]) @ g2.conj().T
+            np.testing.assert_allclose(full[r, c], want.ravel(), rtol=1e-5, atol=1e-5)
+            np.testing.assert_allclose(xx[r, c, 0], g1[0, 0] * v * np.conj(g2[0, 0]),
+                                       rtol=1e-5, atol=1e-5)
+            # diagonal mode: the second value uses the updated first one
+            # (visibilitymodifier.h:359-362)
+            v0 = g1[0, 0] * v * np.conj(g2[0, 0]) + g1[0, 1] * v * np.conj(g2[0, 1])
+            v1 = g1[1, 1] * v * np.conj(g2[1, 1]) + g1[1, 0] * v0 * np.conj(g2[1, 0])
+            np.testing.assert_allclose(dg[r, c], [v0, v1], rtol=1e-5, atol=1e-5)
+
+
 def test_dft_constant_visibility_gives_flat_image(oracle_lib):
     uvw = np.zeros((1, 3))
     freq = np.array([1e8])

@@ -107,6 +107,8 @@ _PROTOS = {
     "wgpu_gridder_add_inversion_data_device": (I, [P, SZ, SZ, P, P, P]),
     "wgpu_gridder_add_inversion_data_corrected": (
         I, [P, I, SZ, SZ, P, P, SZ, P, P, P, P, SZ, SZ, SZ, I]),
+    "wgpu_gridder_predict_visibilities_corrected": (
+        I, [P, I, SZ, SZ, P, P, SZ, P, P, P, SZ, SZ, SZ, I, P]),
     "wgpu_gridder_finalize_image": (I, [P, D]),
     "wgpu_gridder_real_image": (I, [P, P]),
     "wgpu_gridder_initialize_prediction": (I, [P, P]),

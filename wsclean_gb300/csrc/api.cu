@@ -924,6 +924,47 @@ int wgpu_gridder_add_inversion_data_corrected(
   });
 }
 
+int wgpu_gridder_predict_visibilities_corrected(
+    wgpu_gridder_t *g, int mode, size_t n_pol, size_t n_rows, const double *uvw,
+    const double *freq, size_t n_chan, const uint64_t *antenna_pairs,
+    const uint64_t *time_offsets, const float *solutions, size_t nparms, size_t n_times,
+    size_t n_ant, int polarization, float *vis) {
+  if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
+  if (mode < WGPU_GAIN_XX || mode > WGPU_GAIN_FULL)
+    return fail(WGPU_ERR_INVALID, "invalid gain mode");
+  if (n_pol != 1 && n_pol != 2 && n_pol != 4)
+    return fail(WGPU_ERR_INVALID, "n_polarizations must be 1, 2 or 4");
+  const size_t want = mode == WGPU_GAIN_FULL ? 4 : mode == WGPU_GAIN_2VIS_DIAGONAL ? 2 : 1;
+  if (n_pol != want)
+    return fail(WGPU_ERR_INVALID, "gain mode and n_polarizations do not match");
+  if (nparms != 2 && nparms != 4) return fail(WGPU_ERR_INVALID, "nparms must be 2 or 4");
+  if (polarization < 0 || polarization > 7) return fail(WGPU_ERR_INVALID, "invalid polarization");
+  if ((n_rows && n_chan) && (!uvw || !freq || !vis || !antenna_pairs || !time_offsets || !solutions))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kPrediction)
+      throw Error(WGPU_ERR_STATE, "PredictVisibilities before InitializePrediction");
+    if (n_rows == 0 || n_chan == 0) return;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const uint64_t *da = upload(g, kSlotAnt, antenna_pairs, 2 * n_rows);
+    const uint64_t *dt = upload(g, kSlotTimes, time_offsets, n_rows);
+    const float *ds = upload(g, kSlotSol, solutions, 2 * n_times * n_chan * n_ant * nparms);
+    float2 *dp = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n_rows * n_chan);
+    float2 *dout = (float2 *)g->arena.get(kSlotGainVis, sizeof(float2) * n_rows * n_chan * n_pol);
+    int *err = (int *)g->arena.get(kSlotOutVis, sizeof(int) * 4);
+    predict_device(g, n_rows, n_chan, du, df, nullptr, (float *)dp);
+    WGPU_CUDA(cudaMemsetAsync(err, 0, sizeof(int), g->stream));
+    launch_forward_gains(mode, (int)n_pol, (int64_t)n_rows, (int64_t)n_chan, dp, da, dt,
+                         (const float2 *)ds, (int)nparms, (int64_t)n_times, (int64_t)n_ant,
+                         polarization, dout, err, g->stream);
+    int herr = 0;
+    WGPU_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    copy_to_host(g, vis, dout, sizeof(float2) * n_rows * n_chan * n_pol);
+    if (herr) throw Error(WGPU_ERR_INVALID, "antenna index or time offset outside the solution table");
+  });
+}
+
 int wgpu_gridder_finalize_image(wgpu_gridder_t *g, double factor) {
   if (!g) return fail(WGPU_ERR_INVALID, "null gridder");
   return guarded([&] {

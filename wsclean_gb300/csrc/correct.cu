@@ -175,7 +175,115 @@ __global__ void apply_gains_kernel(int mode, int n_pol, int64_t n_rows,
   out[e] = res;
 }
 
+// ---- prediction write-back: forward gains (visibilitymodifier.h:345-370) ----
+// r = a b^H (row-major 2x2)
+__device__ __forceinline__ void mul_herm(const float2 *a, const float2 *b, float2 *r) {
+  r[0] = ca(cm(a[0], cj(b[0])), cm(a[1], cj(b[1])));
+  r[1] = ca(cm(a[0], cj(b[2])), cm(a[1], cj(b[3])));
+  r[2] = ca(cm(a[2], cj(b[0])), cm(a[3], cj(b[1])));
+  r[3] = ca(cm(a[2], cj(b[2])), cm(a[3], cj(b[3])));
+}
+
+// Stokes parameter `pol` (or linear correlation 4-7) of value s as linear
+// correlations (XX, XY, YX, YY): XX = I + Q, YY = I - Q, XY = U + iV,
+// YX = U - iV, the inverse of collapse4 (4-polarisation ExpandData,
+// msgridderdata.h:63-68).
+__device__ __forceinline__ void expand4(float2 s, int pol, float2 *v) {
+  const float2 z = make_float2(0.f, 0.f);
+  v[0] = v[1] = v[2] = v[3] = z;
+  switch (pol) {
+    case 0: v[0] = s; v[3] = s; break;
+    case 1: v[0] = s; v[3] = make_float2(-s.x, -s.y); break;
+    case 2: v[1] = s; v[2] = s; break;
+    case 3: v[1] = make_float2(-s.y, s.x); v[2] = make_float2(s.y, -s.x); break;
+    case 4: v[0] = s; break;
+    case 5: v[1] = s; break;
+    case 6: v[2] = s; break;
+    default: v[3] = s; break;
+  }
+}
+
+// Predicted [row][chan] values -> [row][chan][n_pol] instrumental
+// visibilities: expanded to the correlations (msgridderdata.h:180-202) and
+// multiplied by the forward gains of the row's antennas
+// (visibilitymodifier.cpp:196-228, ApplyGain).
+__global__ void forward_gains_kernel(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
+                                     const float2 *vis_in, const uint64_t *ant_pairs,
+                                     const uint64_t *time_offsets, const float2 *sol, int nparms,
+                                     int64_t n_times, int64_t n_ant, int polarization,
+                                     float2 *out, int *err_flag) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_rows * n_chan) return;
+  const int64_t r = e / n_chan, ch = e - r * n_chan;
+  float2 *o = out + e * n_pol;
+  const uint64_t a1 = ant_pairs[2 * r], a2 = ant_pairs[2 * r + 1];
+  const uint64_t t = time_offsets[r];
+  if (a1 >= (uint64_t)n_ant || a2 >= (uint64_t)n_ant || t >= (uint64_t)n_times) {
+    atomicOr(err_flag, 1);
+    for (int k = 0; k < n_pol; ++k) o[k] = make_float2(0.f, 0.f);
+    return;
+  }
+  const int64_t off = ((int64_t)t * n_chan + ch) * n_ant * nparms;
+  float2 g1[4], g2[4];
+  if (nparms == 2) {
+    g1[0] = sol[off + a1 * 2]; g1[1] = make_float2(0.f, 0.f);
+    g1[2] = make_float2(0.f, 0.f); g1[3] = sol[off + a1 * 2 + 1];
+    g2[0] = sol[off + a2 * 2]; g2[1] = make_float2(0.f, 0.f);
+    g2[2] = make_float2(0.f, 0.f); g2[3] = sol[off + a2 * 2 + 1];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      g1[k] = sol[off + a1 * 4 + k];
+      g2[k] = sol[off + a2 * 4 + k];
+    }
+  }
+  const float2 s = vis_in[e];
+  switch (mode) {
+    case 0: o[0] = cm(cm(g1[0], s), cj(g2[0])); break;
+    case 1: o[0] = cm(cm(g1[3], s), cj(g2[3])); break;
+    case 2: {
+      float2 dd = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) dd = ca(dd, cm(g1[k], cj(g2[k])));
+      o[0] = cm(s, cs(dd, 0.5f));
+      break;
+    }
+    case 3: {
+      // both correlations hold s (ExpandData<2>); the second uses the updated
+      // first one, as ApplyGain does (visibilitymodifier.h:359-362)
+      const float2 v0 = ca(cm(cm(g1[0], s), cj(g2[0])), cm(cm(g1[1], s), cj(g2[1])));
+      const float2 v1 = ca(cm(cm(g1[3], s), cj(g2[3])), cm(cm(g1[2], v0), cj(g2[2])));
+      o[0] = v0;
+      o[1] = v1;
+      break;
+    }
+    default: {
+      float2 v[4], t1[4], t2[4];
+      expand4(s, polarization, v);
+      mat_mul(g1, v, t1);
+      mul_herm(t1, g2, t2);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[k] = t2[k];
+      break;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_forward_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
+                          const float2 *vis_in, const uint64_t *ant_pairs,
+                          const uint64_t *time_offsets, const float2 *sol, int nparms,
+                          int64_t n_times, int64_t n_ant, int polarization, float2 *out,
+                          int *err_flag, cudaStream_t s) {
+  const int64_t n = n_rows * n_chan;
+  if (n <= 0) return;
+  forward_gains_kernel<<<blocks_for(n), kThreads, 0, s>>>(mode, n_pol, n_rows, n_chan, vis_in,
+                                                          ant_pairs, time_offsets, sol, nparms,
+                                                          n_times, n_ant, polarization, out,
+                                                          err_flag);
+  check_launch("forward_gains_kernel");
+}
 
 void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s) {
   const int64_t n = (int64_t)p.width * p.height;

@@ -293,6 +293,13 @@ void launch_restamp(const VisRecord *geom, const uint32_t *perm, const float2 *v
 void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
                               const float2 *acc, int64_t n, float2 *vis,
                               cudaStream_t s);
+// Forward gains on predicted [row][chan] values -> [row][chan][n_pol]
+// (prediction write-back; same layouts and error flag as launch_apply_gains).
+void launch_forward_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
+                          const float2 *vis_in, const uint64_t *ant_pairs,
+                          const uint64_t *time_offsets, const float2 *sol, int nparms,
+                          int64_t n_times, int64_t n_ant, int polarization, float2 *out,
+                          int *err_flag, cudaStream_t s);
 void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                         const float2 *vis_in, const uint64_t *ant_pairs,
                         const uint64_t *time_offsets, const float2 *sol,

@@ -105,6 +105,27 @@ class WGriddingGridder_Simple:
             n_channels, ptr(ant), ptr(vis), ptr(tof), ptr(sol), nparms, n_times, n_antenna,
             int(polarization)))
 
+    def PredictVisibilitiesWithCorrection(self, mode, n_polarizations, n_rows, uvws,
+                                          frequencies, n_channels, antennas, time_offsets,
+                                          solutions, nparms, n_times, n_antenna,
+                                          polarization=_lib.POL_I):
+        """PredictVisibilities followed by the prediction write-back of
+        msgridderdata.h:180-202, 943-1003 (expansion to the correlations and the
+        forward gains of each row's antennas) on the device; returns
+        [n_rows * n_channels * n_polarizations] complex64."""
+        if isinstance(mode, str):
+            mode = GainMode[mode]
+        uvws, frequencies = _f64(uvws), _f64(frequencies)
+        ant = np.ascontiguousarray(antennas, dtype=np.uint64)
+        tof = np.ascontiguousarray(time_offsets, dtype=np.uint64)
+        sol = _c64(solutions)
+        out = np.empty(n_rows * n_channels * n_polarizations, dtype=np.complex64)
+        check(lib().wgpu_gridder_predict_visibilities_corrected(
+            self._h, int(mode), n_polarizations, n_rows, ptr(uvws), ptr(frequencies),
+            n_channels, ptr(ant), ptr(tof), ptr(sol), nparms, n_times, n_antenna,
+            int(polarization), ptr(out)))
+        return out
+
     def FinalizeImage(self, multiplication_factor):
         check(lib().wgpu_gridder_finalize_image(self._h, float(multiplication_factor)))
 
