@@ -184,6 +184,26 @@ class WGriddingGridder_Simple final : public WGriddingGridderBase {
                                                          reinterpret_cast<float *>(vis)));
   }
 
+  /* PredictVisibilities followed by the write-back of msgridderdata.h:180-202,
+   * 943-1003 (expansion to n_polarizations correlations and the forward gains
+   * of each row's antennas), on the device; vis is [row][chan][n_pol]. */
+  void PredictVisibilitiesWithCorrections(GainMode mode, size_t n_polarizations,
+                                          size_t n_rows, const double *uvws,
+                                          const double *frequencies, size_t n_channels,
+                                          const std::pair<size_t, size_t> *antennas,
+                                          const size_t *time_offsets,
+                                          const GpuCorrectionTable &table, size_t n_antenna,
+                                          std::complex<float> *vis) const {
+    static_assert(sizeof(std::pair<size_t, size_t>) == 2 * sizeof(uint64_t),
+                  "antenna pairs are passed as two 64-bit indices");
+    wgpu_detail::check(wgpu_gridder_predict_visibilities_corrected(
+        g_, static_cast<int>(mode), n_polarizations, n_rows, uvws, frequencies, n_channels,
+        reinterpret_cast<const uint64_t *>(antennas),
+        reinterpret_cast<const uint64_t *>(time_offsets),
+        reinterpret_cast<const float *>(table.solutions), table.nparms, table.n_times,
+        n_antenna, table.polarization, reinterpret_cast<float *>(vis)));
+  }
+
   wgpu_gridder_t *handle() const { return g_; }
 
  private:

@@ -59,6 +59,24 @@ int main(int argc, char **argv) {
     std::vector<std::complex<float>> pred(n_rows * n_chan);
     base.PredictVisibilities(n_rows, n_chan, uvw.data(), freq.data(), pred.data());
     write_file(prefix + "pred.bin", pred);
+    // Corrected prediction with one diagonal gain g for every antenna, time
+    // and channel: the XX mode writes g * V * conj(g) = |g|^2 V.
+    const size_t n_ant = 3;
+    std::vector<std::pair<size_t, size_t>> antennas(n_rows);
+    std::vector<size_t> time_offsets(n_rows, 0);
+    for (size_t r = 0; r < n_rows; ++r) antennas[r] = {r % n_ant, (r + 1) % n_ant};
+    std::vector<std::complex<float>> solutions(n_chan * n_ant * 2,
+                                               std::complex<float>(1.5f, 0.5f));
+    wsclean::GpuCorrectionTable table;
+    table.solutions = solutions.data();
+    table.n_times = 1;
+    table.nparms = 2;
+    std::vector<std::complex<float>> pred_corr(n_rows * n_chan);
+    g.PredictVisibilitiesWithCorrections(wsclean::GainMode::kXX, 1, n_rows, uvw.data(),
+                                         freq.data(), n_chan, antennas.data(),
+                                         time_offsets.data(), table, n_ant,
+                                         pred_corr.data());
+    write_file(prefix + "pred_corr.bin", pred_corr);
     // bad argument -> std::runtime_error, as the reference's MR_assert throws
     bool threw = false;
     try {

@@ -52,3 +52,6 @@ def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
     trimmed = model[d:d + Wt, d:d + Wt].ravel()
     pr = oracle_lib.dft_predict(uvw, freq, trimmed, Wt, Wt, dl, dl)
     assert np.linalg.norm(pred - pr) / np.linalg.norm(pr) <= eps
+    # uniform diagonal gain 1.5+0.5i, XX mode: |g|^2 = 2.5 times the prediction
+    pred_corr = np.fromfile(prefix + "pred_corr.bin", np.complex64)
+    np.testing.assert_allclose(pred_corr, 2.5 * pred, rtol=1e-5, atol=1e-6 * np.abs(pred).max())
