@@ -471,6 +471,131 @@ int wgpu_facets_job_plan(const wgpu_facets_t *facets, size_t job, wgpu_plan_t *p
 void *wgpu_facets_stream(wgpu_facets_t *facets);
 void wgpu_facets_destroy(wgpu_facets_t *facets);
 
+/* ---- Imaging weights and per-row preparation ---------------------------
+ * The imaging-weight grid of ImageWeights (structures/imageweights.h,
+ * structures/imageweights.cpp) and the per-row weighting of MsGridderData
+ * (CalculateWeightsImplementation + ApplyWeights + CollapseData,
+ * gridding/msgridderdata.h:36-52, 515-548, 760-886) on the device, so that
+ * raw measurement-set rows (visibilities, weights, selection) are weighted,
+ * collapsed and gridded without a pass over them on the host. */
+
+/* WeightMode::WeightingEnum (structures/weightmode.h:14). */
+#define WGPU_WEIGHT_NATURAL 0
+#define WGPU_WEIGHT_UNIFORM 1
+#define WGPU_WEIGHT_BRIGGS 2
+
+/* VisibilityWeightingMode (gridding/visibilityweightingmode.h:11-15). */
+#define WGPU_VISW_NORMAL 0
+#define WGPU_VISW_SQUARED 1
+#define WGPU_VISW_UNIT 2
+
+/* PsfMode (gridding/msgridderdata.h:26-32). */
+#define WGPU_PSF_NONE 0
+#define WGPU_PSF_SINGLE 1
+#define WGPU_PSF_DIRECTION_DEPENDENT 2
+
+/* Grid operations after FinishGridding (imageweights.cpp:149-351); the
+ * meaning of wgpu_imageweights_taper's a and b per kind. */
+#define WGPU_TAPER_MIN_UV 0      /* SetMinUVRange(a) */
+#define WGPU_TAPER_MAX_UV 1      /* SetMaxUVRange(a) */
+#define WGPU_TAPER_TUKEY 2       /* SetTukeyTaper(a = transition, b = max uv) */
+#define WGPU_TAPER_TUKEY_INNER 3 /* SetTukeyInnerTaper(a = transition, b = min uv) */
+#define WGPU_TAPER_EDGE 4        /* SetEdgeTaper(a) */
+#define WGPU_TAPER_EDGE_TUKEY 5  /* SetEdgeTukeyTaper(a = transition, b = edge) */
+#define WGPU_TAPER_GAUSSIAN 6    /* SetGaussianTaper(a = beam size, radians) */
+#define WGPU_TAPER_RANK_FILTER 7 /* RankFilter(a = rank limit, b = window, <= 256) */
+
+typedef struct wgpu_imageweights wgpu_imageweights_t;
+
+/* ImageWeights(weightMode, imageWidth, imageHeight, pixelScaleX, pixelScaleY,
+ * weightsAsTaper, superWeight) (imageweights.cpp:34-49): a grid of
+ * width x height/2 doubles on the current device, width and height being
+ * round(size / super_weight) made even.  briggs_robustness is used by
+ * WGPU_WEIGHT_BRIGGS only. */
+int wgpu_imageweights_create(int mode, double briggs_robustness, size_t image_width,
+                             size_t image_height, double pixel_scale_x, double pixel_scale_y,
+                             int weights_as_taper, double super_weight,
+                             wgpu_imageweights_t **out);
+void wgpu_imageweights_destroy(wgpu_imageweights_t *iw);
+
+/* ImageWeights::Grid(MSProvider &, BandData) (imageweights.cpp:75-112) over
+ * one chunk of rows: uvw [row][3] metres, freq [n_chan] Hz, weights
+ * [row][chan][n_pol].  Call once per chunk, before FinishGridding. */
+int wgpu_imageweights_grid(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan,
+                           size_t n_pol, const double *uvw, const double *freq,
+                           const float *weights);
+
+/* FinishGridding (imageweights.cpp:114-147); a second call fails with
+ * WGPU_ERR_STATE. */
+int wgpu_imageweights_finish(wgpu_imageweights_t *iw);
+
+/* One of the WGPU_TAPER_* grid operations. */
+int wgpu_imageweights_taper(wgpu_imageweights_t *iw, int kind, double a, double b);
+
+/* SetAllValues (imageweights.h:60). */
+int wgpu_imageweights_set_all(wgpu_imageweights_t *iw, double value);
+
+/* The grid: mirrored = 0 gives the width x height/2 half-plane as stored,
+ * mirrored = 1 the width x height image of GetGrid (imageweights.cpp:284-300). */
+int wgpu_imageweights_get(const wgpu_imageweights_t *iw, int mirrored, double *out);
+
+/* Width(), Height() and the sum of the gridded weights. */
+int wgpu_imageweights_info(const wgpu_imageweights_t *iw, size_t *width, size_t *height,
+                           double *total_sum);
+
+/* GetWeight(u, v) (imageweights.h:36) for n points in wavelengths. */
+int wgpu_imageweights_sample(const wgpu_imageweights_t *iw, size_t n, const double *u,
+                             const double *v, double *out);
+
+/* What CalculateWeightsImplementation reads from the gridder's settings. */
+typedef struct wgpu_row_weighting {
+  int psf_mode;             /* WGPU_PSF_*: grid a point source instead of the data */
+  double psf_dl, psf_dm;    /* its shift: MainImageDL/DM (single) or LShift/MShift */
+  int subtract_model;       /* DoSubtractModel(): vis -= model before weighting */
+  int visibility_weighting; /* WGPU_VISW_* */
+  int polarization;         /* WGPU_POL_* target of the 4-correlation collapse */
+} wgpu_row_weighting_t;
+
+/* The sums ApplyWeights accumulates (msgridderdata.h:760-789); calls add to
+ * them (max: the larger), so zero the struct where the reference resets
+ * them (msgridderdata.h:253-259). */
+typedef struct wgpu_weight_sums {
+  double visibility_weight_sum;      /* VisibilityWeightSum() */
+  double max_gridded_weight;         /* MaxGriddedWeight() */
+  double total_weight;               /* total_weight_ */
+  uint64_t gridded_visibility_count; /* GriddedVisibilityCount() */
+} wgpu_weight_sums_t;
+
+/* CalculateWeights + ApplyWeights + CollapseData for rows without
+ * corrections (msgridderdata.h:515-548, 760-886), on the image weights'
+ * device:
+ *   vis      [row][chan][n_pol] complex64 (not read in PSF mode: may be NULL)
+ *   weights  [row][chan][n_pol] visibility weights
+ *   model    [row][chan][n_pol] complex64 (read when subtract_model)
+ *   selected [row][chan] bytes, 0 = not gridded in this pass (NULL: all)
+ * Outputs: vis_out [row][chan] complex64 (weighted, collapsed to one value),
+ * weights_out [row][chan][n_pol] (the cumulative weights ApplyWeights leaves
+ * in the weight buffer; may be NULL), imaging_weights_out [row][chan] (what
+ * StoreImagingWeights writes; may be NULL); sums may be NULL. */
+int wgpu_prepare_rows(const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw,
+                      size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,
+                      const double *freq, const float *vis, const float *weights,
+                      const float *model, const uint8_t *selected, float *vis_out,
+                      float *weights_out, float *imaging_weights_out,
+                      wgpu_weight_sums_t *sums);
+
+/* GetCollapsedVisibilities followed by AddInversionData for one chunk of raw
+ * rows (WGriddingMSGridder::GridMeasurementSet, wgridder/wgriddingmsgridder.cpp:
+ * 117-180, without corrections): the
+ * rows are weighted and collapsed as in wgpu_prepare_rows, on the gridder's
+ * stream, and gridded without leaving the device. */
+int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *gridder, const wgpu_imageweights_t *iw,
+                                    const wgpu_row_weighting_t *rw, size_t n_pol,
+                                    size_t n_rows, size_t n_chan, const double *uvw,
+                                    const double *freq, const float *vis,
+                                    const float *weights, const float *model,
+                                    const uint8_t *selected, wgpu_weight_sums_t *sums);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,16 @@ def lib():
         L.oracle_forward_gains.argtypes = [I, SZ, SZ, SZ, P, P, P, P, SZ, SZ, I, P]
         L.oracle_apply_conjugated_gain.argtypes = [I, P, P, P]
         L.oracle_apply_gain.argtypes = [I, P, P, P]
+        I64 = C.c_int64
+        L.oracle_weights_dims.argtypes = [SZ, SZ, D, C.POINTER(I64), C.POINTER(I64)]
+        L.oracle_weights_grid.restype = D
+        L.oracle_weights_grid.argtypes = [P, I64, I64, D, D, I, SZ, SZ, SZ, P, P, P]
+        L.oracle_weights_finish.argtypes = [P, I64, I64, I, D, D]
+        L.oracle_weights_taper.argtypes = [P, I64, I64, D, D, I, D, D]
+        L.oracle_weights_mirror.argtypes = [P, I64, I64, P]
+        L.oracle_weights_sample.argtypes = [P, I64, I64, D, D, SZ, P, P, P]
+        L.oracle_prepare_rows.argtypes = [P, I64, I64, D, D, I, D, D, I, I, I, SZ, SZ, SZ, P, P,
+                                          P, P, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -218,3 +228,78 @@ def apply_gain(mode, vis, g1, g2):
     b = np.ascontiguousarray(g2, np.complex64)
     lib().oracle_apply_gain(mode, _p(v), _p(a), _p(b))
     return v
+
+
+class ImageWeights:
+    """The oracle's imaging-weight grid (ImageWeights restated in C): the same
+    operations as the product's wsclean_gb300.weights.ImageWeights, serially
+    and in the reference's order.  grid: (height/2, width) float64."""
+
+    def __init__(self, mode, image_width, image_height, pixel_scale_x, pixel_scale_y,
+                 weights_as_taper=False, super_weight=1.0, briggs_robustness=0.0):
+        w, h = C.c_int64(), C.c_int64()
+        lib().oracle_weights_dims(image_width, image_height, super_weight, C.byref(w),
+                                  C.byref(h))
+        self.width, self.height = w.value, h.value
+        self.mode, self.robustness = int(mode), float(briggs_robustness)
+        self.psx, self.psy = float(pixel_scale_x), float(pixel_scale_y)
+        self.as_taper = bool(weights_as_taper)
+        self.grid = np.zeros((self.height // 2, self.width), np.float64)
+        self.total = 0.0
+
+    def grid_rows(self, uvw, freq, weights):
+        uvw = np.ascontiguousarray(uvw, np.float64)
+        freq = np.ascontiguousarray(freq, np.float64)
+        wts = np.ascontiguousarray(weights, np.float32)
+        n_rows, n_chan = uvw.shape[0], freq.size
+        n_pol = wts.size // (n_rows * n_chan) if n_rows * n_chan else 1
+        self.total += lib().oracle_weights_grid(_p(self.grid), self.width, self.height,
+                                                self.psx, self.psy, int(self.as_taper), n_rows,
+                                                n_chan, n_pol, _p(uvw), _p(freq), _p(wts))
+
+    def finish(self):
+        lib().oracle_weights_finish(_p(self.grid), self.width, self.height, self.mode,
+                                    self.robustness, self.total)
+
+    def taper(self, kind, a, b=0.0):
+        lib().oracle_weights_taper(_p(self.grid), self.width, self.height, self.psx, self.psy,
+                                   int(kind), float(a), float(b))
+
+    def mirrored(self):
+        out = np.zeros((self.height, self.width), np.float64)
+        lib().oracle_weights_mirror(_p(self.grid), self.width, self.height, _p(out))
+        return out
+
+    def sample(self, u, v):
+        u = np.ascontiguousarray(u, np.float64).ravel()
+        v = np.ascontiguousarray(v, np.float64).ravel()
+        out = np.zeros(u.size, np.float64)
+        lib().oracle_weights_sample(_p(self.grid), self.width, self.height, self.psx, self.psy,
+                                    u.size, _p(u), _p(v), _p(out))
+        return out
+
+    def prepare_rows(self, uvw, freq, weights, vis=None, model=None, selected=None,
+                     psf_mode=0, psf_dl=0.0, psf_dm=0.0, visibility_weighting=0,
+                     polarization=0):
+        """CalculateWeights + ApplyWeights + CollapseData over [row][chan][pol]
+        inputs; returns (vis_out [row, chan], weights_out [row, chan, pol],
+        imaging weights [row, chan], sums [vws, max, total, count])."""
+        uvw = np.ascontiguousarray(uvw, np.float64)
+        freq = np.ascontiguousarray(freq, np.float64)
+        wts = np.ascontiguousarray(weights, np.float32)
+        n_rows, n_chan, n_pol = wts.shape
+        vis_a = None if vis is None else np.ascontiguousarray(vis, np.complex64)
+        mod_a = None if model is None else np.ascontiguousarray(model, np.complex64)
+        sel_a = None if selected is None else np.ascontiguousarray(selected, np.uint8)
+        vis_out = np.zeros((n_rows, n_chan), np.complex64)
+        w_out = np.zeros((n_rows, n_chan, n_pol), np.float32)
+        iw_out = np.zeros((n_rows, n_chan), np.float32)
+        sums = np.zeros(4, np.float64)
+        lib().oracle_prepare_rows(
+            _p(self.grid), self.width, self.height, self.psx, self.psy, int(psf_mode),
+            float(psf_dl), float(psf_dm), int(mod_a is not None), int(visibility_weighting),
+            int(polarization), n_pol, n_rows, n_chan, _p(uvw), _p(freq),
+            None if vis_a is None else _p(vis_a), _p(wts), None if mod_a is None else _p(mod_a),
+            None if sel_a is None else _p(sel_a), _p(vis_out), _p(w_out), _p(iw_out),
+            _p(sums))
+        return vis_out, w_out, iw_out, sums

@@ -1047,3 +1047,283 @@ int oracle_apply_gains(int mode, size_t n_pol, size_t n_rows, size_t n_chan,
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Imaging weights (structures/imageweights.{h,cpp}) and raw-row weighting    */
+/* (gridding/msgridderdata.h:36-52, 760-886).                                 */
+/* ------------------------------------------------------------------------ */
+
+void oracle_weights_dims(size_t image_width, size_t image_height, double super_weight,
+                         int64_t *width, int64_t *height) {
+  int64_t w = (int64_t)round((double)image_width / super_weight);
+  int64_t h = (int64_t)round((double)image_height / super_weight);
+  if (w % 2 != 0) ++w;
+  if (h % 2 != 0) ++h;
+  *width = w;
+  *height = h;
+}
+
+/* uvToXY + isWithinLimits (imageweights.h:74-96); -1 outside the grid. */
+static int64_t weights_cell(double u, double v, int64_t W, int64_t H, double psx, double psy) {
+  if (v < 0.0) {
+    u = -u;
+    v = -v;
+  }
+  const double fx = floor(u * (double)W * psx + (double)(W / 2));
+  const double fy = floor(v * (double)H * psy);
+  if (!(fx >= 0.0 && fx < (double)W && fy >= 0.0 && fy < (double)(H / 2))) return -1;
+  return (int64_t)fx + (int64_t)fy * W;
+}
+
+/* xyToUV (imageweights.h:83-91). */
+static void weights_uv(int64_t x, int64_t y, int64_t W, int64_t H, double psx, double psy,
+                       double *u, double *v) {
+  *u = (double)(x - W / 2) / ((double)W * psx);
+  *v = (double)y / ((double)H * psy);
+}
+
+/* tukeyFrom0ToN (imageweights.h:114-116). */
+static double weights_tukey(double x, double n) {
+  return 0.5 * (1.0 + cos((M_PI / n) * (x - n)));
+}
+
+double oracle_weights_grid(double *grid, int64_t W, int64_t H, double psx, double psy,
+                           int as_taper, size_t n_rows, size_t n_chan, size_t n_pol,
+                           const double *uvw, const double *freq, const float *weights) {
+  double total = 0.0;
+  for (size_t r = 0; r < n_rows; ++r) {
+    double um = uvw[3 * r], vm = uvw[3 * r + 1];
+    if (vm < 0.0) {
+      um = -um;
+      vm = -vm;
+    }
+    for (size_t ch = 0; ch < n_chan; ++ch) {
+      const double lambda = C_LIGHT / freq[ch];
+      const double u = um / lambda, v = vm / lambda;
+      for (size_t p = 0; p < n_pol; ++p) {
+        float w = weights[(r * n_chan + ch) * n_pol + p];
+        if (as_taper && w != 0.0f) w = 1.0f;
+        const int64_t cell = weights_cell(u, v, W, H, psx, psy);
+        if (cell >= 0) {
+          grid[cell] += w;
+          total += w;
+        }
+      }
+    }
+  }
+  return total;
+}
+
+void oracle_weights_finish(double *grid, int64_t W, int64_t H, int mode, double robustness,
+                           double total_sum) {
+  const int64_t n = W * (H / 2);
+  if (mode == 2) {
+    double avg_w = 0.0;
+    for (int64_t i = 0; i < n; ++i) avg_w += grid[i] * grid[i];
+    avg_w /= total_sum;
+    const double numerator_sqrt = 5.0 * exp((-M_LN10) * robustness);
+    const double s_sq = numerator_sqrt * numerator_sqrt / avg_w;
+    for (int64_t i = 0; i < n; ++i)
+      if (grid[i] != 0.0) grid[i] = 1.0 / (1.0 + grid[i] * s_sq);
+  } else if (mode == 1) {
+    for (int64_t i = 0; i < n; ++i) grid[i] = grid[i] != 0.0 ? 1.0 / grid[i] : 0.0;
+  } else {
+    for (int64_t i = 0; i < n; ++i)
+      if (grid[i] != 0.0) grid[i] = 1.0;
+  }
+}
+
+/* windowMean (imageweights.cpp:353-388). */
+static double weights_window_mean(const double *grid, int64_t W, int64_t Hh, int64_t x,
+                                  int64_t y, int64_t window) {
+  const int64_t d = window / 2;
+  const int64_t x1 = x <= d ? 0 : x - d, y1 = y <= d ? 0 : y - d;
+  const int64_t x2 = x + d >= W ? W : x + d, y2 = y + d >= Hh ? Hh : y + d;
+  int64_t count = 0;
+  double sum = 0.0;
+  for (int64_t yi = y1; yi < y2; ++yi)
+    for (int64_t xi = x1; xi < x2; ++xi) {
+      const double w = grid[yi * W + xi];
+      if (w != 0.0) {
+        ++count;
+        sum += w;
+      }
+    }
+  return sum / (double)count;
+}
+
+void oracle_weights_taper(double *grid, int64_t W, int64_t H, double psx, double psy, int kind,
+                          double a, double b) {
+  const int64_t Hh = H / 2, n = W * Hh;
+  if (kind == 7) { /* RankFilter (imageweights.cpp:310-326) */
+    double *src = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(src, grid, sizeof(double) * (size_t)n);
+    for (int64_t y = 0; y < Hh; ++y)
+      for (int64_t x = 0; x < W; ++x) {
+        const double w = src[y * W + x];
+        if (w != 0.0) {
+          const double mean = weights_window_mean(src, W, Hh, x, y, (int64_t)b);
+          if (w > mean * a) grid[y * W + x] = mean * a;
+        }
+      }
+    free(src);
+    return;
+  }
+  double m2s2 = 0.0, max_u = 0.0, max_v = 0.0;
+  if (kind == 6) { /* SetGaussianTaper (imageweights.cpp:328-351) */
+    const double half_power_uv = 1.0 / (a * 2.0 * M_PI);
+    const long double sigma_to_hp = 2.0L * sqrtl(2.0L * logl(2.0L));
+    m2s2 = half_power_uv * sigma_to_hp;
+    m2s2 *= -2.0 * m2s2;
+  }
+  weights_uv(W, Hh, W, H, psx, psy, &max_u, &max_v);
+  for (int64_t y = 0; y < Hh; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      double *g = grid + y * W + x;
+      double u, v;
+      weights_uv(x, y, W, H, psx, psy, &u, &v);
+      const double d2 = u * u + v * v;
+      switch (kind) {
+        case 0: /* SetMinUVRange (:149-165) */
+          if (d2 < a * a) *g = 0.0;
+          break;
+        case 1: /* SetMaxUVRange (:167-183) */
+          if (d2 > a * a) *g = 0.0;
+          break;
+        case 2: /* SetTukeyTaper (:185-208): a transition, b max uv */
+          if (d2 > b * b)
+            *g = 0.0;
+          else if (d2 > (b - a) * (b - a))
+            *g *= weights_tukey(b - sqrt(d2), a);
+          break;
+        case 3: /* SetTukeyInnerTaper (:210-233): a transition, b min uv */
+          if (d2 < b * b)
+            *g = 0.0;
+          else if (d2 < (b + a) * (b + a))
+            *g *= weights_tukey(sqrt(d2) - b, a);
+          break;
+        case 4: /* SetEdgeTaper (:235-252) */
+          if (max_u - fabs(u) < a || max_v - fabs(v) < a) *g = 0.0;
+          break;
+        case 5: { /* SetEdgeTukeyTaper (:254-282): a transition, b edge */
+          const double ud = max_u - fabs(u), vd = max_v - fabs(v), total = a + b;
+          if (ud < b || vd < b) {
+            *g = 0.0;
+          } else if (ud < total || vd < total) {
+            double ru = ud - b, rv = vd - b;
+            if (ru > a) ru = a;
+            if (rv > a) rv = a;
+            *g *= weights_tukey(ru, a) * weights_tukey(rv, a);
+          }
+          break;
+        }
+        case 6:
+          if (*g != 0.0) *g = *g * exp(d2 / m2s2);
+          break;
+        default:
+          break;
+      }
+    }
+}
+
+void oracle_weights_mirror(const double *grid, int64_t W, int64_t H, double *image) {
+  for (int64_t y = 0; y < H / 2; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      image[(H / 2 - 1 - y) * W + (W - x - 1)] = grid[y * W + x];
+      image[(H / 2 + y) * W + x] = grid[y * W + x];
+    }
+}
+
+void oracle_weights_sample(const double *grid, int64_t W, int64_t H, double psx, double psy,
+                           size_t n, const double *u, const double *v, double *out) {
+  for (size_t i = 0; i < n; ++i) {
+    const int64_t cell = weights_cell(u[i], v[i], W, H, psx, psy);
+    out[i] = cell >= 0 ? grid[cell] : 0.0;
+  }
+}
+
+void oracle_prepare_rows(const double *grid, int64_t W, int64_t H, double psx, double psy,
+                         int psf_mode, double psf_dl, double psf_dm, int subtract_model,
+                         int visibility_weighting, int polarization, size_t n_pol,
+                         size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+                         const float *vis, const float *weights, const float *model,
+                         const uint8_t *selected, float *vis_out, float *weights_out,
+                         float *imaging_out, double *sums) {
+  float *row = (float *)malloc(sizeof(float) * 2 * n_chan * n_pol);
+  float *wrow = (float *)malloc(sizeof(float) * n_chan * n_pol);
+  float *scratch_iw = (float *)malloc(sizeof(float) * n_chan);
+  for (size_t r = 0; r < n_rows; ++r) {
+    const double *ruvw = uvw + 3 * r;
+    const size_t base = r * n_chan * n_pol;
+    memcpy(wrow, weights + base, sizeof(float) * n_chan * n_pol);
+    if (psf_mode != 0) { /* msgridderdata.h:826-843 */
+      for (size_t i = 0; i < n_chan * n_pol; ++i) {
+        row[2 * i] = 1.0f;
+        row[2 * i + 1] = 0.0f;
+      }
+      if (psf_dl != 0.0 || psf_dm != 0.0) {
+        const double dn = sqrt(1.0 - psf_dl * psf_dl - psf_dm * psf_dm) - 1.0;
+        const double shift = 2.0 * M_PI * (ruvw[0] * psf_dl + ruvw[1] * psf_dm + ruvw[2] * dn);
+        for (size_t ch = 0; ch < n_chan; ++ch) { /* RotateVisibilities, :929-941 */
+          const double rad = shift / (C_LIGHT / freq[ch]);
+          const cf ph = {(float)cos(rad), (float)sin(rad)};
+          for (size_t p = 0; p < n_pol; ++p) {
+            float *c = row + 2 * (ch * n_pol + p);
+            st(c, 0, cmul(ld(c, 0), ph));
+          }
+        }
+      }
+    } else {
+      memcpy(row, vis + 2 * base, sizeof(float) * 2 * n_chan * n_pol);
+    }
+    if (subtract_model) /* :845-852 */
+      for (size_t i = 0; i < 2 * n_chan * n_pol; ++i) row[i] -= model[2 * base + i];
+    for (size_t ch = 0; ch < n_chan; ++ch) /* :857-862 */
+      if (selected && !selected[r * n_chan + ch])
+        for (size_t p = 0; p < n_pol; ++p) wrow[ch * n_pol + p] = 0.0f;
+    for (size_t i = 0; i < n_chan * n_pol; ++i) { /* :864-878 */
+      if (visibility_weighting == 1)
+        wrow[i] *= wrow[i];
+      else if (visibility_weighting == 2 && wrow[i] != 0.0f)
+        wrow[i] = 1.0f;
+    }
+    for (size_t ch = 0; ch < n_chan; ++ch) { /* :880-885 */
+      const double lambda = C_LIGHT / freq[ch];
+      double w;
+      oracle_weights_sample(grid, W, H, psx, psy, 1, (const double[]){ruvw[0] / lambda},
+                            (const double[]){ruvw[1] / lambda}, &w);
+      scratch_iw[ch] = (float)w;
+    }
+    for (size_t ch = 0; ch < n_chan; ++ch) /* ApplyWeights, :760-789 */
+      for (size_t p = 0; p < n_pol; ++p) {
+        const size_t i = ch * n_pol + p;
+        const float cum = wrow[i] * scratch_iw[ch];
+        const int has = cum != 0.0f;
+        if (p == 0) {
+          sums[0] += wrow[i] * (float)has;
+          if ((double)cum > sums[1]) sums[1] = (double)cum;
+          sums[3] += has;
+        }
+        sums[2] += cum;
+        wrow[i] = cum;
+        row[2 * i] *= cum;
+        row[2 * i + 1] *= cum;
+      }
+    for (size_t ch = 0; ch < n_chan; ++ch) { /* CollapseData, :36-52 */
+      const float *c = row + 2 * ch * n_pol;
+      cf out;
+      if (n_pol == 1)
+        out = ld(c, 0);
+      else if (n_pol == 2)
+        out = cadd(ld(c, 0), ld(c, 1));
+      else
+        out = collapse4(c, polarization);
+      st(vis_out + 2 * (r * n_chan + ch), 0, out);
+      if (imaging_out) imaging_out[r * n_chan + ch] = scratch_iw[ch];
+    }
+    if (weights_out) memcpy(weights_out + base, wrow, sizeof(float) * n_chan * n_pol);
+  }
+  free(row);
+  free(wrow);
+  free(scratch_iw);
+}

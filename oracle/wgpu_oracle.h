@@ -130,6 +130,50 @@ void oracle_apply_conjugated_gain(int mode, float *vis, const float *g1,
                                   const float *g2);
 void oracle_apply_gain(int mode, float *vis, const float *g1, const float *g2);
 
+/* ---- Imaging weights and raw-row weighting --------------------------------
+ * ImageWeights (structures/imageweights.h, structures/imageweights.cpp) and
+ * MsGridderData's CalculateWeightsImplementation + ApplyWeights + CollapseData
+ * (gridding/msgridderdata.h:36-52, 760-886), restated in serial loops in the
+ * reference's order.  Parity status: pinned by reading the reference source
+ * (it needs aocommon, which the reference tree does not contain, so it cannot
+ * be built here) and by the pure-Python known-answer restatement in the
+ * tests.  The wavelength of a channel is 299792458 / frequency in double; the
+ * 4-correlation collapse is the convention of collapse4 above (unpinned).
+ * The grid is width x height/2 doubles, cell (x, y) at [x + y * width]. */
+
+/* imageweights.cpp:34-49: the grid size after the super weight. */
+void oracle_weights_dims(size_t image_width, size_t image_height, double super_weight,
+                         int64_t *width, int64_t *height);
+/* Grid(MSProvider &, BandData) (imageweights.cpp:75-112) over one chunk;
+ * returns the weight it added to the total. */
+double oracle_weights_grid(double *grid, int64_t width, int64_t height, double psx, double psy,
+                           int as_taper, size_t n_rows, size_t n_chan, size_t n_pol,
+                           const double *uvw, const double *freq, const float *weights);
+/* FinishGridding (imageweights.cpp:114-147); mode 0 natural, 1 uniform,
+ * 2 Briggs. */
+void oracle_weights_finish(double *grid, int64_t width, int64_t height, int mode,
+                           double robustness, double total_sum);
+/* The WGPU_TAPER_* operations (imageweights.cpp:149-351), same a / b. */
+void oracle_weights_taper(double *grid, int64_t width, int64_t height, double psx, double psy,
+                          int kind, double a, double b);
+/* GetGrid (imageweights.cpp:284-300): width x height image. */
+void oracle_weights_mirror(const double *grid, int64_t width, int64_t height, double *image);
+/* GetWeight (imageweights.h:36, 98-106) for n points. */
+void oracle_weights_sample(const double *grid, int64_t width, int64_t height, double psx,
+                           double psy, size_t n, const double *u, const double *v, double *out);
+/* One chunk of raw rows: vis / model [row][chan][n_pol] complex64 (vis unused
+ * in PSF mode, model unused unless subtract_model), weights [row][chan][n_pol],
+ * selected [row][chan] (NULL: all).  Outputs vis_out [row][chan], weights_out
+ * [row][chan][n_pol], imaging_out [row][chan]; sums[0..3] += visibility weight
+ * sum, max gridded weight (max), total weight, gridded count. */
+void oracle_prepare_rows(const double *grid, int64_t width, int64_t height, double psx,
+                         double psy, int psf_mode, double psf_dl, double psf_dm,
+                         int subtract_model, int visibility_weighting, int polarization,
+                         size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,
+                         const double *freq, const float *vis, const float *weights,
+                         const float *model, const uint8_t *selected, float *vis_out,
+                         float *weights_out, float *imaging_out, double *sums);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,8 +84,27 @@ class FacetsInfo(C.Structure):
                [("job_visibilities", C.c_double), ("last_ms", C.c_double)]
 
 
+class RowWeighting(C.Structure):
+    """wgpu_row_weighting_t: the settings CalculateWeightsImplementation reads."""
+    _fields_ = [("psf_mode", C.c_int), ("psf_dl", C.c_double), ("psf_dm", C.c_double),
+                ("subtract_model", C.c_int), ("visibility_weighting", C.c_int),
+                ("polarization", C.c_int)]
+
+
+class WeightSums(C.Structure):
+    """wgpu_weight_sums_t: the sums ApplyWeights accumulates."""
+    _fields_ = [("visibility_weight_sum", C.c_double), ("max_gridded_weight", C.c_double),
+                ("total_weight", C.c_double), ("gridded_visibility_count", C.c_uint64)]
+
+
 REQUEST_INVERT = 1
 REQUEST_PREDICT = 2
+
+WEIGHT_NATURAL, WEIGHT_UNIFORM, WEIGHT_BRIGGS = range(3)
+VISW_NORMAL, VISW_SQUARED, VISW_UNIT = range(3)
+PSF_NONE, PSF_SINGLE, PSF_DIRECTION_DEPENDENT = range(3)
+(TAPER_MIN_UV, TAPER_MAX_UV, TAPER_TUKEY, TAPER_TUKEY_INNER, TAPER_EDGE, TAPER_EDGE_TUKEY,
+ TAPER_GAUSSIAN, TAPER_RANK_FILTER) = range(8)
 
 _lib = None
 
@@ -150,6 +169,19 @@ _PROTOS = {
     "wgpu_facets_job_plan": (I, [P, SZ, C.POINTER(Plan)]),
     "wgpu_facets_stream": (P, [P]),
     "wgpu_facets_destroy": (None, [P]),
+    "wgpu_imageweights_create": (I, [I, D, SZ, SZ, D, D, I, D, C.POINTER(P)]),
+    "wgpu_imageweights_destroy": (None, [P]),
+    "wgpu_imageweights_grid": (I, [P, SZ, SZ, SZ, P, P, P]),
+    "wgpu_imageweights_finish": (I, [P]),
+    "wgpu_imageweights_taper": (I, [P, I, D, D]),
+    "wgpu_imageweights_set_all": (I, [P, D]),
+    "wgpu_imageweights_get": (I, [P, I, P]),
+    "wgpu_imageweights_info": (I, [P, C.POINTER(SZ), C.POINTER(SZ), C.POINTER(D)]),
+    "wgpu_imageweights_sample": (I, [P, SZ, P, P, P]),
+    "wgpu_prepare_rows": (I, [P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P, P, P, P, P, P, P,
+                              P, C.POINTER(WeightSums)]),
+    "wgpu_gridder_add_inversion_rows": (I, [P, P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P,
+                                            P, P, P, P, C.POINTER(WeightSums)]),
 }
 
 

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwgpu.so")
 
 SOURCES = ["api.cu", "bucket.cu", "grid.cu", "fft.cu", "correct.cu", "util.cu", "server.cu",
-           "facets.cu", "plan.cpp"]
+           "facets.cu", "weights.cu", "plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
@@ -42,7 +42,7 @@ def _digest(paths):
 def _headers():
     out = [os.path.join(ROOT, "include", "wgpu.h")]
     for f in sorted(os.listdir(CSRC)):
-        if f.endswith(".h"):
+        if f.endswith((".h", ".cuh")):
             out.append(os.path.join(CSRC, f))
     return out
 

@@ -882,6 +882,51 @@ int wgpu_gridder_add_inversion_data(wgpu_gridder_t *g, size_t n_rows,
   });
 }
 
+int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *g, const wgpu_imageweights_t *iw,
+                                    const wgpu_row_weighting_t *rw, size_t n_pol,
+                                    size_t n_rows, size_t n_chan, const double *uvw,
+                                    const double *freq, const float *vis,
+                                    const float *weights, const float *model,
+                                    const uint8_t *selected, wgpu_weight_sums_t *sums) {
+  if (!g || !iw || !rw) return fail(WGPU_ERR_INVALID, "null argument");
+  if (rw->psf_mode < WGPU_PSF_NONE || rw->psf_mode > WGPU_PSF_DIRECTION_DEPENDENT ||
+      rw->visibility_weighting < WGPU_VISW_NORMAL || rw->visibility_weighting > WGPU_VISW_UNIT ||
+      rw->polarization < 0 || rw->polarization > 7)
+    return fail(WGPU_ERR_INVALID, "invalid row weighting");
+  if (n_pol != 1 && n_pol != 2 && n_pol != 4)
+    return fail(WGPU_ERR_INVALID, "n_pol must be 1, 2 or 4");
+  if (n_rows && n_chan &&
+      (!uvw || !freq || !weights || (rw->psf_mode == WGPU_PSF_NONE && !vis) ||
+       (rw->subtract_model && !model)))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kInversion)
+      throw Error(WGPU_ERR_STATE, "AddInversionData before InitializeInversion");
+    if (n_rows == 0 || n_chan == 0) return;
+    const size_t n = n_rows * n_chan, nc = n * n_pol;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const float *dw = upload(g, kSlotRowWeights, weights, nc);
+    const float2 *dv =
+        rw->psf_mode == WGPU_PSF_NONE ? (const float2 *)upload(g, kSlotGainVis, vis, 2 * nc)
+                                      : nullptr;
+    const float2 *dm =
+        rw->subtract_model ? (const float2 *)upload(g, kSlotRowModel, model, 2 * nc) : nullptr;
+    const uint8_t *ds = selected ? upload(g, kSlotRowSel, selected, n) : nullptr;
+    float2 *dc = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n);
+    auto *dsum = (WeightSumsDev *)g->arena.get(kSlotRowSums, sizeof(WeightSumsDev));
+    WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(WeightSumsDev), g->stream));
+    launch_prepare_rows(imageweights_view(iw), row_weighting(*rw), (int)n_pol, (int64_t)n_rows,
+                        (int64_t)n_chan, du, df, dv, dw, dm, ds, dc, nullptr, nullptr, dsum,
+                        g->stream);
+    WeightSumsDev hs;
+    WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, g->stream));
+    invert_device(g, n_rows, n_chan, du, df, (const float *)dc);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    add_weight_sums(hs, sums);
+  });
+}
+
 int wgpu_gridder_add_inversion_data_corrected(
     wgpu_gridder_t *g, int mode, size_t n_pol, size_t n_rows, const double *uvw,
     const double *freq, size_t n_chan, const uint64_t *antenna_pairs,

@@ -1,5 +1,6 @@
 // K6 grid correction + image accumulation, the per-pixel n-1 table, the
 // prediction pre-correction and output permutation, and K7 gains + collapse.
+#include "polarization.cuh"
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -72,13 +73,6 @@ __global__ void unpermute_predict_kernel(const VisRecord *rec, const uint32_t *p
 }
 
 // ---- K7: conjugated gains (visibilitymodifier.h:378-401) + collapse -------
-__device__ __forceinline__ float2 cm(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 cj(float2 a) { return make_float2(a.x, -a.y); }
-__device__ __forceinline__ float2 ca(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 cs(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-
 // r = a^H b (row-major 2x2)
 __device__ __forceinline__ void herm_mul(const float2 *a, const float2 *b, float2 *r) {
   const float2 h[4] = {cj(a[0]), cj(a[2]), cj(a[1]), cj(a[3])};
@@ -92,22 +86,6 @@ __device__ __forceinline__ void mat_mul(const float2 *a, const float2 *b, float2
   r[1] = ca(cm(a[0], b[1]), cm(a[1], b[3]));
   r[2] = ca(cm(a[2], b[0]), cm(a[3], b[2]));
   r[3] = ca(cm(a[2], b[1]), cm(a[3], b[3]));
-}
-
-__device__ __forceinline__ float2 collapse4(const float2 *v, int pol) {
-  switch (pol) {
-    case 0: return cs(ca(v[0], v[3]), 0.5f);
-    case 1: return make_float2(0.5f * (v[0].x - v[3].x), 0.5f * (v[0].y - v[3].y));
-    case 2: return cs(ca(v[1], v[2]), 0.5f);
-    case 3: {
-      const float2 d = make_float2(v[2].x - v[1].x, v[2].y - v[1].y);
-      return make_float2(-0.5f * d.y, 0.5f * d.x);
-    }
-    case 4: return v[0];
-    case 5: return v[1];
-    case 6: return v[2];
-    default: return v[3];
-  }
 }
 
 __global__ void apply_gains_kernel(int mode, int n_pol, int64_t n_rows,
@@ -182,25 +160,6 @@ __device__ __forceinline__ void mul_herm(const float2 *a, const float2 *b, float
   r[1] = ca(cm(a[0], cj(b[2])), cm(a[1], cj(b[3])));
   r[2] = ca(cm(a[2], cj(b[0])), cm(a[3], cj(b[1])));
   r[3] = ca(cm(a[2], cj(b[2])), cm(a[3], cj(b[3])));
-}
-
-// Stokes parameter `pol` (or linear correlation 4-7) of value s as linear
-// correlations (XX, XY, YX, YY): XX = I + Q, YY = I - Q, XY = U + iV,
-// YX = U - iV, the inverse of collapse4 (4-polarisation ExpandData,
-// msgridderdata.h:63-68).
-__device__ __forceinline__ void expand4(float2 s, int pol, float2 *v) {
-  const float2 z = make_float2(0.f, 0.f);
-  v[0] = v[1] = v[2] = v[3] = z;
-  switch (pol) {
-    case 0: v[0] = s; v[3] = s; break;
-    case 1: v[0] = s; v[3] = make_float2(-s.x, -s.y); break;
-    case 2: v[1] = s; v[2] = s; break;
-    case 3: v[1] = make_float2(-s.y, s.x); v[2] = make_float2(s.y, -s.x); break;
-    case 4: v[0] = s; break;
-    case 5: v[1] = s; break;
-    case 6: v[2] = s; break;
-    default: v[3] = s; break;
-  }
 }
 
 // Predicted [row][chan] values -> [row][chan][n_pol] instrumental

@@ -300,6 +300,40 @@ void launch_forward_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                           const uint64_t *time_offsets, const float2 *sol, int nparms,
                           int64_t n_times, int64_t n_ant, int polarization, float2 *out,
                           int *err_flag, cudaStream_t s);
+// ---- imaging weights and raw-row preparation (weights.cu) ----------------
+// A finished imaging-weight grid as the kernels read it: width x height/2
+// doubles, cell (x, y) at grid[x + y * width].
+struct WeightGridView {
+  const double *grid;
+  int64_t width, height;
+  double psx, psy;
+};
+WeightGridView imageweights_view(const wgpu_imageweights_t *iw);
+
+// Per-call settings of the row preparation, with the PSF shift's n term
+// (sqrt(1 - dl^2 - dm^2) - 1) computed on the host.
+struct RowWeighting {
+  int psf_mode, subtract_model, visibility_weighting, polarization;
+  double dl, dm, dn;
+};
+RowWeighting row_weighting(const wgpu_row_weighting_t &rw);
+
+// Device-side accumulators of the weight sums (zeroed by the caller).
+struct WeightSumsDev {
+  double visibility_weight_sum;
+  double total_weight;
+  unsigned long long max_bits;  // bits of the largest positive weight (double)
+  unsigned long long count;
+};
+void add_weight_sums(const WeightSumsDev &d, wgpu_weight_sums_t *sums);
+
+// CalculateWeights + ApplyWeights + CollapseData for n_rows x n_chan samples.
+void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_pol,
+                         int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
+                         const float2 *vis, const float *weights, const float2 *model,
+                         const uint8_t *selected, float2 *vis_out, float *weights_out,
+                         float *imaging_out, WeightSumsDev *sums, cudaStream_t s);
+
 void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                         const float2 *vis_in, const uint64_t *ant_pairs,
                         const uint64_t *time_offsets, const float2 *sol,
@@ -359,6 +393,10 @@ enum ArenaSlot {
   kSlotRowOcc,
   kSlotUvwF32,
   kSlotImgIO,
+  kSlotRowWeights,  // raw-row preparation: visibility weights,
+  kSlotRowModel,    // model visibilities,
+  kSlotRowSel,      // selection bytes,
+  kSlotRowSums,     // and the device-side weight sums
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.

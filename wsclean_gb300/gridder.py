@@ -126,6 +126,16 @@ class WGriddingGridder_Simple:
             int(polarization), ptr(out)))
         return out
 
+    def AddInversionRows(self, image_weights, uvw, frequencies, weights, vis=None, model=None,
+                         selected=None, sums=None, **settings):
+        """Raw rows -> weighted, collapsed visibilities -> AddInversionData,
+        all on the device (wgpu_gridder_add_inversion_rows); see
+        wsclean_gb300.weights.prepare_rows for the arguments.  Returns the
+        accumulated weight sums."""
+        from . import weights as _weights
+        return _weights.add_inversion_rows(self, image_weights, uvw, frequencies, weights, vis,
+                                           model, selected, sums, **settings)
+
     def FinalizeImage(self, multiplication_factor):
         check(lib().wgpu_gridder_finalize_image(self._h, float(multiplication_factor)))
 
