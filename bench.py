@@ -44,6 +44,10 @@ WORKLOAD_TEXT = {
                "16 channels 120-180 MHz, 20 sources, eps 1e-4"),
     "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
                   "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
+    "rowweights": ("raw-row weighting: the wide-field array and band, 32640 baselines x 75 x 8 s, "
+                   "64 channels 0.9-1.7 GHz, 4 correlations (XX, XY, YX, YY) with visibility "
+                   "weights, Briggs 0 imaging weights on the 8192x8192 3arcsec grid; "
+                   "CalculateWeights + ApplyWeights + collapse to Stokes I per sample"),
 }
 METRIC = "Gvis/s grid+degrid at rel.err <=1e-5 vs FP64 DFT"
 
@@ -718,6 +722,147 @@ def run_facets(args):
     }
 
 
+def run_rowweights(args):
+    """Raw-row weighting on the device: the imaging-weight grid (Grid +
+    FinishGridding, once) and then, per step, CalculateWeights + ApplyWeights
+    + CollapseData over every sample (wgpu_prepare_rows_device, inputs resident
+    in HBM); e2e through wgpu_prepare_rows with pinned host buffers; the
+    oracle's serial restatement timed on a row sample as the CPU baseline."""
+    import ctypes as C
+    import torch
+    import oracle
+    from wsclean_gb300 import _lib, synthetic
+    from wsclean_gb300.weights import BRIGGS, ImageWeights, prepare_rows_device, row_weighting
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    d = synthetic.make_workload("wide8192", seed=5, with_model=False, n_t=75)
+    uvw, freq = d["uvw"], d["freq"]
+    n_rows, n_chan, n_pol = uvw.shape[0], freq.size, 4
+    n = n_rows * n_chan
+    t_uvw = torch.as_tensor(uvw, device=dev)
+    t_freq = torch.as_tensor(freq, device=dev)
+    t_w = torch.as_tensor(d["weights"], device=dev)[:, :, None].expand(-1, -1, n_pol).contiguous()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    t_vis = torch.randn((n_rows, n_chan, n_pol), generator=gen, dtype=torch.complex64,
+                        device=dev)
+    t_out = torch.empty((n_rows, n_chan), dtype=torch.complex64, device=dev)
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    W, dl = d["width"], d["dl"]
+    iw = ImageWeights(BRIGGS, W, W, dl, dl, False, 1.0, 0.0)
+    stream = torch.cuda.ExternalStream(iw.stream(), device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iw.grid_device(n_rows, n_chan, n_pol, t_uvw.data_ptr(), t_freq.data_ptr(), t_w.data_ptr())
+    iw.FinishGridding()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    grid_ms = e0.elapsed_time(e1)
+    settings = dict(polarization=_lib.POL_I)
+
+    def step():
+        return prepare_rows_device(iw, n_pol, n_rows, n_chan, t_uvw.data_ptr(), t_freq.data_ptr(),
+                                   t_w.data_ptr(), t_out.data_ptr(), d_vis=t_vis.data_ptr(),
+                                   **settings)
+
+    for _ in range(args.warmup):
+        sums = step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib_launches()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = _lib_launches() - l0
+    ms = start.elapsed_time(end) / args.steps
+    value = n / (ms * 1e-3) / 1e9
+
+    # e2e: the host entry point with pinned host buffers (inputs up, prepared
+    # visibilities down, every step)
+    h_uvw = pinned_copy(t_uvw)
+    h_w = pinned_copy(t_w)
+    h_vis = pinned_copy(t_vis)
+    h_out = torch.empty((n_rows, n_chan), dtype=torch.complex64, pin_memory=True)
+    rw = row_weighting(**settings)
+    hs = _lib.WeightSums()
+
+    def e2e_step():
+        _lib.check(_lib.lib().wgpu_prepare_rows(
+            iw.handle, C.byref(rw), n_pol, n_rows, n_chan, h_uvw.data_ptr(), freq.ctypes.data,
+            h_vis.data_ptr(), h_w.data_ptr(), None, None, h_out.data_ptr(), None, None,
+            C.byref(hs)))
+
+    for _ in range(2):
+        e2e_step()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - w0) * 1e3 / args.steps
+    same = bool(torch.equal(h_out.to(dev), t_out))
+
+    # CPU baseline and bit-exactness on a row sample: the oracle's serial
+    # restatement with the device's finished grid
+    ref = oracle.ImageWeights(BRIGGS, W, W, dl, dl, False, 1.0, 0.0)
+    ref.grid[:] = iw.half_grid()
+    n_s = min(n_rows, max(1, args.cpu_sample_rows))
+    sw = t_w[:n_s].cpu().numpy()
+    sv = t_vis[:n_s].cpu().numpy()
+    c0 = time.perf_counter()
+    ref_out = ref.prepare_rows(uvw[:n_s], freq, sw, sv, None, None, 0, 0.0, 0.0, 0,
+                               _lib.POL_I)[0]
+    cpu_s = time.perf_counter() - c0
+    bit_exact = bool(np.array_equal(ref_out, t_out[:n_s].cpu().numpy()))
+    cpu_value = n_s * n_chan / cpu_s / 1e9
+
+    # roofline of prepare_rows_kernel<4>: per sample 4 weights (16 B), 4
+    # correlations (32 B), the imaging-weight cell (8 B) and the output (8 B),
+    # plus 24 B of uvw per row
+    alg_bytes = n * (16 + 32 + 8 + 8) + n_rows * 24 + n_chan * 8
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    h2d = h_uvw.numel() * 8 + freq.nbytes + h_w.numel() * 4 + h_vis.numel() * 8
+    d2h = h_out.numel() * 8
+    grid_bytes = n_rows * 24 + n * n_pol * 4 + n * n_pol * 16
+    return {
+        "metric": "Gsamples/s raw-row weighting (CalculateWeights + ApplyWeights + collapse)",
+        "value": value, "unit": "Gsamples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT["rowweights"], "n_rows": n_rows, "n_chan": n_chan,
+                   "n_samples": n, "correlations": n_pol,
+                   "l2": (f"inputs larger than L2 ({(t_w.numel() * 4 + t_vis.numel() * 8) / 1e9:.1f}"
+                          " GB of weights and visibilities per step)"),
+                   "weight_grid": {"ms": grid_ms, "grid": f"{iw.Width()}x{iw.Height() // 2} doubles",
+                                   "GB/s_algorithmic": grid_bytes / (grid_ms * 1e-3) / 1e9,
+                                   "note": "Grid over every sample (atomic adds) + Briggs "
+                                           "FinishGridding, once per weighting"},
+                   "bit_exact_vs_oracle": bit_exact, "e2e_matches_device": same,
+                   "weight_sums": sums, "datagen_s": round(gen_s, 1)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "prepare_rows_kernel<4>", "peak_source": peak_src,
+                     "bytes_per_sample": 64},
+        "cpu_baseline": {"value": cpu_value, "unit": "Gsamples/s", "cores": 1, "kind": "port",
+                         "sample": f"first {n_s} rows x {n_chan} channels x 4 correlations, "
+                                   "oracle serial restatement"},
+        "clocks": clk,
+        "e2e": {"value": n / (e2e_ms * 1e-3) / 1e9, "unit": "Gsamples/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+    }
+
+
 def _lib_launches():
     from wsclean_gb300 import _lib
     return _lib.lib().wgpu_kernel_launch_count()
@@ -843,6 +988,10 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.impl == "reference" and args.workload == "rowweights":
+        print(json.dumps({"impl": "reference", "unavailable": "the raw-row weighting has no "
+                          "reference arm; its CPU baseline is the cpu_baseline key"}), flush=True)
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
@@ -852,6 +1001,9 @@ def main():
         return
     if args.workload == "fullpol4096":
         print(json.dumps(run_fullpol(args)), flush=True)
+        return
+    if args.workload == "rowweights":
+        print(json.dumps(run_rowweights(args)), flush=True)
         return
     if args.serve_only:
         import torch

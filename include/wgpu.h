@@ -525,6 +525,15 @@ int wgpu_imageweights_grid(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan
                            size_t n_pol, const double *uvw, const double *freq,
                            const float *weights);
 
+/* Same, with device-resident uvw, freq and weights (read on the image
+ * weights' stream, wgpu_imageweights_stream). */
+int wgpu_imageweights_grid_device(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan,
+                                  size_t n_pol, const double *d_uvw, const double *d_freq,
+                                  const float *d_weights);
+
+/* The image weights' CUDA stream (cudaStream_t). */
+void *wgpu_imageweights_stream(wgpu_imageweights_t *iw);
+
 /* FinishGridding (imageweights.cpp:114-147); a second call fails with
  * WGPU_ERR_STATE. */
 int wgpu_imageweights_finish(wgpu_imageweights_t *iw);
@@ -583,6 +592,14 @@ int wgpu_prepare_rows(const wgpu_imageweights_t *iw, const wgpu_row_weighting_t 
                       const float *model, const uint8_t *selected, float *vis_out,
                       float *weights_out, float *imaging_weights_out,
                       wgpu_weight_sums_t *sums);
+
+/* Same on device buffers (the image weights' stream); sums are read back. */
+int wgpu_prepare_rows_device(const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw,
+                             size_t n_pol, size_t n_rows, size_t n_chan, const double *d_uvw,
+                             const double *d_freq, const float *d_vis, const float *d_weights,
+                             const float *d_model, const uint8_t *d_selected, float *d_vis_out,
+                             float *d_weights_out, float *d_imaging_weights_out,
+                             wgpu_weight_sums_t *sums);
 
 /* GetCollapsedVisibilities followed by AddInversionData for one chunk of raw
  * rows (WGriddingMSGridder::GridMeasurementSet, wgridder/wgriddingmsgridder.cpp:

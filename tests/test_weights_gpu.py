@@ -13,7 +13,7 @@ from wsclean_gb300 import _lib, synthetic
 from wsclean_gb300.gridder import WGriddingGridder_Simple
 from wsclean_gb300.weights import BRIGGS, NATURAL, UNIFORM, ImageWeights, prepare_rows
 
-from test_weights_oracle import PREP_CASES, TAPERS, rows
+from test_weights_oracle import PREP_CASES, TAPERS
 
 pytestmark = pytest.mark.gpu
 
@@ -204,7 +204,8 @@ def test_add_inversion_rows_matches_prepared_inversion(oracle_lib, n_pol, pol):
     g2 = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps,
                                  num_t=np.float64)
     g2.InitializeInversion()
-    g2.AddInversionData(uvw.shape[0], freq.size, uvw, freq, prepared)
+    for sl in (slice(0, half), slice(half, None)):  # the same chunks, so the same plans
+        g2.AddInversionData(uvw[sl].shape[0], freq.size, uvw[sl], freq, prepared[sl])
     g2.FinalizeImage(1.0)
     img_prep = g2.RealImage().reshape(W, W)
 
@@ -218,3 +219,32 @@ def test_add_inversion_rows_matches_prepared_inversion(oracle_lib, n_pol, pol):
     assert acc.max_gridded_weight == sums[1]
     np.testing.assert_allclose(acc.total_weight, sums[2], rtol=1e-12)
     np.testing.assert_allclose(acc.visibility_weight_sum, sums[0], rtol=1e-12)
+
+
+def test_device_variants_match_host_variants(oracle_lib):
+    torch = pytest.importorskip("torch")
+    from wsclean_gb300.weights import prepare_rows_device
+    dev = torch.device("cuda", 0)
+    uvw, freq, weights, vis = big_rows(41, n_rows=1200, n_chan=8, n_pol=4, dyadic=False)
+    a = ImageWeights(UNIFORM, 300, 220, PSX, PSX)
+    b = ImageWeights(UNIFORM, 300, 220, PSX, PSX)
+    a.Grid(uvw, freq, weights)
+    t_uvw, t_freq = torch.as_tensor(uvw, device=dev), torch.as_tensor(freq, device=dev)
+    t_w = torch.as_tensor(weights, device=dev)
+    torch.cuda.synchronize()
+    b.grid_device(uvw.shape[0], freq.size, 4, t_uvw.data_ptr(), t_freq.data_ptr(),
+                  t_w.data_ptr())
+    np.testing.assert_allclose(b.half_grid(), a.half_grid(), rtol=1e-12, atol=0)
+    a.FinishGridding()
+    st = dict(visibility_weighting=_lib.VISW_SQUARED, polarization=_lib.POL_Q)
+    out, w, iw, s = prepare_rows(a, uvw, freq, weights, vis, **st)
+    t_vis = torch.as_tensor(vis.view(np.float32), device=dev)
+    t_out = torch.empty(out.size * 2, dtype=torch.float32, device=dev)
+    t_wo = torch.empty(w.size, dtype=torch.float32, device=dev)
+    sd = prepare_rows_device(a, 4, uvw.shape[0], freq.size, t_uvw.data_ptr(), t_freq.data_ptr(),
+                             t_w.data_ptr(), t_out.data_ptr(), d_vis=t_vis.data_ptr(),
+                             d_weights_out=t_wo.data_ptr(), **st)
+    np.testing.assert_array_equal(t_out.cpu().numpy().view(np.complex64).reshape(out.shape), out)
+    np.testing.assert_array_equal(t_wo.cpu().numpy().reshape(w.shape), w)
+    assert sd["gridded_visibility_count"] == s["gridded_visibility_count"] > 0
+    np.testing.assert_allclose(sd["total_weight"], s["total_weight"], rtol=1e-12)

@@ -172,6 +172,8 @@ _PROTOS = {
     "wgpu_imageweights_create": (I, [I, D, SZ, SZ, D, D, I, D, C.POINTER(P)]),
     "wgpu_imageweights_destroy": (None, [P]),
     "wgpu_imageweights_grid": (I, [P, SZ, SZ, SZ, P, P, P]),
+    "wgpu_imageweights_grid_device": (I, [P, SZ, SZ, SZ, P, P, P]),
+    "wgpu_imageweights_stream": (P, [P]),
     "wgpu_imageweights_finish": (I, [P]),
     "wgpu_imageweights_taper": (I, [P, I, D, D]),
     "wgpu_imageweights_set_all": (I, [P, D]),
@@ -180,6 +182,8 @@ _PROTOS = {
     "wgpu_imageweights_sample": (I, [P, SZ, P, P, P]),
     "wgpu_prepare_rows": (I, [P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P, P, P, P, P, P, P,
                               P, C.POINTER(WeightSums)]),
+    "wgpu_prepare_rows_device": (I, [P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P, P, P, P, P,
+                                     P, P, P, C.POINTER(WeightSums)]),
     "wgpu_gridder_add_inversion_rows": (I, [P, P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P,
                                             P, P, P, P, C.POINTER(WeightSums)]),
 }

@@ -508,6 +508,48 @@ bool valid_weighting(const wgpu_row_weighting_t *rw) {
          rw->polarization <= 7;
 }
 
+void grid_device(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan, size_t n_pol,
+                 const double *du, const double *df, const float *dw) {
+  const int64_t n = (int64_t)(n_rows * n_chan);
+  wgpu::weight_grid_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
+      iw->grid, iw->sums, iw->width, iw->height, iw->psx, iw->psy, iw->as_taper ? 1 : 0,
+      (int64_t)n_rows, (int64_t)n_chan, (int)n_pol, du, df, dw);
+  wgpu::check_launch("weight_grid_kernel");
+  WGPU_CUDA(cudaStreamSynchronize(iw->stream));
+}
+
+// The row preparation on device buffers; sums (device, zeroed here) are read
+// back and added to the caller's.
+void prepare_device(wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw, size_t n_pol,
+                    size_t n_rows, size_t n_chan, const double *du, const double *df,
+                    const float2 *dv, const float *dw, const float2 *dm, const uint8_t *ds,
+                    float2 *dvo, float *dwo, float *dio, wgpu_weight_sums_t *sums) {
+  auto *dsum = (wgpu::WeightSumsDev *)scratch(iw, 7, sizeof(wgpu::WeightSumsDev));
+  WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(wgpu::WeightSumsDev), iw->stream));
+  wgpu::launch_prepare_rows(wgpu::imageweights_view(iw), wgpu::row_weighting(*rw), (int)n_pol,
+                            (int64_t)n_rows, (int64_t)n_chan, du, df, dv, dw, dm, ds, dvo, dwo,
+                            dio, dsum, iw->stream);
+  wgpu::WeightSumsDev hs;
+  WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, iw->stream));
+  WGPU_CUDA(cudaStreamSynchronize(iw->stream));
+  wgpu::add_weight_sums(hs, sums);
+}
+
+int check_prepare_args(const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw,
+                       size_t n_pol, size_t n_rows, size_t n_chan, const void *uvw,
+                       const void *freq, const void *vis, const void *weights,
+                       const void *model, const void *vis_out) {
+  if (!iw) return wgpu::report_failure(WGPU_ERR_INVALID, "null image weights");
+  if (!valid_weighting(rw)) return wgpu::report_failure(WGPU_ERR_INVALID, "invalid row weighting");
+  if (n_pol != 1 && n_pol != 2 && n_pol != 4)
+    return wgpu::report_failure(WGPU_ERR_INVALID, "n_pol must be 1, 2 or 4");
+  if (n_rows && n_chan &&
+      (!uvw || !freq || !weights || !vis_out || (rw->psf_mode == WGPU_PSF_NONE && !vis) ||
+       (rw->subtract_model && !model)))
+    return wgpu::report_failure(WGPU_ERR_INVALID, "null data pointer");
+  return WGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -590,14 +632,27 @@ int wgpu_imageweights_grid(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan
     const double *du = upload(iw, 0, uvw, 3 * n_rows);
     const double *df = upload(iw, 1, freq, n_chan);
     const float *dw = upload(iw, 2, weights, n_rows * n_chan * n_pol);
-    const int64_t n = (int64_t)(n_rows * n_chan);
-    wgpu::weight_grid_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
-        iw->grid, iw->sums, iw->width, iw->height, iw->psx, iw->psy, iw->as_taper ? 1 : 0,
-        (int64_t)n_rows, (int64_t)n_chan, (int)n_pol, du, df, dw);
-    wgpu::check_launch("weight_grid_kernel");
-    WGPU_CUDA(cudaStreamSynchronize(iw->stream));
+    grid_device(iw, n_rows, n_chan, n_pol, du, df, dw);
   });
 }
+
+int wgpu_imageweights_grid_device(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan,
+                                  size_t n_pol, const double *d_uvw, const double *d_freq,
+                                  const float *d_weights) {
+  if (!iw) return wgpu::report_failure(WGPU_ERR_INVALID, "null image weights");
+  if (n_pol < 1 || n_pol > 4)
+    return wgpu::report_failure(WGPU_ERR_INVALID, "n_pol must be 1 to 4");
+  if (n_rows && n_chan && (!d_uvw || !d_freq || !d_weights))
+    return wgpu::report_failure(WGPU_ERR_INVALID, "null data pointer");
+  return weights_guarded([&] {
+    if (iw->finished) throw Error(WGPU_ERR_STATE, "Grid() after FinishGridding()");
+    if (n_rows == 0 || n_chan == 0) return;
+    DeviceScope scope(iw->device);
+    grid_device(iw, n_rows, n_chan, n_pol, d_uvw, d_freq, d_weights);
+  });
+}
+
+void *wgpu_imageweights_stream(wgpu_imageweights_t *iw) { return iw ? iw->stream : nullptr; }
 
 int wgpu_imageweights_finish(wgpu_imageweights_t *iw) {
   if (!iw) return wgpu::report_failure(WGPU_ERR_INVALID, "null image weights");
@@ -740,14 +795,9 @@ int wgpu_prepare_rows(const wgpu_imageweights_t *iw_c, const wgpu_row_weighting_
                       const float *model, const uint8_t *selected, float *vis_out,
                       float *weights_out, float *imaging_weights_out,
                       wgpu_weight_sums_t *sums) {
-  if (!iw_c) return wgpu::report_failure(WGPU_ERR_INVALID, "null image weights");
-  if (!valid_weighting(rw)) return wgpu::report_failure(WGPU_ERR_INVALID, "invalid row weighting");
-  if (n_pol != 1 && n_pol != 2 && n_pol != 4)
-    return wgpu::report_failure(WGPU_ERR_INVALID, "n_pol must be 1, 2 or 4");
-  if (n_rows && n_chan &&
-      (!uvw || !freq || !weights || !vis_out || (rw->psf_mode == WGPU_PSF_NONE && !vis) ||
-       (rw->subtract_model && !model)))
-    return wgpu::report_failure(WGPU_ERR_INVALID, "null data pointer");
+  const int st = check_prepare_args(iw_c, rw, n_pol, n_rows, n_chan, uvw, freq, vis, weights,
+                                    model, vis_out);
+  if (st != WGPU_OK) return st;
   auto *iw = const_cast<wgpu_imageweights_t *>(iw_c);
   return weights_guarded([&] {
     if (n_rows == 0 || n_chan == 0) return;
@@ -760,27 +810,40 @@ int wgpu_prepare_rows(const wgpu_imageweights_t *iw_c, const wgpu_row_weighting_
         rw->psf_mode == WGPU_PSF_NONE ? (const float2 *)upload(iw, 3, vis, 2 * nc) : nullptr;
     const float2 *dm = rw->subtract_model ? (const float2 *)upload(iw, 4, model, 2 * nc) : nullptr;
     const uint8_t *ds = selected ? upload(iw, 5, selected, n) : nullptr;
-    // outputs share one buffer: vis_out, weights_out, imaging weights, sums
-    char *o = (char *)scratch(iw, 6, 8 * n + 4 * nc + 4 * n + sizeof(wgpu::WeightSumsDev) + 64);
+    // the outputs share one buffer: vis_out, weights_out, imaging weights
+    char *o = (char *)scratch(iw, 6, 8 * n + 4 * nc + 4 * n);
     float2 *dvo = (float2 *)o;
     float *dwo = (float *)(o + 8 * n);
     float *dio = (float *)(o + 8 * n + 4 * nc);
-    auto *dsum = (wgpu::WeightSumsDev *)(o + ((8 * n + 4 * nc + 4 * n + 15) / 16) * 16);
-    WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(wgpu::WeightSumsDev), iw->stream));
-    wgpu::launch_prepare_rows(wgpu::imageweights_view(iw), wgpu::row_weighting(*rw), (int)n_pol,
-                              (int64_t)n_rows, (int64_t)n_chan, du, df, dv, dw, dm, ds, dvo,
-                              weights_out ? dwo : nullptr, imaging_weights_out ? dio : nullptr,
-                              dsum, iw->stream);
+    prepare_device(iw, rw, n_pol, n_rows, n_chan, du, df, dv, dw, dm, ds, dvo,
+                   weights_out ? dwo : nullptr, imaging_weights_out ? dio : nullptr, sums);
     WGPU_CUDA(cudaMemcpyAsync(vis_out, dvo, 8 * n, cudaMemcpyDeviceToHost, iw->stream));
     if (weights_out)
       WGPU_CUDA(cudaMemcpyAsync(weights_out, dwo, 4 * nc, cudaMemcpyDeviceToHost, iw->stream));
     if (imaging_weights_out)
       WGPU_CUDA(
           cudaMemcpyAsync(imaging_weights_out, dio, 4 * n, cudaMemcpyDeviceToHost, iw->stream));
-    wgpu::WeightSumsDev hs;
-    WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, iw->stream));
     WGPU_CUDA(cudaStreamSynchronize(iw->stream));
-    wgpu::add_weight_sums(hs, sums);
+  });
+}
+
+int wgpu_prepare_rows_device(const wgpu_imageweights_t *iw_c, const wgpu_row_weighting_t *rw,
+                             size_t n_pol, size_t n_rows, size_t n_chan, const double *d_uvw,
+                             const double *d_freq, const float *d_vis, const float *d_weights,
+                             const float *d_model, const uint8_t *d_selected, float *d_vis_out,
+                             float *d_weights_out, float *d_imaging_weights_out,
+                             wgpu_weight_sums_t *sums) {
+  const int st = check_prepare_args(iw_c, rw, n_pol, n_rows, n_chan, d_uvw, d_freq, d_vis,
+                                    d_weights, d_model, d_vis_out);
+  if (st != WGPU_OK) return st;
+  auto *iw = const_cast<wgpu_imageweights_t *>(iw_c);
+  return weights_guarded([&] {
+    if (n_rows == 0 || n_chan == 0) return;
+    DeviceScope scope(iw->device);
+    prepare_device(iw, rw, n_pol, n_rows, n_chan, d_uvw, d_freq,
+                   rw->psf_mode == WGPU_PSF_NONE ? (const float2 *)d_vis : nullptr, d_weights,
+                   rw->subtract_model ? (const float2 *)d_model : nullptr, d_selected,
+                   (float2 *)d_vis_out, d_weights_out, d_imaging_weights_out, sums);
   });
 }
 

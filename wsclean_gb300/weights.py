@@ -32,7 +32,7 @@ class ImageWeights:
                                              float(pixel_scale_y), int(bool(weights_as_taper)),
                                              float(super_weight), C.byref(h)))
         self._h = h
-        w, hh, t = C.c_size_t(), C.c_size_t(), C.c_double()
+        w, hh = C.c_size_t(), C.c_size_t()
         check(lib().wgpu_imageweights_info(self._h, C.byref(w), C.byref(hh), None))
         self._width, self._height = w.value, hh.value
 
@@ -68,6 +68,16 @@ class ImageWeights:
         assert wts.size == n_rows * n_chan * n_pol
         check(lib().wgpu_imageweights_grid(self._h, n_rows, n_chan, n_pol, ptr(uvw), ptr(freq),
                                            ptr(wts)))
+
+    def grid_device(self, n_rows, n_chan, n_pol, d_uvw, d_freq, d_weights):
+        """Grid with device-resident inputs (integer device addresses, e.g.
+        torch tensor data_ptr()), on this object's stream."""
+        check(lib().wgpu_imageweights_grid_device(self._h, n_rows, n_chan, n_pol, d_uvw, d_freq,
+                                                  d_weights))
+
+    def stream(self):
+        """The CUDA stream the weight kernels run on (an integer handle)."""
+        return lib().wgpu_imageweights_stream(self._h)
 
     def FinishGridding(self):
         check(lib().wgpu_imageweights_finish(self._h))
@@ -185,3 +195,16 @@ def add_inversion_rows(gridder, image_weights, uvw, frequencies, weights, vis=No
                                                 ptr(vis_a), ptr(wts), ptr(mod_a), ptr(sel_a),
                                                 C.byref(sums)))
     return sums
+
+
+def prepare_rows_device(image_weights, n_pol, n_rows, n_chan, d_uvw, d_freq, d_weights, d_vis_out,
+                        d_vis=None, d_model=None, d_selected=None, d_weights_out=None,
+                        d_imaging_out=None, **settings):
+    """prepare_rows on device buffers (integer device addresses), on the image
+    weights' stream; returns the sums dict."""
+    rw = row_weighting(**settings)
+    sums = _lib.WeightSums()
+    check(lib().wgpu_prepare_rows_device(image_weights.handle, C.byref(rw), n_pol, n_rows, n_chan,
+                                         d_uvw, d_freq, d_vis, d_weights, d_model, d_selected,
+                                         d_vis_out, d_weights_out, d_imaging_out, C.byref(sums)))
+    return sums_dict(sums)
