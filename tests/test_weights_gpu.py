@@ -248,3 +248,36 @@ def test_device_variants_match_host_variants(oracle_lib):
     np.testing.assert_array_equal(t_wo.cpu().numpy().reshape(w.shape), w)
     assert sd["gridded_visibility_count"] == s["gridded_visibility_count"] > 0
     np.testing.assert_allclose(sd["total_weight"], s["total_weight"], rtol=1e-12)
+
+
+def test_cells_exact_on_and_near_cell_edges(oracle_lib):
+    """Samples placed on cell edges and within 1e-12 .. 1e-3 of them (wavelength
+    1 m, W psx = 2^-6, so u = 64 k metres is an edge) must take the cell the
+    host's double arithmetic gives: the FP32 decision defers them to the exact
+    pass.  Grid and prepared rows are compared bit for bit."""
+    c = 299792458.0
+    rng = np.random.default_rng(77)
+    k = rng.integers(-100, 100, (4000, 2)).astype(np.float64)
+    delta = rng.choice([0.0, 1e-12, -1e-12, 3e-9, -3e-9, 1e-6, -1e-6, 1e-3, -1e-3, 0.37],
+                       (4000, 2))
+    uvw = np.zeros((4000, 3))
+    uvw[:, :2] = 64.0 * k + 64.0 * delta
+    uvw[:, 2] = rng.normal(0, 10, 4000)
+    freq = np.array([c, c / 3.0, 1.4e9, c * 0.5])
+    weights = (rng.integers(0, 9, (4000, freq.size, 2)) / 4.0).astype(np.float32)
+    vis = (rng.standard_normal(weights.shape) + 1j * rng.standard_normal(weights.shape)).astype(
+        np.complex64)
+    args = (UNIFORM, 256, 256, 2.0 ** -14, 2.0 ** -14, False, 1.0, 0.0)
+    dev, ref = ImageWeights(*args), oracle_lib.ImageWeights(*args)
+    dev.Grid(uvw, freq, weights)
+    ref.grid_rows(uvw, freq, weights)
+    np.testing.assert_array_equal(dev.half_grid(), ref.grid)
+    assert dev.TotalSum() == ref.total
+    dev.FinishGridding()
+    ref.finish()
+    np.testing.assert_array_equal(dev.half_grid(), ref.grid)
+    got = prepare_rows(dev, uvw, freq, weights, vis, visibility_weighting=_lib.VISW_UNIT)
+    exp = ref.prepare_rows(uvw, freq, weights, vis, None, None, 0, 0.0, 0.0, 2, 0)
+    for g, e in zip(got[:3], exp[:3]):
+        np.testing.assert_array_equal(g, e)
+    assert got[3]["gridded_visibility_count"] == exp[3][3] > 0

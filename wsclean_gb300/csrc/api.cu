@@ -915,10 +915,11 @@ int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *g, const wgpu_imageweights_t
     const uint8_t *ds = selected ? upload(g, kSlotRowSel, selected, n) : nullptr;
     float2 *dc = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n);
     auto *dsum = (WeightSumsDev *)g->arena.get(kSlotRowSums, sizeof(WeightSumsDev));
+    void *work = g->arena.get(kSlotRowWork, pass_work_bytes((int64_t)n_rows, (int64_t)n_chan));
+    const WeightGridView view = imageweights_view(iw);
     WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(WeightSumsDev), g->stream));
-    launch_prepare_rows(imageweights_view(iw), row_weighting(*rw), (int)n_pol, (int64_t)n_rows,
-                        (int64_t)n_chan, du, df, dv, dw, dm, ds, dc, nullptr, nullptr, dsum,
-                        g->stream);
+    launch_prepare_rows(view, row_weighting(*rw), (int)n_pol, (int64_t)n_rows, (int64_t)n_chan,
+                        du, df, dv, dw, dm, ds, dc, nullptr, nullptr, dsum, work, g->stream);
     WeightSumsDev hs;
     WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, g->stream));
     invert_device(g, n_rows, n_chan, du, df, (const float *)dc);

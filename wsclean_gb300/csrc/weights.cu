@@ -33,9 +33,11 @@ struct wgpu_imageweights {
   int device = 0;
   cudaStream_t stream = nullptr;
   double *grid = nullptr;      // width * height / 2
+  float *gridf = nullptr;      // (float)grid, refreshed before the rows are weighted
+  bool gridf_dirty = true;
   double *sums = nullptr;      // [0] gridded weight sum, [1] sum of squares
   double *partials = nullptr;  // per-block partial sums of the reductions
-  static constexpr int kScratch = 8;
+  static constexpr int kScratch = 10;
   void *scratch[kScratch] = {};
   size_t scratch_bytes[kScratch] = {};
 };
@@ -48,6 +50,12 @@ constexpr int kThreads = 256;
 constexpr int kReduceBlocks = 1024;  // fixed, so reductions add in a fixed order
 
 unsigned blocks_for(int64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// Per-channel constants of the cell computation (chan_scale_kernel).
+struct ChanScale {
+  double lambda;
+  float su, sv;
+};
 
 // uvToXY and isWithinLimits (imageweights.h:74-96): reflect into v >= 0,
 // x = floor(u * W * psx + W / 2), y = floor(v * H * psy), inside when
@@ -102,37 +110,172 @@ __device__ double block_sum(double v) {
   return t;
 }
 
-// ImageWeights::Grid(MSProvider &, BandData) (imageweights.cpp:75-112), one
-// thread per (row, channel): the row's (u, v) is reflected into v >= 0, scaled
-// by the channel's wavelength, and each correlation's weight (1 for a
-// non-zero weight when the weights are a taper) is added to the cell.
-__global__ void weight_grid_kernel(double *grid, double *total, int64_t W, int64_t H, double psx,
-                                   double psy, int as_taper, int64_t n_rows, int64_t n_chan,
-                                   int n_pol, const double *uvw, const double *freq,
-                                   const float *weights) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double local = 0.0;
-  if (e < n_rows * n_chan) {
-    const int64_t r = e / n_chan, ch = e - r * n_chan;
-    double um = uvw[3 * r], vm = uvw[3 * r + 1];
+// Per-channel constants: the wavelength as the host forms it (c / f in
+// double) and the FP32 scales W psx / lambda and H psy / lambda of the cell
+// estimate.
+__global__ void chan_scale_kernel(const double *freq, int64_t n_chan, int64_t W, int64_t H,
+                                  double psx, double psy, ChanScale *t) {
+  const int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch >= n_chan) return;
+  const double lambda = kSpeedOfLight / freq[ch];
+  ChanScale c;
+  c.lambda = lambda;
+  c.su = (float)(((double)W * psx) / lambda);
+  c.sv = (float)(((double)H * psy) / lambda);
+  t[ch] = c;
+}
+
+// The cell of (um, vm) metres at one channel, decided in FP32.  The FP32
+// estimate x' = um * su + W/2 differs from the host's double evaluation
+// (u = um / lambda, then u * W * psx + W / 2, each rounded) by less than
+// 2^-22 (|um su| + |x'|) (three float roundings against five double ones); a
+// cell is decided when both coordinates lie farther than twice that from a
+// cell edge.  Returns the cell, -1 when decided outside the grid, -2 when
+// undecided (also for non-finite, tiny-v or out-of-float-range inputs).
+__device__ __forceinline__ int64_t fast_cell(double um, double vm, const ChanScale &c, int64_t W,
+                                             int64_t H) {
+  if (!(fabs(vm) >= 1e-280 || vm == 0.0)) return -2;  // tiny or NaN v
+  if (vm < 0.0) {
+    um = -um;
+    vm = -vm;
+  }
+  const float uf = (float)um, vf = (float)vm;
+  const float xf = fmaf(uf, c.su, (float)(W / 2));
+  const float bx = 0x1p-21f * (fabsf(uf * c.su) + fabsf(xf)) + 1e-30f;
+  const float kx = floorf(xf), fx = xf - kx;
+  if (!(fx > bx && fx < 1.0f - bx)) return -2;
+  const float yf = vf * c.sv;
+  const float by = 0x1p-20f * fabsf(yf) + 1e-30f;
+  const float ky = floorf(yf), fy = yf - ky;
+  if (!(fy > by && fy < 1.0f - by)) return -2;
+  if (!(kx >= 0.0f && kx < (float)W && ky >= 0.0f && ky < (float)(H / 2))) return -1;
+  return (int64_t)kx + (int64_t)ky * W;
+}
+
+// Float-float accumulator (Knuth's TwoSum), flushed into a double every
+// kFlush additions: sums of float weights in the FP32 pipe with a relative
+// error far below that of the reference's own serial double sum.
+struct FloatSum {
+  double acc = 0.0;
+  float hi = 0.0f, lo = 0.0f;
+  int n = 0;
+  static constexpr int kFlush = 32;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+    if (++n == kFlush) flush();
+  }
+  __device__ __forceinline__ void flush() {
+    acc += (double)hi + (double)lo;
+    hi = lo = 0.0f;
+    n = 0;
+  }
+  __device__ __forceinline__ double value() {
+    flush();
+    return acc;
+  }
+};
+
+// Undecided samples of one pass: block b appends to its own slice
+// [b * cap, (b + 1) * cap) of the list (cap = the samples a block visits),
+// counting in shared memory; counts[b] holds the slice's length afterwards.
+struct Pending {
+  uint32_t *idx;
+  uint32_t *counts;
+  uint32_t cap;
+};
+
+__device__ __forceinline__ void pending_push(const Pending &p, uint32_t *s_count, bool want,
+                                             uint32_t e) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (m == 0) return;
+  const int lane = threadIdx.x & 31;
+  uint32_t base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(s_count, (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  if (want) p.idx[(size_t)blockIdx.x * p.cap + base + __popc(m & ((1u << lane) - 1))] = e;
+}
+
+// Grid(MSProvider &, BandData) (imageweights.cpp:75-112), first pass, over a
+// fixed grid of blocks: for every (row, channel) with an FP32-decided cell the
+// correlations' weights (1 for a non-zero weight when the weights are a
+// taper) are summed and added to the cell; undecided samples go to the
+// pending list.  The row's (u, v) reflection into v >= 0 happens in metres,
+// as in the reference.
+__global__ void __launch_bounds__(kThreads) weight_grid_fast_kernel(
+    double *grid, double *total, int64_t W, int64_t H, int as_taper, uint32_t n,
+    uint32_t n_chan, int n_pol, const double *uvw, const ChanScale *cs, const float *weights,
+    Pending pend) {
+  __shared__ uint32_t s_count;
+  if (threadIdx.x == 0) s_count = 0;
+  __syncthreads();
+  FloatSum tot;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t e = base + threadIdx.x;
+    bool undecided = false;
+    if (e < n) {
+      const uint32_t r = e / n_chan, ch = e - r * n_chan;
+      const int64_t cell = fast_cell(uvw[3 * (size_t)r], uvw[3 * (size_t)r + 1], cs[ch], W, H);
+      undecided = cell == -2;
+      if (cell >= 0) {
+        FloatSum s;
+        for (int p = 0; p < n_pol; ++p) {
+          float w = weights[(size_t)e * n_pol + p];
+          if (as_taper && w != 0.0f) w = 1.0f;
+          s.add(w);
+        }
+        const double sw = s.value();
+        if (sw != 0.0) {
+          atomicAdd(grid + cell, sw);
+          tot.acc += sw;
+        }
+      }
+    }
+    pending_push(pend, &s_count, undecided, e);
+  }
+  const double t = block_sum(tot.value());
+  if (threadIdx.x == 0) {
+    pend.counts[blockIdx.x] = s_count;
+    if (t != 0.0) atomicAdd(total, t);
+  }
+}
+
+// Second pass over the pending samples: the cell as the host computes it, in
+// double (reflection in metres, u = um / lambda, v = vm / lambda).
+__global__ void __launch_bounds__(kThreads) weight_grid_exact_kernel(
+    double *grid, double *total, int64_t W, int64_t H, double psx, double psy, int as_taper,
+    uint32_t n_chan, int n_pol, const double *uvw, const ChanScale *cs, const float *weights,
+    Pending pend) {
+  const uint32_t count = pend.counts[blockIdx.x];
+  const uint32_t *list = pend.idx + (size_t)blockIdx.x * pend.cap;
+  FloatSum tot;
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const uint32_t e = list[i];
+    const uint32_t r = e / n_chan, ch = e - r * n_chan;
+    double um = uvw[3 * (size_t)r], vm = uvw[3 * (size_t)r + 1];
     if (vm < 0.0) {
       um = -um;
       vm = -vm;
     }
-    const double lambda = kSpeedOfLight / freq[ch];
+    const double lambda = cs[ch].lambda;
     const int64_t cell = uv_cell(um / lambda, vm / lambda, W, H, psx, psy);
-    if (cell >= 0) {
-      for (int p = 0; p < n_pol; ++p) {
-        float w = weights[e * n_pol + p];
-        if (as_taper && w != 0.0f) w = 1.0f;
-        if (w != 0.0f) {
-          atomicAdd(grid + cell, (double)w);
-          local += (double)w;
-        }
-      }
+    if (cell < 0) continue;
+    FloatSum s;
+    for (int p = 0; p < n_pol; ++p) {
+      float w = weights[(size_t)e * n_pol + p];
+      if (as_taper && w != 0.0f) w = 1.0f;
+      s.add(w);
+    }
+    const double sw = s.value();
+    if (sw != 0.0) {
+      atomicAdd(grid + cell, sw);
+      tot.acc += sw;
     }
   }
-  const double t = block_sum(local);
+  const double t = block_sum(tot.value());
   if (threadIdx.x == 0 && t != 0.0) atomicAdd(total, t);
 }
 
@@ -285,7 +428,7 @@ __global__ void weight_sample_kernel(const double *grid, int64_t W, int64_t H, d
 }
 
 // CalculateWeightsImplementation + ApplyWeights + CollapseData
-// (msgridderdata.h:36-52, 760-789, 826-886), one thread per (row, channel):
+// (msgridderdata.h:36-52, 760-789, 826-886) for one (row, channel) sample:
 //   1. PSF mode: every correlation is 1, rotated by the phase of a point
 //      source at (dl, dm) when that is not the phase centre (RotateVisibilities,
 //      msgridderdata.h:929-941: the phasor is computed in double, stored as
@@ -298,23 +441,60 @@ __global__ void weight_sample_kernel(const double *grid, int64_t W, int64_t H, d
 //      sums are accumulated (pol 0 for the weight sum, maximum and count);
 //   6. the correlations are collapsed to one value (sum of two, or Stokes /
 //      correlation `polarization` of four).
-template <int NPOL>
-__global__ void prepare_rows_kernel(WeightGridView g, RowWeighting rw, int64_t n_rows,
-                                    int64_t n_chan, const double *uvw, const double *freq,
-                                    const float2 *vis, const float *weights,
-                                    const float2 *model, const uint8_t *selected,
-                                    float2 *vis_out, float *weights_out, float *imaging_out,
-                                    WeightSumsDev *sums) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double vws = 0.0, total = 0.0, vmax = 0.0, count = 0.0;
-  if (e < n_rows * n_chan) {
-    const int64_t r = e / n_chan, ch = e - r * n_chan;
-    const double um = uvw[3 * r], vm = uvw[3 * r + 1], wm = uvw[3 * r + 2];
-    const double lambda = kSpeedOfLight / freq[ch];
-    const int64_t cell = uv_cell(um / lambda, vm / lambda, g.width, g.height, g.psx, g.psy);
-    const float iw = cell >= 0 ? (float)g.grid[cell] : 0.0f;
-    float2 phasor = make_float2(1.0f, 0.0f);
-    if (rw.psf_mode != WGPU_PSF_NONE && (rw.dl != 0.0 || rw.dm != 0.0)) {
+// The streamed inputs are read with evict-first loads so that L2 keeps the
+// imaging-weight table; VEC selects 8- / 16-byte accesses (aligned buffers).
+struct PrepAcc {
+  FloatSum vws, total;
+  float vmax = 0.0f;
+  uint32_t count = 0;
+};
+
+template <int NPOL, bool VEC>
+__device__ __forceinline__ void load_weights(const float *p, float *w) {
+  if constexpr (VEC && NPOL == 4) {
+    const float4 t = __ldcs(reinterpret_cast<const float4 *>(p));
+    w[0] = t.x; w[1] = t.y; w[2] = t.z; w[3] = t.w;
+  } else if constexpr (VEC && NPOL == 2) {
+    const float2 t = __ldcs(reinterpret_cast<const float2 *>(p));
+    w[0] = t.x; w[1] = t.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < NPOL; ++k) w[k] = __ldcs(p + k);
+  }
+}
+
+template <int NPOL, bool VEC>
+__device__ __forceinline__ void load_vis(const float2 *p, float2 *v) {
+  if constexpr (VEC && NPOL >= 2) {
+#pragma unroll
+    for (int k = 0; k < NPOL / 2; ++k) {
+      const float4 t = __ldcs(reinterpret_cast<const float4 *>(p) + k);
+      v[2 * k] = make_float2(t.x, t.y);
+      v[2 * k + 1] = make_float2(t.z, t.w);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NPOL; ++k) v[k] = __ldcs(p + k);
+  }
+}
+
+template <int NPOL, bool VEC>
+__device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, uint32_t r,
+                                            float iw, double lambda, const double *uvw,
+                                            const float2 *vis, const float *weights,
+                                            const float2 *model, const uint8_t *selected,
+                                            float2 *vis_out, float *weights_out,
+                                            float *imaging_out, PrepAcc &acc) {
+  float w[NPOL];
+  float2 v[NPOL];
+  load_weights<NPOL, VEC>(weights + (size_t)e * NPOL, w);
+  if (rw.psf_mode == WGPU_PSF_NONE) {
+    load_vis<NPOL, VEC>(vis + (size_t)e * NPOL, v);
+  } else {
+    float2 ph = make_float2(1.0f, 0.0f);
+    if (rw.dl != 0.0 || rw.dm != 0.0) {
+      const double um = uvw[3 * (size_t)r], vm = uvw[3 * (size_t)r + 1];
+      const double wm = uvw[3 * (size_t)r + 2];
       const double dn =
           sqrt(__dsub_rn(__dsub_rn(1.0, __dmul_rn(rw.dl, rw.dl)), __dmul_rn(rw.dm, rw.dm))) -
           1.0;
@@ -323,69 +503,172 @@ __global__ void prepare_rows_kernel(WeightGridView g, RowWeighting rw, int64_t n
           __dadd_rn(__dadd_rn(__dmul_rn(um, rw.dl), __dmul_rn(vm, rw.dm)), __dmul_rn(wm, dn)));
       double sn, cn;
       sincos(shift / lambda, &sn, &cn);
-      phasor = make_float2((float)cn, (float)sn);
+      ph = make_float2((float)cn, (float)sn);
     }
-    const bool sel = selected == nullptr || selected[e] != 0;
-    float2 c[NPOL];
 #pragma unroll
-    for (int p = 0; p < NPOL; ++p) {
-      const int64_t i = e * NPOL + p;
-      float2 v = rw.psf_mode != WGPU_PSF_NONE ? phasor : vis[i];
-      if (rw.subtract_model) {
-        const float2 m = model[i];
-        v = make_float2(v.x - m.x, v.y - m.y);
-      }
-      float w = sel ? weights[i] : 0.0f;
-      if (rw.visibility_weighting == WGPU_VISW_SQUARED)
-        w = w * w;
-      else if (rw.visibility_weighting == WGPU_VISW_UNIT && w != 0.0f)
-        w = 1.0f;
-      const float cum = w * iw;
-      const bool has = cum != 0.0f;
-      if (p == 0) {
-        vws += (double)(has ? w : 0.0f);
-        vmax = fmax(vmax, (double)cum);
-        count += has ? 1.0 : 0.0;
-      }
-      total += (double)cum;
-      if (weights_out) weights_out[i] = cum;
-      c[p] = make_float2(v.x * cum, v.y * cum);
-    }
-    float2 out;
-    if (NPOL == 1)
-      out = c[0];
-    else if (NPOL == 2)
-      out = ca(c[0], c[NPOL - 1]);
-    else
-      out = collapse4(c, rw.polarization);
-    vis_out[e] = out;
-    if (imaging_out) imaging_out[e] = iw;
+    for (int p = 0; p < NPOL; ++p) v[p] = ph;
   }
-  const double s_vws = block_sum(vws);
-  const double s_total = block_sum(total);
-  const double s_count = block_sum(count);
-  // block maximum of the non-negative per-thread maxima
-  __shared__ double wmax[kThreads / 32];
+  if (rw.subtract_model) {
+    float2 m[NPOL];
+    load_vis<NPOL, VEC>(model + (size_t)e * NPOL, m);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = vmax;
+    for (int p = 0; p < NPOL; ++p) v[p] = make_float2(v[p].x - m[p].x, v[p].y - m[p].y);
+  }
+  const bool sel = selected == nullptr || selected[e] != 0;
+  float2 c[NPOL];
+#pragma unroll
+  for (int p = 0; p < NPOL; ++p) {
+    float wp = sel ? w[p] : 0.0f;
+    if (rw.visibility_weighting == WGPU_VISW_SQUARED)
+      wp = wp * wp;
+    else if (rw.visibility_weighting == WGPU_VISW_UNIT && wp != 0.0f)
+      wp = 1.0f;
+    const float cum = wp * iw;
+    const bool has = cum != 0.0f;
+    if (p == 0) {
+      if (has) acc.vws.add(wp);
+      acc.vmax = fmaxf(acc.vmax, cum);
+      acc.count += has ? 1u : 0u;
+    }
+    acc.total.add(cum);
+    w[p] = cum;
+    c[p] = make_float2(v[p].x * cum, v[p].y * cum);
+  }
+  if (weights_out) {
+    float *o = weights_out + (size_t)e * NPOL;
+    if constexpr (VEC && NPOL == 4)
+      __stcs(reinterpret_cast<float4 *>(o), make_float4(w[0], w[1], w[2], w[3]));
+    else
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) __stcs(o + p, w[p]);
+  }
+  float2 out;
+  if constexpr (NPOL == 1)
+    out = c[0];
+  else if constexpr (NPOL == 2)
+    out = ca(c[0], c[1]);
+  else
+    out = collapse4(c, rw.polarization);
+  __stcs(vis_out + e, out);
+  if (imaging_out) __stcs(imaging_out + e, iw);
+}
+
+// Block reduction of the accumulators and one set of atomics per block.
+__device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
+  const double s_vws = block_sum(acc.vws.value());
+  const double s_total = block_sum(acc.total.value());
+  const double s_count = block_sum((double)acc.count);
+  __shared__ float wmax[kThreads / 32];
+  float m = acc.vmax;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double m = 0.0;
-    for (int k = 0; k < kThreads / 32; ++k) m = fmax(m, wmax[k]);
+    float bm = 0.0f;
+    for (int k = 0; k < kThreads / 32; ++k) bm = fmaxf(bm, wmax[k]);
     if (s_vws != 0.0) atomicAdd(&sums->visibility_weight_sum, s_vws);
     if (s_total != 0.0) atomicAdd(&sums->total_weight, s_total);
     if (s_count != 0.0) atomicAdd(&sums->count, (unsigned long long)s_count);
     // positive doubles order like their bit patterns
-    if (m > 0.0) atomicMax(&sums->max_bits, (unsigned long long)__double_as_longlong(m));
+    if (bm > 0.0f)
+      atomicMax(&sums->max_bits, (unsigned long long)__double_as_longlong((double)bm));
   }
 }
 
+// First pass over a fixed grid of blocks: samples whose imaging-weight cell is
+// decided in FP32 are prepared; the others go to the pending list.
+template <int NPOL, bool VEC>
+__global__ void __launch_bounds__(kThreads) prepare_rows_fast_kernel(
+    WeightGridView g, RowWeighting rw, uint32_t n, uint32_t n_chan, const double *uvw,
+    const ChanScale *cs, const float2 *vis, const float *weights, const float2 *model,
+    const uint8_t *selected, float2 *vis_out, float *weights_out, float *imaging_out,
+    WeightSumsDev *sums, Pending pend) {
+  __shared__ uint32_t s_count;
+  if (threadIdx.x == 0) s_count = 0;
+  __syncthreads();
+  PrepAcc acc;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t e = base + threadIdx.x;
+    bool undecided = false;
+    if (e < n) {
+      const uint32_t r = e / n_chan, ch = e - r * n_chan;
+      const ChanScale c = cs[ch];
+      const int64_t cell = fast_cell(uvw[3 * (size_t)r], uvw[3 * (size_t)r + 1], c, g.width,
+                                     g.height);
+      undecided = cell == -2;
+      if (!undecided)
+        prep_sample<NPOL, VEC>(rw, e, r, cell >= 0 ? g.gridf[cell] : 0.0f, c.lambda, uvw, vis,
+                               weights, model, selected, vis_out, weights_out, imaging_out, acc);
+    }
+    pending_push(pend, &s_count, undecided, e);
+  }
+  finish_prep_sums(acc, sums);
+  if (threadIdx.x == 0) pend.counts[blockIdx.x] = s_count;
+}
+
+// Second pass over the pending samples, with the cell of GetWeight(u, v)
+// computed in double as on the host.
+template <int NPOL, bool VEC>
+__global__ void __launch_bounds__(kThreads) prepare_rows_exact_kernel(
+    WeightGridView g, RowWeighting rw, uint32_t n_chan, const double *uvw, const ChanScale *cs,
+    const float2 *vis, const float *weights, const float2 *model, const uint8_t *selected,
+    float2 *vis_out, float *weights_out, float *imaging_out, WeightSumsDev *sums, Pending pend) {
+  const uint32_t count = pend.counts[blockIdx.x];
+  const uint32_t *list = pend.idx + (size_t)blockIdx.x * pend.cap;
+  PrepAcc acc;
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const uint32_t e = list[i];
+    const uint32_t r = e / n_chan, ch = e - r * n_chan;
+    const double lambda = cs[ch].lambda;
+    const int64_t cell = uv_cell(uvw[3 * (size_t)r] / lambda, uvw[3 * (size_t)r + 1] / lambda,
+                                 g.width, g.height, g.psx, g.psy);
+    prep_sample<NPOL, VEC>(rw, e, r, cell >= 0 ? g.gridf[cell] : 0.0f, lambda, uvw, vis, weights,
+                           model, selected, vis_out, weights_out, imaging_out, acc);
+  }
+  finish_prep_sums(acc, sums);
+}
+
+__global__ void grid_to_float_kernel(const double *grid, int64_t n, float *gridf) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) gridf[i] = (float)grid[i];
+}
+
+// Launch geometry of the two-pass kernels for n samples.
+struct PassShape {
+  unsigned blocks;
+  uint32_t cap;
+};
+
+PassShape pass_shape(uint32_t n) {
+  PassShape s;
+  s.blocks = (unsigned)(8 * sm_count());
+  const uint64_t stride = (uint64_t)s.blocks * kThreads;
+  s.cap = (uint32_t)(((uint64_t)n + stride - 1) / stride * kThreads);
+  return s;
+}
+
+// Samples per launch (row-aligned): indices stay 32-bit.
+int64_t rows_per_launch(int64_t n_chan) { return std::max<int64_t>(1, (1ll << 30) / n_chan); }
+
 }  // namespace
 
-WeightGridView imageweights_view(const wgpu_imageweights_t *iw) {
+
+WeightGridView imageweights_view(const wgpu_imageweights_t *iw_c) {
+  auto *iw = const_cast<wgpu_imageweights_t *>(iw_c);
+  if (iw->gridf_dirty) {
+    // the float copy the row preparation samples: (float)grid, the value
+    // GetWeight's result takes in the reference's float weight buffer
+    const int64_t n = iw->width * (iw->height / 2);
+    grid_to_float_kernel<<<blocks_for(n), kThreads, 0, iw->stream>>>(iw->grid, n, iw->gridf);
+    check_launch("grid_to_float_kernel");
+    WGPU_CUDA(cudaStreamSynchronize(iw->stream));
+    iw->gridf_dirty = false;
+  }
   WeightGridView v;
   v.grid = iw->grid;
+  v.gridf = iw->gridf;
   v.width = iw->width;
   v.height = iw->height;
   v.psx = iw->psx;
@@ -415,32 +698,117 @@ void add_weight_sums(const WeightSumsDev &d, wgpu_weight_sums_t *sums) {
   if (m > sums->max_gridded_weight) sums->max_gridded_weight = m;
 }
 
+namespace {
+
+size_t align16(size_t b) { return (b + 15) / 16 * 16; }
+
+// Work buffer of the two-pass kernels: the channel table, the per-block
+// pending counts and the pending slices of the largest launch.
+struct PassWork {
+  ChanScale *cs;
+  uint32_t *counts;
+  uint32_t *idx;
+};
+
+PassWork carve_work(void *work, int64_t n_chan) {
+  char *p = (char *)work;
+  PassWork w;
+  w.cs = (ChanScale *)p;
+  p += align16(sizeof(ChanScale) * (size_t)n_chan);
+  w.counts = (uint32_t *)p;
+  p += align16(sizeof(uint32_t) * (size_t)(8 * sm_count()));
+  w.idx = (uint32_t *)p;
+  return w;
+}
+
+template <typename T>
+T *at(T *p, size_t k) {
+  return p ? p + k : nullptr;
+}
+
+bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0; }
+
+}  // namespace
+
+size_t pass_work_bytes(int64_t n_rows, int64_t n_chan) {
+  const int64_t rows = std::min(n_rows, rows_per_launch(n_chan));
+  const PassShape ps = pass_shape((uint32_t)(rows * n_chan));
+  return align16(sizeof(ChanScale) * (size_t)n_chan) +
+         align16(sizeof(uint32_t) * (size_t)ps.blocks) + sizeof(uint32_t) * ps.blocks * ps.cap;
+}
+
+void launch_weight_grid(const WeightGridView &g, double *grid, double *total, int as_taper,
+                        int64_t n_rows, int64_t n_chan, int n_pol, const double *uvw,
+                        const double *freq, const float *weights, void *work, cudaStream_t s) {
+  if (n_rows == 0 || n_chan == 0) return;
+  const PassWork w = carve_work(work, n_chan);
+  chan_scale_kernel<<<blocks_for(n_chan), kThreads, 0, s>>>(freq, n_chan, g.width, g.height,
+                                                            g.psx, g.psy, w.cs);
+  check_launch("chan_scale_kernel");
+  const int64_t rpl = rows_per_launch(n_chan);
+  for (int64_t r0 = 0; r0 < n_rows; r0 += rpl) {
+    const int64_t rows = std::min(rpl, n_rows - r0);
+    const uint32_t n = (uint32_t)(rows * n_chan);
+    const size_t off = (size_t)r0 * (size_t)n_chan;
+    const PassShape ps = pass_shape(n);
+    const Pending pend{w.idx, w.counts, ps.cap};
+    weight_grid_fast_kernel<<<ps.blocks, kThreads, 0, s>>>(
+        grid, total, g.width, g.height, as_taper, n, (uint32_t)n_chan, n_pol, uvw + 3 * r0, w.cs,
+        weights + off * n_pol, pend);
+    check_launch("weight_grid_fast_kernel");
+    weight_grid_exact_kernel<<<ps.blocks, kThreads, 0, s>>>(
+        grid, total, g.width, g.height, g.psx, g.psy, as_taper, (uint32_t)n_chan, n_pol,
+        uvw + 3 * r0, w.cs, weights + off * n_pol, pend);
+    check_launch("weight_grid_exact_kernel");
+  }
+}
+
 void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_pol,
                          int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
                          const float2 *vis, const float *weights, const float2 *model,
                          const uint8_t *selected, float2 *vis_out, float *weights_out,
-                         float *imaging_out, WeightSumsDev *sums, cudaStream_t s) {
-  const int64_t n = n_rows * n_chan;
-  if (n == 0) return;
-  const unsigned nb = blocks_for(n);
-  switch (n_pol) {
-    case 1:
-      prepare_rows_kernel<1><<<nb, kThreads, 0, s>>>(g, rw, n_rows, n_chan, uvw, freq, vis,
-                                                      weights, model, selected, vis_out,
-                                                      weights_out, imaging_out, sums);
-      break;
-    case 2:
-      prepare_rows_kernel<2><<<nb, kThreads, 0, s>>>(g, rw, n_rows, n_chan, uvw, freq, vis,
-                                                      weights, model, selected, vis_out,
-                                                      weights_out, imaging_out, sums);
-      break;
-    default:
-      prepare_rows_kernel<4><<<nb, kThreads, 0, s>>>(g, rw, n_rows, n_chan, uvw, freq, vis,
-                                                      weights, model, selected, vis_out,
-                                                      weights_out, imaging_out, sums);
-      break;
+                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s) {
+  if (n_rows == 0 || n_chan == 0) return;
+  const PassWork w = carve_work(work, n_chan);
+  chan_scale_kernel<<<blocks_for(n_chan), kThreads, 0, s>>>(freq, n_chan, g.width, g.height,
+                                                            g.psx, g.psy, w.cs);
+  check_launch("chan_scale_kernel");
+  const bool vec = n_pol >= 2 && aligned16(vis) && aligned16(weights) && aligned16(model) &&
+                   aligned16(weights_out);
+  const int64_t rpl = rows_per_launch(n_chan);
+  for (int64_t r0 = 0; r0 < n_rows; r0 += rpl) {
+    const int64_t rows = std::min(rpl, n_rows - r0);
+    const uint32_t n = (uint32_t)(rows * n_chan);
+    const size_t off = (size_t)r0 * (size_t)n_chan, offp = off * (size_t)n_pol;
+    const PassShape ps = pass_shape(n);
+    const Pending pend{w.idx, w.counts, ps.cap};
+    const double *u = uvw + 3 * r0;
+    const float2 *v = at(vis, offp), *m = at(model, offp);
+    const float *wt = weights + offp;
+    const uint8_t *sl = at(selected, off);
+    float2 *vo = vis_out + off;
+    float *wo = at(weights_out, offp), *io = at(imaging_out, off);
+#define WGPU_PREP_LAUNCH(NP, VEC)                                                              \
+  do {                                                                                         \
+    prepare_rows_fast_kernel<NP, VEC><<<ps.blocks, kThreads, 0, s>>>(                         \
+        g, rw, n, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);            \
+    check_launch("prepare_rows_fast_kernel");                                                  \
+    prepare_rows_exact_kernel<NP, VEC><<<ps.blocks, kThreads, 0, s>>>(                        \
+        g, rw, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);               \
+    check_launch("prepare_rows_exact_kernel");                                                 \
+  } while (0)
+    if (n_pol == 1)
+      WGPU_PREP_LAUNCH(1, false);
+    else if (n_pol == 2 && vec)
+      WGPU_PREP_LAUNCH(2, true);
+    else if (n_pol == 2)
+      WGPU_PREP_LAUNCH(2, false);
+    else if (vec)
+      WGPU_PREP_LAUNCH(4, true);
+    else
+      WGPU_PREP_LAUNCH(4, false);
+#undef WGPU_PREP_LAUNCH
   }
-  check_launch("prepare_rows_kernel");
 }
 
 }  // namespace wgpu
@@ -510,11 +878,17 @@ bool valid_weighting(const wgpu_row_weighting_t *rw) {
 
 void grid_device(wgpu_imageweights_t *iw, size_t n_rows, size_t n_chan, size_t n_pol,
                  const double *du, const double *df, const float *dw) {
-  const int64_t n = (int64_t)(n_rows * n_chan);
-  wgpu::weight_grid_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
-      iw->grid, iw->sums, iw->width, iw->height, iw->psx, iw->psy, iw->as_taper ? 1 : 0,
-      (int64_t)n_rows, (int64_t)n_chan, (int)n_pol, du, df, dw);
-  wgpu::check_launch("weight_grid_kernel");
+  void *work = scratch(iw, 9, wgpu::pass_work_bytes((int64_t)n_rows, (int64_t)n_chan));
+  iw->gridf_dirty = true;
+  wgpu::WeightGridView g;
+  g.grid = iw->grid;
+  g.gridf = nullptr;
+  g.width = iw->width;
+  g.height = iw->height;
+  g.psx = iw->psx;
+  g.psy = iw->psy;
+  wgpu::launch_weight_grid(g, iw->grid, iw->sums, iw->as_taper ? 1 : 0, (int64_t)n_rows,
+                           (int64_t)n_chan, (int)n_pol, du, df, dw, work, iw->stream);
   WGPU_CUDA(cudaStreamSynchronize(iw->stream));
 }
 
@@ -525,10 +899,12 @@ void prepare_device(wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw, siz
                     const float2 *dv, const float *dw, const float2 *dm, const uint8_t *ds,
                     float2 *dvo, float *dwo, float *dio, wgpu_weight_sums_t *sums) {
   auto *dsum = (wgpu::WeightSumsDev *)scratch(iw, 7, sizeof(wgpu::WeightSumsDev));
+  void *work = scratch(iw, 8, wgpu::pass_work_bytes((int64_t)n_rows, (int64_t)n_chan));
+  const wgpu::WeightGridView view = wgpu::imageweights_view(iw);
   WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(wgpu::WeightSumsDev), iw->stream));
-  wgpu::launch_prepare_rows(wgpu::imageweights_view(iw), wgpu::row_weighting(*rw), (int)n_pol,
-                            (int64_t)n_rows, (int64_t)n_chan, du, df, dv, dw, dm, ds, dvo, dwo,
-                            dio, dsum, iw->stream);
+  wgpu::launch_prepare_rows(view, wgpu::row_weighting(*rw), (int)n_pol, (int64_t)n_rows,
+                            (int64_t)n_chan, du, df, dv, dw, dm, ds, dvo, dwo, dio, dsum, work,
+                            iw->stream);
   wgpu::WeightSumsDev hs;
   WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, iw->stream));
   WGPU_CUDA(cudaStreamSynchronize(iw->stream));
@@ -588,6 +964,7 @@ int wgpu_imageweights_create(int mode, double briggs_robustness, size_t image_wi
     WGPU_CUDA(cudaGetDevice(&iw->device));
     WGPU_CUDA(cudaStreamCreateWithFlags(&iw->stream, cudaStreamNonBlocking));
     WGPU_CUDA(cudaMalloc(&iw->grid, sizeof(double) * (size_t)grid_cells(iw)));
+    WGPU_CUDA(cudaMalloc(&iw->gridf, sizeof(float) * (size_t)grid_cells(iw)));
     WGPU_CUDA(cudaMalloc(&iw->sums, sizeof(double) * 2));
     WGPU_CUDA(cudaMalloc(&iw->partials, sizeof(double) * wgpu::kReduceBlocks));
     WGPU_CUDA(cudaMemsetAsync(iw->grid, 0, sizeof(double) * (size_t)grid_cells(iw), iw->stream));
@@ -611,6 +988,7 @@ void wgpu_imageweights_destroy(wgpu_imageweights_t *iw) {
   for (int k = 0; k < wgpu_imageweights::kScratch; ++k)
     if (iw->scratch[k]) cudaFree(iw->scratch[k]);
   if (iw->grid) cudaFree(iw->grid);
+  if (iw->gridf) cudaFree(iw->gridf);
   if (iw->sums) cudaFree(iw->sums);
   if (iw->partials) cudaFree(iw->partials);
   if (iw->stream) cudaStreamDestroy(iw->stream);
@@ -682,6 +1060,7 @@ int wgpu_imageweights_finish(wgpu_imageweights_t *iw) {
     wgpu::check_launch("weight_finish_kernel");
     WGPU_CUDA(cudaStreamSynchronize(iw->stream));
     iw->finished = true;
+    iw->gridf_dirty = true;
   });
 }
 
@@ -703,6 +1082,7 @@ int wgpu_imageweights_taper(wgpu_imageweights_t *iw, int kind, double a, double 
       wgpu::rank_filter_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
           src, iw->grid, iw->width, iw->height / 2, a, (int64_t)b);
       wgpu::check_launch("rank_filter_kernel");
+      iw->gridf_dirty = true;
     } else {
       double pa = a;
       if (kind == WGPU_TAPER_GAUSSIAN) {
@@ -717,6 +1097,7 @@ int wgpu_imageweights_taper(wgpu_imageweights_t *iw, int kind, double a, double 
       wgpu::weight_taper_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
           iw->grid, iw->width, iw->height, iw->psx, iw->psy, kind, pa, b);
       wgpu::check_launch("weight_taper_kernel");
+      iw->gridf_dirty = true;
     }
     WGPU_CUDA(cudaStreamSynchronize(iw->stream));
   });
@@ -730,6 +1111,7 @@ int wgpu_imageweights_set_all(wgpu_imageweights_t *iw, double value) {
     wgpu::weight_fill_kernel<<<wgpu::blocks_for(n), wgpu::kThreads, 0, iw->stream>>>(
         iw->grid, n, value);
     wgpu::check_launch("weight_fill_kernel");
+    iw->gridf_dirty = true;
     WGPU_CUDA(cudaStreamSynchronize(iw->stream));
   });
 }

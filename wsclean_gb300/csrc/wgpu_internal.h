@@ -305,6 +305,7 @@ void launch_forward_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
 // doubles, cell (x, y) at grid[x + y * width].
 struct WeightGridView {
   const double *grid;
+  const float *gridf;  // the same values as float (what the row weighting samples)
   int64_t width, height;
   double psx, psy;
 };
@@ -327,12 +328,21 @@ struct WeightSumsDev {
 };
 void add_weight_sums(const WeightSumsDev &d, wgpu_weight_sums_t *sums);
 
+// Work buffer (bytes) of launch_weight_grid / launch_prepare_rows for a chunk
+// of n_rows x n_chan samples.
+size_t pass_work_bytes(int64_t n_rows, int64_t n_chan);
+
+// ImageWeights::Grid over n_rows x n_chan samples into grid / total.
+void launch_weight_grid(const WeightGridView &g, double *grid, double *total, int as_taper,
+                        int64_t n_rows, int64_t n_chan, int n_pol, const double *uvw,
+                        const double *freq, const float *weights, void *work, cudaStream_t s);
+
 // CalculateWeights + ApplyWeights + CollapseData for n_rows x n_chan samples.
 void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_pol,
                          int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
                          const float2 *vis, const float *weights, const float2 *model,
                          const uint8_t *selected, float2 *vis_out, float *weights_out,
-                         float *imaging_out, WeightSumsDev *sums, cudaStream_t s);
+                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s);
 
 void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                         const float2 *vis_in, const uint64_t *ant_pairs,
@@ -396,7 +406,8 @@ enum ArenaSlot {
   kSlotRowWeights,  // raw-row preparation: visibility weights,
   kSlotRowModel,    // model visibilities,
   kSlotRowSel,      // selection bytes,
-  kSlotRowSums,     // and the device-side weight sums
+  kSlotRowSums,     // the device-side weight sums
+  kSlotRowWork,     // and the two-pass work buffer
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
