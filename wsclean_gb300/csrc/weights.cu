@@ -520,10 +520,10 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, 
   for (int p = 0; p < NPOL; ++p) {
     float wp = sel ? w[p] : 0.0f;
     if (rw.visibility_weighting == WGPU_VISW_SQUARED)
-      wp = wp * wp;
+      wp = __fmul_rn(wp, wp);
     else if (rw.visibility_weighting == WGPU_VISW_UNIT && wp != 0.0f)
       wp = 1.0f;
-    const float cum = wp * iw;
+    const float cum = __fmul_rn(wp, iw);
     const bool has = cum != 0.0f;
     if (p == 0) {
       if (has) acc.vws.add(wp);
@@ -532,7 +532,8 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, 
     }
     acc.total.add(cum);
     w[p] = cum;
-    c[p] = make_float2(v[p].x * cum, v[p].y * cum);
+    // rounded products: the collapse's sums must not fuse with them
+    c[p] = make_float2(__fmul_rn(v[p].x, cum), __fmul_rn(v[p].y, cum));
   }
   if (weights_out) {
     float *o = weights_out + (size_t)e * NPOL;
