@@ -736,7 +736,8 @@ def run_rowweights(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     t0 = time.time()
-    d = synthetic.make_workload("wide8192", seed=5, with_model=False, n_t=75)
+    d = synthetic.make_workload("wide8192", seed=5, with_model=False, n_t=75,
+                                max_rows=args.max_rows)
     uvw, freq = d["uvw"], d["freq"]
     n_rows, n_chan, n_pol = uvw.shape[0], freq.size, 4
     n = n_rows * n_chan
