@@ -125,21 +125,66 @@ __global__ void chan_scale_kernel(const double *freq, int64_t n_chan, int64_t W,
   t[ch] = c;
 }
 
+// Conversions between float and double done with integer operations on the
+// bit patterns: this GPU's FP64 pipe (which also executes F2F conversions and
+// double compares) is a small fraction of its FP32 rate, and the per-sample
+// paths below use none of it.
+//
+// float -> double, exact (zeros, subnormals, infinities and NaNs included).
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned long long r;
+  if (e == 0xffu) {
+    r = 0x7ff0000000000000ull | ((unsigned long long)m << 29);
+  } else if (e != 0u) {
+    r = ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+  } else if (m == 0u) {
+    r = 0ull;
+  } else {  // subnormal m * 2^-149 with its top bit at position p
+    const int p = 31 - __clz((int)m);
+    r = ((unsigned long long)(p + 874) << 52) |
+        (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+  }
+  return __longlong_as_double((long long)(sign | r));
+}
+
+// double -> float by truncating the mantissa (error below one float ulp);
+// magnitudes under 2^-126 become zero; false when beyond the float range,
+// infinite or NaN.
+__device__ __forceinline__ bool d2f_trunc(unsigned long long b, float *out) {
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned sign = hi & 0x80000000u;
+  if (e >= 255) return false;
+  if (e <= 0) {
+    *out = __uint_as_float(sign);
+    return true;
+  }
+  *out = __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  return true;
+}
+
 // The cell of (um, vm) metres at one channel, decided in FP32.  The FP32
-// estimate x' = um * su + W/2 differs from the host's double evaluation
-// (u = um / lambda, then u * W * psx + W / 2, each rounded) by less than
-// 2^-22 (|um su| + |x'|) (three float roundings against five double ones); a
-// cell is decided when both coordinates lie farther than twice that from a
-// cell edge.  Returns the cell, -1 when decided outside the grid, -2 when
-// undecided (also for non-finite, tiny-v or out-of-float-range inputs).
+// estimate x' = um * su + W/2 (um truncated to float: < 1 ulp; su and the
+// fused multiply-add rounded: 1/2 ulp each) differs from the host's double
+// evaluation (u = um / lambda, then u * W * psx + W / 2, each rounded) by less
+// than 2^-22 (|um su| + |x'|); y' = vm * sv by less than 2^-22 |y'|.  A cell
+// is decided when both coordinates lie farther than twice (x) or four times
+// (y) that from a cell edge.  Returns the cell, -1 when decided outside the
+// grid, -2 when undecided (also for non-finite inputs, |vm| below 2^-930,
+// whose sign the division by the wavelength could lose, and values beyond the
+// float range).  Reflection into v >= 0 flips the signs exactly.
 __device__ __forceinline__ int64_t fast_cell(double um, double vm, const ChanScale &c, int64_t W,
                                              int64_t H) {
-  if (!(fabs(vm) >= 1e-280 || vm == 0.0)) return -2;  // tiny or NaN v
-  if (vm < 0.0) {
-    um = -um;
-    vm = -vm;
-  }
-  const float uf = (float)um, vf = (float)vm;
+  const unsigned long long bu = (unsigned long long)__double_as_longlong(um);
+  const unsigned long long bv = (unsigned long long)__double_as_longlong(vm);
+  const unsigned long long av = bv & 0x7fffffffffffffffull;
+  if (!(av == 0ull || (av >= 0x05d0000000000000ull && av <= 0x7ff0000000000000ull))) return -2;
+  const unsigned long long flip = (bv >> 63 != 0ull && av != 0ull) ? (1ull << 63) : 0ull;
+  float uf, vf;
+  if (!d2f_trunc(bu ^ flip, &uf) || !d2f_trunc(av, &vf)) return -2;
   const float xf = fmaf(uf, c.su, (float)(W / 2));
   const float bx = 0x1p-21f * (fabsf(uf * c.su) + fabsf(xf)) + 1e-30f;
   const float kx = floorf(xf), fx = xf - kx;
@@ -168,7 +213,7 @@ struct FloatSum {
     if (++n == kFlush) flush();
   }
   __device__ __forceinline__ void flush() {
-    acc += (double)hi + (double)lo;
+    acc += f2d_bits(hi) + f2d_bits(lo);
     hi = lo = 0.0f;
     n = 0;
   }
@@ -198,6 +243,30 @@ __device__ __forceinline__ void pending_push(const Pending &p, uint32_t *s_count
   if (want) p.idx[(size_t)blockIdx.x * p.cap + base + __popc(m & ((1u << lane) - 1))] = e;
 }
 
+// Adds one sample's correlation weights (1 for a non-zero weight when the
+// weights are a taper) to its cell: their float-float sum (hi, lo) goes to
+// the cell as one or two double atomic adds, which L2 performs.
+__device__ __forceinline__ void grid_sample(double *cellp, const float *w, int n_pol,
+                                            int as_taper, FloatSum &tot) {
+  float hi = 0.0f, lo = 0.0f;
+  for (int p = 0; p < n_pol; ++p) {
+    float x = w[p];
+    if (as_taper && x != 0.0f) x = 1.0f;
+    const float sum = hi + x;
+    const float bp = sum - hi;
+    lo += (hi - (sum - bp)) + (x - bp);
+    hi = sum;
+  }
+  if (hi != 0.0f) {
+    atomicAdd(cellp, f2d_bits(hi));
+    tot.add(hi);
+  }
+  if (lo != 0.0f) {
+    atomicAdd(cellp, f2d_bits(lo));
+    tot.add(lo);
+  }
+}
+
 // Grid(MSProvider &, BandData) (imageweights.cpp:75-112), first pass, over a
 // fixed grid of blocks: for every (row, channel) with an FP32-decided cell the
 // correlations' weights (1 for a non-zero weight when the weights are a
@@ -220,19 +289,7 @@ __global__ void __launch_bounds__(kThreads) weight_grid_fast_kernel(
       const uint32_t r = e / n_chan, ch = e - r * n_chan;
       const int64_t cell = fast_cell(uvw[3 * (size_t)r], uvw[3 * (size_t)r + 1], cs[ch], W, H);
       undecided = cell == -2;
-      if (cell >= 0) {
-        FloatSum s;
-        for (int p = 0; p < n_pol; ++p) {
-          float w = weights[(size_t)e * n_pol + p];
-          if (as_taper && w != 0.0f) w = 1.0f;
-          s.add(w);
-        }
-        const double sw = s.value();
-        if (sw != 0.0) {
-          atomicAdd(grid + cell, sw);
-          tot.acc += sw;
-        }
-      }
+      if (cell >= 0) grid_sample(grid + cell, weights + (size_t)e * n_pol, n_pol, as_taper, tot);
     }
     pending_push(pend, &s_count, undecided, e);
   }
@@ -262,18 +319,7 @@ __global__ void __launch_bounds__(kThreads) weight_grid_exact_kernel(
     }
     const double lambda = cs[ch].lambda;
     const int64_t cell = uv_cell(um / lambda, vm / lambda, W, H, psx, psy);
-    if (cell < 0) continue;
-    FloatSum s;
-    for (int p = 0; p < n_pol; ++p) {
-      float w = weights[(size_t)e * n_pol + p];
-      if (as_taper && w != 0.0f) w = 1.0f;
-      s.add(w);
-    }
-    const double sw = s.value();
-    if (sw != 0.0) {
-      atomicAdd(grid + cell, sw);
-      tot.acc += sw;
-    }
+    if (cell >= 0) grid_sample(grid + cell, weights + (size_t)e * n_pol, n_pol, as_taper, tot);
   }
   const double t = block_sum(tot.value());
   if (threadIdx.x == 0 && t != 0.0) atomicAdd(total, t);
@@ -580,7 +626,7 @@ __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
 // First pass over a fixed grid of blocks: samples whose imaging-weight cell is
 // decided in FP32 are prepared; the others go to the pending list.
 template <int NPOL, bool VEC>
-__global__ void __launch_bounds__(kThreads) prepare_rows_fast_kernel(
+__global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
     WeightGridView g, RowWeighting rw, uint32_t n, uint32_t n_chan, const double *uvw,
     const ChanScale *cs, const float2 *vis, const float *weights, const float2 *model,
     const uint8_t *selected, float2 *vis_out, float *weights_out, float *imaging_out,
@@ -642,12 +688,22 @@ struct PassShape {
   uint32_t cap;
 };
 
-PassShape pass_shape(uint32_t n) {
+constexpr int kMaxBlocksPerSm = 8;
+
+// All blocks resident at once (a grid-stride loop over the samples).
+PassShape pass_shape(uint32_t n, int blocks_per_sm) {
   PassShape s;
-  s.blocks = (unsigned)(8 * sm_count());
+  s.blocks = (unsigned)(std::max(1, std::min(blocks_per_sm, kMaxBlocksPerSm)) * sm_count());
   const uint64_t stride = (uint64_t)s.blocks * kThreads;
   s.cap = (uint32_t)(((uint64_t)n + stride - 1) / stride * kThreads);
   return s;
+}
+
+template <typename Kernel>
+int resident_blocks(Kernel k) {
+  int nb = 0;
+  WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, 0));
+  return nb;
 }
 
 // Samples per launch (row-aligned): indices stay 32-bit.
@@ -717,7 +773,7 @@ PassWork carve_work(void *work, int64_t n_chan) {
   w.cs = (ChanScale *)p;
   p += align16(sizeof(ChanScale) * (size_t)n_chan);
   w.counts = (uint32_t *)p;
-  p += align16(sizeof(uint32_t) * (size_t)(8 * sm_count()));
+  p += align16(sizeof(uint32_t) * (size_t)(kMaxBlocksPerSm * sm_count()));
   w.idx = (uint32_t *)p;
   return w;
 }
@@ -732,10 +788,11 @@ bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15) == 0;
 }  // namespace
 
 size_t pass_work_bytes(int64_t n_rows, int64_t n_chan) {
+  // blocks * cap <= n + blocks * kThreads for any number of blocks
   const int64_t rows = std::min(n_rows, rows_per_launch(n_chan));
-  const PassShape ps = pass_shape((uint32_t)(rows * n_chan));
-  return align16(sizeof(ChanScale) * (size_t)n_chan) +
-         align16(sizeof(uint32_t) * (size_t)ps.blocks) + sizeof(uint32_t) * ps.blocks * ps.cap;
+  const size_t max_blocks = (size_t)kMaxBlocksPerSm * (size_t)sm_count();
+  return align16(sizeof(ChanScale) * (size_t)n_chan) + align16(sizeof(uint32_t) * max_blocks) +
+         sizeof(uint32_t) * ((size_t)(rows * n_chan) + max_blocks * kThreads);
 }
 
 void launch_weight_grid(const WeightGridView &g, double *grid, double *total, int as_taper,
@@ -751,7 +808,7 @@ void launch_weight_grid(const WeightGridView &g, double *grid, double *total, in
     const int64_t rows = std::min(rpl, n_rows - r0);
     const uint32_t n = (uint32_t)(rows * n_chan);
     const size_t off = (size_t)r0 * (size_t)n_chan;
-    const PassShape ps = pass_shape(n);
+    const PassShape ps = pass_shape(n, resident_blocks(weight_grid_fast_kernel));
     const Pending pend{w.idx, w.counts, ps.cap};
     weight_grid_fast_kernel<<<ps.blocks, kThreads, 0, s>>>(
         grid, total, g.width, g.height, as_taper, n, (uint32_t)n_chan, n_pol, uvw + 3 * r0, w.cs,
@@ -781,7 +838,10 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
     const int64_t rows = std::min(rpl, n_rows - r0);
     const uint32_t n = (uint32_t)(rows * n_chan);
     const size_t off = (size_t)r0 * (size_t)n_chan, offp = off * (size_t)n_pol;
-    const PassShape ps = pass_shape(n);
+    const int bps = n_pol == 1 ? resident_blocks(prepare_rows_fast_kernel<1, false>)
+                    : n_pol == 2 ? resident_blocks(prepare_rows_fast_kernel<2, true>)
+                                 : resident_blocks(prepare_rows_fast_kernel<4, true>);
+    const PassShape ps = pass_shape(n, bps);
     const Pending pend{w.idx, w.counts, ps.cap};
     const double *u = uvw + 3 * r0;
     const float2 *v = at(vis, offp), *m = at(model, offp);
