@@ -613,6 +613,58 @@ int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *gridder, const wgpu_imagewei
                                     const float *weights, const float *model,
                                     const uint8_t *selected, wgpu_weight_sums_t *sums);
 
+/* ---- Resampling and trimming around the boundary -------------------------
+ * WGriddingMSGridder::FinishInversion / StartPredict
+ * (wgridder/wgriddingmsgridder.cpp:273-340) move the image between the padded
+ * image size and the inversion size of the small inversion with an FFT
+ * resampler (schaapcommon's, absent from the reference tree; restated as the
+ * published method: half-spectrum copy of the low frequencies, inverse, factor
+ * 1 / (in_w * in_h)) and trim / untrim it around the centre. */
+
+/* CalculateFFTSize (math/calculatefftsize.h:24-35): the Nyquist-sampled size of
+ * `size` pixels of pixel_scale for a beam of beam_size (radians), and the
+ * next multiple of 4 with only factors 2, 3, 5, 7 (at most size). */
+int wgpu_calculate_fft_size(size_t size, double pixel_scale, double beam_size,
+                            size_t *minimal_size, size_t *optimal_size);
+
+/* The small-inversion sizes of MsGridder::CalculateOverallMetaData
+ * (gridding/msgridder.cpp:42-75): when the optimal FFT size is smaller than
+ * the image, the inversion size (at least 32) and its larger pixels;
+ * otherwise the inputs unchanged. */
+int wgpu_small_inversion_size(size_t width, size_t height, double pixel_size_x,
+                              double pixel_size_y, double beam_size, size_t *inversion_width,
+                              size_t *inversion_height, double *inversion_pixel_x,
+                              double *inversion_pixel_y);
+
+/* getActualTrimmedSize (wgridder/wgriddingmsgridder.cpp:243-260): the
+ * gridder's trimmed size for an inversion size and image padding. */
+int wgpu_actual_trimmed_size(size_t inversion_width, size_t inversion_height,
+                             double image_padding, size_t *trimmed_width,
+                             size_t *trimmed_height);
+
+/* FFT resampling of a row-major in_w x in_h float image to out_w x out_h
+ * (sizes 1 to 65536 whose prime factors are at most 64); non-finite input
+ * pixels count as 0.  The device variant runs on `stream` (cudaStream_t, NULL
+ * for the default stream). */
+int wgpu_resample(const float *in, size_t in_w, size_t in_h, float *out, size_t out_w,
+                  size_t out_h);
+int wgpu_resample_device(const float *d_in, size_t in_w, size_t in_h, float *d_out,
+                         size_t out_w, size_t out_h, void *stream);
+
+/* FinishInversion after FinalizeImage: the gridder's image (RealImage, at the
+ * inversion size = the gridder's width x height) resampled to image_width x
+ * image_height when those differ, then trimmed to trim_width x trim_height
+ * (centred), into `image`; all on the device. */
+int wgpu_gridder_finish_inversion(wgpu_gridder_t *gridder, size_t image_width,
+                                  size_t image_height, size_t trim_width, size_t trim_height,
+                                  float *image);
+
+/* StartPredict: the trim_width x trim_height model untrimmed (zero padded,
+ * centred) to image_width x image_height, resampled to the gridder's width x
+ * height when those differ, then InitializePrediction; all on the device. */
+int wgpu_gridder_start_predict(wgpu_gridder_t *gridder, size_t trim_width, size_t trim_height,
+                               size_t image_width, size_t image_height, const float *model);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,11 +24,32 @@ class OraclePlan(C.Structure):
 _lib = None
 
 
+REF_FFTSIZE = os.path.join(HERE, "_ref", "libref_fftsize.so")
+
+
 def build():
     r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    # the reference's own header-only code, where the reference tree exists
+    subprocess.run(["make", "-C", HERE, "ref"], capture_output=True, text=True)
     return LIB_PATH
+
+
+def ref_calculate_fft_size():
+    """The reference's CalculateFFTSize compiled from its own header
+    (oracle/_ref), or None where the reference tree was absent at build."""
+    if not os.path.exists(REF_FFTSIZE):
+        return None
+    L = C.CDLL(REF_FFTSIZE)
+    L.ref_calculate_fft_size.argtypes = [C.c_size_t, C.c_double, C.c_double,
+                                         C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+
+    def fn(size, pixel_scale, beam_size):
+        mn, opt = C.c_size_t(), C.c_size_t()
+        L.ref_calculate_fft_size(size, pixel_scale, beam_size, C.byref(mn), C.byref(opt))
+        return mn.value, opt.value
+    return fn
 
 
 def lib():

@@ -184,6 +184,14 @@ _PROTOS = {
                               P, C.POINTER(WeightSums)]),
     "wgpu_prepare_rows_device": (I, [P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P, P, P, P, P,
                                      P, P, P, C.POINTER(WeightSums)]),
+    "wgpu_calculate_fft_size": (I, [SZ, D, D, C.POINTER(SZ), C.POINTER(SZ)]),
+    "wgpu_small_inversion_size": (I, [SZ, SZ, D, D, D, C.POINTER(SZ), C.POINTER(SZ),
+                                      C.POINTER(D), C.POINTER(D)]),
+    "wgpu_actual_trimmed_size": (I, [SZ, SZ, D, C.POINTER(SZ), C.POINTER(SZ)]),
+    "wgpu_resample": (I, [P, SZ, SZ, P, SZ, SZ]),
+    "wgpu_resample_device": (I, [P, SZ, SZ, P, SZ, SZ, P]),
+    "wgpu_gridder_finish_inversion": (I, [P, SZ, SZ, SZ, SZ, P]),
+    "wgpu_gridder_start_predict": (I, [P, SZ, SZ, SZ, SZ, P]),
     "wgpu_gridder_add_inversion_rows": (I, [P, P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P,
                                             P, P, P, P, C.POINTER(WeightSums)]),
 }

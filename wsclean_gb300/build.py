@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwgpu.so")
 
 SOURCES = ["api.cu", "bucket.cu", "grid.cu", "fft.cu", "correct.cu", "util.cu", "server.cu",
-           "facets.cu", "weights.cu", "plan.cpp"]
+           "facets.cu", "weights.cu", "resample.cu", "plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]

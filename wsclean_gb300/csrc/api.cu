@@ -1055,6 +1055,84 @@ int wgpu_gridder_initialize_prediction(wgpu_gridder_t *g, const float *image) {
   });
 }
 
+int wgpu_gridder_finish_inversion(wgpu_gridder_t *g, size_t image_width, size_t image_height,
+                                  size_t trim_width, size_t trim_height, float *image) {
+  if (!g || !image) return fail(WGPU_ERR_INVALID, "null argument");
+  if (!image_width || !image_height || trim_width > image_width || trim_height > image_height ||
+      !trim_width || !trim_height || image_width > 65536 || image_height > 65536)
+    return fail(WGPU_ERR_INVALID, "invalid image or trim size");
+  return guarded([&] {
+    if (!g->d_img) throw Error(WGPU_ERR_STATE, "FinishInversion without an image");
+    cudaStream_t s = g->stream;
+    // RealImage at the inversion size (NaN outside the gridder's trimmed
+    // region), resampled to the image size, trimmed (wgriddingmsgridder.cpp:
+    // 285-309)
+    const int64_t w = (int64_t)g->width, h = (int64_t)g->height;
+    float *d_full = (float *)g->arena.get(kSlotImgIO, sizeof(float) * (size_t)(w * h));
+    image_out_kernel<<<(unsigned)((w * h + 255) / 256), 256, 0, s>>>(
+        g->d_img, g->prec, (int64_t)g->width_t, (int64_t)g->height_t, w, h, d_full);
+    check_launch("image_out_kernel");
+    const float *src = d_full;
+    int64_t sw = w, sh = h;
+    if ((int64_t)image_width != w || (int64_t)image_height != h) {
+      float *d_rs = (float *)g->arena.get(kSlotResampleOut,
+                                          sizeof(float) * image_width * image_height);
+      void *work = g->arena.get(kSlotResampleWork,
+                                resample_work_bytes(w, h, image_width, image_height));
+      resample_device(d_full, w, h, d_rs, (int64_t)image_width, (int64_t)image_height, work, s);
+      src = d_rs;
+      sw = (int64_t)image_width;
+      sh = (int64_t)image_height;
+    }
+    if ((int64_t)trim_width != sw || (int64_t)trim_height != sh) {
+      float *d_t = (float *)g->arena.get(kSlotResampleTrim,
+                                         sizeof(float) * trim_width * trim_height);
+      launch_trim(src, sw, sh, d_t, (int64_t)trim_width, (int64_t)trim_height, s);
+      src = d_t;
+    }
+    copy_to_host(g, image, src, sizeof(float) * trim_width * trim_height);
+  });
+}
+
+int wgpu_gridder_start_predict(wgpu_gridder_t *g, size_t trim_width, size_t trim_height,
+                               size_t image_width, size_t image_height, const float *model) {
+  if (!g || !model) return fail(WGPU_ERR_INVALID, "null argument");
+  if (!image_width || !image_height || trim_width > image_width || trim_height > image_height ||
+      !trim_width || !trim_height || image_width > 65536 || image_height > 65536)
+    return fail(WGPU_ERR_INVALID, "invalid image or trim size");
+  return guarded([&] {
+    ensure_image(g);
+    cudaStream_t s = g->stream;
+    // untrim to the image size, resample to the inversion size, then the
+    // gridder's InitializePrediction (wgriddingmsgridder.cpp:311-340)
+    const int64_t w = (int64_t)g->width, h = (int64_t)g->height;
+    float *d_m = (float *)g->arena.get(kSlotResampleTrim, sizeof(float) * trim_width * trim_height);
+    copy_to_device(g, d_m, model, sizeof(float) * trim_width * trim_height);
+    const float *src = d_m;
+    int64_t sw = (int64_t)trim_width, sh = (int64_t)trim_height;
+    if (trim_width != image_width || trim_height != image_height) {
+      float *d_u = (float *)g->arena.get(kSlotResampleOut,
+                                         sizeof(float) * image_width * image_height);
+      launch_untrim(d_m, sw, sh, d_u, (int64_t)image_width, (int64_t)image_height, s);
+      src = d_u;
+      sw = (int64_t)image_width;
+      sh = (int64_t)image_height;
+    }
+    if (sw != w || sh != h) {
+      float *d_full = (float *)g->arena.get(kSlotImgIO, sizeof(float) * (size_t)(w * h));
+      void *work = g->arena.get(kSlotResampleWork, resample_work_bytes(sw, sh, w, h));
+      resample_device(src, sw, sh, d_full, w, h, work, s);
+      src = d_full;
+    }
+    const int64_t nt = (int64_t)(g->width_t * g->height_t);
+    image_in_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(
+        src, g->prec, (int64_t)g->width_t, (int64_t)g->height_t, w, h, g->d_img);
+    check_launch("image_in_kernel");
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    g->mode = wgpu_gridder::Mode::kPrediction;
+  });
+}
+
 int wgpu_gridder_predict_visibilities_device(wgpu_gridder_t *g, size_t n_rows,
                                              size_t n_chan, const double *d_uvw,
                                              const double *d_freq, float *d_vis) {

@@ -344,6 +344,18 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
                          const uint8_t *selected, float2 *vis_out, float *weights_out,
                          float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s);
 
+// ---- resampling and trimming (resample.cu) ---------------------------------
+size_t resample_work_bytes(int64_t in_w, int64_t in_h, int64_t out_w, int64_t out_h);
+// FFT resampling of a row-major float image (non-finite pixels count as 0).
+void resample_device(const float *in, int64_t in_w, int64_t in_h, float *out, int64_t out_w,
+                     int64_t out_h, void *work, cudaStream_t s);
+// The centred out_w x out_h window of an in_w x in_h image, and its inverse
+// (zero outside the window).
+void launch_trim(const float *in, int64_t in_w, int64_t in_h, float *out, int64_t out_w,
+                 int64_t out_h, cudaStream_t s);
+void launch_untrim(const float *in, int64_t in_w, int64_t in_h, float *out, int64_t out_w,
+                   int64_t out_h, cudaStream_t s);
+
 void launch_apply_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                         const float2 *vis_in, const uint64_t *ant_pairs,
                         const uint64_t *time_offsets, const float2 *sol,
@@ -363,7 +375,7 @@ class DeviceArena {
   void release();
 
  private:
-  static constexpr int kSlots = 40;
+  static constexpr int kSlots = 48;
   void *ptr_[kSlots] = {};
   size_t size_[kSlots] = {};
 };
@@ -408,6 +420,9 @@ enum ArenaSlot {
   kSlotRowSel,      // selection bytes,
   kSlotRowSums,     // the device-side weight sums
   kSlotRowWork,     // and the two-pass work buffer
+  kSlotResampleWork,  // resampling around the boundary: FFT work images,
+  kSlotResampleOut,   // the image at the padded image size,
+  kSlotResampleTrim,  // and at the trimmed size
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.

@@ -150,6 +150,26 @@ class WGriddingGridder_Simple:
         check(lib().wgpu_gridder_real_image(self._h, ptr(out)))
         return out
 
+    def FinishInversion(self, image_width, image_height, trim_width, trim_height):
+        """After FinalizeImage: RealImage resampled from the gridder's size to
+        image_width x image_height (when different) and trimmed to
+        trim_width x trim_height, as WGriddingMSGridder::FinishInversion does
+        (wgriddingmsgridder.cpp:273-309); returns (trim_height, trim_width)."""
+        out = np.empty((trim_height, trim_width), np.float32)
+        check(lib().wgpu_gridder_finish_inversion(self._h, image_width, image_height, trim_width,
+                                                  trim_height, ptr(out)))
+        return out
+
+    def StartPredict(self, model, image_width, image_height):
+        """The (trim_height, trim_width) model untrimmed to image_width x
+        image_height, resampled to the gridder's size and set as the
+        prediction image, as WGriddingMSGridder::StartPredict does
+        (wgriddingmsgridder.cpp:311-340)."""
+        m = np.ascontiguousarray(model, np.float32)
+        th, tw = m.shape
+        check(lib().wgpu_gridder_start_predict(self._h, tw, th, image_width, image_height,
+                                               ptr(m)))
+
     def InitializePrediction(self, image_data):
         img = np.ascontiguousarray(image_data, dtype=np.float32).ravel()
         assert img.size == self.width * self.height
