@@ -16,7 +16,9 @@ TOL = 1e-5
 
 
 def rel(a, b):
-    return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
+    a = np.asarray(a)
+    a = a.astype(np.complex128) if np.iscomplexobj(a) else a.astype(np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
 SHAPES = [((48, 64), (60, 80)), ((90, 100), (50, 64)), ((45, 63), (33, 77)),
