@@ -44,6 +44,9 @@ WORKLOAD_TEXT = {
                "16 channels 120-180 MHz, 20 sources, eps 1e-4"),
     "plain1024": ("plain 1024x1024, 10arcsec pixels, 64 antennas in a 3 km disk, 2016 baselines "
                   "x 60 x 10 s, 16 channels 120-180 MHz, 20 sources, eps 1e-4"),
+    "resample": ("boundary resampling: an 8192x8192 image resampled to the 5120x5120 small-"
+                 "inversion size and back (FinishInversion / StartPredict resampler), FFT "
+                 "method, FP32"),
     "rowweights": ("raw-row weighting: the wide-field array and band, 32640 baselines x 75 x 8 s, "
                    "64 channels 0.9-1.7 GHz, 4 correlations (XX, XY, YX, YY) with visibility "
                    "weights, Briggs 0 imaging weights on the 8192x8192 3arcsec grid; "
@@ -864,6 +867,102 @@ def run_rowweights(args):
     }
 
 
+def run_resample(args):
+    """The boundary resampler: 8192^2 -> 5120^2 and 5120^2 -> 8192^2 per step,
+    device buffers (wgpu_resample_device), the host entry point for e2e, and
+    numpy's FFT restatement (the oracle) as the CPU baseline."""
+    import torch
+    from oracle import resample as ores
+    from wsclean_gb300 import _lib
+    from wsclean_gb300.resample import resample_device
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    big, small = 8192, 5120
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(3)
+    t_big = torch.randn((big, big), generator=gen, dtype=torch.float32, device=dev)
+    t_small = torch.empty((small, small), dtype=torch.float32, device=dev)
+    t_back = torch.empty((big, big), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        resample_device(t_big.data_ptr(), big, big, t_small.data_ptr(), small, small, sp)
+        resample_device(t_small.data_ptr(), small, small, t_back.data_ptr(), big, big, sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib_launches()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = _lib_launches() - l0
+    ms = start.elapsed_time(end) / args.steps
+    # accuracy against the FP64 numpy restatement on this image
+    h_big = t_big.cpu().numpy()
+    c0 = time.perf_counter()
+    ref_small = ores.resample(h_big, small, small)
+    cpu_s = time.perf_counter() - c0
+    rel_small = float(np.linalg.norm(t_small.cpu().numpy() - ref_small) / np.linalg.norm(ref_small))
+    # e2e through the host entry point (pinned host buffers)
+    from wsclean_gb300.resample import resample as resample_host
+    p_big = pinned_copy(t_big)
+    w0 = time.perf_counter()
+    out_small = resample_host(p_big.numpy(), small, small)
+    e2e_ms = (time.perf_counter() - w0) * 1e3
+    same = bool(np.array_equal(out_small, t_small.cpu().numpy()))
+    # one read and one write of the complex work image per transform pass
+    def fft_bytes(n_elems, n):
+        passes = 0
+        m = n
+        for r in (8, 4, 2, 3, 5, 7):
+            while m % r == 0:
+                passes += 1
+                m //= r
+        return passes * n_elems * 16
+    def leg_bytes(iw, ih, ow, oh):
+        return (iw * ih * 4 + fft_bytes(iw * ih, iw) + fft_bytes(ih * (iw // 2 + 1), ih) +
+                fft_bytes(oh * (ow // 2 + 1), oh) + fft_bytes(ow * oh, ow) + ow * oh * 4)
+    alg = leg_bytes(big, big, small, small) + leg_bytes(small, small, big, big)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg / (ms * 1e-3) / 1e9
+    pixels = 2 * big * big + 2 * small * small  # input + output pixels of both legs
+    return {
+        "metric": "Gpixels/s boundary resampling (FFT method, in + out pixels)",
+        "value": pixels / (ms * 1e-3) / 1e9, "unit": "Gpixels/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT["resample"], "sizes": [big, small],
+                   "l2": "work images (512 MB complex) larger than L2",
+                   "accuracy": {"rel_l2_vs_fp64_oracle": rel_small},
+                   "e2e_matches_device": same},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": "fft_stage_kernel (all passes)",
+                     "peak_source": peak_src,
+                     "bytes": "one read + one write of the complex work image per pass"},
+        "cpu_baseline": {"value": (big * big + small * small) / cpu_s / 1e9,
+                         "unit": "Gpixels/s", "cores": 1, "kind": "port",
+                         "sample": "8192^2 -> 5120^2, numpy FFT (FP64) restatement"},
+        "clocks": clk,
+        "e2e": {"value": (big * big + small * small) / (e2e_ms * 1e-3) / 1e9, "unit": "Gpixels/s",
+                "h2d_bytes_per_step": big * big * 4, "d2h_bytes_per_step": small * small * 4,
+                "note": "one leg (8192^2 -> 5120^2) through wgpu_resample"},
+        "gpu_launches": int(launches),
+    }
+
+
 def _lib_launches():
     from wsclean_gb300 import _lib
     return _lib.lib().wgpu_kernel_launch_count()
@@ -989,8 +1088,8 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
-    if args.impl == "reference" and args.workload == "rowweights":
-        print(json.dumps({"impl": "reference", "unavailable": "the raw-row weighting has no "
+    if args.impl == "reference" and args.workload in ("rowweights", "resample"):
+        print(json.dumps({"impl": "reference", "unavailable": "this workload has no "
                           "reference arm; its CPU baseline is the cpu_baseline key"}), flush=True)
         return
     if args.impl == "reference":
@@ -1005,6 +1104,9 @@ def main():
         return
     if args.workload == "rowweights":
         print(json.dumps(run_rowweights(args)), flush=True)
+        return
+    if args.workload == "resample":
+        print(json.dumps(run_resample(args)), flush=True)
         return
     if args.serve_only:
         import torch
