@@ -855,7 +855,8 @@ def run_rowweights(args):
                    "weight_sums": sums, "datagen_s": round(gen_s, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "prepare_rows_kernel<4>", "peak_source": peak_src,
+                     "kernel": "prepare_rows_fast_kernel<4, true> + exact pass",
+                     "peak_source": peak_src,
                      "bytes_per_sample": 64},
         "cpu_baseline": {"value": cpu_value, "unit": "Gsamples/s", "cores": 1, "kind": "port",
                          "sample": f"first {n_s} rows x {n_chan} channels x 4 correlations, "
