@@ -613,6 +613,25 @@ int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *gridder, const wgpu_imagewei
                                     const float *weights, const float *model,
                                     const uint8_t *selected, wgpu_weight_sums_t *sums);
 
+/* GetCollapsedVisibilities with h5parm corrections followed by
+ * AddInversionData (ApplyWeightsAndCorrections, msgridderdata.h:888-927,
+ * through VisibilityModifier::ApplyConjugatedParmResponse,
+ * visibilitymodifier.h:538-594): each raw row is weighted as in
+ * wgpu_prepare_rows, the conjugated gains of its antennas are applied to its
+ * correlations before ApplyWeights, and it is collapsed and gridded, all on
+ * the device.  mode / n_pol, antenna_pairs, time_offsets and the solution
+ * table as in wgpu_gridder_add_inversion_data_corrected.  correction_sum
+ * (TRACE only; NULL otherwise) accumulates the scalar AverageCorrection sum
+ * |g|^2 w iw (averagecorrection.h:36-50); the matrix-valued sums of the other
+ * modes are not provided. */
+int wgpu_gridder_add_inversion_rows_corrected(
+    wgpu_gridder_t *gridder, const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw,
+    int mode, size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,
+    const double *freq, const float *vis, const float *weights, const float *model,
+    const uint8_t *selected, const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+    const float *solutions, size_t nparms, size_t n_times, size_t n_ant,
+    wgpu_weight_sums_t *sums, double *correction_sum);
+
 /* ---- Resampling and trimming around the boundary -------------------------
  * WGriddingMSGridder::FinishInversion / StartPredict
  * (wgridder/wgriddingmsgridder.cpp:273-340) move the image between the padded

@@ -88,6 +88,9 @@ def lib():
         L.oracle_weights_sample.argtypes = [P, I64, I64, D, D, SZ, P, P, P]
         L.oracle_prepare_rows.argtypes = [P, I64, I64, D, D, I, D, D, I, I, I, SZ, SZ, SZ, P, P,
                                           P, P, P, P, P, P, P, P]
+        L.oracle_prepare_rows_corrected.argtypes = [P, I64, I64, D, D, I, D, D, I, I, I, SZ, SZ,
+                                                    SZ, P, P, P, P, P, P, P, P, P, P, I, P, P, P,
+                                                    SZ, SZ, P]
         _lib = L
     return _lib
 
@@ -301,10 +304,13 @@ class ImageWeights:
 
     def prepare_rows(self, uvw, freq, weights, vis=None, model=None, selected=None,
                      psf_mode=0, psf_dl=0.0, psf_dm=0.0, visibility_weighting=0,
-                     polarization=0):
+                     polarization=0, gains=None):
         """CalculateWeights + ApplyWeights + CollapseData over [row][chan][pol]
         inputs; returns (vis_out [row, chan], weights_out [row, chan, pol],
-        imaging weights [row, chan], sums [vws, max, total, count])."""
+        imaging weights [row, chan], sums [vws, max, total, count]).  gains =
+        (mode, antenna_pairs, time_offsets, solutions, nparms, n_ant) applies
+        the conjugated gains before ApplyWeights; the TRACE correction sum is
+        then sums[4]."""
         uvw = np.ascontiguousarray(uvw, np.float64)
         freq = np.ascontiguousarray(freq, np.float64)
         wts = np.ascontiguousarray(weights, np.float32)
@@ -315,12 +321,22 @@ class ImageWeights:
         vis_out = np.zeros((n_rows, n_chan), np.complex64)
         w_out = np.zeros((n_rows, n_chan, n_pol), np.float32)
         iw_out = np.zeros((n_rows, n_chan), np.float32)
-        sums = np.zeros(4, np.float64)
-        lib().oracle_prepare_rows(
-            _p(self.grid), self.width, self.height, self.psx, self.psy, int(psf_mode),
-            float(psf_dl), float(psf_dm), int(mod_a is not None), int(visibility_weighting),
-            int(polarization), n_pol, n_rows, n_chan, _p(uvw), _p(freq),
-            None if vis_a is None else _p(vis_a), _p(wts), None if mod_a is None else _p(mod_a),
-            None if sel_a is None else _p(sel_a), _p(vis_out), _p(w_out), _p(iw_out),
-            _p(sums))
+        sums = np.zeros(5, np.float64)
+        args = (_p(self.grid), self.width, self.height, self.psx, self.psy, int(psf_mode),
+                float(psf_dl), float(psf_dm), int(mod_a is not None), int(visibility_weighting),
+                int(polarization), n_pol, n_rows, n_chan, _p(uvw), _p(freq),
+                None if vis_a is None else _p(vis_a), _p(wts),
+                None if mod_a is None else _p(mod_a), None if sel_a is None else _p(sel_a),
+                _p(vis_out), _p(w_out), _p(iw_out), _p(sums))
+        if gains is None:
+            lib().oracle_prepare_rows(*args)
+            return vis_out, w_out, iw_out, sums[:4]
+        mode, ant, tof, sol, nparms, n_ant = gains
+        ant = np.ascontiguousarray(ant, np.uint64)
+        tof = np.ascontiguousarray(tof, np.uint64)
+        sol = np.ascontiguousarray(sol, np.complex64)
+        corr = np.zeros(1, np.float64)
+        lib().oracle_prepare_rows_corrected(*args, int(mode), _p(ant), _p(tof), _p(sol), nparms,
+                                            n_ant, _p(corr))
+        sums[4] = corr[0]
         return vis_out, w_out, iw_out, sums

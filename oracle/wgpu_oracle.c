@@ -1242,13 +1242,19 @@ void oracle_weights_sample(const double *grid, int64_t W, int64_t H, double psx,
   }
 }
 
-void oracle_prepare_rows(const double *grid, int64_t W, int64_t H, double psx, double psy,
-                         int psf_mode, double psf_dl, double psf_dm, int subtract_model,
-                         int visibility_weighting, int polarization, size_t n_pol,
-                         size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
-                         const float *vis, const float *weights, const float *model,
-                         const uint8_t *selected, float *vis_out, float *weights_out,
-                         float *imaging_out, double *sums) {
+/* With a gain table (sol != NULL): ApplyConjugatedParmResponse between the
+ * weighting and ApplyWeights (msgridderdata.h:888-927,
+ * visibilitymodifier.h:538-594), and for TRACE the scalar AverageCorrection
+ * sum (averagecorrection.h:36-50) into *corr. */
+static void prepare_rows_impl(const double *grid, int64_t W, int64_t H, double psx, double psy,
+                              int psf_mode, double psf_dl, double psf_dm, int subtract_model,
+                              int visibility_weighting, int polarization, size_t n_pol,
+                              size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+                              const float *vis, const float *weights, const float *model,
+                              const uint8_t *selected, float *vis_out, float *weights_out,
+                              float *imaging_out, double *sums, int mode,
+                              const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+                              const float *solutions, size_t nparms, size_t n_ant, double *corr) {
   float *row = (float *)malloc(sizeof(float) * 2 * n_chan * n_pol);
   float *wrow = (float *)malloc(sizeof(float) * n_chan * n_pol);
   float *scratch_iw = (float *)malloc(sizeof(float) * n_chan);
@@ -1294,6 +1300,27 @@ void oracle_prepare_rows(const double *grid, int64_t W, int64_t H, double psx, d
                             (const double[]){ruvw[1] / lambda}, &w);
       scratch_iw[ch] = (float)w;
     }
+    if (solutions) /* ApplyCorrections, visibilitymodifier.h:538-594 */
+      for (size_t ch = 0; ch < n_chan; ++ch) {
+        const size_t off = (time_offsets[r] * n_chan + ch) * n_ant * nparms;
+        const float *s1 = solutions + 2 * (off + antenna_pairs[2 * r] * nparms);
+        const float *s2 = solutions + 2 * (off + antenna_pairs[2 * r + 1] * nparms);
+        float g1[8] = {0}, g2[8] = {0};
+        if (nparms == 2) {
+          g1[0] = s1[0]; g1[1] = s1[1]; g1[6] = s1[2]; g1[7] = s1[3];
+          g2[0] = s2[0]; g2[1] = s2[1]; g2[6] = s2[2]; g2[7] = s2[3];
+        } else {
+          memcpy(g1, s1, sizeof(float) * 8);
+          memcpy(g2, s2, sizeof(float) * 8);
+        }
+        oracle_apply_conjugated_gain(mode, row + 2 * ch * n_pol, g1, g2);
+        if (mode == 2) { /* AverageCorrection::Add, scalar (kTrace) */
+          const cf a = cmul(ld(g2, 0), cconj(ld(g1, 0))), b = cmul(ld(g2, 3), cconj(ld(g1, 3)));
+          const cf g = {0.5f * (a.re + b.re), 0.5f * (a.im + b.im)};
+          const float norm = g.re * g.re + g.im * g.im;
+          *corr += norm * (wrow[ch * n_pol] * scratch_iw[ch]);
+        }
+      }
     for (size_t ch = 0; ch < n_chan; ++ch) /* ApplyWeights, :760-789 */
       for (size_t p = 0; p < n_pol; ++p) {
         const size_t i = ch * n_pol + p;
@@ -1326,4 +1353,33 @@ void oracle_prepare_rows(const double *grid, int64_t W, int64_t H, double psx, d
   free(row);
   free(wrow);
   free(scratch_iw);
+}
+
+void oracle_prepare_rows(const double *grid, int64_t W, int64_t H, double psx, double psy,
+                         int psf_mode, double psf_dl, double psf_dm, int subtract_model,
+                         int visibility_weighting, int polarization, size_t n_pol,
+                         size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+                         const float *vis, const float *weights, const float *model,
+                         const uint8_t *selected, float *vis_out, float *weights_out,
+                         float *imaging_out, double *sums) {
+  prepare_rows_impl(grid, W, H, psx, psy, psf_mode, psf_dl, psf_dm, subtract_model,
+                    visibility_weighting, polarization, n_pol, n_rows, n_chan, uvw, freq, vis,
+                    weights, model, selected, vis_out, weights_out, imaging_out, sums, 0, NULL,
+                    NULL, NULL, 2, 0, NULL);
+}
+
+void oracle_prepare_rows_corrected(const double *grid, int64_t W, int64_t H, double psx,
+                                   double psy, int psf_mode, double psf_dl, double psf_dm,
+                                   int subtract_model, int visibility_weighting, int polarization,
+                                   size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,
+                                   const double *freq, const float *vis, const float *weights,
+                                   const float *model, const uint8_t *selected, float *vis_out,
+                                   float *weights_out, float *imaging_out, double *sums, int mode,
+                                   const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+                                   const float *solutions, size_t nparms, size_t n_ant,
+                                   double *correction_sum) {
+  prepare_rows_impl(grid, W, H, psx, psy, psf_mode, psf_dl, psf_dm, subtract_model,
+                    visibility_weighting, polarization, n_pol, n_rows, n_chan, uvw, freq, vis,
+                    weights, model, selected, vis_out, weights_out, imaging_out, sums, mode,
+                    antenna_pairs, time_offsets, solutions, nparms, n_ant, correction_sum);
 }

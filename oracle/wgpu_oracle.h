@@ -174,6 +174,23 @@ void oracle_prepare_rows(const double *grid, int64_t width, int64_t height, doub
                          const float *model, const uint8_t *selected, float *vis_out,
                          float *weights_out, float *imaging_out, double *sums);
 
+/* The same with h5parm corrections: the conjugated gains of each row's
+ * antennas applied to its correlations between the weighting and
+ * ApplyWeights (msgridderdata.h:888-927, visibilitymodifier.h:538-594);
+ * layouts as oracle_apply_gains.  For TRACE (mode 2) *correction_sum +=
+ * |g|^2 w iw with g = (g2[0] conj(g1[0]) + g2[3] conj(g1[3])) / 2
+ * (averagecorrection.h:36-50, 104-118). */
+void oracle_prepare_rows_corrected(const double *grid, int64_t width, int64_t height, double psx,
+                                   double psy, int psf_mode, double psf_dl, double psf_dm,
+                                   int subtract_model, int visibility_weighting, int polarization,
+                                   size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,
+                                   const double *freq, const float *vis, const float *weights,
+                                   const float *model, const uint8_t *selected, float *vis_out,
+                                   float *weights_out, float *imaging_out, double *sums, int mode,
+                                   const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+                                   const float *solutions, size_t nparms, size_t n_ant,
+                                   double *correction_sum);
+
 #ifdef __cplusplus
 }
 #endif

@@ -281,3 +281,69 @@ def test_cells_exact_on_and_near_cell_edges(oracle_lib):
     for g, e in zip(got[:3], exp[:3]):
         np.testing.assert_array_equal(g, e)
     assert got[3]["gridded_visibility_count"] == exp[3][3] > 0
+
+
+@pytest.mark.parametrize("mode,n_pol,nparms", [(0, 1, 2), (1, 1, 4), (2, 1, 4), (3, 2, 2),
+                                               (4, 4, 4)])
+def test_add_inversion_rows_corrected_matches_oracle(oracle_lib, mode, n_pol, nparms):
+    """Raw rows with h5parm gains: weighting, conjugated gains before
+    ApplyWeights, collapse and gridding on the device give the image of the
+    oracle-prepared rows (gains in FP32 with fused multiply-adds: 1e-5), and
+    the TRACE correction sum matches the oracle's."""
+    from wsclean_gb300.weights import add_inversion_rows_corrected
+    W, Wt, dl, eps = 160, 128, 4e-4, 1e-5
+    uvw, freq, vis1 = synthetic.random_points(700, 5, Wt, dl, seed=51, w_scale=2.0)
+    rng = np.random.default_rng(52 + mode)
+    n_rows, n_chan, n_ant, n_t = uvw.shape[0], freq.size, 7, 3
+    vis = (np.repeat(vis1[:, :, None], n_pol, axis=2) *
+           (1.0 + 0.2 * rng.standard_normal((n_rows, n_chan, n_pol)))).astype(np.complex64)
+    weights = rng.uniform(0.2, 2.0, vis.shape).astype(np.float32)
+    sel = rng.random((n_rows, n_chan)) > 0.1
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)], axis=1)
+    tof = rng.integers(0, n_t, n_rows).astype(np.uint64)
+    sol = (1.0 + 0.3 * (rng.standard_normal((n_t, n_chan, n_ant, nparms)) +
+                        1j * rng.standard_normal((n_t, n_chan, n_ant, nparms)))).astype(
+        np.complex64)
+    args = (UNIFORM, Wt, Wt, dl, dl, False, 1.0, 0.0)
+    dev, ref = ImageWeights(*args), oracle_lib.ImageWeights(*args)
+    dev.Grid(uvw, freq, weights)
+    dev.FinishGridding()
+    ref.grid[:] = dev.half_grid()
+    full = np.zeros((n_t, n_chan, n_ant, 4), np.complex64)
+    if nparms == 2:
+        full[..., 0], full[..., 3] = sol[..., 0], sol[..., 1]
+    else:
+        full[:] = sol
+    prepared, _, _, sums = ref.prepare_rows(uvw, freq, weights, vis, None, sel, 0, 0.0, 0.0, 0,
+                                            _lib.POL_I, gains=(mode, ant, tof, full, 4, n_ant))
+
+    g1 = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps,
+                                 num_t=np.float64)
+    g1.InitializeInversion()
+    acc, corr = add_inversion_rows_corrected(g1, dev, mode, uvw, freq, weights, vis, ant, tof,
+                                             sol, nparms, n_t, n_ant, selected=sel,
+                                             with_correction_sum=(mode == 2))
+    g1.FinalizeImage(1.0)
+    a = g1.RealImage().reshape(W, W)
+    g2 = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps,
+                                 num_t=np.float64)
+    g2.InitializeInversion()
+    g2.AddInversionData(n_rows, n_chan, uvw, freq, prepared)
+    g2.FinalizeImage(1.0)
+    b = g2.RealImage().reshape(W, W)
+    d = (W - Wt) // 2
+    a, b = a[d:d + Wt, d:d + Wt].astype(np.float64), b[d:d + Wt, d:d + Wt].astype(np.float64)
+    assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    assert acc.gridded_visibility_count == sums[3] > 0
+    np.testing.assert_allclose(acc.total_weight, sums[2], rtol=1e-12)
+    if mode == 2:
+        assert corr > 0
+        np.testing.assert_allclose(corr, sums[4], rtol=1e-5)
+    # an antenna index outside the table is reported
+    bad = ant.copy()
+    bad[3, 0] = n_ant
+    g3 = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps)
+    g3.InitializeInversion()
+    with pytest.raises(_lib.WgpuError):
+        add_inversion_rows_corrected(g3, dev, mode, uvw, freq, weights, vis, bad, tof, sol,
+                                     nparms, n_t, n_ant)

@@ -326,3 +326,31 @@ def test_prepare_rows_match_restatement(oracle_lib, case):
         np.testing.assert_array_equal(g, e)
     np.testing.assert_array_equal(got[3], exp[3])
     assert exp[3][3] > 0 and np.count_nonzero(got[0]) > 0
+
+
+@pytest.mark.parametrize("mode,n_pol,pol", [(0, 1, 0), (1, 1, 0), (2, 1, 0), (3, 2, 0), (4, 4, 0),
+                                            (4, 4, 3)])
+def test_prepare_rows_corrected_composition(oracle_lib, mode, n_pol, pol):
+    """Gains applied between weighting and ApplyWeights: identity gains leave
+    the rows as they are; a real gain of 2 on both antennas (conj(2) V 2 = 4 V,
+    exact in float) scales every prepared value by exactly 4, and the TRACE
+    correction sum is |(2*2 + 2*2) / 2|^2 = 16 times the sum of w[0] * iw."""
+    iw, _ = oracle_weights(oracle_lib, 1)
+    iw.finish()
+    uvw, freq, weights, vis = rows(21, n_rows=25, n_pol=n_pol)
+    n_rows, n_chan, n_ant = uvw.shape[0], freq.size, 5
+    ant = np.stack([np.arange(n_rows) % n_ant, (np.arange(n_rows) + 2) % n_ant], axis=1)
+    tof = np.zeros(n_rows, np.uint64)
+    base = iw.prepare_rows(uvw, freq, weights, vis, None, None, 0, 0.0, 0.0, 0, pol)
+    for value, factor in ((1.0, 1.0), (2.0, 4.0)):
+        sol = np.zeros((1, n_chan, n_ant, 4), np.complex64)
+        sol[..., 0] = value
+        sol[..., 3] = value
+        got = iw.prepare_rows(uvw, freq, weights, vis, None, None, 0, 0.0, 0.0, 0, pol,
+                              gains=(mode, ant, tof, sol, 4, n_ant))
+        np.testing.assert_array_equal(got[0], base[0] * np.float32(factor))
+        np.testing.assert_array_equal(got[1], base[1])
+        np.testing.assert_array_equal(got[3][:4], base[3])
+        if mode == 2:
+            w0 = base[1][:, :, 0].astype(np.float64)  # w[0] * iw
+            np.testing.assert_allclose(got[3][4], factor * factor * w0.sum(), rtol=1e-12)

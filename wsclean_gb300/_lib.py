@@ -184,6 +184,9 @@ _PROTOS = {
                               P, C.POINTER(WeightSums)]),
     "wgpu_prepare_rows_device": (I, [P, C.POINTER(RowWeighting), SZ, SZ, SZ, P, P, P, P, P, P,
                                      P, P, P, C.POINTER(WeightSums)]),
+    "wgpu_gridder_add_inversion_rows_corrected": (
+        I, [P, P, C.POINTER(RowWeighting), I, SZ, SZ, SZ, P, P, P, P, P, P, P, P, P, SZ, SZ, SZ,
+            C.POINTER(WeightSums), C.POINTER(D)]),
     "wgpu_calculate_fft_size": (I, [SZ, D, D, C.POINTER(SZ), C.POINTER(SZ)]),
     "wgpu_small_inversion_size": (I, [SZ, SZ, D, D, D, C.POINTER(SZ), C.POINTER(SZ),
                                       C.POINTER(D), C.POINTER(D)]),

@@ -928,6 +928,75 @@ int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *g, const wgpu_imageweights_t
   });
 }
 
+int wgpu_gridder_add_inversion_rows_corrected(
+    wgpu_gridder_t *g, const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw, int mode,
+    size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw, const double *freq,
+    const float *vis, const float *weights, const float *model, const uint8_t *selected,
+    const uint64_t *antenna_pairs, const uint64_t *time_offsets, const float *solutions,
+    size_t nparms, size_t n_times, size_t n_ant, wgpu_weight_sums_t *sums,
+    double *correction_sum) {
+  if (!g || !iw || !rw) return fail(WGPU_ERR_INVALID, "null argument");
+  if (rw->psf_mode < WGPU_PSF_NONE || rw->psf_mode > WGPU_PSF_DIRECTION_DEPENDENT ||
+      rw->visibility_weighting < WGPU_VISW_NORMAL || rw->visibility_weighting > WGPU_VISW_UNIT ||
+      rw->polarization < 0 || rw->polarization > 7)
+    return fail(WGPU_ERR_INVALID, "invalid row weighting");
+  if (mode < WGPU_GAIN_XX || mode > WGPU_GAIN_FULL)
+    return fail(WGPU_ERR_INVALID, "invalid gain mode");
+  const size_t want = mode == WGPU_GAIN_FULL ? 4 : mode == WGPU_GAIN_2VIS_DIAGONAL ? 2 : 1;
+  if (n_pol != want) return fail(WGPU_ERR_INVALID, "gain mode and n_polarizations do not match");
+  if (nparms != 2 && nparms != 4) return fail(WGPU_ERR_INVALID, "nparms must be 2 or 4");
+  if (correction_sum && mode != WGPU_GAIN_TRACE)
+    return fail(WGPU_ERR_INVALID,
+                "correction sums are available for the TRACE gain mode only (scalar "
+                "AverageCorrection)");
+  if (n_rows && n_chan &&
+      (!uvw || !freq || !weights || (rw->psf_mode == WGPU_PSF_NONE && !vis) ||
+       (rw->subtract_model && !model) || !antenna_pairs || !time_offsets || !solutions))
+    return fail(WGPU_ERR_INVALID, "null data pointer");
+  return guarded([&] {
+    if (g->mode != wgpu_gridder::Mode::kInversion)
+      throw Error(WGPU_ERR_STATE, "AddInversionData before InitializeInversion");
+    if (n_rows == 0 || n_chan == 0) return;
+    const size_t n = n_rows * n_chan, nc = n * n_pol;
+    const double *du = upload(g, kSlotUvw, uvw, 3 * n_rows);
+    const double *df = upload(g, kSlotFreq, freq, n_chan);
+    const float *dw = upload(g, kSlotRowWeights, weights, nc);
+    const float2 *dv =
+        rw->psf_mode == WGPU_PSF_NONE ? (const float2 *)upload(g, kSlotGainVis, vis, 2 * nc)
+                                      : nullptr;
+    const float2 *dm =
+        rw->subtract_model ? (const float2 *)upload(g, kSlotRowModel, model, 2 * nc) : nullptr;
+    const uint8_t *ds = selected ? upload(g, kSlotRowSel, selected, n) : nullptr;
+    GainTable gt;
+    gt.ant = upload(g, kSlotAnt, antenna_pairs, 2 * n_rows);
+    gt.tof = upload(g, kSlotTimes, time_offsets, n_rows);
+    gt.sol = (const float2 *)upload(g, kSlotSol, solutions, 2 * n_times * n_chan * n_ant * nparms);
+    gt.nparms = (int)nparms;
+    gt.mode = mode;
+    gt.n_times = (int64_t)n_times;
+    gt.n_ant = (int64_t)n_ant;
+    gt.err = (int *)g->arena.get(kSlotOutVis, sizeof(int) * 4);
+    float2 *dc = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n);
+    auto *dsum = (WeightSumsDev *)g->arena.get(kSlotRowSums, sizeof(WeightSumsDev));
+    void *work = g->arena.get(kSlotRowWork, pass_work_bytes((int64_t)n_rows, (int64_t)n_chan));
+    const WeightGridView view = imageweights_view(iw);
+    WGPU_CUDA(cudaMemsetAsync(dsum, 0, sizeof(WeightSumsDev), g->stream));
+    WGPU_CUDA(cudaMemsetAsync(gt.err, 0, sizeof(int), g->stream));
+    launch_prepare_rows(view, row_weighting(*rw), (int)n_pol, (int64_t)n_rows, (int64_t)n_chan,
+                        du, df, dv, dw, dm, ds, dc, nullptr, nullptr, dsum, work, g->stream, &gt);
+    WeightSumsDev hs;
+    int herr = 0;
+    WGPU_CUDA(cudaMemcpyAsync(&hs, dsum, sizeof(hs), cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaMemcpyAsync(&herr, gt.err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    if (herr) throw Error(WGPU_ERR_INVALID, "antenna index or time offset outside the solution table");
+    invert_device(g, n_rows, n_chan, du, df, (const float *)dc);
+    WGPU_CUDA(cudaStreamSynchronize(g->stream));
+    add_weight_sums(hs, sums);
+    if (correction_sum) *correction_sum += hs.correction;
+  });
+}
+
 int wgpu_gridder_add_inversion_data_corrected(
     wgpu_gridder_t *g, int mode, size_t n_pol, size_t n_rows, const double *uvw,
     const double *freq, size_t n_chan, const uint64_t *antenna_pairs,

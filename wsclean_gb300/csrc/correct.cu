@@ -73,21 +73,6 @@ __global__ void unpermute_predict_kernel(const VisRecord *rec, const uint32_t *p
 }
 
 // ---- K7: conjugated gains (visibilitymodifier.h:378-401) + collapse -------
-// r = a^H b (row-major 2x2)
-__device__ __forceinline__ void herm_mul(const float2 *a, const float2 *b, float2 *r) {
-  const float2 h[4] = {cj(a[0]), cj(a[2]), cj(a[1]), cj(a[3])};
-  r[0] = ca(cm(h[0], b[0]), cm(h[1], b[2]));
-  r[1] = ca(cm(h[0], b[1]), cm(h[1], b[3]));
-  r[2] = ca(cm(h[2], b[0]), cm(h[3], b[2]));
-  r[3] = ca(cm(h[2], b[1]), cm(h[3], b[3]));
-}
-__device__ __forceinline__ void mat_mul(const float2 *a, const float2 *b, float2 *r) {
-  r[0] = ca(cm(a[0], b[0]), cm(a[1], b[2]));
-  r[1] = ca(cm(a[0], b[1]), cm(a[1], b[3]));
-  r[2] = ca(cm(a[2], b[0]), cm(a[3], b[2]));
-  r[3] = ca(cm(a[2], b[1]), cm(a[3], b[3]));
-}
-
 __global__ void apply_gains_kernel(int mode, int n_pol, int64_t n_rows,
                                    int64_t n_chan, const float2 *vis_in,
                                    const uint64_t *ant_pairs,

@@ -490,7 +490,7 @@ __global__ void weight_sample_kernel(const double *grid, int64_t W, int64_t H, d
 // The streamed inputs are read with evict-first loads so that L2 keeps the
 // imaging-weight table; VEC selects 8- / 16-byte accesses (aligned buffers).
 struct PrepAcc {
-  FloatSum vws, total;
+  FloatSum vws, total, corr;
   float vmax = 0.0f;
   uint32_t count = 0;
 };
@@ -524,13 +524,48 @@ __device__ __forceinline__ void load_vis(const float2 *p, float2 *v) {
   }
 }
 
-template <int NPOL, bool VEC>
-__device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, uint32_t r,
+// With CORR the conjugated gains of the row's antennas are applied between
+// the weighting and ApplyWeights (ApplyWeightsAndCorrections,
+// msgridderdata.h:888-927, through VisibilityModifier::
+// ApplyConjugatedParmResponse, visibilitymodifier.h:538-594), and for TRACE
+// the correction sum |g|^2 w iw of AverageCorrection::Add
+// (averagecorrection.h:36-50, g = (g2[0] conj(g1[0]) + g2[3] conj(g1[3])) / 2)
+// is accumulated.  A row whose antenna or time index is outside the solution
+// table sets the error flag and contributes nothing.
+template <int NPOL, bool VEC, bool CORR>
+__device__ __forceinline__ void prep_sample(const RowWeighting &rw, const GainTable &gt,
+                                            uint32_t e, uint32_t r, uint32_t ch, uint32_t n_chan,
                                             float iw, double lambda, const double *uvw,
                                             const float2 *vis, const float *weights,
                                             const float2 *model, const uint8_t *selected,
                                             float2 *vis_out, float *weights_out,
                                             float *imaging_out, PrepAcc &acc) {
+  float2 g1[4], g2[4];
+  if constexpr (CORR) {
+    const uint64_t a1 = gt.ant[2 * (size_t)r], a2 = gt.ant[2 * (size_t)r + 1];
+    const uint64_t t = gt.tof[r];
+    if (a1 >= (uint64_t)gt.n_ant || a2 >= (uint64_t)gt.n_ant || t >= (uint64_t)gt.n_times) {
+      atomicOr(gt.err, 1);
+      __stcs(vis_out + e, make_float2(0.0f, 0.0f));
+      if (weights_out)
+        for (int p = 0; p < NPOL; ++p) __stcs(weights_out + (size_t)e * NPOL + p, 0.0f);
+      if (imaging_out) __stcs(imaging_out + e, iw);
+      return;
+    }
+    const size_t off = (((size_t)t * n_chan + ch) * (size_t)gt.n_ant) * (size_t)gt.nparms;
+    if (gt.nparms == 2) {
+      g1[0] = gt.sol[off + a1 * 2]; g1[1] = g1[2] = make_float2(0.f, 0.f);
+      g1[3] = gt.sol[off + a1 * 2 + 1];
+      g2[0] = gt.sol[off + a2 * 2]; g2[1] = g2[2] = make_float2(0.f, 0.f);
+      g2[3] = gt.sol[off + a2 * 2 + 1];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        g1[k] = gt.sol[off + a1 * 4 + k];
+        g2[k] = gt.sol[off + a2 * 4 + k];
+      }
+    }
+  }
   float w[NPOL];
   float2 v[NPOL];
   load_weights<NPOL, VEC>(weights + (size_t)e * NPOL, w);
@@ -561,7 +596,6 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, 
     for (int p = 0; p < NPOL; ++p) v[p] = make_float2(v[p].x - m[p].x, v[p].y - m[p].y);
   }
   const bool sel = selected == nullptr || selected[e] != 0;
-  float2 c[NPOL];
 #pragma unroll
   for (int p = 0; p < NPOL; ++p) {
     float wp = sel ? w[p] : 0.0f;
@@ -569,6 +603,20 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, uint32_t e, 
       wp = __fmul_rn(wp, wp);
     else if (rw.visibility_weighting == WGPU_VISW_UNIT && wp != 0.0f)
       wp = 1.0f;
+    w[p] = wp;
+  }
+  if constexpr (CORR) {
+    apply_conjugated_gain<NPOL>(gt.mode, v, g1, g2);
+    if (gt.mode == WGPU_GAIN_TRACE) {
+      const float2 a = cm(g2[0], cj(g1[0])), b = cm(g2[3], cj(g1[3]));
+      const float2 g = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+      acc.corr.add(__fmul_rn(g.x * g.x + g.y * g.y, __fmul_rn(w[0], iw)));
+    }
+  }
+  float2 c[NPOL];
+#pragma unroll
+  for (int p = 0; p < NPOL; ++p) {
+    const float wp = w[p];
     const float cum = __fmul_rn(wp, iw);
     const bool has = cum != 0.0f;
     if (p == 0) {
@@ -605,6 +653,7 @@ __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
   const double s_vws = block_sum(acc.vws.value());
   const double s_total = block_sum(acc.total.value());
   const double s_count = block_sum((double)acc.count);
+  const double s_corr = block_sum(acc.corr.value());
   __shared__ float wmax[kThreads / 32];
   float m = acc.vmax;
 #pragma unroll
@@ -617,6 +666,7 @@ __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
     if (s_vws != 0.0) atomicAdd(&sums->visibility_weight_sum, s_vws);
     if (s_total != 0.0) atomicAdd(&sums->total_weight, s_total);
     if (s_count != 0.0) atomicAdd(&sums->count, (unsigned long long)s_count);
+    if (s_corr != 0.0) atomicAdd(&sums->correction, s_corr);
     // positive doubles order like their bit patterns
     if (bm > 0.0f)
       atomicMax(&sums->max_bits, (unsigned long long)__double_as_longlong((double)bm));
@@ -625,12 +675,12 @@ __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
 
 // First pass over a fixed grid of blocks: samples whose imaging-weight cell is
 // decided in FP32 are prepared; the others go to the pending list.
-template <int NPOL, bool VEC>
+template <int NPOL, bool VEC, bool CORR>
 __global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
-    WeightGridView g, RowWeighting rw, uint32_t n, uint32_t n_chan, const double *uvw,
-    const ChanScale *cs, const float2 *vis, const float *weights, const float2 *model,
-    const uint8_t *selected, float2 *vis_out, float *weights_out, float *imaging_out,
-    WeightSumsDev *sums, Pending pend) {
+    WeightGridView g, RowWeighting rw, GainTable gt, uint32_t n, uint32_t n_chan,
+    const double *uvw, const ChanScale *cs, const float2 *vis, const float *weights,
+    const float2 *model, const uint8_t *selected, float2 *vis_out, float *weights_out,
+    float *imaging_out, WeightSumsDev *sums, Pending pend) {
   __shared__ uint32_t s_count;
   if (threadIdx.x == 0) s_count = 0;
   __syncthreads();
@@ -646,8 +696,9 @@ __global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
                                      g.height);
       undecided = cell == -2;
       if (!undecided)
-        prep_sample<NPOL, VEC>(rw, e, r, cell >= 0 ? g.gridf[cell] : 0.0f, c.lambda, uvw, vis,
-                               weights, model, selected, vis_out, weights_out, imaging_out, acc);
+        prep_sample<NPOL, VEC, CORR>(rw, gt, e, r, ch, n_chan, cell >= 0 ? g.gridf[cell] : 0.0f,
+                                     c.lambda, uvw, vis, weights, model, selected, vis_out,
+                                     weights_out, imaging_out, acc);
     }
     pending_push(pend, &s_count, undecided, e);
   }
@@ -657,11 +708,12 @@ __global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
 
 // Second pass over the pending samples, with the cell of GetWeight(u, v)
 // computed in double as on the host.
-template <int NPOL, bool VEC>
+template <int NPOL, bool VEC, bool CORR>
 __global__ void __launch_bounds__(kThreads) prepare_rows_exact_kernel(
-    WeightGridView g, RowWeighting rw, uint32_t n_chan, const double *uvw, const ChanScale *cs,
-    const float2 *vis, const float *weights, const float2 *model, const uint8_t *selected,
-    float2 *vis_out, float *weights_out, float *imaging_out, WeightSumsDev *sums, Pending pend) {
+    WeightGridView g, RowWeighting rw, GainTable gt, uint32_t n_chan, const double *uvw,
+    const ChanScale *cs, const float2 *vis, const float *weights, const float2 *model,
+    const uint8_t *selected, float2 *vis_out, float *weights_out, float *imaging_out,
+    WeightSumsDev *sums, Pending pend) {
   const uint32_t count = pend.counts[blockIdx.x];
   const uint32_t *list = pend.idx + (size_t)blockIdx.x * pend.cap;
   PrepAcc acc;
@@ -671,8 +723,9 @@ __global__ void __launch_bounds__(kThreads) prepare_rows_exact_kernel(
     const double lambda = cs[ch].lambda;
     const int64_t cell = uv_cell(uvw[3 * (size_t)r] / lambda, uvw[3 * (size_t)r + 1] / lambda,
                                  g.width, g.height, g.psx, g.psy);
-    prep_sample<NPOL, VEC>(rw, e, r, cell >= 0 ? g.gridf[cell] : 0.0f, lambda, uvw, vis, weights,
-                           model, selected, vis_out, weights_out, imaging_out, acc);
+    prep_sample<NPOL, VEC, CORR>(rw, gt, e, r, ch, n_chan, cell >= 0 ? g.gridf[cell] : 0.0f,
+                                 lambda, uvw, vis, weights, model, selected, vis_out, weights_out,
+                                 imaging_out, acc);
   }
   finish_prep_sums(acc, sums);
 }
@@ -825,9 +878,11 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
                          int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
                          const float2 *vis, const float *weights, const float2 *model,
                          const uint8_t *selected, float2 *vis_out, float *weights_out,
-                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s) {
+                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s,
+                         const GainTable *gains) {
   if (n_rows == 0 || n_chan == 0) return;
   const PassWork w = carve_work(work, n_chan);
+  const GainTable gt0 = gains ? *gains : GainTable();
   chan_scale_kernel<<<blocks_for(n_chan), kThreads, 0, s>>>(freq, n_chan, g.width, g.height,
                                                             g.psx, g.psy, w.cs);
   check_launch("chan_scale_kernel");
@@ -838,9 +893,15 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
     const int64_t rows = std::min(rpl, n_rows - r0);
     const uint32_t n = (uint32_t)(rows * n_chan);
     const size_t off = (size_t)r0 * (size_t)n_chan, offp = off * (size_t)n_pol;
-    const int bps = n_pol == 1 ? resident_blocks(prepare_rows_fast_kernel<1, false>)
-                    : n_pol == 2 ? resident_blocks(prepare_rows_fast_kernel<2, true>)
-                                 : resident_blocks(prepare_rows_fast_kernel<4, true>);
+    const int bps = n_pol == 1 ? resident_blocks(prepare_rows_fast_kernel<1, false, false>)
+                    : n_pol == 2 ? resident_blocks(prepare_rows_fast_kernel<2, true, false>)
+                                 : resident_blocks(prepare_rows_fast_kernel<4, true, false>);
+    // the gain table's rows start at this launch's first row
+    GainTable gt = gt0;
+    if (gains) {
+      gt.ant = gt0.ant + 2 * r0;
+      gt.tof = gt0.tof + r0;
+    }
     const PassShape ps = pass_shape(n, bps);
     const Pending pend{w.idx, w.counts, ps.cap};
     const double *u = uvw + 3 * r0;
@@ -849,25 +910,33 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
     const uint8_t *sl = at(selected, off);
     float2 *vo = vis_out + off;
     float *wo = at(weights_out, offp), *io = at(imaging_out, off);
-#define WGPU_PREP_LAUNCH(NP, VEC)                                                              \
+#define WGPU_PREP_LAUNCH(NP, VEC, CORR)                                                        \
   do {                                                                                         \
-    prepare_rows_fast_kernel<NP, VEC><<<ps.blocks, kThreads, 0, s>>>(                         \
-        g, rw, n, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);            \
+    prepare_rows_fast_kernel<NP, VEC, CORR><<<ps.blocks, kThreads, 0, s>>>(                   \
+        g, rw, gt, n, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);        \
     check_launch("prepare_rows_fast_kernel");                                                  \
-    prepare_rows_exact_kernel<NP, VEC><<<ps.blocks, kThreads, 0, s>>>(                        \
-        g, rw, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);               \
+    prepare_rows_exact_kernel<NP, VEC, CORR><<<ps.blocks, kThreads, 0, s>>>(                  \
+        g, rw, gt, (uint32_t)n_chan, u, w.cs, v, wt, m, sl, vo, wo, io, sums, pend);           \
     check_launch("prepare_rows_exact_kernel");                                                 \
   } while (0)
-    if (n_pol == 1)
-      WGPU_PREP_LAUNCH(1, false);
-    else if (n_pol == 2 && vec)
-      WGPU_PREP_LAUNCH(2, true);
-    else if (n_pol == 2)
-      WGPU_PREP_LAUNCH(2, false);
-    else if (vec)
-      WGPU_PREP_LAUNCH(4, true);
+#define WGPU_PREP_DISPATCH(CORR)          \
+  do {                                    \
+    if (n_pol == 1)                       \
+      WGPU_PREP_LAUNCH(1, false, CORR);   \
+    else if (n_pol == 2 && vec)           \
+      WGPU_PREP_LAUNCH(2, true, CORR);    \
+    else if (n_pol == 2)                  \
+      WGPU_PREP_LAUNCH(2, false, CORR);   \
+    else if (vec)                         \
+      WGPU_PREP_LAUNCH(4, true, CORR);    \
+    else                                  \
+      WGPU_PREP_LAUNCH(4, false, CORR);   \
+  } while (0)
+    if (gains)
+      WGPU_PREP_DISPATCH(true);
     else
-      WGPU_PREP_LAUNCH(4, false);
+      WGPU_PREP_DISPATCH(false);
+#undef WGPU_PREP_DISPATCH
 #undef WGPU_PREP_LAUNCH
   }
 }

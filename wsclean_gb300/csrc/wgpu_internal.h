@@ -325,6 +325,19 @@ struct WeightSumsDev {
   double total_weight;
   unsigned long long max_bits;  // bits of the largest positive weight (double)
   unsigned long long count;
+  double correction;  // TRACE correction sum (corrected rows)
+};
+
+// Cached parm-response table of a corrected raw-row chunk (layouts as in
+// wgpu_gridder_add_inversion_data_corrected); err is a device flag set for a
+// row whose antenna or time index is outside the table.
+struct GainTable {
+  const float2 *sol = nullptr;
+  const uint64_t *ant = nullptr;
+  const uint64_t *tof = nullptr;
+  int nparms = 2, mode = 0;
+  int64_t n_times = 0, n_ant = 0;
+  int *err = nullptr;
 };
 void add_weight_sums(const WeightSumsDev &d, wgpu_weight_sums_t *sums);
 
@@ -342,7 +355,8 @@ void launch_prepare_rows(const WeightGridView &g, const RowWeighting &rw, int n_
                          int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
                          const float2 *vis, const float *weights, const float2 *model,
                          const uint8_t *selected, float2 *vis_out, float *weights_out,
-                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s);
+                         float *imaging_out, WeightSumsDev *sums, void *work, cudaStream_t s,
+                         const GainTable *gains = nullptr);
 
 // ---- resampling and trimming (resample.cu) ---------------------------------
 size_t resample_work_bytes(int64_t in_w, int64_t in_h, int64_t out_w, int64_t out_h);

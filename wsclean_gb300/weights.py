@@ -208,3 +208,26 @@ def prepare_rows_device(image_weights, n_pol, n_rows, n_chan, d_uvw, d_freq, d_w
                                          d_uvw, d_freq, d_vis, d_weights, d_model, d_selected,
                                          d_vis_out, d_weights_out, d_imaging_out, C.byref(sums)))
     return sums_dict(sums)
+
+
+def add_inversion_rows_corrected(gridder, image_weights, mode, uvw, frequencies, weights, vis,
+                                 antennas, time_offsets, solutions, nparms, n_times, n_antenna,
+                                 model=None, selected=None, sums=None, with_correction_sum=False,
+                                 **settings):
+    """GetCollapsedVisibilities with h5parm corrections + AddInversionData on
+    the device (wgpu_gridder_add_inversion_rows_corrected).  Returns (sums,
+    correction sum or None); the correction sum exists for the TRACE mode."""
+    rw = row_weighting(**settings)
+    uvw, freq, wts, vis_a, mod_a, sel_a, (n_rows, n_chan, n_pol) = _row_inputs(
+        uvw, frequencies, weights, vis, model, selected, rw)
+    ant = np.ascontiguousarray(antennas, np.uint64)
+    tof = np.ascontiguousarray(time_offsets, np.uint64)
+    sol = np.ascontiguousarray(solutions, np.complex64)
+    if sums is None:
+        sums = _lib.WeightSums()
+    corr = C.c_double(0.0)
+    check(lib().wgpu_gridder_add_inversion_rows_corrected(
+        gridder._h, image_weights.handle, C.byref(rw), int(mode), n_pol, n_rows, n_chan, ptr(uvw),
+        ptr(freq), ptr(vis_a), ptr(wts), ptr(mod_a), ptr(sel_a), ptr(ant), ptr(tof), ptr(sol),
+        nparms, n_times, n_antenna, C.byref(sums), C.byref(corr) if with_correction_sum else None))
+    return sums, (corr.value if with_correction_sum else None)
