@@ -178,6 +178,9 @@ __device__ __forceinline__ bool d2f_trunc(unsigned long long b, float *out) {
 // float range).  Reflection into v >= 0 flips the signs exactly.
 __device__ __forceinline__ int64_t fast_cell(double um, double vm, const ChanScale &c, int64_t W,
                                              int64_t H) {
+  // grid sizes are below 2^21: 32-bit integer <-> float conversions (the
+  // 64-bit ones also run on the FP64 pipe)
+  const int w32 = (int)W, hh32 = (int)(H / 2);
   const unsigned long long bu = (unsigned long long)__double_as_longlong(um);
   const unsigned long long bv = (unsigned long long)__double_as_longlong(vm);
   const unsigned long long av = bv & 0x7fffffffffffffffull;
@@ -185,7 +188,7 @@ __device__ __forceinline__ int64_t fast_cell(double um, double vm, const ChanSca
   const unsigned long long flip = (bv >> 63 != 0ull && av != 0ull) ? (1ull << 63) : 0ull;
   float uf, vf;
   if (!d2f_trunc(bu ^ flip, &uf) || !d2f_trunc(av, &vf)) return -2;
-  const float xf = fmaf(uf, c.su, (float)(W / 2));
+  const float xf = fmaf(uf, c.su, (float)(w32 / 2));
   const float bx = 0x1p-21f * (fabsf(uf * c.su) + fabsf(xf)) + 1e-30f;
   const float kx = floorf(xf), fx = xf - kx;
   if (!(fx > bx && fx < 1.0f - bx)) return -2;
@@ -193,8 +196,8 @@ __device__ __forceinline__ int64_t fast_cell(double um, double vm, const ChanSca
   const float by = 0x1p-20f * fabsf(yf) + 1e-30f;
   const float ky = floorf(yf), fy = yf - ky;
   if (!(fy > by && fy < 1.0f - by)) return -2;
-  if (!(kx >= 0.0f && kx < (float)W && ky >= 0.0f && ky < (float)(H / 2))) return -1;
-  return (int64_t)kx + (int64_t)ky * W;
+  if (!(kx >= 0.0f && kx < (float)w32 && ky >= 0.0f && ky < (float)hh32)) return -1;
+  return (int64_t)(int)kx + (int64_t)(int)ky * (int64_t)w32;
 }
 
 // Float-float accumulator (Knuth's TwoSum), flushed into a double every
