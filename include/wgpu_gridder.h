@@ -11,8 +11,10 @@
  * Standalone use: define nothing; GainMode, BandData and MsGridder are
  * declared here.  Inside WSClean: define WGPU_WITH_WSCLEAN before including, so
  * that WSClean's own GainMode / aocommon::BandData / MsGridder are used and the
- * correction callback reads the gridder's cached solution table (see
- * INTEGRATION.md for the accessor it needs).
+ * correction callback reads the gridder's cached solution table through an
+ * accessor MsGridder::GpuCorrections() returning a GpuCorrectionTable (the
+ * cached parm response of VisibilityModifier, its time count, values per
+ * solution and polarisation).
  */
 #ifndef WGPU_GRIDDER_H_
 #define WGPU_GRIDDER_H_
@@ -202,6 +204,42 @@ class WGriddingGridder_Simple final : public WGriddingGridderBase {
         reinterpret_cast<const uint64_t *>(time_offsets),
         reinterpret_cast<const float *>(table.solutions), table.nparms, table.n_times,
         n_antenna, table.polarization, reinterpret_cast<float *>(vis)));
+  }
+
+  /* WGriddingMSGridder::FinishInversion after FinalizeImage
+   * (wgriddingmsgridder.cpp:273-309): RealImage resampled from the gridder's
+   * size to image_width x image_height when those differ, then trimmed to
+   * trim_width x trim_height, on the device. */
+  std::vector<float> FinishInversion(size_t image_width, size_t image_height, size_t trim_width,
+                                     size_t trim_height) {
+    std::vector<float> image(trim_width * trim_height);
+    wgpu_detail::check(wgpu_gridder_finish_inversion(g_, image_width, image_height, trim_width,
+                                                     trim_height, image.data()));
+    return image;
+  }
+
+  /* WGriddingMSGridder::StartPredict (wgriddingmsgridder.cpp:311-340): the
+   * trim_width x trim_height model untrimmed, resampled to the gridder's size
+   * and set as the prediction image, on the device. */
+  void StartPredict(const float *model, size_t trim_width, size_t trim_height,
+                    size_t image_width, size_t image_height) {
+    wgpu_detail::check(wgpu_gridder_start_predict(g_, trim_width, trim_height, image_width,
+                                                  image_height, model));
+  }
+
+  /* GetCollapsedVisibilities + AddInversionData on raw rows
+   * (wgpu_gridder_add_inversion_rows): vis / weights [row][chan][n_pol],
+   * selected [row][chan] (nullptr: all). */
+  void AddInversionRows(const wgpu_imageweights_t *image_weights,
+                        const wgpu_row_weighting_t &weighting, size_t n_polarizations,
+                        size_t n_rows, size_t n_chan, const double *uvws,
+                        const double *frequencies, const std::complex<float> *visibilities,
+                        const float *weights, const std::complex<float> *model,
+                        const uint8_t *selected, wgpu_weight_sums_t &sums) {
+    wgpu_detail::check(wgpu_gridder_add_inversion_rows(
+        g_, image_weights, &weighting, n_polarizations, n_rows, n_chan, uvws, frequencies,
+        reinterpret_cast<const float *>(visibilities), weights,
+        reinterpret_cast<const float *>(model), selected, &sums));
   }
 
   wgpu_gridder_t *handle() const { return g_; }

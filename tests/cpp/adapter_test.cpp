@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "wgpu_gridder.h"
+#include "wgpu_imageweights.h"
 
 template <typename T>
 static std::vector<T> read_file(const char *path, size_t n) {
@@ -55,6 +56,8 @@ int main(int argc, char **argv) {
                           vis.data() + half * n_chan);
     base.FinalizeImage(1.0);
     write_file(prefix + "image.bin", base.RealImage());
+    // FinishInversion: resampled to (W + 32)^2, trimmed to Wt^2
+    write_file(prefix + "finish.bin", g.FinishInversion(W + 32, W + 32, Wt, Wt));
     base.InitializePrediction(model.data());
     std::vector<std::complex<float>> pred(n_rows * n_chan);
     base.PredictVisibilities(n_rows, n_chan, uvw.data(), freq.data(), pred.data());
@@ -77,6 +80,24 @@ int main(int argc, char **argv) {
                                          time_offsets.data(), table, n_ant,
                                          pred_corr.data());
     write_file(prefix + "pred_corr.bin", pred_corr);
+    // raw rows with uniform imaging weights (unit visibility weights)
+    {
+      std::vector<float> ones(n_rows * n_chan, 1.0f);
+      wsclean::GpuImageWeights iw(WGPU_WEIGHT_UNIFORM, 0.0, Wt, Wt, dl, dl, false, 1.0);
+      iw.Grid(n_rows, n_chan, 1, uvw.data(), freq.data(), ones.data());
+      iw.FinishGridding();
+      wsclean::WGriddingGridder_Simple<double> g2(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, eps);
+      wgpu_row_weighting_t rw = {WGPU_PSF_NONE, 0.0, 0.0, 0, WGPU_VISW_NORMAL, WGPU_POL_STOKES_I};
+      wgpu_weight_sums_t sums = {0.0, 0.0, 0.0, 0};
+      g2.InitializeInversion();
+      g2.AddInversionRows(iw.handle(), rw, 1, n_rows, n_chan, uvw.data(), freq.data(),
+                          vis.data(), ones.data(), nullptr, nullptr, sums);
+      g2.FinalizeImage(1.0);
+      write_file(prefix + "rows.bin", g2.RealImage());
+      std::vector<double> s4 = {sums.visibility_weight_sum, sums.max_gridded_weight,
+                                sums.total_weight, (double)sums.gridded_visibility_count};
+      write_file(prefix + "sums.bin", s4);
+    }
     // bad argument -> std::runtime_error, as the reference's MR_assert throws
     bool threw = false;
     try {

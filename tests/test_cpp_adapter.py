@@ -52,6 +52,27 @@ def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
     trimmed = model[d:d + Wt, d:d + Wt].ravel()
     pr = oracle_lib.dft_predict(uvw, freq, trimmed, Wt, Wt, dl, dl)
     assert np.linalg.norm(pred - pr) / np.linalg.norm(pr) <= eps
+    # FinishInversion: RealImage resampled to (W + 32)^2 and trimmed to Wt^2
+    from oracle import resample as ores
+    fin = np.fromfile(prefix + "finish.bin", np.float32).reshape(Wt, Wt)
+    exp = ores.trim(ores.resample(img, W + 32, W + 32), Wt, Wt)
+    assert np.linalg.norm(fin - exp) <= 1e-5 * np.linalg.norm(exp)
+    # raw rows through GpuImageWeights + AddInversionRows = the Python API path
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    from wsclean_gb300.weights import UNIFORM, ImageWeights
+    ones = np.ones((uvw.shape[0], freq.size, 1), np.float32)
+    iw = ImageWeights(UNIFORM, Wt, Wt, dl, dl)
+    iw.Grid(uvw, freq, ones)
+    iw.FinishGridding()
+    g = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps, num_t=np.float64)
+    g.InitializeInversion()
+    sums = g.AddInversionRows(iw, uvw, freq, ones, vis.astype(np.complex64)[:, :, None])
+    g.FinalizeImage(1.0)
+    py_rows = g.RealImage().reshape(W, W)[d:d + Wt, d:d + Wt]
+    rows = np.fromfile(prefix + "rows.bin", np.float32).reshape(W, W)[d:d + Wt, d:d + Wt]
+    np.testing.assert_allclose(rows, py_rows, rtol=0, atol=1e-6 * np.abs(py_rows).max())
+    s4 = np.fromfile(prefix + "sums.bin", np.float64)
+    assert s4[3] == sums.gridded_visibility_count > 0
     # uniform diagonal gain 1.5+0.5i, XX mode: |g|^2 = 2.5 times the prediction
     pred_corr = np.fromfile(prefix + "pred_corr.bin", np.complex64)
     np.testing.assert_allclose(pred_corr, 2.5 * pred, rtol=1e-5, atol=1e-6 * np.abs(pred).max())
