@@ -854,7 +854,9 @@ def run_rowweights(args):
                    "bit_exact_vs_oracle": bit_exact, "e2e_matches_device": same,
                    "weight_sums": sums, "datagen_s": round(gen_s, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": _traffic("prepare_rows_fast_kernel")[0],
+                     "traffic_unit": "GB per launch",
+                     "traffic_source": _traffic("prepare_rows_fast_kernel")[1],
                      "kernel": "prepare_rows_fast_kernel<4, true> + exact pass",
                      "peak_source": peak_src,
                      "bytes_per_sample": 64},
@@ -950,7 +952,10 @@ def run_resample(args):
                    "accuracy": {"rel_l2_vs_fp64_oracle": rel_small},
                    "e2e_matches_device": same},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "fft_stage_kernel (all passes)",
+                     "frac": achieved / peak, "traffic": _traffic("fft_stage_kernel")[0],
+                     "traffic_unit": "GB per radix-8 row pass",
+                     "traffic_source": _traffic("fft_stage_kernel")[1],
+                     "kernel": "fft_stage_kernel (all passes)",
                      "peak_source": peak_src,
                      "bytes": "one read + one write of the complex work image per pass"},
         "cpu_baseline": {"value": (big * big + small * small) / cpu_s / 1e9,
@@ -962,6 +967,18 @@ def run_resample(args):
                 "note": "one leg (8192^2 -> 5120^2) through wgpu_resample"},
         "gpu_launches": int(launches),
     }
+
+
+def _traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summaries
+    (profiles/traffic.json), in GB, with where they come from."""
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tpath):
+        return None, None
+    t = json.load(open(tpath)).get(kernel)
+    if not t:
+        return None, None
+    return float(t["traffic_bytes_per_launch"]) / 1e9, t["how"]
 
 
 def _lib_launches():
