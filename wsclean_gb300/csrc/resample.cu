@@ -162,6 +162,91 @@ __global__ void fft_stage_kernel(const float2 *x, float2 *y, int64_t n, int64_t 
   stage_body<R>(x, y, n, i, b, bstride, estride, p, tw, rc, inverse, radix);
 }
 
+// Row transforms of power-of-two length n in [512, 8192] whose radices are
+// 8, 4 and 2, in shared memory: one block of n / 16 threads per row loads the
+// row once, runs every pass in place (each thread holds its 16 values in
+// registers between the barriers of a pass) and writes the row once.  The
+// butterflies i = threadIdx.x + b * blockDim.x, b < 16 / R, cover [0, n / R)
+// exactly.
+struct RowStages {
+  int n_st;
+  int radix[16];
+  int p[16];
+  int tw_off[16];
+  int rc_off[16];
+};
+
+template <int R>
+__device__ __forceinline__ void smem_pass(float2 *buf, int n, int p, const float2 *tw,
+                                          const float2 *rc, int inverse) {
+  constexpr int PER = 16 / R;
+  const int nq = n / R;
+  float2 out[16];
+  int jj[PER];
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int i = threadIdx.x + b * blockDim.x;
+    const int k = i & (p - 1);
+    jj[b] = (i - k) * R + k;
+    float2 u[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      float2 v = buf[i + q * nq];
+      if (q > 0 && k > 0) {
+        float2 w = tw[(q - 1) * p + k];
+        if (inverse) w = cconj(w);
+        v = cmul(v, w);
+      }
+      u[q] = v;
+    }
+#pragma unroll
+    for (int o = 0; o < R; ++o) {
+      float2 acc = u[0];
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        float2 w = rc[(q * o) % R];
+        if (inverse) w = cconj(w);
+        const float2 t = cmul(u[q], w);
+        acc.x += t.x;
+        acc.y += t.y;
+      }
+      out[b * R + o] = acc;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < PER; ++b)
+#pragma unroll
+    for (int o = 0; o < R; ++o) buf[jj[b] + o * p] = out[b * R + o];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(512, 2) fft_rows_smem_kernel(float2 *data, int n, int64_t stride,
+                                                             RowStages st, const float2 *tw,
+                                                             int inverse) {
+  extern __shared__ float2 buf[];
+  float2 *row = data + (int64_t)blockIdx.x * stride;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) buf[e] = row[e];
+  __syncthreads();
+  for (int s = 0; s < st.n_st; ++s) {
+    const float2 *t = tw + st.tw_off[s], *rc = tw + st.rc_off[s];
+    if (st.radix[s] == 8)
+      smem_pass<8>(buf, n, st.p[s], t, rc, inverse);
+    else if (st.radix[s] == 4)
+      smem_pass<4>(buf, n, st.p[s], t, rc, inverse);
+    else
+      smem_pass<2>(buf, n, st.p[s], t, rc, inverse);
+  }
+  for (int e = threadIdx.x; e < n; e += blockDim.x) row[e] = buf[e];
+}
+
+bool rows_in_smem(const std::vector<Stage> &st, int64_t n) {
+  if (n < 512 || n > 8192 || (n & (n - 1)) != 0 || st.size() > 16) return false;
+  for (const Stage &g : st)
+    if (g.radix != 8 && g.radix != 4 && g.radix != 2) return false;
+  return true;
+}
+
 // Real image (row-major, w x h) -> complex work image, non-finite pixels 0.
 __global__ void load_real_kernel(const float *in, int64_t n, float2 *a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,6 +294,22 @@ __global__ void store_real_kernel(const float2 *b, int64_t n, float scale, float
 void run_fft(const std::vector<Stage> &st, float2 **cur, float2 **alt, int64_t n, int64_t batch,
              int64_t bstride, int64_t estride, bool batch_fastest, const float2 *d_tw,
              bool inverse, cudaStream_t s) {
+  if (!batch_fastest && estride == 1 && rows_in_smem(st, n)) {
+    RowStages rs{};
+    rs.n_st = (int)st.size();
+    for (size_t k = 0; k < st.size(); ++k) {
+      rs.radix[k] = st[k].radix;
+      rs.p[k] = (int)st[k].p;
+      rs.tw_off[k] = (int)st[k].tw_off;
+      rs.rc_off[k] = (int)st[k].rc_off;
+    }
+    const size_t smem = sizeof(float2) * (size_t)n;
+    ensure_dynamic_smem((const void *)fft_rows_smem_kernel, smem);
+    fft_rows_smem_kernel<<<(unsigned)batch, (unsigned)(n / 16), smem, s>>>(
+        *cur, (int)n, bstride, rs, d_tw, inverse ? 1 : 0);
+    check_launch("fft_rows_smem_kernel");
+    return;  // transformed in place
+  }
   for (const Stage &g : st) {
     const int64_t threads = n / g.radix * batch;
     const float2 *tw = d_tw + g.tw_off, *rc = d_tw + g.rc_off;
