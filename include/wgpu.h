@@ -466,6 +466,21 @@ int wgpu_facets_bind(wgpu_facets_t *facets, size_t n_rows, size_t n_chan,
 int wgpu_facets_invert(wgpu_facets_t *facets, const float *vis, float *images);
 int wgpu_facets_invert_device(wgpu_facets_t *facets, const float *d_vis,
                               float *d_images);
+/* Facets with direction-dependent corrections (facet h5parm solutions, as
+ * WSClean's facet gridding applies them per row through the correction
+ * callback, callback_implementation.h:53-101): the batch is bound with one
+ * corrected visibility buffer per facet; each inversion uploads the
+ * uncorrected [row][chan][n_pol] visibilities and the facets' solution tables
+ * once ([facet][t][chan][ant][nparms] complex64, layouts otherwise as in
+ * wgpu_gridder_add_inversion_data_corrected), applies each facet's
+ * conjugated gains and collapse on the device and runs the batch's graph. */
+int wgpu_facets_bind_corrected(wgpu_facets_t *facets, size_t n_rows, size_t n_chan,
+                               const double *uvw, const double *freq);
+int wgpu_facets_invert_corrected(wgpu_facets_t *facets, int mode, size_t n_pol,
+                                 const float *vis, const uint64_t *antenna_pairs,
+                                 const uint64_t *time_offsets, const float *solutions,
+                                 size_t nparms, size_t n_times, size_t n_ant, int polarization,
+                                 float *images);
 int wgpu_facets_info(const wgpu_facets_t *facets, wgpu_facets_info_t *info);
 int wgpu_facets_job_plan(const wgpu_facets_t *facets, size_t job, wgpu_plan_t *plan);
 void *wgpu_facets_stream(wgpu_facets_t *facets);

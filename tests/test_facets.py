@@ -94,3 +94,50 @@ def test_facet_batch_validates_arguments(wgpu_lib):
     with pytest.raises(_lib.WgpuError) as e:
         FacetBatch([dict(width=64, height=64, dl=1e-3)], [0, 2], epsilon=0.0)
     assert e.value.status == _lib.WGPU_ERR_INVALID
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,n_pol,nparms", [(4, 4, 4), (3, 2, 2), (2, 1, 4)])
+def test_facet_corrections_match_oracle_gains(wgpu_lib, oracle_lib, mode, n_pol, nparms):
+    """Direction-dependent gains: each facet's jobs see its own conjugated gains
+    (applied on the device from one upload of the uncorrected visibilities and
+    all facets' solution tables).  A facet's images equal the plain batch run
+    on the oracle's gain-applied, collapsed visibilities for that facet (FP32
+    gains with fused multiply-adds: 1e-5), and are within epsilon of the FP64
+    direct FT of those visibilities."""
+    from wsclean_gb300.facets import FacetBatch
+    uvw, freq, vis1 = _data()
+    rng = np.random.default_rng(90 + mode)
+    n_rows, n_chan, n_ant, n_t = uvw.shape[0], freq.size, 6, 2
+    vis = (np.repeat(vis1[:, :, None], n_pol, axis=2) *
+           (1.0 + 0.2 * rng.standard_normal((n_rows, n_chan, n_pol)))).astype(np.complex64)
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)], axis=1)
+    tof = rng.integers(0, n_t, n_rows).astype(np.uint64)
+    sol = (1.0 + 0.3 * (rng.standard_normal((len(FACETS), n_t, n_chan, n_ant, nparms)) +
+                        1j * rng.standard_normal((len(FACETS), n_t, n_chan, n_ant, nparms)))
+           ).astype(np.complex64)
+    eps = 1e-4
+    fb = FacetBatch(FACETS, GROUPS, epsilon=eps)
+    fb.bind(uvw, freq, corrected=True)
+    images = fb.invert_corrected(mode, vis, ant, tof, sol, nparms, n_t, n_ant)
+    with pytest.raises(_lib.WgpuError):
+        fb.invert(vis1)  # a corrected binding needs the corrected inversion
+    plain = FacetBatch(FACETS, GROUPS, epsilon=eps)
+    plain.bind(uvw, freq)
+    for fi, f in enumerate(FACETS):
+        corrected = oracle_lib.apply_gains(mode, n_pol, vis, ant, tof, sol[fi], nparms, n_ant)
+        ref_images = plain.invert(corrected)
+        for gi in range(len(GROUPS) - 1):
+            job = gi * len(FACETS) + fi
+            assert rel(images[job], ref_images[job]) <= 1e-5, job
+            c0, c1 = GROUPS[gi], GROUPS[gi + 1]
+            dft = oracle_lib.dft_invert(uvw, freq[c0:c1], np.ascontiguousarray(corrected[:, c0:c1]),
+                                        f["width"], f["height"], f["dl"], f["dl"], f["l_shift"],
+                                        f["m_shift"]).reshape(f["height"], f["width"])
+            assert rel(images[job], dft) <= eps, job
+    bad = ant.copy()
+    bad[0, 1] = n_ant
+    with pytest.raises(_lib.WgpuError):
+        fb.invert_corrected(mode, vis, bad, tof, sol, nparms, n_t, n_ant)
+    fb.close()
+    plain.close()

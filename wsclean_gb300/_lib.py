@@ -165,6 +165,8 @@ _PROTOS = {
     "wgpu_facets_bind": (I, [P, SZ, SZ, P, P]),
     "wgpu_facets_invert": (I, [P, P, P]),
     "wgpu_facets_invert_device": (I, [P, P, P]),
+    "wgpu_facets_bind_corrected": (I, [P, SZ, SZ, P, P]),
+    "wgpu_facets_invert_corrected": (I, [P, I, SZ, P, P, P, P, SZ, SZ, SZ, I, P]),
     "wgpu_facets_info": (I, [P, C.POINTER(FacetsInfo)]),
     "wgpu_facets_job_plan": (I, [P, SZ, C.POINTER(Plan)]),
     "wgpu_facets_stream": (P, [P]),

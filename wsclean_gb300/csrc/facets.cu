@@ -95,6 +95,16 @@ struct wgpu_facets {
   size_t n_rows = 0, n_chan = 0;
   double *d_uvw = nullptr, *d_freq = nullptr;
   float2 *d_vis = nullptr;
+  // per-facet corrections: each facet's corrected, collapsed visibilities
+  // (restamped by that facet's jobs), the shared uncorrected inputs
+  bool per_facet = false;
+  std::vector<float2 *> d_vis_facet;
+  float *d_vis_raw = nullptr;
+  size_t vis_raw_floats = 0;
+  uint64_t *d_ant = nullptr, *d_tof = nullptr;
+  float *d_sol = nullptr;
+  size_t sol_floats = 0;
+  int *d_err = nullptr;
   float *d_images = nullptr;
   size_t image_elems = 0;
   float2 *pool = nullptr;
@@ -171,6 +181,18 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   f->d_uvw = (double *)f->alloc(sizeof(double) * 3 * n_rows);
   f->d_freq = (double *)f->alloc(sizeof(double) * n_chan);
   f->d_vis = (float2 *)f->alloc(sizeof(float2) * n_rows * n_chan);
+  f->d_vis_facet.clear();
+  f->d_vis_raw = nullptr;
+  f->vis_raw_floats = 0;
+  f->d_sol = nullptr;
+  f->sol_floats = 0;
+  if (f->per_facet) {
+    for (size_t i = 0; i < f->facets.size(); ++i)
+      f->d_vis_facet.push_back((float2 *)f->alloc(sizeof(float2) * n_rows * n_chan));
+    f->d_ant = (uint64_t *)f->alloc(sizeof(uint64_t) * 2 * n_rows);
+    f->d_tof = (uint64_t *)f->alloc(sizeof(uint64_t) * n_rows);
+    f->d_err = (int *)f->alloc(sizeof(int) * 4);
+  }
   WGPU_CUDA(cudaMemcpyAsync(f->d_uvw, uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
   WGPU_CUDA(cudaMemcpyAsync(f->d_freq, freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
   DeviceArena arena;  // bucketing scratch, released at return
@@ -361,11 +383,15 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   const uint64_t k0 = thread_launch_count();
   WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   try {
-    for (Job &j : f->jobs) {
+    for (size_t ji = 0; ji < f->jobs.size(); ++ji) {
+      Job &j = f->jobs[ji];
       const int64_t n = j.n_out;
+      // job = group * n_facets + facet: with per-facet corrections a job
+      // restamps its facet's corrected visibilities
+      const float2 *src = f->per_facet ? f->d_vis_facet[ji % f->facets.size()] : f->d_vis;
       if (n > 0) {
         restamp_channels_kernel<<<(unsigned)((n + kFacetThreads - 1) / kFacetThreads),
-                                  kFacetThreads, 0, s>>>(j.geom, j.perm, f->d_vis, n, j.nch,
+                                  kFacetThreads, 0, s>>>(j.geom, j.perm, src, n, j.nch,
                                                          (int)f->n_chan, j.c0, j.work);
         check_launch("restamp_channels_kernel");
       }
@@ -418,6 +444,48 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   f->bound = true;
 }
 
+// Per-facet corrections: the uncorrected [row][chan][n_pol] visibilities and
+// the facets' solution tables (one upload for all facets), then each facet's
+// conjugated gains and collapse into its own buffer (the corrected inversion's
+// kernel, callback_implementation.h:53-101 per facet).
+void correct_facets(wgpu_facets *f, int mode, int n_pol, const float *vis,
+                    const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+                    const float *solutions, int nparms, int64_t n_times, int64_t n_ant,
+                    int polarization) {
+  cudaStream_t s = f->stream;
+  const size_t nv = f->n_rows * f->n_chan;
+  const size_t vis_floats = 2 * nv * (size_t)n_pol;
+  if (f->vis_raw_floats < vis_floats) {
+    f->d_vis_raw = (float *)f->alloc(sizeof(float) * vis_floats);
+    f->vis_raw_floats = vis_floats;
+  }
+  const size_t table_floats = 2 * (size_t)n_times * f->n_chan * (size_t)n_ant * (size_t)nparms;
+  const size_t sol_floats = table_floats * f->facets.size();
+  if (f->sol_floats < sol_floats) {
+    f->d_sol = (float *)f->alloc(sizeof(float) * sol_floats);
+    f->sol_floats = sol_floats;
+  }
+  WGPU_CUDA(cudaMemcpyAsync(f->d_vis_raw, vis, sizeof(float) * vis_floats,
+                            cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->d_ant, antenna_pairs, sizeof(uint64_t) * 2 * f->n_rows,
+                            cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->d_tof, time_offsets, sizeof(uint64_t) * f->n_rows,
+                            cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemcpyAsync(f->d_sol, solutions, sizeof(float) * sol_floats,
+                            cudaMemcpyHostToDevice, s));
+  WGPU_CUDA(cudaMemsetAsync(f->d_err, 0, sizeof(int), s));
+  for (size_t i = 0; i < f->facets.size(); ++i)
+    launch_apply_gains(mode, n_pol, (int64_t)f->n_rows, (int64_t)f->n_chan,
+                       (const float2 *)f->d_vis_raw, f->d_ant, f->d_tof,
+                       (const float2 *)(f->d_sol + i * table_floats), nparms, n_times, n_ant,
+                       polarization, f->d_vis_facet[i], f->d_err, s);
+  int herr = 0;
+  WGPU_CUDA(cudaMemcpyAsync(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  if (herr) throw Error(WGPU_ERR_INVALID, "antenna index or time offset outside the solution table");
+}
+
+// vis == nullptr: the visibilities are already in place (per-facet buffers).
 void invert_facets(wgpu_facets *f, const float *vis, bool device, float *images) {
   if (!f->bound) throw Error(WGPU_ERR_STATE, "no bound visibility set");
   cudaStream_t s = f->stream;
@@ -425,8 +493,9 @@ void invert_facets(wgpu_facets *f, const float *vis, bool device, float *images)
   WGPU_CUDA(cudaEventCreate(&e0));
   WGPU_CUDA(cudaEventCreate(&e1));
   WGPU_CUDA(cudaEventRecord(e0, s));
-  WGPU_CUDA(cudaMemcpyAsync(f->d_vis, vis, sizeof(float2) * f->n_rows * f->n_chan,
-                            device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  if (vis)
+    WGPU_CUDA(cudaMemcpyAsync(f->d_vis, vis, sizeof(float2) * f->n_rows * f->n_chan,
+                              device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   WGPU_CUDA(cudaGraphLaunch(f->exec, s));
   count_launch((int)f->graph_kernels);
   if (images)
@@ -513,13 +582,52 @@ int wgpu_facets_bind(wgpu_facets_t *f, size_t n_rows, size_t n_chan, const doubl
   if (!f || !uvw || !freq) return report_failure(WGPU_ERR_INVALID, "null argument");
   return facets_guarded([&] {
     WGPU_CUDA(cudaSetDevice(f->device));
+    f->per_facet = false;
     bind_facets(f, n_rows, n_chan, uvw, freq);
   });
 }
 
 int wgpu_facets_invert(wgpu_facets_t *f, const float *vis, float *images) {
   if (!f || !vis) return report_failure(WGPU_ERR_INVALID, "null argument");
-  return facets_guarded([&] { invert_facets(f, vis, false, images); });
+  return facets_guarded([&] {
+    if (f->per_facet)
+      throw Error(WGPU_ERR_STATE, "bound with per-facet corrections: use the corrected inversion");
+    invert_facets(f, vis, false, images);
+  });
+}
+
+int wgpu_facets_bind_corrected(wgpu_facets_t *f, size_t n_rows, size_t n_chan, const double *uvw,
+                               const double *freq) {
+  if (!f || !uvw || !freq) return report_failure(WGPU_ERR_INVALID, "null argument");
+  return facets_guarded([&] {
+    WGPU_CUDA(cudaSetDevice(f->device));
+    f->per_facet = true;
+    bind_facets(f, n_rows, n_chan, uvw, freq);
+  });
+}
+
+int wgpu_facets_invert_corrected(wgpu_facets_t *f, int mode, size_t n_pol, const float *vis,
+                                 const uint64_t *antenna_pairs, const uint64_t *time_offsets,
+                                 const float *solutions, size_t nparms, size_t n_times,
+                                 size_t n_ant, int polarization, float *images) {
+  if (!f || !vis || !antenna_pairs || !time_offsets || !solutions)
+    return report_failure(WGPU_ERR_INVALID, "null argument");
+  if (mode < WGPU_GAIN_XX || mode > WGPU_GAIN_FULL)
+    return report_failure(WGPU_ERR_INVALID, "invalid gain mode");
+  const size_t want = mode == WGPU_GAIN_FULL ? 4 : mode == WGPU_GAIN_2VIS_DIAGONAL ? 2 : 1;
+  if (n_pol != want)
+    return report_failure(WGPU_ERR_INVALID, "gain mode and n_polarizations do not match");
+  if (nparms != 2 && nparms != 4) return report_failure(WGPU_ERR_INVALID, "nparms must be 2 or 4");
+  if (polarization < 0 || polarization > 7)
+    return report_failure(WGPU_ERR_INVALID, "invalid polarization");
+  return facets_guarded([&] {
+    if (!f->bound || !f->per_facet)
+      throw Error(WGPU_ERR_STATE, "not bound with per-facet corrections");
+    WGPU_CUDA(cudaSetDevice(f->device));
+    correct_facets(f, mode, (int)n_pol, vis, antenna_pairs, time_offsets, solutions, (int)nparms,
+                   (int64_t)n_times, (int64_t)n_ant, polarization);
+    invert_facets(f, nullptr, false, images);
+  });
 }
 
 int wgpu_facets_invert_device(wgpu_facets_t *f, const float *d_vis, float *d_images) {

@@ -42,11 +42,14 @@ class FacetBatch:
         except Exception:
             pass
 
-    def bind(self, uvw, freq):
+    def bind(self, uvw, freq, corrected=False):
+        """Binds the rows; corrected=True keeps one corrected visibility buffer
+        per facet for invert_corrected (direction-dependent gains)."""
         self._uvw = np.ascontiguousarray(uvw, dtype=np.float64).reshape(-1, 3)
         self._freq = np.ascontiguousarray(freq, dtype=np.float64)
-        check(lib().wgpu_facets_bind(self._h, self._uvw.shape[0], self._freq.size,
-                                     self._uvw.ctypes.data, self._freq.ctypes.data))
+        fn = lib().wgpu_facets_bind_corrected if corrected else lib().wgpu_facets_bind
+        check(fn(self._h, self._uvw.shape[0], self._freq.size, self._uvw.ctypes.data,
+                 self._freq.ctypes.data))
 
     def info(self):
         i = _lib.FacetsInfo()
@@ -64,6 +67,30 @@ class FacetBatch:
         vis = np.ascontiguousarray(vis, dtype=np.complex64)
         out = np.empty(int(self.info()["image_elems"]), np.float32)
         check(lib().wgpu_facets_invert(self._h, vis.ctypes.data, out.ctypes.data))
+        return self._split(out)
+
+    def invert_corrected(self, mode, vis, antennas, time_offsets, solutions, nparms, n_times,
+                         n_antenna, polarization=_lib.POL_I):
+        """Dirty images with each facet's conjugated gains applied on the
+        device: vis (rows, chans, n_pol) uncorrected, solutions (n_facets,
+        n_times, chans, n_antenna, nparms) complex64; bind(corrected=True)
+        first."""
+        if isinstance(mode, str):
+            mode = {"xx": 0, "yy": 1, "trace": 2, "diagonal": 3, "full": 4}[mode]
+        vis = np.ascontiguousarray(vis, dtype=np.complex64)
+        n_pol = vis.size // (self._uvw.shape[0] * self._freq.size)
+        ant = np.ascontiguousarray(antennas, dtype=np.uint64)
+        tof = np.ascontiguousarray(time_offsets, dtype=np.uint64)
+        sol = np.ascontiguousarray(solutions, dtype=np.complex64)
+        assert sol.size == len(self.facets) * n_times * self._freq.size * n_antenna * nparms
+        out = np.empty(int(self.info()["image_elems"]), np.float32)
+        check(lib().wgpu_facets_invert_corrected(self._h, int(mode), n_pol, vis.ctypes.data,
+                                                 ant.ctypes.data, tof.ctypes.data,
+                                                 sol.ctypes.data, nparms, n_times, n_antenna,
+                                                 int(polarization), out.ctypes.data))
+        return self._split(out)
+
+    def _split(self, out):
         images, o = [], 0
         for _ in range(self.n_groups):
             for f in self.facets:
