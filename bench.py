@@ -695,6 +695,44 @@ def run_facets(args):
                                                       np.linalg.norm(dft))
     for gg in gp.values():
         gg.close()
+    corrections = None
+    if args.facet_corrections:
+        # direction-dependent gains: 4-correlation visibilities (XX = YY = V)
+        # and a full-Jones solution table per facet (per time step, channel,
+        # antenna), one upload per inversion, gains applied per facet on the
+        # device (host entry point: uploads inside the timed region)
+        n_ant, n_t = d["n_ant"], d["n_t"]
+        vis4 = np.zeros((n_rows, n_chan, 4), np.complex64)
+        vis4[:, :, 0] = h_vis.reshape(n_rows, n_chan)
+        vis4[:, :, 3] = vis4[:, :, 0]
+        ant = np.stack([d["ant1"], d["ant2"]], axis=1).astype(np.uint64)
+        tof = np.asarray(d["time_index"], np.uint64)
+        crng = np.random.default_rng(5)
+        sol = np.zeros((len(facets), n_t, n_chan, n_ant, 4), np.complex64)
+        sol[..., 0] = 1.0
+        sol[..., 3] = 1.0
+        sol += (0.05 * (crng.standard_normal(sol.shape) + 1j * crng.standard_normal(sol.shape))
+                ).astype(np.complex64)
+        fc = FacetBatch(facets, groups, epsilon=eps)
+        t0 = time.time()
+        fc.bind(d["uvw"], d["freq"], corrected=True)
+        cbind_s = time.time() - t0
+        fc.invert_corrected(4, vis4, ant, tof, sol, 4, n_t, n_ant)
+        w0 = time.perf_counter()
+        for _ in range(e_steps):
+            cimgs = fc.invert_corrected(4, vis4, ant, tof, sol, 4, n_t, n_ant)
+        c_ms = (time.perf_counter() - w0) * 1e3 / e_steps
+        # job 0 (facet 0, first group) against the plain batch on the oracle's
+        # gain-applied visibilities for facet 0
+        cvis = oracle.apply_gains(4, 4, vis4, ant, tof, sol[0], 4, n_ant)
+        ref0 = fb.invert(cvis)[0]
+        corrections = {
+            "ms_per_inversion": c_ms, "gvis_s": job_vis / (c_ms * 1e-3) / 1e9,
+            "uncorrected_e2e_ms": e_ms, "bind_s": round(cbind_s, 2),
+            "upload_bytes": int(vis4.nbytes + sol.nbytes + ant.nbytes + tof.nbytes),
+            "job0_vs_plain_on_oracle_gains_rel_l2": rel_l2(cimgs[0], ref0),
+            "note": "full-Jones per-facet solutions (37 tables), 4 correlations, host buffers"}
+        fc.close()
     fb.close()
     value = job_vis / (ms * 1e-3) / 1e9
     plain_value = job_vis / plain_s / 1e9
@@ -715,6 +753,7 @@ def run_facets(args):
                    "plain_one_at_a_time_gvis_s": plain_value,
                    "batched_over_plain": value / plain_value,
                    "checks": checks, "datagen_s": round(gen_s, 1),
+                   "direction_dependent_corrections": corrections,
                    "step": "one inversion of every facet x channel job (graph replay), device "
                            "visibilities in, device images out"},
         "clocks": clk,
@@ -976,6 +1015,12 @@ def run_resample(args):
     }
 
 
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 def _traffic(kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summaries
     (profiles/traffic.json), in GB, with where they come from."""
@@ -1097,6 +1142,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rows", type=int, default=200000)
     ap.add_argument("--cpu-planes", type=int, default=2)
+    ap.add_argument("--facet-corrections", action="store_true",
+                    help="also time the facet batch with per-facet full-Jones corrections")
     ap.add_argument("--facet-times", type=int, default=620,
                     help="time steps of the facet workload (6200 in the full workload)")
     ap.add_argument("--serve-requests", type=int, default=64,
