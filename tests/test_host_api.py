@@ -136,3 +136,53 @@ def test_constant_memory_formula_matches_reference():
     # gridder_simple_implementation.h:53-61: sigma_max^2 * w_t * h_t * 8 + w_t * h_t * sizeof(NumT)
     w_t, h_t = 1000, 800
     assert int(4.0 * w_t * h_t * 8) + w_t * h_t * 4 == 4 * 8 * 800_000 + 3_200_000
+
+
+def test_weighting_and_resampling_validate_then_need_a_device(wgpu_lib):
+    """Imaging weights, row preparation and resampling check their arguments
+    first (WGPU_ERR_INVALID) and fail loudly without a device (WGPU_ERR_CUDA):
+    there is no CPU fallback."""
+    import ctypes as C
+    from wsclean_gb300 import resample as wres
+    from wsclean_gb300.weights import ImageWeights
+    L = _lib.lib()
+    out = C.c_void_p()
+    for args in ((5, 0.0, 64, 64, 1e-3, 1e-3, 0, 1.0),    # weighting mode
+                 (1, 0.0, 64, 64, 0.0, 1e-3, 0, 1.0),    # pixel scale
+                 (1, 0.0, 64, 64, 1e-3, 1e-3, 0, 0.0),   # super weight
+                 (1, 0.0, 0, 64, 1e-3, 1e-3, 0, 1.0)):   # empty grid (odd sizes round up)
+        assert L.wgpu_imageweights_create(*args, C.byref(out)) == _lib.WGPU_ERR_INVALID
+    with pytest.raises(_lib.WgpuError) as e:
+        ImageWeights(1, 64, 64, 1e-3, 1e-3)
+    assert e.value.status == _lib.WGPU_ERR_CUDA
+    rw = _lib.RowWeighting(0, 0.0, 0.0, 0, 0, 0)
+    sums = _lib.WeightSums()
+    assert L.wgpu_prepare_rows(None, C.byref(rw), 1, 1, 1, None, None, None, None, None, None,
+                               None, None, None, C.byref(sums)) == _lib.WGPU_ERR_INVALID
+    assert L.wgpu_gridder_add_inversion_rows(None, None, C.byref(rw), 1, 1, 1, None, None, None,
+                                             None, None, None, None) == _lib.WGPU_ERR_INVALID
+    img = np.zeros((8, 8), np.float32)
+    with pytest.raises(_lib.WgpuError) as e:
+        wres.resample(img, 0, 8)
+    assert e.value.status == _lib.WGPU_ERR_INVALID
+    with pytest.raises(_lib.WgpuError) as e:
+        wres.resample(img, 16, 16)
+    assert e.value.status == _lib.WGPU_ERR_CUDA
+    with pytest.raises(_lib.WgpuError) as e:
+        wres.calculate_fft_size(100, 0.0, 1e-3)
+    assert e.value.status == _lib.WGPU_ERR_INVALID
+    assert L.wgpu_facets_invert_corrected(None, 4, 4, None, None, None, None, 4, 1, 1, 0,
+                                          None) == _lib.WGPU_ERR_INVALID
+    assert L.wgpu_gridder_finish_inversion(None, 8, 8, 8, 8, None) == _lib.WGPU_ERR_INVALID
+
+
+def test_sizing_functions_run_without_a_device(wgpu_lib):
+    """CalculateFFTSize, the small-inversion size and the gridder's trimmed
+    size are host functions."""
+    from wsclean_gb300 import resample as wres
+    assert wres.calculate_fft_size(1000, 1e-4, 1e-3) == (200, 200)
+    mn, opt = wres.calculate_fft_size(1000, 1e-4, 0.9e-3)
+    assert mn == 223 and opt % 4 == 0 and opt >= mn
+    assert wres.actual_trimmed_size(1000, 600, 1.2) == (836, 500)
+    w, h, px, py = wres.small_inversion_size(1000, 1000, 1e-4, 1e-4, 1e-3)
+    assert (w, h) == (200, 200) and abs(px - 5e-4) < 1e-15
