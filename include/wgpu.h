@@ -520,6 +520,8 @@ void wgpu_facets_destroy(wgpu_facets_t *facets);
 #define WGPU_TAPER_GAUSSIAN 6    /* SetGaussianTaper(a = beam size, radians) */
 #define WGPU_TAPER_RANK_FILTER 7 /* RankFilter(a = rank limit, b = window, <= 256) */
 
+/* An image-weights object, like a gridder, is used by one thread at a time
+ * (its float copy of the grid is refreshed on first use after a change). */
 typedef struct wgpu_imageweights wgpu_imageweights_t;
 
 /* ImageWeights(weightMode, imageWidth, imageHeight, pixelScaleX, pixelScaleY,
