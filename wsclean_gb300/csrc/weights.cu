@@ -797,7 +797,6 @@ RowWeighting row_weighting(const wgpu_row_weighting_t &rw) {
   r.polarization = rw.polarization;
   r.dl = rw.psf_dl;
   r.dm = rw.psf_dm;
-  r.dn = 0.0;  // formed on the device, rounded like the host expression
   return r;
 }
 

@@ -311,11 +311,11 @@ struct WeightGridView {
 };
 WeightGridView imageweights_view(const wgpu_imageweights_t *iw);
 
-// Per-call settings of the row preparation, with the PSF shift's n term
-// (sqrt(1 - dl^2 - dm^2) - 1) computed on the host.
+// Per-call settings of the row preparation (the PSF shift's n term is formed
+// on the device, rounded like the host expression).
 struct RowWeighting {
   int psf_mode, subtract_model, visibility_weighting, polarization;
-  double dl, dm, dn;
+  double dl, dm;
 };
 RowWeighting row_weighting(const wgpu_row_weighting_t &rw);
 
