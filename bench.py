@@ -864,7 +864,7 @@ def run_rowweights(args):
     bit_exact = bool(np.array_equal(ref_out, t_out[:n_s].cpu().numpy()))
     cpu_value = n_s * n_chan / cpu_s / 1e9
 
-    # roofline of prepare_rows_kernel<4>: per sample 4 weights (16 B), 4
+    # roofline of prepare_rows_fast_kernel<4, true>: per sample 4 weights (16 B), 4
     # correlations (32 B), the imaging-weight cell (8 B) and the output (8 B),
     # plus 24 B of uvw per row
     alg_bytes = n * (16 + 32 + 8 + 8) + n_rows * 24 + n_chan * 8
