@@ -25,14 +25,34 @@ _lib = None
 
 
 REF_FFTSIZE = os.path.join(HERE, "_ref", "libref_fftsize.so")
+CUDA_LIB_PATH = os.path.join(HERE, "_build", "liboracle_cuda.so")
+# The reference tree, read only to compile its header-only code into
+# oracle/_ref (absent on machines that only run the prebuilt files).
+REFERENCE_TREE = os.environ.get("WGPU_REFERENCE_TREE", "/root/reference")
+
+
+def _nvcc():
+    import shutil
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    return None
 
 
 def build():
     r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    nvcc = _nvcc()
+    if nvcc is not None:
+        r = subprocess.run(["make", "-C", HERE, "cuda", f"NVCC={nvcc}"], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle CUDA twin build failed:\n" + r.stdout + r.stderr)
     # the reference's own header-only code, where the reference tree exists
-    subprocess.run(["make", "-C", HERE, "ref"], capture_output=True, text=True)
+    if os.path.isdir(REFERENCE_TREE):
+        subprocess.run(["make", "-C", HERE, "ref", f"REFERENCE={REFERENCE_TREE}"],
+                       capture_output=True, text=True)
     return LIB_PATH
 
 
@@ -140,6 +160,85 @@ def dft_predict(uvw, freq, image, width, height, dl, dm, l_shift=0.0, m_shift=0.
                              height, dl, dm, l_shift, m_shift, _p(vis_index), vis_index.size,
                              n_threads, _p(out))
     return out[0::2] + 1j * out[1::2]
+
+
+_cuda_lib = None
+
+
+def cuda_lib():
+    """The FP64 direct-transform twin for the GPU (oracle/dft_cuda.cu)."""
+    global _cuda_lib
+    if _cuda_lib is None:
+        if not os.path.exists(CUDA_LIB_PATH):
+            build()
+        L = C.CDLL(CUDA_LIB_PATH)
+        P, SZ, D = C.c_void_p, C.c_size_t, C.c_double
+        L.oracle_cuda_last_error.restype = C.c_char_p
+        L.oracle_cuda_dft_invert.restype = C.c_int
+        L.oracle_cuda_dft_invert.argtypes = [SZ, SZ, P, P, P, SZ, SZ, D, D, D, D, P, SZ, P, P]
+        L.oracle_cuda_dft_predict.restype = C.c_int
+        L.oracle_cuda_dft_predict.argtypes = [SZ, SZ, P, P, P, SZ, SZ, D, D, D, D, P, P, P, P,
+                                              P]
+        _cuda_lib = L
+    return _cuda_lib
+
+
+def _ptr(a, dtype=None):
+    """Address of a numpy array (made contiguous in `dtype`) or of a torch tensor
+    (host or device; used in place).  Returns (address, keep-alive object)."""
+    if a is None:
+        return None, None
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr(), a
+    arr = np.ascontiguousarray(a, dtype) if dtype is not None else np.ascontiguousarray(a)
+    return arr.ctypes.data, arr
+
+
+def _cuda_check(r):
+    if r != 0:
+        raise RuntimeError("oracle CUDA twin: " + cuda_lib().oracle_cuda_last_error().decode())
+
+
+def cuda_dft_invert(uvw, freq, vis, width, height, dl, dm, l_shift=0.0, m_shift=0.0,
+                    pixels=None, n_rows=None, n_chan=None, stream=0):
+    """oracle_dft_invert on the GPU in FP64 (every row, selected pixels).  uvw
+    and vis may be numpy arrays or torch tensors (host or device)."""
+    freq = np.ascontiguousarray(freq, np.float64)
+    n_chan = freq.size if n_chan is None else n_chan
+    n_rows = uvw.shape[0] if n_rows is None else n_rows
+    if pixels is None:
+        pixels = np.arange(width * height, dtype=np.int64)
+    pixels = np.ascontiguousarray(pixels, np.int64)
+    pu, ku = _ptr(uvw, np.float64)
+    pv, kv = _ptr(vis, np.complex64)
+    out = np.zeros(pixels.size, np.float64)
+    _cuda_check(cuda_lib().oracle_cuda_dft_invert(n_rows, n_chan, pu, _p(freq), pv, width,
+                                                  height, dl, dm, l_shift, m_shift, _p(pixels),
+                                                  pixels.size, _p(out), stream))
+    return out
+
+
+def cuda_dft_predict(uvw, freq, image, width, height, dl, dm, l_shift=0.0, m_shift=0.0,
+                     mask=None, pred=None, want_values=False, n_rows=None, stream=0):
+    """oracle_dft_predict on the GPU in FP64 at every sample.  Returns
+    (values or None, sum |pred - ref|^2, sum |ref|^2) with the sums over the
+    samples where mask != 0 (every sample without a mask).  uvw, mask and pred
+    may be numpy arrays or torch tensors (host or device)."""
+    freq = np.ascontiguousarray(freq, np.float64)
+    image = np.ascontiguousarray(image, np.float64).ravel()
+    n_rows = uvw.shape[0] if n_rows is None else n_rows
+    pu, ku = _ptr(uvw, np.float64)
+    pm, km = _ptr(mask, np.uint8)
+    pp, kp = _ptr(pred, np.complex64)
+    vals = np.zeros(n_rows * freq.size, np.complex128) if want_values else None
+    sums = np.zeros(2, np.float64)
+    _cuda_check(cuda_lib().oracle_cuda_dft_predict(n_rows, freq.size, pu, _p(freq), _p(image),
+                                                   width, height, dl, dm, l_shift, m_shift, pm,
+                                                   pp, None if vals is None else _p(vals),
+                                                   _p(sums), stream))
+    return vals, float(sums[0]), float(sums[1])
 
 
 def bucket(plan, uvw, freq, vis, skip_zero):
