@@ -186,35 +186,51 @@ def survey_request_bytes(p, n_vis, n_rows):
 
 
 # ------------------------------------------------------------ CPU baseline ---
-def cpu_baseline(d, vis_rows, plan, n_vis_total, sample_rows, n_planes_timed, seed=3):
-    """Times the oracle's FP64 CPU w-gridder (all host threads) on a bounded
-    sample: spreading of a random row subset over every plane it touches, and
-    n_planes_timed plane FFT + w-screen passes; extrapolates to the workload.
-    vis_rows(rows) returns the visibilities of the sampled rows."""
+def cpu_sample_step(d, plan, vis_rows, n_baselines, plane_fraction, seed):
+    """One bounded CPU step on a sample of the workload: the oracle's FP64 CPU
+    w-gridder (all host threads) grids, then predicts, the samples of
+    n_baselines random baselines (every time step and channel: whole uv
+    tracks, so the sample keeps the data's locality along a track) over all
+    the planes they touch, and runs plane_fraction of one plane pass in each
+    direction.  Returns (measured seconds, extrapolated seconds of the whole
+    inversion + prediction, sample description).  vis_rows(rows) returns the
+    visibilities of the sampled rows (zero where the sample is not gridded)."""
     import oracle
     rng = np.random.default_rng(seed)
     n_rows = d["uvw"].shape[0]
-    rows = np.sort(rng.choice(n_rows, size=min(sample_rows, n_rows), replace=False))
+    n_bl = d["n_ant"] * (d["n_ant"] - 1) // 2
+    n_t = -(-n_rows // n_bl)
+    bls = np.sort(rng.choice(n_bl, size=min(n_baselines, n_bl), replace=False))
+    rows = (np.arange(n_t)[:, None] * n_bl + bls[None, :]).ravel()
+    rows = np.sort(rows[rows < n_rows])
     uvw = d["uvw"][rows]
     vis = vis_rows(rows)
     n_sample = int(np.count_nonzero(vis))
     cores = os.cpu_count()
-    t_vis, t_planes = oracle.wgrid_time_parts(plan, uvw, d["freq"], vis, n_threads=cores,
-                                              n_planes_timed=n_planes_timed)
-    per_vis = t_vis / max(n_sample, 1)
-    per_plane = t_planes / n_planes_timed
+    w0 = time.perf_counter()
+    t_grid, t_pi = oracle.wgrid_time_parts(plan, uvw, d["freq"], vis, n_threads=cores,
+                                           plane_fraction=plane_fraction)
+    t_degrid, t_pp = oracle.wgrid_time_predict_parts(plan, uvw, d["freq"], vis, n_threads=cores,
+                                                     plane_fraction=plane_fraction)
+    wall = time.perf_counter() - w0
     n_gridded = int(d["n_gridded"])
-    t_grid = per_vis * n_gridded + per_plane * plan.n_planes
-    # the degrid pass moves the same data in the other direction: charged equal
-    t_step = 2.0 * t_grid
-    return dict(value=n_vis_total / t_step / 1e9, unit="Gvis/s", cores=cores, kind="port",
-                sample=(f"FP64 CPU w-gridder (oracle port, {cores} threads): {rows.size} rows "
-                        f"({n_sample} non-zero vis) spread over all their planes in "
-                        f"{t_vis:.2f} s, {n_planes_timed} plane FFT+screen passes of "
-                        f"{plan.nu}x{plan.nv} in {t_planes:.2f} s; extrapolated to "
-                        f"{n_gridded} vis x {plan.n_planes} planes, degrid charged equal "
-                        f"to grid"),
-                seconds_per_step=t_step)
+    n_planes = int(plan["n_planes"])
+    full = ((t_grid + t_degrid) * n_gridded / max(n_sample, 1) +
+            (t_pi + t_pp) / plane_fraction * n_planes)
+    text = (f"FP64 CPU w-gridder (oracle port, {cores} threads): {bls.size} random baselines "
+            f"x {n_t} time steps ({rows.size} rows, {n_sample} gridded samples) gridded in "
+            f"{t_grid:.2f} s and predicted in {t_degrid:.2f} s over all their planes; "
+            f"{plane_fraction:g} of one {plan['nu']}x{plan['nv']} plane pass in each direction "
+            f"in {t_pi:.2f} s + {t_pp:.2f} s; extrapolated to {n_gridded} samples x "
+            f"{n_planes} planes per direction ({full:.0f} s per inversion + prediction)")
+    return wall, full, text
+
+
+def cpu_baseline(d, vis_rows, plan, n_vis_total, n_baselines, plane_fraction, seed=3):
+    """The CPU baseline of the GPU arm: one bounded CPU step (cpu_sample_step)."""
+    wall, full, text = cpu_sample_step(d, plan, vis_rows, n_baselines, plane_fraction, seed)
+    return dict(value=n_vis_total / full / 1e9, unit="Gvis/s", cores=os.cpu_count(),
+                kind="port", sample=text, seconds_measured=round(wall, 2))
 
 
 def accuracy_full(d, g, d_out, n_pix=4096, cpu_rows=20000, cpu_pix=64, seed=4):
@@ -476,8 +492,8 @@ def run_gpu(args, rank, world, local):
         free_b, _ = torch.cuda.mem_get_info()
         result["serving"] = run_serving(args, 0.7 * free_b)
     if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(d, lambda r: d["h_vis"][r], plan_inv, n_vis,
-                                              args.cpu_sample_rows, args.cpu_planes)
+        result["cpu_baseline"] = cpu_baseline(d, lambda r: d["h_vis"][r], plan_inv.as_dict(),
+                                              n_vis, args.cpu_baselines, args.cpu_plane_fraction)
         result["cpu_baseline"].pop("seconds_per_step", None)
     g.close()
     return result
@@ -1104,13 +1120,22 @@ def run_serving(args, device_bytes):
 
 # ---------------------------------------------------------- reference arm ---
 def run_reference(args):
-    """CPU implementation of the path (the oracle's FP64 w-gridder port; the
-    reference's own wgridder is ducc0, which is absent from the reference tree
-    and cannot be built here), timed on all host cores, each step a bounded
-    sample of the same workload, extrapolated to the metric."""
-    from wsclean_gb300 import _lib, synthetic
+    """The CPU implementation of the path on the host cores: the reference's own
+    w-gridder is ducc0, which is absent from the reference tree and cannot be
+    built here, so the oracle's FP64 CPU w-gridder port is timed instead.  This
+    arm loads only oracle code: the gridding plan (grid size, support, w
+    planes) comes from oracle/plans.json, the planner's choices for this
+    workload recorded beside the oracle, not from the product library.  Each
+    step is one bounded sample (cpu_sample_step): both directions timed, the
+    step's own wall time reported as ms_per_step, the rate extrapolated from
+    the sample to the whole workload as value."""
+    from oracle import make_plans
+    from wsclean_gb300 import synthetic
+    if args.workload not in make_plans.WORKLOADS:
+        return {"impl": "reference", "unavailable": f"no recorded plan for {args.workload}"}
     d = synthetic.make_workload(args.workload, seed=2, max_rows=args.max_rows, with_model=False)
     n_rows, n_chan = d["uvw"].shape[0], d["freq"].size
+    plan = make_plans.load(args.workload)
 
     def vis_rows(rows):
         # random unit-variance visibilities on the non-flagged samples
@@ -1120,30 +1145,37 @@ def run_reference(args):
         return np.where(w > 0, v, 0).astype(np.complex64)
 
     d["n_gridded"] = int(np.count_nonzero(d["weights"]))
-    keep = d["weights"] > 0
-    wl = d["uvw"][:, 2:3] * (d["freq"] / 299792458.0)[None, :]
-    plan = _lib.make_plan(width=d["width"], height=d["height"], dl=d["dl"], dm=d["dl"],
-                          epsilon=d["epsilon"], w_min=float(wl[keep].min()),
-                          w_max=float(wl[keep].max()), n_vis=d["n_gridded"])
-    vals = []
+    walls, rates, texts = [], [], []
+    w_start = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(d, vis_rows, plan, n_rows * n_chan, args.cpu_sample_rows // 2, 1,
-                          seed=100 + i)
+        wall, full, text = cpu_sample_step(d, plan, vis_rows, args.ref_baselines,
+                                           args.ref_plane_fraction, seed=100 + i)
         if i >= args.warmup:
-            vals.append(cb)
-    v = float(np.median([c["value"] for c in vals]))
-    ms = float(np.median([c["seconds_per_step"] for c in vals])) * 1e3
-    cb = vals[-1]
-    cb.pop("seconds_per_step", None)
-    cb["value"] = v
+            walls.append(wall)
+            rates.append(n_rows * n_chan / full / 1e9)
+            texts.append(text)
+    timed_s = float(np.sum(walls))
+    v = float(np.median(rates))
+    ms = timed_s * 1e3 / args.steps
+    cores = os.cpu_count()
+    cb = {"value": v, "unit": "Gvis/s", "cores": cores, "kind": "port",
+          "sample": (f"per step: {texts[-1]}; value = median over the {args.steps} timed steps "
+                     "of the extrapolated rate")}
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gvis/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
             "data": "synthetic",
             "config": {"workload": WORKLOAD_TEXT.get(args.workload, args.workload),
                        "n_vis": n_rows * n_chan, "n_vis_gridded": d["n_gridded"],
+                       "plan": {k: plan[k] for k in ("nu", "support", "sigma", "n_planes")},
+                       "plan_source": "oracle/plans.json (recorded planner output; the product "
+                                      "library is not loaded by this arm)",
+                       "timed_region_s": round(timed_s, 2),
+                       "arm_wall_s": round(time.perf_counter() - w_start, 2),
                        "note": "ducc0 (the reference's wgridder) is absent from the reference "
-                               "tree; the FP64 CPU restatement is timed instead"},
+                               "tree; the oracle's FP64 CPU w-gridder port is timed instead. "
+                               "ms_per_step is the measured time of one sample step; value is "
+                               "the workload rate extrapolated from the samples"},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "Gvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -1160,8 +1192,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the full-data error against the FP64 direct transform")
-    ap.add_argument("--cpu-sample-rows", type=int, default=200000)
-    ap.add_argument("--cpu-planes", type=int, default=2)
+    ap.add_argument("--cpu-sample-rows", type=int, default=200000,
+                    help="rows of the raw-row weighting CPU sample")
+    ap.add_argument("--cpu-baselines", type=int, default=200,
+                    help="baselines (all time steps) in the CPU baseline's sample")
+    ap.add_argument("--cpu-plane-fraction", type=float, default=0.25,
+                    help="fraction of one plane pass per direction in the CPU baseline")
+    ap.add_argument("--ref-baselines", type=int, default=48,
+                    help="baselines per step of the reference arm's CPU sample")
+    ap.add_argument("--ref-plane-fraction", type=float, default=1.0 / 16,
+                    help="fraction of one plane pass per direction per reference step")
     ap.add_argument("--facet-corrections", action="store_true",
                     help="also time the facet batch with per-facet full-Jones corrections")
     ap.add_argument("--facet-times", type=int, default=620,

@@ -86,8 +86,11 @@ def lib():
         L.oracle_wgrid_invert.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, P]
         L.oracle_wgrid_predict.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, P]
         L.oracle_wgrid_time_parts.restype = D
-        L.oracle_wgrid_time_parts.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, I,
+        L.oracle_wgrid_time_parts.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P, I, D,
                                               C.POINTER(D)]
+        L.oracle_wgrid_time_predict_parts.restype = D
+        L.oracle_wgrid_time_predict_parts.argtypes = [C.POINTER(OraclePlan), SZ, SZ, P, P, P,
+                                                      I, D, C.POINTER(D)]
         L.oracle_es_kernel.restype = D
         L.oracle_es_kernel.argtypes = [D, D]
         L.oracle_es_fourier.restype = D
@@ -286,14 +289,30 @@ def wgrid_predict(plan, uvw, freq, image, n_threads=0):
     return out[0::2] + 1j * out[1::2]
 
 
-def wgrid_time_parts(plan, uvw, freq, vis, n_threads=0, n_planes_timed=1):
+def wgrid_time_parts(plan, uvw, freq, vis, n_threads=0, plane_fraction=1.0):
+    """Seconds of the CPU inversion's spreading of the samples with vis != 0
+    over all their planes, and of plane_fraction of one plane pass."""
     op = to_oracle_plan(plan)
     uvw = np.ascontiguousarray(uvw, np.float64)
     freq = np.ascontiguousarray(freq, np.float64)
     vis = np.ascontiguousarray(vis, np.complex64)
     ps = C.c_double()
     t = lib().oracle_wgrid_time_parts(C.byref(op), uvw.shape[0], freq.size, _p(uvw), _p(freq),
-                                      _p(vis), n_threads, n_planes_timed, C.byref(ps))
+                                      _p(vis), n_threads, float(plane_fraction), C.byref(ps))
+    return t, ps.value
+
+
+def wgrid_time_predict_parts(plan, uvw, freq, vis, n_threads=0, plane_fraction=1.0):
+    """Seconds of the CPU prediction's interpolation of the samples with
+    vis != 0 over all their planes, and of plane_fraction of one plane pass."""
+    op = to_oracle_plan(plan)
+    uvw = np.ascontiguousarray(uvw, np.float64)
+    freq = np.ascontiguousarray(freq, np.float64)
+    vis = np.ascontiguousarray(vis, np.complex64)
+    ps = C.c_double()
+    t = lib().oracle_wgrid_time_predict_parts(C.byref(op), uvw.shape[0], freq.size, _p(uvw),
+                                              _p(freq), _p(vis), n_threads,
+                                              float(plane_fraction), C.byref(ps))
     return t, ps.value
 
 

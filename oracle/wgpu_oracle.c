@@ -496,16 +496,33 @@ static void correction_table(const OraclePlan *P, const double *nu_w,
   free(cy);
 }
 
-/* grid all vis touching plane p into grid (nv x nu complex doubles). */
+/* Row stripes of the grid: samples whose footprint starts in stripe s write
+ * rows [s * stripe, s * stripe + stripe + W - 1), so stripes two apart never
+ * share a row and can be gridded by different threads. */
+static int64_t stripe_rows(const OraclePlan *P) {
+  return 64 > P->support ? 64 : P->support;
+}
+static int64_t stripe_count(const OraclePlan *P) {
+  const int64_t n = P->nv / stripe_rows(P);
+  return n > 0 ? n : 1;
+}
+static int64_t stripe_of(const OraclePlan *P, int64_t iv) {
+  const int64_t s = iv / stripe_rows(P);
+  return s < stripe_count(P) ? s : stripe_count(P) - 1;
+}
+
+/* grid all vis touching plane p into grid (nv x nu complex doubles).  sorder /
+ * sstart list the samples of first plane q and stripe s (index
+ * q * n_stripes + s) by footprint corner; every cell therefore receives its
+ * samples in ascending (first plane, corner, sample) order. */
 static void grid_plane(const OraclePlan *P, const GridVis *g, size_t n,
-                       const size_t *order, const size_t *pstart, int p,
+                       const size_t *sorder, const size_t *sstart, int p,
                        double *grid, int clear) {
   const int W = (int)P->support, nW = plane_count_w(P);
   const int64_t nu = P->nu, nv = P->nv;
   if (clear) memset(grid, 0, sizeof(double) * 2 * nu * nv);
   /* vis with ip in [p - nW + 1, p]; grouped by stripe parity for threads */
-  const int64_t stripe = 64 > W ? 64 : W;
-  const int64_t n_stripes = nv / stripe > 0 ? nv / stripe : 1;
+  const int64_t n_stripes = stripe_count(P);
   for (int color = 0; color < 3; ++color) {
 #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t s = 0; s < n_stripes; ++s) {
@@ -514,11 +531,9 @@ static void grid_plane(const OraclePlan *P, const GridVis *g, size_t n,
       if (c != color) continue;
       for (int q = p - nW + 1; q <= p; ++q) {
         if (q < 0) continue;
-        for (size_t ii = pstart[q]; ii < pstart[q + 1]; ++ii) {
-          const GridVis *v = &g[order[ii]];
-          int64_t vs = v->iv / stripe;
-          if (vs >= n_stripes) vs = n_stripes - 1;
-          if (vs != s) continue;
+        const size_t b = (size_t)q * (size_t)n_stripes + (size_t)s;
+        for (size_t ii = sstart[b]; ii < sstart[b + 1]; ++ii) {
+          const GridVis *v = &g[sorder[ii]];
           const double kwv = v->kw[p - q];
           for (int j = 0; j < W; ++j) {
             const int64_t row = (v->iv + j) % nv;
@@ -599,6 +614,48 @@ static void sort_by_plane(const OraclePlan *P, const GridVis *g, size_t n,
   *pstart = st;
 }
 
+typedef struct {
+  int64_t corner; /* iv * nu + iu */
+  size_t index;
+} CornerKey;
+
+static int corner_cmp(const void *a, const void *b) {
+  const CornerKey *x = (const CornerKey *)a, *y = (const CornerKey *)b;
+  if (x->corner != y->corner) return x->corner < y->corner ? -1 : 1;
+  return x->index < y->index ? -1 : (x->index > y->index);
+}
+
+/* Counting sort of the samples by (first plane, stripe), each bucket ordered
+ * by footprint corner (iv, iu) and then by sample index, so that a thread
+ * walks its stripe's cells in address order: sorder lists the samples,
+ * sstart[q * n_stripes + s] is where bucket (q, s) begins. */
+static void sort_by_plane_stripe(const OraclePlan *P, const GridVis *g, size_t n,
+                                 size_t **sorder, size_t **sstart) {
+  const size_t ns = (size_t)stripe_count(P);
+  const size_t nb = (size_t)P->n_planes * ns;
+  size_t *st = calloc(nb + 2, sizeof(size_t));
+  for (size_t i = 0; i < n; ++i)
+    st[(size_t)g[i].ip * ns + (size_t)stripe_of(P, g[i].iv) + 1]++;
+  for (size_t b = 0; b < nb; ++b) st[b + 1] += st[b];
+  size_t *cur = malloc(sizeof(size_t) * (nb + 1));
+  memcpy(cur, st, sizeof(size_t) * (nb + 1));
+  CornerKey *k = malloc(sizeof(CornerKey) * (n + 1));
+  for (size_t i = 0; i < n; ++i) {
+    CornerKey *e = &k[cur[(size_t)g[i].ip * ns + (size_t)stripe_of(P, g[i].iv)]++];
+    e->corner = g[i].iv * P->nu + g[i].iu;
+    e->index = i;
+  }
+  free(cur);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (size_t b = 0; b < nb; ++b)
+    if (st[b + 1] - st[b] > 1) qsort(k + st[b], st[b + 1] - st[b], sizeof(CornerKey), corner_cmp);
+  size_t *o = malloc(sizeof(size_t) * (n + 1));
+  for (size_t i = 0; i < n; ++i) o[i] = k[i].index;
+  free(k);
+  *sorder = o;
+  *sstart = st;
+}
+
 int oracle_wgrid_invert(const OraclePlan *P, size_t n_rows, size_t n_chan,
                         const double *uvw, const double *freq, const float *vis,
                         int n_threads, double *dirty) {
@@ -611,7 +668,7 @@ int oracle_wgrid_invert(const OraclePlan *P, size_t n_rows, size_t n_chan,
   size_t n;
   if (prepare_vis(P, n_rows, n_chan, uvw, freq, vis, 1, &g, &n)) return -1;
   size_t *order, *pstart;
-  sort_by_plane(P, g, n, &order, &pstart);
+  sort_by_plane_stripe(P, g, n, &order, &pstart);
   const int64_t W = P->width, H = P->height;
   double *grid = malloc(sizeof(double) * 2 * P->nu * P->nv);
   double *img = malloc(sizeof(double) * 2 * W * H);
@@ -740,50 +797,183 @@ int oracle_wgrid_predict(const OraclePlan *P, size_t n_rows, size_t n_chan,
   return 0;
 }
 
+/* Rows and columns of one plane pass that a timing run of `fraction` of a
+ * pass transforms (at least one of each). */
+static int64_t timed_count(int64_t total, double fraction) {
+  int64_t k = (int64_t)ceil(fraction * (double)total);
+  if (k < 1) k = 1;
+  return k < total ? k : total;
+}
+
 double oracle_wgrid_time_parts(const OraclePlan *P, size_t n_rows,
                                size_t n_chan, const double *uvw,
                                const double *freq, const float *vis,
-                               int n_threads, int n_planes_timed,
+                               int n_threads, double plane_fraction,
                                double *plane_seconds) {
   if (n_threads > 0) omp_set_num_threads(n_threads);
+  const int64_t nu = P->nu, nv = P->nv, W = P->width, H = P->height;
+  FftPlan pu, pv;
+  if (fft_plan((int)nu, &pu) || fft_plan((int)nv, &pv)) return -1.0;
   const double t0 = omp_get_wtime();
   GridVis *g;
   size_t n;
   if (prepare_vis(P, n_rows, n_chan, uvw, freq, vis, 1, &g, &n)) return -1.0;
   size_t *order, *pstart;
-  sort_by_plane(P, g, n, &order, &pstart);
-  double *grid = calloc(2 * P->nu * P->nv, sizeof(double));
+  sort_by_plane_stripe(P, g, n, &order, &pstart);
+  double *grid = calloc(2 * nu * nv, sizeof(double));
   /* spreading cost of every sample over all the planes it touches (the
    * per-plane clearing is charged to the plane part below) */
   for (int p = 0; p < P->n_planes; ++p)
     grid_plane(P, g, n, order, pstart, p, grid, 0);
   const double t1 = omp_get_wtime();
-  const int64_t W = P->width, H = P->height;
-  double *img = malloc(sizeof(double) * 2 * W * H);
   double *nu_w = malloc(sizeof(double) * W * H);
   double *dirty = calloc(W * H, sizeof(double));
   pixel_nu_table(P, nu_w);
+  const int64_t rows_t = timed_count(nv, plane_fraction);
+  const int64_t cols_t = timed_count(W, plane_fraction);
+  const double wp = P->w0;
   const double t2 = omp_get_wtime();
-  for (int p = 0; p < n_planes_timed; ++p) {
-    memset(grid, 0, sizeof(double) * 2 * P->nu * P->nv);
-    fft_forward_crop(P, grid, img);
-    const double wp = P->w0 + (double)p * P->dw;
-#pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < W * H; ++i) {
-      double s, c;
-      sincos_turns(wp * nu_w[i], &s, &c);
-      dirty[i] += img[2 * i] * c + img[2 * i + 1] * s;
+  /* `plane_fraction` of one inversion plane pass (fft_forward_crop plus the
+   * screen): clear and transform rows_t rows, then cols_t cropped columns,
+   * screened and accumulated into their pixels */
+  memset(grid, 0, sizeof(double) * 2 * nu * rows_t);
+#pragma omp parallel
+  {
+    double *tmp = malloc(sizeof(double) * 2 * (nu > nv ? nu : nv));
+    double *col = malloc(sizeof(double) * 2 * nv);
+#pragma omp for schedule(static)
+    for (int64_t r = 0; r < rows_t; ++r) fft_run(&pu, grid + 2 * r * nu, tmp, -1);
+#pragma omp for schedule(static)
+    for (int64_t x = 0; x < cols_t; ++x) {
+      const int64_t a = (((W / 2 - x) % nu) + nu) % nu;
+      for (int64_t b = 0; b < nv; ++b) {
+        col[2 * b] = grid[2 * (b * nu + a)];
+        col[2 * b + 1] = grid[2 * (b * nu + a) + 1];
+      }
+      fft_run(&pv, col, tmp, -1);
+      for (int64_t y = 0; y < H; ++y) {
+        const int64_t bb = (((y - H / 2) % nv) + nv) % nv;
+        const int64_t i = x + y * W;
+        double sn, cs;
+        sincos_turns(wp * nu_w[i], &sn, &cs);
+        dirty[i] += col[2 * bb] * cs + col[2 * bb + 1] * sn;
+      }
     }
+    free(tmp);
+    free(col);
   }
   const double t3 = omp_get_wtime();
   *plane_seconds = t3 - t2;
   free(grid);
-  free(img);
   free(nu_w);
   free(dirty);
   free(order);
   free(pstart);
   free(g);
+  fft_free(&pu);
+  fft_free(&pv);
+  return t1 - t0;
+}
+
+double oracle_wgrid_time_predict_parts(const OraclePlan *P, size_t n_rows,
+                                       size_t n_chan, const double *uvw,
+                                       const double *freq, const float *vis,
+                                       int n_threads, double plane_fraction,
+                                       double *plane_seconds) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+  const int64_t W = P->width, H = P->height, nu = P->nu, nv = P->nv;
+  const int nW = plane_count_w(P), Ws = (int)P->support;
+  FftPlan pu, pv;
+  if (fft_plan((int)nu, &pu) || fft_plan((int)nv, &pv)) return -1.0;
+  /* a plane in real (written) memory, so that the interpolation reads real
+   * pages rather than the kernel's shared zero page */
+  double *grid = malloc(sizeof(double) * 2 * nu * nv);
+  memset(grid, 0, sizeof(double) * 2 * nu * nv);
+  const double t0 = omp_get_wtime();
+  GridVis *g;
+  size_t n;
+  /* the samples a masked prediction evaluates (vis != 0) */
+  if (prepare_vis(P, n_rows, n_chan, uvw, freq, vis, 1, &g, &n)) return -1.0;
+  size_t *order, *pstart;
+  sort_by_plane(P, g, n, &order, &pstart);
+  double *acc = calloc(2 * n + 2, sizeof(double));
+  /* interpolation of every sample over all the planes it touches, as in
+   * oracle_wgrid_predict (the plane transforms are charged below) */
+  for (int p = 0; p < P->n_planes; ++p) {
+    for (int q = p - nW + 1; q <= p; ++q) {
+      if (q < 0) continue;
+#pragma omp parallel for schedule(static)
+      for (size_t ii = pstart[q]; ii < pstart[q + 1]; ++ii) {
+        const size_t k = order[ii];
+        const GridVis *v = &g[k];
+        const double kwv = v->kw[p - q];
+        double sr = 0.0, si = 0.0;
+        for (int j = 0; j < Ws; ++j) {
+          const int64_t row = (v->iv + j) % nv;
+          const double wy = kwv * v->ky[j];
+          const double *gr = grid + 2 * row * nu;
+          for (int i = 0; i < Ws; ++i) {
+            const int64_t col = (v->iu + i) % nu;
+            const double wt = wy * v->kx[i];
+            sr += wt * gr[2 * col];
+            si += wt * gr[2 * col + 1];
+          }
+        }
+        acc[2 * k] += sr;
+        acc[2 * k + 1] += si;
+      }
+    }
+  }
+  const double t1 = omp_get_wtime();
+  double *nu_w = malloc(sizeof(double) * W * H);
+  double *corr = calloc(W * H, sizeof(double));
+  pixel_nu_table(P, nu_w);
+  memset(grid, 0, sizeof(double) * 2 * nu * nv);
+  const double t2 = omp_get_wtime();
+  /* `plane_fraction` of one prediction plane pass: the screened image into
+   * cols_t of its columns with their inverse column FFTs, then rows_t inverse
+   * row FFTs */
+  const int64_t rows_t = timed_count(nv, plane_fraction);
+  const int64_t cols_t = timed_count(W, plane_fraction);
+  const double wp = P->w0;
+#pragma omp parallel
+  {
+    double *col = malloc(sizeof(double) * 2 * nv);
+    double *tmp = malloc(sizeof(double) * 2 * (nu > nv ? nu : nv));
+#pragma omp for schedule(static)
+    for (int64_t x = 0; x < cols_t; ++x) {
+      memset(col, 0, sizeof(double) * 2 * nv);
+      for (int64_t y = 0; y < H; ++y) {
+        const int64_t i = x + y * W;
+        double s, c;
+        sincos_turns(wp * nu_w[i], &s, &c);
+        const int64_t bb = (((y - H / 2) % nv) + nv) % nv;
+        col[2 * bb] = corr[i] * c;
+        col[2 * bb + 1] = corr[i] * s;
+      }
+      fft_run(&pv, col, tmp, +1);
+      const int64_t a = (((W / 2 - x) % nu) + nu) % nu;
+      for (int64_t b = 0; b < nv; ++b) {
+        grid[2 * (b * nu + a)] = col[2 * b];
+        grid[2 * (b * nu + a) + 1] = col[2 * b + 1];
+      }
+    }
+#pragma omp for schedule(static)
+    for (int64_t r = 0; r < rows_t; ++r) fft_run(&pu, grid + 2 * r * nu, tmp, +1);
+    free(col);
+    free(tmp);
+  }
+  const double t3 = omp_get_wtime();
+  *plane_seconds = t3 - t2;
+  free(grid);
+  free(acc);
+  free(nu_w);
+  free(corr);
+  free(order);
+  free(pstart);
+  free(g);
+  fft_free(&pu);
+  fft_free(&pv);
   return t1 - t0;
 }
 

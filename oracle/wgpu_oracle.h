@@ -90,13 +90,24 @@ int oracle_wgrid_predict(const OraclePlan *plan, size_t n_rows, size_t n_chan,
 
 /* Timing helper for the CPU baseline: grids (no FFT) the included visibilities
  * onto the planes they touch, in FP64, and returns seconds spent; and runs
- * n_planes_timed full plane FFT+screen steps, returning seconds spent in
- * *plane_seconds. */
+ * plane_fraction (0 < f <= 1) of one inversion plane pass (the row FFTs and
+ * cropped column FFTs + screen of that fraction of rows and columns),
+ * returning its seconds in *plane_seconds. */
 double oracle_wgrid_time_parts(const OraclePlan *plan, size_t n_rows,
                                size_t n_chan, const double *uvw,
                                const double *freq, const float *vis,
-                               int n_threads, int n_planes_timed,
+                               int n_threads, double plane_fraction,
                                double *plane_seconds);
+
+/* The prediction's counterpart: interpolates the samples with vis != 0 from
+ * the planes they touch (no FFT), in FP64, returning seconds spent; and runs
+ * plane_fraction of one prediction plane pass (screen, inverse column and row
+ * FFTs), returning its seconds in *plane_seconds. */
+double oracle_wgrid_time_predict_parts(const OraclePlan *plan, size_t n_rows,
+                                       size_t n_chan, const double *uvw,
+                                       const double *freq, const float *vis,
+                                       int n_threads, double plane_fraction,
+                                       double *plane_seconds);
 
 /* ES kernel value at z in [-1,1] and its continuous FT in cell units. */
 double oracle_es_kernel(double beta, double z);
