@@ -265,6 +265,8 @@ int64_t oracle_bucket(const OraclePlan *P, size_t n_rows, size_t n_chan,
       (P->nu / P->tile) * (P->nv / P->tile) * 4 * P->n_planes;
   const size_t n_el = n_rows * n_chan;
   int64_t *ekey = malloc(sizeof(int64_t) * (n_el + 1));
+  uint8_t *ecorner = malloc(n_el + 1);
+  size_t corner_count[257] = {0};
   memset(offsets, 0, sizeof(int64_t) * (n_keys + 1));
   for (size_t r = 0; r < n_rows; ++r)
     for (size_t c = 0; c < n_chan; ++c) {
@@ -276,16 +278,28 @@ int64_t oracle_bucket(const OraclePlan *P, size_t n_rows, size_t n_chan,
       Footprint f;
       footprint(P, su, sv, sw, inv_dw, uvw + 3 * r, c, &f);
       ekey[e] = f.key;
+      /* the footprint corner inside its tile, the order within a key */
+      ecorner[e] = (uint8_t)((f.iv % P->tile) * P->tile + f.iu % P->tile);
+      corner_count[ecorner[e] + 1]++;
       offsets[f.key + 1]++;
     }
+  /* stable order by corner, then a stable counting sort by key over it: the
+   * samples come out by (key, corner, element index) */
+  for (int b = 0; b < 256; ++b) corner_count[b + 1] += corner_count[b];
+  size_t *by_corner = malloc(sizeof(size_t) * (n_el + 1));
+  for (size_t e = 0; e < n_el; ++e)
+    if (ekey[e] >= 0) by_corner[corner_count[ecorner[e]]++] = e;
+  const size_t n_kept = corner_count[255];
   for (int64_t k = 0; k < n_keys; ++k) offsets[k + 1] += offsets[k];
   int64_t *cursor = malloc(sizeof(int64_t) * (n_keys + 1));
   memcpy(cursor, offsets, sizeof(int64_t) * (n_keys + 1));
-  for (size_t e = 0; e < n_el; ++e) {
-    if (ekey[e] < 0) continue;
+  for (size_t i = 0; i < n_kept; ++i) {
+    const size_t e = by_corner[i];
     const int64_t s = cursor[ekey[e]]++;
     perm[s] = (uint32_t)e;
   }
+  free(by_corner);
+  free(ecorner);
   const int64_t n_out = offsets[n_keys];
   for (int64_t s = 0; s < n_out; ++s) {
     const size_t e = perm[s];

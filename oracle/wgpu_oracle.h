@@ -66,7 +66,9 @@ typedef struct {
 
 /* Bucketing reference: for every included element (inversion: vis != 0;
  * prediction: all) computes the integer footprint corner, fractions and key
- * exactly as the GPU pass defines them, then stable counting-sorts by key.
+ * exactly as the GPU pass defines them, then orders the elements by (key,
+ * footprint corner inside the tile as (iv mod tile) * tile + iu mod tile,
+ * element index).
  * Outputs (n_out elements): perm[s] = element index, key[s], iu/iv/ip, fu/fv/fw.
  * offsets has n_tiles*n_planes+1 entries.  Returns n_out. */
 int64_t oracle_bucket(const OraclePlan *plan, size_t n_rows, size_t n_chan,

@@ -70,7 +70,11 @@ def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
     g.FinalizeImage(1.0)
     py_rows = g.RealImage().reshape(W, W)[d:d + Wt, d:d + Wt]
     rows = np.fromfile(prefix + "rows.bin", np.float32).reshape(W, W)[d:d + Wt, d:d + Wt]
-    np.testing.assert_allclose(rows, py_rows, rtol=0, atol=1e-6 * np.abs(py_rows).max())
+    # the same rows on the same plan through two front ends: the gridding kernel
+    # adds footprints into its shared-memory tile with float atomics, so the two
+    # runs differ only in the order of float additions (FP32 rounding, which the
+    # grid correction magnifies at the image border)
+    assert np.linalg.norm(rows - py_rows) <= 1e-6 * np.linalg.norm(py_rows)
     s4 = np.fromfile(prefix + "sums.bin", np.float64)
     assert s4[3] == sums.gridded_visibility_count > 0
     # uniform diagonal gain 1.5+0.5i, XX mode: |g|^2 = 2.5 times the prediction

@@ -169,10 +169,11 @@ def test_bucket_golden_fixture(oracle_lib):
     b = oracle_lib.bucket(plan, g["uvw"], g["freq"], g["vis"], True)
     for k in ("perm", "key", "iu", "iv", "ip", "fu", "fv", "fw", "offsets"):
         np.testing.assert_array_equal(b[k], g[k], err_msg=k)
-    # properties: sorted keys, stable (perm increasing within a key), offsets
-    assert np.all(np.diff(b["key"]) >= 0)
-    same = np.diff(b["key"]) == 0
-    assert np.all(np.diff(b["perm"].astype(np.int64))[same] > 0)
+    # properties: sorted by (key, corner inside the tile, element index), offsets
+    tile = int(plan["tile"])
+    corner = (b["iv"] % tile) * tile + b["iu"] % tile
+    order = np.lexsort((b["perm"], corner, b["key"]))
+    np.testing.assert_array_equal(order, np.arange(b["perm"].size))
     assert b["offsets"][-1] == b["perm"].size
     assert np.all(g["vis"].ravel()[b["perm"]] != 0)
 

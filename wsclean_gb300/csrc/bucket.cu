@@ -3,10 +3,12 @@
 // Every visibility (row, chan) gets the corner of its W x W x W footprint on
 // the oversampled (u, v, w-plane) grid, computed in FP64 from uvw x frequency,
 // and a key = (uv tile, first w plane).  A stable LSD radix sort orders the
-// visibilities by key; the bucket offsets come from a key histogram and an
-// exclusive scan; finally one 32-byte record per visibility is written in
-// sorted order, carrying the visibility times its shift phase (inversion) or
-// the phase factor itself (prediction).
+// visibilities by key and, within a key, by the footprint corner inside the
+// tile (its first pass sorts by the corner byte), so that the samples sharing
+// an exact footprint corner are consecutive; the bucket offsets come from a
+// key histogram and an exclusive scan; finally one 32-byte record per
+// visibility is written in sorted order, carrying the visibility times its
+// shift phase (inversion) or the phase factor itself (prediction).
 //
 // The footprint arithmetic uses explicitly rounded operations (__dmul_rn,
 // __dsub_rn, never contracted into FMAs) so that the integer corners, the
@@ -152,8 +154,8 @@ __device__ __forceinline__ bool wrap_decided(int c, int n, int *out) {
 // Key (and corner row / first plane) of a sample decided in FP32; false
 // when any of the three corners needs the FP64 footprint.
 __device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
-                                            const ChannelScale &cs, uint32_t *key, int *iv_out,
-                                            int *ip_out) {
+                                            const ChannelScale &cs, uint32_t *key, int *iu_out,
+                                            int *iv_out, int *ip_out) {
   const float half = 0.5f * (float)p.support;
   int iu0, iv0, iu, iv, ip = 0;
   if (!ceil_decided(rf.x, cs.fsu, half, &iu0) || !ceil_decided(rf.y, cs.fsv, half, &iv0))
@@ -187,9 +189,16 @@ __device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
                                             p.support)) *
              (uint32_t)p.n_planes +
          (uint32_t)ip;
+  *iu_out = iu;
   *iv_out = iv;
   *ip_out = ip;
   return true;
+}
+
+// The footprint corner inside its 16 x 16 tile as one byte: (iv mod 16) * 16
+// + (iu mod 16), the minor sort key within a (tile, class, first plane) key.
+__host__ __device__ __forceinline__ uint8_t corner_byte(int iu, int iv) {
+  return (uint8_t)(((iv & 15) << 4) | (iu & 15));
 }
 
 __device__ __forceinline__ bool is_zero(const float2 v) {
@@ -279,21 +288,25 @@ __global__ void __launch_bounds__(kThreads)
                Selector sel, int64_t n_rows, int64_t n_chan,
                uint32_t sentinel, uint32_t *keys,
                uint32_t *vals, uint32_t *counts, uint8_t *corners,
-               uint32_t *pending, uint32_t *n_pending, const float4 *__restrict__ uvwf) {
+               uint32_t *pending, uint32_t *n_pending, const float4 *__restrict__ uvwf,
+               uint8_t *__restrict__ minor) {
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const int64_t r = e / n_chan, c = e - r * n_chan;
   uint32_t key = sentinel;
+  uint8_t cb = 0;
   bool defer = false;
   if (sel(e)) {
-    int iv, ip;
-    if (key_decided(p, row_float(uvwf, uvw, r), cs[c], &key, &iv, &ip)) {
+    int iu, iv, ip;
+    if (key_decided(p, row_float(uvwf, uvw, r), cs[c], &key, &iu, &iv, &ip)) {
       if (corners) corners[(size_t)ip * p.nv + iv] = 1;
+      cb = corner_byte(iu, iv);
     } else {
       defer = true;
     }
   }
+  minor[e] = cb;
   {
     // samples the FP32 test cannot decide go to the FP64 pass (key_fix_kernel)
     const unsigned dm = __ballot_sync(__activemask(), defer);
@@ -322,13 +335,14 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void __launch_bounds__(kThreads)
     key_fix_kernel(DevPlan p, const double *uvw, const ChannelScale *cs, int64_t n_chan,
                    const uint32_t *__restrict__ pending, const uint32_t *__restrict__ n_pending,
-                   uint32_t *keys, uint32_t *counts, uint8_t *corners) {
+                   uint32_t *keys, uint32_t *counts, uint8_t *corners, uint8_t *minor) {
   const uint32_t n = *n_pending;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t e = pending[i];
     const int64_t r = e / n_chan, c = e - r * n_chan;
     const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
     keys[e] = f.key;
+    minor[e] = corner_byte(f.iu, f.iv);
     if (corners) corners[(size_t)f.ip * p.nv + f.iv] = 1;
     atomicAdd(&counts[f.key], 1u);
   }
@@ -338,9 +352,11 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kThreads * kSortItems;  // 2048 elements per block
 
+// digits: when non-null, element i's digit is digits[i] instead of the key's
+// 8 bits at `shift` (the corner pass).
 __global__ void __launch_bounds__(kThreads)
-    radix_hist_kernel(const uint32_t *keys, int64_t n, int shift,
-                      uint32_t *hist, int64_t n_blocks, bool drop, uint32_t drop_key) {
+    radix_hist_kernel(const uint32_t *keys, const uint8_t *__restrict__ digits, int64_t n,
+                      int shift, uint32_t *hist, int64_t n_blocks, bool drop, uint32_t drop_key) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -350,7 +366,8 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t i = base + r * kThreads + threadIdx.x;
     if (i < n) {
       const uint32_t k = keys[i];
-      if (!(drop && k == drop_key)) atomicAdd(&h[(k >> shift) & 255u], 1u);
+      const uint32_t d = digits ? (uint32_t)digits[i] : (k >> shift) & 255u;
+      if (!(drop && k == drop_key)) atomicAdd(&h[d], 1u);
     }
   }
   __syncthreads();
@@ -367,8 +384,8 @@ __global__ void __launch_bounds__(kThreads)
 // them too) and n_kept elements come out.
 __global__ void __launch_bounds__(kThreads)
     radix_scatter_kernel(const uint32_t *keys_in, const uint32_t *vals_in,
-                         int64_t n, int shift, const uint32_t *hist,
-                         int64_t n_blocks, uint32_t *keys_out,
+                         const uint8_t *__restrict__ digits, int64_t n, int shift,
+                         const uint32_t *hist, int64_t n_blocks, uint32_t *keys_out,
                          uint32_t *vals_out, bool drop, uint32_t drop_key, uint32_t n_kept) {
   __shared__ uint32_t base[256];    // global position of the tile's first element of digit d
   __shared__ uint32_t tstart[256];  // first position of digit d in the tile's sorted order
@@ -377,6 +394,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t wsum[kThreads / 32];
   __shared__ uint32_t tile_kept;
   __shared__ uint32_t skey[kSortTile], sval[kSortTile];
+  __shared__ uint8_t sdig[kSortTile];
   static_assert(kThreads == 256, "one thread per digit");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
@@ -414,7 +432,7 @@ __global__ void __launch_bounds__(kThreads)
     if (valid) {
       key = keys_in[tile0 + t];
       val = vals_in[tile0 + t];
-      d = (key >> shift) & 255u;
+      d = digits ? (uint32_t)digits[tile0 + t] : (key >> shift) & 255u;
       if (drop && key == drop_key) {
         valid = false;
         d = 256;
@@ -439,14 +457,14 @@ __global__ void __launch_bounds__(kThreads)
       const uint32_t pos = tstart[d] + wcnt[warp][d] + rank;
       skey[pos] = key;
       sval[pos] = val;
+      sdig[pos] = (uint8_t)d;
     }
     __syncthreads();  // wcnt is cleared for the next round
   }
   for (int j = threadIdx.x; j < (int)tile_kept; j += kThreads) {
-    const uint32_t key = skey[j];
-    const uint32_t d = (key >> shift) & 255u;
+    const uint32_t d = sdig[j];
     const uint32_t out = base[d] + ((uint32_t)j - tstart[d]);
-    keys_out[out] = key;
+    keys_out[out] = skey[j];
     vals_out[out] = sval[j];
   }
 }
@@ -654,28 +672,32 @@ unsigned grid_for(int64_t n, int threads) {
 }  // namespace
 
 namespace {
-// Stable LSD radix sort of (key, value) pairs over `bits` key bits.  The first
-// pass drops the elements whose key is `sentinel` (samples that take no part),
-// so the n_kept others come out; kin / vin end up naming the sorted buffers.
-// scan(d, n) is an exclusive scan of n uint32 values in place.
+// Stable LSD radix sort of (key, value) pairs by (key over `bits` bits, minor
+// byte): the first pass orders by minor[i] (element i of the unsorted input),
+// the following ones by the key's 8-bit digits.  The first pass drops the
+// elements whose key is `sentinel` (samples that take no part), so the n_kept
+// others come out; kin / vin end up naming the sorted buffers.  scan(d, n) is
+// an exclusive scan of n uint32 values in place.
 template <class Scan>
 void radix_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *&vout,
-                     int64_t n, uint32_t n_kept, int bits, uint32_t sentinel, uint32_t *hist,
-                     Scan scan, cudaStream_t s) {
+                     const uint8_t *minor, int64_t n, uint32_t n_kept, int bits,
+                     uint32_t sentinel, uint32_t *hist, Scan scan, cudaStream_t s) {
   int64_t cur = n;
-  for (int shift = 0; shift < bits && cur > 0 && n_kept > 0; shift += 8) {
-    const bool drop = shift == 0;
+  for (int pass = -1, shift = 0; shift < bits && cur > 0 && n_kept > 0; ++pass) {
+    const bool drop = pass == -1;
+    const uint8_t *digits = pass == -1 ? minor : nullptr;
     const int64_t n_blocks = (cur + kSortTile - 1) / kSortTile;
-    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, cur, shift, hist, n_blocks,
-                                                              drop, sentinel);
+    radix_hist_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(kin, digits, cur, shift, hist,
+                                                              n_blocks, drop, sentinel);
     check_launch("radix_hist_kernel");
     scan(hist, 256 * n_blocks);
     radix_scatter_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(
-        kin, vin, cur, shift, hist, n_blocks, kout, vout, drop, sentinel, n_kept);
+        kin, vin, digits, cur, shift, hist, n_blocks, kout, vout, drop, sentinel, n_kept);
     check_launch("radix_scatter_kernel");
     std::swap(kin, kout);
     std::swap(vin, vout);
     cur = n_kept;
+    if (pass >= 0) shift += 8;
   }
 }
 }  // namespace
@@ -741,6 +763,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   uint32_t *vals = (uint32_t *)arena.get(kSlotVals, sizeof(uint32_t) * (n + 1));
   uint32_t *vals2 = (uint32_t *)arena.get(kSlotValsAlt, sizeof(uint32_t) * (n + 1));
   uint32_t *offsets = (uint32_t *)arena.get(kSlotOffsets, sizeof(uint32_t) * (res.n_keys + 1));
+  uint8_t *minor = (uint8_t *)arena.get(kSlotCorner, (size_t)n + 16);
 
   const double gu = p.dl * (double)p.nu, gv = p.dm * (double)p.nv;
   channel_scales_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, n_chan, gu, gv, cs);
@@ -762,10 +785,10 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
         n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners(), keys2, n_pending,
-        uvwf);
+        uvwf, minor);
     check_launch("key_kernel");
     key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, n_pending,
-                                                        keys, offsets, res.rows.corners());
+                                                        keys, offsets, res.rows.corners(), minor);
     check_launch("key_fix_kernel");
   }
   build_row_occupancy(res.rows, p.support, s);
@@ -780,7 +803,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
   uint32_t *hist = (uint32_t *)arena.get(kSlotHist, sizeof(uint32_t) * (256 * n_blocks + 1));
   uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  radix_sort_kept(kin, vin, kout, vout, n, total, bits, sentinel, hist,
+  radix_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, hist,
                   [&](uint32_t *d, int64_t m) { exclusive_scan_u32(arena, d, m, s); }, s);
   res.n_out = total;
   res.perm = vin;
@@ -826,8 +849,9 @@ constexpr size_t kNoallocSortBytes = 4 * sizeof(uint32_t) * kNoallocMaxVis;
 constexpr size_t kNoallocHistBytes = sizeof(uint32_t) * 256 * kNoallocBlocks;
 constexpr size_t kNoallocScanBytes = sizeof(uint32_t) * kNoallocScanWords;
 constexpr size_t kNoallocScaleBytes = (sizeof(ChannelScale) * kNoallocMaxChan + 255) / 256 * 256;
-constexpr size_t kNoallocBytes =
-    kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes + kNoallocScaleBytes;
+constexpr size_t kNoallocCornerBytes = (size_t)kNoallocMaxVis;
+constexpr size_t kNoallocBytes = kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes +
+                                 kNoallocScaleBytes + kNoallocCornerBytes;
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_bucket_scratch[kNoallocBytes];
@@ -884,6 +908,8 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
   uint32_t *scan_tmp = (uint32_t *)(base + kNoallocSortBytes + kNoallocHistBytes);
   ChannelScale *cs =
       (ChannelScale *)(base + kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes);
+  uint8_t *minor = base + kNoallocSortBytes + kNoallocHistBytes + kNoallocScanBytes +
+                   kNoallocScaleBytes;
 
   const double gu = p.dl * (double)p.nu, gv = p.dm * (double)p.nv;
   if (n_chan > 0) {
@@ -898,10 +924,10 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
     WGPU_CUDA(cudaMemsetAsync(vals2, 0, sizeof(uint32_t), s));
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, nullptr}, n_rows,
-        n_chan, sentinel, keys, vals, d_offsets, nullptr, keys2, vals2, nullptr);
+        n_chan, sentinel, keys, vals, d_offsets, nullptr, keys2, vals2, nullptr, minor);
     check_launch("key_kernel");
     key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, vals2, keys,
-                                                        d_offsets, nullptr);
+                                                        d_offsets, nullptr, minor);
     check_launch("key_fix_kernel");
   }
   exclusive_scan_u32_scratch(d_offsets, n_keys + 1, scan_tmp, s);
@@ -910,7 +936,7 @@ int64_t bucket_visibilities_noalloc(const DevPlan &p, const double *d_uvw, const
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
   uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  radix_sort_kept(kin, vin, kout, vout, n, total, bits, sentinel, hist,
+  radix_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, hist,
                   [&](uint32_t *d, int64_t m) { exclusive_scan_u32_scratch(d, m, scan_tmp, s); },
                   s);
   if (total > 0) {

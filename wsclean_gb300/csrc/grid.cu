@@ -379,8 +379,253 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   __syncthreads();
 }
 
+// ---- gridding by corner runs (W <= 8) -------------------------------------
+//
+// The bucketing orders the samples of every (tile, class, first plane) key by
+// their footprint corner inside the tile, so the samples that share an exact
+// corner (iu, iv, ip) are consecutive; in the wide-field workload half of the
+// samples lie in runs of eight or more.  A warp takes a contiguous chunk of
+// the item's reads and holds a whole 8 x 8 x 8 footprint in registers: lane l
+// owns footprint column i = l % 8, rows j = l / 8 and l / 8 + 4, and all eight
+// planes (16 complex accumulators).  Each read adds its kernel-weighted
+// visibility to the accumulators; only when the corner changes (and at the
+// end of the chunk) does the warp add the footprint into the halo, with
+// shared-memory atomics because the warps' footprints may overlap.  Kernel
+// values are evaluated once per read by the lane that stages it (eight
+// values along each axis; the w values already multiplied by the visibility).
+constexpr int kRunWarps = kThreads / 32;
+constexpr int kRunBatch = 32;  // reads staged per warp at a time
+struct __align__(16) RunStage {
+  float kx[8];    // u kernel values (zero beyond W)
+  float2 ky2[4];  // (ky[j], ky[j + 4])
+  float2 vz[8];   // visibility times the w kernel value of footprint plane k
+  int meta;       // iu_rel | iv_rel << 8 | (ip_rel + 128) << 16
+  int pad[3];
+};
+static_assert(sizeof(RunStage) == 144, "run stage layout");
+
 template <int T, int G, int W>
-__global__ void __launch_bounds__(kThreads)
+constexpr size_t grid_runs_smem_bytes() {
+  return sizeof(float2) * G * halo_plane(T, W) + sizeof(RunStage) * kRunWarps * kRunBatch;
+}
+
+// The footprint of the current run (corner `meta`) into the halo cells of the
+// group's planes.
+template <int T, int G, int W>
+__device__ __forceinline__ void run_flush(float2 *cells, int meta, int nq, int i, int jb,
+                                          const float2 (&acc)[2][8]) {
+  constexpr int R = halo_rows(T, W);
+  constexpr int PS = halo_plane(T, W);
+  const int iu_rel = meta & 255, iv_rel = (meta >> 8) & 255, ip_rel = (meta >> 16) - 128;
+  if (i >= W) return;
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const int j = jb + 4 * t;
+    if (j >= W) continue;
+    float2 *row = cells + (iv_rel + j) * R + iu_rel + i;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const int z = ip_rel + k;
+      if (z >= 0 && z < nq) {
+        float2 *c = row + z * PS;
+        atomicAdd(&c->x, acc[t][k].x);
+        atomicAdd(&c->y, acc[t][k].y);
+      }
+    }
+  }
+}
+
+template <int T, int G, int W>
+__device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord *__restrict__ rec,
+                                               const uint32_t *__restrict__ off, int p_begin,
+                                               int n_batch, const uint32_t *__restrict__ item_off,
+                                               const int *__restrict__ slots,
+                                               float2 *__restrict__ spill, uint32_t d,
+                                               uint32_t item, float2 *__restrict__ planes,
+                                               float2 *cells, RunStage *stage, uint32_t *rs0,
+                                               uint32_t *rcum) {
+  static_assert(W <= 8, "runs gridding holds an 8 x 8 x 8 footprint");
+  constexpr int R = halo_rows(T, W);
+  constexpr int PS = halo_plane(T, W);
+  constexpr int B = spill_cells(T, W);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = lane & 7, jb = lane >> 3;
+  const float inv_half = 2.0f / (float)W;
+  const int n_tiles = p.ntu * p.ntv;
+  const size_t plane_elems = (size_t)p.nu * p.nv;
+  const int unit = (int)(d & 0x7fffffffu);
+  const int tile = unit % n_tiles, group = unit / n_tiles;
+  const int tu = tile % p.ntu, tv = tile / p.ntu;
+  const int q0 = p_begin + group * G;
+  const int q1 = min(q0 + G, p_begin + n_batch);
+  const int nq = q1 - q0;
+  if (d & 0x80000000u) {
+    // no visibility reaches this unit: its own cells are zero
+    for (int c = threadIdx.x; c < nq * T * T; c += kThreads) {
+      const int pq = c / (T * T), rem = c - pq * (T * T);
+      const int rr = rem / T, cc = rem - rr * T;
+      planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + rr) * p.nu +
+             tu * T + cc] = make_float2(0.f, 0.f);
+    }
+    return;
+  }
+  const uint32_t first = __ldg(item_off + unit);
+  const uint32_t n_items = __ldg(item_off + unit + 1) - first;
+  if (threadIdx.x < 4) {
+    uint32_t a, b;
+    unit_range(p, off, tile, q0, q1, threadIdx.x, &a, &b);
+    rs0[threadIdx.x] = a;
+    rcum[threadIdx.x + 1] = b - a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    rcum[0] = 0;
+    for (int r = 0; r < 4; ++r) rcum[r + 1] += rcum[r];
+  }
+  __syncthreads();
+  const uint32_t lo = (item - first) * kItemVis;
+  const uint32_t hi = min(lo + kItemVis, rcum[4]);
+  // this warp's contiguous chunk of the item's reads
+  const uint32_t per = (hi - lo + kRunWarps - 1) / kRunWarps;
+  const uint32_t c0 = min(lo + (uint32_t)warp * per, hi);
+  const uint32_t c1 = min(c0 + per, hi);
+  RunStage *ws = stage + warp * kRunBatch;
+  float2 acc[2][8];
+#pragma unroll
+  for (int t = 0; t < 2; ++t)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[t][k] = make_float2(0.f, 0.f);
+  int cur = -1;
+  for (uint32_t b0 = c0; b0 < c1; b0 += kRunBatch) {
+    __syncwarp();  // the previous batch has been read
+    {
+      const uint32_t pos = b0 + (uint32_t)lane;
+      if (pos < c1) {
+        int r = 0;
+        while (pos >= rcum[r + 1]) ++r;
+        const VisRecord v = load_record(rec + rs0[r] + (pos - rcum[r]));
+        RunStage &st = ws[lane];
+        float ky[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          st.kx[k] = k < W ? es_eval(p.beta, (v.fu + (float)k) * inv_half) : 0.f;
+          ky[k] = k < W ? es_eval(p.beta, (v.fv + (float)k) * inv_half) : 0.f;
+          const float kz = k >= W ? 0.f
+                           : p.n_planes == 1 ? (k == 0 ? 1.0f : 0.0f)
+                                             : es_eval(p.beta, (v.fw + (float)k) * inv_half);
+          st.vz[k] = make_float2(v.re * kz, v.im * kz);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) st.ky2[k] = make_float2(ky[k], ky[k + 4]);
+        st.meta = (v.iu - tu * T) | ((v.iv - tv * T) << 8) | ((v.ip - q0 + 128) << 16);
+      }
+    }
+    __syncwarp();
+    const int n_b = (int)min((uint32_t)kRunBatch, c1 - b0);
+    int m = 0;
+    while (m < n_b) {
+      // a new corner (warp-uniform: every lane reads the same read)
+      const int meta = ws[m].meta;
+      if (meta != cur) {
+        if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, acc);
+#pragma unroll
+        for (int t = 0; t < 2; ++t)
+#pragma unroll
+          for (int k = 0; k < 8; ++k) acc[t][k] = make_float2(0.f, 0.f);
+        cur = meta;
+      }
+      // the batch's reads of this corner, accumulated in registers
+      do {
+        const RunStage &st = ws[m];
+        const float kx = st.kx[i];
+        const float2 ky = st.ky2[jb];
+        const float w0 = kx * ky.x, w1 = kx * ky.y;
+#pragma unroll
+        for (int k = 0; k < W; k += 2) {
+          if (k + 1 < W) {
+            const float4 z = *reinterpret_cast<const float4 *>(&st.vz[k]);
+            acc[0][k].x = fmaf(w0, z.x, acc[0][k].x);
+            acc[0][k].y = fmaf(w0, z.y, acc[0][k].y);
+            acc[1][k].x = fmaf(w1, z.x, acc[1][k].x);
+            acc[1][k].y = fmaf(w1, z.y, acc[1][k].y);
+            acc[0][k + 1].x = fmaf(w0, z.z, acc[0][k + 1].x);
+            acc[0][k + 1].y = fmaf(w0, z.w, acc[0][k + 1].y);
+            acc[1][k + 1].x = fmaf(w1, z.z, acc[1][k + 1].x);
+            acc[1][k + 1].y = fmaf(w1, z.w, acc[1][k + 1].y);
+          } else {
+            const float2 z = st.vz[k];
+            acc[0][k].x = fmaf(w0, z.x, acc[0][k].x);
+            acc[0][k].y = fmaf(w0, z.y, acc[0][k].y);
+            acc[1][k].x = fmaf(w1, z.x, acc[1][k].x);
+            acc[1][k].y = fmaf(w1, z.y, acc[1][k].y);
+          }
+        }
+        ++m;
+      } while (m < n_b && ws[m].meta == cur);
+    }
+  }
+  if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, acc);
+  __syncthreads();
+  // flush: the tile's cells to the planes (a split unit adds into cells
+  // zeroed beforehand), the border cells to the unit's spill slot; plane by
+  // plane, cell c of the R x R region at row c / R, column c % R
+  const int slot = __ldg(slots + unit);
+  float2 *sp = spill + (size_t)slot * G * B;
+  for (int pq = 0; pq < nq; ++pq) {
+    float2 *plane = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
+                    (size_t)(tv * T) * p.nu + tu * T;
+    float2 *cp = cells + pq * PS;
+    float2 *spq = sp + (size_t)pq * B;
+    for (int c = threadIdx.x; c < R * R; c += kThreads) {
+      const int rr = c / R, cc = c - (c / R) * R;
+      const float2 val = cp[c];
+      cp[c] = make_float2(0.f, 0.f);
+      float2 *dst = (rr < T && cc < T) ? plane + (size_t)rr * p.nu + cc
+                                       : spq + border_index(T, W, rr, cc);
+      if (n_items == 1)
+        *dst = val;
+      else
+        atomicAdd(dst, val);
+    }
+  }
+  __syncthreads();
+}
+
+// Shared memory of the gridding kernels: the halo cells and either the
+// round-staging of grid_item (W > 8) or the per-warp run staging (W <= 8).
+template <int T, int G, int W>
+constexpr size_t grid_kernel_smem_bytes() {
+  if constexpr (W <= 8)
+    return grid_runs_smem_bytes<T, G, W>();
+  else
+    return grid_smem_bytes<T, G, W>();
+}
+
+// One gridding work item with the variant for the support.
+template <int T, int G, int W>
+__device__ __forceinline__ void grid_item_any(const DevPlan &p, const VisRecord *__restrict__ rec,
+                                              const uint32_t *__restrict__ off, int p_begin,
+                                              int n_batch, const uint32_t *__restrict__ item_off,
+                                              const int *__restrict__ slots,
+                                              float2 *__restrict__ spill, uint32_t d,
+                                              uint32_t item, float2 *__restrict__ planes,
+                                              float4 *smem4, uint32_t *rs0, uint32_t *rcum) {
+  if constexpr (W <= 8) {
+    float2 *cells = reinterpret_cast<float2 *>(smem4);
+    RunStage *stage = reinterpret_cast<RunStage *>(cells + G * halo_plane(T, W));
+    grid_item_runs<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item,
+                            planes, cells, stage, rs0, rcum);
+  } else {
+    const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
+    grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item, planes,
+                       sm);
+  }
+}
+
+// Two blocks per SM for the run variant (its shared memory allows two), three
+// for the round variant; both fit in 128 registers per thread.
+template <int T, int G, int W>
+__global__ void __launch_bounds__(kThreads, 2)
     grid_kernel(DevPlan p, const VisRecord *__restrict__ rec,
                 const uint32_t *__restrict__ off, int p_begin, int n_batch,
                 const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
@@ -389,13 +634,13 @@ __global__ void __launch_bounds__(kThreads)
   static_assert(kThreads == 256, "eight warps own the halo rows modulo 8");
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
-  const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
+  float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
-    sm.cells[c] = make_float2(0.f, 0.f);
+    cells[c] = make_float2(0.f, 0.f);
   __syncthreads();
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x)
-    grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill,
-                       __ldg(desc + item), item, planes, sm);
+    grid_item_any<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill,
+                           __ldg(desc + item), item, planes, smem4, rs0, rcum);
 }
 
 // Several gridding jobs (facets x channel groups, each with its own plan,
@@ -403,7 +648,7 @@ __global__ void __launch_bounds__(kThreads)
 // item i belongs to the job j with job_base[j] <= i < job_base[j + 1]; the
 // block keeps the current job's description in shared memory.
 template <int T, int G, int W>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     grid_kernel_multi(const GridJob *__restrict__ jobs, const uint32_t *__restrict__ job_base,
                       int n_jobs, uint32_t total) {
   static_assert(kThreads == 256, "eight warps own the halo rows modulo 8");
@@ -411,9 +656,9 @@ __global__ void __launch_bounds__(kThreads)
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
   __shared__ GridJob job;
-  const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
+  float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
-    sm.cells[c] = make_float2(0.f, 0.f);
+    cells[c] = make_float2(0.f, 0.f);
   int cur = -1;
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     int lo = 0, hi = n_jobs - 1;  // last job whose base is <= item
@@ -430,8 +675,9 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     const uint32_t local = item - __ldg(job_base + lo);
-    grid_item<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off, job.slot,
-                       job.spill, __ldg(job.desc + local), local, job.planes, sm);
+    grid_item_any<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off,
+                           job.slot, job.spill, __ldg(job.desc + local), local, job.planes, smem4,
+                           rs0, rcum);
   }
 }
 
@@ -802,7 +1048,7 @@ template <int T, int G, int W>
 void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
                 int n_batch, const WorkItems &wi, float2 *planes, cudaStream_t s) {
   if (wi.total == 0) return;
-  const size_t smem = grid_smem_bytes<T, G, W>();
+  const size_t smem = grid_kernel_smem_bytes<T, G, W>();
   ensure_dynamic_smem((const void *)grid_kernel<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel<T, G, W>,
@@ -835,7 +1081,7 @@ template <int T, int G, int W>
 void grid_items_multi(const GridJob *d_jobs, const uint32_t *d_base, int n_jobs, uint32_t total,
                       cudaStream_t s) {
   if (total == 0) return;
-  const size_t smem = grid_smem_bytes<T, G, W>();
+  const size_t smem = grid_kernel_smem_bytes<T, G, W>();
   ensure_dynamic_smem((const void *)grid_kernel_multi<T, G, W>, smem);
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_kernel_multi<T, G, W>,
@@ -957,7 +1203,7 @@ void grid_multi_prepare(int support) {
   if constexpr (W <= kMaxSupport) {
     if (support == W)
       ensure_dynamic_smem((const void *)grid_kernel_multi<T, grid_group(W), W>,
-                          grid_smem_bytes<T, grid_group(W), W>());
+                          grid_kernel_smem_bytes<T, grid_group(W), W>());
     else
       grid_multi_prepare<T, W + 1>(support);
   }

@@ -437,6 +437,7 @@ enum ArenaSlot {
   kSlotResampleWork,  // resampling around the boundary: FFT work images,
   kSlotResampleOut,   // the image at the padded image size,
   kSlotResampleTrim,  // and at the trimmed size
+  kSlotCorner,        // bucketing: footprint corner within the tile, per sample
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
