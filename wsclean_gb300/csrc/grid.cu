@@ -393,6 +393,15 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
 // shared-memory atomics because the warps' footprints may overlap.  Kernel
 // values are evaluated once per read by the lane that stages it (eight
 // values along each axis; the w values already multiplied by the visibility).
+//
+// The halo holds fixed-point integers: a run's float sums are scaled by
+// S = 2^30 / sum over the item's reads of (|re| + |im|), rounded and added
+// with native integer atomics, and converted back when the halo is written
+// out.  Every kernel value is at most one, so no cell component can exceed
+// 2^30 (no overflow), and the integer sums are exact and independent of the
+// order in which the warps add them.  Each flush rounds by at most half a
+// unit, i.e. 2^-31 of the item's summed magnitude; an item holds at most 2048
+// reads, which bounds that step.
 constexpr int kRunWarps = kThreads / 32;
 constexpr int kRunBatch = 32;  // reads staged per warp at a time
 struct __align__(16) RunStage {
@@ -409,11 +418,11 @@ constexpr size_t grid_runs_smem_bytes() {
   return sizeof(float2) * G * halo_plane(T, W) + sizeof(RunStage) * kRunWarps * kRunBatch;
 }
 
-// The footprint of the current run (corner `meta`) into the halo cells of the
-// group's planes.
+// The footprint of the current run (corner `meta`) into the fixed-point halo
+// cells of the group's planes, scaled by `scale`.
 template <int T, int G, int W>
-__device__ __forceinline__ void run_flush(float2 *cells, int meta, int nq, int i, int jb,
-                                          const float2 (&acc)[2][8]) {
+__device__ __forceinline__ void run_flush(int2 *cells, int meta, int nq, int i, int jb,
+                                          float scale, const float2 (&acc)[2][8]) {
   constexpr int R = halo_rows(T, W);
   constexpr int PS = halo_plane(T, W);
   const int iu_rel = meta & 255, iv_rel = (meta >> 8) & 255, ip_rel = (meta >> 16) - 128;
@@ -422,14 +431,14 @@ __device__ __forceinline__ void run_flush(float2 *cells, int meta, int nq, int i
   for (int t = 0; t < 2; ++t) {
     const int j = jb + 4 * t;
     if (j >= W) continue;
-    float2 *row = cells + (iv_rel + j) * R + iu_rel + i;
+    int2 *row = cells + (iv_rel + j) * R + iu_rel + i;
 #pragma unroll
     for (int k = 0; k < W; ++k) {
       const int z = ip_rel + k;
       if (z >= 0 && z < nq) {
-        float2 *c = row + z * PS;
-        atomicAdd(&c->x, acc[t][k].x);
-        atomicAdd(&c->y, acc[t][k].y);
+        int2 *c = row + z * PS;
+        atomicAdd(&c->x, __float2int_rn(acc[t][k].x * scale));
+        atomicAdd(&c->y, __float2int_rn(acc[t][k].y * scale));
       }
     }
   }
@@ -442,9 +451,10 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
                                                const int *__restrict__ slots,
                                                float2 *__restrict__ spill, uint32_t d,
                                                uint32_t item, float2 *__restrict__ planes,
-                                               float2 *cells, RunStage *stage, uint32_t *rs0,
-                                               uint32_t *rcum) {
+                                               int2 *cells, RunStage *stage, uint32_t *rs0,
+                                               uint32_t *rcum, float *red) {
   static_assert(W <= 8, "runs gridding holds an 8 x 8 x 8 footprint");
+  static_assert(kThreads == T * T, "one thread per tile cell in the write-out");
   constexpr int R = halo_rows(T, W);
   constexpr int PS = halo_plane(T, W);
   constexpr int B = spill_cells(T, W);
@@ -485,6 +495,28 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
   __syncthreads();
   const uint32_t lo = (item - first) * kItemVis;
   const uint32_t hi = min(lo + kItemVis, rcum[4]);
+  // fixed-point scale of the halo: 2^30 over the item's summed magnitudes
+  // (with a margin for the float sum and kernel values rounded above one)
+  {
+    float part = 0.f;
+    for (uint32_t pos = lo + threadIdx.x; pos < hi; pos += kThreads) {
+      int r = 0;
+      while (pos >= rcum[r + 1]) ++r;
+      const float2 v = __ldg(reinterpret_cast<const float2 *>(rec + rs0[r] + (pos - rcum[r])));
+      part += fabsf(v.x) + fabsf(v.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float sum = 0.f;
+      for (int w = 0; w < kRunWarps; ++w) sum += red[w];
+      red[kRunWarps] = sum > 0.f ? 1073741824.0f / (sum * 1.001f) : 1.0f;
+    }
+    __syncthreads();
+  }
+  const float scale = red[kRunWarps];
   // this warp's contiguous chunk of the item's reads
   const uint32_t per = (hi - lo + kRunWarps - 1) / kRunWarps;
   const uint32_t c0 = min(lo + (uint32_t)warp * per, hi);
@@ -527,7 +559,7 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
       // a new corner (warp-uniform: every lane reads the same read)
       const int meta = ws[m].meta;
       if (meta != cur) {
-        if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, acc);
+        if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, scale, acc);
 #pragma unroll
         for (int t = 0; t < 2; ++t)
 #pragma unroll
@@ -564,28 +596,49 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
       } while (m < n_b && ws[m].meta == cur);
     }
   }
-  if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, acc);
+  if (cur >= 0) run_flush<T, G, W>(cells, cur, nq, i, jb, scale, acc);
   __syncthreads();
-  // flush: the tile's cells to the planes (a split unit adds into cells
-  // zeroed beforehand), the border cells to the unit's spill slot; plane by
-  // plane, cell c of the R x R region at row c / R, column c % R
+  // write-out, plane by plane: the tile's T x T cells to the planes (one per
+  // thread; a split unit adds into cells zeroed beforehand), the border cells
+  // to the unit's spill slot in spill order (border_index); the halo is left
+  // zero
+  const float inv = 1.0f / scale;
+  const bool add = n_items > 1;
   const int slot = __ldg(slots + unit);
   float2 *sp = spill + (size_t)slot * G * B;
+  const int tr = threadIdx.x / T, tc = threadIdx.x % T;
   for (int pq = 0; pq < nq; ++pq) {
-    float2 *plane = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
-                    (size_t)(tv * T) * p.nu + tu * T;
-    float2 *cp = cells + pq * PS;
-    float2 *spq = sp + (size_t)pq * B;
-    for (int c = threadIdx.x; c < R * R; c += kThreads) {
-      const int rr = c / R, cc = c - (c / R) * R;
-      const float2 val = cp[c];
-      cp[c] = make_float2(0.f, 0.f);
-      float2 *dst = (rr < T && cc < T) ? plane + (size_t)rr * p.nu + cc
-                                       : spq + border_index(T, W, rr, cc);
-      if (n_items == 1)
-        *dst = val;
-      else
+    int2 *cp = cells + pq * PS;
+    {
+      int2 *src = cp + tr * R + tc;
+      const int2 q = *src;
+      *src = make_int2(0, 0);
+      const float2 val = make_float2((float)q.x * inv, (float)q.y * inv);
+      float2 *dst = planes + (size_t)(q0 + pq - p_begin) * plane_elems +
+                    (size_t)(tv * T + tr) * p.nu + tu * T + tc;
+      if (add)
         atomicAdd(dst, val);
+      else
+        *dst = val;
+    }
+    float2 *spq = sp + (size_t)pq * B;
+    for (int b = threadIdx.x; b < B; b += kThreads) {
+      int rr, cc;
+      if (b < (W - 1) * R) {
+        rr = b / (W - 1);
+        cc = T + b - rr * (W - 1);
+      } else {
+        rr = T + (b - (W - 1) * R) / T;
+        cc = (b - (W - 1) * R) % T;
+      }
+      int2 *src = cp + rr * R + cc;
+      const int2 q = *src;
+      *src = make_int2(0, 0);
+      const float2 val = make_float2((float)q.x * inv, (float)q.y * inv);
+      if (add)
+        atomicAdd(spq + b, val);
+      else
+        spq[b] = val;
     }
   }
   __syncthreads();
@@ -609,12 +662,13 @@ __device__ __forceinline__ void grid_item_any(const DevPlan &p, const VisRecord 
                                               const int *__restrict__ slots,
                                               float2 *__restrict__ spill, uint32_t d,
                                               uint32_t item, float2 *__restrict__ planes,
-                                              float4 *smem4, uint32_t *rs0, uint32_t *rcum) {
+                                              float4 *smem4, uint32_t *rs0, uint32_t *rcum,
+                                              float *red) {
   if constexpr (W <= 8) {
-    float2 *cells = reinterpret_cast<float2 *>(smem4);
+    int2 *cells = reinterpret_cast<int2 *>(smem4);
     RunStage *stage = reinterpret_cast<RunStage *>(cells + G * halo_plane(T, W));
     grid_item_runs<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item,
-                            planes, cells, stage, rs0, rcum);
+                            planes, cells, stage, rs0, rcum, red);
   } else {
     const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
     grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item, planes,
@@ -634,13 +688,14 @@ __global__ void __launch_bounds__(kThreads, 2)
   static_assert(kThreads == 256, "eight warps own the halo rows modulo 8");
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
+  __shared__ float red[kRunWarps + 1];
   float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
     cells[c] = make_float2(0.f, 0.f);
   __syncthreads();
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x)
     grid_item_any<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill,
-                           __ldg(desc + item), item, planes, smem4, rs0, rcum);
+                           __ldg(desc + item), item, planes, smem4, rs0, rcum, red);
 }
 
 // Several gridding jobs (facets x channel groups, each with its own plan,
@@ -655,6 +710,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   static_assert(sizeof(GridJob) % 8 == 0, "job copied in 8-byte words");
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
+  __shared__ float red[kRunWarps + 1];
   __shared__ GridJob job;
   float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
@@ -677,7 +733,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t local = item - __ldg(job_base + lo);
     grid_item_any<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off,
                            job.slot, job.spill, __ldg(job.desc + local), local, job.planes, smem4,
-                           rs0, rcum);
+                           rs0, rcum, red);
   }
 }
 
