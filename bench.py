@@ -155,18 +155,20 @@ def pinned_copy(t):
 
 
 # ------------------------------------------------------- algorithmic bytes ---
-def stage_bytes(stage, direction, p, n_vis, n_batch_avg):
-    """Minimum HBM bytes of one launch of `stage` (per plane batch)."""
+def stage_bytes(stage, direction, p, n_vis, n_rows, n_batch_avg, n_batches):
+    """Minimum HBM bytes of one launch of `stage` (per plane batch), from the
+    per-request terms of the survey's byte count: the gridded planes written
+    (read when degridding) once, and the samples' 8 B plus 24 B of uvw per
+    row spread over the batches (the samples are read by the inversion and
+    written by the prediction)."""
     nu, nv, W, H = p.nu, p.nv, p.width, p.height
     rs = (W + 31) // 32 * 32
     nb = n_batch_avg
     plane = 8.0 * nu * nv * nb
     rows = 8.0 * rs * nv * nb
-    touch = 32.0 * n_vis * min(1.0, (nb + p.support - 1) / p.n_planes)
-    if stage == "grid":
-        return plane + touch
-    if stage == "degrid":
-        return plane + touch + 8.0 * n_vis * min(1.0, (nb + p.support - 1) / p.n_planes)
+    samples = (8.0 * n_vis + 24.0 * n_rows) / n_batches
+    if stage in ("grid", "degrid"):
+        return plane + samples
     if stage == "fft_rows":
         return plane + rows
     if stage == "fft_cols_a":
@@ -280,6 +282,70 @@ def accuracy_full(d, g, d_out, n_pix=4096, cpu_rows=20000, cpu_pix=64, seed=4):
             "twin_vs_cpu_sample": f"{rows.size} rows x {n_chan} channels x {cpu_pix} pixels"}
 
 
+def run_bound(d, g, d_out, inv_weight, stream, cycles=4, warmup=1):
+    """Major cycles on a bound visibility set, as WSClean runs them: the rows
+    (uvw, frequencies, the gridded-sample mask) are bound once
+    (wgpu_gridder_bind: plan, bucketing and the two captured pipelines), then
+    every cycle grids the visibilities and predicts the model image by
+    replaying the graphs.  Reports the bind time, the per-cycle time and the
+    agreement with the plain (per-call) path on the same data."""
+    import torch
+    n_rows, n_chan = d["uvw"].shape[0], d["freq"].size
+    n_vis = n_rows * n_chan
+    mask = d["d_mask"].cpu().numpy()
+    # the plain path's image and prediction of this data, for the agreement
+    g.InitializeInversion()
+    g.AddInversionDataDevice(n_rows, n_chan, d["d_uvw"].data_ptr(), d["d_freq"].data_ptr(),
+                             d["d_vis"].data_ptr())
+    g.FinalizeImage(inv_weight)
+    img_plain = g.RealImage().astype(np.float64)
+    g.InitializePrediction(d["model"])
+    g.PredictVisibilitiesMaskedDevice(n_rows, n_chan, d["d_uvw"].data_ptr(),
+                                      d["d_freq"].data_ptr(), d["d_mask"].data_ptr(),
+                                      d_out.data_ptr())
+    pred_plain = d_out.clone()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.Bind(n_rows, n_chan, d["uvw"], d["freq"], mask)
+    torch.cuda.synchronize()
+    bind_s = time.perf_counter() - t0
+    stages = {}
+
+    def cycle():
+        g.InitializeInversion()
+        g.InvertBoundDevice(d["d_vis"].data_ptr())
+        stages["invert"] = g.last_timings()
+        g.FinalizeImage(inv_weight)
+        g.InitializePrediction(d["model"])
+        g.PredictBoundDevice(d_out.data_ptr())
+        stages["predict"] = g.last_timings()
+
+    for _ in range(warmup):
+        cycle()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(cycles):
+        cycle()
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / cycles
+    img_bound = g.RealImage().astype(np.float64)
+    ok = np.isfinite(img_plain)
+    img_rel = float(np.linalg.norm(img_bound[ok] - img_plain[ok]) / np.linalg.norm(img_plain[ok]))
+    pred_rel = float(torch.linalg.vector_norm(d_out - pred_plain).item() /
+                     torch.linalg.vector_norm(pred_plain).item())
+    g.Unbind()
+    return {"ms_per_cycle": ms, "gvis_s": n_vis / (ms * 1e-3) / 1e9, "cycles": cycles,
+            "bind_s": round(bind_s, 2),
+            "stages": {f"{k}:{n}": round(v[0], 3) for k, st in stages.items()
+                       for n, v in st.items()},
+            "bound_vs_plain_rel_l2": {"image": img_rel, "prediction": pred_rel},
+            "cycle": "InitializeInversion + invert_bound (graph replay) + FinalizeImage + "
+                     "InitializePrediction + predict_bound (graph replay), device buffers; "
+                     "bucketing paid once at bind"}
+
+
 # -------------------------------------------------------------- GPU arm -----
 def run_gpu(args, rank, world, local):
     import torch
@@ -387,7 +453,7 @@ def run_gpu(args, rank, world, local):
         n_batches = math.ceil(plan.n_planes / plan.plane_batch)
         nb_avg = plan.n_planes / n_batches
         for name, (sms, cnt) in stages.items():
-            b = stage_bytes(name, direction, plan, d["n_gridded"], nb_avg)
+            b = stage_bytes(name, direction, plan, d["n_gridded"], n_rows, nb_avg, n_batches)
             rows.append(dict(direction=direction, stage=name, ms=sms, launches=cnt,
                              bytes_per_launch=b))
     dom = max(rows, key=lambda r: r["ms"])
@@ -484,6 +550,8 @@ def run_gpu(args, rank, world, local):
 
     if rank == 0 and not args.no_accuracy:
         result["config"]["accuracy"] = accuracy_full(d, g, d_out)
+    if not args.no_bound:
+        result["bound"] = run_bound(d, g, d_out, inv_weight, stream)
     if args.serve_requests > 0:
         g.close()  # release the wide-field gridder's planes before serving
         del d_out
@@ -1190,6 +1258,8 @@ def main():
     ap.add_argument("--max-rows", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-bound", action="store_true",
+                    help="skip the major cycles on a bound visibility set")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the full-data error against the FP64 direct transform")
     ap.add_argument("--cpu-sample-rows", type=int, default=200000,

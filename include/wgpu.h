@@ -57,6 +57,27 @@ extern "C" {
 #define WGPU_POL_XY 5
 #define WGPU_POL_YX 6
 #define WGPU_POL_YY 7
+/* Further polarisations WSClean can request; wgpu_select_gain_mode tells them
+ * apart as SelectGainMode does (the collapse accepts only the eight above). */
+#define WGPU_POL_RR 8
+#define WGPU_POL_RL 9
+#define WGPU_POL_LR 10
+#define WGPU_POL_LL 11
+#define WGPU_POL_FULL_STOKES 12
+#define WGPU_POL_INSTRUMENTAL 13
+#define WGPU_POL_DIAGONAL_INSTRUMENTAL 14
+
+/* gridding/gainmode.h:33-46 (GetNVisibilities): visibilities per sample that
+ * a gain mode corrects (1, 2 or 4); 0 for a number that is no gain mode. */
+size_t wgpu_gain_mode_n_visibilities(int mode);
+
+/* gridding/gainmode.h:52-95 (SelectGainMode): the gain mode for a requested
+ * polarisation (WGPU_POL_*) when n_visibility_polarizations are stored per
+ * sample.  One stored polarisation: XX -> XX, YY -> YY, anything else ->
+ * TRACE.  Two: Stokes I, diagonal instrumental, XX or YY -> 2VIS_DIAGONAL.
+ * Four: full Stokes, instrumental, Stokes I/Q/U/V, XX or YY -> FULL.  Every
+ * other combination returns WGPU_ERR_INVALID (the reference throws). */
+int wgpu_select_gain_mode(int polarization, size_t n_visibility_polarizations, int *mode);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *wgpu_last_error(void);

@@ -8,13 +8,14 @@
  * ducc0-backed class.  Errors from the C ABI are rethrown as
  * std::runtime_error, as the reference's MR_assert / exceptions are.
  *
- * Standalone use: define nothing; GainMode, BandData and MsGridder are
- * declared here.  Inside WSClean: define WGPU_WITH_WSCLEAN before including, so
- * that WSClean's own GainMode / aocommon::BandData / MsGridder are used and the
- * correction callback reads the gridder's cached solution table through an
- * accessor MsGridder::GpuCorrections() returning a GpuCorrectionTable (the
- * cached parm response of VisibilityModifier, its time count, values per
- * solution and polarisation).
+ * Standalone use: define nothing; GainMode (with GetNVisibilities and
+ * SelectGainMode), BandData and MsGridder are declared here.  Inside WSClean:
+ * define WGPU_WITH_WSCLEAN before including, so that WSClean's own GainMode /
+ * aocommon::BandData / MsGridder are used; the correction callback then reads
+ * the gridder's cached h5parm solutions through VisibilityModifier, which
+ * needs two read-only accessors the reference keeps private:
+ *   VisibilityModifier::CachedParmResponse(ms_index)  (_cachedParmResponse)
+ *   MsGridderData::OriginalMsIndex()                  (original_ms_index_)
  */
 #ifndef WGPU_GRIDDER_H_
 #define WGPU_GRIDDER_H_
@@ -29,9 +30,11 @@
 #include "wgpu.h"
 
 #ifdef WGPU_WITH_WSCLEAN
+/* WSClean's source root is on the include path */
 #include <aocommon/banddata.h>
-#include "../gridding/gainmode.h"
-#include "../gridding/msgridder.h"
+#include <aocommon/polarization.h>
+#include "gridding/gainmode.h"
+#include "gridding/msgridder.h"
 #else
 namespace aocommon {
 class BandData;
@@ -39,6 +42,20 @@ class BandData;
 namespace wsclean {
 /* gridding/gainmode.h:16-31 */
 enum class GainMode { kXX, kYY, kTrace, k2VisDiagonal, kFull };
+
+/* gridding/gainmode.h:33-46 */
+constexpr std::size_t GetNVisibilities(GainMode mode) {
+  return mode == GainMode::k2VisDiagonal ? 2 : mode == GainMode::kFull ? 4 : 1;
+}
+
+/* gridding/gainmode.h:52-95 with the polarisation as a WGPU_POL_* value;
+ * throws for the combinations the reference rejects. */
+inline GainMode SelectGainMode(int polarization, std::size_t n_visibility_polarizations) {
+  int mode = 0;
+  if (wgpu_select_gain_mode(polarization, n_visibility_polarizations, &mode) != WGPU_OK)
+    throw std::runtime_error(std::string("wgpu: ") + wgpu_last_error());
+  return static_cast<GainMode>(mode);
+}
 class MsGridder;
 }  // namespace wsclean
 #endif
@@ -54,6 +71,56 @@ struct GpuCorrectionTable {
   size_t nparms = 2;
   int polarization = WGPU_POL_STOKES_I;
 };
+
+#ifdef WGPU_WITH_WSCLEAN
+/* aocommon::PolarizationEnum -> the WGPU_POL_* target of the device collapse
+ * (msgridderdata.h:36-52 collapses to these). */
+inline int WgpuPolarization(aocommon::PolarizationEnum polarization) {
+  switch (polarization) {
+    case aocommon::Polarization::StokesI: return WGPU_POL_STOKES_I;
+    case aocommon::Polarization::StokesQ: return WGPU_POL_STOKES_Q;
+    case aocommon::Polarization::StokesU: return WGPU_POL_STOKES_U;
+    case aocommon::Polarization::StokesV: return WGPU_POL_STOKES_V;
+    case aocommon::Polarization::XX: return WGPU_POL_XX;
+    case aocommon::Polarization::XY: return WGPU_POL_XY;
+    case aocommon::Polarization::YX: return WGPU_POL_YX;
+    case aocommon::Polarization::YY: return WGPU_POL_YY;
+    default:
+      throw std::runtime_error("wgpu: the device collapse supports Stokes I/Q/U/V and the "
+                               "linear correlations only");
+  }
+}
+
+/* What MsGridderData::ApplyCorrections (msgridderdata.h:710-758) applies to the
+ * rows of a correction callback, as a solution table for the device.  Returns
+ * false where the reference applies no correction (not a facet, or the PSF of
+ * the main image, or no h5parm solutions); fills *table with the gridder's
+ * cached solutions (VisibilityModifier::_cachedParmResponse of this
+ * measurement set, n_times x n_channels x n_antennas x nparms) and returns
+ * true otherwise.  Throws for the two cases the device path does not cover:
+ * facet beams (evaluated by EveryBeam on the host) and the direction-
+ * dependent PSF (forward, then conjugated solutions). */
+inline bool WgpuCorrectionTable(const MsGridder &gridder, size_t n_channels, size_t n_antennas,
+                                GpuCorrectionTable *table) {
+  if (!gridder.IsFacet() || gridder.GetPsfMode() == PsfMode::kSingle) return false;
+  const Settings &settings = gridder.GetSettings();
+  if (settings.applyFacetBeam || settings.gridWithBeam)
+    throw std::runtime_error("wgpu: facet beam corrections are evaluated by EveryBeam on the "
+                             "host; the GPU correction path applies h5parm solutions only");
+  const VisibilityModifier &modifier = gridder.GetVisibilityModifier();
+  if (!modifier.HasH5Parm()) return false;
+  if (gridder.GetPsfMode() == PsfMode::kDirectionDependent)
+    throw std::runtime_error("wgpu: direction-dependent PSF gridding (forward, then conjugated "
+                             "solutions) is not on the device");
+  const size_t ms_index = gridder.OriginalMsIndex();
+  const std::vector<std::complex<float>> &solutions = modifier.CachedParmResponse(ms_index);
+  table->solutions = solutions.data();
+  table->nparms = modifier.NValuesPerSolution(ms_index);
+  table->n_times = solutions.size() / (n_channels * n_antennas * table->nparms);
+  table->polarization = WgpuPolarization(gridder.Polarization());
+  return true;
+}
+#endif
 
 /* gridder_simple.h:19-41 */
 class WGriddingGridderBase {
@@ -136,10 +203,26 @@ class WGriddingGridder_Simple final : public WGriddingGridderBase {
       MsGridder *gridder, size_t n_antenna) override {
     (void)selected_band;
 #ifdef WGPU_WITH_WSCLEAN
-    const GpuCorrectionTable table = gridder->GpuCorrections();
-    AddInversionDataWithCorrections(mode, n_polarizations, n_rows, uvws, frequencies,
-                                    n_channels, antennas, visibilities, time_offsets, table,
-                                    n_antenna);
+    GpuCorrectionTable table;
+    if (WgpuCorrectionTable(*gridder, n_channels, n_antenna, &table)) {
+      AddInversionDataWithCorrections(mode, n_polarizations, n_rows, uvws, frequencies,
+                                      n_channels, antennas, visibilities, time_offsets, table,
+                                      n_antenna);
+    } else {
+      // no correction applies; the rows are still collapsed
+      // (callback_implementation.h:91-94): unit solutions, one time slot
+      const size_t nparms = n_polarizations == 4 ? 4 : 2;
+      std::vector<std::complex<float>> unit(n_channels * n_antenna * nparms);
+      for (size_t k = 0; k < unit.size(); k += nparms) unit[k] = unit[k + nparms - 1] = 1.0f;
+      const std::vector<size_t> first_slot(n_rows, 0);
+      table.solutions = unit.data();
+      table.n_times = 1;
+      table.nparms = nparms;
+      table.polarization = WgpuPolarization(gridder->Polarization());
+      AddInversionDataWithCorrections(mode, n_polarizations, n_rows, uvws, frequencies,
+                                      n_channels, antennas, visibilities, first_slot.data(),
+                                      table, n_antenna);
+    }
 #else
     (void)mode; (void)n_polarizations; (void)n_rows; (void)uvws; (void)frequencies;
     (void)n_channels; (void)antennas; (void)visibilities; (void)time_offsets;

@@ -80,3 +80,65 @@ def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
     # uniform diagonal gain 1.5+0.5i, XX mode: |g|^2 = 2.5 times the prediction
     pred_corr = np.fromfile(prefix + "pred_corr.bin", np.complex64)
     np.testing.assert_allclose(pred_corr, 2.5 * pred, rtol=1e-5, atol=1e-6 * np.abs(pred).max())
+
+
+CALLBACK_SRC = os.path.join(ROOT, "tests", "cpp", "wsclean_callback_test.cpp")
+WSCLEAN_IFACE = os.path.join(ROOT, "tests", "cpp", "wsclean_iface")
+
+
+def _build_callback(tmp_path):
+    exe = str(tmp_path / "wsclean_callback_test")
+    lib_dir = os.path.join(ROOT, "wsclean_gb300", "_build")
+    cmd = ["g++", "-std=c++17", "-O1", "-DWGPU_WITH_WSCLEAN", "-I", os.path.join(ROOT, "include"),
+           "-I", WSCLEAN_IFACE, CALLBACK_SRC, "-o", exe, "-L", lib_dir, "-lwgpu",
+           f"-Wl,-rpath,{lib_dir}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def test_wsclean_callback_path_compiles(tmp_path, wgpu_lib):
+    """The correction callback as WSClean builds it (WGPU_WITH_WSCLEAN): it names
+    only existing MsGridder / VisibilityModifier members and the two accessors
+    the drop-in adds."""
+    assert os.path.exists(_build_callback(tmp_path))
+
+
+@pytest.mark.gpu
+def test_wsclean_callback_reads_cached_solutions(tmp_path, wgpu_lib, oracle_lib):
+    """The callback reads the gridder's cached full-Jones solutions: the image
+    equals the explicit-table path's; outside a facet it applies no gains (the
+    rows are only collapsed, as the oracle collapses them); the direction-
+    dependent PSF and facet beams are rejected."""
+    exe = _build_callback(tmp_path)
+    W, dl, n_chan, n_ant, n_t = 128, 4e-4, 4, 6, 3
+    uvw, freq, _ = synthetic.random_points(600, n_chan, W, dl, seed=51, w_scale=1.0)
+    rng = np.random.default_rng(52)
+    n_rows = uvw.shape[0]
+    vis4 = (rng.standard_normal((n_rows, n_chan, 4)) +
+            1j * rng.standard_normal((n_rows, n_chan, 4))).astype(np.complex64)
+    ant = np.stack([rng.integers(0, n_ant, n_rows), rng.integers(0, n_ant, n_rows)],
+                   1).astype(np.uint64)
+    tof = rng.integers(0, n_t, n_rows).astype(np.uint64)
+    eye = np.array([1, 0, 0, 1], np.complex64)
+    sol = (eye + 0.2 * (rng.standard_normal((n_t, n_chan, n_ant, 4)) +
+                        1j * rng.standard_normal((n_t, n_chan, n_ant, 4)))).astype(np.complex64)
+    files = []
+    for name, arr in (("uvw", uvw), ("freq", freq), ("vis", vis4), ("ant", ant), ("tof", tof),
+                      ("sol", sol)):
+        path = str(tmp_path / f"{name}.bin")
+        np.ascontiguousarray(arr).tofile(path)
+        files.append(path)
+    prefix = str(tmp_path / "out_")
+    r = subprocess.run([exe, str(W), str(n_rows), str(n_chan), str(n_ant), str(n_t), repr(dl)] +
+                       files, capture_output=True, text=True, env=dict(os.environ, OUT=prefix))
+    assert r.returncode == 0, r.stderr
+    img = lambda n: np.fromfile(prefix + n + ".bin", np.float32).astype(np.float64)
+    cb, ex, unc = img("callback"), img("explicit"), img("uncorrected")
+    ok = np.isfinite(ex)
+    assert np.linalg.norm(cb[ok] - ex[ok]) <= 1e-6 * np.linalg.norm(ex[ok])
+    # outside a facet: identity gains, Stokes I collapse, plain gridding
+    unit = np.broadcast_to(eye, sol.shape).copy()
+    collapsed = oracle_lib.apply_gains(4, 4, vis4, ant, tof, unit, 4, n_ant)
+    ref = oracle_lib.dft_invert(uvw, freq, collapsed, W, W, dl, dl)
+    assert np.linalg.norm(unc - ref) <= 1e-4 * np.linalg.norm(ref)
+    assert list(np.fromfile(prefix + "threw.bin", np.int32)) == [1, 1]

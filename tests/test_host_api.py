@@ -186,3 +186,37 @@ def test_sizing_functions_run_without_a_device(wgpu_lib):
     assert wres.actual_trimmed_size(1000, 600, 1.2) == (836, 500)
     w, h, px, py = wres.small_inversion_size(1000, 1000, 1e-4, 1e-4, 1e-3)
     assert (w, h) == (200, 200) and abs(px - 5e-4) < 1e-15
+
+
+def test_gain_mode_visibility_counts(wgpu_lib):
+    """GetNVisibilities, gridding/gainmode.h:33-46."""
+    assert [_lib.gain_mode_n_visibilities(m) for m in range(5)] == [1, 1, 1, 2, 4]
+    assert _lib.gain_mode_n_visibilities(5) == 0
+    assert _lib.gain_mode_n_visibilities(-1) == 0
+
+
+def test_select_gain_mode_every_combination(wgpu_lib):
+    """SelectGainMode, gridding/gainmode.h:52-95, over every polarisation the
+    library names and stored-polarisation counts 0..5: the accepted pairs and
+    their modes, everything else rejected."""
+    P = _lib
+    stokes = {P.POL_I, P.POL_Q, P.POL_U, P.POL_V}
+    all_pols = list(range(15))
+    expected = {}
+    for pol in all_pols:
+        # one stored polarisation: XX, YY, or the trace for anything else
+        expected[(pol, 1)] = (P.GAIN_XX if pol == P.POL_XX else
+                              P.GAIN_YY if pol == P.POL_YY else P.GAIN_TRACE)
+        if pol in (P.POL_I, P.POL_DIAGONAL_INSTRUMENTAL, P.POL_XX, P.POL_YY):
+            expected[(pol, 2)] = P.GAIN_2VIS_DIAGONAL
+        if pol in stokes | {P.POL_FULL_STOKES, P.POL_INSTRUMENTAL, P.POL_XX, P.POL_YY}:
+            expected[(pol, 4)] = P.GAIN_FULL
+    for pol in all_pols:
+        for n in range(6):
+            if (pol, n) in expected:
+                assert P.select_gain_mode(pol, n) == expected[(pol, n)], (pol, n)
+            else:
+                with pytest.raises(P.WgpuError):
+                    P.select_gain_mode(pol, n)
+    with pytest.raises(P.WgpuError):
+        P.select_gain_mode(15, 1)

@@ -21,7 +21,8 @@ NOALLOC_MAX_VISIBILITIES = 1 << 20
 NOALLOC_MAX_CHANNELS = 4096
 
 GAIN_XX, GAIN_YY, GAIN_TRACE, GAIN_2VIS_DIAGONAL, GAIN_FULL = range(5)
-POL_I, POL_Q, POL_U, POL_V, POL_XX, POL_XY, POL_YX, POL_YY = range(8)
+(POL_I, POL_Q, POL_U, POL_V, POL_XX, POL_XY, POL_YX, POL_YY, POL_RR, POL_RL, POL_LR, POL_LL,
+ POL_FULL_STOKES, POL_INSTRUMENTAL, POL_DIAGONAL_INSTRUMENTAL) = range(15)
 
 
 class WgpuError(RuntimeError):
@@ -116,6 +117,8 @@ I = C.c_int
 _PROTOS = {
     "wgpu_last_error": (C.c_char_p, []),
     "wgpu_version": (C.c_char_p, []),
+    "wgpu_gain_mode_n_visibilities": (SZ, [I]),
+    "wgpu_select_gain_mode": (I, [I, SZ, C.POINTER(I)]),
     "wgpu_plan_make": (I, [C.POINTER(PlanRequest), C.POINTER(Plan)]),
     "wgpu_gridder_create": (I, [SZ, SZ, SZ, SZ, D, D, D, D, SZ, D, SZ, I, I, C.POINTER(P)]),
     "wgpu_gridder_destroy": (None, [P]),
@@ -216,6 +219,19 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def gain_mode_n_visibilities(mode):
+    """GetNVisibilities (gridding/gainmode.h:33-46)."""
+    return int(lib().wgpu_gain_mode_n_visibilities(mode))
+
+
+def select_gain_mode(polarization, n_visibility_polarizations):
+    """SelectGainMode (gridding/gainmode.h:52-95); raises WgpuError for the
+    combinations the reference rejects."""
+    m = C.c_int()
+    check(lib().wgpu_select_gain_mode(polarization, n_visibility_polarizations, C.byref(m)))
+    return m.value
 
 
 def exported_symbols():

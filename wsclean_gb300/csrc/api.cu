@@ -753,6 +753,56 @@ const char *wgpu_last_error(void) { return g_last_error.c_str(); }
 
 const char *wgpu_version(void) { return "wgpu 0.1 (sm_103a)"; }
 
+size_t wgpu_gain_mode_n_visibilities(int mode) {
+  switch (mode) {
+    case WGPU_GAIN_XX:
+    case WGPU_GAIN_YY:
+    case WGPU_GAIN_TRACE:
+      return 1;
+    case WGPU_GAIN_2VIS_DIAGONAL:
+      return 2;
+    case WGPU_GAIN_FULL:
+      return 4;
+    default:
+      return 0;
+  }
+}
+
+int wgpu_select_gain_mode(int polarization, size_t n_visibility_polarizations, int *mode) {
+  if (!mode) return fail(WGPU_ERR_INVALID, "null mode");
+  if (polarization < WGPU_POL_STOKES_I || polarization > WGPU_POL_DIAGONAL_INSTRUMENTAL)
+    return fail(WGPU_ERR_INVALID, "unknown polarization");
+  const bool stokes = polarization <= WGPU_POL_STOKES_V;
+  const bool xx_or_yy = polarization == WGPU_POL_XX || polarization == WGPU_POL_YY;
+  switch (n_visibility_polarizations) {
+    case 1:
+      // every polarisation other than XX and YY (Stokes I, RR, other Stokes)
+      // is corrected with the trace
+      *mode = polarization == WGPU_POL_XX   ? WGPU_GAIN_XX
+              : polarization == WGPU_POL_YY ? WGPU_GAIN_YY
+                                            : WGPU_GAIN_TRACE;
+      return WGPU_OK;
+    case 2:
+      if (polarization == WGPU_POL_STOKES_I || polarization == WGPU_POL_DIAGONAL_INSTRUMENTAL ||
+          xx_or_yy) {
+        *mode = WGPU_GAIN_2VIS_DIAGONAL;
+        return WGPU_OK;
+      }
+      break;
+    case 4:
+      if (polarization == WGPU_POL_FULL_STOKES || polarization == WGPU_POL_INSTRUMENTAL ||
+          stokes || xx_or_yy) {
+        *mode = WGPU_GAIN_FULL;
+        return WGPU_OK;
+      }
+      break;
+  }
+  return fail(WGPU_ERR_INVALID, "invalid combination of polarization (" +
+                                    std::to_string(polarization) +
+                                    ") and n_visibility_polarizations (" +
+                                    std::to_string(n_visibility_polarizations) + ")");
+}
+
 int wgpu_plan_make(const wgpu_plan_request_t *request, wgpu_plan_t *plan) {
   if (!request || !plan) return fail(WGPU_ERR_INVALID, "null argument");
   return guarded([&] { *plan = make_plan(*request); });
