@@ -658,10 +658,19 @@ int wgpu_gridder_add_inversion_rows(wgpu_gridder_t *gridder, const wgpu_imagewei
  * wgpu_prepare_rows, the conjugated gains of its antennas are applied to its
  * correlations before ApplyWeights, and it is collapsed and gridded, all on
  * the device.  mode / n_pol, antenna_pairs, time_offsets and the solution
- * table as in wgpu_gridder_add_inversion_data_corrected.  correction_sum
- * (TRACE only; NULL otherwise) accumulates the scalar AverageCorrection sum
- * |g|^2 w iw (averagecorrection.h:36-50); the matrix-valued sums of the other
- * modes are not provided. */
+ * table as in wgpu_gridder_add_inversion_data_corrected.  correction_sum (may
+ * be NULL) accumulates the AverageCorrection sum (averagecorrection.h:36-50)
+ * of the gridded samples, with w the visibility weight of the first
+ * correlation times the imaging weight:
+ *   TRACE:  correction_sum[0] += |g|^2 w, g = (g2[0] conj(g1[0]) +
+ *           g2[3] conj(g1[3])) / 2;
+ *   others: correction_sum[0..31] += 0.5 w (a^H a + b^H b) with the
+ *           Kronecker products a = G1 (x) G2 and b = G2 (x) G1, a Hermitian
+ *           4 x 4 complex matrix stored row-major as (re, im) pairs (element
+ *           (2i + k, 2j + l) of G1 (x) G2 is G1[i][j] G2[k][l]).  aocommon's
+ *           packed HMatrix4x4 storage is not reproduced; a^H a is used where
+ *           the reference's HermitianSquare order is not pinned (the two orders
+ *           agree for diagonal solutions, which its known answers fix). */
 int wgpu_gridder_add_inversion_rows_corrected(
     wgpu_gridder_t *gridder, const wgpu_imageweights_t *iw, const wgpu_row_weighting_t *rw,
     int mode, size_t n_pol, size_t n_rows, size_t n_chan, const double *uvw,

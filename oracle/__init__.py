@@ -100,6 +100,7 @@ def lib():
         L.oracle_forward_gains.restype = I
         L.oracle_forward_gains.argtypes = [I, SZ, SZ, SZ, P, P, P, P, SZ, SZ, I, P]
         L.oracle_apply_conjugated_gain.argtypes = [I, P, P, P]
+        L.oracle_correction_matrix_add.argtypes = [P, P, D, P]
         L.oracle_apply_gain.argtypes = [I, P, P, P]
         I64 = C.c_int64
         L.oracle_weights_dims.argtypes = [SZ, SZ, D, C.POINTER(I64), C.POINTER(I64)]
@@ -364,6 +365,19 @@ def apply_conjugated_gain(mode, vis, g1, g2):
     return v
 
 
+def correction_matrix_add(g1, g2, weight, total=None):
+    """AverageCorrection::Add in matrix form: returns total (4 x 4 complex,
+    zero when None) plus 0.5 w (a^H a + b^H b), a = G1 (x) G2, b = G2 (x) G1."""
+    a = np.ascontiguousarray(g1, np.complex64)
+    b = np.ascontiguousarray(g2, np.complex64)
+    s = np.zeros(32, np.float64)
+    if total is not None:
+        t = np.asarray(total, np.complex128).ravel()
+        s[0::2], s[1::2] = t.real, t.imag
+    lib().oracle_correction_matrix_add(_p(a), _p(b), float(weight), _p(s))
+    return (s[0::2] + 1j * s[1::2]).reshape(4, 4)
+
+
 def apply_gain(mode, vis, g1, g2):
     v = np.ascontiguousarray(vis, np.complex64).copy()
     a = np.ascontiguousarray(g1, np.complex64)
@@ -453,8 +467,9 @@ class ImageWeights:
         ant = np.ascontiguousarray(ant, np.uint64)
         tof = np.ascontiguousarray(tof, np.uint64)
         sol = np.ascontiguousarray(sol, np.complex64)
-        corr = np.zeros(1, np.float64)
+        corr = np.zeros(33, np.float64)
         lib().oracle_prepare_rows_corrected(*args, int(mode), _p(ant), _p(tof), _p(sol), nparms,
                                             n_ant, _p(corr))
         sums[4] = corr[0]
+        self.correction_matrix = (corr[1::2] + 1j * corr[2::2]).reshape(4, 4)
         return vis_out, w_out, iw_out, sums

@@ -1446,10 +1446,48 @@ void oracle_weights_sample(const double *grid, int64_t W, int64_t H, double psx,
   }
 }
 
+/* AverageCorrection::Add for the modes with a matrix sum (every mode but
+ * TRACE, averagecorrection.h:36-50): the Kronecker products a = G1 (x) G2 and
+ * b = G2 (x) G1 of the 2 x 2 gains (row-major, complex64 pairs) in double, and
+ * 0.5 w (a^H a + b^H b) added to sum, the 4 x 4 complex matrix row-major as
+ * 32 doubles (re, im).  Element ((i, k), (j, l)) of G1 (x) G2 is
+ * G1[i][j] G2[k][l], at row 2 i + k and column 2 j + l. */
+void oracle_correction_matrix_add(const float *g1, const float *g2, double w, double *sum) {
+  double a[32], b[32];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j)
+      for (int k = 0; k < 2; ++k)
+        for (int l = 0; l < 2; ++l) {
+          const int at = 2 * ((2 * i + k) * 4 + 2 * j + l);
+          const double x1 = g1[2 * (2 * i + j)], y1 = g1[2 * (2 * i + j) + 1];
+          const double x2 = g2[2 * (2 * k + l)], y2 = g2[2 * (2 * k + l) + 1];
+          a[at] = x1 * x2 - y1 * y2;
+          a[at + 1] = x1 * y2 + y1 * x2;
+          const double u1 = g2[2 * (2 * i + j)], v1 = g2[2 * (2 * i + j) + 1];
+          const double u2 = g1[2 * (2 * k + l)], v2 = g1[2 * (2 * k + l) + 1];
+          b[at] = u1 * u2 - v1 * v2;
+          b[at + 1] = u1 * v2 + v1 * u2;
+        }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      double re = 0.0, im = 0.0;
+      for (int q = 0; q < 4; ++q) {
+        /* conj(m[q][r]) m[q][c] for m = a and b */
+        const double *ar = a + 2 * (q * 4 + r), *ac = a + 2 * (q * 4 + c);
+        const double *br = b + 2 * (q * 4 + r), *bc = b + 2 * (q * 4 + c);
+        re += ar[0] * ac[0] + ar[1] * ac[1] + br[0] * bc[0] + br[1] * bc[1];
+        im += ar[0] * ac[1] - ar[1] * ac[0] + br[0] * bc[1] - br[1] * bc[0];
+      }
+      sum[2 * (r * 4 + c)] += 0.5 * w * re;
+      sum[2 * (r * 4 + c) + 1] += 0.5 * w * im;
+    }
+}
+
 /* With a gain table (sol != NULL): ApplyConjugatedParmResponse between the
  * weighting and ApplyWeights (msgridderdata.h:888-927,
- * visibilitymodifier.h:538-594), and for TRACE the scalar AverageCorrection
- * sum (averagecorrection.h:36-50) into *corr. */
+ * visibilitymodifier.h:538-594), and the AverageCorrection sum
+ * (averagecorrection.h:36-50): for TRACE the scalar into corr[0], for the other
+ * modes the matrix into corr[1..32] (oracle_correction_matrix_add). */
 static void prepare_rows_impl(const double *grid, int64_t W, int64_t H, double psx, double psy,
                               int psf_mode, double psf_dl, double psf_dm, int subtract_model,
                               int visibility_weighting, int polarization, size_t n_pol,
@@ -1522,7 +1560,10 @@ static void prepare_rows_impl(const double *grid, int64_t W, int64_t H, double p
           const cf a = cmul(ld(g2, 0), cconj(ld(g1, 0))), b = cmul(ld(g2, 3), cconj(ld(g1, 3)));
           const cf g = {0.5f * (a.re + b.re), 0.5f * (a.im + b.im)};
           const float norm = g.re * g.re + g.im * g.im;
-          *corr += norm * (wrow[ch * n_pol] * scratch_iw[ch]);
+          corr[0] += norm * (wrow[ch * n_pol] * scratch_iw[ch]);
+        } else { /* the matrix form of the other modes */
+          oracle_correction_matrix_add(g1, g2, (double)(wrow[ch * n_pol] * scratch_iw[ch]),
+                                       corr + 1);
         }
       }
     for (size_t ch = 0; ch < n_chan; ++ch) /* ApplyWeights, :760-789 */

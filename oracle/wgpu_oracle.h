@@ -111,6 +111,14 @@ double oracle_wgrid_time_predict_parts(const OraclePlan *plan, size_t n_rows,
                                        int n_threads, double plane_fraction,
                                        double *plane_seconds);
 
+/* AverageCorrection::Add, matrix form (averagecorrection.h:36-50): adds
+ * 0.5 w ((G1 (x) G2)^H (G1 (x) G2) + (G2 (x) G1)^H (G2 (x) G1)) to sum, a 4 x 4
+ * complex matrix stored row-major as 32 doubles (re, im).  g1, g2: 2 x 2
+ * gains, row-major, interleaved complex64.  aocommon's HermitianSquare is
+ * absent from the reference tree; M^H M is used (for diagonal gains both
+ * orders agree, which the reference's known answers pin). */
+void oracle_correction_matrix_add(const float *g1, const float *g2, double w, double *sum);
+
 /* ES kernel value at z in [-1,1] and its continuous FT in cell units. */
 double oracle_es_kernel(double beta, double z);
 double oracle_es_fourier(double beta, int support, double f);
@@ -190,9 +198,11 @@ void oracle_prepare_rows(const double *grid, int64_t width, int64_t height, doub
 /* The same with h5parm corrections: the conjugated gains of each row's
  * antennas applied to its correlations between the weighting and
  * ApplyWeights (msgridderdata.h:888-927, visibilitymodifier.h:538-594);
- * layouts as oracle_apply_gains.  For TRACE (mode 2) *correction_sum +=
- * |g|^2 w iw with g = (g2[0] conj(g1[0]) + g2[3] conj(g1[3])) / 2
- * (averagecorrection.h:36-50, 104-118). */
+ * layouts as oracle_apply_gains.  correction_sum holds 33 doubles: for TRACE
+ * (mode 2) correction_sum[0] += |g|^2 w iw with g = (g2[0] conj(g1[0]) +
+ * g2[3] conj(g1[3])) / 2 (averagecorrection.h:36-50, 104-118); for the other
+ * modes correction_sum[1..32] accumulates the matrix sum of
+ * oracle_correction_matrix_add with weight w iw. */
 void oracle_prepare_rows_corrected(const double *grid, int64_t width, int64_t height, double psx,
                                    double psy, int psf_mode, double psf_dl, double psf_dm,
                                    int subtract_model, int visibility_weighting, int polarization,

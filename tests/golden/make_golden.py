@@ -3,8 +3,9 @@
 gains_kat.json
     The known-answer cases of the reference's gain tests
     (tests/gridding/tvisibilitymodifier.cpp:13-28 constants; expectations of
-    apply_h5parm :107-115 and apply_conjugate_h5parm :117-139), evaluated in
-    complex64 exactly as the test states them.
+    apply_h5parm :107-115 and apply_conjugate_h5parm :117-139, including the
+    latter's correction-sum elements), evaluated in complex64 / float exactly
+    as the test states them.
 dft_small.npz
     A 64 x 64 direct-FT inversion and prediction of a seeded random case,
     computed by the oracle (FP64).  Pins the oracle across host architectures.
@@ -49,10 +50,18 @@ def gains_kat():
                                     yy * A1_PARM_Y * np.conj(A2_PARM_Y)])))
     # apply_conjugate_h5parm: ApplyConjugatedParmResponse<kApplyAndSum, k2VisDiagonal> on {-1, 2}
     xx, yy = np.complex64(-1.0), np.complex64(2.0)
+    # and its correction sum (:128-136): elements 0, 5, 10, 15 of the 4 x 4
+    # matrix (row-major), unit visibility and imaging weights
+    nx = np.float32(abs(A1_PARM_X) ** 2 * abs(A2_PARM_X) ** 2)
+    ny = np.float32(abs(A1_PARM_Y) ** 2 * abs(A2_PARM_Y) ** 2)
+    nxy = np.float32(0.5 * (abs(A1_PARM_X * np.conj(A2_PARM_Y)) ** 2 +
+                            abs(A2_PARM_X * np.conj(A1_PARM_Y)) ** 2))
     cases.append(dict(name="apply_conjugate_h5parm", direction="conjugated", mode=3,
                       vis=c2l([xx, yy]), g1=c2l(g1), g2=c2l(g2),
                       expected=c2l([xx * np.conj(A1_PARM_X) * A2_PARM_X,
-                                    yy * np.conj(A1_PARM_Y) * A2_PARM_Y])))
+                                    yy * np.conj(A1_PARM_Y) * A2_PARM_Y]),
+                      correction_sum={"0": float(nx), "5": float(nxy), "10": float(nxy),
+                                      "15": float(ny)}))
     return dict(tolerance=1e-5, source="tests/gridding/tvisibilitymodifier.cpp", cases=cases)
 
 

@@ -203,3 +203,27 @@ def test_es_fourier_matches_numeric_integral(oracle_lib):
     for f in (0.0, 0.1, 0.37):
         num = (W / 2) * np.trapezoid(phi * np.cos(np.pi * f * W * z), z)
         assert abs(oracle_lib.es_fourier(beta, W, f) - num) < 1e-6 * abs(num)
+
+
+def test_correction_matrix_known_answers(oracle_lib):
+    """AverageCorrection::Add in matrix form against the correction-sum known
+    answers of tests/gridding/tvisibilitymodifier.cpp:128-136 (diagonal gains,
+    unit weights), and its algebra: Hermitian, and for full Jones the
+    symmetrised Kronecker form 0.5 w (P (x) Q + Q (x) P), P = G1^H G1,
+    Q = G2^H G2."""
+    kat = json.load(open(os.path.join(GOLDEN, "gains_kat.json")))
+    case = next(c for c in kat["cases"] if "correction_sum" in c)
+    m = oracle_lib.correction_matrix_add(_cplx(case["g1"]), _cplx(case["g2"]), 1.0)
+    for k, v in case["correction_sum"].items():
+        np.testing.assert_allclose(m.ravel()[int(k)].real, v, rtol=kat["tolerance"])
+    rng = np.random.default_rng(8)
+    g1 = (rng.standard_normal(4) + 1j * rng.standard_normal(4)).astype(np.complex64)
+    g2 = (rng.standard_normal(4) + 1j * rng.standard_normal(4)).astype(np.complex64)
+    m = oracle_lib.correction_matrix_add(g1, g2, 0.7)
+    np.testing.assert_allclose(m, m.conj().T, atol=1e-12)
+    G1, G2 = g1.astype(np.complex128).reshape(2, 2), g2.astype(np.complex128).reshape(2, 2)
+    P, Q = G1.conj().T @ G1, G2.conj().T @ G2
+    np.testing.assert_allclose(m, 0.5 * 0.7 * (np.kron(P, Q) + np.kron(Q, P)), rtol=1e-12)
+    # sums accumulate
+    np.testing.assert_allclose(oracle_lib.correction_matrix_add(g1, g2, 0.7, total=m), 2 * m,
+                               rtol=1e-12)

@@ -289,7 +289,8 @@ def test_add_inversion_rows_corrected_matches_oracle(oracle_lib, mode, n_pol, np
     """Raw rows with h5parm gains: weighting, conjugated gains before
     ApplyWeights, collapse and gridding on the device give the image of the
     oracle-prepared rows (gains in FP32 with fused multiply-adds: 1e-5), and
-    the TRACE correction sum matches the oracle's."""
+    the correction sum (TRACE: scalar; the other modes: the 4 x 4 matrix of
+    AverageCorrection::Add) matches the oracle's to 1e-5."""
     from wsclean_gb300.weights import add_inversion_rows_corrected
     W, Wt, dl, eps = 160, 128, 4e-4, 1e-5
     uvw, freq, vis1 = synthetic.random_points(700, 5, Wt, dl, seed=51, w_scale=2.0)
@@ -322,7 +323,7 @@ def test_add_inversion_rows_corrected_matches_oracle(oracle_lib, mode, n_pol, np
     g1.InitializeInversion()
     acc, corr = add_inversion_rows_corrected(g1, dev, mode, uvw, freq, weights, vis, ant, tof,
                                              sol, nparms, n_t, n_ant, selected=sel,
-                                             with_correction_sum=(mode == 2))
+                                             with_correction_sum=True)
     g1.FinalizeImage(1.0)
     a = g1.RealImage().reshape(W, W)
     g2 = WGriddingGridder_Simple(W, W, Wt, Wt, dl, dl, 0.0, 0.0, 1, epsilon=eps,
@@ -339,6 +340,11 @@ def test_add_inversion_rows_corrected_matches_oracle(oracle_lib, mode, n_pol, np
     if mode == 2:
         assert corr > 0
         np.testing.assert_allclose(corr, sums[4], rtol=1e-5)
+    else:
+        mat = ref.correction_matrix
+        assert np.abs(mat).max() > 0
+        np.testing.assert_allclose(corr, corr.conj().T, atol=1e-9 * np.abs(mat).max())
+        assert np.abs(corr - mat).max() <= 1e-5 * np.abs(mat).max()
     # an antenna index outside the table is reported
     bad = ant.copy()
     bad[3, 0] = n_ant

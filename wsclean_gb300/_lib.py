@@ -191,7 +191,7 @@ _PROTOS = {
                                      P, P, P, C.POINTER(WeightSums)]),
     "wgpu_gridder_add_inversion_rows_corrected": (
         I, [P, P, C.POINTER(RowWeighting), I, SZ, SZ, SZ, P, P, P, P, P, P, P, P, P, SZ, SZ, SZ,
-            C.POINTER(WeightSums), C.POINTER(D)]),
+            C.POINTER(WeightSums), P]),
     "wgpu_calculate_fft_size": (I, [SZ, D, D, C.POINTER(SZ), C.POINTER(SZ)]),
     "wgpu_small_inversion_size": (I, [SZ, SZ, D, D, D, C.POINTER(SZ), C.POINTER(SZ),
                                       C.POINTER(D), C.POINTER(D)]),

@@ -995,10 +995,6 @@ int wgpu_gridder_add_inversion_rows_corrected(
   const size_t want = mode == WGPU_GAIN_FULL ? 4 : mode == WGPU_GAIN_2VIS_DIAGONAL ? 2 : 1;
   if (n_pol != want) return fail(WGPU_ERR_INVALID, "gain mode and n_polarizations do not match");
   if (nparms != 2 && nparms != 4) return fail(WGPU_ERR_INVALID, "nparms must be 2 or 4");
-  if (correction_sum && mode != WGPU_GAIN_TRACE)
-    return fail(WGPU_ERR_INVALID,
-                "correction sums are available for the TRACE gain mode only (scalar "
-                "AverageCorrection)");
   if (n_rows && n_chan &&
       (!uvw || !freq || !weights || (rw->psf_mode == WGPU_PSF_NONE && !vis) ||
        (rw->subtract_model && !model) || !antenna_pairs || !time_offsets || !solutions))
@@ -1026,6 +1022,7 @@ int wgpu_gridder_add_inversion_rows_corrected(
     gt.n_times = (int64_t)n_times;
     gt.n_ant = (int64_t)n_ant;
     gt.err = (int *)g->arena.get(kSlotOutVis, sizeof(int) * 4);
+    gt.sum_matrix = correction_sum != nullptr && mode != WGPU_GAIN_TRACE;
     float2 *dc = (float2 *)g->arena.get(kSlotVis, sizeof(float2) * n);
     auto *dsum = (WeightSumsDev *)g->arena.get(kSlotRowSums, sizeof(WeightSumsDev));
     void *work = g->arena.get(kSlotRowWork, pass_work_bytes((int64_t)n_rows, (int64_t)n_chan));
@@ -1043,7 +1040,23 @@ int wgpu_gridder_add_inversion_rows_corrected(
     invert_device(g, n_rows, n_chan, du, df, (const float *)dc);
     WGPU_CUDA(cudaStreamSynchronize(g->stream));
     add_weight_sums(hs, sums);
-    if (correction_sum) *correction_sum += hs.correction;
+    if (correction_sum) {
+      if (mode == WGPU_GAIN_TRACE) {
+        *correction_sum += hs.correction;
+      } else {
+        // the Hermitian matrix, row-major, (re, im) per element
+        static const int kRow[6] = {0, 0, 0, 1, 1, 2}, kCol[6] = {1, 2, 3, 2, 3, 3};
+        for (int d = 0; d < 4; ++d) correction_sum[2 * (d * 4 + d)] += hs.matrix[d];
+        for (int e = 0; e < 6; ++e) {
+          const double re = hs.matrix[4 + 2 * e], im = hs.matrix[5 + 2 * e];
+          const int r = kRow[e], c = kCol[e];
+          correction_sum[2 * (r * 4 + c)] += re;
+          correction_sum[2 * (r * 4 + c) + 1] += im;
+          correction_sum[2 * (c * 4 + r)] += re;
+          correction_sum[2 * (c * 4 + r) + 1] -= im;
+        }
+      }
+    }
   });
 }
 

@@ -496,7 +496,49 @@ struct PrepAcc {
   FloatSum vws, total, corr;
   float vmax = 0.0f;
   uint32_t count = 0;
+  double mat[16] = {};  // matrix correction sum (WeightSumsDev::matrix layout)
 };
+
+// AverageCorrection::Add in matrix form (averagecorrection.h:36-50) for one
+// sample: 0.5 w (a^H a + b^H b) with a = G1 (x) G2, b = G2 (x) G1.  By the
+// mixed-product rule a^H a = P (x) Q and b^H b = Q (x) P with the 2 x 2
+// Hermitian P = G1^H G1, Q = G2^H G2, so the sum is 0.5 w (P (x) Q + Q (x) P);
+// its 16 independent reals are added to mat (WeightSumsDev::matrix layout).
+__device__ __forceinline__ void add_correction_matrix(const float2 *g1, const float2 *g2,
+                                                      float w, double *mat) {
+  // H = G^H G for G = [[g0, g1], [g2, g3]]: diagonal h0, h1 and h01
+  auto herm = [](const float2 *g, float *d0, float *d1, float2 *o) {
+    *d0 = g[0].x * g[0].x + g[0].y * g[0].y + g[2].x * g[2].x + g[2].y * g[2].y;
+    *d1 = g[1].x * g[1].x + g[1].y * g[1].y + g[3].x * g[3].x + g[3].y * g[3].y;
+    const float2 a = cm(cj(g[0]), g[1]), b = cm(cj(g[2]), g[3]);
+    *o = make_float2(a.x + b.x, a.y + b.y);
+  };
+  float p0, p1, q0, q1;
+  float2 p01, q01;
+  herm(g1, &p0, &p1, &p01);
+  herm(g2, &q0, &q1, &q01);
+  // element (2i + k, 2j + l) of P (x) Q + Q (x) P is P_ij Q_kl + Q_ij P_kl
+  auto el = [](float d0, float d1, float2 o, int i, int j) -> float2 {
+    if (i == j) return make_float2(i == 0 ? d0 : d1, 0.0f);
+    return i < j ? o : cj(o);
+  };
+  const double hw = 0.5 * (double)w;
+  constexpr int kRow[10] = {0, 1, 2, 3, 0, 0, 0, 1, 1, 2};
+  constexpr int kCol[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+#pragma unroll
+  for (int e = 0; e < 10; ++e) {
+    const int r = kRow[e], c = kCol[e];
+    const int i = r >> 1, k = r & 1, j = c >> 1, l = c & 1;
+    const float2 a = cm(el(p0, p1, p01, i, j), el(q0, q1, q01, k, l));
+    const float2 b = cm(el(q0, q1, q01, i, j), el(p0, p1, p01, k, l));
+    if (e < 4) {
+      mat[e] += hw * (double)(a.x + b.x);
+    } else {
+      mat[4 + 2 * (e - 4)] += hw * (double)(a.x + b.x);
+      mat[5 + 2 * (e - 4)] += hw * (double)(a.y + b.y);
+    }
+  }
+}
 
 template <int NPOL, bool VEC>
 __device__ __forceinline__ void load_weights(const float *p, float *w) {
@@ -614,6 +656,8 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, const GainTa
       const float2 a = cm(g2[0], cj(g1[0])), b = cm(g2[3], cj(g1[3]));
       const float2 g = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
       acc.corr.add(__fmul_rn(g.x * g.x + g.y * g.y, __fmul_rn(w[0], iw)));
+    } else if (gt.sum_matrix) {
+      add_correction_matrix(g1, g2, __fmul_rn(w[0], iw), acc.mat);
     }
   }
   float2 c[NPOL];
@@ -651,8 +695,20 @@ __device__ __forceinline__ void prep_sample(const RowWeighting &rw, const GainTa
   if (imaging_out) __stcs(imaging_out + e, iw);
 }
 
-// Block reduction of the accumulators and one set of atomics per block.
+// Block reduction of the accumulators and one set of atomics per block; with
+// MAT the matrix correction sum too (warp reductions, one atomic per warp and
+// value).
+template <bool MAT>
 __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
+  if constexpr (MAT) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      double v = acc.mat[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&sums->matrix[k], v);
+    }
+  }
   const double s_vws = block_sum(acc.vws.value());
   const double s_total = block_sum(acc.total.value());
   const double s_count = block_sum((double)acc.count);
@@ -679,7 +735,7 @@ __device__ void finish_prep_sums(PrepAcc &acc, WeightSumsDev *sums) {
 // First pass over a fixed grid of blocks: samples whose imaging-weight cell is
 // decided in FP32 are prepared; the others go to the pending list.
 template <int NPOL, bool VEC, bool CORR>
-__global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
+__global__ void __launch_bounds__(kThreads, CORR ? 2 : 5) prepare_rows_fast_kernel(
     WeightGridView g, RowWeighting rw, GainTable gt, uint32_t n, uint32_t n_chan,
     const double *uvw, const ChanScale *cs, const float2 *vis, const float *weights,
     const float2 *model, const uint8_t *selected, float2 *vis_out, float *weights_out,
@@ -705,7 +761,7 @@ __global__ void __launch_bounds__(kThreads, 5) prepare_rows_fast_kernel(
     }
     pending_push(pend, &s_count, undecided, e);
   }
-  finish_prep_sums(acc, sums);
+  finish_prep_sums<CORR>(acc, sums);
   if (threadIdx.x == 0) pend.counts[blockIdx.x] = s_count;
 }
 
@@ -730,7 +786,7 @@ __global__ void __launch_bounds__(kThreads) prepare_rows_exact_kernel(
                                  lambda, uvw, vis, weights, model, selected, vis_out, weights_out,
                                  imaging_out, acc);
   }
-  finish_prep_sums(acc, sums);
+  finish_prep_sums<CORR>(acc, sums);
 }
 
 __global__ void grid_to_float_kernel(const double *grid, int64_t n, float *gridf) {

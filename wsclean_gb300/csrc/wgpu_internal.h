@@ -326,6 +326,10 @@ struct WeightSumsDev {
   unsigned long long max_bits;  // bits of the largest positive weight (double)
   unsigned long long count;
   double correction;  // TRACE correction sum (corrected rows)
+  // matrix correction sum of the other modes (corrected rows): the Hermitian
+  // 4 x 4 matrix's diagonal (0,0) (1,1) (2,2) (3,3), then the real and
+  // imaginary parts of (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+  double matrix[16];
 };
 
 // Cached parm-response table of a corrected raw-row chunk (layouts as in
@@ -338,6 +342,7 @@ struct GainTable {
   int nparms = 2, mode = 0;
   int64_t n_times = 0, n_ant = 0;
   int *err = nullptr;
+  bool sum_matrix = false;  // accumulate the matrix correction sum (modes but TRACE)
 };
 void add_weight_sums(const WeightSumsDev &d, wgpu_weight_sums_t *sums);
 

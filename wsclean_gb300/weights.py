@@ -216,7 +216,8 @@ def add_inversion_rows_corrected(gridder, image_weights, mode, uvw, frequencies,
                                  **settings):
     """GetCollapsedVisibilities with h5parm corrections + AddInversionData on
     the device (wgpu_gridder_add_inversion_rows_corrected).  Returns (sums,
-    correction sum or None); the correction sum exists for the TRACE mode."""
+    correction sum or None): with with_correction_sum a float for TRACE and a
+    4 x 4 complex Hermitian matrix for the other modes."""
     rw = row_weighting(**settings)
     uvw, freq, wts, vis_a, mod_a, sel_a, (n_rows, n_chan, n_pol) = _row_inputs(
         uvw, frequencies, weights, vis, model, selected, rw)
@@ -225,9 +226,13 @@ def add_inversion_rows_corrected(gridder, image_weights, mode, uvw, frequencies,
     sol = np.ascontiguousarray(solutions, np.complex64)
     if sums is None:
         sums = _lib.WeightSums()
-    corr = C.c_double(0.0)
+    corr = np.zeros(32, np.float64)
     check(lib().wgpu_gridder_add_inversion_rows_corrected(
         gridder._h, image_weights.handle, C.byref(rw), int(mode), n_pol, n_rows, n_chan, ptr(uvw),
         ptr(freq), ptr(vis_a), ptr(wts), ptr(mod_a), ptr(sel_a), ptr(ant), ptr(tof), ptr(sol),
-        nparms, n_times, n_antenna, C.byref(sums), C.byref(corr) if with_correction_sum else None))
-    return sums, (corr.value if with_correction_sum else None)
+        nparms, n_times, n_antenna, C.byref(sums), ptr(corr) if with_correction_sum else None))
+    if not with_correction_sum:
+        return sums, None
+    if mode == _lib.GAIN_TRACE:
+        return sums, float(corr[0])
+    return sums, (corr[0::2] + 1j * corr[1::2]).reshape(4, 4)
