@@ -218,7 +218,8 @@ void end_call(wgpu_gridder *g) {
     *g->h_flags = 0;
     WGPU_CUDA(cudaMemsetAsync(g->d_flags, 0, sizeof(unsigned), g->stream));
     WGPU_CUDA(cudaStreamSynchronize(g->stream));
-    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (row transform prefetch)");
+    throw Error(WGPU_ERR_TIMEOUT,
+                "a bounded device wait expired (row transform prefetch or degridding staging)");
   }
 }
 
@@ -546,7 +547,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     g->timer.mark("fft_rows");
     launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, sel, g->d_flags, s);
     g->timer.mark("degrid");
-    launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, s);
+    launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, g->d_flags, s);
   }
   g->timer.mark("finalize");
   launch_unpermute_predict(b.records, b.perm, vacc, b.n_out, (float2 *)d_vis, s);
@@ -680,7 +681,8 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                         +1.0f, sel, s);
       launch_fft_rows_backward_pad(*g->fft, dp, b->rows, rstride, b->planes, nb, sel, g->d_flags,
                                    s);
-      launch_degrid_items(dp, b->geom, b->offsets, p0, nb, b->ditems[i], b->planes, b->vacc, s);
+      launch_degrid_items(dp, b->geom, b->offsets, p0, nb, b->ditems[i], b->planes, b->vacc,
+                          g->d_flags, s);
     }
     WGPU_CUDA(cudaMemsetAsync(b->vis_out, 0, sizeof(float2) * n, s));
     launch_unpermute_predict(b->geom, b->perm, b->vacc, b->n_out, b->vis_out, s);

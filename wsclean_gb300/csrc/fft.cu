@@ -28,6 +28,7 @@
 #include <mutex>
 #include <vector>
 
+#include "tma.cuh"
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -345,42 +346,6 @@ struct RowStages {
   int tw_off[kMaxStages];  // offset of each stage's table in the row table
 };
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
-                                              uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
-  return ok != 0;
-}
-// Waits for the phase of `parity` for at most `cycles` SM clock cycles (the
-// row kernels give about two seconds); returns false if the wait expired.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
-                                                  long long cycles = 4ll << 30) {
-  const long long deadline = clock64() + cycles;
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() > deadline) return false;
-  return true;
-}
-
 // Self-test of the bounded wait: waits on an mbarrier that nothing arrives
 // at, so the wait must expire; records the expiry and returns.
 __global__ void bounded_wait_selftest_kernel(long long cycles, unsigned *err) {
@@ -389,9 +354,6 @@ __global__ void bounded_wait_selftest_kernel(long long cycles, unsigned *err) {
   __syncthreads();
   const bool ok = mbar_wait_bounded(&bar, 0, cycles);
   if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicAdd(err, 1u);
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Loads element a of the stage input.

@@ -23,6 +23,7 @@
 // per-visibility accumulator.
 #include <algorithm>
 
+#include "tma.cuh"
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -798,6 +799,14 @@ __global__ void __launch_bounds__(kThreads)
 // each (lane i sums footprint column i over the rows and planes, a three-step
 // shuffle reduction forms the record's sum).  W > 8: one warp per record,
 // lanes own footprint cells and a warp-wide reduction forms the sum.
+//
+// Both stagings are bulk copies (cp.async.bulk, the TMA engine) completing on
+// one mbarrier: each halo row is RS cells copied from its plane row (two
+// copies where the row wraps around the grid's u edge; every row start is a
+// multiple of 16 cells, so every copy is 16-byte aligned), and a round of
+// records is at most four contiguous chunks, one per class range.  The waits
+// are bounded; a copy that does not complete in time is recorded in *err and
+// the block leaves after waiting (bounded) for its copies in flight.
 __host__ __device__ constexpr int degrid_row_stride(int R) { return (R + 7) / 16 * 16 + 8; }
 template <int T, int G, int W>
 constexpr size_t degrid_smem_bytes() {
@@ -812,20 +821,41 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
                   const uint32_t *__restrict__ off, int p_begin, int n_batch,
                   const uint32_t *__restrict__ item_off, const uint32_t *__restrict__ desc,
                   uint32_t total, const float2 *__restrict__ planes,
-                  float2 *__restrict__ acc) {
+                  float2 *__restrict__ acc, unsigned *__restrict__ err) {
   constexpr int R = T + W - 1;
   constexpr int RS = degrid_row_stride(R);
   constexpr int kPlane = R * RS;
   constexpr int kFoot = W * W;
   constexpr int kLaneCells = (kFoot + 31) / 32;
-  extern __shared__ float2 halo[];  // [G][R][RS]
+  static_assert((RS * sizeof(float2)) % 16 == 0, "halo rows are whole 16-byte units");
+  extern __shared__ __align__(16) float2 halo[];  // [G][R][RS]
   __shared__ uint32_t rs0[4], rcum[5];
-  __shared__ float4 stage[kThreads][2];
+  __shared__ __align__(16) float4 stage[kThreads][2];
   __shared__ uint32_t stage_s[kThreads];
+  __shared__ __align__(8) uint64_t bar;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_half = 2.0f / (float)W;
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  // waits for the current phase of the staging barrier; false: the copies did
+  // not complete in time (recorded once per block, after which the block
+  // waits once more for them and stops)
+  auto staged = [&]() -> bool {
+    const bool ok = mbar_wait_bounded(&bar, phase);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicAdd(err, 1u);
+      mbar_wait_bounded(&bar, phase);
+      return false;
+    }
+    phase ^= 1u;
+    return true;
+  };
 
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     const int unit = (int)(__ldg(desc + item) & 0x7fffffffu);
@@ -836,19 +866,25 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
     const uint32_t lo = (item - __ldg(item_off + unit)) * kItemVis;
 
     const int nq = q1 - q0;
-    // halo load: asynchronous 8-byte copies straight into shared memory
-    // (cp.async), each thread waiting for its own before the barrier below
-    const int n_halo = nq * R * R;
-    for (int idx = threadIdx.x; idx < n_halo; idx += kThreads) {
-      const int pq = idx / (R * R), rem = idx - pq * R * R;
-      const int r = rem / R, c = rem - r * R;
-      int gv = tv * T + r;
-      if (gv >= p.nv) gv -= p.nv;
-      int gu = tu * T + c;
-      if (gu >= p.nu) gu -= p.nu;
-      const float2 *src = planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu + gu;
-      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(halo + pq * kPlane + r * RS + c);
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+    // halo: warp 0 copies the nq x R rows of RS cells; the first cell of a
+    // row is at u = tu * T, and the copy wraps to u = 0 at the grid's edge
+    if (warp == 0) {
+      const int gu = tu * T;
+      const int seg1 = min(RS, p.nu - gu), seg2 = RS - seg1;
+      if (lane == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(&bar, (uint32_t)(nq * R * RS * sizeof(float2)));
+      }
+      __syncwarp();
+      for (int k = lane; k < nq * R; k += 32) {
+        const int pq = k / R, r = k - pq * R;
+        int gv = tv * T + r;
+        if (gv >= p.nv) gv -= p.nv;
+        const float2 *row = planes + (size_t)(q0 + pq - p_begin) * plane_elems + (size_t)gv * p.nu;
+        float2 *dst = halo + pq * kPlane + r * RS;
+        bulk_copy_g2s(dst, row + gu, (uint32_t)(seg1 * sizeof(float2)), &bar);
+        if (seg2 > 0) bulk_copy_g2s(dst + seg1, row, (uint32_t)(seg2 * sizeof(float2)), &bar);
+      }
     }
     if (threadIdx.x < 4) {
       uint32_t a, b;
@@ -856,8 +892,7 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
       rs0[threadIdx.x] = a;
       rcum[threadIdx.x + 1] = b - a;
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();
+    if (!staged()) return;
     if (threadIdx.x == 0) {
       rcum[0] = 0;
       for (int r = 0; r < 4; ++r) rcum[r + 1] += rcum[r];
@@ -866,24 +901,27 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
     const uint32_t hi = min(lo + kItemVis, rcum[4]);
 
     for (uint32_t rb = lo; rb < hi; rb += kThreads) {
+      const uint32_t re = min(rb + (uint32_t)kThreads, hi);
+      // the round's records: one bulk copy per class range it overlaps
+      if (threadIdx.x == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(&bar, (re - rb) * (uint32_t)sizeof(VisRecord));
+        for (int r = 0; r < 4; ++r) {
+          const uint32_t a = max(rb, rcum[r]), b = min(re, rcum[r + 1]);
+          if (a < b)
+            bulk_copy_g2s(&stage[a - rb][0], rec + rs0[r] + (a - rcum[r]),
+                          (b - a) * (uint32_t)sizeof(VisRecord), &bar);
+        }
+      }
       {
         const uint32_t pos = rb + threadIdx.x;
-        if (pos < hi) {
+        if (pos < re) {
           int r = 0;
           while (pos >= rcum[r + 1]) ++r;
-          const uint32_t s = rs0[r] + (pos - rcum[r]);
-          // the 32-byte record into the stage with two 16-byte cp.async copies
-          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&stage[threadIdx.x][0]);
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(rec + s)
-                       : "memory");
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u),
-                       "l"(reinterpret_cast<const float4 *>(rec + s) + 1)
-                       : "memory");
-          stage_s[threadIdx.x] = s;
+          stage_s[threadIdx.x] = rs0[r] + (pos - rcum[r]);
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
       }
-      __syncthreads();
+      if (!staged()) return;
       const int n_round = (int)min((uint32_t)kThreads, hi - rb);
       if constexpr (W <= 8) {
         // groups of eight lanes, one record each: lane i of a group owns
@@ -1119,8 +1157,11 @@ void grid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int
 template <int T, int G, int W>
 void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, int p_begin,
                   int n_batch, const WorkItems &wi, const float2 *planes, float2 *acc,
-                  cudaStream_t s) {
+                  unsigned *err, cudaStream_t s) {
   if (wi.total == 0) return;
+  // a halo row (RS cells, wrapping once at the u edge) must fit in a grid row
+  if (p.nu < degrid_row_stride(T + W - 1) || p.nv < T + W - 1)
+    throw Error(WGPU_ERR_INVALID, "grid smaller than the degridding halo");
   const size_t smem = degrid_smem_bytes<T, G, W>();
   ensure_dynamic_smem((const void *)degrid_kernel<T, G, W>, smem);
   int per_sm = 0;
@@ -1129,7 +1170,7 @@ void degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off, i
   const uint32_t blocks = std::min<uint32_t>(wi.total, (uint32_t)(sm_count() * std::max(per_sm, 1)));
   degrid_kernel<T, G, W><<<blocks, kThreads, smem, s>>>(p, rec, off, p_begin, n_batch,
                                                         wi.item_off, wi.desc, wi.total, planes,
-                                                        acc);
+                                                        acc, err);
   check_launch("degrid_kernel");
 }
 
@@ -1178,14 +1219,15 @@ void grid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const ui
 template <int T, int G, int W = 4>
 void degrid_dispatch(int support, const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                      int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
-                     float2 *acc, cudaStream_t s) {
+                     float2 *acc, unsigned *err, cudaStream_t s) {
   if constexpr (W > kMaxSupport || (G > 8 && W > 8)) {
     throw Error(WGPU_ERR_INVALID, "kernel support out of range");
   } else {
     if (support == W)
-      degrid_items<T, G, W>(p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+      degrid_items<T, G, W>(p, rec, off, p_begin, n_batch, wi, planes, acc, err, s);
     else
-      degrid_dispatch<T, G, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+      degrid_dispatch<T, G, W + 1>(support, p, rec, off, p_begin, n_batch, wi, planes, acc, err,
+                                   s);
   }
 }
 
@@ -1276,10 +1318,10 @@ void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t 
 
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                          int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
-                         float2 *acc, cudaStream_t s) {
+                         float2 *acc, unsigned *err, cudaStream_t s) {
   check_plan(p);
   degrid_dispatch<kTile, kDegridPlanes>(p.support, p, rec, off, p_begin, n_batch, wi, planes, acc,
-                                        s);
+                                        err, s);
 }
 
 static ItemAlloc arena_alloc(DeviceArena &arena) {
@@ -1302,9 +1344,9 @@ void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
 
 void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                    const uint32_t *off, int p_begin, int n_batch, const float2 *planes,
-                   float2 *acc, cudaStream_t s) {
+                   float2 *acc, unsigned *err, cudaStream_t s) {
   const WorkItems wi = plan_degrid_items(p, off, p_begin, n_batch, arena_alloc(arena), s);
-  launch_degrid_items(p, rec, off, p_begin, n_batch, wi, planes, acc, s);
+  launch_degrid_items(p, rec, off, p_begin, n_batch, wi, planes, acc, err, s);
 }
 
 }  // namespace wgpu

@@ -217,15 +217,17 @@ void launch_spill_fixup(const DevPlan &p, const WorkItems &wi, int p_begin, int 
 void prepare_grid_items_multi(int support);
 void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
                              int n_jobs, uint32_t total, cudaStream_t s);
+// err: device word counting staging waits that expired (reported by the
+// caller as WGPU_ERR_TIMEOUT).
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                          int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
-                         float2 *acc, cudaStream_t s);
+                         float2 *acc, unsigned *err, cudaStream_t s);
 void launch_grid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                  const uint32_t *off, int p_begin, int n_batch, float2 *planes,
                  cudaStream_t s);
 void launch_degrid(DeviceArena &arena, const DevPlan &p, const VisRecord *rec,
                    const uint32_t *off, int p_begin, int n_batch,
-                   const float2 *planes, float2 *acc, cudaStream_t s);
+                   const float2 *planes, float2 *acc, unsigned *err, cudaStream_t s);
 int grid_plane_group();
 
 // ---- FFT (fft.cu) ----
