@@ -354,7 +354,7 @@ def run_gpu(args, rank, world, local):
     import torch
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    from wsclean_gb300 import _lib
+    from wsclean_gb300 import _lib, replicas
     from wsclean_gb300.gridder import WGriddingGridder_Simple
     _lib.lib()
 
@@ -417,10 +417,9 @@ def run_gpu(args, rank, world, local):
         ms = start.elapsed_time(end)
         launches = _lib.lib().wgpu_kernel_launch_count() - launches0
         if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            # replicas: the slowest rank's time (no collective on the data path)
+            ms = replicas.max_over_ranks(ms, device=dev)
             torch.distributed.barrier()
-            ms = float(t.item())
         return ms, wall, launches
 
     clocks = ClockSampler(local)
@@ -428,7 +427,7 @@ def run_gpu(args, rank, world, local):
     ms, wall, launches = timed(step_device, args.steps, args.warmup)
     clk = clocks.stop()
     ms_per_step = ms / args.steps
-    value = world * n_vis / (ms_per_step * 1e-3) / 1e9
+    value = replicas.aggregate_rate([n_vis] * world, ms_per_step * 1e-3) / 1e9
 
     # plans of the last step
     g.InitializeInversion()

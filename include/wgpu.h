@@ -342,7 +342,7 @@ int wgpu_bucket_debug_rows(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan
  * the device-wide synchronisation that cudaMalloc / cudaFree can cause.  The
  * caller passes device inputs and device outputs; the scratch (sort keys,
  * histograms, scan sums) lives in a static device array of
- * wgpu_bucket_noalloc_scratch_bytes() bytes (about 17 MB) that every GPU
+ * wgpu_bucket_noalloc_scratch_bytes() bytes (about 18 MB) that every GPU
  * loading the library holds until the process exits.  No cudaMalloc, cudaFree
  * or allocating library routine is called.
  *
@@ -359,7 +359,10 @@ int wgpu_bucket_debug_rows(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan
  * n_rows * n_chan entries; *n_out receives the number written.
  *
  * The first call on a device looks up the array's device address (with that
- * device current); make that first call before any stream capture.  All calls
+ * device current) and keeps it for the life of the process; make that first
+ * call before any stream capture.  The kept address belongs to the device's
+ * primary context: after cudaDeviceReset, or from a non-primary context on the
+ * same device, the entry point must not be called again.  All calls
  * share the array and it keeps the last call's contents: calls whose work
  * overlaps on the GPU (different streams or host threads) race and must be
  * serialised by the caller.  stream may be NULL (the legacy default stream). */

@@ -85,3 +85,26 @@ def test_noalloc_rejects_oversize_requests(wgpu_lib):
                                         d.data_ptr(), d.data_ptr(), None, C.byref(n_out))
     assert st == _lib.WGPU_ERR_INVALID
     assert b"at most" in _lib.lib().wgpu_last_error()
+    # sizes whose product wraps around 64 bits are refused before it is formed
+    for rows, chans in (((1 << 62) + 1, 4), (1 << 33, 1 << 31), (3, _lib.NOALLOC_MAX_CHANNELS + 1)):
+        st = _lib.lib().wgpu_bucket_noalloc(C.byref(plan), rows, chans, d.data_ptr(),
+                                            d.data_ptr(), d.data_ptr(), 0, d.data_ptr(),
+                                            d.data_ptr(), d.data_ptr(), None, C.byref(n_out))
+        assert st == _lib.WGPU_ERR_INVALID
+        assert b"at most" in _lib.lib().wgpu_last_error()
+
+
+def test_noalloc_bucketing_at_the_sample_limit(wgpu_lib):
+    """Exactly WGPU_NOALLOC_MAX_VISIBILITIES samples, twice in a row: the
+    largest request the static scratch takes."""
+    n_chan = 16
+    n_rows = _lib.NOALLOC_MAX_VISIBILITIES // n_chan
+    uvw, freq, vis = synthetic.random_points(n_rows, n_chan, 512, 1e-4, 33, w_scale=1.5,
+                                             frac_zero=0.1)
+    assert uvw.shape[0] * freq.size == _lib.NOALLOC_MAX_VISIBILITIES
+    plan = _plan(uvw, freq, vis, 512, 1e-4)
+    ref = bucket_debug(plan, uvw.shape[0], freq.size, uvw, freq, vis, True)
+    for _ in range(2):
+        got = _noalloc(plan, uvw, freq, vis, True)
+        for k in ("perm", "iu", "iv", "ip", "fu", "fv", "fw", "offsets"):
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=k)

@@ -1537,6 +1537,15 @@ int wgpu_bucket_noalloc(const wgpu_plan_t *plan, size_t n_rows, size_t n_chan,
   if (!d_offsets) return fail(WGPU_ERR_INVALID, "null offsets pointer");
   if (skip_zero && !d_vis && n_rows && n_chan)
     return fail(WGPU_ERR_INVALID, "inversion bucketing needs the visibilities");
+  // the limits before any product of the sizes (which could wrap)
+  if (n_chan > (size_t)WGPU_NOALLOC_MAX_CHANNELS)
+    return fail(WGPU_ERR_INVALID, "allocation-free bucketing takes at most " +
+                                      std::to_string(WGPU_NOALLOC_MAX_CHANNELS) + " channels");
+  if (n_rows > (size_t)WGPU_NOALLOC_MAX_VISIBILITIES ||
+      (n_chan != 0 && n_rows > (size_t)WGPU_NOALLOC_MAX_VISIBILITIES / n_chan))
+    return fail(WGPU_ERR_INVALID, "allocation-free bucketing takes at most " +
+                                      std::to_string(WGPU_NOALLOC_MAX_VISIBILITIES) +
+                                      " visibilities");
   return guarded([&] {
     const DevPlan dp = to_dev_plan(*plan);
     *n_out = bucket_visibilities_noalloc(dp, d_uvw, d_freq, d_vis, (int64_t)n_rows,

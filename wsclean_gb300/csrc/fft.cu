@@ -1084,16 +1084,6 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
 
 void set_smem(const void *fn, size_t bytes) { ensure_dynamic_smem(fn, bytes); }
 
-int sm_count_fft() {
-  static const int n = [] {
-    int dev = 0, v = 0;
-    WGPU_CUDA(cudaGetDevice(&dev));
-    WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-    return v;
-  }();
-  return n;
-}
-
 }  // namespace
 
 // Per-stage twiddle tables of the row schedule of length L (cached).
@@ -1186,7 +1176,7 @@ static void launch_persistent(const FftDesc &d, const RowStages &st, const float
   int per_sm = 0;
   WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   if (per_sm < 1) throw Error(WGPU_ERR_INVALID, "row transform does not fit on an SM");
-  const int blocks = std::min(n_rows, sm_count_fft() * per_sm);
+  const int blocks = std::min(n_rows, sm_count() * per_sm);
   kern<<<blocks, threads, smem, s>>>(d, st, tws, in, in_stride, in_bytes, out, out_stride,
                                       n_batch, p.nv, sel, p.width, buf_elems, mid_tab, err);
   check_launch(FWD ? "fft_rows_persistent_kernel<forward>"

@@ -46,14 +46,20 @@ void check_launch(const char *what) {
 DeviceArena::~DeviceArena() { release(); }
 
 int sm_count() {
-  // initialised once, thread-safely (gridders run on several host threads)
-  static const int n = [] {
-    int dev = 0, v = 0;
-    WGPU_CUDA(cudaGetDevice(&dev));
+  // SM count of the current device, looked up once per device ordinal
+  // (gridders run on several host threads and may use different devices)
+  static std::mutex mu;
+  static int count[256] = {};
+  int dev = 0;
+  WGPU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) throw Error(WGPU_ERR_CUDA, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (count[dev] == 0) {
+    int v = 0;
     WGPU_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-    return v;
-  }();
-  return n;
+    count[dev] = v > 0 ? v : 1;
+  }
+  return count[dev];
 }
 
 void *DeviceArena::get(int slot, size_t bytes) {
