@@ -679,10 +679,153 @@ def run_fullpol(args):
     }
 
 
+def _facet_layout(rng, dl):
+    """37 facets of seeded uniform 512-3072 pixels (multiples of 4), centres
+    within a 6 degree field."""
+    half = math.radians(3.0)
+    facets = []
+    for _ in range(37):
+        side = int(rng.uniform(512, 3072)) // 4 * 4
+        facets.append(dict(width=side, height=side, dl=dl, dm=dl,
+                           l_shift=float(rng.uniform(-half, half)),
+                           m_shift=float(rng.uniform(-half, half))))
+    return facets
+
+
+def run_facets_full(args):
+    """The batched-facet workload at its full size (6200 time steps, 2.0e8
+    samples): the 296 jobs' sorted records (about 240 GB) cannot all stay on
+    the device, so every step binds and inverts one output-channel group at a
+    time: 37 facets sharing that group's two channels, bucketed, gridded in one
+    multi-job launch per wave and transformed from one CUDA graph, then
+    released.  Compared with the same 296 jobs through the plain per-call
+    path; job 0 is checked against the plain path on its plan and against the
+    FP64 direct transform on the GPU (all of its samples, 4096 pixels)."""
+    import torch
+    import oracle
+    from wsclean_gb300 import synthetic
+    from wsclean_gb300.facets import FacetBatch
+    from wsclean_gb300.gridder import WGriddingGridder_Simple
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(4)
+    t0 = time.time()
+    d = synthetic.make_workload("plain1024", seed=4, with_model=False, n_t=args.facet_times)
+    vis = synthetic.model_vis_torch(d["uvw"], d["freq"], d["sources"], dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    vis = vis + 0.01 * math.sqrt(2.0) * torch.randn(vis.shape, generator=g, dtype=vis.dtype,
+                                                    device=dev)
+    groups = list(range(0, 17, 2))
+    n_groups = len(groups) - 1
+    # each group's two channels as their own contiguous [row][2] input
+    d_vis_g = [vis[:, c0:c0 + 2].contiguous() for c0 in groups[:-1]]
+    del vis
+    gen_s = time.time() - t0
+    dl, eps = d["dl"], 1e-4
+    facets = _facet_layout(rng, dl)
+    n_rows = d["uvw"].shape[0]
+    freq = d["freq"]
+    img_elems = sum(f["width"] * f["height"] for f in facets)
+    outs = [torch.empty(img_elems, dtype=torch.float32, device=dev) for _ in range(n_groups)]
+    info = {}
+
+    def step():
+        for gi in range(n_groups):
+            c0 = groups[gi]
+            fb = FacetBatch(facets, [0, 2], epsilon=eps)
+            fb.bind(d["uvw"], freq[c0:c0 + 2])
+            fb.invert_device(d_vis_g[gi].data_ptr(), outs[gi].data_ptr())
+            if gi == 0:
+                info.update(fb.info())
+                info["plan0"] = fb.job_plan(0)
+            fb.close()
+        torch.cuda.synchronize()
+
+    for _ in range(min(args.warmup, 1)):
+        step()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib_launches()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    ms = (time.perf_counter() - w0) * 1e3 / args.steps
+    clk = clocks.stop()
+    launches = _lib_launches() - l0
+    job_vis = float(n_rows) * 16 * len(facets)
+    # the same jobs one at a time through the plain per-call path
+    d_uvw = torch.as_tensor(d["uvw"], device=dev)
+    d_freq = torch.as_tensor(freq, device=dev)
+    gp = [WGriddingGridder_Simple(f["width"], f["height"], f["width"], f["height"], dl, dl,
+                                  f["l_shift"], f["m_shift"], 1, epsilon=eps) for f in facets]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for gi in range(n_groups):
+        c0 = groups[gi]
+        for gg in gp:
+            gg.InitializeInversion()
+            gg.AddInversionDataDevice(n_rows, 2, d_uvw.data_ptr(), d_freq[c0:c0 + 2].data_ptr(),
+                                      d_vis_g[gi].data_ptr())
+            gg.FinalizeImage(1.0)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - w0
+    for gg in gp:
+        gg.close()
+    # job 0 (facet 0, first group) against the plain path on its plan and the DFT
+    f = facets[0]
+    n0 = f["width"] * f["height"]
+    img = outs[0][:n0].cpu().numpy().astype(np.float64)
+    gg = WGriddingGridder_Simple(f["width"], f["height"], f["width"], f["height"], dl, dl,
+                                 f["l_shift"], f["m_shift"], 1, epsilon=eps)
+    gg.pin_plan(info["plan0"])
+    gg.InitializeInversion()
+    gg.AddInversionDataDevice(n_rows, 2, d_uvw.data_ptr(), d_freq[0:2].data_ptr(),
+                              d_vis_g[0].data_ptr())
+    gg.FinalizeImage(1.0)
+    ref = gg.RealImage().astype(np.float64)
+    gg.close()
+    pix = rng.choice(n0, 4096, replace=False)
+    dft = oracle.cuda_dft_invert(d_uvw, freq[0:2], d_vis_g[0], f["width"], f["height"], dl, dl,
+                                 f["l_shift"], f["m_shift"], pixels=pix)
+    checks = {"job0_vs_plain_rel_l2": rel_l2(img, ref),
+              "job0_vs_fp64_dft_rel_l2": rel_l2(img[pix], dft),
+              "dft_sample": f"all {n_rows * 2} samples of job 0 at 4096 pixels, FP64 direct "
+                            "transform on the GPU"}
+    value = job_vis / (ms * 1e-3) / 1e9
+    plain_value = job_vis / plain_s / 1e9
+    sides = [f["width"] for f in facets]
+    return {
+        "metric": "Gvis/s batched facet inversion (job-samples: facets x channel groups)",
+        "value": value, "unit": "Gvis/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT["facets"].replace(" (scaled from 6200)", "")
+                   .replace("620", str(args.facet_times)),
+                   "n_rows": n_rows, "n_chan": 16, "samples": n_rows * 16,
+                   "facet_sides": [min(sides), max(sides)], "jobs": len(facets) * n_groups,
+                   "per_group": {k: int(info[k]) for k in ("n_jobs", "n_waves", "support",
+                                                           "graph_kernels")},
+                   "job_samples": job_vis,
+                   "plain_one_at_a_time_gvis_s": plain_value,
+                   "batched_over_plain": value / plain_value, "checks": checks,
+                   "datagen_s": round(gen_s, 1),
+                   "l2": "working set larger than L2 (planes of every wave, 1.6 GB of samples)",
+                   "step": "per output-channel group: bind (upload, plan, bucket 37 jobs, "
+                           "capture) + one graph replay + release; host wall time with the "
+                           "device synchronised on both sides"},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+
+
 def run_facets(args):
     """Batched facet inversion (all facet x channel jobs, one multi-job gridding
     launch per wave, one CUDA graph) against the same jobs run one at a time
     through the plain per-call path."""
+    if args.facet_times > args.facet_resident_times:
+        return run_facets_full(args)
     import torch
     import oracle
     from wsclean_gb300 import synthetic
@@ -1157,7 +1300,16 @@ def run_serving(args, device_bytes):
     gen_s = time.time() - t0
     keep = tuple(r["id"] for r in reqs[:6])
     planes = device_bytes / (2.0 * args.serve_slots)
-    plain, kept_plain = serving.one_at_a_time(pool, reqs, device_bytes, planes, keep)
+    # the one-at-a-time path over the whole stream, or over a seeded sample of
+    # it (the rates compare: both are samples of the same request distribution)
+    n_plain = args.serve_plain_requests or len(reqs)
+    if n_plain < len(reqs):
+        pick = np.sort(np.random.default_rng(23).choice(len(reqs), n_plain, replace=False))
+        plain_reqs = [reqs[i] for i in pick]
+        keep = tuple(r["id"] for r in plain_reqs[:6])
+    else:
+        plain_reqs = reqs
+    plain, kept_plain = serving.one_at_a_time(pool, plain_reqs, device_bytes, planes, keep)
     sat, kept_sat = serving.saturated(pool, reqs, device_bytes, planes, args.serve_slots, keep)
     rate = 0.8 * len(reqs) / sat["wall_s"]
     poi = serving.poisson(pool, reqs, device_bytes, planes, args.serve_slots, rate)
@@ -1179,6 +1331,7 @@ def run_serving(args, device_bytes):
                      f"from the 64-antenna 3 km array, eps 1e-4/1e-5, {args.serve_cycles} major "
                      f"cycles per request with state resident"),
         "slots": args.serve_slots, "device_budget_gb": device_bytes / 1e9,
+        "one_at_a_time_requests": len(plain_reqs),
         "visibilities": serving.total_vis(reqs),
         "one_at_a_time": plain, "saturated": sat, "poisson": poi,
         "served_over_plain": sat["gvis_s"] / plain["gvis_s"],
@@ -1276,14 +1429,19 @@ def main():
                     help="fraction of one plane pass per direction per reference step")
     ap.add_argument("--facet-corrections", action="store_true",
                     help="also time the facet batch with per-facet full-Jones corrections")
-    ap.add_argument("--facet-times", type=int, default=620,
+    ap.add_argument("--facet-times", type=int, default=6200,
                     help="time steps of the facet workload (6200 in the full workload)")
+    ap.add_argument("--facet-resident-times", type=int, default=1000,
+                    help="above this many time steps the facet workload binds one "
+                         "output-channel group at a time (the jobs' records do not fit)")
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests in the serving stream (0 skips it)")
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-cycles", type=int, default=5)
     ap.add_argument("--serve-max-vis", type=float, default=1e7)
     ap.add_argument("--serve-max-side", type=int, default=4096)
+    ap.add_argument("--serve-plain-requests", type=int, default=0,
+                    help="requests of the stream timed one at a time (0: all of them)")
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving stream and print its JSON")
     ap.add_argument("--traffic", type=float, default=None,

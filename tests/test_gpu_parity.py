@@ -490,3 +490,27 @@ def test_bounded_wait_expires_and_device_stays_usable(wgpu_lib):
     g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
     assert np.isfinite(g.RealImage()).all()
     g.close()
+
+
+def test_row_length_6912_inversion_and_prediction(wgpu_lib, oracle_lib):
+    """A 5088-pixel image plans 6912-cell rows, the longest row the one-CTA-per-
+    row transform takes: its thread count is clamped to the kernel's launch
+    bound (6912 / 16 = 432 threads, not a whole number of warps)."""
+    W, dl, eps = 5088, 4.848e-5, 1e-4
+    uvw, freq, vis = synthetic.random_points(400, 4, W, dl, seed=61, w_scale=0.02)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=eps)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    assert g.last_plan().nu == 6912
+    img = g.RealImage().astype(np.float64)
+    rng = np.random.default_rng(62)
+    pix = rng.choice(W * W, 256, replace=False)
+    ref = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, pixels=pix)
+    assert rel(img[pix], ref) <= eps
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, 5, replace=False)] = 1.0
+    g.InitializePrediction(model)
+    pv = g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq)
+    pr = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl)
+    assert rel(pv.ravel(), pr) <= eps
+    g.close()

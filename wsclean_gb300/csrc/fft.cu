@@ -587,9 +587,13 @@ __device__ __forceinline__ void row_stage_pp(const float2 *__restrict__ src, flo
   __syncthreads();
 }
 
-// Ping-pong row kernel, one CTA per row (rows up to kRowPingPongMax).
+// Ping-pong row kernel, one CTA per row (rows up to kRowPingPongMax), launched
+// with L / 16 threads rounded up to whole warps, at most kRowPingPongThreads
+// (every loop of the kernel strides by blockDim.x, and no warp-wide
+// intrinsic is used, so the last warp may be partial).
+constexpr int kRowPingPongThreads = kRowPingPongMax / 16;
 template <bool FWD>
-__global__ void __launch_bounds__(kRowPingPongMax / 16, 2)
+__global__ void __launch_bounds__(kRowPingPongThreads, 2)
     fft_rows_pingpong_kernel(FftDesc d, RowStages st, const float2 *__restrict__ tws,
                              const float2 *__restrict__ in, int in_stride,
                              float2 *__restrict__ out, int out_stride, int n_batch, int nv,
@@ -1211,7 +1215,7 @@ static void launch_rows(FftTables &t, const DevPlan &p, const float2 *in, int in
                                        err, s);
     return;
   }
-  const int threads = std::max(64, (p.nu / 16 + 31) / 32 * 32);
+  const int threads = std::min(kRowPingPongThreads, std::max(64, (p.nu / 16 + 31) / 32 * 32));
   const size_t smem = 2 * sizeof(float2) * (size_t)row_buffer(p.nu);
   set_smem((const void *)fft_rows_pingpong_kernel<FWD>, smem);
   fft_rows_pingpong_kernel<FWD><<<(unsigned)n_rows, threads, smem, s>>>(
