@@ -309,6 +309,8 @@ def run_bound(d, g, d_out, inv_weight, stream, cycles=4, warmup=1):
     g.Bind(n_rows, n_chan, d["uvw"], d["freq"], mask)
     torch.cuda.synchronize()
     bind_s = time.perf_counter() - t0
+    trials = g.last_tuning()
+    bp = g.last_plan()
     stages = {}
 
     def cycle(keep_image=False):
@@ -339,14 +341,20 @@ def run_bound(d, g, d_out, inv_weight, stream, cycles=4, warmup=1):
     pred_rel = float(torch.linalg.vector_norm(d_out - pred_plain).item() /
                      torch.linalg.vector_norm(pred_plain).item())
     g.Unbind()
-    return {"ms_per_cycle": ms, "gvis_s": n_vis / (ms * 1e-3) / 1e9, "cycles": cycles,
-            "bind_s": round(bind_s, 2),
-            "stages": {f"{k}:{n}": round(v[0], 3) for k, st in stages.items()
-                       for n, v in st.items()},
-            "bound_vs_plain_rel_l2": {"image": img_rel, "prediction": pred_rel},
-            "cycle": "InitializeInversion + invert_bound (graph replay) + FinalizeImage + "
-                     "InitializePrediction + predict_bound (graph replay), device buffers; "
-                     "bucketing paid once at bind"}
+    out = {"ms_per_cycle": ms, "gvis_s": n_vis / (ms * 1e-3) / 1e9, "cycles": cycles,
+           "bind_s": round(bind_s, 2),
+           "plan": {"support": bp.support, "sigma": bp.sigma, "nu": bp.nu,
+                    "n_planes": bp.n_planes, "plane_batch": bp.plane_batch},
+           "stages": {f"{k}:{n}": round(v[0], 3) for k, st in stages.items()
+                      for n, v in st.items()},
+           "bound_vs_plain_rel_l2": {"image": img_rel, "prediction": pred_rel},
+           "cycle": "InitializeInversion + invert_bound (graph replay) + FinalizeImage + "
+                    "InitializePrediction + predict_bound (graph replay), device buffers; "
+                    "bucketing paid once at bind"}
+    if trials:
+        out["tuning"] = [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in t.items()}
+                         for t in trials]
+    return out
 
 
 # -------------------------------------------------------------- GPU arm -----
@@ -549,11 +557,23 @@ def run_gpu(args, rank, world, local):
     req_bytes = (survey_request_bytes(plan_inv, d["n_gridded"], n_rows) +
                  survey_request_bytes(plan_pred, d["n_gridded"], n_rows))
     result["config"]["request_bytes_roofline_frac"] = (req_bytes / (ms_per_step * 1e-3) / 1e9) / peak
+    # `value` counts every sample handed to the step, as the reference's calls
+    # receive them; the samples beyond the image's Nyquist limit are zero and
+    # neither gridded nor predicted, so the rate of processed samples is lower
+    result["config"]["gridded_gvis_s"] = (world * d["n_gridded"] / (ms_per_step * 1e-3) / 1e9)
 
     if rank == 0 and not args.no_accuracy:
         result["config"]["accuracy"] = accuracy_full(d, g, d_out)
     if not args.no_bound:
         result["bound"] = run_bound(d, g, d_out, inv_weight, stream)
+    if args.tune_bound:
+        # the same major cycles on a gridder created with tuning = 1: the bind
+        # times the best candidate plans on these rows and keeps the fastest
+        gt = WGriddingGridder_Simple(W, W, W, W, d["dl"], d["dl"], 0.0, 0.0, os.cpu_count(),
+                                     epsilon=eps, num_t=num_t, tuning=True)
+        st = torch.cuda.ExternalStream(gt.stream(), device=dev)
+        result["bound_tuned"] = run_bound(d, gt, d_out, inv_weight, st)
+        gt.close()
     if args.serve_requests > 0:
         g.close()  # release the wide-field gridder's planes before serving
         del d_out
@@ -730,16 +750,18 @@ def run_facets_full(args):
     outs = [torch.empty(img_elems, dtype=torch.float32, device=dev) for _ in range(n_groups)]
     info = {}
 
+    # one batch object re-bound per channel group: its device memory and
+    # bucketing scratch stay allocated from one bind to the next
+    fb = FacetBatch(facets, [0, 2], epsilon=eps)
+
     def step():
         for gi in range(n_groups):
             c0 = groups[gi]
-            fb = FacetBatch(facets, [0, 2], epsilon=eps)
             fb.bind(d["uvw"], freq[c0:c0 + 2])
             fb.invert_device(d_vis_g[gi].data_ptr(), outs[gi].data_ptr())
             if gi == 0:
                 info.update(fb.info())
                 info["plan0"] = fb.job_plan(0)
-            fb.close()
         torch.cuda.synchronize()
 
     for _ in range(min(args.warmup, 1)):
@@ -754,6 +776,7 @@ def run_facets_full(args):
     ms = (time.perf_counter() - w0) * 1e3 / args.steps
     clk = clocks.stop()
     launches = _lib_launches() - l0
+    fb.close()
     job_vis = float(n_rows) * 16 * len(facets)
     # the same jobs one at a time through the plain per-call path
     d_uvw = torch.as_tensor(d["uvw"], device=dev)
@@ -812,9 +835,10 @@ def run_facets_full(args):
                    "batched_over_plain": value / plain_value, "checks": checks,
                    "datagen_s": round(gen_s, 1),
                    "l2": "working set larger than L2 (planes of every wave, 1.6 GB of samples)",
-                   "step": "per output-channel group: bind (upload, plan, bucket 37 jobs, "
-                           "capture) + one graph replay + release; host wall time with the "
-                           "device synchronised on both sides"},
+                   "step": "per output-channel group: re-bind of one batch object (upload, "
+                           "plan, bucket 37 jobs, capture; device memory kept from the previous "
+                           "bind) + one graph replay; host wall time with the device "
+                           "synchronised on both sides"},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -1314,7 +1338,8 @@ def run_serving(args, device_bytes):
     rate = 0.8 * len(reqs) / sat["wall_s"]
     poi = serving.poisson(pool, reqs, device_bytes, planes, args.serve_slots, rate)
     # served (mixed) against one-at-a-time (alone) results of the same requests:
-    # the runs differ only in the order of the float atomic additions
+    # the runs can differ in the plane batch (the memory budget differs) and in
+    # the order of the float atomic additions of split uv tiles
     same, same_eps = 0.0, 0.0
     eps_of = {r["id"]: r["eps"] for r in reqs}
     for i in keep:
@@ -1415,6 +1440,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bound", action="store_true",
                     help="skip the major cycles on a bound visibility set")
+    ap.add_argument("--tune-bound", action="store_true",
+                    help="also run the bound major cycles on a tuning gridder")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the full-data error against the FP64 direct transform")
     ap.add_argument("--cpu-sample-rows", type=int, default=200000,

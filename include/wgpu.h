@@ -125,6 +125,25 @@ typedef struct wgpu_plan_request {
 
 int wgpu_plan_make(const wgpu_plan_request_t *request, wgpu_plan_t *plan);
 
+/* The plans that meet the request's epsilon, lowest cost-model time first
+ * (the first is wgpu_plan_make's choice): the candidates a tuning gridder
+ * times.  Writes at most max_plans entries and their number to *n_plans. */
+int wgpu_plan_candidates(const wgpu_plan_request_t *request, wgpu_plan_t *plans,
+                         int max_plans, int *n_plans);
+
+/* One candidate timed by a tuning gridder (tuning = 1 at creation; the
+ * reference's flag selects ducc0's ms2dirty_tuning / dirty2ms_tuning,
+ * gridder_simple.h:216-225, gridder_simple_implementation.h:185-194). */
+typedef struct wgpu_tuning_trial {
+  int64_t support;     /* kernel support W */
+  double sigma;        /* oversampling */
+  int64_t nu, nv;      /* grid */
+  int64_t n_planes;    /* w planes */
+  double est_seconds;  /* cost-model estimate */
+  double measured_ms;  /* device time on the call's samples */
+  int chosen;          /* 1 for the plan that was used */
+} wgpu_tuning_trial_t;
+
 /* ------------------------------------------------------------------------ */
 /* Gridder instance: WGriddingGridder_Simple<NumT>                            */
 /* ------------------------------------------------------------------------ */
@@ -282,6 +301,18 @@ int wgpu_gridder_last_timings(const wgpu_gridder_t *gridder, double *ms,
  * across the major cycles of an imaging run keeps the grids comparable; it
  * has no counterpart in the reference, where ducc0 plans every call. */
 int wgpu_gridder_pin_plan(wgpu_gridder_t *gridder, const wgpu_plan_t *plan);
+
+/* Candidates timed by the last planning of a tuning gridder.  A gridder
+ * created with tuning = 1 times the best few plans (wgpu_plan_candidates) on
+ * the call's own samples, on this device, and uses the fastest; the choice is
+ * remembered per device and request shape for the life of the process, so a
+ * call that reuses it (or a gridder without tuning, or a pinned plan) reports
+ * *n_trials = 0.  Writes at most max_trials entries. */
+int wgpu_gridder_last_tuning(const wgpu_gridder_t *gridder, wgpu_tuning_trial_t *trials,
+                             int max_trials, int *n_trials);
+
+/* Forget every remembered tuning choice (the next tuning call times again). */
+void wgpu_tuning_cache_clear(void);
 
 /* Cap, in bytes, on the device memory of the w-plane batch that this
  * gridder's plans keep resident (0 = 40% of free device memory, at most 64 GB).

@@ -70,10 +70,11 @@ def test_adapter_matches_oracle(tmp_path, wgpu_lib, oracle_lib):
     g.FinalizeImage(1.0)
     py_rows = g.RealImage().reshape(W, W)[d:d + Wt, d:d + Wt]
     rows = np.fromfile(prefix + "rows.bin", np.float32).reshape(W, W)[d:d + Wt, d:d + Wt]
-    # the same rows on the same plan through two front ends: the gridding kernel
-    # adds footprints into its shared-memory tile with float atomics, so the two
-    # runs differ only in the order of float additions (FP32 rounding, which the
-    # grid correction magnifies at the image border)
+    # the same rows on the same plan through two front ends: a uv tile whose
+    # samples are split over several work items adds each item's cells to the
+    # plane with float atomics, so the two runs can differ in the order of those
+    # float additions (FP32 rounding, which the grid correction magnifies at the
+    # image border)
     assert np.linalg.norm(rows - py_rows) <= 1e-6 * np.linalg.norm(py_rows)
     s4 = np.fromfile(prefix + "sums.bin", np.float64)
     assert s4[3] == sums.gridded_visibility_count > 0

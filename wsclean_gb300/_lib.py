@@ -52,6 +52,16 @@ class PlanRequest(C.Structure):
                 ("memory_budget_bytes", C.c_double)]
 
 
+class TuningTrial(C.Structure):
+    """wgpu_tuning_trial_t: one candidate plan timed by a tuning gridder."""
+    _fields_ = [("support", C.c_int64), ("sigma", C.c_double), ("nu", C.c_int64),
+                ("nv", C.c_int64), ("n_planes", C.c_int64), ("est_seconds", C.c_double),
+                ("measured_ms", C.c_double), ("chosen", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Request(C.Structure):
     """wgpu_request_t: one inversion or prediction request for the server."""
     _fields_ = [("kind", C.c_int), ("session", C.c_uint64),
@@ -120,6 +130,9 @@ _PROTOS = {
     "wgpu_gain_mode_n_visibilities": (SZ, [I]),
     "wgpu_select_gain_mode": (I, [I, SZ, C.POINTER(I)]),
     "wgpu_plan_make": (I, [C.POINTER(PlanRequest), C.POINTER(Plan)]),
+    "wgpu_plan_candidates": (I, [C.POINTER(PlanRequest), C.POINTER(Plan), I, C.POINTER(I)]),
+    "wgpu_gridder_last_tuning": (I, [P, C.POINTER(TuningTrial), I, C.POINTER(I)]),
+    "wgpu_tuning_cache_clear": (None, []),
     "wgpu_gridder_create": (I, [SZ, SZ, SZ, SZ, D, D, D, D, SZ, D, SZ, I, I, C.POINTER(P)]),
     "wgpu_gridder_destroy": (None, [P]),
     "wgpu_gridder_constant_memory": (SZ, [P]),
@@ -256,3 +269,18 @@ def make_plan(**kw):
     p = Plan()
     check(lib().wgpu_plan_make(C.byref(r), C.byref(p)))
     return p
+
+
+def plan_candidates(max_plans=64, **kw):
+    """The plans meeting the request's epsilon, lowest cost-model time first."""
+    r = PlanRequest()
+    for k, v in kw.items():
+        setattr(r, k, v)
+    out = (Plan * max_plans)()
+    n = C.c_int()
+    check(lib().wgpu_plan_candidates(C.byref(r), out, max_plans, C.byref(n)))
+    return [out[i] for i in range(n.value)]
+
+
+def tuning_cache_clear():
+    lib().wgpu_tuning_cache_clear()

@@ -4,8 +4,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <limits>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -194,6 +197,7 @@ struct wgpu_gridder {
   std::string corr_key;  // geometry of the correction tables in the arena
   std::string nuw_key;   // geometry (and buffer) of the n - 1 table in the arena
   std::unique_ptr<BoundState> bound;
+  std::vector<wgpu_tuning_trial_t> last_trials;  // candidates timed by the last tuning
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
   unsigned *d_flags = nullptr;  // device: expired bounded waits
   unsigned *h_flags = nullptr;  // pinned host copy, read after each call
@@ -397,11 +401,8 @@ void check_pinned_plan(const wgpu_gridder *g, double w_min, double w_max) {
   }
 }
 
-wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis) {
-  if (g->pinned) {
-    check_pinned_plan(g, w_min, w_max);
-    return g->pinned_plan;
-  }
+wgpu_plan_request_t plan_request(const wgpu_gridder *g, double w_min, double w_max,
+                                 int64_t n_vis) {
   wgpu_plan_request_t r;
   std::memset(&r, 0, sizeof(r));
   r.width = (int64_t)g->width_t;
@@ -424,7 +425,203 @@ wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis)
     const double gb = std::atof(env);
     if (gb > 0) r.memory_budget_bytes = gb * 1e9;
   }
-  return make_plan(r);
+  return r;
+}
+
+wgpu_plan_t plan_for(wgpu_gridder *g, double w_min, double w_max, int64_t n_vis) {
+  if (g->pinned) {
+    check_pinned_plan(g, w_min, w_max);
+    return g->pinned_plan;
+  }
+  return make_plan(plan_request(g, w_min, w_max, n_vis));
+}
+
+// ---- autotuning: candidate plans timed on the caller's own samples ----------
+// The reference's `tuning` flag selects ducc0's tuned entry points
+// (wgridder/gridder_simple.h:216-225, gridder_simple_implementation.h:185-194),
+// whose internals are not part of the reference tree.  Here the flag makes the
+// plan a measured choice: the cost model ranks the (support, sigma) entries
+// that meet epsilon, and the best kTuneCandidates of them are run on the
+// call's own samples on this device (bucketing, then every plane batch's
+// gridding and forward FFT passes, or backward FFT passes and degridding),
+// timed with events on the gridder's stream.  The fastest is used.  The choice
+// is remembered per device and request shape: image geometry, epsilon,
+// direction, the sample count to within a factor of sqrt(2) and the w range to
+// within 2^(1/4).  Later calls of that shape, including those of new gridders
+// (WSClean creates one per major cycle), plan without timing.  The uv tile is
+// not a tuning dimension: the gridding kernels give one thread to each of its
+// 16 x 16 cells.
+constexpr size_t kTuneCandidates = 3;
+
+struct TuneChoice {
+  int64_t support;
+  double sigma;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneChoice> g_tune_cache;
+
+std::string tune_key(const wgpu_gridder *g, char direction, double w_min, double w_max,
+                     int64_t n_vis) {
+  const double wr = w_max - w_min;
+  char buf[384];
+  std::snprintf(buf, sizeof(buf), "%d|%c|%zu|%zu|%.17g|%.17g|%.17g|%.17g|%.17g|%.17g|%d|%d",
+                g->device, direction, g->width_t, g->height_t, g->dl, g->dm, g->l_shift,
+                g->m_shift, g->epsilon, g->plane_budget,
+                (int)std::floor(2.0 * std::log2((double)std::max<int64_t>(n_vis, 1))),
+                wr > 0 ? (int)std::floor(4.0 * std::log2(wr)) : -100000);
+  return buf;
+}
+
+// Device time of one plan on the given samples: the bucketing, then every
+// plane batch of the inversion (gridding, forward FFT passes into a scratch
+// accumulator) and/or of the prediction (backward FFT passes of a zero image,
+// degridding into scratch sums).  Nothing the gridder keeps is written.  A
+// short run is repeated (up to three times) and the least time kept, so that
+// first-launch costs do not decide between small plans.
+double time_plan(wgpu_gridder *g, const wgpu_plan_t &plan, const double *d_uvw,
+                 const double *d_freq, const float *d_vis, const uint8_t *d_mask,
+                 size_t n_rows, size_t n_chan, bool skip_zero, bool inversion,
+                 bool prediction) {
+  cudaStream_t s = g->stream;
+  const DevPlan dp = to_dev_plan(plan);
+  const int64_t npix = plan.width * plan.height;
+  const int rstride = (int)((plan.width + 31) / 32 * 32);
+  const int64_t B = plan.plane_batch;
+  // tables outside the timed region (their creation copies synchronously)
+  fft_twiddles(*g->fft, (int)plan.nu);
+  fft_twiddles(*g->fft, (int)plan.nv);
+  fft_twiddles(*g->fft, (int)plan.fft_n1);
+  fft_twiddles(*g->fft, (int)plan.fft_n2);
+  fft_prepare_rows(*g->fft, (int)plan.nu);
+  double *nu_w = nu_table_for(g, plan, dp);
+  float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
+  float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
+  float2 *acc = inversion ? (float2 *)g->arena.get(kSlotAcc, sizeof(float2) * npix) : nullptr;
+  float *img = prediction ? (float *)g->arena.get(kSlotImgCorr, sizeof(float) * npix) : nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  WGPU_CUDA(cudaEventCreate(&e0));
+  WGPU_CUDA(cudaEventCreate(&e1));
+  double best = std::numeric_limits<double>::infinity();
+  try {
+    for (int rep = 0; rep < 3; ++rep) {
+      WGPU_CUDA(cudaStreamSynchronize(s));
+      WGPU_CUDA(cudaEventRecord(e0, s));
+      const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis, d_mask,
+                                                 (int64_t)n_rows, (int64_t)n_chan, skip_zero, s);
+      if (inversion) {
+        WGPU_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * npix, s));
+        for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
+          const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+          const RowSel sel = row_sel(b.rows, (int)p0);
+          launch_grid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, s);
+          launch_fft_rows_forward_crop(*g->fft, dp, planes, R, rstride, nb, sel, g->d_flags, s);
+          launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb,
+                            -1.0f, sel, s);
+          launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                               R, rstride, nb, (int)p0, nu_w, acc, sel, s);
+        }
+      }
+      if (prediction) {
+        float2 *vacc = (float2 *)g->arena.get(kSlotVisAcc, sizeof(float2) * (b.n_out + 1));
+        WGPU_CUDA(cudaMemsetAsync(img, 0, sizeof(float) * npix, s));
+        WGPU_CUDA(cudaMemsetAsync(vacc, 0, sizeof(float2) * (b.n_out + 1), s));
+        for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
+          const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
+          const RowSel sel = row_sel(b.rows, (int)p0);
+          launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
+                                            img, nu_w, R, rstride, nb, (int)p0, s);
+          launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb,
+                            +1.0f, sel, s);
+          launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, sel, g->d_flags, s);
+          launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc,
+                        g->d_flags, s);
+        }
+      }
+      WGPU_CUDA(cudaEventRecord(e1, s));
+      WGPU_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      WGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, (double)ms);
+      if (ms > 20.f) break;
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+}  // namespace
+
+void tuning_cache_clear() {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache.clear();
+}
+
+namespace {
+
+// The plan for a call of a tuning gridder (see above).  `run` times one
+// candidate plan.  A shape seen before takes its remembered choice when that
+// entry still meets the request; the trials of the last tuning are kept in
+// the gridder.
+wgpu_plan_t tuned_plan(wgpu_gridder *g, char direction, double w_min, double w_max,
+                       int64_t n_vis, const std::function<double(const wgpu_plan_t &)> &run) {
+  g->last_trials.clear();
+  if (g->pinned) return plan_for(g, w_min, w_max, n_vis);
+  const wgpu_plan_request_t r = plan_request(g, w_min, w_max, n_vis);
+  const std::vector<wgpu_plan_t> all = plan_candidates(r, 1000);
+  const std::string key = tune_key(g, direction, w_min, w_max, n_vis);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end())
+      for (const wgpu_plan_t &p : all)
+        if (p.support == it->second.support && p.sigma == it->second.sigma) return p;
+  }
+  std::vector<wgpu_plan_t> cands(all.begin(),
+                                 all.begin() + std::min(all.size(), kTuneCandidates));
+  size_t best = 0;
+  if (cands.size() > 1) {
+    // one untimed run of the plan with the largest buffers first, so that the
+    // arena's allocations are not charged to whichever candidate runs first
+    size_t big = 0;
+    for (size_t i = 1; i < cands.size(); ++i)
+      if (cands[i].n_planes * cands[i].nu * cands[i].nv >
+          cands[big].n_planes * cands[big].nu * cands[big].nv)
+        big = i;
+    run(cands[big]);
+    std::vector<double> ms(cands.size());
+    for (size_t i = 0; i < cands.size(); ++i) {
+      ms[i] = run(cands[i]);
+      if (ms[i] < ms[best]) best = i;
+    }
+    for (size_t i = 0; i < cands.size(); ++i) {
+      wgpu_tuning_trial_t t;
+      std::memset(&t, 0, sizeof(t));
+      t.support = cands[i].support;
+      t.sigma = cands[i].sigma;
+      t.nu = cands[i].nu;
+      t.nv = cands[i].nv;
+      t.n_planes = cands[i].n_planes;
+      t.est_seconds = cands[i].est_seconds;
+      t.measured_ms = ms[i];
+      t.chosen = i == best ? 1 : 0;
+      g->last_trials.push_back(t);
+    }
+    if (g->verbosity > 0)
+      for (const wgpu_tuning_trial_t &t : g->last_trials)
+        std::fprintf(stderr, "wgpu tuning: W=%lld sigma=%.2f grid %lld planes %lld: %.2f ms%s\n",
+                     (long long)t.support, t.sigma, (long long)t.nu, (long long)t.n_planes,
+                     t.measured_ms, t.chosen ? " (chosen)" : "");
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = TuneChoice{cands[best].support, cands[best].sigma};
+  }
+  return cands[best];
 }
 
 void log_plan(const wgpu_gridder *g, const char *what, const wgpu_plan_t &p,
@@ -455,7 +652,14 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     end_call(g);
     return;
   }
-  const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
+  g->timer.mark("tune");
+  const wgpu_plan_t plan =
+      g->tuning ? tuned_plan(g, 'i', w_min, w_max, count,
+                             [&](const wgpu_plan_t &c) {
+                               return time_plan(g, c, d_uvw, d_freq, d_vis, nullptr, n_rows,
+                                                n_chan, true, true, false);
+                             })
+                : plan_for(g, w_min, w_max, count);
   g->last_plan = plan;
   log_plan(g, "invert", plan, count);
   const DevPlan dp = to_dev_plan(plan);
@@ -515,7 +719,14 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
       return;
     }
   }
-  const wgpu_plan_t plan = plan_for(g, w_min, w_max, count);
+  g->timer.mark("tune");
+  const wgpu_plan_t plan =
+      g->tuning ? tuned_plan(g, 'p', w_min, w_max, count,
+                             [&](const wgpu_plan_t &c) {
+                               return time_plan(g, c, d_uvw, d_freq, nullptr, d_mask, n_rows,
+                                                n_chan, false, false, true);
+                             })
+                : plan_for(g, w_min, w_max, count);
   g->last_plan = plan;
   log_plan(g, "predict", plan, count);
   const DevPlan dp = to_dev_plan(plan);
@@ -579,7 +790,13 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   compute_w_extent(b->uvw, b->freq, nullptr, b->mask, b->n_rows, b->n_chan, false, &w_min,
                    &w_max, &count, g->arena.get(kSlotErr, 64), s);
   if (count == 0) throw Error(WGPU_ERR_INVALID, "the mask selects no visibility");
-  b->plan = plan_for(g, w_min, w_max, count);
+  BoundState *bs = b.get();
+  b->plan = g->tuning ? tuned_plan(g, 'b', w_min, w_max, count,
+                                   [&](const wgpu_plan_t &c) {
+                                     return time_plan(g, c, bs->uvw, bs->freq, nullptr, bs->mask,
+                                                      n_rows, n_chan, false, true, true);
+                                   })
+                      : plan_for(g, w_min, w_max, count);
   g->last_plan = b->plan;
   log_plan(g, "bind", b->plan, count);
   const wgpu_plan_t &plan = b->plan;
@@ -808,6 +1025,19 @@ int wgpu_select_gain_mode(int polarization, size_t n_visibility_polarizations, i
 int wgpu_plan_make(const wgpu_plan_request_t *request, wgpu_plan_t *plan) {
   if (!request || !plan) return fail(WGPU_ERR_INVALID, "null argument");
   return guarded([&] { *plan = make_plan(*request); });
+}
+
+int wgpu_plan_candidates(const wgpu_plan_request_t *request, wgpu_plan_t *plans, int max_plans,
+                         int *n_plans) {
+  if (!request || !n_plans || max_plans < 0 || (max_plans > 0 && !plans))
+    return fail(WGPU_ERR_INVALID, "null argument or negative count");
+  *n_plans = 0;
+  return guarded([&] {
+    const std::vector<wgpu_plan_t> c = plan_candidates(*request, (size_t)max_plans);
+    const int n = (int)std::min<size_t>(c.size(), (size_t)max_plans);
+    for (int i = 0; i < n; ++i) plans[i] = c[i];
+    *n_plans = n;
+  });
 }
 
 int wgpu_gridder_create(size_t width, size_t height, size_t width_t,
@@ -1345,6 +1575,18 @@ int wgpu_gridder_pin_plan(wgpu_gridder_t *g, const wgpu_plan_t *plan) {
   g->pinned = true;
   return WGPU_OK;
 }
+
+int wgpu_gridder_last_tuning(const wgpu_gridder_t *g, wgpu_tuning_trial_t *trials,
+                             int max_trials, int *n_trials) {
+  if (!g || !n_trials || max_trials < 0 || (max_trials > 0 && !trials))
+    return fail(WGPU_ERR_INVALID, "null argument or negative count");
+  const int n = (int)std::min<size_t>(g->last_trials.size(), (size_t)max_trials);
+  for (int i = 0; i < n; ++i) trials[i] = g->last_trials[i];
+  *n_trials = n;
+  return WGPU_OK;
+}
+
+void wgpu_tuning_cache_clear(void) { wgpu::tuning_cache_clear(); }
 
 int wgpu_gridder_last_timings(const wgpu_gridder_t *g, double *ms, int *counts,
                               int max_entries, char *names, size_t names_len,

@@ -90,7 +90,6 @@ struct wgpu_facets {
   cudaStream_t side[kSide] = {};
   cudaEvent_t ev_grid = nullptr, ev_side[kSide] = {};
   FftTables *fft = nullptr;
-  std::vector<void *> owned;
   std::vector<Job> jobs;
   size_t n_rows = 0, n_chan = 0;
   double *d_uvw = nullptr, *d_freq = nullptr;
@@ -117,26 +116,74 @@ struct wgpu_facets {
   bool bound = false;
   double last_ms = 0;
 
+  // Device memory of the bound state: regions bumped out of chunks that
+  // outlive a bind, so that re-binding the batch (the next channel group, the
+  // next chunk of rows) reuses them instead of allocating and freeing each
+  // buffer.  Every region starts on a 512-byte boundary (the row transforms
+  // read planes with 16-byte bulk copies and vector loads).
+  struct Chunk {
+    char *base;
+    size_t size, used;
+  };
+  std::vector<Chunk> chunks;
+  static constexpr size_t kChunkMin = 256ull << 20;
+  DeviceArena scratch;  // bucketing scratch, kept across binds
+
   void *alloc(size_t bytes) {
-    void *p = nullptr;
-    WGPU_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
-    owned.push_back(p);
+    bytes = (std::max<size_t>(bytes, 16) + 511) & ~size_t(511);
+    for (Chunk &c : chunks)
+      if (c.size - c.used >= bytes) {
+        void *p = c.base + c.used;
+        c.used += bytes;
+        return p;
+      }
+    size_t want = std::max(bytes, kChunkMin);
+    char *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      want = bytes;
+      const cudaError_t e = cudaMalloc(&p, want);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(WGPU_ERR_NOMEM, "device allocation of " + std::to_string(bytes) +
+                                        " bytes failed: " + cudaGetErrorString(e));
+      }
+    }
+    chunks.push_back(Chunk{p, want, bytes});
     return p;
   }
-  void release() {
+  // Ends the bound state.  Its memory stays for the next bind; when the last
+  // bind needed more than one chunk, the chunks are merged into one of the
+  // size it used (plus an eighth) so that a similar bind fits without growing.
+  void release(bool keep_memory = true) {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
-    for (void *p : owned) cudaFree(p);
-    owned.clear();
     jobs.clear();
     waves.clear();
     bound = false;
+    size_t used = 0;
+    for (const Chunk &c : chunks) used += c.used;
+    if (!keep_memory || chunks.size() > 1) {
+      if (!chunks.empty() && stream) cudaStreamSynchronize(stream);
+      for (const Chunk &c : chunks) cudaFree(c.base);
+      chunks.clear();
+      if (keep_memory && used > 0) {
+        const size_t want = (used + used / 8 + 511) & ~size_t(511);
+        char *p = nullptr;
+        if (cudaMalloc(&p, want) == cudaSuccess)
+          chunks.push_back(Chunk{p, want, 0});
+        else
+          cudaGetLastError();
+      }
+    }
+    for (Chunk &c : chunks) c.used = 0;
+    if (!keep_memory) scratch.release();
   }
   ~wgpu_facets() {
     if (stream) cudaStreamSynchronize(stream);
-    release();
+    release(false);
     if (d_flags) cudaFree(d_flags);
     if (h_flags) cudaFreeHost(h_flags);
     if (fft) fft_tables_destroy(fft);
@@ -195,7 +242,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   }
   WGPU_CUDA(cudaMemcpyAsync(f->d_uvw, uvw, sizeof(double) * 3 * n_rows, cudaMemcpyHostToDevice, s));
   WGPU_CUDA(cudaMemcpyAsync(f->d_freq, freq, sizeof(double) * n_chan, cudaMemcpyHostToDevice, s));
-  DeviceArena arena;  // bucketing scratch, released at return
+  DeviceArena &arena = f->scratch;
 
   // jobs: group-major (job = group * n_facets + facet); w extent per group
   const size_t n_groups = f->groups.size() - 1;
@@ -297,7 +344,6 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     fft_twiddles(*f->fft, (int)j.plan.fft_n2);
     fft_prepare_rows(*f->fft, (int)j.plan.nu);
   }
-  arena.release();
 
   // waves of (job, plane batch) pairs within the plane budget
   std::vector<Slot> pending;

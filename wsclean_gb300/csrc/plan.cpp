@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <vector>
 
 #include "es_table.h"
 #include "wgpu_internal.h"
@@ -139,7 +140,9 @@ void nm1_range(int64_t width, int64_t height, double dl, double dm,
   *hi = mx;
 }
 
-wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
+namespace {
+
+void check_request(const wgpu_plan_request_t &req) {
   if (req.width < 2 || req.height < 2 || (req.width & 1) || (req.height & 1))
     throw Error(WGPU_ERR_INVALID, "trimmed image dimensions must be even and >= 2");
   if (!(req.dl > 0.0) || !(req.dm > 0.0))
@@ -148,25 +151,26 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     throw Error(WGPU_ERR_INVALID, "epsilon must be positive");
   if (!(req.w_max >= req.w_min))
     throw Error(WGPU_ERR_INVALID, "w_max < w_min");
+}
+
+// Every table entry within sigma_min..sigma_max (and the forced fields) whose
+// error estimate meets epsilon, as a plan without its plane batch, in table
+// order.  `fallback` receives the most accurate entry whatever its estimate.
+std::vector<wgpu_plan_t> feasible_plans(const wgpu_plan_request_t &req,
+                                        const EsKernelEntry **fallback, double *fallback_err) {
   const double smin = req.sigma_min > 0 ? req.sigma_min : 1.1;
   const double smax = req.sigma_max > 0 ? req.sigma_max : 2.0;
-
   double lo, hi;
-  nm1_range(req.width, req.height, req.dl, req.dm, req.l_shift, req.m_shift,
-            &lo, &hi);
+  nm1_range(req.width, req.height, req.dl, req.dm, req.l_shift, req.m_shift, &lo, &hi);
   const double wrange = req.w_max - req.w_min;
   // w-gridding is skipped only when the whole w spread changes the phase of
   // any pixel by a negligible fraction of epsilon.
   const bool use_w = M_PI * wrange * (hi - lo) > 1e-3 * req.epsilon;
   const double ndim = use_w ? 3.0 : 2.0;
   const double n_vis = std::max<double>(1.0, (double)req.n_vis);
-
-  wgpu_plan_t best;
-  std::memset(&best, 0, sizeof(best));
-  double best_cost = std::numeric_limits<double>::infinity();
-  double fallback_err = std::numeric_limits<double>::infinity();
-  const EsKernelEntry *fallback = nullptr;
-
+  *fallback = nullptr;
+  *fallback_err = std::numeric_limits<double>::infinity();
+  std::vector<wgpu_plan_t> out;
   for (int i = 0; i < kEsKernelTableSize; ++i) {
     const EsKernelEntry &e = kEsKernelTable[i];
     if (e.sigma < smin - 1e-9 || e.sigma > smax + 1e-9) continue;
@@ -180,9 +184,9 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     const double alias = std::sqrt(ndim) * e.err_max;
     const double fp32 = kFp32Noise * std::pow(e.amp_rms, ndim);
     const double est = std::sqrt(alias * alias + fp32 * fp32);
-    if (est < fallback_err) {
-      fallback_err = est;
-      fallback = &e;
+    if (est < *fallback_err) {
+      *fallback_err = est;
+      *fallback = &e;
     }
     if (est > req.epsilon) continue;
 
@@ -193,8 +197,8 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     p.support = e.support;
     p.sigma = e.sigma;
     p.beta = e.beta;
-    // uv tiles of 16 x 16 cells (the gridding work units pair them with 16
-    // w planes); the grid spans at least two tiles per axis
+    // uv tiles of 16 x 16 cells: the gridding kernels give one thread to each
+    // tile cell and pair a tile with 16 w planes
     const int64_t tile = 16;
     if (req.force_tile > 0 && req.force_tile != tile) continue;
     // row length: the next size with a row-transform schedule
@@ -231,12 +235,38 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     const double t_fft = 2.0 * (double)p.n_planes *
                          (16.0 * nu * nv + 40.0 * nv * rstride) / kByteRate;
     p.est_seconds = t_grid + t_fft;
-    if (p.est_seconds < best_cost) {
-      best_cost = p.est_seconds;
-      best = p;
-    }
+    out.push_back(p);
   }
-  if (!std::isfinite(best_cost)) {
+  return out;
+}
+
+// Planes resident per pipeline step, and the column decomposition.
+void finish_plan(wgpu_plan_t &p, const wgpu_plan_request_t &req) {
+  const int64_t rstride = (p.width + 31) / 32 * 32;
+  // plane + cropped rows + the gridding units' spilled border cells (at most
+  // (W - 1)(2T + W - 1) cells per T x T tile)
+  const double spill = (double)(p.support - 1) * (2.0 * p.tile + p.support - 1) /
+                       ((double)p.tile * p.tile);
+  const double per_plane = 8.0 * p.nu * p.nv * (1.0 + spill) + 8.0 * p.nv * rstride;
+  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 64e9;
+  int64_t batch = (int64_t)std::floor(budget / per_plane);
+  int64_t cap = req.max_plane_batch > 0 ? req.max_plane_batch : 32;
+  batch = std::max<int64_t>(1, std::min<int64_t>(std::min(batch, cap), p.n_planes));
+  // whole 16-plane gridding groups where the batch allows it
+  const int64_t group = grid_plane_group();
+  if (batch > group && batch < p.n_planes) batch -= batch % group;
+  p.plane_batch = batch;
+  fft_decompose(p.nv, &p.fft_n1, &p.fft_n2);
+}
+
+}  // namespace
+
+wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
+  check_request(req);
+  const EsKernelEntry *fallback;
+  double fallback_err;
+  const std::vector<wgpu_plan_t> c = feasible_plans(req, &fallback, &fallback_err);
+  if (c.empty()) {
     if (fallback == nullptr || req.force_support > 0)
       throw Error(WGPU_ERR_INVALID, "no kernel configuration satisfies the request");
     // Most accurate entry available: retry pinned to it.
@@ -246,23 +276,27 @@ wgpu_plan_t make_plan(const wgpu_plan_request_t &req) {
     r2.epsilon = std::max(req.epsilon, fallback_err * 1.0001);
     return make_plan(r2);
   }
-  // Planes resident per pipeline step.
-  const int64_t rstride = (best.width + 31) / 32 * 32;
-  // plane + cropped rows + the gridding units' spilled border cells (at most
-  // (W - 1)(2T + W - 1) cells per T x T tile)
-  const double spill = (double)(best.support - 1) * (2.0 * best.tile + best.support - 1) /
-                       ((double)best.tile * best.tile);
-  const double per_plane = 8.0 * best.nu * best.nv * (1.0 + spill) + 8.0 * best.nv * rstride;
-  const double budget = req.memory_budget_bytes > 0 ? req.memory_budget_bytes : 64e9;
-  int64_t batch = (int64_t)std::floor(budget / per_plane);
-  int64_t cap = req.max_plane_batch > 0 ? req.max_plane_batch : 32;
-  batch = std::max<int64_t>(1, std::min<int64_t>(std::min(batch, cap), best.n_planes));
-  // whole 16-plane gridding groups where the batch allows it
-  const int64_t group = grid_plane_group();
-  if (batch > group && batch < best.n_planes) batch -= batch % group;
-  best.plane_batch = batch;
-  fft_decompose(best.nv, &best.fft_n1, &best.fft_n2);
-  return best;
+  // lowest cost-model time; the first in table order on ties
+  size_t best = 0;
+  for (size_t i = 1; i < c.size(); ++i)
+    if (c[i].est_seconds < c[best].est_seconds) best = i;
+  wgpu_plan_t p = c[best];
+  finish_plan(p, req);
+  return p;
+}
+
+std::vector<wgpu_plan_t> plan_candidates(const wgpu_plan_request_t &req, size_t max_plans) {
+  const wgpu_plan_t first = make_plan(req);  // validates; handles the fallback
+  const EsKernelEntry *fallback;
+  double fallback_err;
+  std::vector<wgpu_plan_t> c = feasible_plans(req, &fallback, &fallback_err);
+  if (c.empty()) return {first};
+  std::stable_sort(c.begin(), c.end(), [](const wgpu_plan_t &a, const wgpu_plan_t &b) {
+    return a.est_seconds < b.est_seconds;
+  });
+  if (c.size() > max_plans) c.resize(std::max<size_t>(1, max_plans));
+  for (wgpu_plan_t &p : c) finish_plan(p, req);
+  return c;
 }
 
 DevPlan to_dev_plan(const wgpu_plan_t &p) {

@@ -87,6 +87,9 @@ void correction_tables(const wgpu_plan_t &plan, std::vector<float> &hx, std::vec
 
 // ---- planner (plan.cpp) ----
 wgpu_plan_t make_plan(const wgpu_plan_request_t &req);
+// The plans that meet the request's epsilon, lowest cost-model time first (at
+// most max_plans; the first is make_plan's choice).
+std::vector<wgpu_plan_t> plan_candidates(const wgpu_plan_request_t &req, size_t max_plans);
 void nm1_range(int64_t width, int64_t height, double dl, double dm,
                double l_shift, double m_shift, double *lo, double *hi);
 int64_t good_fft_size(int64_t n, int64_t multiple);

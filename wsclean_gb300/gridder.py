@@ -245,6 +245,15 @@ class WGriddingGridder_Simple:
         keys = names.value.decode().split(";") if n.value else []
         return {k: (ms[i], cnt[i]) for i, k in enumerate(keys)}
 
+    def last_tuning(self):
+        """Candidates timed by the last planning of a tuning gridder (an empty
+        list when the plan came from a remembered choice, a pinned plan or a
+        gridder without tuning)."""
+        trials = (_lib.TuningTrial * 64)()
+        n = C.c_int()
+        check(lib().wgpu_gridder_last_tuning(self._h, trials, 64, C.byref(n)))
+        return [trials[i].as_dict() for i in range(n.value)]
+
     def pin_plan(self, plan):
         """Use `plan` (a Plan from last_plan()) for following calls; None unpins."""
         check(lib().wgpu_gridder_pin_plan(self._h, None if plan is None else C.byref(plan)))
