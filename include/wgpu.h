@@ -452,6 +452,9 @@ typedef struct wgpu_server_stats {
   double peak_device_bytes;   /* largest device_bytes_in_use */
   double visibilities;        /* n_rows * n_chan of completed requests */
   double elapsed_s;           /* first submission to last completion */
+  uint64_t held_for_memory;   /* requests passed over at least once because the
+                                 memory left in the budget could not take them
+                                 (or an earlier request that did not fit) */
 } wgpu_server_stats_t;
 
 typedef struct wgpu_server wgpu_server_t;

@@ -118,6 +118,7 @@ def test_admission_by_device_memory(wgpu_lib):
         out = [srv.wait(t).copy() for t in tickets]
         stats = srv.stats()
     assert stats["peak_running"] == 1
+    assert stats["held_for_memory"] >= 1  # later requests waited for the budget
     alone = _run_alone(reqs)
     for a, b in zip(out, alone):
         assert rel(a, b) <= SAME

@@ -79,7 +79,8 @@ class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_uint64),
                 ("running", C.c_uint64), ("peak_running", C.c_uint64),
                 ("device_bytes_in_use", C.c_double), ("peak_device_bytes", C.c_double),
-                ("visibilities", C.c_double), ("elapsed_s", C.c_double)]
+                ("visibilities", C.c_double), ("elapsed_s", C.c_double),
+                ("held_for_memory", C.c_uint64)]
 
 
 class Facet(C.Structure):

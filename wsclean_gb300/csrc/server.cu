@@ -42,6 +42,7 @@ struct Ticket {
   int status = WGPU_OK;
   std::string error;
   bool done = false;
+  bool held = false;  // passed over at least once for lack of device memory
 };
 
 struct Session {
@@ -112,7 +113,7 @@ struct wgpu_server {
   uint64_t next_id = 1;
   bool stopping = false;
   std::vector<std::thread> workers;
-  uint64_t completed = 0, failed = 0;
+  uint64_t completed = 0, failed = 0, held_for_memory = 0;
   double vis_done = 0;
   Clock::time_point first_submit, last_finish;
   bool any_submit = false;
@@ -137,6 +138,10 @@ struct wgpu_server {
       const bool fits = used + need <= budget || running == 0;
       if (need > 0 && (memory_blocked || !fits)) {
         memory_blocked = true;
+        if (!t->held) {
+          t->held = true;
+          ++held_for_memory;
+        }
         if (sid != 0) blocked.insert(sid);
         continue;
       }
@@ -386,6 +391,7 @@ int wgpu_server_stats(wgpu_server_t *s, wgpu_server_stats_t *out) {
   out->device_bytes_in_use = s->used;
   out->peak_device_bytes = s->peak_used;
   out->visibilities = s->vis_done;
+  out->held_for_memory = s->held_for_memory;
   out->elapsed_s =
       s->any_submit && s->completed + s->failed > 0
           ? std::chrono::duration<double>(s->last_finish - s->first_submit).count()

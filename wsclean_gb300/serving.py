@@ -183,7 +183,9 @@ def _serve(pool, reqs, device_bytes, plane_budget, slots, arrivals, keep_ids=())
         raise RuntimeError("; ".join(errors[:5]))
     return dict(wall_s=wall, gvis_s=total_vis(reqs) / wall / 1e9,
                 peak_running=int(stats["peak_running"]),
-                peak_device_gb=stats["peak_device_bytes"] / 1e9, **_percentiles(lat)), kept
+                peak_device_gb=stats["peak_device_bytes"] / 1e9,
+                submissions_held_for_memory=int(stats["held_for_memory"]),
+                **_percentiles(lat)), kept
 
 
 def saturated(pool, reqs, device_bytes, plane_budget, slots, keep_ids=()):
