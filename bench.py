@@ -569,6 +569,9 @@ def run_gpu(args, rank, world, local):
     if args.tune_bound:
         # the same major cycles on a gridder created with tuning = 1: the bind
         # times the best candidate plans on these rows and keeps the fastest
+        # (the untuned gridder's buffers are released first)
+        g.close()
+        torch.cuda.empty_cache()
         gt = WGriddingGridder_Simple(W, W, W, W, d["dl"], d["dl"], 0.0, 0.0, os.cpu_count(),
                                      epsilon=eps, num_t=num_t, tuning=True)
         st = torch.cuda.ExternalStream(gt.stream(), device=dev)

@@ -585,6 +585,17 @@ wgpu_plan_t tuned_plan(wgpu_gridder *g, char direction, double w_min, double w_m
                                  all.begin() + std::min(all.size(), kTuneCandidates));
   size_t best = 0;
   if (cands.size() > 1) {
+    // A candidate whose buffers do not fit in the device memory left is
+    // skipped (its time counts as infinite); the first, untuned plan is the
+    // one that must run.
+    auto timed = [&](const wgpu_plan_t &c, bool required) -> double {
+      try {
+        return run(c);
+      } catch (const Error &e) {
+        if (e.status != WGPU_ERR_NOMEM || required) throw;
+        return std::numeric_limits<double>::infinity();
+      }
+    };
     // one untimed run of the plan with the largest buffers first, so that the
     // arena's allocations are not charged to whichever candidate runs first
     size_t big = 0;
@@ -592,10 +603,10 @@ wgpu_plan_t tuned_plan(wgpu_gridder *g, char direction, double w_min, double w_m
       if (cands[i].n_planes * cands[i].nu * cands[i].nv >
           cands[big].n_planes * cands[big].nu * cands[big].nv)
         big = i;
-    run(cands[big]);
+    timed(cands[big], false);
     std::vector<double> ms(cands.size());
     for (size_t i = 0; i < cands.size(); ++i) {
-      ms[i] = run(cands[i]);
+      ms[i] = timed(cands[i], i == 0);
       if (ms[i] < ms[best]) best = i;
     }
     for (size_t i = 0; i < cands.size(); ++i) {
@@ -797,6 +808,10 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                                                       n_rows, n_chan, false, true, true);
                                    })
                       : plan_for(g, w_min, w_max, count);
+  if (g->tuning)
+    // the bound set owns its batch buffers: drop the ones the timing runs used
+    for (int slot : {kSlotPlanes, kSlotRows, kSlotAcc, kSlotImgCorr, kSlotVisAcc})
+      g->arena.release(slot);
   g->last_plan = b->plan;
   log_plan(g, "bind", b->plan, count);
   const wgpu_plan_t &plan = b->plan;

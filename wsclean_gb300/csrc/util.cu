@@ -98,11 +98,14 @@ size_t DeviceArena::total() const {
 }
 
 void DeviceArena::release() {
-  for (int i = 0; i < kSlots; ++i) {
-    if (ptr_[i]) cudaFree(ptr_[i]);
-    ptr_[i] = nullptr;
-    size_[i] = 0;
-  }
+  for (int i = 0; i < kSlots; ++i) release(i);
+}
+
+void DeviceArena::release(int slot) {
+  if (slot < 0 || slot >= kSlots) return;
+  if (ptr_[slot]) cudaFree(ptr_[slot]);
+  ptr_[slot] = nullptr;
+  size_[slot] = 0;
 }
 
 // ---------------------------------------------------------------------------

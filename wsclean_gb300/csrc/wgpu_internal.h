@@ -32,7 +32,7 @@ struct Error : std::runtime_error {
   } while (0)
 
 void count_launch(int n = 1);
-int sm_count();  // multiprocessors of the current device (first call's device)
+int sm_count();  // multiprocessors of the current device (cached per device)
 uint64_t launch_count();
 uint64_t thread_launch_count();  // launches issued by the calling thread
 
@@ -397,6 +397,7 @@ class DeviceArena {
   void *get(int slot, size_t bytes);
   size_t total() const;
   void release();
+  void release(int slot);  // frees one slot (the next get allocates it again)
 
  private:
   static constexpr int kSlots = 48;
