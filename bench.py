@@ -757,15 +757,22 @@ def run_facets_full(args):
     # bucketing scratch stay allocated from one bind to the next
     fb = FacetBatch(facets, [0, 2], epsilon=eps)
 
+    phase_s = {"bind": 0.0, "invert": 0.0}
+
     def step():
         for gi in range(n_groups):
             c0 = groups[gi]
+            t0 = time.perf_counter()
             fb.bind(d["uvw"], freq[c0:c0 + 2])
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
             fb.invert_device(d_vis_g[gi].data_ptr(), outs[gi].data_ptr())
+            torch.cuda.synchronize()
+            phase_s["bind"] += t1 - t0
+            phase_s["invert"] += time.perf_counter() - t1
             if gi == 0:
                 info.update(fb.info())
                 info["plan0"] = fb.job_plan(0)
-        torch.cuda.synchronize()
 
     for _ in range(min(args.warmup, 1)):
         step()
@@ -773,6 +780,7 @@ def run_facets_full(args):
     clocks.start()
     l0 = _lib_launches()
     torch.cuda.synchronize()
+    phase_s.update(bind=0.0, invert=0.0)
     w0 = time.perf_counter()
     for _ in range(args.steps):
         step()
@@ -780,6 +788,7 @@ def run_facets_full(args):
     clk = clocks.stop()
     launches = _lib_launches() - l0
     fb.close()
+    per_group_ms = {k: round(v * 1e3 / (args.steps * n_groups), 1) for k, v in phase_s.items()}
     job_vis = float(n_rows) * 16 * len(facets)
     # the same jobs one at a time through the plain per-call path
     d_uvw = torch.as_tensor(d["uvw"], device=dev)
@@ -836,6 +845,7 @@ def run_facets_full(args):
                    "job_samples": job_vis,
                    "plain_one_at_a_time_gvis_s": plain_value,
                    "batched_over_plain": value / plain_value, "checks": checks,
+                   "per_group_ms": per_group_ms,
                    "datagen_s": round(gen_s, 1),
                    "l2": "working set larger than L2 (planes of every wave, 1.6 GB of samples)",
                    "step": "per output-channel group: re-bind of one batch object (upload, "

@@ -97,50 +97,6 @@ struct StageTimer {
   }
 };
 
-namespace wgpu {
-// Grid-correction tables of a plan: 1/psihat per image column and row, and
-// the Gauss-Legendre nodes (z_q, w_q phi(z_q)) of the per-pixel w factor.
-void correction_tables(const wgpu_plan_t &plan, std::vector<float> &hx, std::vector<float> &hy,
-                       std::vector<float> &hg) {
-  constexpr int kGlNodes = kCorrGlNodes;
-  hx.resize(plan.width);
-  hy.resize(plan.height);
-  hg.resize(2 * kGlNodes);
-  for (int64_t x = 0; x < plan.width; ++x)
-    hx[x] = (float)(1.0 / es_fourier(plan.beta, (int)plan.support,
-                                     (double)(plan.width / 2 - x) / (double)plan.nu));
-  for (int64_t y = 0; y < plan.height; ++y)
-    hy[y] = (float)(1.0 / es_fourier(plan.beta, (int)plan.support,
-                                     (double)(y - plan.height / 2) / (double)plan.nv));
-  // Gauss-Legendre rule of 2*kGlNodes points on [-1, 1], positive half
-  const int n = 2 * kGlNodes;
-  for (int i = 0; i < kGlNodes; ++i) {
-    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
-    for (int it = 0; it < 100; ++it) {
-      double p0 = 1.0, p1 = z;
-      for (int k = 2; k <= n; ++k) {
-        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-        p0 = p1;
-        p1 = p2;
-      }
-      dp = n * (z * p1 - p0) / (z * z - 1.0);
-      const double dz = p1 / dp;
-      z -= dz;
-      if (std::fabs(dz) < 1e-16) break;
-    }
-    double p0 = 1.0, p1 = z;
-    for (int k = 2; k <= n; ++k) {
-      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-      p0 = p1;
-      p1 = p2;
-    }
-    dp = n * (z * p1 - p0) / (z * z - 1.0);
-    const double w = 2.0 / ((1.0 - z * z) * dp * dp);
-    hg[2 * i] = (float)z;
-    hg[2 * i + 1] = (float)(w * es_kernel(plan.beta, z));
-  }
-}
-}  // namespace wgpu
 
 // Device-resident state of a bound visibility set (see wgpu_gridder_bind):
 // bucketing, work items, buffers and the captured inversion / prediction
@@ -338,8 +294,9 @@ __global__ void image_in_kernel(const float *__restrict__ in, int prec, int64_t 
     ((float *)img)[i] = v;
 }
 
-// Host-side correction tables for one plan: cx, cy (1/psihat per column/row)
-// and the quadrature nodes (z_q, w_q phi(z_q)) for the per-pixel w factor.
+// Correction tables for one plan, computed on the device: cx, cy (1/psihat per
+// column/row) and the quadrature nodes (z_q, w_q phi(z_q)) of the per-pixel w
+// factor.
 void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
                         float **cy, float **gl) {
   // The tables depend on the kernel and grid geometry only: reuse them while
@@ -354,16 +311,10 @@ void upload_corrections(wgpu_gridder *g, const wgpu_plan_t &plan, float **cx,
     *gl = (float *)g->arena.get(kSlotGl, sizeof(float) * 2 * kGlNodes);
     return;
   }
-  std::vector<float> hx, hy, hg;
-  correction_tables(plan, hx, hy, hg);
   *cx = (float *)g->arena.get(kSlotCorrX, sizeof(float) * plan.width);
   *cy = (float *)g->arena.get(kSlotCorrY, sizeof(float) * plan.height);
   *gl = (float *)g->arena.get(kSlotGl, sizeof(float) * 2 * kGlNodes);
-  WGPU_CUDA(cudaMemcpyAsync(*cx, hx.data(), sizeof(float) * plan.width, cudaMemcpyHostToDevice, g->stream));
-  WGPU_CUDA(cudaMemcpyAsync(*cy, hy.data(), sizeof(float) * plan.height, cudaMemcpyHostToDevice, g->stream));
-  WGPU_CUDA(cudaMemcpyAsync(*gl, hg.data(), sizeof(float) * 2 * kGlNodes, cudaMemcpyHostToDevice, g->stream));
-  // the host vectors die at return: make the copies complete first
-  WGPU_CUDA(cudaStreamSynchronize(g->stream));
+  launch_correction_tables(plan, *cx, *cy, *gl, g->stream);
   g->corr_key = key;
 }
 

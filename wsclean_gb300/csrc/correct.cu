@@ -1,5 +1,8 @@
 // K6 grid correction + image accumulation, the per-pixel n-1 table, the
 // prediction pre-correction and output permutation, and K7 gains + collapse.
+#include <cmath>
+#include <vector>
+
 #include "polarization.cuh"
 #include "wgpu_internal.h"
 
@@ -23,6 +26,32 @@ __global__ void nu_table_kernel(DevPlan p, double *nu_w) {
   const double r2 = l * l + m * m;
   const double nm1 = r2 >= 1.0 ? 0.0 : -r2 / (sqrt(1.0 - r2) + 1.0);
   nu_w[i] = nm1 - p.nm1_center;
+}
+
+// Grid-correction tables: thread t < width gives cx[t] = 1 / psihat((width/2 -
+// t) / nu), the next height threads cy[y] = 1 / psihat((y - height/2) / nv),
+// psihat(f) = W sum_i g_i cos(pi f W z_i) over the planner's quadrature (the
+// same sum as es_fourier, in FP64); the first 2 kCorrGlNodes threads also copy
+// the w-factor nodes.
+struct CorrQuad {
+  double z[kEsQuadNodes], g[kEsQuadNodes];
+  float gl[2 * kCorrGlNodes];
+};
+
+__global__ void correction_tables_kernel(const CorrQuad q, int width, int height, int nu, int nv,
+                                         int support, float *cx, float *cy, float *gl) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * kCorrGlNodes) gl[t] = q.gl[t];
+  if (t >= width + height) return;
+  const double f = t < width ? (double)(width / 2 - t) / (double)nu
+                             : (double)(t - width - height / 2) / (double)nv;
+  double acc = 0.0;
+  for (int i = 0; i < kEsQuadNodes; ++i) acc += q.g[i] * cos(M_PI * f * support * q.z[i]);
+  const float v = (float)(1.0 / (support * acc));
+  if (t < width)
+    cx[t] = v;
+  else
+    cy[t - width] = v;
 }
 
 // 1 / psihat(dw * nu) by Gauss-Legendre quadrature over the positive half:
@@ -227,6 +256,57 @@ void launch_forward_gains(int mode, int n_pol, int64_t n_rows, int64_t n_chan,
                                                           n_times, n_ant, polarization, out,
                                                           err_flag);
   check_launch("forward_gains_kernel");
+}
+
+// The Gauss-Legendre rule of 2 kCorrGlNodes points on [-1, 1] (positive
+// half), computed once.
+const std::vector<double> &corr_gl_rule() {
+  static const std::vector<double> rule = [] {
+    std::vector<double> r(2 * kCorrGlNodes);
+    const int n = 2 * kCorrGlNodes;
+    for (int i = 0; i < kCorrGlNodes; ++i) {
+      double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+      for (int it = 0; it < 100; ++it) {
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; ++k) {
+          const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+          p0 = p1;
+          p1 = p2;
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        const double dz = p1 / dp;
+        z -= dz;
+        if (std::fabs(dz) < 1e-16) break;
+      }
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      r[2 * i] = z;
+      r[2 * i + 1] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+    return r;
+  }();
+  return rule;
+}
+
+void launch_correction_tables(const wgpu_plan_t &plan, float *cx, float *cy, float *gl,
+                              cudaStream_t s) {
+  CorrQuad q;
+  es_quadrature(plan.beta, q.z, q.g);
+  const std::vector<double> &rule = corr_gl_rule();
+  for (int i = 0; i < kCorrGlNodes; ++i) {
+    q.gl[2 * i] = (float)rule[2 * i];
+    q.gl[2 * i + 1] = (float)(rule[2 * i + 1] * es_kernel(plan.beta, rule[2 * i]));
+  }
+  const int n = (int)std::max<int64_t>(plan.width + plan.height, 2 * kCorrGlNodes);
+  correction_tables_kernel<<<blocks_for(n), kThreads, 0, s>>>(
+      q, (int)plan.width, (int)plan.height, (int)plan.nu, (int)plan.nv, (int)plan.support, cx, cy,
+      gl);
+  check_launch("correction_tables_kernel");
 }
 
 void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s) {

@@ -317,15 +317,10 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     j.acc = (float2 *)f->alloc(sizeof(float2) * npix);
     j.nu_w = (double *)f->alloc(sizeof(double) * npix);
     launch_nu_table(j.dp, j.nu_w, s);
-    std::vector<float> hx, hy, hg;
-    correction_tables(j.plan, hx, hy, hg);
-    j.cx = (float *)f->alloc(sizeof(float) * hx.size());
-    j.cy = (float *)f->alloc(sizeof(float) * hy.size());
-    j.gl = (float *)f->alloc(sizeof(float) * hg.size());
-    WGPU_CUDA(cudaMemcpyAsync(j.cx, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice, s));
-    WGPU_CUDA(cudaMemcpyAsync(j.cy, hy.data(), sizeof(float) * hy.size(), cudaMemcpyHostToDevice, s));
-    WGPU_CUDA(cudaMemcpyAsync(j.gl, hg.data(), sizeof(float) * hg.size(), cudaMemcpyHostToDevice, s));
-    WGPU_CUDA(cudaStreamSynchronize(s));  // host tables die at the end of the iteration
+    j.cx = (float *)f->alloc(sizeof(float) * j.plan.width);
+    j.cy = (float *)f->alloc(sizeof(float) * j.plan.height);
+    j.gl = (float *)f->alloc(sizeof(float) * 2 * kCorrGlNodes);
+    launch_correction_tables(j.plan, j.cx, j.cy, j.gl, s);
     j.img = f->d_images + img_off;
     img_off += j.facet.width * j.facet.height;
     wgpu_facets *fp = f;

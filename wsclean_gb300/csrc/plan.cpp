@@ -82,6 +82,14 @@ double es_kernel(double beta, double z) {
   return std::exp(beta * (std::sqrt(1.0 - z * z) - 1.0));
 }
 
+void es_quadrature(double beta, double *z, double *g) {
+  const GaussLegendre &q = gl();
+  for (int i = 0; i < GaussLegendre::kN; ++i) {
+    z[i] = q.x[i];
+    g[i] = q.w[i] * es_kernel(beta, q.x[i]);
+  }
+}
+
 double es_fourier(double beta, int support, double f) {
   const GaussLegendre &g = gl();
   double acc = 0.0;

@@ -81,8 +81,11 @@ struct GridJob {
 };
 
 constexpr int kCorrGlNodes = 48;  // Gauss-Legendre nodes (positive half) of the w correction
-void correction_tables(const wgpu_plan_t &plan, std::vector<float> &hx, std::vector<float> &hy,
-                       std::vector<float> &hg);
+// Grid-correction tables of a plan, computed on the device on stream s:
+// cx[width] and cy[height] (1 / psihat per image column and row) and gl[2 *
+// kCorrGlNodes] (nodes z_q and weights w_q phi(z_q) of the per-pixel w factor).
+void launch_correction_tables(const wgpu_plan_t &plan, float *cx, float *cy, float *gl,
+                              cudaStream_t s);
 
 
 // ---- planner (plan.cpp) ----
@@ -96,6 +99,11 @@ int64_t good_fft_size(int64_t n, int64_t multiple);
 void fft_decompose(int64_t n, int64_t *n1, int64_t *n2);
 // ES kernel FT in cell units (FP64 Gauss-Legendre).
 double es_fourier(double beta, int support, double f);
+// The quadrature es_fourier sums: kEsQuadNodes nodes z of the positive half of
+// [-1, 1] and their weights times the kernel, so that es_fourier(beta, W, f) =
+// W * sum_i g[i] cos(pi f W z[i]).
+constexpr int kEsQuadNodes = 256;
+void es_quadrature(double beta, double *z, double *g);
 double es_kernel(double beta, double z);
 
 // ---- bucketing (bucket.cu) ----
