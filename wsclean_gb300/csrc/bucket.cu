@@ -349,8 +349,8 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------- stable LSD radix sort, 8-bit digits ----------------------
-constexpr int kSortItems = 8;
-constexpr int kSortTile = kThreads * kSortItems;  // 2048 elements per block
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kThreads * kSortItems;  // 4096 elements per block
 
 // digits: when non-null, element i's digit is digits[i] instead of the key's
 // 8 bits at `shift` (the corner pass).
