@@ -18,6 +18,7 @@
 
 #include <mutex>
 
+#include "record_ff.cuh"
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -28,7 +29,8 @@ constexpr int kThreads = 256;
 
 struct ChannelScale {
   double su, sv, sw;  // U = uvw_u * su (cells), V = uvw_v * sv, w = uvw_w * sw
-  float fsu, fsv, fsw, pad;  // the same rounded to float (FP32 footprint tests)
+  float fsu, fsv, fsw;  // the same rounded to float (FP32 footprint tests)
+  float lsu, lsv, lsw;  // the rests rounded to float (float-float records)
 };
 
 __global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
@@ -43,16 +45,23 @@ __global__ void channel_scales_kernel(const double *freq, int64_t n_chan,
   out[c].fsu = __double2float_rn(out[c].su);
   out[c].fsv = __double2float_rn(out[c].sv);
   out[c].fsw = __double2float_rn(fl);
-  out[c].pad = 0.f;
+  out[c].lsu = __double2float_rn(__dsub_rn(out[c].su, (double)out[c].fsu));
+  out[c].lsv = __double2float_rn(__dsub_rn(out[c].sv, (double)out[c].fsv));
+  out[c].lsw = __double2float_rn(__dsub_rn(fl, (double)out[c].fsw));
 }
 
-// uvw rows rounded to float (FP32 footprint tests), one float4 per row.
+// uvw rows rounded to float (FP32 footprint tests), one float4 per row, and
+// the rests rounded to float (float-float records), one float4 per row.
 __global__ void uvw_float_kernel(const double *__restrict__ uvw, int64_t n_rows,
-                                 float4 *__restrict__ out) {
+                                 float4 *__restrict__ out, float4 *__restrict__ out_lo) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
-  out[r] = make_float4(__double2float_rn(uvw[3 * r]), __double2float_rn(uvw[3 * r + 1]),
-                       __double2float_rn(uvw[3 * r + 2]), 0.f);
+  const double u = uvw[3 * r], v = uvw[3 * r + 1], w = uvw[3 * r + 2];
+  const float fu = __double2float_rn(u), fv = __double2float_rn(v), fw = __double2float_rn(w);
+  out[r] = make_float4(fu, fv, fw, 0.f);
+  out_lo[r] = make_float4(__double2float_rn(__dsub_rn(u, (double)fu)),
+                          __double2float_rn(__dsub_rn(v, (double)fv)),
+                          __double2float_rn(__dsub_rn(w, (double)fw)), 0.f);
 }
 
 // The float row of sample row r: from the table when there is one.
@@ -151,11 +160,13 @@ __device__ __forceinline__ bool wrap_decided(int c, int n, int *out) {
   return true;
 }
 
-// Key (and corner row / first plane) of a sample decided in FP32; false
-// when any of the three corners needs the FP64 footprint.
-__device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
-                                            const ChannelScale &cs, uint32_t *key, int *iu_out,
-                                            int *iv_out, int *ip_out) {
+// The footprint corner of a sample decided in FP32: the unwrapped corners
+// iu0, iv0, the wrapped iu, iv and the first plane ip; false when any of them
+// needs the FP64 footprint.
+__device__ __forceinline__ bool corners_decided(const DevPlan &p, const float4 rf,
+                                                const ChannelScale &cs, int *iu0_out,
+                                                int *iv0_out, int *iu_out, int *iv_out,
+                                                int *ip_out) {
   const float half = 0.5f * (float)p.support;
   int iu0, iv0, iu, iv, ip = 0;
   if (!ceil_decided(rf.x, cs.fsu, half, &iu0) || !ceil_decided(rf.y, cs.fsv, half, &iv0))
@@ -182,6 +193,21 @@ __device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
       ip = min(max((int)fy + 1, 0), ip_max);
     }
   }
+  *iu0_out = iu0;
+  *iv0_out = iv0;
+  *iu_out = iu;
+  *iv_out = iv;
+  *ip_out = ip;
+  return true;
+}
+
+// Key (and corner row / first plane) of a sample decided in FP32; false
+// when any of the three corners needs the FP64 footprint.
+__device__ __forceinline__ bool key_decided(const DevPlan &p, const float4 rf,
+                                            const ChannelScale &cs, uint32_t *key, int *iu_out,
+                                            int *iv_out, int *ip_out) {
+  int iu0, iv0, iu, iv, ip;
+  if (!corners_decided(p, rf, cs, &iu0, &iv0, &iu, &iv, &ip)) return false;
   const int tu = p.tile == 16 ? iu >> 4 : iu / p.tile;
   const int tv = p.tile == 16 ? iv >> 4 : iv / p.tile;
   const uint32_t tile = (uint32_t)(tv * p.ntu + tu);
@@ -529,15 +555,31 @@ __device__ __forceinline__ Footprint record_footprint(const DevPlan &p, const do
   return f;
 }
 
-// SHIFT: the image has an l or m shift (else the phase needs only w).
+// Writes record s as float4 pairs: (re, im, fu, fv), (fw, iu, iv, ip).
+__device__ __forceinline__ void store_record(VisRecord *rec, int64_t s, const float2 *vis,
+                                             uint32_t e, float sn, float cn, float fu, float fv,
+                                             float fw, int iu, int iv, int ip) {
+  float re, im;
+  if (vis) {
+    const float2 v = vis[e];
+    re = v.x * cn + v.y * sn;
+    im = v.y * cn - v.x * sn;
+  } else {
+    re = cn;
+    im = -sn;
+  }
+  reinterpret_cast<float4 *>(rec + s)[0] = make_float4(re, im, fu, fv);
+  reinterpret_cast<float4 *>(rec + s)[1] =
+      make_float4(fw, __int_as_float(iu), __int_as_float(iv), __int_as_float(ip));
+}
+
+// Record s (sample e) with the fractions and the phase argument from the FP64
+// chains.  SHIFT: the image has an l or m shift (else the phase needs only w).
 template <bool SHIFT>
-__global__ void __launch_bounds__(kThreads)
-    record_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
-                  const float2 *vis, int64_t n_chan, const uint32_t *perm,
-                  int64_t n_out, VisRecord *rec, const float4 *__restrict__ uvwf) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n_out) return;
-  const uint32_t e = perm[s];
+__device__ __forceinline__ void record_fp64(const DevPlan &p, const double *uvw,
+                                            const ChannelScale *cs, const float2 *vis,
+                                            int64_t n_chan, uint32_t e, int64_t s,
+                                            VisRecord *rec, const float4 *uvwf) {
   const uint32_t r = e / (uint32_t)n_chan, c = e - r * (uint32_t)n_chan;  // e < 2^32
   const double *row = uvw + 3 * (size_t)r;
   const ChannelScale sc = cs[c];
@@ -556,24 +598,84 @@ __global__ void __launch_bounds__(kThreads)
   t -= rint(t);
   float sn, cn;
   sincospif(2.0f * (float)t, &sn, &cn);
-  VisRecord o;
-  if (vis) {
-    const float2 v = vis[e];
-    o.re = v.x * cn + v.y * sn;
-    o.im = v.y * cn - v.x * sn;
-  } else {
-    o.re = cn;
-    o.im = -sn;
+  store_record(rec, s, vis, e, sn, cn, f.fu, f.fv, f.fw, f.iu, f.iv, f.ip);
+}
+
+template <bool SHIFT>
+__global__ void __launch_bounds__(kThreads)
+    record_kernel(DevPlan p, const double *uvw, const ChannelScale *cs,
+                  const float2 *vis, int64_t n_chan, const uint32_t *perm,
+                  int64_t n_out, VisRecord *rec, const float4 *__restrict__ uvwf) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_out) return;
+  record_fp64<SHIFT>(p, uvw, cs, vis, n_chan, perm[s], s, rec, uvwf);
+}
+
+// Records of a plan without shifts from float-float arithmetic (record_ff.cuh):
+// the corners decided in FP32 as key_kernel decides them, the fractions and
+// the phase argument where the error bound proves them equal to the FP64
+// chains.  Each block takes kRecordBlock consecutive records and lists the
+// ones it cannot decide in its own slice of `pending` (block b's entries from
+// b * kRecordBlock, their number in counts[b]); record_fix_kernel does those
+// in FP64.
+constexpr int kRecordBlock = 4 * kThreads;
+
+__global__ void __launch_bounds__(kThreads)
+    record_ff_kernel(DevPlan p, const ChannelScale *__restrict__ cs, const float2 *vis,
+                     int64_t n_chan, const uint32_t *__restrict__ perm, int64_t n_out,
+                     VisRecord *rec, const float4 *__restrict__ uvwf,
+                     const float4 *__restrict__ uvwl, uint32_t *__restrict__ pending,
+                     uint32_t *__restrict__ counts) {
+  __shared__ uint32_t n_left;
+  if (threadIdx.x == 0) n_left = 0;
+  __syncthreads();
+  const int64_t b0 = (int64_t)blockIdx.x * kRecordBlock;
+  const ff::PlanPairs pp{ff::Pair{p.w0f, p.w0l}, ff::Pair{p.inv_dwf, p.inv_dwl},
+                         ff::Pair{p.nm1_center_f, p.nm1_center_l}, p.n_planes > 1};
+  for (int k = 0; k < kRecordBlock / kThreads; ++k) {
+    const int64_t s = b0 + k * kThreads + threadIdx.x;
+    if (s >= n_out) break;
+    const uint32_t e = perm[s];
+    const uint32_t r = e / (uint32_t)n_chan, c = e - r * (uint32_t)n_chan;
+    const float4 hi = __ldg(uvwf + r), lo = __ldg(uvwl + r);
+    const ChannelScale sc = cs[c];
+    int iu0, iv0, iu, iv, ip;
+    float fu, fv, fw, arg;
+    const bool ok =
+        corners_decided(p, hi, sc, &iu0, &iv0, &iu, &iv, &ip) &&
+        ff::decide(ff::Pair{hi.x, lo.x}, ff::Pair{hi.y, lo.y}, ff::Pair{hi.z, lo.z},
+                   ff::Scales{ff::Pair{sc.fsu, sc.lsu}, ff::Pair{sc.fsv, sc.lsv},
+                              ff::Pair{sc.fsw, sc.lsw}},
+                   pp, iu0, iv0, ip, &fu, &fv, &fw, &arg);
+    if (!ok) {
+      pending[b0 + atomicAdd(&n_left, 1u)] = (uint32_t)s;
+      continue;
+    }
+    float sn, cn;
+    sincospif(2.0f * arg, &sn, &cn);
+    store_record(rec, s, vis, e, sn, cn, fu, fv, fw, iu, iv, ip);
   }
-  o.fu = f.fu;
-  o.fv = f.fv;
-  o.fw = f.fw;
-  o.iu = f.iu;
-  o.iv = f.iv;
-  o.ip = f.ip;
-  reinterpret_cast<float4 *>(rec + s)[0] = make_float4(o.re, o.im, o.fu, o.fv);
-  reinterpret_cast<float4 *>(rec + s)[1] =
-      make_float4(o.fw, __int_as_float(o.iu), __int_as_float(o.iv), __int_as_float(o.ip));
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = n_left;
+}
+
+// The records record_ff_kernel left undecided, in FP64: one warp per record
+// block's slice, so that the FP64 chains run with the warp's lanes full.
+__global__ void __launch_bounds__(kThreads)
+    record_fix_kernel(DevPlan p, const double *uvw, const ChannelScale *cs, const float2 *vis,
+                      int64_t n_chan, const uint32_t *__restrict__ perm, int64_t n_blocks,
+                      VisRecord *rec, const float4 *__restrict__ uvwf,
+                      const uint32_t *__restrict__ pending, const uint32_t *__restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b = w0; b < n_blocks; b += n_warps) {
+    const uint32_t cnt = counts[b];
+    for (uint32_t i = lane; i < cnt; i += 32) {
+      const uint32_t s = pending[b * kRecordBlock + i];
+      record_fp64<false>(p, uvw, cs, vis, n_chan, perm[s], s, rec, uvwf);
+    }
+  }
 }
 
 // ---------------- row occupancy ----------------------------------------------
@@ -757,7 +859,8 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   const uint32_t sentinel = (uint32_t)(((uint64_t)1 << bits) - 1);
 
   ChannelScale *cs = (ChannelScale *)arena.get(kSlotExtent, sizeof(ChannelScale) * (n_chan + 1) + 64);
-  float4 *uvwf = (float4 *)arena.get(kSlotUvwF32, sizeof(float4) * (n_rows + 1));
+  float4 *uvwf = (float4 *)arena.get(kSlotUvwF32, sizeof(float4) * 2 * (n_rows + 1));
+  float4 *uvwl = uvwf + (n_rows + 1);
   uint32_t *keys = (uint32_t *)arena.get(kSlotKeys, sizeof(uint32_t) * (n + 1));
   uint32_t *keys2 = (uint32_t *)arena.get(kSlotKeysAlt, sizeof(uint32_t) * (n + 1));
   uint32_t *vals = (uint32_t *)arena.get(kSlotVals, sizeof(uint32_t) * (n + 1));
@@ -780,7 +883,8 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     // their count in the word after the channel scales
     uint32_t *n_pending = (uint32_t *)(cs + n_chan + 1);
     WGPU_CUDA(cudaMemsetAsync(n_pending, 0, sizeof(uint32_t), s));
-    uvw_float_kernel<<<grid_for(n_rows, kThreads), kThreads, 0, s>>>(d_uvw, n_rows, uvwf);
+    uvw_float_kernel<<<grid_for(n_rows, kThreads), kThreads, 0, s>>>(d_uvw, n_rows, uvwf,
+                                                                         uvwl);
     check_launch("uvw_float_kernel");
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
@@ -811,11 +915,22 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   res.records = (VisRecord *)arena.get(kSlotRecords, sizeof(VisRecord) * (res.n_out + 1));
   if (res.n_out > 0) {
     const bool shift = p.l_shift != 0.0 || p.m_shift != 0.0;
-    (shift ? record_kernel<true> : record_kernel<false>)<<<grid_for(res.n_out, kThreads),
-                                                          kThreads, 0, s>>>(
-        p, d_uvw, cs, skip_zero ? (const float2 *)d_vis : nullptr, n_chan,
-        res.perm, res.n_out, res.records, uvwf);
-    check_launch("record_kernel");
+    const float2 *vis = skip_zero ? (const float2 *)d_vis : nullptr;
+    if (shift) {
+      record_kernel<true><<<grid_for(res.n_out, kThreads), kThreads, 0, s>>>(
+          p, d_uvw, cs, vis, n_chan, res.perm, res.n_out, res.records, uvwf);
+      check_launch("record_kernel");
+    } else {
+      // undecided records listed in kout (free after the sort), counts per
+      // record block in vout
+      const int64_t n_blocks = (res.n_out + kRecordBlock - 1) / kRecordBlock;
+      record_ff_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(
+          p, cs, vis, n_chan, res.perm, res.n_out, res.records, uvwf, uvwl, kout, vout);
+      check_launch("record_ff_kernel");
+      record_fix_kernel<<<sm_count() * 8, kThreads, 0, s>>>(
+          p, d_uvw, cs, vis, n_chan, res.perm, n_blocks, res.records, uvwf, kout, vout);
+      check_launch("record_fix_kernel");
+    }
   }
   return res;
 }

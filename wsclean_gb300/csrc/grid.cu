@@ -694,9 +694,13 @@ __global__ void __launch_bounds__(kThreads, 2)
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
     cells[c] = make_float2(0.f, 0.f);
   __syncthreads();
-  for (uint32_t item = blockIdx.x; item < total; item += gridDim.x)
-    grid_item_any<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill,
-                           __ldg(desc + item), item, planes, smem4, rs0, rcum, red);
+  uint32_t d_next = blockIdx.x < total ? __ldg(desc + blockIdx.x) : 0u;
+  for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+    const uint32_t d_cur = d_next;  // the next item's descriptor is loaded meanwhile
+    if (item + gridDim.x < total) d_next = __ldg(desc + item + gridDim.x);
+    grid_item_any<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d_cur, item,
+                           planes, smem4, rs0, rcum, red);
+  }
 }
 
 // Several gridding jobs (facets x channel groups, each with its own plan,
@@ -857,8 +861,13 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
     return true;
   };
 
+  // each item's descriptor is loaded one item ahead, so that the halo copies
+  // can be issued as soon as the item starts
+  uint32_t d_next = blockIdx.x < total ? __ldg(desc + blockIdx.x) : 0u;
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
-    const int unit = (int)(__ldg(desc + item) & 0x7fffffffu);
+    const uint32_t d_cur = d_next;
+    if (item + gridDim.x < total) d_next = __ldg(desc + item + gridDim.x);
+    const int unit = (int)(d_cur & 0x7fffffffu);
     const int tile = unit % n_tiles, group = unit / n_tiles;
     const int tu = tile % p.ntu, tv = tile / p.ntu;
     const int q0 = p_begin + group * G;

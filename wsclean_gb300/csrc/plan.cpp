@@ -329,6 +329,10 @@ DevPlan to_dev_plan(const wgpu_plan_t &p) {
   d.nm1_center = p.nm1_center;
   d.w0f = (float)d.w0;
   d.inv_dwf = (float)d.inv_dw;
+  d.w0l = (float)(d.w0 - (double)d.w0f);
+  d.inv_dwl = (float)(d.inv_dw - (double)d.inv_dwf);
+  d.nm1_center_f = (float)d.nm1_center;
+  d.nm1_center_l = (float)(d.nm1_center - (double)d.nm1_center_f);
   return d;
 }
 
