@@ -557,6 +557,13 @@ def run_gpu(args, rank, world, local):
     req_bytes = (survey_request_bytes(plan_inv, d["n_gridded"], n_rows) +
                  survey_request_bytes(plan_pred, d["n_gridded"], n_rows))
     result["config"]["request_bytes_roofline_frac"] = (req_bytes / (ms_per_step * 1e-3) / 1e9) / peak
+    # the plan-independent ratio: only the visibility term, both directions
+    vis_bytes = 2.0 * (8.0 * d["n_gridded"] + 24.0 * n_rows)
+    result["config"]["visibility_bytes_roofline_frac"] = (
+        (vis_bytes / (ms_per_step * 1e-3) / 1e9) / peak)
+    result["config"]["request_bytes_plan"] = {
+        "sigma": plan_inv.sigma, "support": plan_inv.support, "n_w": plan_inv.n_planes,
+        "nu": plan_inv.nu, "nv": plan_inv.nv}
     # `value` counts every sample handed to the step, as the reference's calls
     # receive them; the samples beyond the image's Nyquist limit are zero and
     # neither gridded nor predicted, so the rate of processed samples is lower
@@ -596,7 +603,8 @@ def run_gpu(args, rank, world, local):
 def run_fullpol(args):
     """Corrected inversion (full-Jones gains applied on the device, collapsed to
     Stokes I) followed by prediction of the model image, through the host API;
-    accuracy against the oracle's gain application and FP64 DFT on a sample."""
+    accuracy over every sample against the oracle's gain application and the
+    FP64 direct transform on the GPU."""
     import torch
     import oracle
     from wsclean_gb300 import synthetic
@@ -650,28 +658,19 @@ def run_fullpol(args):
     ms = max(start.elapsed_time(end), wall * 1e3) / args.steps
     n_vis = n_rows * n_chan
     plan = g.last_plan()
-    # accuracy on a seeded row sample, with the full-data plan pinned
+    # accuracy over every sample: the oracle's gain application and collapse of
+    # all rows, then the FP64 direct transform on the GPU (the checker, outside
+    # the timed region) at 4096 seeded pixels for the inversion and at every
+    # sample for the prediction of the model image
     rng = np.random.default_rng(7)
-    rows = np.sort(rng.choice(n_rows, 300, replace=False))
-    corrected = oracle.apply_gains(4, 4, vis4[rows], ant[rows], tof[rows], sol, 4, n_ant)
-    gs = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=eps)
-    gs.pin_plan(plan)
-    gs.InitializeInversion()
-    gs.AddInversionDataWithCorrectionCallback("full", 4, rows.size, d["uvw"][rows], freq, n_chan,
-                                              ant[rows], vis4[rows], tof[rows], sol, 4, n_t,
-                                              n_ant)
-    img = gs.RealImage().astype(np.float64)
+    corrected = oracle.apply_gains(4, 4, vis4, ant, tof, sol, 4, n_ant)
+    img = out["img"].astype(np.float64)
     pix = rng.choice(W * W, 4096, replace=False)
-    ref = oracle.dft_invert(d["uvw"][rows], freq, corrected, W, W, dl, dl, pixels=pix,
-                            n_threads=os.cpu_count())
+    ref = oracle.cuda_dft_invert(d["uvw"], freq, corrected, W, W, dl, dl, pixels=pix)
     inv_err = float(np.linalg.norm(img[pix] - ref) / np.linalg.norm(ref))
-    gs.InitializePrediction(model)
-    pv = gs.PredictVisibilities(rows.size, n_chan, d["uvw"][rows], freq)
-    sel = rng.choice(pv.size, 4096, replace=False)
-    pr = oracle.dft_predict(d["uvw"][rows], freq, model, W, W, dl, dl, vis_index=sel,
-                            n_threads=os.cpu_count())
-    pred_err = float(np.linalg.norm(pv[sel] - pr) / np.linalg.norm(pr))
-    gs.close()
+    _, e2, r2 = oracle.cuda_dft_predict(d["uvw"], freq, model, W, W, dl, dl,
+                                        pred=np.ascontiguousarray(out["pv"]).ravel())
+    pred_err = float(math.sqrt(e2 / r2))
     g.close()
     value = n_vis / (ms * 1e-3) / 1e9
     h2d = uvw.nbytes * 2 + freq.nbytes * 2 + vis_p.nbytes + ant.nbytes + tof.nbytes + sol.nbytes + model.nbytes
@@ -692,8 +691,10 @@ def run_fullpol(args):
                    "plan": {k: getattr(plan, k) for k in ("nu", "support", "sigma", "n_planes",
                                                           "plane_batch", "est_error")},
                    "accuracy": {"invert_rel_l2": inv_err, "predict_rel_l2": pred_err,
-                                "sample": "300 rows x 32 channels: oracle gains + FP64 DFT on "
-                                          "4096 pixels (invert), 4096 vis (predict)"},
+                                "sample": (f"all {n_vis} samples: the oracle's gains and "
+                                           "collapse, then the FP64 direct transform on the GPU "
+                                           "at 4096 seeded pixels (inversion) and at every "
+                                           "sample (prediction)")},
                    "datagen_s": round(gen_s, 1)},
         "clocks": clk,
         "e2e": {"value": value, "unit": "Gvis/s", "h2d_bytes_per_step": int(h2d),
