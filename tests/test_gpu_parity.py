@@ -514,3 +514,33 @@ def test_row_length_6912_inversion_and_prediction(wgpu_lib, oracle_lib):
     pr = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl)
     assert rel(pv.ravel(), pr) <= eps
     g.close()
+
+
+@pytest.mark.parametrize("n_chan,order", [(24, "ascending"), (24, "descending"), (24, "shuffled"),
+                                          (8, "ascending"), (64, "ascending")])
+def test_device_w_extent_gives_the_host_plan(wgpu_lib, n_chan, order):
+    """The w range a call plans from (the device extent pass over the selected
+    samples) equals the host's FP64 extent exactly, so the call's plan is the
+    host plan bit for bit, for inversions (zero visibilities skipped) and
+    masked predictions, with ascending, descending and unordered channels."""
+    W, dl = 192, 3e-4
+    uvw, freq, vis = synthetic.random_points(900, n_chan, W, dl, seed=71, w_scale=3.0,
+                                             frac_zero=0.3)
+    if order == "descending":
+        freq = freq[::-1].copy()
+    elif order == "shuffled":
+        freq = np.random.default_rng(5).permutation(freq)
+    vis[:40] = 0  # whole rows without a sample
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=1e-4)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    got = g.last_plan()
+    ref = _plan_for(uvw, freq, vis, W, dl, 1e-4)
+    assert (got.w0, got.dw, got.n_planes) == (ref.w0, ref.dw, ref.n_planes)
+    mask = (vis != 0).astype(np.uint8)
+    model = np.zeros(W * W, np.float32)
+    model[W * W // 2 + 7] = 1.0
+    g.InitializePrediction(model)
+    g.PredictVisibilitiesMasked(uvw.shape[0], freq.size, uvw, freq, mask)
+    got = g.last_plan()
+    assert (got.w0, got.dw, got.n_planes) == (ref.w0, ref.dw, ref.n_planes)

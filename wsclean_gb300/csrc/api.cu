@@ -208,6 +208,16 @@ bool host_is_pinned(const void *p) {
   return a.type == cudaMemoryTypeHost;
 }
 
+// WGPU_DEBUG_COPIES=1 reports every host copy (direction, bytes, path) on
+// stderr, to tell which caller buffers the driver sees as page-locked.
+bool debug_copies() {
+  static const bool on = [] {
+    const char *e = std::getenv("WGPU_DEBUG_COPIES");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
 void ensure_staging(wgpu_gridder *g) {
   for (int k = 0; k < 2; ++k) {
     if (!g->stage_buf[k])
@@ -221,6 +231,9 @@ void ensure_staging(wgpu_gridder *g) {
 // been read (the device copy may still be running).
 void copy_to_device(wgpu_gridder *g, void *d, const void *h, size_t bytes) {
   if (bytes == 0) return;
+  if (debug_copies())
+    std::fprintf(stderr, "wgpu copy h2d %zu bytes %s\n", bytes,
+                 host_is_pinned(h) ? "page-locked" : "pageable");
   if (bytes <= kDirectCopyMax || host_is_pinned(h)) {
     WGPU_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream));
     return;
@@ -241,6 +254,9 @@ void copy_to_device(wgpu_gridder *g, void *d, const void *h, size_t bytes) {
 // the caller's memory holds the data.
 void copy_to_host(wgpu_gridder *g, void *h, const void *d, size_t bytes) {
   if (bytes == 0) return;
+  if (debug_copies())
+    std::fprintf(stderr, "wgpu copy d2h %zu bytes %s\n", bytes,
+                 host_is_pinned(h) ? "page-locked" : "pageable");
   if (bytes <= kDirectCopyMax || host_is_pinned(h)) {
     WGPU_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g->stream));
     WGPU_CUDA(cudaStreamSynchronize(g->stream));

@@ -821,7 +821,7 @@ void compute_w_extent(const double *d_uvw, const double *d_freq,
   unsigned long long *d = (unsigned long long *)scratch8;
   WGPU_CUDA(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, s));
   const int64_t n = n_rows * n_chan;
-  unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), 152 * 8);
+  unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), (int64_t)sm_count() * 8);
   const Selector sel{skip_zero ? (const float2 *)d_vis : nullptr, d_mask};
   if (n_chan <= 4096) {
     w_extent_kernel<true><<<blocks, kThreads, sizeof(double) * n_chan, s>>>(d_uvw, d_freq, sel,
