@@ -759,6 +759,7 @@ def run_facets_full(args):
     fb = FacetBatch(facets, [0, 2], epsilon=eps)
 
     phase_s = {"bind": 0.0, "invert": 0.0}
+    bind_phases = [0.0] * 4  # upload and planning, bucketing, waves, graph capture
 
     def step():
         for gi in range(n_groups):
@@ -767,6 +768,8 @@ def run_facets_full(args):
             fb.bind(d["uvw"], freq[c0:c0 + 2])
             torch.cuda.synchronize()
             t1 = time.perf_counter()
+            for k, v in enumerate(fb.info()["bind_ms"]):
+                bind_phases[k] += v
             fb.invert_device(d_vis_g[gi].data_ptr(), outs[gi].data_ptr())
             torch.cuda.synchronize()
             phase_s["bind"] += t1 - t0
@@ -782,6 +785,7 @@ def run_facets_full(args):
     l0 = _lib_launches()
     torch.cuda.synchronize()
     phase_s.update(bind=0.0, invert=0.0)
+    bind_phases[:] = [0.0] * 4
     w0 = time.perf_counter()
     for _ in range(args.steps):
         step()
@@ -790,6 +794,10 @@ def run_facets_full(args):
     launches = _lib_launches() - l0
     fb.close()
     per_group_ms = {k: round(v * 1e3 / (args.steps * n_groups), 1) for k, v in phase_s.items()}
+    per_group_ms["bind_phases"] = {
+        name: round(v / (args.steps * n_groups), 1)
+        for name, v in zip(("upload_extents_planning", "bucketing_and_job_tables", "waves",
+                            "graph_capture_instantiate"), bind_phases)}
     job_vis = float(n_rows) * 16 * len(facets)
     # the same jobs one at a time through the plain per-call path
     d_uvw = torch.as_tensor(d["uvw"], device=dev)

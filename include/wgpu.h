@@ -511,6 +511,9 @@ typedef struct wgpu_facets_info {
   uint64_t n_jobs, n_waves, support, graph_kernels, image_elems;
   double job_visibilities; /* samples gridded over all jobs per inversion */
   double last_ms;          /* device time of the last inversion, incl. copies */
+  double bind_ms[4];       /* host time of the last bind: upload, w extents and
+                              planning; bucketing and per-job tables; waves;
+                              graph capture and instantiation */
 } wgpu_facets_info_t;
 
 typedef struct wgpu_facets wgpu_facets_t;

@@ -93,7 +93,8 @@ class Facet(C.Structure):
 class FacetsInfo(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("n_jobs", "n_waves", "support", "graph_kernels",
                                            "image_elems")] + \
-               [("job_visibilities", C.c_double), ("last_ms", C.c_double)]
+               [("job_visibilities", C.c_double), ("last_ms", C.c_double),
+                ("bind_ms", C.c_double * 4)]
 
 
 class RowWeighting(C.Structure):

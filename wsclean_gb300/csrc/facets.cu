@@ -18,6 +18,7 @@
 // pairs' FFT chains spread over four streams, joined before the next wave);
 // per job the grid correction finishes the image.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -79,6 +80,13 @@ struct Slot {
 
 using namespace wgpu;
 
+namespace {
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t).count();
+}
+}  // namespace
+
 struct wgpu_facets {
   std::vector<wgpu_facet_t> facets;
   std::vector<size_t> groups;  // channel boundaries, n_groups + 1
@@ -115,6 +123,9 @@ struct wgpu_facets {
   unsigned *d_flags = nullptr, *h_flags = nullptr;
   bool bound = false;
   double last_ms = 0;
+  // host time of the last bind's phases: upload, extents and planning;
+  // bucketing and per-job tables; waves; graph capture and instantiation
+  double bind_ms[4] = {};
 
   // Device memory of the bound state: regions bumped out of chunks that
   // outlive a bind, so that re-binding the batch (the next channel group, the
@@ -220,6 +231,7 @@ wgpu_plan_request_t job_request(const wgpu_facets &f, const Job &j, int64_t forc
 void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw,
                  const double *freq) {
   f->release();
+  auto t_bind = Clock::now();
   cudaStream_t s = f->stream;
   if (n_rows == 0 || n_chan == 0) throw Error(WGPU_ERR_INVALID, "empty visibility set");
   if (f->groups.back() > n_chan) throw Error(WGPU_ERR_INVALID, "channel group beyond n_chan");
@@ -292,6 +304,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     j.rstride = (int)((j.plan.width + 31) / 32 * 32);
   }
 
+  f->bind_ms[0] = ms_since(t_bind);
+  t_bind = Clock::now();
   // per job: bucketing into owned buffers, tables, work items
   f->image_elems = 0;
   for (Job &j : f->jobs) f->image_elems += j.facet.width * j.facet.height;
@@ -340,6 +354,9 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     fft_prepare_rows(*f->fft, (int)j.plan.nu);
   }
 
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  f->bind_ms[1] = ms_since(t_bind);
+  t_bind = Clock::now();
   // waves of (job, plane batch) pairs within the plane budget
   std::vector<Slot> pending;
   for (int ji = 0; ji < (int)f->jobs.size(); ++ji) {
@@ -419,6 +436,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     totals.push_back(total);
   }
 
+  f->bind_ms[2] = ms_since(t_bind);
+  t_bind = Clock::now();
   // one graph for the whole inversion
   prepare_grid_items_multi(f->support);
   const uint64_t k0 = thread_launch_count();
@@ -482,6 +501,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   WGPU_CUDA(cudaGraphInstantiate(&f->exec, f->graph, 0));
   f->graph_kernels = thread_launch_count() - k0;
   count_launch(-(int)f->graph_kernels);  // captured, not run
+  f->bind_ms[3] = ms_since(t_bind);
   f->bound = true;
 }
 
@@ -687,6 +707,7 @@ int wgpu_facets_info(const wgpu_facets_t *f, wgpu_facets_info_t *info) {
   for (const Job &j : f->jobs) vis += (double)j.n_out;
   info->job_visibilities = vis;
   info->last_ms = f->last_ms;
+  for (int k = 0; k < 4; ++k) info->bind_ms[k] = f->bind_ms[k];
   return WGPU_OK;
 }
 

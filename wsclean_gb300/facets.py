@@ -54,7 +54,9 @@ class FacetBatch:
     def info(self):
         i = _lib.FacetsInfo()
         check(lib().wgpu_facets_info(self._h, C.byref(i)))
-        return {k: getattr(i, k) for k, _ in i._fields_}
+        out = {k: getattr(i, k) for k, _ in i._fields_}
+        out["bind_ms"] = list(i.bind_ms)
+        return out
 
     def job_plan(self, job):
         p = _lib.Plan()
