@@ -152,6 +152,10 @@ __host__ __device__ constexpr int halo_plane(int T, int W) {
 __host__ __device__ constexpr int spill_cells(int T, int W) {
   return (W - 1) * halo_rows(T, W) + (W - 1) * T;
 }
+// A unit's spill slot: its G planes' border cells, then one cell whose first
+// word is the mask of the planes the slot holds (bit q: plane q of the group
+// was written; the fix-up reads no other plane).
+__host__ __device__ constexpr int slot_cells(int G, int B) { return G * B + 1; }
 __host__ __device__ __forceinline__ int border_index(int T, int W, int r, int c) {
   return c >= T ? r * (W - 1) + (c - T) : (W - 1) * halo_rows(T, W) + (r - T) * T + c;
 }
@@ -359,7 +363,15 @@ __device__ __forceinline__ void grid_item(const DevPlan &p, const VisRecord *__r
   // flush: the tile's cells to the planes (a split unit adds into cells
   // zeroed beforehand), the border cells to the unit's spill slot
   const int slot = __ldg(slots + unit);
-  float2 *sp = spill + (size_t)slot * G * B;
+  float2 *sp = spill + (size_t)slot * slot_cells(G, B);
+  if (threadIdx.x == 0) {
+    unsigned *mask = reinterpret_cast<unsigned *>(sp + G * B);
+    const unsigned all = (1u << nq) - 1u;
+    if (n_items == 1)
+      *mask = all;
+    else
+      atomicOr(mask, all);
+  }
   for (int c = threadIdx.x; c < nq * R * R; c += kThreads) {
     const int pq = c / (R * R), rem = c - pq * (R * R);
     const int rr = rem / R, cc = rem - rr * R;
@@ -453,7 +465,7 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
                                                float2 *__restrict__ spill, uint32_t d,
                                                uint32_t item, float2 *__restrict__ planes,
                                                int2 *cells, RunStage *stage, uint32_t *rs0,
-                                               uint32_t *rcum, float *red) {
+                                               uint32_t *rcum, float *red, int *prange) {
   static_assert(W <= 8, "runs gridding holds an 8 x 8 x 8 footprint");
   static_assert(kThreads == T * T, "one thread per tile cell in the write-out");
   constexpr int R = halo_rows(T, W);
@@ -498,17 +510,30 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
   const uint32_t hi = min(lo + kItemVis, rcum[4]);
   // fixed-point scale of the halo: 2^30 over the item's summed magnitudes
   // (with a margin for the float sum and kernel values rounded above one)
+  // and the range of the group's planes the item's footprints touch (first
+  // planes ip_lo..ip_hi, footprints W planes deep)
+  int ip_lo = 0x7fffffff, ip_hi = -0x7fffffff;
   {
     float part = 0.f;
     for (uint32_t pos = lo + threadIdx.x; pos < hi; pos += kThreads) {
       int r = 0;
       while (pos >= rcum[r + 1]) ++r;
-      const float2 v = __ldg(reinterpret_cast<const float2 *>(rec + rs0[r] + (pos - rcum[r])));
+      const VisRecord *vr = rec + rs0[r] + (pos - rcum[r]);
+      const float2 v = __ldg(reinterpret_cast<const float2 *>(vr));
+      const int ip = __ldg(&vr->ip);
       part += fabsf(v.x) + fabsf(v.y);
+      ip_lo = min(ip_lo, ip);
+      ip_hi = max(ip_hi, ip);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if (lane == 0) red[warp] = part;
+    ip_lo = __reduce_min_sync(0xffffffffu, ip_lo);
+    ip_hi = __reduce_max_sync(0xffffffffu, ip_hi);
+    if (lane == 0) {
+      red[warp] = part;
+      atomicMin(&prange[0], ip_lo);
+      atomicMax(&prange[1], ip_hi);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       float sum = 0.f;
@@ -518,6 +543,8 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
     __syncthreads();
   }
   const float scale = red[kRunWarps];
+  // planes [z_lo, z_hi) of the group hold this item's footprints
+  const int z_lo = max(prange[0] - q0, 0), z_hi = min(prange[1] - q0 + W, nq);
   // this warp's contiguous chunk of the item's reads
   const uint32_t per = (hi - lo + kRunWarps - 1) / kRunWarps;
   const uint32_t c0 = min(lo + (uint32_t)warp * per, hi);
@@ -606,9 +633,28 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
   const float inv = 1.0f / scale;
   const bool add = n_items > 1;
   const int slot = __ldg(slots + unit);
-  float2 *sp = spill + (size_t)slot * G * B;
+  float2 *sp = spill + (size_t)slot * slot_cells(G, B);
   const int tr = threadIdx.x / T, tc = threadIdx.x % T;
+  if (threadIdx.x == 0) {
+    unsigned *mask = reinterpret_cast<unsigned *>(sp + G * B);
+    const unsigned bits = z_hi > z_lo ? ((1u << z_hi) - 1u) & ~((1u << z_lo) - 1u) : 0u;
+    if (add)
+      atomicOr(mask, bits);
+    else
+      *mask = bits;
+    prange[0] = 0x7fffffff;  // for the block's next item (read before the barrier above)
+    prange[1] = -0x7fffffff;
+  }
   for (int pq = 0; pq < nq; ++pq) {
+    if (pq < z_lo || pq >= z_hi) {
+      // a plane the item does not touch: its halo cells are zero; the unit's
+      // own cells get zeros unless a split unit's were zeroed beforehand, and
+      // its spill is not written (the mask leaves it out)
+      if (!add)
+        planes[(size_t)(q0 + pq - p_begin) * plane_elems + (size_t)(tv * T + tr) * p.nu +
+               tu * T + tc] = make_float2(0.f, 0.f);
+      continue;
+    }
     int2 *cp = cells + pq * PS;
     {
       int2 *src = cp + tr * R + tc;
@@ -664,12 +710,12 @@ __device__ __forceinline__ void grid_item_any(const DevPlan &p, const VisRecord 
                                               float2 *__restrict__ spill, uint32_t d,
                                               uint32_t item, float2 *__restrict__ planes,
                                               float4 *smem4, uint32_t *rs0, uint32_t *rcum,
-                                              float *red) {
+                                              float *red, int *prange) {
   if constexpr (W <= 8) {
     int2 *cells = reinterpret_cast<int2 *>(smem4);
     RunStage *stage = reinterpret_cast<RunStage *>(cells + G * halo_plane(T, W));
     grid_item_runs<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item,
-                            planes, cells, stage, rs0, rcum, red);
+                            planes, cells, stage, rs0, rcum, red, prange);
   } else {
     const GridSmem sm = grid_smem<T, G, W>(smem4, rs0, rcum);
     grid_item<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d, item, planes,
@@ -690,16 +736,21 @@ __global__ void __launch_bounds__(kThreads, 2)
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
   __shared__ float red[kRunWarps + 1];
+  __shared__ int prange[2];  // first planes of the current item's reads
   float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
     cells[c] = make_float2(0.f, 0.f);
+  if (threadIdx.x == 0) {
+    prange[0] = 0x7fffffff;
+    prange[1] = -0x7fffffff;
+  }
   __syncthreads();
   uint32_t d_next = blockIdx.x < total ? __ldg(desc + blockIdx.x) : 0u;
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     const uint32_t d_cur = d_next;  // the next item's descriptor is loaded meanwhile
     if (item + gridDim.x < total) d_next = __ldg(desc + item + gridDim.x);
     grid_item_any<T, G, W>(p, rec, off, p_begin, n_batch, item_off, slots, spill, d_cur, item,
-                           planes, smem4, rs0, rcum, red);
+                           planes, smem4, rs0, rcum, red, prange);
   }
 }
 
@@ -716,10 +767,15 @@ __global__ void __launch_bounds__(kThreads, 2)
   extern __shared__ float4 smem4[];
   __shared__ uint32_t rs0[4], rcum[5];
   __shared__ float red[kRunWarps + 1];
+  __shared__ int prange[2];
   __shared__ GridJob job;
   float2 *cells = reinterpret_cast<float2 *>(smem4);
   for (int c = threadIdx.x; c < G * halo_plane(T, W); c += kThreads)
     cells[c] = make_float2(0.f, 0.f);
+  if (threadIdx.x == 0) {
+    prange[0] = 0x7fffffff;
+    prange[1] = -0x7fffffff;
+  }
   int cur = -1;
   for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
     int lo = 0, hi = n_jobs - 1;  // last job whose base is <= item
@@ -738,21 +794,27 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t local = item - __ldg(job_base + lo);
     grid_item_any<T, G, W>(job.p, job.rec, job.off, job.p_begin, job.n_batch, job.item_off,
                            job.slot, job.spill, __ldg(job.desc + local), local, job.planes, smem4,
-                           rs0, rcum, red);
+                           rs0, rcum, red, prange);
   }
 }
 
 // Fix-up after a gridding pass: every tile cell within W - 1 of the tile's
 // left or lower edge receives the border cells that its left, lower and
-// lower-left neighbours spilled (one block per unit, one thread per cell).
+// lower-left neighbours spilled (one block per unit, one thread per cell of a
+// plane).  Only the planes a neighbour's slot mask names are read; a plane
+// that no neighbour wrote is skipped.
 __global__ void __launch_bounds__(kThreads)
     spill_fixup_kernel(DevPlan p, int G, int p_begin, int n_batch, int n_units,
                        const int *__restrict__ slots, const float2 *__restrict__ spill,
                        float2 *__restrict__ planes) {
   constexpr int T = kTile;
+  static_assert(kThreads == T * T, "one thread per tile cell");
   const int W = p.support, B = (W - 1) * (T + W - 1) + (W - 1) * T;
+  const int SC = slot_cells(G, B);
   const int n_tiles = p.ntu * p.ntv;
   const size_t plane_elems = (size_t)p.nu * p.nv;
+  const int r = threadIdx.x / T, col = threadIdx.x % T;
+  const bool from_left = col < W - 1, from_low = r < W - 1;
   for (int unit = blockIdx.x; unit < n_units; unit += gridDim.x) {
     const int tile = unit % n_tiles, group = unit / n_tiles;
     const int tu = tile % p.ntu, tv = tile / p.ntu;
@@ -763,26 +825,28 @@ __global__ void __launch_bounds__(kThreads)
     const int s_left = __ldg(slots + base + tv * p.ntu + tl);
     const int s_low = __ldg(slots + base + tb * p.ntu + tu);
     const int s_diag = __ldg(slots + base + tb * p.ntu + tl);
-    if (s_left < 0 && s_low < 0 && s_diag < 0) continue;
-    for (int c = threadIdx.x; c < nq * T * T; c += blockDim.x) {
-      const int pq = c / (T * T), rem = c - pq * (T * T);
-      const int r = rem / T, col = rem - r * T;
-      const bool from_left = col < W - 1, from_low = r < W - 1;
-      if (!from_left && !from_low) continue;
+    auto mask_of = [&](int sl) -> unsigned {
+      return sl < 0 ? 0u : __float_as_uint(__ldg(&spill[(size_t)sl * SC + G * B].x));
+    };
+    const unsigned m_left = mask_of(s_left), m_low = mask_of(s_low), m_diag = mask_of(s_diag);
+    const unsigned m_any = m_left | m_low | m_diag;
+    if (m_any == 0u || (!from_left && !from_low)) continue;
+    for (int pq = 0; pq < nq; ++pq) {
+      if (!((m_any >> pq) & 1u)) continue;
       float2 add = make_float2(0.f, 0.f);
-      if (from_left && s_left >= 0) {
-        const float2 v = __ldg(spill + ((size_t)s_left * G + pq) * B + border_index(T, W, r, col + T));
+      if (from_left && ((m_left >> pq) & 1u)) {
+        const float2 v = __ldg(spill + (size_t)s_left * SC + pq * B + border_index(T, W, r, col + T));
         add.x += v.x;
         add.y += v.y;
       }
-      if (from_low && s_low >= 0) {
-        const float2 v = __ldg(spill + ((size_t)s_low * G + pq) * B + border_index(T, W, r + T, col));
+      if (from_low && ((m_low >> pq) & 1u)) {
+        const float2 v = __ldg(spill + (size_t)s_low * SC + pq * B + border_index(T, W, r + T, col));
         add.x += v.x;
         add.y += v.y;
       }
-      if (from_left && from_low && s_diag >= 0) {
+      if (from_left && from_low && ((m_diag >> pq) & 1u)) {
         const float2 v =
-            __ldg(spill + ((size_t)s_diag * G + pq) * B + border_index(T, W, r + T, col + T));
+            __ldg(spill + (size_t)s_diag * SC + pq * B + border_index(T, W, r + T, col + T));
         add.x += v.x;
         add.y += v.y;
       }
@@ -1091,8 +1155,9 @@ __global__ void __launch_bounds__(kThreads)
   const int slot = slots[unit];
   if (slot >= 0) {
     const int B = (p.support - 1) * (T + p.support - 1) + (p.support - 1) * T;
-    float2 *sp = spill + (size_t)slot * G * B;
+    float2 *sp = spill + (size_t)slot * slot_cells(G, B);
     for (int c = lane; c < (q1 - q0) * B; c += 32) sp[c] = make_float2(0.f, 0.f);
+    if (lane == 0) sp[G * B] = make_float2(0.f, 0.f);  // the plane mask
   }
 }
 
@@ -1142,7 +1207,7 @@ WorkItems plan_items(const DevPlan &p, const uint32_t *off, int p_begin, int n_b
     wi.slot = (int *)slots;
     wi.n_slots = (int)totals[1];
     const size_t B = (size_t)spill_cells(T, p.support);
-    wi.spill = (float2 *)alloc(3, sizeof(float2) * ((size_t)wi.n_slots * G * B + 1));
+    wi.spill = (float2 *)alloc(3, sizeof(float2) * ((size_t)wi.n_slots * slot_cells(G, (int)B) + 1));
   }
   return wi;
 }
@@ -1285,7 +1350,7 @@ void launch_zero_split_units(const DevPlan &p, const WorkItems &wi, int p_begin,
 
 size_t grid_spill_elems(const DevPlan &p, const WorkItems &wi) {
   const int G = p.support <= 8 ? grid_group(8) : grid_group(16);
-  return (size_t)wi.n_slots * G * spill_cells(kTile, p.support);
+  return (size_t)wi.n_slots * slot_cells(G, spill_cells(kTile, p.support));
 }
 
 void launch_spill_fixup(const DevPlan &p, const WorkItems &wi, int p_begin, int n_batch,
