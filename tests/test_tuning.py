@@ -142,3 +142,17 @@ def test_pinned_plan_is_not_tuned(wgpu_lib):
     g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
     assert g.last_tuning() == []
     assert g.last_plan().support == 6
+
+
+def test_fallback_plan_fits_the_row_transform(wgpu_lib):
+    """When no entry meets epsilon the plan is the most accurate one whose grid
+    the transforms take: at 8192 pixels sigma = 2 would need 16384-point rows,
+    above the 12288 the row transform holds, so the fallback keeps sigma <= 1.5
+    rather than failing."""
+    req = dict(width=8192, height=8192, dl=1.4544e-5, dm=1.4544e-5, epsilon=1e-7,
+               w_min=-9000.0, w_max=9000.0, n_vis=473_000_000)
+    p = _lib.make_plan(**req)
+    assert p.nu <= 12288 and p.nv <= 12288
+    assert p.est_error > 1e-7  # the best available, reported honestly
+    tighter = [c for c in _lib.plan_candidates(**dict(req, epsilon=1e-5))]
+    assert p.est_error <= min(c.est_error for c in tighter)

@@ -70,6 +70,12 @@ const GaussLegendre &gl() {
 constexpr double kCellRate = 6.3e11;
 constexpr double kByteRate = 1.4e12;
 
+// Supports above 8 use the gridding kernel without register runs (every
+// read adds its whole footprint into shared memory); measured on the 8192^2
+// wide-field workload its plans took 2.4 times as long as the W = 8 plan
+// (1379 and 1366 ms against 582 ms per bound inversion + prediction).
+constexpr double kWideSupportFactor = 2.4;
+
 // Relative FP32 round-off of the gridded planes per unit of correction
 // amplification; measured on GB300 as 2-3e-8 (random visibilities, 2D and 3D
 // plans), rounded up.
@@ -163,7 +169,8 @@ void check_request(const wgpu_plan_request_t &req) {
 
 // Every table entry within sigma_min..sigma_max (and the forced fields) whose
 // error estimate meets epsilon, as a plan without its plane batch, in table
-// order.  `fallback` receives the most accurate entry whatever its estimate.
+// order.  `fallback` receives the most accurate entry whose grid the row and
+// column transforms take, whatever its estimate.
 std::vector<wgpu_plan_t> feasible_plans(const wgpu_plan_request_t &req,
                                         const EsKernelEntry **fallback, double *fallback_err) {
   const double smin = req.sigma_min > 0 ? req.sigma_min : 1.1;
@@ -192,11 +199,6 @@ std::vector<wgpu_plan_t> feasible_plans(const wgpu_plan_request_t &req,
     const double alias = std::sqrt(ndim) * e.err_max;
     const double fp32 = kFp32Noise * std::pow(e.amp_rms, ndim);
     const double est = std::sqrt(alias * alias + fp32 * fp32);
-    if (est < *fallback_err) {
-      *fallback_err = est;
-      *fallback = &e;
-    }
-    if (est > req.epsilon) continue;
 
     wgpu_plan_t p;
     std::memset(&p, 0, sizeof(p));
@@ -217,6 +219,13 @@ std::vector<wgpu_plan_t> feasible_plans(const wgpu_plan_request_t &req,
     if (e.support > tile) continue;
     int64_t f1, f2;
     if (nu > fft_row_max_length() || !try_decompose(nv, &f1, &f2)) continue;
+    // the most accurate entry whose grid the transforms take: the plan used
+    // when no entry meets epsilon
+    if (est < *fallback_err) {
+      *fallback_err = est;
+      *fallback = &e;
+    }
+    if (est > req.epsilon) continue;
     p.tile = tile;
     p.nu = nu;
     p.nv = nv;
@@ -239,7 +248,8 @@ std::vector<wgpu_plan_t> feasible_plans(const wgpu_plan_request_t &req,
     p.est_error = est;
     const int64_t rstride = (req.width + 31) / 32 * 32;
     const double w_planes_per_vis = use_w ? (double)e.support : 1.0;
-    const double t_grid = 2.0 * n_vis * e.support * e.support * w_planes_per_vis / kCellRate;
+    const double t_grid = 2.0 * n_vis * e.support * e.support * w_planes_per_vis / kCellRate *
+                          (e.support > 8 ? kWideSupportFactor : 1.0);
     const double t_fft = 2.0 * (double)p.n_planes *
                          (16.0 * nu * nv + 40.0 * nv * rstride) / kByteRate;
     p.est_seconds = t_grid + t_fft;
