@@ -24,6 +24,7 @@ struct Case {
   double u, v, w;        // metres
   double su, sv, sw;     // per-channel scales (cells per metre, wavelengths per metre)
   double w0, inv_dw, c;  // plan
+  double ls, ms;         // l and m shift (0: no shift)
   int support, n_planes;
 };
 
@@ -54,6 +55,7 @@ Ref reference(const Case &k) {
     r.fw = 0.0f;
   }
   double t = wl * k.c;
+  if (k.ls != 0.0 || k.ms != 0.0) t = ((k.u * k.sw) * k.ls + (k.v * k.sw) * k.ms) + t;
   t -= std::rint(t);
   r.arg = (float)t;
   return r;
@@ -65,7 +67,9 @@ bool same(float a, float b) { return wgpu::ff::bits(a) == wgpu::ff::bits(b); }
 int check(const Case &k) {
   const Ref r = reference(k);
   wgpu::ff::Scales cs{split(k.su), split(k.sv), split(k.sw)};
-  wgpu::ff::PlanPairs pp{split(k.w0), split(k.inv_dw), split(k.c), k.n_planes > 1};
+  wgpu::ff::PlanPairs pp{split(k.w0),  split(k.inv_dw),  split(k.c),
+                         split(k.ls),  split(k.ms),      k.n_planes > 1,
+                         k.ls != 0.0 || k.ms != 0.0};
   float fu, fv, fw, arg;
   if (!wgpu::ff::decide(split(k.u), split(k.v), split(k.w), cs, pp, r.iu0, r.iv0, r.ip, &fu, &fv,
                         &fw, &arg))
@@ -97,6 +101,10 @@ Case random_case(std::mt19937_64 &g) {
   k.inv_dw = 1.0 / dw;
   k.n_planes = (int)std::ceil((w_max - w_min) / dw) + k.support;
   k.c = -0.016 - 0.002 * uni(g);
+  // half the samples belong to a shifted image (a facet centre within 3 deg)
+  const bool shifted = uni(g) < 0.5;
+  k.ls = shifted ? (2.0 * uni(g) - 1.0) * 0.05 : 0.0;
+  k.ms = shifted ? (2.0 * uni(g) - 1.0) * 0.05 : 0.0;
   return k;
 }
 
@@ -121,20 +129,16 @@ Case edge_case(std::mt19937_64 &g, int which) {
     const float f = (float)((double)iu0 - U);
     const double target = (double)iu0 - midpoint_above(f) + jitter * std::fabs(U);
     k.u = target / k.su;
-  } else if (which == 1) {
-    // the phase near a half-integer
-    const double wl = k.w * k.sw;
-    const double t = wl * k.c;
-    const double target = std::floor(t) + 0.5 + jitter * std::fabs(t);
-    k.w = target / k.c / k.sw;
-  } else if (which == 2) {
-    // the phase argument near a float midpoint
-    const double wl = k.w * k.sw;
-    double t = wl * k.c;
+  } else if (which == 1 || which == 2) {
+    // the phase near a half-integer (1) or its argument near a float
+    // midpoint (2): w chosen so that the full phase lands there
+    const double tuv = (k.ls != 0.0 || k.ms != 0.0) ? (k.u * k.sw) * k.ls + (k.v * k.sw) * k.ms
+                                                     : 0.0;
+    const double t = tuv + (k.w * k.sw) * k.c;
     const double n = std::rint(t);
-    const float a = (float)(t - n);
-    const double target = n + midpoint_above(a) + jitter * std::fabs(t);
-    k.w = target / k.c / k.sw;
+    const double target = which == 1 ? std::floor(t) + 0.5 + jitter * std::fabs(t)
+                                     : n + midpoint_above((float)(t - n)) + jitter * std::fabs(t);
+    k.w = (target - tuv) / k.c / k.sw;
   } else {
     // fw near a float midpoint
     const double wl = k.w * k.sw;

@@ -4,9 +4,10 @@ The bucketing writes each record's footprint fractions and phase argument
 from float-float arithmetic where an error bound proves them equal to the FP64
 chains (bit for bit), and in FP64 otherwise.  This test compiles the same
 header for the host and checks the decision against the FP64 chains on random
-wide-field samples and on samples placed next to float rounding boundaries and
-half-integer phases: a decided value must never differ from FP64, and random
-samples must almost all be decided.  The GPU side is checked bit for bit
+wide-field samples (half of them in images with an l/m shift) and on samples
+placed next to float rounding boundaries and half-integer phases: a decided
+value must never differ from FP64, and random samples must almost all be
+decided.  The GPU side is checked bit for bit
 against the oracle by the bucketing parity tests.
 """
 import os
@@ -27,6 +28,8 @@ def test_float_float_records_match_fp64(tmp_path):
     got = dict((k, (int(n), int(d), int(m))) for k, n, d, m in
                re.findall(r"(\w+) (\d+) decided (\d+) mismatches (\d+)", r.stdout))
     n, decided, bad = got["random"]
-    assert bad == 0 and decided >= 0.97 * n
+    # half the random samples belong to shifted images, whose phase sums terms
+    # of thousands of turns: their bound is wider and about 8% fall back
+    assert bad == 0 and decided >= 0.93 * n
     n, decided, bad = got["edge"]
     assert bad == 0 and 0 < decided < n  # near boundaries some fall back, some are decided

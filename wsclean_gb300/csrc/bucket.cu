@@ -588,12 +588,13 @@ __device__ __forceinline__ void record_fp64(const DevPlan &p, const double *uvw,
   // shift phase theta = u l_shift + v m_shift + w c_n (turns), FP64 argument,
   // reduced to [-1/2, 1/2] before the FP32 sincos.  Without shifts the first
   // two terms are zero and theta = fl(w f / c) c_n, the same value.
-  double t;
+  // (every step rounded as written: the float-float pass reproduces this chain)
+  double t = __dmul_rn(wl, p.nm1_center);
   if (SHIFT) {
     const double fl = sc.sw;
-    t = row[0] * fl * p.l_shift + row[1] * fl * p.m_shift + row[2] * fl * p.nm1_center;
-  } else {
-    t = __dmul_rn(wl, p.nm1_center);
+    const double tuv = __dadd_rn(__dmul_rn(__dmul_rn(row[0], fl), p.l_shift),
+                                 __dmul_rn(__dmul_rn(row[1], fl), p.m_shift));
+    t = __dadd_rn(tuv, t);
   }
   t -= rint(t);
   float sn, cn;
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(kThreads)
   record_fp64<SHIFT>(p, uvw, cs, vis, n_chan, perm[s], s, rec, uvwf);
 }
 
-// Records of a plan without shifts from float-float arithmetic (record_ff.cuh):
+// Records from float-float arithmetic (record_ff.cuh):
 // the corners decided in FP32 as key_kernel decides them, the fractions and
 // the phase argument where the error bound proves them equal to the FP64
 // chains.  Each block takes kRecordBlock consecutive records and lists the
@@ -620,6 +621,7 @@ __global__ void __launch_bounds__(kThreads)
 // in FP64.
 constexpr int kRecordBlock = 4 * kThreads;
 
+template <bool SHIFT>
 __global__ void __launch_bounds__(kThreads)
     record_ff_kernel(DevPlan p, const ChannelScale *__restrict__ cs, const float2 *vis,
                      int64_t n_chan, const uint32_t *__restrict__ perm, int64_t n_out,
@@ -631,7 +633,9 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const int64_t b0 = (int64_t)blockIdx.x * kRecordBlock;
   const ff::PlanPairs pp{ff::Pair{p.w0f, p.w0l}, ff::Pair{p.inv_dwf, p.inv_dwl},
-                         ff::Pair{p.nm1_center_f, p.nm1_center_l}, p.n_planes > 1};
+                         ff::Pair{p.nm1_center_f, p.nm1_center_l},
+                         ff::Pair{p.l_shift_f, p.l_shift_l}, ff::Pair{p.m_shift_f, p.m_shift_l},
+                         p.n_planes > 1, SHIFT};
   for (int k = 0; k < kRecordBlock / kThreads; ++k) {
     const int64_t s = b0 + k * kThreads + threadIdx.x;
     if (s >= n_out) break;
@@ -661,6 +665,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // The records record_ff_kernel left undecided, in FP64: one warp per record
 // block's slice, so that the FP64 chains run with the warp's lanes full.
+template <bool SHIFT>
 __global__ void __launch_bounds__(kThreads)
     record_fix_kernel(DevPlan p, const double *uvw, const ChannelScale *cs, const float2 *vis,
                       int64_t n_chan, const uint32_t *__restrict__ perm, int64_t n_blocks,
@@ -673,7 +678,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t cnt = counts[b];
     for (uint32_t i = lane; i < cnt; i += 32) {
       const uint32_t s = pending[b * kRecordBlock + i];
-      record_fp64<false>(p, uvw, cs, vis, n_chan, perm[s], s, rec, uvwf);
+      record_fp64<SHIFT>(p, uvw, cs, vis, n_chan, perm[s], s, rec, uvwf);
     }
   }
 }
@@ -916,21 +921,17 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   if (res.n_out > 0) {
     const bool shift = p.l_shift != 0.0 || p.m_shift != 0.0;
     const float2 *vis = skip_zero ? (const float2 *)d_vis : nullptr;
-    if (shift) {
-      record_kernel<true><<<grid_for(res.n_out, kThreads), kThreads, 0, s>>>(
-          p, d_uvw, cs, vis, n_chan, res.perm, res.n_out, res.records, uvwf);
-      check_launch("record_kernel");
-    } else {
-      // undecided records listed in kout (free after the sort), counts per
-      // record block in vout
-      const int64_t n_blocks = (res.n_out + kRecordBlock - 1) / kRecordBlock;
-      record_ff_kernel<<<(unsigned)n_blocks, kThreads, 0, s>>>(
-          p, cs, vis, n_chan, res.perm, res.n_out, res.records, uvwf, uvwl, kout, vout);
-      check_launch("record_ff_kernel");
-      record_fix_kernel<<<sm_count() * 8, kThreads, 0, s>>>(
-          p, d_uvw, cs, vis, n_chan, res.perm, n_blocks, res.records, uvwf, kout, vout);
-      check_launch("record_fix_kernel");
-    }
+    // undecided records listed in kout (free after the sort), counts per
+    // record block in vout
+    const int64_t n_blocks = (res.n_out + kRecordBlock - 1) / kRecordBlock;
+    (shift ? record_ff_kernel<true> : record_ff_kernel<false>)<<<(unsigned)n_blocks, kThreads,
+                                                                  0, s>>>(
+        p, cs, vis, n_chan, res.perm, res.n_out, res.records, uvwf, uvwl, kout, vout);
+    check_launch("record_ff_kernel");
+    (shift ? record_fix_kernel<true> : record_fix_kernel<false>)<<<sm_count() * 8, kThreads, 0,
+                                                                    s>>>(
+        p, d_uvw, cs, vis, n_chan, res.perm, n_blocks, res.records, uvwf, kout, vout);
+    check_launch("record_fix_kernel");
   }
   return res;
 }

@@ -343,6 +343,10 @@ DevPlan to_dev_plan(const wgpu_plan_t &p) {
   d.inv_dwl = (float)(d.inv_dw - (double)d.inv_dwf);
   d.nm1_center_f = (float)d.nm1_center;
   d.nm1_center_l = (float)(d.nm1_center - (double)d.nm1_center_f);
+  d.l_shift_f = (float)d.l_shift;
+  d.l_shift_l = (float)(d.l_shift - (double)d.l_shift_f);
+  d.m_shift_f = (float)d.m_shift;
+  d.m_shift_l = (float)(d.m_shift - (double)d.m_shift_f);
   return d;
 }
 

@@ -3,8 +3,9 @@
 //
 // The records' fractions are FP64 values rounded to float: fu = fl32(iu0 -
 // fl64(u * su)), fv likewise, fw = fl32(ip - fl64(fl64(fl64(w * sw) - w0) *
-// inv_dw)), and the phase argument of a plan without shifts is
-// fl32(t - rint(t)) with t = fl64(fl64(w * sw) * c).  Here the same chains run
+// inv_dw)), and the phase argument is fl32(t - rint(t)) with
+// t = fl64(fl64(w * sw) * c) without shifts, and the same term added to
+// fl64(fl64(fl64(u * sw) * l_shift) + fl64(fl64(v * sw) * m_shift)) with them.  Here the same chains run
 // on (hi, lo) float pairs (every double split into its nearest float and the
 // nearest float to the rest), which carry about 46 significant bits, and each
 // result comes with a bound on its distance to the FP64 chain's value.  When
@@ -105,6 +106,14 @@ WGPU_FF_HD Pair mul(Pair a, Pair b) {
   return Pair{s, fsub(c, fsub(s, p))};
 }
 
+// a + b within 2^-47 (|a| + |b|) of the exact sum of the pairs' values
+// (renormalised with a full two-sum: the high parts may cancel).
+WGPU_FF_HD Pair add(Pair a, Pair b) {
+  const Pair d = two_sum(a.hi, b.hi);
+  const float c = fadd(d.lo, fadd(a.lo, b.lo));
+  return two_sum(d.hi, c);
+}
+
 // a - b within 2^-47 (|a| + |b|) of the exact difference of the pairs' values
 // (renormalised with a full two-sum: the high parts may cancel).
 WGPU_FF_HD Pair sub(Pair a, Pair b) {
@@ -145,7 +154,9 @@ struct Scales {
 };
 struct PlanPairs {
   Pair w0, inv_dw, c;  // w0, 1 / dw, c_n (the n - 1 centre)
+  Pair l, m;           // l_shift, m_shift
   bool w_planes;       // n_planes > 1
+  bool shift;          // the phase has the l and m terms
 };
 
 // 2^-43: the bound factor of every chain below.  A float-float product is
@@ -178,10 +189,24 @@ WGPU_FF_HD bool decide(Pair u, Pair v, Pair w, const Scales &cs, const PlanPairs
   } else {
     *fw = 0.0f;
   }
-  // phase: t = fl64(wl c), reduced by its nearest integer
-  const Pair t = mul(wl, pp.c);
+  // phase: t = fl64(wl c) without shifts; with them
+  // t = fl64(fl64(fl64(fl64(u f) l) + fl64(fl64(v f) m)) + fl64(wl c)), f the
+  // channel's w scale (the chain the FP64 record pass rounds step by step);
+  // then reduced by its nearest integer
+  Pair t = mul(wl, pp.c);
+  float tb = fmul(kBound, fabsf(t.hi));
+  if (pp.shift) {
+    const Pair tu = mul(mul(u, cs.sw), pp.l), tv = mul(mul(v, cs.sw), pp.m);
+    const Pair t12 = add(tu, tv);
+    const Pair t3 = t;
+    t = add(t12, t3);
+    // each term's product chain, the two sums and their FP64 roundings,
+    // relative to the magnitudes involved
+    tb = fmul(kBound, fadd(fadd(fadd(fabsf(tu.hi), fabsf(tv.hi)), fadd(fabsf(t3.hi),
+                                                                      fabsf(t12.hi))),
+                           fabsf(t.hi)));
+  }
   if (!(fabsf(t.hi) < 4194304.0f)) return false;  // 2^22
-  const float tb = fmul(kBound, fabsf(t.hi));
   const float n = rintf(t.hi);
   const Pair f = two_sum(fsub(t.hi, n), t.lo);  // t.hi - n is exact
   if (!(fabsf(f.hi) + fabsf(f.lo) + tb < 0.4999f)) return false;  // rint(t) == n

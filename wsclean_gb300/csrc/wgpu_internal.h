@@ -60,9 +60,10 @@ struct DevPlan {
   int nu, nv, width, height, support, tile, ntu, ntv, n_planes;
   float beta;
   float w0f, inv_dwf;  // w0 and inv_dw rounded to float (FP32 footprint tests)
-  // the rests of w0, inv_dw and nm1_center rounded to float, and nm1_center
-  // rounded to float (float-float records)
+  // the rests of w0, inv_dw and nm1_center rounded to float, nm1_center
+  // rounded to float, and the shifts as float pairs (float-float records)
   float w0l, inv_dwl, nm1_center_f, nm1_center_l;
+  float l_shift_f, l_shift_l, m_shift_f, m_shift_l;
   double dl, dm, l_shift, m_shift, w0, dw, inv_dw, nm1_center;
 };
 
