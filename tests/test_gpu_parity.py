@@ -477,6 +477,32 @@ def test_bound_split_units_over_plane_batches(wgpu_lib, oracle_lib):
     ref_g.close()
 
 
+@pytest.mark.parametrize("shift", [(0.0, 0.0), (0.03, -0.02)])
+def test_many_w_planes_within_epsilon(wgpu_lib, oracle_lib, shift):
+    """A wide field (0.5 rad across) with large w needs about 650 w planes in
+    batches of 32: the screen phase of plane q, formed from per-pixel
+    fixed-point terms as (a + q k) 2^-32 + q r turns, stays within epsilon of
+    the FP64 direct transform for every q, in both directions."""
+    W, dl, eps = 64, 8e-3, 1e-5
+    uvw, freq, vis = synthetic.random_points(300, 4, W, dl, seed=81, w_scale=60.0)
+    g = WGriddingGridder_Simple(W, W, W, W, dl, dl, shift[0], shift[1], 1, epsilon=eps)
+    g.InitializeInversion()
+    g.AddInversionData(uvw.shape[0], freq.size, uvw, freq, vis)
+    plan = g.last_plan()
+    assert plan.n_planes > 600 and plan.n_planes > 8 * plan.plane_batch
+    img = g.RealImage().astype(np.float64)
+    ref = oracle_lib.dft_invert(uvw, freq, vis, W, W, dl, dl, *shift)
+    assert rel(img, ref) <= eps
+    rng = np.random.default_rng(5)
+    model = np.zeros(W * W, np.float32)
+    model[rng.choice(W * W, 20, replace=False)] = rng.uniform(-1, 1, 20)
+    g.InitializePrediction(model)
+    pv = g.PredictVisibilities(uvw.shape[0], freq.size, uvw, freq)
+    pr = oracle_lib.dft_predict(uvw, freq, model, W, W, dl, dl, *shift)
+    assert rel(pv.ravel(), pr.ravel()) <= eps
+    g.close()
+
+
 def test_bounded_wait_expires_and_device_stays_usable(wgpu_lib):
     """A bounded device wait on a barrier that nothing arrives at expires,
     is reported as WGPU_ERR_TIMEOUT, and later work runs normally."""

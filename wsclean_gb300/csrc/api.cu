@@ -107,6 +107,7 @@ struct BoundState {
   int64_t n_rows = 0, n_chan = 0, n_out = 0;
   std::vector<void *> owned;
   double *uvw = nullptr, *freq = nullptr, *nu_w = nullptr;
+  wgpu::ScreenTable scr;
   uint8_t *mask = nullptr;
   wgpu::VisRecord *geom = nullptr, *work = nullptr;
   uint32_t *perm = nullptr, *offsets = nullptr;
@@ -152,6 +153,7 @@ struct wgpu_gridder {
   std::vector<StageTimer::Stage> last_timings;
   std::string corr_key;  // geometry of the correction tables in the arena
   std::string nuw_key;   // geometry (and buffer) of the n - 1 table in the arena
+  std::string scr_key;   // plan (and buffer) of the w-screen terms in the arena
   std::unique_ptr<BoundState> bound;
   std::vector<wgpu_tuning_trial_t> last_trials;  // candidates timed by the last tuning
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
@@ -349,6 +351,22 @@ double *nu_table_for(wgpu_gridder *g, const wgpu_plan_t &plan, const DevPlan &dp
   return nu_w;
 }
 
+// Per-pixel w-screen terms of the plan (w0, dw and the geometry of nu_w), in
+// the arena; recomputed only when the plan's w planes or the buffers change.
+ScreenTable screen_table_for(wgpu_gridder *g, const wgpu_plan_t &plan, const DevPlan &dp,
+                             const double *nu_w) {
+  const int64_t npix = plan.width * plan.height;
+  void *buf = g->arena.get(kSlotScreen, kScreenBytesPerPixel * npix);
+  char key[400];
+  std::snprintf(key, sizeof(key), "%s/%p/%.17g/%.17g", g->nuw_key.c_str(), buf, dp.w0, dp.dw);
+  const ScreenTable scr = screen_table_at(buf, npix);
+  if (g->scr_key != key) {
+    launch_screen_table(dp, nu_w, scr, g->stream);
+    g->scr_key = key;
+  }
+  return scr;
+}
+
 // A pinned plan is used as long as it covers the data: every visibility's w
 // footprint must fall inside its planes (a clamped footprint would be wrong).
 void check_pinned_plan(const wgpu_gridder *g, double w_min, double w_max) {
@@ -460,7 +478,7 @@ double time_plan(wgpu_gridder *g, const wgpu_plan_t &plan, const double *d_uvw,
   fft_twiddles(*g->fft, (int)plan.fft_n1);
   fft_twiddles(*g->fft, (int)plan.fft_n2);
   fft_prepare_rows(*g->fft, (int)plan.nu);
-  double *nu_w = nu_table_for(g, plan, dp);
+  const ScreenTable scr = screen_table_for(g, plan, dp, nu_table_for(g, plan, dp));
   float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
   float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
   float2 *acc = inversion ? (float2 *)g->arena.get(kSlotAcc, sizeof(float2) * npix) : nullptr;
@@ -485,7 +503,7 @@ double time_plan(wgpu_gridder *g, const wgpu_plan_t &plan, const double *d_uvw,
           launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb,
                             -1.0f, sel, s);
           launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                               R, rstride, nb, (int)p0, nu_w, acc, sel, s);
+                                               R, rstride, nb, (int)p0, scr, acc, sel, s);
         }
       }
       if (prediction) {
@@ -496,7 +514,7 @@ double time_plan(wgpu_gridder *g, const wgpu_plan_t &plan, const double *d_uvw,
           const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
           const RowSel sel = row_sel(b.rows, (int)p0);
           launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                            img, nu_w, R, rstride, nb, (int)p0, s);
+                                            img, scr, R, rstride, nb, (int)p0, s);
           launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb,
                             +1.0f, sel, s);
           launch_fft_rows_backward_pad(*g->fft, dp, R, rstride, planes, nb, sel, g->d_flags, s);
@@ -648,6 +666,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
   double *nu_w = nu_table_for(g, plan, dp);
+  const ScreenTable scr = screen_table_for(g, plan, dp, nu_w);
   float2 *acc = (float2 *)g->arena.get(kSlotAcc, sizeof(float2) * npix);
   const int64_t B = plan.plane_batch;
   float2 *planes = (float2 *)g->arena.get(kSlotPlanes, sizeof(float2) * B * plan.nu * plan.nv);
@@ -665,7 +684,7 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
                       sel, s);
     g->timer.mark("fft_cols_b_screen");
     launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R,
-                                         rstride, nb, (int)p0, nu_w, acc, sel, s);
+                                         rstride, nb, (int)p0, scr, acc, sel, s);
     if (g->verbosity >= 2)
       std::fprintf(stderr, "wgpu invert: planes %lld..%lld\n", (long long)p0,
                    (long long)(p0 + nb - 1));
@@ -715,6 +734,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
   double *nu_w = nu_table_for(g, plan, dp);
+  const ScreenTable scr = screen_table_for(g, plan, dp, nu_w);
   float *img_corr = (float *)g->arena.get(kSlotImgCorr, sizeof(float) * npix);
   float2 *vacc = (float2 *)g->arena.get(kSlotVisAcc, sizeof(float2) * (b.n_out + 1));
   const int64_t B = plan.plane_batch;
@@ -728,7 +748,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
     g->timer.mark("fft_cols_b_screen");
     launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                      img_corr, nu_w, R, rstride, nb, (int)p0, s);
+                                      img_corr, scr, R, rstride, nb, (int)p0, s);
     g->timer.mark("fft_cols_a");
     const RowSel sel = row_sel(b.rows, (int)p0);
     launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, R, rstride, nb, +1.0f,
@@ -775,10 +795,12 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                                                       n_rows, n_chan, false, true, true);
                                    })
                       : plan_for(g, w_min, w_max, count);
-  if (g->tuning)
+  if (g->tuning) {
     // the bound set owns its batch buffers: drop the ones the timing runs used
-    for (int slot : {kSlotPlanes, kSlotRows, kSlotAcc, kSlotImgCorr, kSlotVisAcc})
+    for (int slot : {kSlotPlanes, kSlotRows, kSlotAcc, kSlotImgCorr, kSlotVisAcc, kSlotScreen})
       g->arena.release(slot);
+    g->scr_key.clear();
+  }
   g->last_plan = b->plan;
   log_plan(g, "bind", b->plan, count);
   const wgpu_plan_t &plan = b->plan;
@@ -808,11 +830,13 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   b->rows = (float2 *)b->alloc(sizeof(float2) * B * plan.nv * rstride);
   b->acc = (float2 *)b->alloc(sizeof(float2) * npix);
   b->nu_w = (double *)b->alloc(sizeof(double) * npix);
+  b->scr = screen_table_at(b->alloc(kScreenBytesPerPixel * npix), npix);
   b->img_corr = (float *)b->alloc(sizeof(float) * npix);
   b->cx = (float *)b->alloc(sizeof(float) * plan.width);
   b->cy = (float *)b->alloc(sizeof(float) * plan.height);
   b->gl = (float *)b->alloc(sizeof(float) * 2 * kGlNodes);
   launch_nu_table(dp, b->nu_w, s);
+  launch_screen_table(dp, b->nu_w, b->scr, s);
   float *cx, *cy, *gl;
   upload_corrections(g, plan, &cx, &cy, &gl);
   WGPU_CUDA(cudaMemcpyAsync(b->cx, cx, sizeof(float) * plan.width, cudaMemcpyDeviceToDevice, s));
@@ -850,7 +874,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
                         -1.0f, sel, s);
       launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                           b->rows, rstride, nb, p0, b->nu_w, b->acc, sel, s);
+                                           b->rows, rstride, nb, p0, b->scr, b->acc, sel, s);
     }
     launch_finalize_add(dp, b->acc, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, g->d_img, g->prec, s);
   } catch (...) {
@@ -874,7 +898,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       const int p0 = (int)(i * B);
       const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
       launch_fft_cols_b_backward_screen(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
-                                        b->img_corr, b->nu_w, b->rows, rstride, nb, p0, s);
+                                        b->img_corr, b->scr, b->rows, rstride, nb, p0, s);
       const RowSel sel = row_sel(b->rows_occ, p0);
       launch_fft_cols_a(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2, b->rows, rstride, nb,
                         +1.0f, sel, s);

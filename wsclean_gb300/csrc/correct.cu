@@ -28,6 +28,28 @@ __global__ void nu_table_kernel(DevPlan p, double *nu_w) {
   nu_w[i] = nm1 - p.nm1_center;
 }
 
+// w-screen terms per pixel: the screen of plane q, w_q = w0 + q dw, is
+// exp(-+2 pi i w_q nu), the per-plane screen of ducc0's w-gridding behind
+// ms2dirty / dirty2ms (wgridder/gridder_simple.h:216-225), whose argument is
+// formed in FP64.  w0 nu and dw nu are reduced
+// modulo one turn in FP64 and kept as 32-bit fixed-point turns, so that
+// a + q k in wrapping uint32 arithmetic is (w0 + q dw) nu modulo one turn for
+// every q, rounded to 2^-33 turns; r carries dw nu below 2^-33 for large q.
+__global__ void screen_table_kernel(DevPlan p, const double *nu_w, ScreenTable scr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)p.width * p.height) return;
+  const double nu = nu_w[i];
+  constexpr double kTurn = 4294967296.0;  // 2^32
+  double a = p.w0 * nu;
+  a -= rint(a);
+  double k = p.dw * nu;
+  k -= rint(k);
+  const double kq = rint(k * kTurn);
+  scr.a[i] = (uint32_t)(int64_t)rint(a * kTurn);
+  scr.k[i] = (uint32_t)(int64_t)kq;
+  scr.r[i] = (float)(k - kq * (1.0 / kTurn));
+}
+
 // Grid-correction tables: thread t < width gives cx[t] = 1 / psihat((width/2 -
 // t) / nu), the next height threads cy[y] = 1 / psihat((y - height/2) / nv),
 // psihat(f) = W sum_i g_i cos(pi f W z_i) over the planner's quadrature (the
@@ -313,6 +335,21 @@ void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s) {
   const int64_t n = (int64_t)p.width * p.height;
   nu_table_kernel<<<blocks_for(n), kThreads, 0, s>>>(p, nu_w);
   check_launch("nu_table_kernel");
+}
+
+ScreenTable screen_table_at(void *buf, int64_t npix) {
+  ScreenTable t;
+  t.a = (uint32_t *)buf;
+  t.k = t.a + npix;
+  t.r = (float *)(t.k + npix);
+  return t;
+}
+
+void launch_screen_table(const DevPlan &p, const double *nu_w, const ScreenTable &scr,
+                         cudaStream_t s) {
+  const int64_t n = (int64_t)p.width * p.height;
+  screen_table_kernel<<<blocks_for(n), kThreads, 0, s>>>(p, nu_w, scr);
+  check_launch("screen_table_kernel");
 }
 
 void launch_finalize_add(const DevPlan &p, const float2 *acc,

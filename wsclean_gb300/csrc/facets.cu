@@ -64,6 +64,7 @@ struct Job {
   RowOccupancy rows_occ;  // plane rows the job's footprints touch
   float2 *acc = nullptr;
   double *nu_w = nullptr;
+  ScreenTable scr;
   float *cx = nullptr, *cy = nullptr, *gl = nullptr;
   float *img = nullptr;  // width * height, row-major
   std::vector<WorkItems> items;  // per plane batch
@@ -331,6 +332,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     j.acc = (float2 *)f->alloc(sizeof(float2) * npix);
     j.nu_w = (double *)f->alloc(sizeof(double) * npix);
     launch_nu_table(j.dp, j.nu_w, s);
+    j.scr = screen_table_at(f->alloc(kScreenBytesPerPixel * npix), npix);
+    launch_screen_table(j.dp, j.nu_w, j.scr, s);
     j.cx = (float *)f->alloc(sizeof(float) * j.plan.width);
     j.cy = (float *)f->alloc(sizeof(float) * j.plan.height);
     j.gl = (float *)f->alloc(sizeof(float) * 2 * kCorrGlNodes);
@@ -482,7 +485,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
                           sl.nb, -1.0f, sel, ss);
         launch_fft_cols_b_forward_accumulate(*f->fft, j.dp, (int)j.plan.fft_n1,
                                              (int)j.plan.fft_n2, rows, j.rstride, sl.nb, sl.p0,
-                                             j.nu_w, j.acc, sel, ss);
+                                             j.scr, j.acc, sel, ss);
       }
       for (int k = 0; k < wgpu_facets::kSide; ++k) {
         WGPU_CUDA(cudaEventRecord(f->ev_side[k], f->side[k]));

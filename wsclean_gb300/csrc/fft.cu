@@ -712,51 +712,40 @@ __device__ __forceinline__ int image_row_of(int k, int nv, int height) {
   return -1;
 }
 
-// Phase of the w-screen for the planes b of a batch: t_b = (wq0 + b dw) nu
-// turns.  The FP64 products wq0 nu and dw nu are reduced modulo 1 once per
-// pixel; dw nu is split into a head with 16 fractional bits, for which b * head
-// is exact in FP32 (b < 256), and a tail below 2^-17.  The FP32 sum then
-// carries an error of about 1e-7 turns.
-constexpr float kNoPixel = 8.0f;  // phase marker of panel elements outside the image
-__device__ __forceinline__ void screen_phase(double wq0, double dw, double nu, float *a,
-                                             float *bh, float *bl) {
-  double ta = wq0 * nu;
-  ta -= rint(ta);
-  double tb = dw * nu;
-  tb -= rint(tb);
-  const double h = rint(tb * 65536.0) * (1.0 / 65536.0);
-  *a = (float)ta;
-  *bh = (float)h;
-  *bl = (float)(tb - h);
-}
-__device__ __forceinline__ void screen_b(float a, float bh, float bl, int b, float *sn,
+// Phase of the w-screen of plane q at a pixel from its screen terms (a, k, r):
+// t = (a + q k) 2^-32 + q r turns, the fixed-point part wrapping modulo one
+// turn in uint32 arithmetic (exact for every q), so no FP64 and no range
+// reduction remain per plane; the result carries about 5e-8 turns of error
+// from the two FP32 roundings.
+constexpr float kNoPixel = 8.0f;  // remainder marker of panel elements outside the image
+__device__ __forceinline__ void screen_b(uint32_t a, uint32_t k, float r, int q, float *sn,
                                          float *cs) {
-  float h = (float)b * bh;  // exact
-  h -= rintf(h);
-  float t = a + h + (float)b * bl;
-  t -= rintf(t);
-  sincospif(2.0f * t, sn, cs);
+  const int32_t t = (int32_t)(a + (uint32_t)q * k);  // turns in 2^-32, within [-1/2, 1/2)
+  // sincospi of 2 t: t 2^-31 plus 2 q r
+  sincospif(fmaf((float)t, 0x1p-31f, (float)(2 * q) * r), sn, cs);
 }
 
 // Shared layout of the column-B kernels: the two FFT buffers (n2 * kPanel
-// each), then the per-element phase terms a, bh, bl (n2 * kPanel each).
+// each), then the per-element screen terms a, k, r (n2 * kPanel each).
 __host__ __device__ constexpr size_t cols_b_smem(int n2) {
   return (size_t)n2 * kPanel * (2 * sizeof(float2) + 3 * sizeof(float));
 }
 
-// Phase terms of the panel elements of this block (kNoPixel outside the image).
+// Screen terms of the panel elements of this block (r = kNoPixel outside the image).
 __device__ __forceinline__ void cols_b_phases(const DevPlan &p, int n1, int n2, int cg, int k1,
-                                              int p_begin, const double *__restrict__ nu_w,
-                                              float *pa, float *pbh, float *pbl) {
-  const double wq0 = p.w0 + (double)p_begin * p.dw;
+                                              const ScreenTable &scr, uint32_t *pa,
+                                              uint32_t *pk, float *pr) {
   for (int e = threadIdx.x; e < n2 * kPanel; e += blockDim.x) {
     const int k2 = e / kPanel, col = e % kPanel;
     const int x = cg * kPanel + col;
     const int y = image_row_of(k1 + n1 * k2, p.nv, p.height);
     if (x < p.width && y >= 0) {
-      screen_phase(wq0, p.dw, __ldg(nu_w + (size_t)y * p.width + x), &pa[e], &pbh[e], &pbl[e]);
+      const size_t i = (size_t)y * p.width + x;
+      pa[e] = __ldg(scr.a + i);
+      pk[e] = __ldg(scr.k + i);
+      pr[e] = __ldg(scr.r + i);
     } else {
-      pa[e] = kNoPixel;
+      pr[e] = kNoPixel;
     }
   }
 }
@@ -768,7 +757,7 @@ __global__ void __launch_bounds__(kColThreads, 2)
     fft_cols_forward_accumulate_kernel(FftDesc d2, DevPlan p, int n1,
                                        float2 *__restrict__ R, int rstride,
                                        int n_batch, int p_begin,
-                                       const double *__restrict__ nu_w,
+                                       const ScreenTable scr,
                                        float2 *__restrict__ acc,
                                        const float2 *__restrict__ tw2,
                                        const uint8_t *__restrict__ flags) {
@@ -777,9 +766,10 @@ __global__ void __launch_bounds__(kColThreads, 2)
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
   const int ne = n2 * kPanel;
-  float *pa = reinterpret_cast<float *>(s + 2 * ne);
-  float *pbh = pa + ne, *pbl = pbh + ne;
-  cols_b_phases(p, n1, n2, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  uint32_t *pa = reinterpret_cast<uint32_t *>(s + 2 * ne);
+  uint32_t *pk = pa + ne;
+  float *pr = reinterpret_cast<float *>(pk + ne);
+  cols_b_phases(p, n1, n2, cg, k1, scr, pa, pk, pr);
   float part[NE];
 #pragma unroll
   for (int c = 0; c < NE; ++c) part[c] = 0.f;
@@ -794,11 +784,11 @@ __global__ void __launch_bounds__(kColThreads, 2)
     for (int c = 0; c < NE; ++c) {
       const int e = threadIdx.x + c * blockDim.x;
       if (e < ne) {
-        const float a = pa[e];
-        if (a != kNoPixel) {
+        const float r = pr[e];
+        if (r != kNoPixel) {
           const float2 v = res[e];
           float sn, cs;
-          screen_b(a, pbh[e], pbl[e], b, &sn, &cs);
+          screen_b(pa[e], pk[e], r, p_begin + b, &sn, &cs);
           // Re(v exp(-2 pi i t)) = v.re cos + v.im sin
           part[c] += v.x * cs + v.y * sn;
         }
@@ -809,7 +799,7 @@ __global__ void __launch_bounds__(kColThreads, 2)
 #pragma unroll
   for (int c = 0; c < NE; ++c) {
     const int e = threadIdx.x + c * blockDim.x;
-    if (e < ne && pa[e] != kNoPixel) {
+    if (e < ne && pr[e] != kNoPixel) {
       const int k2 = e / kPanel, col = e % kPanel;
       const int x = cg * kPanel + col;
       const int y = image_row_of(k1 + n1 * k2, nv, p.height);
@@ -830,7 +820,7 @@ template <int NE>
 __global__ void __launch_bounds__(kColThreads, 2)
     fft_cols_backward_screen_kernel(FftDesc d2, DevPlan p, int n1,
                                     const float *__restrict__ img_corr,
-                                    const double *__restrict__ nu_w,
+                                    const ScreenTable scr,
                                     float2 *__restrict__ R, int rstride,
                                     int n_batch, int p_begin,
                                     const float2 *__restrict__ tw2,
@@ -840,9 +830,10 @@ __global__ void __launch_bounds__(kColThreads, 2)
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
   const int ne = n2 * kPanel;
-  float *pa = reinterpret_cast<float *>(s + 2 * ne);
-  float *pbh = pa + ne, *pbl = pbh + ne;
-  cols_b_phases(p, n1, n2, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  uint32_t *pa = reinterpret_cast<uint32_t *>(s + 2 * ne);
+  uint32_t *pk = pa + ne;
+  float *pr = reinterpret_cast<float *>(pk + ne);
+  cols_b_phases(p, n1, n2, cg, k1, scr, pa, pk, pr);
   float val[NE];  // pre-corrected image value of each element
 #pragma unroll
   for (int c = 0; c < NE; ++c) {
@@ -864,7 +855,7 @@ __global__ void __launch_bounds__(kColThreads, 2)
         float2 v = make_float2(0.f, 0.f);
         if (val[c] != 0.0f) {
           float sn, cs;
-          screen_b(pa[e], pbh[e], pbl[e], b, &sn, &cs);
+          screen_b(pa[e], pk[e], pr[e], p_begin + b, &sn, &cs);
           v = make_float2(val[c] * cs, val[c] * sn);  // a exp(+2 pi i t)
         }
         s[e] = v;
@@ -979,7 +970,7 @@ template <int R2>
 __global__ void __launch_bounds__(kPanelThreads, 2)
     fft_cols_forward_accumulate16_kernel(DevPlan p, int n1, float2 *__restrict__ R, int rstride,
                                          int n_batch, int p_begin,
-                                         const double *__restrict__ nu_w,
+                                         const ScreenTable scr,
                                          float2 *__restrict__ acc,
                                          const float2 *__restrict__ tw2,
                                          const uint8_t *__restrict__ flags) {
@@ -987,9 +978,10 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
   constexpr int N = 16 * R2, ne = N * kPanel;
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
-  float *pa = reinterpret_cast<float *>(s + ne);
-  float *pbh = pa + ne, *pbl = pbh + ne;
-  cols_b_phases(p, n1, N, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  uint32_t *pa = reinterpret_cast<uint32_t *>(s + ne);
+  uint32_t *pk = pa + ne;
+  float *pr = reinterpret_cast<float *>(pk + ne);
+  cols_b_phases(p, n1, N, cg, k1, scr, pa, pk, pr);
   float part[2 * R2];
 #pragma unroll
   for (int c = 0; c < 2 * R2; ++c) part[c] = 0.f;
@@ -1002,10 +994,10 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
     };
     auto store = [&](int slot, int k2, int c, float2 v) {
       const int e = k2 * kPanel + c;
-      const float a = pa[e];
-      if (a != kNoPixel) {
+      const float r = pr[e];
+      if (r != kNoPixel) {
         float sn, cs;
-        screen_b(a, pbh[e], pbl[e], b, &sn, &cs);
+        screen_b(pa[e], pk[e], r, p_begin + b, &sn, &cs);
         // Re(v exp(-2 pi i t)) = v.re cos + v.im sin
         part[slot] += v.x * cs + v.y * sn;
       }
@@ -1020,7 +1012,7 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
     for (int q = 0; q < R2; ++q) {
       const int k2 = (threadIdx.x >> 5) + 8 * it + 16 * q;
       const int e = k2 * kPanel + col;
-      if (pa[e] != kNoPixel) {
+      if (pr[e] != kNoPixel) {
         const int x = cg * kPanel + col;
         const int y = image_row_of(k1 + n1 * k2, nv, p.height);
         float2 *a = acc + (size_t)y * p.width + x;
@@ -1041,7 +1033,7 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
 template <int R2>
 __global__ void __launch_bounds__(kPanelThreads, 2)
     fft_cols_backward_screen16_kernel(DevPlan p, int n1, const float *__restrict__ img_corr,
-                                      const double *__restrict__ nu_w, float2 *__restrict__ R,
+                                      const ScreenTable scr, float2 *__restrict__ R,
                                       int rstride, int n_batch, int p_begin,
                                       const float2 *__restrict__ tw2,
                                       const float2 *__restrict__ twN) {
@@ -1049,9 +1041,10 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
   constexpr int N = 16 * R2, ne = N * kPanel;
   const int nv = p.nv;
   const int cg = blockIdx.x, k1 = blockIdx.y;
-  float *pa = reinterpret_cast<float *>(s + ne);
-  float *pbh = pa + ne, *pbl = pbh + ne;
-  cols_b_phases(p, n1, N, cg, k1, p_begin, nu_w, pa, pbh, pbl);
+  uint32_t *pa = reinterpret_cast<uint32_t *>(s + ne);
+  uint32_t *pk = pa + ne;
+  float *pr = reinterpret_cast<float *>(pk + ne);
+  cols_b_phases(p, n1, N, cg, k1, scr, pa, pk, pr);
   const int col = threadIdx.x & 31, i1 = threadIdx.x >> 5;
   float val[16];
 #pragma unroll
@@ -1070,7 +1063,7 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
       if (val[t] == 0.0f) return make_float2(0.f, 0.f);
       const int idx = e * kPanel + c;
       float sn, cs;
-      screen_b(pa[idx], pbh[idx], pbl[idx], b, &sn, &cs);
+      screen_b(pa[idx], pk[idx], pr[idx], p_begin + b, &sn, &cs);
       return make_float2(val[t] * cs, val[t] * sn);  // a exp(+2 pi i t)
     };
     auto store = [&](int, int r2, int c, float2 v) {
@@ -1283,7 +1276,7 @@ void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R
 void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1,
                                           int n2, float2 *R, int rstride,
                                           int n_batch, int p_begin,
-                                          const double *nu_w, float2 *acc,
+                                          const ScreenTable &scr, float2 *acc,
                                           const RowSel &sel, cudaStream_t s) {
   // after a pass A every row of R holds data; without one, R is as the row
   // transforms left it
@@ -1296,7 +1289,7 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
 #define WGPU_PASS_B16(X)                                                                  \
   set_smem((const void *)fft_cols_forward_accumulate16_kernel<X>, smem);                  \
   fft_cols_forward_accumulate16_kernel<X><<<grid, kPanelThreads, smem, s>>>(              \
-      p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags)
+      p, n1, R, rstride, n_batch, p_begin, scr, acc, tw, flags)
     WGPU_PANEL_SWITCH(r2p, WGPU_PASS_B16)
 #undef WGPU_PASS_B16
     check_launch("fft_cols_forward_accumulate16_kernel");
@@ -1309,18 +1302,18 @@ void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1
   if (n2 * kPanel <= 8 * kColThreads) {
     set_smem((const void *)fft_cols_forward_accumulate_kernel<8>, smem);
     fft_cols_forward_accumulate_kernel<8><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags);
+        d2, p, n1, R, rstride, n_batch, p_begin, scr, acc, tw, flags);
   } else {
     set_smem((const void *)fft_cols_forward_accumulate_kernel<16>, smem);
     fft_cols_forward_accumulate_kernel<16><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, R, rstride, n_batch, p_begin, nu_w, acc, tw, flags);
+        d2, p, n1, R, rstride, n_batch, p_begin, scr, acc, tw, flags);
   }
   check_launch("fft_cols_forward_accumulate_kernel");
 }
 
 void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        int n2, const float *img_corr,
-                                       const double *nu_w, float2 *R,
+                                       const ScreenTable &scr, float2 *R,
                                        int rstride, int n_batch, int p_begin,
                                        cudaStream_t s) {
   const int ncg = rstride / kPanel;
@@ -1331,7 +1324,7 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
 #define WGPU_PASS_B16B(X)                                                                 \
   set_smem((const void *)fft_cols_backward_screen16_kernel<X>, smem);                     \
   fft_cols_backward_screen16_kernel<X><<<grid, kPanelThreads, smem, s>>>(                 \
-      p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN)
+      p, n1, img_corr, scr, R, rstride, n_batch, p_begin, tw, twN)
     WGPU_PANEL_SWITCH(r2p, WGPU_PASS_B16B)
 #undef WGPU_PASS_B16B
     check_launch("fft_cols_backward_screen16_kernel");
@@ -1344,11 +1337,11 @@ void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
   if (n2 * kPanel <= 8 * kColThreads) {
     set_smem((const void *)fft_cols_backward_screen_kernel<8>, smem);
     fft_cols_backward_screen_kernel<8><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN);
+        d2, p, n1, img_corr, scr, R, rstride, n_batch, p_begin, tw, twN);
   } else {
     set_smem((const void *)fft_cols_backward_screen_kernel<16>, smem);
     fft_cols_backward_screen_kernel<16><<<grid, kColThreads, smem, s>>>(
-        d2, p, n1, img_corr, nu_w, R, rstride, n_batch, p_begin, tw, twN);
+        d2, p, n1, img_corr, scr, R, rstride, n_batch, p_begin, tw, twN);
   }
   check_launch("fft_cols_backward_screen_kernel");
 }

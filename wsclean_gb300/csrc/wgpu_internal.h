@@ -279,20 +279,35 @@ int bounded_wait_selftest(double timeout_ms);
 void launch_fft_cols_a(FftTables &t, const DevPlan &p, int n1, int n2, float2 *R,
                        int rstride, int n_batch, float sign, const RowSel &sel,
                        cudaStream_t s);
+// Per-pixel w-screen terms of a plan (three planar arrays of width * height):
+// the screen phase of plane q at a pixel is t = (a + q k) 2^-32 + q r turns,
+// a = w0 (n - 1 - c_n) and k = dw (n - 1 - c_n) modulo one turn in 2^-32
+// steps (wrapping uint32 arithmetic), r the remainder of the latter.
+struct ScreenTable {
+  uint32_t *a = nullptr;
+  uint32_t *k = nullptr;
+  float *r = nullptr;
+};
+constexpr size_t kScreenBytesPerPixel = 2 * sizeof(uint32_t) + sizeof(float);
+// Views npix pixels of screen terms in a buffer of kScreenBytesPerPixel * npix.
+ScreenTable screen_table_at(void *buf, int64_t npix);
 // sel: the rows the forward row transforms wrote (read when n1 <= 1).
 void launch_fft_cols_b_forward_accumulate(FftTables &t, const DevPlan &p, int n1,
                                           int n2, float2 *R, int rstride,
                                           int n_batch, int p_begin,
-                                          const double *nu_w, float2 *acc,
+                                          const ScreenTable &scr, float2 *acc,
                                           const RowSel &sel, cudaStream_t s);
 void launch_fft_cols_b_backward_screen(FftTables &t, const DevPlan &p, int n1,
                                        int n2, const float *img_corr,
-                                       const double *nu_w, float2 *R,
+                                       const ScreenTable &scr, float2 *R,
                                        int rstride, int n_batch, int p_begin,
                                        cudaStream_t s);
 
 // ---- corrections (correct.cu) ----
 void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s);
+// The screen terms of plan p from its n - 1 - c_n table (FP64, once per plan).
+void launch_screen_table(const DevPlan &p, const double *nu_w, const ScreenTable &scr,
+                         cudaStream_t s);
 // tdirty * corr added into the accumulated image (float or double).
 void launch_finalize_add(const DevPlan &p, const float2 *acc,
                          const double *nu_w, const float *cx, const float *cy,
@@ -461,6 +476,7 @@ enum ArenaSlot {
   kSlotResampleOut,   // the image at the padded image size,
   kSlotResampleTrim,  // and at the trimmed size
   kSlotCorner,        // bucketing: footprint corner within the tile, per sample
+  kSlotScreen,        // per-pixel w-screen terms of the current plan
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
