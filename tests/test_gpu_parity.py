@@ -39,6 +39,10 @@ BUCKET_CASES = [
     dict(W=128, dl=5e-4, rows=1500, chan=3, w_scale=0.0, zero=0.1, seed=3, shift=(0, 0), inv=True),
     dict(W=512, dl=1e-4, rows=5000, chan=16, w_scale=2.0, zero=0.3, seed=4, shift=(0, 0.003),
          inv=True),
+    # 2.56 M samples: several hundred 4096-element sort tiles, more than the
+    # sort's resident blocks, so blocks take several tiles each
+    dict(W=1024, dl=5e-5, rows=40000, chan=64, w_scale=2.0, zero=0.25, seed=5, shift=(0, 0),
+         inv=True),
 ]
 
 

@@ -180,8 +180,8 @@ void end_call(wgpu_gridder *g) {
     *g->h_flags = 0;
     WGPU_CUDA(cudaMemsetAsync(g->d_flags, 0, sizeof(unsigned), g->stream));
     WGPU_CUDA(cudaStreamSynchronize(g->stream));
-    throw Error(WGPU_ERR_TIMEOUT,
-                "a bounded device wait expired (row transform prefetch or degridding staging)");
+    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (bucket sort look-back, row "
+                                  "transform prefetch or degridding staging)");
   }
 }
 
@@ -492,7 +492,8 @@ double time_plan(wgpu_gridder *g, const wgpu_plan_t &plan, const double *d_uvw,
       WGPU_CUDA(cudaStreamSynchronize(s));
       WGPU_CUDA(cudaEventRecord(e0, s));
       const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis, d_mask,
-                                                 (int64_t)n_rows, (int64_t)n_chan, skip_zero, s);
+                                                 (int64_t)n_rows, (int64_t)n_chan, skip_zero,
+                                                 g->d_flags, s);
       if (inversion) {
         WGPU_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * npix, s));
         for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
@@ -661,7 +662,8 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   const DevPlan dp = to_dev_plan(plan);
   g->timer.mark("bucket");
   const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, d_vis, nullptr,
-                                             (int64_t)n_rows, (int64_t)n_chan, true, s);
+                                             (int64_t)n_rows, (int64_t)n_chan, true, g->d_flags,
+                                             s);
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
@@ -729,7 +731,8 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   const DevPlan dp = to_dev_plan(plan);
   g->timer.mark("bucket");
   const BucketResult b = bucket_visibilities(g->arena, dp, d_uvw, d_freq, nullptr, d_mask,
-                                             (int64_t)n_rows, (int64_t)n_chan, false, s);
+                                             (int64_t)n_rows, (int64_t)n_chan, false, g->d_flags,
+                                             s);
   g->timer.mark("setup");
   const int64_t npix = plan.width * plan.height;
   const int rstride = (int)((plan.width + 31) / 32 * 32);
@@ -807,7 +810,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   b->dp = to_dev_plan(plan);
   const DevPlan &dp = b->dp;
   const BucketResult br = bucket_visibilities(g->arena, dp, b->uvw, b->freq, nullptr, b->mask,
-                                              b->n_rows, b->n_chan, false, s);
+                                              b->n_rows, b->n_chan, false, g->d_flags, s);
   b->n_out = br.n_out;
   b->geom = (VisRecord *)b->alloc(sizeof(VisRecord) * (br.n_out + 1));
   b->work = (VisRecord *)b->alloc(sizeof(VisRecord) * (br.n_out + 1));
@@ -919,6 +922,15 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   WGPU_CUDA(cudaGraphInstantiate(&b->xpred, b->gpred, 0));
   b->pred_kernels = thread_launch_count() - k0;
   count_launch(-(int)b->pred_kernels);
+  // the bucketing's bounded waits report into the flag word
+  WGPU_CUDA(cudaMemcpyAsync(g->h_flags, g->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  if (*g->h_flags != 0) {
+    *g->h_flags = 0;
+    WGPU_CUDA(cudaMemsetAsync(g->d_flags, 0, sizeof(unsigned), s));
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (bucket sort look-back)");
+  }
   g->bound = std::move(b);
 }
 
@@ -1712,7 +1724,7 @@ static int bucket_debug_impl(const wgpu_plan_t *plan, size_t n_rows, size_t n_ch
         WGPU_CUDA(cudaMemcpyAsync(dv, vis, sizeof(float2) * n_rows * n_chan, cudaMemcpyHostToDevice, s));
       }
       const BucketResult b = bucket_visibilities(arena, dp, du, df, dv, nullptr, (int64_t)n_rows,
-                                                 (int64_t)n_chan, skip_zero != 0, s);
+                                                 (int64_t)n_chan, skip_zero != 0, nullptr, s);
       std::vector<VisRecord> rec(b.n_out);
       if (b.n_out) {
         WGPU_CUDA(cudaMemcpyAsync(rec.data(), b.records, sizeof(VisRecord) * b.n_out, cudaMemcpyDeviceToHost, s));

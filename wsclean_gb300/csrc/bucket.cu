@@ -495,6 +495,304 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ---------------- stable LSD radix sort, one kernel per 8-bit digit ----------
+// The same sort as above without the per-pass histogram and scan.  The digit
+// totals of every pass are counted beforehand (the corner byte by
+// corner_count_kernel, the key bytes from the bucket offsets by
+// key_byte_totals_kernel).  Blocks take
+// tiles of kThreads * ITEMS elements in order from a counter, so every lower
+// tile belongs to a block that has already started.  A block ranks its tile's
+// elements by digit (each warp a contiguous run of 32 * ITEMS elements, with
+// warp-private counts), publishes the tile's count of each digit, and adds up
+// the counts of the lower tiles by looking back over their published words:
+// a tile first publishes its own count (an aggregate), then, once its
+// look-back has ended, the inclusive sum over all tiles up to itself (a
+// prefix); a look-back stops at the first prefix it meets and reads
+// kSweepWindow lower tiles per round trip.  This is the single-pass prefix
+// scan with decoupled look-back (Merrill and Garland, 2016) applied per digit,
+// as in the Onesweep sort (Adinets and Merrill, 2022).  Each published word
+// carries its flag and count together, so relaxed loads and stores suffice.
+// A wait on a lower tile gives up after kSweepSpinLimit polls and reports
+// through the caller's flag word.
+constexpr uint64_t kSweepAggregate = 1ull << 62;
+constexpr uint64_t kSweepPrefix = 2ull << 62;
+constexpr uint64_t kSweepFlags = 3ull << 62;
+constexpr uint32_t kSweepSpinLimit = 1u << 20;
+constexpr int kSweepWindow = 8;        // lower tiles read per look-back step
+constexpr int kSweepMaxKeyPasses = 4;  // 32-bit keys
+// the library's configuration: elements per thread, resident blocks per SM
+constexpr int kSweepItems = 12;
+constexpr int kSweepMinBlocks = 3;
+
+template <int ITEMS>
+__host__ __device__ constexpr int sweep_tile() {
+  return kThreads * ITEMS;
+}
+// dynamic shared memory: warp counts, tile keys and values, tile digits
+template <int ITEMS>
+__host__ __device__ constexpr size_t sweep_smem() {
+  return sizeof(uint32_t) * ((kThreads / 32) * 256 + 2 * sweep_tile<ITEMS>()) +
+         sweep_tile<ITEMS>();
+}
+
+__device__ __forceinline__ void store_relaxed_u64(uint64_t *p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t load_relaxed_u64(const uint64_t *p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Exclusive scan of one value per thread over the block (kThreads threads);
+// *total receives the sum.  Ends with a barrier.
+__device__ __forceinline__ uint32_t sweep_block_scan(uint32_t v, uint32_t *wsum,
+                                                     uint32_t *total) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+#pragma unroll
+  for (int w = 0; w < kThreads / 32; ++w) {
+    const uint32_t s = wsum[w];
+    if (w < warp) before += s;
+    all += s;
+  }
+  *total = all;
+  __syncthreads();
+  return before + x - v;
+}
+
+// Counts of the corner byte over the elements whose key is not drop_key.
+__global__ void __launch_bounds__(kThreads)
+    corner_count_kernel(const uint32_t *__restrict__ keys, const uint8_t *__restrict__ minor,
+                        int64_t n, uint32_t drop_key, uint32_t *totals) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t n4 = n / 4, stride = (int64_t)gridDim.x * kThreads;
+  const uint4 *k4 = reinterpret_cast<const uint4 *>(keys);
+  const uint32_t *m4 = reinterpret_cast<const uint32_t *>(minor);
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n4; i += stride) {
+    const uint4 k = __ldg(k4 + i);
+    const uint32_t m = __ldg(m4 + i);  // bytes 4i .. 4i+3, the first in the low bits
+    if (k.x != drop_key) atomicAdd(&h[m & 255u], 1u);
+    if (k.y != drop_key) atomicAdd(&h[(m >> 8) & 255u], 1u);
+    if (k.z != drop_key) atomicAdd(&h[(m >> 16) & 255u], 1u);
+    if (k.w != drop_key) atomicAdd(&h[m >> 24], 1u);
+  }
+  for (int64_t i = 4 * n4 + (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += stride)
+    if (keys[i] != drop_key) atomicAdd(&h[minor[i]], 1u);
+  __syncthreads();
+  if (h[threadIdx.x]) atomicAdd(&totals[threadIdx.x], h[threadIdx.x]);
+}
+
+// Counts of bytes 0 .. n_bytes - 1 of the keys over the sorted elements, from
+// the bucket offsets (exclusive scan: key k holds off[k + 1] - off[k]
+// elements).  A warp takes 32 consecutive keys per step, four steps at a
+// time; a step's keys have the same bytes above the lowest (one warp sum and
+// one atomic each per step), and lane l's lowest byte is (step % 8) * 32 + l,
+// summed in eight registers.
+__global__ void __launch_bounds__(kThreads)
+    key_byte_totals_kernel(const uint32_t *__restrict__ off, int64_t n_keys, int n_bytes,
+                           uint32_t *totals) {
+  __shared__ uint32_t h[kSweepMaxKeyPasses][256];
+  for (int i = threadIdx.x; i < kSweepMaxKeyPasses * 256; i += kThreads) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kWarps = kThreads / 32, kSteps = 4;
+  uint32_t low[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int64_t n_steps = (n_keys + 31) / 32;
+  for (int64_t step0 = ((int64_t)blockIdx.x * kWarps + warp) * kSteps; step0 < n_steps;
+       step0 += (int64_t)gridDim.x * kWarps * kSteps) {
+    uint32_t c[kSteps];
+#pragma unroll
+    for (int u = 0; u < kSteps; ++u) {
+      const int64_t k = (step0 + u) * 32 + lane;
+      c[u] = k < n_keys ? __ldg(off + k + 1) - __ldg(off + k) : 0u;
+    }
+    const bool upper = (step0 & 4) != 0;  // step0 is a multiple of 4: steps are step0 % 8 + u
+#pragma unroll
+    for (int u = 0; u < kSteps; ++u) {
+      if (upper)
+        low[4 + u] += c[u];
+      else
+        low[u] += c[u];
+      uint32_t sum = c[u];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0 && sum)
+        for (int b = 1; b < n_bytes; ++b)
+          atomicAdd(&h[b][(uint32_t)(((step0 + u) * 32) >> (8 * b)) & 255u], sum);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (low[j]) atomicAdd(&h[0][j * 32 + lane], low[j]);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_bytes * 256; i += kThreads)
+    if ((&h[0][0])[i]) atomicAdd(totals + i, (&h[0][0])[i]);
+}
+
+// Status words of kSweepWindow lower tiles q, q - 1, ... for digit t (below
+// tile 0: a prefix of zero).
+__device__ __forceinline__ void sweep_window(const uint64_t *status, int64_t q, int t,
+                                             uint64_t (&x)[kSweepWindow]) {
+#pragma unroll
+  for (int j = 0; j < kSweepWindow; ++j)
+    x[j] = q - j >= 0 ? load_relaxed_u64(status + (q - j) * 256 + t) : kSweepPrefix;
+}
+
+// One stable pass over the n elements of (keys_in, vals_in) by the 8-bit digit
+// at `shift` (FIRST: by minor[i], leaving out the elements whose key is
+// drop_key).  totals: the pass's count of each digit.  status: 256 words
+// per tile, zero at launch; tile_counter zero at launch.
+template <bool FIRST, int ITEMS, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    sweep_kernel(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+                 const uint8_t *__restrict__ minor, int64_t n, int shift, uint32_t drop_key,
+                 const uint32_t *__restrict__ totals, uint64_t *status, uint32_t *tile_counter,
+                 uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
+                 unsigned *wait_flags) {
+  constexpr int kTile = sweep_tile<ITEMS>(), kRun = 32 * ITEMS;
+  static_assert(kRun <= 0xffff, "warp ranks are 16-bit");
+  extern __shared__ uint32_t sweep_smem[];
+  uint32_t(*wcnt)[256] = reinterpret_cast<uint32_t(*)[256]>(sweep_smem);
+  uint32_t *skey = sweep_smem + (kThreads / 32) * 256;
+  uint32_t *sval = skey + kTile;
+  uint8_t *sdig = reinterpret_cast<uint8_t *>(sval + kTile);
+  __shared__ uint32_t tstart[256], gbase[256], wsum[kThreads / 32];
+  __shared__ uint32_t s_tile, s_kept;
+  static_assert(kThreads == 256, "one thread per digit");
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, t = threadIdx.x;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t n_tiles = (n + kTile - 1) / kTile;
+  // the pass's first position of each digit
+  uint32_t unused;
+  const uint32_t dstart = sweep_block_scan(totals[t], wsum, &unused);
+  for (;;) {
+    if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = lane; i < 256; i += 32) wcnt[warp][i] = 0;
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (tile >= n_tiles) break;
+    const int64_t run0 = tile * kTile + warp * kRun;
+    uint32_t kr[ITEMS], vr[ITEMS], dr[ITEMS];
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const int64_t i = run0 + r * 32 + lane;
+      uint32_t d = 256;  // no element
+      kr[r] = 0;
+      vr[r] = 0;
+      if (i < n) {
+        kr[r] = keys_in[i];
+        vr[r] = vals_in[i];
+        if (FIRST) {
+          if (kr[r] != drop_key) d = minor[i];
+        } else {
+          d = (kr[r] >> shift) & 255u;
+        }
+      }
+      dr[r] = d;
+    }
+    // rank within the warp's run: earlier rounds, then lower lanes
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const uint32_t d = dr[r];
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      uint32_t before = 0;
+      if (d < 256) before = wcnt[warp][d];
+      __syncwarp();
+      if (d < 256 && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
+      __syncwarp();
+      dr[r] = (d << 16) | (before + __popc(peers & lt));
+    }
+    __syncthreads();
+    // thread t: digit t's offsets of the warps and the tile's count
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+      const uint32_t c = wcnt[w][t];
+      wcnt[w][t] = cnt;
+      cnt += c;
+    }
+    uint64_t *mine = status + tile * 256 + t;
+    store_relaxed_u64(mine, (tile == 0 ? kSweepPrefix : kSweepAggregate) | cnt);
+    // the first look-back window is in flight while the tile is placed
+    int64_t q = tile - 1;
+    uint64_t x[kSweepWindow];
+    if (tile > 0) sweep_window(status, q, t, x);
+    uint32_t kept;
+    const uint32_t first = sweep_block_scan(cnt, wsum, &kept);
+    tstart[t] = first;
+    if (t == 0) s_kept = kept;
+    __syncthreads();  // tile positions and warp offsets of every digit
+    // the tile in digit order in shared memory
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const uint32_t d = dr[r] >> 16;
+      if (d < 256) {
+        const uint32_t pos = tstart[d] + wcnt[warp][d] + (dr[r] & 0xffffu);
+        skey[pos] = kr[r];
+        sval[pos] = vr[r];
+        sdig[pos] = (uint8_t)d;
+      }
+    }
+    // digit t's count over the lower tiles: tiles q, q - 1, ... are added
+    // while they have published, up to the first prefix; an unpublished tile
+    // is read again in the next window
+    uint32_t excl = 0;
+    if (tile > 0) {
+      uint32_t polls = 0;
+      for (;;) {
+        int added = 0;
+        bool done = false, stop = false;
+#pragma unroll
+        for (int j = 0; j < kSweepWindow; ++j) {
+          const uint64_t f = x[j] & kSweepFlags;
+          if (!stop) {
+            if (f == 0) {
+              stop = true;
+            } else {
+              excl += (uint32_t)x[j];
+              ++added;
+              if (f == kSweepPrefix) done = stop = true;
+            }
+          }
+        }
+        if (done) break;
+        q -= added;
+        if (added == 0) {
+          if (++polls > kSweepSpinLimit) {
+            atomicOr(wait_flags, 1u);
+            break;
+          }
+          if (polls > 32) __nanosleep(64);
+        }
+        sweep_window(status, q, t, x);
+      }
+      store_relaxed_u64(mine, kSweepPrefix | (uint32_t)(excl + cnt));
+    }
+    gbase[t] = dstart + excl;
+    __syncthreads();
+    const uint32_t tile_kept = s_kept;
+    for (uint32_t j = t; j < tile_kept; j += kThreads) {
+      const uint32_t d = sdig[j];
+      const uint32_t o = gbase[d] + (j - tstart[d]);
+      const uint32_t k = skey[j];
+      keys_out[o] = k;
+      vals_out[o] = sval[j];
+    }
+    __syncthreads();  // the next tile reuses the shared buffers
+  }
+}
+
 // Footprint of a record: corners decided in FP32 where possible (see
 // key_decided), fractions from the FP64 coordinates; identical to footprint().
 __device__ __forceinline__ Footprint record_footprint(const DevPlan &p, const double *row,
@@ -807,6 +1105,67 @@ void radix_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *
     if (pass >= 0) shift += 8;
   }
 }
+
+// 64-bit words of look-back status that sweep_sort_kept needs for n elements
+// (tiles of kThreads * ITEMS), followed by sweep_counter_words() words of counters.
+template <int ITEMS = kSweepItems>
+int64_t sweep_status_words(int64_t n) {
+  return 256 * ((n + sweep_tile<ITEMS>() - 1) / sweep_tile<ITEMS>());
+}
+constexpr int64_t sweep_counter_words() { return 8 + (1 + kSweepMaxKeyPasses) * 256; }
+
+// The same sort as radix_sort_kept with one sweep_kernel per digit.
+// status: sweep_status_words<ITEMS>(n) words, then the counters; wait_flags:
+// the word an expired look-back wait is reported in.
+// key_offsets: the exclusive scan of the number of kept elements of each of
+// the n_keys keys.
+template <int ITEMS = kSweepItems, int MINB = kSweepMinBlocks>
+void sweep_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *&vout,
+                     const uint8_t *minor, int64_t n, uint32_t n_kept, int bits,
+                     uint32_t sentinel, const uint32_t *key_offsets, int64_t n_keys,
+                     uint64_t *status, unsigned *wait_flags, cudaStream_t s) {
+  if (n <= 0 || n_kept == 0) return;
+  const int n_key_passes = (bits + 7) / 8;
+  if (n_key_passes > kSweepMaxKeyPasses)
+    throw Error(WGPU_ERR_INVALID, "sort key wider than 32 bits");
+  constexpr int kTile = sweep_tile<ITEMS>();
+  constexpr size_t kSmem = sweep_smem<ITEMS>();
+  uint32_t *counters = (uint32_t *)(status + sweep_status_words<ITEMS>(n));
+  uint32_t *tile_counters = counters;  // one per pass
+  uint32_t *totals = counters + 8;     // per pass, 256 digits
+  WGPU_CUDA(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * sweep_counter_words(), s));
+  corner_count_kernel<<<sm_count() * 4, kThreads, 0, s>>>(kin, minor, n, sentinel, totals);
+  check_launch("corner_count_kernel");
+  key_byte_totals_kernel<<<sm_count() * 16, kThreads, 0, s>>>(key_offsets, n_keys, n_key_passes,
+                                                               totals + 256);
+  check_launch("key_byte_totals_kernel");
+  auto first = sweep_kernel<true, ITEMS, MINB>;
+  auto later = sweep_kernel<false, ITEMS, MINB>;
+  ensure_dynamic_smem((const void *)first, kSmem);
+  ensure_dynamic_smem((const void *)later, kSmem);
+  int64_t cur = n;
+  for (int pass = 0; pass <= n_key_passes; ++pass) {
+    const int64_t tiles = (cur + kTile - 1) / kTile;
+    WGPU_CUDA(cudaMemsetAsync(status, 0, sizeof(uint64_t) * 256 * tiles, s));
+    int per_sm = 0;
+    WGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, pass == 0 ? (const void *)first : (const void *)later, kThreads, kSmem));
+    const unsigned blocks =
+        (unsigned)std::min<int64_t>(tiles, (int64_t)sm_count() * std::max(per_sm, 1));
+    if (pass == 0) {
+      first<<<blocks, kThreads, kSmem, s>>>(kin, vin, minor, cur, 0, sentinel, totals, status,
+                                            tile_counters, kout, vout, wait_flags);
+    } else {
+      later<<<blocks, kThreads, kSmem, s>>>(kin, vin, nullptr, cur, 8 * (pass - 1), sentinel,
+                                            totals + 256 * pass, status, tile_counters + pass,
+                                            kout, vout, wait_flags);
+    }
+    check_launch("sweep_kernel");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+    cur = n_kept;
+  }
+}
 }  // namespace
 
 RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_t s) {
@@ -851,7 +1210,7 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  const double *d_uvw, const double *d_freq,
                                  const float *d_vis, const uint8_t *d_mask,
                                  int64_t n_rows, int64_t n_chan, bool skip_zero,
-                                 cudaStream_t s) {
+                                 unsigned *wait_flags, cudaStream_t s) {
   const int64_t n = n_rows * n_chan;
   if (n >= (int64_t)0xFFFFFFFFll)
     throw Error(WGPU_ERR_INVALID, "more than 2^32-1 visibilities in one call");
@@ -909,11 +1268,21 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                             cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
   // radix sort over the key bits in use, the unselected samples dropped
-  const int64_t n_blocks = (n + kSortTile - 1) / kSortTile;
-  uint32_t *hist = (uint32_t *)arena.get(kSlotHist, sizeof(uint32_t) * (256 * n_blocks + 1));
+  const int64_t status_words = sweep_status_words(n);
+  uint64_t *status = (uint64_t *)arena.get(
+      kSlotHist, sizeof(uint64_t) * status_words + sizeof(uint32_t) * (sweep_counter_words() + 1));
+  // without a caller's flag word, expired waits are counted in the word after the counters
+  unsigned *own_flag = (unsigned *)(status + status_words) + sweep_counter_words();
+  if (!wait_flags) WGPU_CUDA(cudaMemsetAsync(own_flag, 0, sizeof(unsigned), s));
   uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  radix_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, hist,
-                  [&](uint32_t *d, int64_t m) { exclusive_scan_u32(arena, d, m, s); }, s);
+  sweep_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, offsets, res.n_keys,
+                  status, wait_flags ? wait_flags : own_flag, s);
+  if (!wait_flags && n > 0 && total > 0) {
+    unsigned expired = 0;
+    WGPU_CUDA(cudaMemcpyAsync(&expired, own_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    if (expired) throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (bucket sort)");
+  }
   res.n_out = total;
   res.perm = vin;
   res.offsets = offsets;

@@ -314,7 +314,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
   size_t img_off = 0;
   for (Job &j : f->jobs) {
     const BucketResult br = bucket_visibilities(arena, j.dp, f->d_uvw, f->d_freq + j.c0, nullptr,
-                                                nullptr, (int64_t)n_rows, j.nch, false, s);
+                                                nullptr, (int64_t)n_rows, j.nch, false,
+                                                f->d_flags, s);
     j.n_out = br.n_out;
     j.n_keys = br.n_keys;
     j.geom = (VisRecord *)f->alloc(sizeof(VisRecord) * (br.n_out + 1));
@@ -357,7 +358,15 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     fft_prepare_rows(*f->fft, (int)j.plan.nu);
   }
 
+  // the bucketing's bounded waits report into the flag word
+  WGPU_CUDA(cudaMemcpyAsync(f->h_flags, f->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   WGPU_CUDA(cudaStreamSynchronize(s));
+  if (*f->h_flags != 0) {
+    *f->h_flags = 0;
+    WGPU_CUDA(cudaMemsetAsync(f->d_flags, 0, sizeof(unsigned), s));
+    WGPU_CUDA(cudaStreamSynchronize(s));
+    throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (bucket sort look-back)");
+  }
   f->bind_ms[1] = ms_since(t_bind);
   t_bind = Clock::now();
   // waves of (job, plane batch) pairs within the plane budget

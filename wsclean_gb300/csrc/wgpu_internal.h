@@ -180,11 +180,13 @@ void compute_w_extent(const double *d_uvw, const double *d_freq,
                       cudaStream_t s);
 
 class DeviceArena;
+// wait_flags: device word that an expired bounded wait of the sort is
+// reported in (the caller checks it); null: checked here, WGPU_ERR_TIMEOUT.
 BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
                                  const double *d_uvw, const double *d_freq,
                                  const float *d_vis, const uint8_t *d_mask,
                                  int64_t n_rows, int64_t n_chan, bool skip_zero,
-                                 cudaStream_t s);
+                                 unsigned *wait_flags, cudaStream_t s);
 
 // Bucketing with scratch in a static device array (no device allocation).
 size_t bucket_noalloc_scratch_bytes();
