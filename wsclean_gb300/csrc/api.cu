@@ -762,7 +762,7 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
     launch_degrid(g->arena, dp, b.records, b.offsets, (int)p0, nb, planes, vacc, g->d_flags, s);
   }
   g->timer.mark("finalize");
-  launch_unpermute_predict(b.records, b.perm, vacc, b.n_out, (float2 *)d_vis, s);
+  launch_unpermute_predict(b.perm, vacc, b.n_out, (float2 *)d_vis, s);
   end_call(g);
 }
 
@@ -911,7 +911,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                           g->d_flags, s);
     }
     WGPU_CUDA(cudaMemsetAsync(b->vis_out, 0, sizeof(float2) * n, s));
-    launch_unpermute_predict(b->geom, b->perm, b->vacc, b->n_out, b->vis_out, s);
+    launch_unpermute_predict(b->perm, b->vacc, b->n_out, b->vis_out, s);
   } catch (...) {
     cudaGraph_t junk;
     cudaStreamEndCapture(s, &junk);

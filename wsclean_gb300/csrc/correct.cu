@@ -111,16 +111,13 @@ __global__ void precorrect_kernel(DevPlan p, const NumT *img, const double *nu_w
   out[i] = v == 0.0f ? 0.0f : v * cx[x] * cy[y] * w_correction(p, nu_w[i], gl_zw, n_gl);
 }
 
-__global__ void unpermute_predict_kernel(const VisRecord *rec, const uint32_t *perm,
-                                         const float2 *acc, int64_t n,
+// The degridded sums (already times the conjugate of each record's phase
+// factor) back into sample order.
+__global__ void unpermute_predict_kernel(const uint32_t *perm, const float2 *acc, int64_t n,
                                          float2 *vis) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const float4 r = __ldg(reinterpret_cast<const float4 *>(rec + s));
-  const float2 a = acc[s];
-  // record holds exp(-2 pi i theta); multiply by its conjugate
-  const float c = r.x, sn = -r.y;
-  vis[perm[s]] = make_float2(a.x * c - a.y * sn, a.x * sn + a.y * c);
+  vis[__ldg(perm + s)] = acc[s];
 }
 
 // ---- K7: conjugated gains (visibilitymodifier.h:378-401) + collapse -------
@@ -376,11 +373,10 @@ void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
   check_launch("precorrect_kernel");
 }
 
-void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
-                              const float2 *acc, int64_t n, float2 *vis,
+void launch_unpermute_predict(const uint32_t *perm, const float2 *acc, int64_t n, float2 *vis,
                               cudaStream_t s) {
   if (n <= 0) return;
-  unpermute_predict_kernel<<<blocks_for(n), kThreads, 0, s>>>(rec, perm, acc, n, vis);
+  unpermute_predict_kernel<<<blocks_for(n), kThreads, 0, s>>>(perm, acc, n, vis);
   check_launch("unpermute_predict_kernel");
 }
 

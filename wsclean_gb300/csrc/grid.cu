@@ -1055,7 +1055,9 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
             sr += __shfl_xor_sync(0xffffffffu, sr, o);
             si += __shfl_xor_sync(0xffffffffu, si, o);
           }
-          if (i == 0 && pa <= pb) atomicAdd(&acc[s], make_float2(sr, si));
+          // times the conjugate of the record's phase factor (re, im)
+          if (i == 0 && pa <= pb)
+            atomicAdd(&acc[s], make_float2(fmaf(sr, a.x, si * a.y), fmaf(si, a.x, -sr * a.y)));
         }
       } else {
         // one warp per record (W > 8): lanes own footprint cells
@@ -1120,7 +1122,9 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
             sr += __shfl_xor_sync(0xffffffffu, sr, o);
             si += __shfl_xor_sync(0xffffffffu, si, o);
           }
-          if (lane == 0) atomicAdd(&acc[s], make_float2(sr, si));
+          // times the conjugate of the record's phase factor
+          if (lane == 0)
+            atomicAdd(&acc[s], make_float2(fmaf(sr, v.re, si * v.im), fmaf(si, v.re, -sr * v.im)));
         }
       }
       __syncthreads();

@@ -144,13 +144,47 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
   return warp_base + x - v;
 }
 
+// The chunk's elements as groups of four: thread t takes groups t, t + 256,
+// t + 512 and t + 768 (16-byte loads, consecutive threads on consecutive
+// groups); a group that runs past n is read element by element.
+__device__ __forceinline__ uint4 load_group(const uint32_t *d, int64_t k, int64_t n) {
+  if (k + 3 < n) return *reinterpret_cast<const uint4 *>(d + k);
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (k < n) v.x = d[k];
+  if (k + 1 < n) v.y = d[k + 1];
+  if (k + 2 < n) v.z = d[k + 2];
+  return v;
+}
+__device__ __forceinline__ void store_group(uint32_t *d, int64_t k, int64_t n, uint4 v) {
+  if (k + 3 < n) {
+    *reinterpret_cast<uint4 *>(d + k) = v;
+    return;
+  }
+  if (k < n) d[k] = v.x;
+  if (k + 1 < n) d[k + 1] = v.y;
+  if (k + 2 < n) d[k + 2] = v.z;
+}
+constexpr int kScanGroups = kScanPerThread / 4;  // groups of four per thread
+
+// ALIGNED: d is 16-byte aligned (group loads); otherwise element loads.
+template <bool ALIGNED>
 __global__ void __launch_bounds__(kScanThreads)
     scan_chunk_sums(const uint32_t *d, int64_t n, uint32_t *sums) {
   const int64_t base = (int64_t)blockIdx.x * kScanChunk;
   uint32_t s = 0;
-  for (int i = threadIdx.x; i < kScanChunk; i += kScanThreads) {
-    const int64_t k = base + i;
-    if (k < n) s += d[k];
+  if (ALIGNED) {
+    uint4 v[kScanGroups];
+#pragma unroll
+    for (int j = 0; j < kScanGroups; ++j)
+      v[j] = load_group(d, base + 4 * (threadIdx.x + kScanThreads * j), n);
+#pragma unroll
+    for (int j = 0; j < kScanGroups; ++j) s += v[j].x + v[j].y + v[j].z + v[j].w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanPerThread; ++i) {
+      const int64_t k = base + threadIdx.x + (int64_t)kScanThreads * i;
+      if (k < n) s += d[k];
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -164,8 +198,28 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+template <bool ALIGNED>
 __global__ void __launch_bounds__(kScanThreads)
     scan_chunk_local(uint32_t *d, int64_t n, const uint32_t *bases) {
+  uint32_t carry = bases ? bases[blockIdx.x] : 0u;
+  if (ALIGNED) {
+    // groups in chunk order g = t + 256 j: one block scan per j, carried over
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+    uint4 v[kScanGroups];
+#pragma unroll
+    for (int j = 0; j < kScanGroups; ++j)
+      v[j] = load_group(d, base + 4 * (threadIdx.x + kScanThreads * j), n);
+#pragma unroll
+    for (int j = 0; j < kScanGroups; ++j) {
+      uint32_t total;
+      const uint32_t ex = block_exclusive_scan(v[j].x + v[j].y + v[j].z + v[j].w, &total) + carry;
+      carry += total;
+      const uint4 o = make_uint4(ex, ex + v[j].x, ex + v[j].x + v[j].y,
+                                 ex + v[j].x + v[j].y + v[j].z);
+      store_group(d, base + 4 * (threadIdx.x + kScanThreads * j), n, o);
+    }
+    return;
+  }
   const int64_t base = (int64_t)blockIdx.x * kScanChunk +
                        (int64_t)threadIdx.x * kScanPerThread;
   uint32_t v[kScanPerThread];
@@ -177,8 +231,7 @@ __global__ void __launch_bounds__(kScanThreads)
     s += v[i];
   }
   uint32_t total;
-  uint32_t run = block_exclusive_scan(s, &total);
-  run += bases ? bases[blockIdx.x] : 0u;
+  uint32_t run = block_exclusive_scan(s, &total) + carry;
 #pragma unroll
   for (int i = 0; i < kScanPerThread; ++i) {
     const int64_t k = base + i;
@@ -189,15 +242,19 @@ __global__ void __launch_bounds__(kScanThreads)
 
 void scan_level(uint32_t *d, int64_t n, uint32_t *tmp, cudaStream_t s) {
   const int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+  const bool aligned = ((uintptr_t)d & 15) == 0;
   if (nb <= 1) {
-    scan_chunk_local<<<1, kScanThreads, 0, s>>>(d, n, nullptr);
+    (aligned ? scan_chunk_local<true> : scan_chunk_local<false>)<<<1, kScanThreads, 0, s>>>(
+        d, n, nullptr);
     check_launch("scan_chunk_local");
     return;
   }
-  scan_chunk_sums<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, tmp);
+  (aligned ? scan_chunk_sums<true> : scan_chunk_sums<false>)<<<(unsigned)nb, kScanThreads, 0,
+                                                                s>>>(d, n, tmp);
   check_launch("scan_chunk_sums");
   scan_level(tmp, nb, tmp + nb, s);
-  scan_chunk_local<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, tmp);
+  (aligned ? scan_chunk_local<true> : scan_chunk_local<false>)<<<(unsigned)nb, kScanThreads, 0,
+                                                                  s>>>(d, n, tmp);
   check_launch("scan_chunk_local");
 }
 }  // namespace

@@ -234,8 +234,9 @@ void launch_spill_fixup(const DevPlan &p, const WorkItems &wi, int p_begin, int 
 void prepare_grid_items_multi(int support);
 void launch_grid_items_multi(int support, const GridJob *d_jobs, const uint32_t *d_base,
                              int n_jobs, uint32_t total, cudaStream_t s);
-// err: device word counting staging waits that expired (reported by the
-// caller as WGPU_ERR_TIMEOUT).
+// Degridding adds into acc[s] each record's sum over the batch's planes times
+// the conjugate of its phase factor (re, im).  err: device word counting
+// staging waits that expired (reported by the caller as WGPU_ERR_TIMEOUT).
 void launch_degrid_items(const DevPlan &p, const VisRecord *rec, const uint32_t *off,
                          int p_begin, int n_batch, const WorkItems &wi, const float2 *planes,
                          float2 *acc, unsigned *err, cudaStream_t s);
@@ -324,8 +325,9 @@ void launch_scale_image(void *img, int precision_bytes, int64_t n,
                         double factor, cudaStream_t s);
 void launch_restamp(const VisRecord *geom, const uint32_t *perm, const float2 *vis,
                     int64_t n, VisRecord *out, cudaStream_t s);
-void launch_unpermute_predict(const VisRecord *rec, const uint32_t *perm,
-                              const float2 *acc, int64_t n, float2 *vis,
+// vis[perm[s]] = acc[s]: the degridded sums, which the degridding already
+// multiplied by the conjugate of each record's phase factor.
+void launch_unpermute_predict(const uint32_t *perm, const float2 *acc, int64_t n, float2 *vis,
                               cudaStream_t s);
 // Forward gains on predicted [row][chan] values -> [row][chan][n_pol]
 // (prediction write-back; same layouts and error flag as launch_apply_gains).
