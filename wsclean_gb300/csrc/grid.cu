@@ -600,24 +600,22 @@ __device__ __forceinline__ void grid_item_runs(const DevPlan &p, const VisRecord
         const float kx = st.kx[i];
         const float2 ky = st.ky2[jb];
         const float w0 = kx * ky.x, w1 = kx * ky.y;
+        // (re, im) pairs in one paired FP32 FMA each (the same roundings as
+        // two scalar FMAs)
+        const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
 #pragma unroll
         for (int k = 0; k < W; k += 2) {
           if (k + 1 < W) {
             const float4 z = *reinterpret_cast<const float4 *>(&st.vz[k]);
-            acc[0][k].x = fmaf(w0, z.x, acc[0][k].x);
-            acc[0][k].y = fmaf(w0, z.y, acc[0][k].y);
-            acc[1][k].x = fmaf(w1, z.x, acc[1][k].x);
-            acc[1][k].y = fmaf(w1, z.y, acc[1][k].y);
-            acc[0][k + 1].x = fmaf(w0, z.z, acc[0][k + 1].x);
-            acc[0][k + 1].y = fmaf(w0, z.w, acc[0][k + 1].y);
-            acc[1][k + 1].x = fmaf(w1, z.z, acc[1][k + 1].x);
-            acc[1][k + 1].y = fmaf(w1, z.w, acc[1][k + 1].y);
+            const float2 za = make_float2(z.x, z.y), zb = make_float2(z.z, z.w);
+            acc[0][k] = __ffma2_rn(w02, za, acc[0][k]);
+            acc[1][k] = __ffma2_rn(w12, za, acc[1][k]);
+            acc[0][k + 1] = __ffma2_rn(w02, zb, acc[0][k + 1]);
+            acc[1][k + 1] = __ffma2_rn(w12, zb, acc[1][k + 1]);
           } else {
             const float2 z = st.vz[k];
-            acc[0][k].x = fmaf(w0, z.x, acc[0][k].x);
-            acc[0][k].y = fmaf(w0, z.y, acc[0][k].y);
-            acc[1][k].x = fmaf(w1, z.x, acc[1][k].x);
-            acc[1][k].y = fmaf(w1, z.y, acc[1][k].y);
+            acc[0][k] = __ffma2_rn(w02, z, acc[0][k]);
+            acc[1][k] = __ffma2_rn(w12, z, acc[1][k]);
           }
         }
         ++m;
@@ -1022,34 +1020,31 @@ __global__ void __launch_bounds__(kThreads, W <= 8 ? 5 : 3)
             kw = p.n_planes == 1 ? (i == 0 ? 1.0f : 0.0f)
                                  : es_eval(p.beta, (b.x + (float)i) * inv_half);
           }
-          float kvj[W];
+          float2 kvj[W];  // the v weights as (w, w) pairs for paired FMAs
 #pragma unroll
-          for (int j = 0; j < W; ++j) kvj[j] = __shfl_sync(0xffffffffu, kv, gbase + j);
+          for (int j = 0; j < W; ++j) {
+            const float k = __shfl_sync(0xffffffffu, kv, gbase + j);
+            kvj[j] = make_float2(k, k);
+          }
           // the union of the four records' planes; each group reads only its
           // own footprint cells (rows outside every footprint may hold
           // anything in prediction)
           const int qa = __reduce_min_sync(0xffffffffu, pa <= pb ? pa : 0x7fffffff);
           const int qb = __reduce_max_sync(0xffffffffu, pa <= pb ? pb : -0x7fffffff);
           const float2 *col = halo + iv_rel * RS + iu_rel + i;
-          float sr = 0.f, si = 0.f;
+          float2 s2 = make_float2(0.f, 0.f);
           for (int q = qa; q <= qb; ++q) {
             const int dz = q - ip;
             const float kwq = __shfl_sync(0xffffffffu, kw, gbase + min(max(dz, 0), 7));
             if (q >= pa && q <= pb && i < W) {
               const float2 *c = col + (q - q0) * kPlane;
-              float cr = 0.f, cim = 0.f;
+              float2 cc = make_float2(0.f, 0.f);
 #pragma unroll
-              for (int j = 0; j < W; ++j) {
-                const float2 gv = c[j * RS];
-                cr = fmaf(kvj[j], gv.x, cr);
-                cim = fmaf(kvj[j], gv.y, cim);
-              }
-              sr = fmaf(kwq, cr, sr);
-              si = fmaf(kwq, cim, si);
+              for (int j = 0; j < W; ++j) cc = __ffma2_rn(kvj[j], c[j * RS], cc);
+              s2 = __ffma2_rn(make_float2(kwq, kwq), cc, s2);
             }
           }
-          sr *= ku;
-          si *= ku;
+          float sr = s2.x * ku, si = s2.y * ku;
 #pragma unroll
           for (int o = 4; o > 0; o >>= 1) {
             sr += __shfl_xor_sync(0xffffffffu, sr, o);
