@@ -694,7 +694,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
         kr[r] = keys_in[i];
         vr[r] = vals_in[i];
         if (FIRST) {
-          if (kr[r] != drop_key) d = minor[i];
+          const uint32_t m = minor[i];  // loaded with the key, not after it
+          d = kr[r] != drop_key ? m : 256u;
         } else {
           d = (kr[r] >> shift) & 255u;
         }
