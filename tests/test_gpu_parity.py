@@ -547,12 +547,14 @@ def test_row_length_6912_inversion_and_prediction(wgpu_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("n_chan,order", [(24, "ascending"), (24, "descending"), (24, "shuffled"),
-                                          (8, "ascending"), (64, "ascending")])
+                                          (24, "repeated"), (8, "ascending"), (64, "ascending")])
 def test_device_w_extent_gives_the_host_plan(wgpu_lib, n_chan, order):
     """The w range a call plans from (the device extent pass over the selected
     samples) equals the host's FP64 extent exactly, so the call's plan is the
     host plan bit for bit, for inversions (zero visibilities skipped) and
-    masked predictions, with ascending, descending and unordered channels."""
+    masked predictions, with ascending, descending, unordered and repeated
+    channel frequencies, with 16 or more channels (one warp per row, two
+    products per row) and with fewer (one product per sample)."""
     W, dl = 192, 3e-4
     uvw, freq, vis = synthetic.random_points(900, n_chan, W, dl, seed=71, w_scale=3.0,
                                              frac_zero=0.3)
@@ -560,6 +562,8 @@ def test_device_w_extent_gives_the_host_plan(wgpu_lib, n_chan, order):
         freq = freq[::-1].copy()
     elif order == "shuffled":
         freq = np.random.default_rng(5).permutation(freq)
+    elif order == "repeated":  # equal frequencies: ranks tie-broken by channel
+        freq = np.random.default_rng(6).permutation(np.repeat(freq[: n_chan // 3], 3))
     vis[:40] = 0  # whole rows without a sample
     g = WGriddingGridder_Simple(W, W, W, W, dl, dl, 0.0, 0.0, 1, epsilon=1e-4)
     g.InitializeInversion()

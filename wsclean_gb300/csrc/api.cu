@@ -644,7 +644,8 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   double w_min, w_max;
   int64_t count;
   compute_w_extent(d_uvw, d_freq, d_vis, nullptr, (int64_t)n_rows, (int64_t)n_chan, true,
-                   &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
+                   &w_min, &w_max, &count,
+                   g->arena.get(kSlotErr, w_extent_scratch_bytes((int64_t)n_chan)), s);
   if (count == 0) {
     end_call(g);
     return;
@@ -710,7 +711,8 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   double w_min, w_max;
   int64_t count;
   compute_w_extent(d_uvw, d_freq, nullptr, d_mask, (int64_t)n_rows, (int64_t)n_chan, false,
-                   &w_min, &w_max, &count, g->arena.get(kSlotErr, 64), s);
+                   &w_min, &w_max, &count,
+                   g->arena.get(kSlotErr, w_extent_scratch_bytes((int64_t)n_chan)), s);
   if (d_mask) {
     WGPU_CUDA(cudaMemsetAsync(d_vis, 0, sizeof(float2) * n_rows * n_chan, s));
     if (count == 0) {
@@ -789,7 +791,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   double w_min, w_max;
   int64_t count;
   compute_w_extent(b->uvw, b->freq, nullptr, b->mask, b->n_rows, b->n_chan, false, &w_min,
-                   &w_max, &count, g->arena.get(kSlotErr, 64), s);
+                   &w_max, &count, g->arena.get(kSlotErr, w_extent_scratch_bytes(b->n_chan)), s);
   if (count == 0) throw Error(WGPU_ERR_INVALID, "the mask selects no visibility");
   BoundState *bs = b.get();
   b->plan = g->tuning ? tuned_plan(g, 'b', w_min, w_max, count,

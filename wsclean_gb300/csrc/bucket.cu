@@ -26,6 +26,8 @@ namespace wgpu {
 namespace {
 
 constexpr int kThreads = 256;
+// channel counts for which the w extent runs one warp per row
+constexpr int64_t kExtentRowsMinChan = 16, kExtentRowsMaxChan = 2048;
 
 struct ChannelScale {
   double su, sv, sw;  // U = uvw_u * su (cells), V = uvw_v * sv, w = uvw_w * sw
@@ -288,6 +290,100 @@ __global__ void __launch_bounds__(kThreads)
     wmin = fmin(wmin, wl);
     wmax = fmax(wmax, wl);
     ++cnt;
+  }
+  typedef cub::BlockReduce<double, kThreads> BR;
+  typedef cub::BlockReduce<unsigned long long, kThreads> BRU;
+  __shared__ union {
+    typename BR::TempStorage d;
+    typename BRU::TempStorage u;
+  } tmp;
+  const double bmin = BR(tmp.d).Reduce(wmin, MinOp());
+  __syncthreads();
+  const double bmax = BR(tmp.d).Reduce(wmax, MaxOp());
+  __syncthreads();
+  const unsigned long long bcnt = BRU(tmp.u).Sum(cnt);
+  if (threadIdx.x == 0) {
+    if (bcnt > 0) {
+      atomicMin(&out[0], dkey(bmin));
+      atomicMax(&out[1], dkey(bmax));
+      atomicAdd(&out[2], bcnt);
+    }
+  }
+}
+
+// Rank of each channel among the channels by frequency (ties by index), and
+// 1/wavelength of the channels in rank order.  1/wavelength = f / c rounded
+// is non-decreasing in f, so rank order is 1/wavelength order.
+__global__ void channel_rank_kernel(const double *__restrict__ freq, int n_chan, int *rank,
+                                    double *by_rank) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chan) return;
+  const double f = freq[c];
+  int r = 0;
+  for (int j = 0; j < n_chan; ++j) {
+    const double g = freq[j];
+    r += (g < f || (g == f && j < c)) ? 1 : 0;
+  }
+  rank[c] = r;
+  by_rank[r] = __ddiv_rn(f, kSpeedOfLight);
+}
+
+// The same extent as w_extent_kernel with one warp per row: the row's
+// selected channels give their lowest and highest rank, and only those two
+// products are formed.  fl(w x) is monotone in x (non-decreasing for w >= 0,
+// non-increasing below), so they are the row's extreme products, bit for bit.
+// Shared memory: n_chan doubles (1/wavelength by rank), then n_chan ints (ranks).
+__global__ void __launch_bounds__(kThreads)
+    w_extent_rows_kernel(const double *uvw, const int *__restrict__ rank_g,
+                         const double *__restrict__ by_rank_g, Selector sel, int64_t n_rows,
+                         int n_chan, unsigned long long *out /*[3]: min key, max key, count*/) {
+  extern __shared__ double by_rank[];
+  int *rank = reinterpret_cast<int *>(by_rank + n_chan);
+  for (int c = threadIdx.x; c < n_chan; c += blockDim.x) {
+    by_rank[c] = by_rank_g[c];
+    rank[c] = rank_g[c];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double wmin = 1e300, wmax = -1e300;
+  unsigned long long cnt = 0;
+  // kRows consecutive rows per warp step, their loads issued together
+  constexpr int kRows = 4;
+  for (int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRows; r0 < n_rows;
+       r0 += n_warps * kRows) {
+    double w[kRows];
+    unsigned lo[kRows], hi[kRows], k[kRows];
+#pragma unroll
+    for (int j = 0; j < kRows; ++j) {
+      w[j] = r0 + j < n_rows ? uvw[3 * (r0 + j) + 2] : 0.0;
+      lo[j] = 0xffffffffu;
+      hi[j] = 0u;
+      k[j] = 0u;
+    }
+    for (int c = lane; c < n_chan; c += 32) {
+      const unsigned q = (unsigned)rank[c];
+#pragma unroll
+      for (int j = 0; j < kRows; ++j) {
+        if (r0 + j < n_rows && sel((r0 + j) * n_chan + c)) {
+          lo[j] = min(lo[j], q);
+          hi[j] = max(hi[j], q);
+          ++k[j];
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kRows; ++j) {
+      const unsigned l = __reduce_min_sync(0xffffffffu, lo[j]);
+      const unsigned h = __reduce_max_sync(0xffffffffu, hi[j]);
+      const unsigned kk = __reduce_add_sync(0xffffffffu, k[j]);
+      if (kk > 0 && lane == 0) {
+        const double a = __dmul_rn(w[j], by_rank[l]), b = __dmul_rn(w[j], by_rank[h]);
+        wmin = fmin(wmin, fmin(a, b));
+        wmax = fmax(wmax, fmax(a, b));
+        cnt += kk;
+      }
+    }
   }
   typedef cub::BlockReduce<double, kThreads> BR;
   typedef cub::BlockReduce<unsigned long long, kThreads> BRU;
@@ -1177,6 +1273,10 @@ RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_
   return o;
 }
 
+size_t w_extent_scratch_bytes(int64_t n_chan) {
+  return 64 + (sizeof(int) + sizeof(double)) * (size_t)(n_chan + 2);
+}
+
 void compute_w_extent(const double *d_uvw, const double *d_freq,
                       const float *d_vis, const uint8_t *d_mask, int64_t n_rows,
                       int64_t n_chan, bool skip_zero, double *w_min,
@@ -1188,7 +1288,18 @@ void compute_w_extent(const double *d_uvw, const double *d_freq,
   const int64_t n = n_rows * n_chan;
   unsigned blocks = (unsigned)std::min<int64_t>(grid_for(n, kThreads), (int64_t)sm_count() * 8);
   const Selector sel{skip_zero ? (const float2 *)d_vis : nullptr, d_mask};
-  if (n_chan <= 4096) {
+  if (n_chan >= kExtentRowsMinChan && n_chan <= kExtentRowsMaxChan) {
+    // one warp per row, two products per row
+    int *rank = (int *)(d + 8);
+    double *by_rank = (double *)(rank + ((n_chan + 1) & ~(int64_t)1));
+    channel_rank_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, (int)n_chan, rank, by_rank);
+    check_launch("channel_rank_kernel");
+    const unsigned rblocks =
+        (unsigned)std::min<int64_t>((n_rows + kThreads / 8 - 1) / (kThreads / 8),
+                                    (int64_t)sm_count() * 8);
+    w_extent_rows_kernel<<<rblocks, kThreads, (sizeof(double) + sizeof(int)) * n_chan, s>>>(
+        d_uvw, rank, by_rank, sel, n_rows, (int)n_chan, d);
+  } else if (n_chan <= 4096) {
     w_extent_kernel<true><<<blocks, kThreads, sizeof(double) * n_chan, s>>>(d_uvw, d_freq, sel,
                                                                            n_rows, n_chan, d);
   } else {

@@ -264,7 +264,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     double w_min, w_max;
     int64_t count;
     compute_w_extent(f->d_uvw, f->d_freq + c0, nullptr, nullptr, (int64_t)n_rows, nch, false,
-                     &w_min, &w_max, &count, arena.get(kSlotErr, 64), s);
+                     &w_min, &w_max, &count, arena.get(kSlotErr, w_extent_scratch_bytes(nch)), s);
     for (const wgpu_facet_t &fc : f->facets) {
       Job j;
       j.facet = fc;

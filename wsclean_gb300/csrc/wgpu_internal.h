@@ -172,7 +172,9 @@ struct BucketResult {
 // and returns the view on the copy.
 RowOccupancy copy_row_occupancy(const RowOccupancy &rows, void *dst, cudaStream_t s);
 // Extents of the (non-zero when skip_zero) visibilities: w min/max in
-// wavelengths and the count.
+// wavelengths and the count.  scratch8: w_extent_scratch_bytes(n_chan) bytes
+// of device memory.
+size_t w_extent_scratch_bytes(int64_t n_chan);
 void compute_w_extent(const double *d_uvw, const double *d_freq,
                       const float *d_vis, const uint8_t *d_mask, int64_t n_rows,
                       int64_t n_chan, bool skip_zero, double *w_min,
