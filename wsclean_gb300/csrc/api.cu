@@ -114,7 +114,7 @@ struct BoundState {
   wgpu::RowOccupancy rows_occ;  // rows the bound set's footprints touch
   float2 *vis_in = nullptr, *vis_out = nullptr, *vacc = nullptr;
   float2 *planes = nullptr, *rows = nullptr, *acc = nullptr;
-  float *img_corr = nullptr, *cx = nullptr, *cy = nullptr, *gl = nullptr;
+  float *img_corr = nullptr, *cx = nullptr, *cy = nullptr, *gl = nullptr, *wcorr = nullptr;
   std::vector<wgpu::WorkItems> gitems, ditems;
   cudaGraph_t ginv = nullptr, gpred = nullptr;
   cudaGraphExec_t xinv = nullptr, xpred = nullptr;
@@ -154,6 +154,7 @@ struct wgpu_gridder {
   std::string corr_key;  // geometry of the correction tables in the arena
   std::string nuw_key;   // geometry (and buffer) of the n - 1 table in the arena
   std::string scr_key;   // plan (and buffer) of the w-screen terms in the arena
+  std::string wcorr_key; // plan (and buffers) of the w-correction table in the arena
   std::unique_ptr<BoundState> bound;
   std::vector<wgpu_tuning_trial_t> last_trials;  // candidates timed by the last tuning
   double plane_budget = 0;  // >0 caps the plane-batch bytes of every plan
@@ -365,6 +366,21 @@ ScreenTable screen_table_for(wgpu_gridder *g, const wgpu_plan_t &plan, const Dev
     g->scr_key = key;
   }
   return scr;
+}
+
+// Per-pixel w correction of the plan, in the arena; recomputed only when the
+// plan's w planes, kernel or the buffers change.
+const float *wcorr_table_for(wgpu_gridder *g, const wgpu_plan_t &plan, const DevPlan &dp,
+                             const double *nu_w, const float *gl) {
+  float *wc = (float *)g->arena.get(kSlotWCorr, sizeof(float) * plan.width * plan.height);
+  char key[480];
+  std::snprintf(key, sizeof(key), "%s/%p/%p/%.17g/%.17g/%d/%lld", g->nuw_key.c_str(), (void *)wc,
+                (const void *)gl, dp.dw, (double)dp.beta, dp.support, (long long)dp.n_planes);
+  if (g->wcorr_key != key) {
+    launch_wcorr_table(dp, nu_w, gl, kGlNodes, wc, g->stream);
+    g->wcorr_key = key;
+  }
+  return wc;
 }
 
 // A pinned plan is used as long as it covers the data: every visibility's w
@@ -695,7 +711,8 @@ void invert_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   g->timer.mark("finalize");
   float *cx, *cy, *gl;
   upload_corrections(g, plan, &cx, &cy, &gl);
-  launch_finalize_add(dp, acc, nu_w, cx, cy, gl, kGlNodes, g->d_img, g->prec, s);
+  launch_finalize_add(dp, acc, wcorr_table_for(g, plan, dp, nu_w, gl), cx, cy, g->d_img, g->prec,
+                      s);
   end_call(g);
 }
 
@@ -747,7 +764,8 @@ void predict_device(wgpu_gridder *g, size_t n_rows, size_t n_chan,
   float2 *R = (float2 *)g->arena.get(kSlotRows, sizeof(float2) * B * plan.nv * rstride);
   float *cx, *cy, *gl;
   upload_corrections(g, plan, &cx, &cy, &gl);
-  launch_precorrect(dp, g->d_img, g->prec, nu_w, cx, cy, gl, kGlNodes, img_corr, s);
+  launch_precorrect(dp, g->d_img, g->prec, wcorr_table_for(g, plan, dp, nu_w, gl), cx, cy,
+                    img_corr, s);
   WGPU_CUDA(cudaMemsetAsync(vacc, 0, sizeof(float2) * (b.n_out + 1), s));
   for (int64_t p0 = 0; p0 < plan.n_planes; p0 += B) {
     const int nb = (int)std::min<int64_t>(B, plan.n_planes - p0);
@@ -802,9 +820,11 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
                       : plan_for(g, w_min, w_max, count);
   if (g->tuning) {
     // the bound set owns its batch buffers: drop the ones the timing runs used
-    for (int slot : {kSlotPlanes, kSlotRows, kSlotAcc, kSlotImgCorr, kSlotVisAcc, kSlotScreen})
+    for (int slot : {kSlotPlanes, kSlotRows, kSlotAcc, kSlotImgCorr, kSlotVisAcc, kSlotScreen,
+                     kSlotWCorr})
       g->arena.release(slot);
     g->scr_key.clear();
+    g->wcorr_key.clear();
   }
   g->last_plan = b->plan;
   log_plan(g, "bind", b->plan, count);
@@ -847,6 +867,8 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   WGPU_CUDA(cudaMemcpyAsync(b->cx, cx, sizeof(float) * plan.width, cudaMemcpyDeviceToDevice, s));
   WGPU_CUDA(cudaMemcpyAsync(b->cy, cy, sizeof(float) * plan.height, cudaMemcpyDeviceToDevice, s));
   WGPU_CUDA(cudaMemcpyAsync(b->gl, gl, sizeof(float) * 2 * kGlNodes, cudaMemcpyDeviceToDevice, s));
+  b->wcorr = (float *)b->alloc(sizeof(float) * npix);
+  launch_wcorr_table(dp, b->nu_w, b->gl, kGlNodes, b->wcorr, s);
   // twiddle tables are created outside the capture (they are copied synchronously)
   fft_twiddles(*g->fft, (int)plan.nu);
   fft_twiddles(*g->fft, (int)plan.nv);
@@ -881,7 +903,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
       launch_fft_cols_b_forward_accumulate(*g->fft, dp, (int)plan.fft_n1, (int)plan.fft_n2,
                                            b->rows, rstride, nb, p0, b->scr, b->acc, sel, s);
     }
-    launch_finalize_add(dp, b->acc, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, g->d_img, g->prec, s);
+    launch_finalize_add(dp, b->acc, b->wcorr, b->cx, b->cy, g->d_img, g->prec, s);
   } catch (...) {
     cudaGraph_t junk;
     cudaStreamEndCapture(s, &junk);
@@ -897,7 +919,7 @@ void bind_visibilities(wgpu_gridder *g, size_t n_rows, size_t n_chan, const doub
   k0 = thread_launch_count();
   WGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   try {
-    launch_precorrect(dp, g->d_img, g->prec, b->nu_w, b->cx, b->cy, b->gl, kGlNodes, b->img_corr, s);
+    launch_precorrect(dp, g->d_img, g->prec, b->wcorr, b->cx, b->cy, b->img_corr, s);
     WGPU_CUDA(cudaMemsetAsync(b->vacc, 0, sizeof(float2) * (b->n_out + 1), s));
     for (size_t i = 0; i < b->ditems.size(); ++i) {
       const int p0 = (int)(i * B);

@@ -87,28 +87,35 @@ __device__ __forceinline__ float w_correction(const DevPlan &p, double nu,
   return 1.0f / ((float)p.support * acc);
 }
 
+// The w correction of every pixel, once per plan (finalize_add_kernel and
+// precorrect_kernel read it).
+__global__ void wcorr_table_kernel(DevPlan p, const double *nu_w, const float *gl_zw, int n_gl,
+                                   float *wcorr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)p.width * p.height) return;
+  wcorr[i] = w_correction(p, nu_w[i], gl_zw, n_gl);
+}
+
 template <typename NumT>
 __global__ void finalize_add_kernel(DevPlan p, const float2 *acc,
-                                    const double *nu_w, const float *cx,
-                                    const float *cy, const float *gl_zw,
-                                    int n_gl, NumT *img) {
+                                    const float *wcorr, const float *cx,
+                                    const float *cy, NumT *img) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)p.width * p.height) return;
   const int x = (int)(i % p.width), y = (int)(i / p.width);
   const float2 a = acc[i];
-  const float v = (a.x - a.y) * cx[x] * cy[y] * w_correction(p, nu_w[i], gl_zw, n_gl);
+  const float v = (a.x - a.y) * cx[x] * cy[y] * wcorr[i];
   img[i] += (NumT)v;
 }
 
 template <typename NumT>
-__global__ void precorrect_kernel(DevPlan p, const NumT *img, const double *nu_w,
-                                  const float *cx, const float *cy,
-                                  const float *gl_zw, int n_gl, float *out) {
+__global__ void precorrect_kernel(DevPlan p, const NumT *img, const float *wcorr,
+                                  const float *cx, const float *cy, float *out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)p.width * p.height) return;
   const int x = (int)(i % p.width), y = (int)(i / p.width);
   const float v = (float)img[i];
-  out[i] = v == 0.0f ? 0.0f : v * cx[x] * cy[y] * w_correction(p, nu_w[i], gl_zw, n_gl);
+  out[i] = v == 0.0f ? 0.0f : v * cx[x] * cy[y] * wcorr[i];
 }
 
 // The degridded sums (already times the conjugate of each record's phase
@@ -349,27 +356,32 @@ void launch_screen_table(const DevPlan &p, const double *nu_w, const ScreenTable
   check_launch("screen_table_kernel");
 }
 
-void launch_finalize_add(const DevPlan &p, const float2 *acc,
-                         const double *nu_w, const float *cx, const float *cy,
-                         const float *gl_zw, int n_gl, void *img,
-                         int precision_bytes, cudaStream_t s) {
+void launch_wcorr_table(const DevPlan &p, const double *nu_w, const float *gl_zw, int n_gl,
+                        float *wcorr, cudaStream_t s) {
+  const int64_t n = (int64_t)p.width * p.height;
+  wcorr_table_kernel<<<blocks_for(n), kThreads, 0, s>>>(p, nu_w, gl_zw, n_gl, wcorr);
+  check_launch("wcorr_table_kernel");
+}
+
+void launch_finalize_add(const DevPlan &p, const float2 *acc, const float *wcorr,
+                         const float *cx, const float *cy, void *img, int precision_bytes,
+                         cudaStream_t s) {
   const int64_t n = (int64_t)p.width * p.height;
   if (precision_bytes == 8)
-    finalize_add_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, acc, nu_w, cx, cy, gl_zw, n_gl, (double *)img);
+    finalize_add_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, acc, wcorr, cx, cy, (double *)img);
   else
-    finalize_add_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, acc, nu_w, cx, cy, gl_zw, n_gl, (float *)img);
+    finalize_add_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, acc, wcorr, cx, cy, (float *)img);
   check_launch("finalize_add_kernel");
 }
 
 void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
-                       const double *nu_w, const float *cx, const float *cy,
-                       const float *gl_zw, int n_gl, float *img_corr,
+                       const float *wcorr, const float *cx, const float *cy, float *img_corr,
                        cudaStream_t s) {
   const int64_t n = (int64_t)p.width * p.height;
   if (precision_bytes == 8)
-    precorrect_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, (const double *)img, nu_w, cx, cy, gl_zw, n_gl, img_corr);
+    precorrect_kernel<double><<<blocks_for(n), kThreads, 0, s>>>(p, (const double *)img, wcorr, cx, cy, img_corr);
   else
-    precorrect_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, (const float *)img, nu_w, cx, cy, gl_zw, n_gl, img_corr);
+    precorrect_kernel<float><<<blocks_for(n), kThreads, 0, s>>>(p, (const float *)img, wcorr, cx, cy, img_corr);
   check_launch("precorrect_kernel");
 }
 

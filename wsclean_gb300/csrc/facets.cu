@@ -65,7 +65,7 @@ struct Job {
   float2 *acc = nullptr;
   double *nu_w = nullptr;
   ScreenTable scr;
-  float *cx = nullptr, *cy = nullptr, *gl = nullptr;
+  float *cx = nullptr, *cy = nullptr, *gl = nullptr, *wcorr = nullptr;
   float *img = nullptr;  // width * height, row-major
   std::vector<WorkItems> items;  // per plane batch
   int rstride = 0;
@@ -339,6 +339,8 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
     j.cy = (float *)f->alloc(sizeof(float) * j.plan.height);
     j.gl = (float *)f->alloc(sizeof(float) * 2 * kCorrGlNodes);
     launch_correction_tables(j.plan, j.cx, j.cy, j.gl, s);
+    j.wcorr = (float *)f->alloc(sizeof(float) * npix);
+    launch_wcorr_table(j.dp, j.nu_w, j.gl, kCorrGlNodes, j.wcorr, s);
     j.img = f->d_images + img_off;
     img_off += j.facet.width * j.facet.height;
     wgpu_facets *fp = f;
@@ -502,7 +504,7 @@ void bind_facets(wgpu_facets *f, size_t n_rows, size_t n_chan, const double *uvw
       }
     }
     for (Job &j : f->jobs)
-      launch_finalize_add(j.dp, j.acc, j.nu_w, j.cx, j.cy, j.gl, kCorrGlNodes, j.img, 4, s);
+      launch_finalize_add(j.dp, j.acc, j.wcorr, j.cx, j.cy, j.img, 4, s);
   } catch (...) {
     cudaGraph_t junk = nullptr;
     cudaStreamEndCapture(s, &junk);

@@ -956,7 +956,7 @@ __global__ void __launch_bounds__(kPanelThreads)
 }
 
 // Shared bytes of the two-stage pass B kernels: the FFT buffer (n2 * kPanel
-// float2) and the phase terms a, bh, bl (n2 * kPanel floats each).
+// float2) and the screen terms a, k, r (n2 * kPanel words each).
 __host__ __device__ constexpr size_t cols_b16_smem(int n2) {
   return (size_t)n2 * kPanel * (sizeof(float2) + 3 * sizeof(float));
 }
@@ -1056,7 +1056,7 @@ __global__ void __launch_bounds__(kPanelThreads, 2)
       if (x < p.width && y >= 0) val[t] = __ldg(img_corr + (size_t)y * p.width + x);
     }
   }
-  __syncthreads();  // phase terms
+  __syncthreads();  // screen terms
   for (int b = 0; b < n_batch; ++b) {
     float2 *base = R + (size_t)b * nv * rstride + (size_t)N * k1 * rstride + cg * kPanel;
     auto load = [&](int t, int e, int c) -> float2 {

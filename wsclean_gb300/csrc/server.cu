@@ -91,7 +91,7 @@ double estimate_bytes(const wgpu_request_t &r, double plane_budget) {
                        ((double)p.tile * p.tile);
   const double planes = (double)p.plane_batch * 8.0 * (double)p.nu * (double)p.nv * (1.0 + spill);
   const double rows = (double)p.plane_batch * 8.0 * (double)p.nv * (double)((p.width + 31) / 32 * 32);
-  const double img = 36.0 * (double)r.width * (double)r.height;
+  const double img = 40.0 * (double)r.width * (double)r.height;
   const double keys = 4.0 * (double)(p.nu / p.tile) * (double)(p.nv / p.tile) * 4.0 * (double)p.n_planes;
   return 64.0 * n + 24.0 * (double)r.n_rows + planes + rows + img + keys + 64e6;
 }

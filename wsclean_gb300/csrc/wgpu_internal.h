@@ -313,15 +313,18 @@ void launch_nu_table(const DevPlan &p, double *nu_w, cudaStream_t s);
 // The screen terms of plan p from its n - 1 - c_n table (FP64, once per plan).
 void launch_screen_table(const DevPlan &p, const double *nu_w, const ScreenTable &scr,
                          cudaStream_t s);
-// tdirty * corr added into the accumulated image (float or double).
-void launch_finalize_add(const DevPlan &p, const float2 *acc,
-                         const double *nu_w, const float *cx, const float *cy,
-                         const float *gl_zw, int n_gl, void *img,
-                         int precision_bytes, cudaStream_t s);
+// The per-pixel w correction 1 / psihat(dw (n - 1 - c_n)) of plan p, from its
+// n - 1 - c_n table and the n_gl quadrature nodes gl_zw (once per plan).
+void launch_wcorr_table(const DevPlan &p, const double *nu_w, const float *gl_zw, int n_gl,
+                        float *wcorr, cudaStream_t s);
+// tdirty * corr added into the accumulated image (float or double); corr =
+// cx[x] cy[y] wcorr[pixel].
+void launch_finalize_add(const DevPlan &p, const float2 *acc, const float *wcorr,
+                         const float *cx, const float *cy, void *img, int precision_bytes,
+                         cudaStream_t s);
 // img * corr -> img_corr (prediction pre-correction).
 void launch_precorrect(const DevPlan &p, const void *img, int precision_bytes,
-                       const double *nu_w, const float *cx, const float *cy,
-                       const float *gl_zw, int n_gl, float *img_corr,
+                       const float *wcorr, const float *cx, const float *cy, float *img_corr,
                        cudaStream_t s);
 void launch_scale_image(void *img, int precision_bytes, int64_t n,
                         double factor, cudaStream_t s);
@@ -483,6 +486,7 @@ enum ArenaSlot {
   kSlotResampleTrim,  // and at the trimmed size
   kSlotCorner,        // bucketing: footprint corner within the tile, per sample
   kSlotScreen,        // per-pixel w-screen terms of the current plan
+  kSlotWCorr,         // per-pixel w correction of the current plan
 };
 
 // Exclusive scan of n uint32 values in place (device), returning the total.
