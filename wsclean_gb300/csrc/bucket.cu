@@ -333,7 +333,7 @@ __global__ void channel_rank_kernel(const double *__restrict__ freq, int n_chan,
 // products are formed.  fl(w x) is monotone in x (non-decreasing for w >= 0,
 // non-increasing below), so they are the row's extreme products, bit for bit.
 // Shared memory: n_chan doubles (1/wavelength by rank), then n_chan ints (ranks).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     w_extent_rows_kernel(const double *uvw, const int *__restrict__ rank_g,
                          const double *__restrict__ by_rank_g, Selector sel, int64_t n_rows,
                          int n_chan, unsigned long long *out /*[3]: min key, max key, count*/) {
@@ -361,14 +361,28 @@ __global__ void __launch_bounds__(kThreads)
       hi[j] = 0u;
       k[j] = 0u;
     }
-    for (int c = lane; c < n_chan; c += 32) {
-      const unsigned q = (unsigned)rank[c];
+    // 64 channels of the kRows rows per round: every selection load of the
+    // round is issued before any is used
+    for (int c0 = 0; c0 < n_chan; c0 += 64) {
+      bool on[kRows][2];
 #pragma unroll
-      for (int j = 0; j < kRows; ++j) {
-        if (r0 + j < n_rows && sel((r0 + j) * n_chan + c)) {
-          lo[j] = min(lo[j], q);
-          hi[j] = max(hi[j], q);
-          ++k[j];
+      for (int j = 0; j < kRows; ++j)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int c = c0 + 32 * u + lane;
+          on[j][u] = r0 + j < n_rows && c < n_chan && sel((r0 + j) * n_chan + c);
+        }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int c = c0 + 32 * u + lane;
+        const unsigned q = c < n_chan ? (unsigned)rank[c] : 0u;
+#pragma unroll
+        for (int j = 0; j < kRows; ++j) {
+          if (on[j][u]) {
+            lo[j] = min(lo[j], q);
+            hi[j] = max(hi[j], q);
+            ++k[j];
+          }
         }
       }
     }
