@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   uint32_t *skey = sweep_smem + (kThreads / 32) * 256;
   uint32_t *sval = skey + kTile;
   uint8_t *sdig = reinterpret_cast<uint8_t *>(sval + kTile);
-  __shared__ uint32_t tstart[256], gbase[256], wsum[kThreads / 32];
+  __shared__ uint32_t gbase[256], wsum[kThreads / 32];
   __shared__ uint32_t s_tile, s_kept;
   static_assert(kThreads == 256, "one thread per digit");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, t = threadIdx.x;
@@ -841,15 +841,17 @@ __global__ void __launch_bounds__(kThreads, MINB)
     if (tile > 0) sweep_window(status, q, t, x);
     uint32_t kept;
     const uint32_t first = sweep_block_scan(cnt, wsum, &kept);
-    tstart[t] = first;
+    // each warp's first tile position of digit t
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) wcnt[w][t] += first;
     if (t == 0) s_kept = kept;
-    __syncthreads();  // tile positions and warp offsets of every digit
+    __syncthreads();  // tile positions of every digit
     // the tile in digit order in shared memory
 #pragma unroll
     for (int r = 0; r < ITEMS; ++r) {
       const uint32_t d = dr[r] >> 16;
       if (d < 256) {
-        const uint32_t pos = tstart[d] + wcnt[warp][d] + (dr[r] & 0xffffu);
+        const uint32_t pos = wcnt[warp][d] + (dr[r] & 0xffffu);
         skey[pos] = kr[r];
         sval[pos] = vr[r];
         sdig[pos] = (uint8_t)d;
@@ -890,12 +892,14 @@ __global__ void __launch_bounds__(kThreads, MINB)
       }
       store_relaxed_u64(mine, kSweepPrefix | (uint32_t)(excl + cnt));
     }
-    gbase[t] = dstart + excl;
+    // output position of tile position j of digit d: gbase[d] + j (the
+    // tile's first position of the digit taken off, modulo 2^32)
+    gbase[t] = dstart + excl - first;
     __syncthreads();
     const uint32_t tile_kept = s_kept;
     for (uint32_t j = t; j < tile_kept; j += kThreads) {
       const uint32_t d = sdig[j];
-      const uint32_t o = gbase[d] + (j - tstart[d]);
+      const uint32_t o = gbase[d] + j;
       const uint32_t k = skey[j];
       keys_out[o] = k;
       vals_out[o] = sval[j];
