@@ -433,9 +433,12 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t key = sentinel;
   uint8_t cb = 0;
   bool defer = false;
+  // the row and channel terms are loaded with the selection, not after it
+  const float4 rf = row_float(uvwf, uvw, r);
+  const ChannelScale sc = cs[c];
   if (sel(e)) {
     int iu, iv, ip;
-    if (key_decided(p, row_float(uvwf, uvw, r), cs[c], &key, &iu, &iv, &ip)) {
+    if (key_decided(p, rf, sc, &key, &iu, &iv, &ip)) {
       if (corners) corners[(size_t)ip * p.nv + iv] = 1;
       cb = corner_byte(iu, iv);
     } else {
