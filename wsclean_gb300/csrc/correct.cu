@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "polarization.cuh"
+#include "screen.cuh"
 #include "wgpu_internal.h"
 
 namespace wgpu {
@@ -28,26 +29,17 @@ __global__ void nu_table_kernel(DevPlan p, double *nu_w) {
   nu_w[i] = nm1 - p.nm1_center;
 }
 
-// w-screen terms per pixel: the screen of plane q, w_q = w0 + q dw, is
-// exp(-+2 pi i w_q nu), the per-plane screen of ducc0's w-gridding behind
-// ms2dirty / dirty2ms (wgridder/gridder_simple.h:216-225), whose argument is
-// formed in FP64.  w0 nu and dw nu are reduced
-// modulo one turn in FP64 and kept as 32-bit fixed-point turns, so that
-// a + q k in wrapping uint32 arithmetic is (w0 + q dw) nu modulo one turn for
-// every q, rounded to 2^-33 turns; r carries dw nu below 2^-33 for large q.
+// w-screen terms per pixel (screen.cuh): the screen of plane q, w_q = w0 +
+// q dw, is exp(-+2 pi i w_q nu), the per-plane screen of ducc0's w-gridding
+// behind ms2dirty / dirty2ms (wgridder/gridder_simple.h:216-225), whose
+// argument is formed in FP64.
 __global__ void screen_table_kernel(DevPlan p, const double *nu_w, ScreenTable scr) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)p.width * p.height) return;
-  const double nu = nu_w[i];
-  constexpr double kTurn = 4294967296.0;  // 2^32
-  double a = p.w0 * nu;
-  a -= rint(a);
-  double k = p.dw * nu;
-  k -= rint(k);
-  const double kq = rint(k * kTurn);
-  scr.a[i] = (uint32_t)(int64_t)rint(a * kTurn);
-  scr.k[i] = (uint32_t)(int64_t)kq;
-  scr.r[i] = (float)(k - kq * (1.0 / kTurn));
+  const ScreenTerms t = screen_terms(p.w0, p.dw, nu_w[i]);
+  scr.a[i] = t.a;
+  scr.k[i] = t.k;
+  scr.r[i] = t.r;
 }
 
 // Grid-correction tables: thread t < width gives cx[t] = 1 / psihat((width/2 -

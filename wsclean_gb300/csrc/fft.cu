@@ -28,6 +28,7 @@
 #include <mutex>
 #include <vector>
 
+#include "screen.cuh"
 #include "tma.cuh"
 #include "wgpu_internal.h"
 
@@ -712,17 +713,11 @@ __device__ __forceinline__ int image_row_of(int k, int nv, int height) {
   return -1;
 }
 
-// Phase of the w-screen of plane q at a pixel from its screen terms (a, k, r):
-// t = (a + q k) 2^-32 + q r turns, the fixed-point part wrapping modulo one
-// turn in uint32 arithmetic (exact for every q), so no FP64 and no range
-// reduction remain per plane; the result carries about 5e-8 turns of error
-// from the two FP32 roundings.
+// The w-screen of plane q at a pixel from its screen terms (screen.cuh).
 constexpr float kNoPixel = 8.0f;  // remainder marker of panel elements outside the image
 __device__ __forceinline__ void screen_b(uint32_t a, uint32_t k, float r, int q, float *sn,
                                          float *cs) {
-  const int32_t t = (int32_t)(a + (uint32_t)q * k);  // turns in 2^-32, within [-1/2, 1/2)
-  // sincospi of 2 t: t 2^-31 plus 2 q r
-  sincospif(fmaf((float)t, 0x1p-31f, (float)(2 * q) * r), sn, cs);
+  sincospif(screen_arg2(a, k, r, q), sn, cs);
 }
 
 // Shared layout of the column-B kernels: the two FFT buffers (n2 * kPanel
