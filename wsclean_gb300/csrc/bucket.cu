@@ -1200,7 +1200,10 @@ namespace {
 // the following ones by the key's 8-bit digits.  The first pass drops the
 // elements whose key is `sentinel` (samples that take no part), so the n_kept
 // others come out; kin / vin end up naming the sorted buffers.  scan(d, n) is
-// an exclusive scan of n uint32 values in place.
+// an exclusive scan of n uint32 values in place.  Three kernels per pass (a
+// per-tile histogram, the scan, a scatter) with scratch the caller sizes: the
+// allocation-free bucketing uses it; bucket_visibilities uses sweep_sort_kept,
+// which gives the same order.
 template <class Scan>
 void radix_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *&vout,
                      const uint8_t *minor, int64_t n, uint32_t n_kept, int bits,
