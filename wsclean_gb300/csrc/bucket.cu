@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kThreads)
   }
   keys[e] = key;
   vals[e] = (uint32_t)e;
-  if (key != sentinel) {
+  if (counts && key != sentinel) {
     // warp-aggregated histogram update
     const unsigned active = __activemask();
     const unsigned peers = __match_any_sync(active, key);
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // FP64 footprints of the samples key_kernel deferred: key, corner mark and
-// histogram count.
+// (counts non-null) histogram count.
 __global__ void __launch_bounds__(kThreads)
     key_fix_kernel(DevPlan p, const double *uvw, const ChannelScale *cs, int64_t n_chan,
                    const uint32_t *__restrict__ pending, const uint32_t *__restrict__ n_pending,
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(kThreads)
     keys[e] = f.key;
     minor[e] = corner_byte(f.iu, f.iv);
     if (corners) corners[(size_t)f.ip * p.nv + f.iv] = 1;
-    atomicAdd(&counts[f.key], 1u);
+    if (counts) atomicAdd(&counts[f.key], 1u);
   }
 }
 
@@ -611,8 +611,7 @@ __global__ void __launch_bounds__(kThreads)
 // ---------------- stable LSD radix sort, one kernel per 8-bit digit ----------
 // The same sort as above without the per-pass histogram and scan.  The digit
 // totals of every pass are counted beforehand (the corner byte by
-// corner_count_kernel, the key bytes from the bucket offsets by
-// key_byte_totals_kernel).  Blocks take
+// corner_count_kernel, the key bytes during the first pass).  Blocks take
 // tiles of kThreads * ITEMS elements in order from a counter, so every lower
 // tile belongs to a block that has already started.  A block ranks its tile's
 // elements by digit (each warp a contiguous run of 32 * ITEMS elements, with
@@ -641,10 +640,11 @@ template <int ITEMS>
 __host__ __device__ constexpr int sweep_tile() {
   return kThreads * ITEMS;
 }
-// dynamic shared memory: warp counts, tile keys and values, tile digits
+// dynamic shared memory: warp counts, next-pass counts, tile keys and values, tile digits
 template <int ITEMS>
 __host__ __device__ constexpr size_t sweep_smem() {
-  return sizeof(uint32_t) * ((kThreads / 32) * 256 + 2 * sweep_tile<ITEMS>()) +
+  return sizeof(uint32_t) *
+             ((kThreads / 32) * 256 + kSweepMaxKeyPasses * 256 + 2 * sweep_tile<ITEMS>()) +
          sweep_tile<ITEMS>();
 }
 
@@ -682,10 +682,11 @@ __device__ __forceinline__ uint32_t sweep_block_scan(uint32_t v, uint32_t *wsum,
   return before + x - v;
 }
 
-// Counts of the corner byte over the elements whose key is not drop_key.
+// Counts of the corner byte over the elements whose key is not drop_key, and
+// their number in *kept.
 __global__ void __launch_bounds__(kThreads)
     corner_count_kernel(const uint32_t *__restrict__ keys, const uint8_t *__restrict__ minor,
-                        int64_t n, uint32_t drop_key, uint32_t *totals) {
+                        int64_t n, uint32_t drop_key, uint32_t *totals, uint32_t *kept) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -703,54 +704,24 @@ __global__ void __launch_bounds__(kThreads)
   for (int64_t i = 4 * n4 + (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += stride)
     if (keys[i] != drop_key) atomicAdd(&h[minor[i]], 1u);
   __syncthreads();
-  if (h[threadIdx.x]) atomicAdd(&totals[threadIdx.x], h[threadIdx.x]);
+  const uint32_t c = h[threadIdx.x];
+  if (c) atomicAdd(&totals[threadIdx.x], c);
+  uint32_t sum = c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(kept, sum);
 }
 
-// Counts of bytes 0 .. n_bytes - 1 of the keys over the sorted elements, from
-// the bucket offsets (exclusive scan: key k holds off[k + 1] - off[k]
-// elements).  A warp takes 32 consecutive keys per step, four steps at a
-// time; a step's keys have the same bytes above the lowest (one warp sum and
-// one atomic each per step), and lane l's lowest byte is (step % 8) * 32 + l,
-// summed in eight registers.
+// Number of elements of each key, from the keys in sorted order (equal keys
+// are consecutive: one warp-aggregated atomic per key and warp, on counters
+// in increasing order).
 __global__ void __launch_bounds__(kThreads)
-    key_byte_totals_kernel(const uint32_t *__restrict__ off, int64_t n_keys, int n_bytes,
-                           uint32_t *totals) {
-  __shared__ uint32_t h[kSweepMaxKeyPasses][256];
-  for (int i = threadIdx.x; i < kSweepMaxKeyPasses * 256; i += kThreads) (&h[0][0])[i] = 0;
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int kWarps = kThreads / 32, kSteps = 4;
-  uint32_t low[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const int64_t n_steps = (n_keys + 31) / 32;
-  for (int64_t step0 = ((int64_t)blockIdx.x * kWarps + warp) * kSteps; step0 < n_steps;
-       step0 += (int64_t)gridDim.x * kWarps * kSteps) {
-    uint32_t c[kSteps];
-#pragma unroll
-    for (int u = 0; u < kSteps; ++u) {
-      const int64_t k = (step0 + u) * 32 + lane;
-      c[u] = k < n_keys ? __ldg(off + k + 1) - __ldg(off + k) : 0u;
-    }
-    const bool upper = (step0 & 4) != 0;  // step0 is a multiple of 4: steps are step0 % 8 + u
-#pragma unroll
-    for (int u = 0; u < kSteps; ++u) {
-      if (upper)
-        low[4 + u] += c[u];
-      else
-        low[u] += c[u];
-      uint32_t sum = c[u];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0 && sum)
-        for (int b = 1; b < n_bytes; ++b)
-          atomicAdd(&h[b][(uint32_t)(((step0 + u) * 32) >> (8 * b)) & 255u], sum);
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 8; ++j)
-    if (low[j]) atomicAdd(&h[0][j * 32 + lane], low[j]);
-  __syncthreads();
-  for (int i = threadIdx.x; i < n_bytes * 256; i += kThreads)
-    if ((&h[0][0])[i]) atomicAdd(totals + i, (&h[0][0])[i]);
+    count_sorted_keys_kernel(const uint32_t *__restrict__ keys, int64_t n, uint32_t *counts) {
+  const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  const unsigned peers = __match_any_sync(__activemask(), k);
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&counts[k], (uint32_t)__popc(peers));
 }
 
 // Status words of kSweepWindow lower tiles q, q - 1, ... for digit t (below
@@ -764,7 +735,8 @@ __device__ __forceinline__ void sweep_window(const uint64_t *status, int64_t q, 
 
 // One stable pass over the n elements of (keys_in, vals_in) by the 8-bit digit
 // at `shift` (FIRST: by minor[i], leaving out the elements whose key is
-// drop_key).  totals: the pass's count of each digit.  status: 256 words
+// drop_key, and counting the kept keys' n_next bytes into next_totals for the
+// later passes).  totals: the pass's count of each digit.  status: 256 words
 // per tile, zero at launch; tile_counter zero at launch.
 template <bool FIRST, int ITEMS, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
@@ -772,12 +744,13 @@ __global__ void __launch_bounds__(kThreads, MINB)
                  const uint8_t *__restrict__ minor, int64_t n, int shift, uint32_t drop_key,
                  const uint32_t *__restrict__ totals, uint64_t *status, uint32_t *tile_counter,
                  uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
-                 unsigned *wait_flags) {
+                 uint32_t *next_totals, int n_next, unsigned *wait_flags) {
   constexpr int kTile = sweep_tile<ITEMS>(), kRun = 32 * ITEMS;
   static_assert(kRun <= 0xffff, "warp ranks are 16-bit");
   extern __shared__ uint32_t sweep_smem[];
   uint32_t(*wcnt)[256] = reinterpret_cast<uint32_t(*)[256]>(sweep_smem);
-  uint32_t *skey = sweep_smem + (kThreads / 32) * 256;
+  uint32_t(*ncnt)[256] = reinterpret_cast<uint32_t(*)[256]>(sweep_smem + (kThreads / 32) * 256);
+  uint32_t *skey = sweep_smem + (kThreads / 32 + kSweepMaxKeyPasses) * 256;
   uint32_t *sval = skey + kTile;
   uint8_t *sdig = reinterpret_cast<uint8_t *>(sval + kTile);
   __shared__ uint32_t gbase[256], wsum[kThreads / 32];
@@ -786,6 +759,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, t = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
   const int64_t n_tiles = (n + kTile - 1) / kTile;
+  if (FIRST)
+    for (int j = 0; j < kSweepMaxKeyPasses; ++j) ncnt[j][t] = 0;
   // the pass's first position of each digit
   uint32_t unused;
   const uint32_t dstart = sweep_block_scan(totals[t], wsum, &unused);
@@ -906,9 +881,16 @@ __global__ void __launch_bounds__(kThreads, MINB)
       const uint32_t k = skey[j];
       keys_out[o] = k;
       vals_out[o] = sval[j];
+      // the key bytes of the later passes, counted in corner order (in input
+      // order equal bytes bunch up in a warp and their atomics collide)
+      if (FIRST)
+        for (int b = 0; b < n_next; ++b) atomicAdd(&ncnt[b][(k >> (8 * b)) & 255u], 1u);
     }
     __syncthreads();  // the next tile reuses the shared buffers
   }
+  if (FIRST)
+    for (int b = 0; b < n_next; ++b)
+      if (ncnt[b][t]) atomicAdd(&next_totals[b * 256 + t], ncnt[b][t]);
 }
 
 // Footprint of a record: corners decided in FP32 where possible (see
@@ -1233,18 +1215,36 @@ template <int ITEMS = kSweepItems>
 int64_t sweep_status_words(int64_t n) {
   return 256 * ((n + sweep_tile<ITEMS>() - 1) / sweep_tile<ITEMS>());
 }
+// counters: one tile counter per pass, the kept count, then 256 digit totals per pass
+constexpr int64_t kSweepKeptWord = 6;
 constexpr int64_t sweep_counter_words() { return 8 + (1 + kSweepMaxKeyPasses) * 256; }
 
-// The same sort as radix_sort_kept with one sweep_kernel per digit.
+// First step of sweep_sort_kept: zeroes the counters and counts the corner
+// bytes and the number of kept elements (counters word kSweepKeptWord).
+template <int ITEMS = kSweepItems>
+void sweep_count(const uint32_t *keys, const uint8_t *minor, int64_t n, uint32_t sentinel,
+                 uint64_t *status, cudaStream_t s) {
+  uint32_t *counters = (uint32_t *)(status + sweep_status_words<ITEMS>(n));
+  WGPU_CUDA(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * sweep_counter_words(), s));
+  if (n <= 0) return;
+  corner_count_kernel<<<sm_count() * 4, kThreads, 0, s>>>(keys, minor, n, sentinel, counters + 8,
+                                                          counters + kSweepKeptWord);
+  check_launch("corner_count_kernel");
+}
+template <int ITEMS = kSweepItems>
+const uint32_t *sweep_kept_word(const uint64_t *status, int64_t n) {
+  return (const uint32_t *)(status + sweep_status_words<ITEMS>(n)) + kSweepKeptWord;
+}
+
+// The same sort as radix_sort_kept with one sweep_kernel per digit, after
+// sweep_count on the same keys and status; n_kept is the count it made.
 // status: sweep_status_words<ITEMS>(n) words, then the counters; wait_flags:
 // the word an expired look-back wait is reported in.
-// key_offsets: the exclusive scan of the number of kept elements of each of
-// the n_keys keys.
 template <int ITEMS = kSweepItems, int MINB = kSweepMinBlocks>
 void sweep_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *&vout,
                      const uint8_t *minor, int64_t n, uint32_t n_kept, int bits,
-                     uint32_t sentinel, const uint32_t *key_offsets, int64_t n_keys,
-                     uint64_t *status, unsigned *wait_flags, cudaStream_t s) {
+                     uint32_t sentinel, uint64_t *status, unsigned *wait_flags,
+                     cudaStream_t s) {
   if (n <= 0 || n_kept == 0) return;
   const int n_key_passes = (bits + 7) / 8;
   if (n_key_passes > kSweepMaxKeyPasses)
@@ -1254,12 +1254,6 @@ void sweep_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *
   uint32_t *counters = (uint32_t *)(status + sweep_status_words<ITEMS>(n));
   uint32_t *tile_counters = counters;  // one per pass
   uint32_t *totals = counters + 8;     // per pass, 256 digits
-  WGPU_CUDA(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * sweep_counter_words(), s));
-  corner_count_kernel<<<sm_count() * 4, kThreads, 0, s>>>(kin, minor, n, sentinel, totals);
-  check_launch("corner_count_kernel");
-  key_byte_totals_kernel<<<sm_count() * 16, kThreads, 0, s>>>(key_offsets, n_keys, n_key_passes,
-                                                               totals + 256);
-  check_launch("key_byte_totals_kernel");
   auto first = sweep_kernel<true, ITEMS, MINB>;
   auto later = sweep_kernel<false, ITEMS, MINB>;
   ensure_dynamic_smem((const void *)first, kSmem);
@@ -1275,11 +1269,12 @@ void sweep_sort_kept(uint32_t *&kin, uint32_t *&vin, uint32_t *&kout, uint32_t *
         (unsigned)std::min<int64_t>(tiles, (int64_t)sm_count() * std::max(per_sm, 1));
     if (pass == 0) {
       first<<<blocks, kThreads, kSmem, s>>>(kin, vin, minor, cur, 0, sentinel, totals, status,
-                                            tile_counters, kout, vout, wait_flags);
+                                            tile_counters, kout, vout, totals + 256,
+                                            n_key_passes, wait_flags);
     } else {
       later<<<blocks, kThreads, kSmem, s>>>(kin, vin, nullptr, cur, 8 * (pass - 1), sentinel,
                                             totals + 256 * pass, status, tile_counters + pass,
-                                            kout, vout, wait_flags);
+                                            kout, vout, nullptr, 0, wait_flags);
     }
     check_launch("sweep_kernel");
     std::swap(kin, kout);
@@ -1371,7 +1366,6 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
   const double gu = p.dl * (double)p.nu, gv = p.dm * (double)p.nv;
   channel_scales_kernel<<<grid_for(n_chan, 128), 128, 0, s>>>(d_freq, n_chan, gu, gv, cs);
   check_launch("channel_scales_kernel");
-  WGPU_CUDA(cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (res.n_keys + 1), s));
   if ((uint64_t)p.n_planes * (uint64_t)p.nv >= 0xFFFFFFFFull)
     throw Error(WGPU_ERR_INVALID, "too many (plane, row) pairs");
   res.rows.n_planes = p.n_planes;
@@ -1386,39 +1380,48 @@ BucketResult bucket_visibilities(DeviceArena &arena, const DevPlan &p,
     uvw_float_kernel<<<grid_for(n_rows, kThreads), kThreads, 0, s>>>(d_uvw, n_rows, uvwf,
                                                                          uvwl);
     check_launch("uvw_float_kernel");
+    // no histogram here: the keys are counted after the sort, in key order
     key_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
         p, d_uvw, cs, Selector{skip_zero ? (const float2 *)d_vis : nullptr, d_mask},
-        n_rows, n_chan, sentinel, keys, vals, offsets, res.rows.corners(), keys2, n_pending,
+        n_rows, n_chan, sentinel, keys, vals, nullptr, res.rows.corners(), keys2, n_pending,
         uvwf, minor);
     check_launch("key_kernel");
     key_fix_kernel<<<sm_count() * 4, kThreads, 0, s>>>(p, d_uvw, cs, n_chan, keys2, n_pending,
-                                                        keys, offsets, res.rows.corners(), minor);
+                                                        keys, nullptr, res.rows.corners(), minor);
     check_launch("key_fix_kernel");
   }
   build_row_occupancy(res.rows, p.support, s);
-  exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
 
-  // number of bucketed elements = offsets[n_keys]
-  uint32_t total = 0;
-  WGPU_CUDA(cudaMemcpyAsync(&total, offsets + res.n_keys, sizeof(uint32_t),
-                            cudaMemcpyDeviceToHost, s));
-  WGPU_CUDA(cudaStreamSynchronize(s));
-  // radix sort over the key bits in use, the unselected samples dropped
+  // the number of bucketed elements (and the first sort pass's digit totals)
   const int64_t status_words = sweep_status_words(n);
   uint64_t *status = (uint64_t *)arena.get(
       kSlotHist, sizeof(uint64_t) * status_words + sizeof(uint32_t) * (sweep_counter_words() + 1));
+  sweep_count(keys, minor, n, sentinel, status, s);
+  uint32_t total = 0;
+  WGPU_CUDA(cudaMemcpyAsync(&total, sweep_kept_word(status, n), sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+  WGPU_CUDA(cudaStreamSynchronize(s));
+  // radix sort over the key bits in use, the unselected samples dropped
   // without a caller's flag word, expired waits are counted in the word after the counters
   unsigned *own_flag = (unsigned *)(status + status_words) + sweep_counter_words();
   if (!wait_flags) WGPU_CUDA(cudaMemsetAsync(own_flag, 0, sizeof(unsigned), s));
   uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  sweep_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, offsets, res.n_keys,
-                  status, wait_flags ? wait_flags : own_flag, s);
+  sweep_sort_kept(kin, vin, kout, vout, minor, n, total, bits, sentinel, status,
+                  wait_flags ? wait_flags : own_flag, s);
   if (!wait_flags && n > 0 && total > 0) {
     unsigned expired = 0;
     WGPU_CUDA(cudaMemcpyAsync(&expired, own_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     WGPU_CUDA(cudaStreamSynchronize(s));
     if (expired) throw Error(WGPU_ERR_TIMEOUT, "a bounded device wait expired (bucket sort)");
   }
+  // bucket offsets: the number of elements of each key (counted on the
+  // sorted keys), then their exclusive scan
+  WGPU_CUDA(cudaMemsetAsync(offsets, 0, sizeof(uint32_t) * (res.n_keys + 1), s));
+  if (total > 0) {
+    count_sorted_keys_kernel<<<grid_for(total, kThreads), kThreads, 0, s>>>(kin, total, offsets);
+    check_launch("count_sorted_keys_kernel");
+  }
+  exclusive_scan_u32(arena, offsets, res.n_keys + 1, s);
   res.n_out = total;
   res.perm = vin;
   res.offsets = offsets;
