@@ -6,7 +6,7 @@
 // visibilities by key and, within a key, by the footprint corner inside the
 // tile (its first pass sorts by the corner byte), so that the samples sharing
 // an exact footprint corner are consecutive; the bucket offsets come from a
-// key histogram and an exclusive scan; finally one 32-byte record per
+// histogram of the sorted keys and an exclusive scan; finally one 32-byte record per
 // visibility is written in sorted order, carrying the visibility times its
 // shift phase (inversion) or the phase factor itself (prediction).
 //
