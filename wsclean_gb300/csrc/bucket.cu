@@ -386,17 +386,27 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
       }
     }
+    // lane j takes row j's two products, so that the FP64 work of the kRows
+    // rows is one set of warp instructions
+    unsigned my_l = 0, my_h = 0, my_k = 0;
+    double my_w = 0.0;
 #pragma unroll
     for (int j = 0; j < kRows; ++j) {
       const unsigned l = __reduce_min_sync(0xffffffffu, lo[j]);
       const unsigned h = __reduce_max_sync(0xffffffffu, hi[j]);
       const unsigned kk = __reduce_add_sync(0xffffffffu, k[j]);
-      if (kk > 0 && lane == 0) {
-        const double a = __dmul_rn(w[j], by_rank[l]), b = __dmul_rn(w[j], by_rank[h]);
-        wmin = fmin(wmin, fmin(a, b));
-        wmax = fmax(wmax, fmax(a, b));
-        cnt += kk;
+      if (lane == j) {
+        my_l = l;
+        my_h = h;
+        my_k = kk;
+        my_w = w[j];
       }
+    }
+    if (my_k > 0) {
+      const double a = __dmul_rn(my_w, by_rank[my_l]), b = __dmul_rn(my_w, by_rank[my_h]);
+      wmin = fmin(wmin, fmin(a, b));
+      wmax = fmax(wmax, fmax(a, b));
+      cnt += my_k;
     }
   }
   typedef cub::BlockReduce<double, kThreads> BR;
