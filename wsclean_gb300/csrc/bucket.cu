@@ -439,7 +439,9 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t n = n_rows * n_chan;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  const int64_t r = e / n_chan, c = e - r * n_chan;
+  // n < 2^32 (the callers check it): 32-bit division, which needs no FP64
+  const uint32_t r32 = (uint32_t)e / (uint32_t)n_chan;
+  const int64_t r = r32, c = (int64_t)((uint32_t)e - r32 * (uint32_t)n_chan);
   uint32_t key = sentinel;
   uint8_t cb = 0;
   bool defer = false;
@@ -488,7 +490,8 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t n = *n_pending;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t e = pending[i];
-    const int64_t r = e / n_chan, c = e - r * n_chan;
+    const uint32_t r32 = e / (uint32_t)n_chan;
+    const int64_t r = r32, c = (int64_t)(e - r32 * (uint32_t)n_chan);
     const Footprint f = footprint(p, uvw + 3 * r, cs[c]);
     keys[e] = f.key;
     minor[e] = corner_byte(f.iu, f.iv);

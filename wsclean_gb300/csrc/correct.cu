@@ -15,6 +15,13 @@ constexpr int kThreads = 256;
 
 unsigned blocks_for(int64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
+// Row of sample e (n samples, n_chan per row): 32-bit division when n < 2^32
+// (the common case; it needs no FP64), 64-bit otherwise.
+__device__ __forceinline__ int64_t row_of(int64_t e, int64_t n, int64_t n_chan) {
+  if (n < (int64_t)0xFFFFFFFFll) return (int64_t)((uint32_t)e / (uint32_t)n_chan);
+  return e / n_chan;
+}
+
 // n - 1 - c_n per trimmed pixel, FP64.  Pixel (x, y) at l = (width/2 - x) dl +
 // l_shift, m = (y - height/2) dm + m_shift, n - 1 := 0 beyond the horizon
 // (gridding/directmsgridder.cpp:205-229).
@@ -130,7 +137,7 @@ __global__ void apply_gains_kernel(int mode, int n_pol, int64_t n_rows,
                                    int *err_flag) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_rows * n_chan) return;
-  const int64_t r = e / n_chan, ch = e - r * n_chan;
+  const int64_t r = row_of(e, n_rows * n_chan, n_chan), ch = e - r * n_chan;
   const uint64_t a1 = ant_pairs[2 * r], a2 = ant_pairs[2 * r + 1];
   const uint64_t t = time_offsets[r];
   if (a1 >= (uint64_t)n_ant || a2 >= (uint64_t)n_ant || t >= (uint64_t)n_times) {
@@ -205,7 +212,7 @@ __global__ void forward_gains_kernel(int mode, int n_pol, int64_t n_rows, int64_
                                      float2 *out, int *err_flag) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_rows * n_chan) return;
-  const int64_t r = e / n_chan, ch = e - r * n_chan;
+  const int64_t r = row_of(e, n_rows * n_chan, n_chan), ch = e - r * n_chan;
   float2 *o = out + e * n_pol;
   const uint64_t a1 = ant_pairs[2 * r], a2 = ant_pairs[2 * r + 1];
   const uint64_t t = time_offsets[r];
